@@ -1,0 +1,350 @@
+"""Benchmark: mixed-precision MPM step on the 2,000,000-point column.
+
+One "step" is one ExplicitIntegrator::flow step (mpmgrains2d) of the
+2,000,000-point granular column on a 2048 x 1024 grid (h = 1 mm, dt = 2e-6 s),
+the large mixed-precision configuration. Prints one JSON line:
+
+  value      particle-steps/s of the MIXED path with the particle state resident
+             in HBM (all ranks together);
+  e2e        the same metric through the public C ABI with host buffers: every
+             step uploads the particle state from pinned host memory, steps and
+             downloads it again;
+  fp64       the plain FP64 GPU step on the same workload, and the one-step
+             grid-velocity error of the MIXED path against it;
+  roofline   the fused G2P/P2G kernel's algorithmic bytes / measured kernel time
+             against the measured HBM copy bandwidth;
+  cpu_baseline  the CPU oracle (FP64 restatement of the reference, OpenMP
+             over the host cores) on a bounded sample of the same workload.
+
+``--impl reference`` times the CPU oracle alone on the same workload (the
+reference itself cannot be built here).
+Multi-GPU runs are replicas: every rank steps its own copy of the scene.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s mixed vs FP64 GPU at stated error; batched p50/p99 latency"
+UNIT = "particle-steps/s"
+# Algorithmic bytes of the fused G2P/P2G kernel: each persistent particle
+# field read once (u 16 + v 8 + m,V 8 + strain 16 + flags 1 = 49 B) and the
+# updated ones written once (u 16 + v 8 + strain 16 + flags 1 = 41 B); per
+# active node the grid velocity/acceleration read (16 B) and the accumulated
+# mass/momentum/force written (20 B).
+BYTES_PER_PARTICLE = 90
+BYTES_PER_ACTIVE_NODE = 36
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.QUERY,
+                                      "--format=csv,noheader,nounits"], capture_output=True,
+                                     text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([s.strip() for s in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        sm = [float(s[1]) for s in self.samples if len(s) > 8 and s[1].replace(".", "").isdigit()]
+        smax = [float(s[2]) for s in self.samples if len(s) > 8 and s[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            if len(s) > 8:
+                for k, name in enumerate(names):
+                    if s[5 + k].lower().startswith("active"):
+                        reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def scene():
+    from libhybridgrains_gb300 import scenes
+    cfg = scenes.mpm_column("column_2M")
+    pts = scenes.seed_column_points(cfg)
+    return cfg, pts
+
+
+def make_mpm(ctx, cfg, precision, n):
+    import libhybridgrains_gb300 as hg
+    from libhybridgrains_gb300 import scenes
+    return hg.MPM(ctx, cfg["grid_min"], cfg["grid_max"], cfg["h"], cfg["shear_modulus"],
+                  cfg["bulk_modulus"], cfg["dp_alpha"], cfg["flip_alpha"], scenes.GRAVITY,
+                  cfg["planes"], precision=precision, capacity=n)
+
+
+def cpu_oracle_rate(cfg, pts, steps, threads):
+    """Oracle (FP64, OpenMP) particle-steps/s on `steps` steps of the scene."""
+    import oracle
+    from libhybridgrains_gb300 import scenes
+    o = oracle.MPM(cfg["grid_min"], cfg["grid_max"], cfg["h"],
+                   shear_modulus=cfg["shear_modulus"], bulk_modulus=cfg["bulk_modulus"],
+                   dp_alpha=cfg["dp_alpha"], flip_alpha=cfg["flip_alpha"],
+                   gravity=scenes.GRAVITY, threads=threads)
+    for (x, n, st, lb) in cfg["planes"]:
+        o.add_plane(x, n, st, lb)
+    o.set_particles(pts["q"], pts["v"], pts["m"], pts["vol"], pts["hl"])
+    o.step(cfg["dt"], 1)  # warm-up (allocates the per-thread grids)
+    t0 = time.perf_counter()
+    o.step(cfg["dt"], steps)
+    dt = time.perf_counter() - t0
+    return len(pts["m"]) * steps / dt, dt
+
+
+def barrier_max(value, world):
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def init_dist(world):
+    if world <= 1:
+        return
+    import torch.distributed as dist
+    if not dist.is_initialized():
+        dist.init_process_group("gloo")
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_reference(args, rank, world):
+    """CPU oracle alone (the reference's own CPU path cannot be built here)."""
+    if rank != 0:
+        return
+    cfg, pts = scene()
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_oracle_rate(cfg, pts, 1, threads)
+    rate, secs = cpu_oracle_rate(cfg, pts, args.steps, threads)
+    line = {"metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": "column_2M: 2,000,000-point MPM granular column, 2048x1024 "
+                                   "grid, h=1 mm, dt=2e-6 s", "particles": len(pts["m"])},
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "%d steps of the 2,000,000-point column" % args.steps},
+            "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local):
+    import libhybridgrains_gb300 as hg
+    from libhybridgrains_gb300 import build as gbuild
+    gbuild.build()
+    ctx = hg.Context(local)
+    cfg, pts = scene()
+    n = len(pts["m"])
+    dt = cfg["dt"]
+
+    # ---- resident MIXED step ------------------------------------------------
+    mix = make_mpm(ctx, cfg, hg.MIXED, n)
+    mix.upload(pts["q"], pts["v"], pts["m"], pts["vol"], pts["hl"])
+    mix.flow(dt, args.warmup)
+    ctx.synchronize()
+    barrier(world)
+    launches0 = hg.kernel_launch_count()
+    mix.profile(True)
+    with ClockSampler(local) as clk:
+        ctx.timer_begin()
+        mix.flow(dt, args.steps)
+        ms = ctx.timer_end()
+    launches = hg.kernel_launch_count() - launches0
+    g2p2g_ms, update_ms, prof_steps = mix.profile_read()
+    mix.profile(False)
+    barrier(world)
+    ms = barrier_max(ms, world)
+    value = n * args.steps * world / (ms * 1e-3)
+    status = mix.status()
+    G = mix.grid()
+    n_active = int((G["mass"] > 0).sum())
+
+    # ---- plain FP64 GPU step on the same workload ------------------------------
+    fp64 = None
+    if args.fp64_steps > 0:
+        f64 = make_mpm(ctx, cfg, hg.FP64, n)
+        f64.upload(pts["q"], pts["v"], pts["m"], pts["vol"], pts["hl"])
+        f64.flow(dt, 3)
+        fsteps = args.fp64_steps
+        barrier(world)
+        ctx.timer_begin()
+        f64.flow(dt, fsteps)
+        fms = ctx.timer_end()
+        fp64_value = n * fsteps * world / (barrier_max(fms, world) * 1e-3)
+        # one-step grid-velocity error of MIXED against FP64 from the same state
+        st = f64.download()
+        chk = make_mpm(ctx, cfg, hg.MIXED, n)
+        chk.upload(st["q"], st["v"], pts["m"], pts["vol"], pts["hl"], st["be"], st["J"], st["jh"])
+        chk.flow(dt, 1)
+        f64.flow(dt, 1)
+        Gm, Gf = chk.grid(), f64.grid()
+        act = Gf["mass"] > 0
+        vel_err = float(np.linalg.norm(Gm["vel"][act] - Gf["vel"][act]) /
+                        max(np.linalg.norm(Gf["vel"][act]), 1e-300))
+        fp64 = {"value": fp64_value, "unit": UNIT, "steps": fsteps,
+                "ms_per_step": fms / fsteps, "speedup_mixed_over_fp64": value / fp64_value,
+                "grid_velocity_rel_error": vel_err,
+                "error_state": "after %d FP64 steps from rest" % (fsteps + 3)}
+        del chk, f64
+
+    # ---- end to end through the C ABI with host buffers --------------------------
+    e2e = None
+    if args.e2e_steps > 0:
+        import torch
+        host = {k: torch.empty(v.shape, dtype=torch.float64, pin_memory=True).numpy()
+                for k, v in (("q", pts["q"]), ("v", pts["v"]), ("m", pts["m"]),
+                             ("vol", pts["vol"]))}
+        for k in ("q", "v", "m", "vol"):
+            host[k][...] = pts[k]
+        host["be"] = torch.empty((n, 4), dtype=torch.float64, pin_memory=True).numpy()
+        host["be"][...] = [1.0, 0.0, 0.0, 1.0]
+        host["J"] = torch.ones(n, dtype=torch.float64, pin_memory=True).numpy()
+        host["jh"] = torch.zeros(n, dtype=torch.int32, pin_memory=True).numpy()
+        e2 = make_mpm(ctx, cfg, hg.MIXED, n)
+
+        def one():
+            e2.upload(host["q"], host["v"], host["m"], host["vol"], None, host["be"], host["J"],
+                      host["jh"])
+            e2.flow(dt, 1)
+            e2.download_into(host["q"], host["v"], host["be"], host["J"], host["jh"])
+
+        one()
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            one()
+        e2e_s = barrier_max(time.perf_counter() - t0, world)
+        h2d = n * (16 + 16 + 8 + 8 + 32 + 8 + 4)
+        d2h = n * (16 + 16 + 32 + 8 + 4)
+        e2e = {"value": n * args.e2e_steps * world / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "steps": args.e2e_steps, "ms_per_step": 1e3 * e2e_s / args.e2e_steps}
+        del e2
+
+    if rank != 0:
+        return
+    peaks = measured_peaks()
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if peak else "fallback"
+    peak = peak or 6800.0
+    alg_bytes = n * BYTES_PER_PARTICLE + n_active * BYTES_PER_ACTIVE_NODE
+    per_launch_s = (g2p2g_ms * 1e-3) / max(prof_steps, 1)
+    achieved = alg_bytes / per_launch_s / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "kx_g2p2g_column_2M.traffic")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = float(f.read().split()[0])
+
+    cpu = None
+    if world == 1 and args.cpu_steps > 0:
+        threads = os.cpu_count() or 1
+        rate, secs = cpu_oracle_rate(cfg, pts, args.cpu_steps, threads)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "%d steps of the 2,000,000-point column (%.1f s)" % (args.cpu_steps, secs)}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 positions)",
+        "data": "synthetic",
+        "config": {"workload": "column_2M: 2,000,000-point MPM granular column, 2048x1024 grid, "
+                               "h=1 mm, dt=2e-6 s, linear basis, mixed precision",
+                   "particles": n, "grid_cells": [2048, 1024], "active_nodes": n_active,
+                   "l2": "inputs larger than L2 (particle state 180 MB per step)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "fp64": fp64,
+        "roofline": {"bound": "hbm", "kernel": "kx_g2p2g", "achieved": achieved, "peak": peak,
+                     "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "algorithmic_bytes": alg_bytes,
+                     "kernel_ms": per_launch_s * 1e3,
+                     "grid_update_ms": update_ms / max(prof_steps, 1)},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "status_word": status,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-steps", type=int, default=10)
+    ap.add_argument("--fp64-steps", type=int, default=10)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, local = dist_env()
+    init_dist(world)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

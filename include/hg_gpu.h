@@ -1,0 +1,272 @@
+/*
+ * hg_gpu.h - C ABI of the GB300-native granular time-step library
+ * (libhg_gpu.so).
+ *
+ * This is the drop-in boundary for the per-timestep core of libHybridGrains:
+ * the explicit MPM step of mpmgrains2d, the penalty-DEM disk step of
+ * rigidbody2d and the node-node coupling of hybridgrains2dnew. Each entry
+ * point names the reference interface it replaces. The reference interfaces
+ * are C++ member functions operating on caller-owned Eigen arrays; here state
+ * lives on the device between calls and the host exchanges plain arrays in the
+ * reference's memory layouts:
+ *   - MPM positions/velocities: 2 x N column-major doubles (x0 y0 x1 y1 ...),
+ *     like Matrix2Xsc::data();
+ *   - be_bar: N column-major 2x2 blocks (b00 b10 b01 b11), like
+ *     std::vector<Matrix22sc>;
+ *   - DEM q and v: 3 x N doubles (x y theta / vx vy omega), like
+ *     RigidBody2DState::q() / v().
+ * The library copies; the caller keeps ownership of every host buffer.
+ *
+ * Conventions: every call returns an hg_status; no C++ exception crosses the
+ * ABI; hg_last_error() gives a message for the calling thread's last failure.
+ * Calls on one context are asynchronous on that context's CUDA stream until a
+ * download, hg_*_status or hg_context_synchronize. One host thread per
+ * context. Kernels never trap: device-side faults in the data (NaN, particles
+ * leaving the grid, capacity overflow) set bits of a per-object status word.
+ */
+#ifndef HG_GPU_H
+#define HG_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t hg_status;
+
+enum {
+  HG_OK = 0,
+  HG_ERR_INVALID_ARGUMENT = 1,
+  HG_ERR_CUDA = 2,
+  HG_ERR_OUT_OF_MEMORY = 3,
+  HG_ERR_CAPACITY = 4,
+  HG_ERR_UNSUPPORTED = 5,
+  HG_ERR_DEVICE_STATUS = 6
+};
+
+/* Bits of the device status word (hg_mpm_status / hg_dem_status). */
+enum {
+  HG_STATUS_NONFINITE = 1u << 0,        /* NaN/Inf produced in particle state */
+  HG_STATUS_OUT_OF_GRID = 1u << 1,      /* a particle left the MPM grid */
+  HG_STATUS_CONTACT_OVERFLOW = 1u << 2, /* DEM contact capacity exceeded */
+  HG_STATUS_CELL_OVERFLOW = 1u << 3,    /* DEM broadphase bucket overflow */
+  HG_STATUS_NEGATIVE_MASS = 1u << 4     /* a grain coupled to an empty node */
+};
+
+typedef struct hg_context hg_context;
+typedef struct hg_mpm hg_mpm;
+typedef struct hg_dem hg_dem;
+typedef struct hg_hybrid hg_hybrid;
+
+/* ---- context -------------------------------------------------------------- */
+
+hg_status hg_context_create(int32_t device, hg_context **out);
+hg_status hg_context_destroy(hg_context *ctx);
+hg_status hg_context_synchronize(hg_context *ctx);
+const char *hg_status_string(hg_status s);
+const char *hg_last_error(void);
+/* Number of kernels this library has launched in the process so far. */
+int64_t hg_kernel_launch_count(void);
+/* Measurement hooks (no counterpart in the reference): CUDA events recorded
+ * on the context's stream; _end synchronises and returns the elapsed time. */
+hg_status hg_context_timer_begin(hg_context *ctx);
+hg_status hg_context_timer_end(hg_context *ctx, double *ms);
+
+/* ---- MPM (mpmgrains2d) ------------------------------------------------------ */
+
+enum { HG_BASIS_LINEAR = 0, HG_BASIS_UGIMP = 1 };
+enum { HG_PRECISION_FP64 = 0, HG_PRECISION_MIXED = 1 };
+enum { HG_MAX_PLANES = 8 };
+
+/* MPMStaticPlane (mpmgrains2d/StaticPlane.h:6-22). The normal is normalised
+ * on creation, like the reference constructor (StaticPlane.cpp:6-12). */
+typedef struct {
+  double x[2];
+  double n[2];
+  int32_t sticking; /* 0 = SLIDING, 1 = STICKING */
+  int32_t pad_;
+  double lower_bound; /* -inf when absent */
+} hg_mpm_plane;
+
+/* Inputs of InitialSimulationState::generateSimulationState
+ * (mpmgrains2d/InitialSimulationState.cpp:147-228) minus the particles. */
+typedef struct {
+  double grid_min[2];
+  double grid_max[2];
+  double cell_width;
+  int32_t basis;     /* HG_BASIS_* (shape_function_category / order) */
+  int32_t precision; /* HG_PRECISION_* */
+  double shear_modulus;
+  double bulk_modulus;
+  double dp_alpha;   /* Drucker_Prager_alpha (<material alpha=...>) */
+  double flip_alpha; /* PIC/FLIP blend (<integrator alpha=...>) */
+  double gravity[2];
+  int32_t num_planes;
+  int32_t pad_;
+  hg_mpm_plane planes[HG_MAX_PLANES];
+  int64_t capacity; /* maximum number of material points */
+} hg_mpm_desc;
+
+/* Replaces SimulationState construction (PhysicsGrid::setDimensions,
+ * mpmgrains2d/PhysicsGrid.cpp:14-55). */
+hg_status hg_mpm_create(hg_context *ctx, const hg_mpm_desc *desc, hg_mpm **out);
+hg_status hg_mpm_destroy(hg_mpm *m);
+/* PhysicsGrid::min / max / cell_count after setDimensions. */
+hg_status hg_mpm_grid_info(hg_mpm *m, double grid_min[2], double grid_max[2],
+                           int32_t cell_count[2]);
+
+/* InitialSimulationState rasterizeRectangle
+ * (mpmgrains2d/InitialSimulationState.cpp:48-145) on the host: writes at most
+ * cap points (q, v as 2 x N) and returns the generated count in *count. Pass
+ * cap = 0 and NULL buffers to query the count. */
+hg_status hg_mpm_seed_rectangle(hg_mpm *m, const double rmin[2],
+                                const double rmax[2], double density,
+                                int32_t samples_per_dim, const double vel[2],
+                                double omega, int64_t cap, double *q, double *v,
+                                double *mass, double *volume, double *hl,
+                                int64_t *count);
+
+/* MaterialPoints::setPoints (mpmgrains2d/MaterialPoints.cpp). Optional
+ * arrays may be NULL: be_bar = I, J = 1, just_homogenized = 0,
+ * kinematic = 0. */
+hg_status hg_mpm_upload(hg_mpm *m, int64_t n, const double *q, const double *v,
+                        const double *mass, const double *volume,
+                        const double *hl, const double *be_bar,
+                        const double *J, const int32_t *just_homogenized,
+                        const uint8_t *kinematic);
+/* Material point state in upload order; any pointer may be NULL. */
+hg_status hg_mpm_download(hg_mpm *m, double *q, double *v, double *be_bar,
+                          double *J, int32_t *just_homogenized);
+hg_status hg_mpm_num_particles(hg_mpm *m, int64_t *n);
+
+/* ExplicitIntegrator::flow (mpmgrains2d/ExplicitIntegrator.cpp:63-67),
+ * nsteps times. */
+hg_status hg_mpm_step(hg_mpm *m, double dt, int32_t nsteps);
+/* ExplicitIntegrator::flow_zero_phase / flow_first_phase /
+ * flow_second_phase (ExplicitIntegrator.cpp:5-61); FP64 precision only.
+ * The internal-force scatter is done in phase 0, which is equivalent because
+ * the material points do not change between phase 0 and phase 1. */
+hg_status hg_mpm_phase0(hg_mpm *m);
+hg_status hg_mpm_phase1(hg_mpm *m, double dt);
+hg_status hg_mpm_phase2(hg_mpm *m, double dt);
+
+/* PhysicsGrid fields ((cell_count+1) node-major, 2 x nodes for vectors).
+ * MIXED precision keeps mass, velocity and acceleration of the last grid
+ * update only; requesting momentum, momentum_new or force from a MIXED
+ * object returns HG_ERR_UNSUPPORTED. */
+hg_status hg_mpm_download_grid(hg_mpm *m, double *mass, double *momentum,
+                               double *momentum_new, double *force,
+                               double *velocity, double *acceleration);
+/* Cell of each material point, floor((x - grid_min) / cell_width) per axis
+ * (2 ints per point, upload order): the first stencil index of the linear
+ * basis (LinearBasisFunctions.cpp:49-62) and the key the MIXED path sorts
+ * by. */
+hg_status hg_mpm_cell_index(hg_mpm *m, int32_t *cells);
+/* Synchronises and returns the device status word (HG_STATUS_* bits). */
+hg_status hg_mpm_status(hg_mpm *m, uint32_t *word);
+hg_status hg_mpm_clear_status(hg_mpm *m);
+/* Number of particle re-sorts performed so far (MIXED precision). */
+hg_status hg_mpm_rebin_count(hg_mpm *m, int64_t *count);
+/* Measurement hooks (no counterpart in the reference), MIXED precision:
+ * while enabled, every step records CUDA events around its grid-update and
+ * fused G2P/P2G kernels; _read synchronises and returns the summed kernel
+ * times since enabling and the number of steps recorded. */
+hg_status hg_mpm_profile(hg_mpm *m, int32_t enable);
+hg_status hg_mpm_profile_read(hg_mpm *m, double *g2p2g_ms,
+                              double *grid_update_ms, int64_t *steps);
+
+/* ---- DEM (rigidbody2d, penalty map) --------------------------------------- */
+
+/* RigidBody2DStaticPlane, static (v = 0, omega = 0). */
+typedef struct {
+  double x[2];
+  double n[2];
+} hg_dem_plane;
+
+/* PenaltyImpactFrictionMap parameters (rigidbody2d/PenaltyImpactFrictionMap.
+ * cpp:15-26) plus NearEarthGravityForce and the body/contact capacities. */
+typedef struct {
+  double gravity[2];
+  double kn, kt, gamman, gammat, mu;
+  double cell_scale; /* SpatialGrid cell scale (reporting only) */
+  int32_t num_planes;
+  int32_t pad_;
+  hg_dem_plane planes[HG_MAX_PLANES];
+  int64_t capacity;         /* bodies */
+  int64_t contact_capacity; /* active contacts */
+} hg_dem_desc;
+
+hg_status hg_dem_create(hg_context *ctx, const hg_dem_desc *desc, hg_dem **out);
+hg_status hg_dem_destroy(hg_dem *d);
+/* RigidBody2DState::addBody for circles (rigidbody2d/RigidBody2DState.cpp:
+ * 237-336): q, v as 3 x N; mass = rho pi r^2, inertia = m r^2 / 2. Resets the
+ * contact history. */
+hg_status hg_dem_upload(hg_dem *d, int64_t n, const double *q, const double *v,
+                        const double *radius, const double *mass,
+                        const double *inertia, const uint8_t *fixed);
+/* RigidBody2DState::updateCurrentMassUsingMassWeights
+ * (RigidBody2DState.cpp:1182-1200). */
+hg_status hg_dem_set_weights(hg_dem *d, const double *w);
+hg_status hg_dem_set_state(hg_dem *d, const double *q, const double *v);
+hg_status hg_dem_download(hg_dem *d, double *q, double *v);
+/* PenaltyImpactFrictionMap::flow / flowWithWeights
+ * (PenaltyImpactFrictionMap.cpp:1083-1149) through RigidBody2DSim::flow /
+ * flowWithWeight (RigidBody2DSim.cpp:1013-1069), nsteps times. */
+hg_status hg_dem_step(hg_dem *d, double dt, int32_t nsteps, int32_t weighted);
+hg_status hg_dem_num_contacts(hg_dem *d, int64_t *n);
+/* The collision cache (PenaltyImpactFrictionMap::getCollisionCache), one
+ * record of HG_DEM_RECORD_WIDTH doubles per contact, ordered plane contacts
+ * (body-major), circle-circle (body-major), kinematic circle-circle
+ * (body-major): kind, first, second, depth, n[2], delta_s[2], vrel[2],
+ * r0[2], r1[2], weight, contact_point[2], normal_force[2],
+ * friction_force[2], 0. */
+enum { HG_DEM_RECORD_WIDTH = 22 };
+hg_status hg_dem_download_contacts(hg_dem *d, int64_t cap, double *records,
+                                   int64_t *count);
+hg_status hg_dem_status(hg_dem *d, uint32_t *word);
+/* SpatialGrid::getPotentialOverlaps (rigidbody2d/SpatialGrid.cpp:90-118) on
+ * explicit AABBs (2 x N min and max): the sorted set of (i, j), i < j, whose
+ * boxes overlap. Writes at most cap pairs; *count is the full count. */
+hg_status hg_dem_candidate_pairs(hg_context *ctx, int64_t n,
+                                 const double *aabb_min, const double *aabb_max,
+                                 int64_t cap, int32_t *pairs, int64_t *count);
+
+/* ---- hybrid node-node coupling (hybridgrains2dnew) ------------------------ */
+
+enum {
+  HG_HYBRID_HOMOGENIZE_STRESS = 1,
+  HG_HYBRID_HOMOGENIZE_VELOCITY = 2
+};
+
+/* HybridGrains2DSim over an FP64 MPM object and a DEM object on the same
+ * context (hybridgrains2dnew/HybridGrains2DSim.cpp:21-73). */
+hg_status hg_hybrid_create(hg_context *ctx, hg_mpm *m, hg_dem *d,
+                           hg_hybrid **out);
+hg_status hg_hybrid_destroy(hg_hybrid *h);
+/* HybridGrains2DSim::stepSystem_constraintSetUp_prediction_correction_
+ * advection_node_node (HybridGrains2DSim.cpp:116-220), nsteps times; flags
+ * add the per-step ResamplingTools::homogenizeStress / homogenizeVelocity
+ * accumulation (ResamplingTools.cpp:744-884). Resampling and zone
+ * relabelling run on the host between calls. */
+hg_status hg_hybrid_step(hg_hybrid *h, double dt, int32_t nsteps,
+                         int32_t flags);
+/* ResamplingTools::clearHomogenizedStress / clearHomogenizedVelocity. */
+hg_status hg_hybrid_clear_homogenized(hg_hybrid *h);
+hg_status hg_hybrid_num_packed(hg_hybrid *h, int64_t *num_grains,
+                               int64_t *num_nodes);
+/* Coupling buffers of the last step (Coupling.h:52-70): packed coupled
+ * grain and node lists, DEM mass/momentum grids, v/a after coupling, grid
+ * homog_factor, homogenized stress (4 per node) and velocity (2 per node).
+ * Any pointer may be NULL. */
+hg_status hg_hybrid_download(hg_hybrid *h, int32_t *packed_grains,
+                             int32_t *packed_nodes, double *dem_mass_grid,
+                             double *dem_momentum_grid, double *v_after,
+                             double *a_after, double *homog_factor,
+                             double *homog_stress, double *homog_velocity);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HG_GPU_H */

@@ -1,0 +1,362 @@
+"""GB300-native per-timestep core of libHybridGrains (Python host binding).
+
+The compute lives in ``libhg_gpu.so`` (hand-written sm_103a CUDA behind the C
+ABI of ``include/hg_gpu.h``). This module binds that ABI with ctypes and numpy
+and mirrors the reference's integrator surface:
+
+* ``MPM``     - SimulationState + ExplicitIntegrator (mpmgrains2d):
+                ``flow(dt)``, ``flow_zero_phase()``, ``flow_first_phase(dt)``,
+                ``flow_second_phase(dt)``.
+* ``DEM``     - RigidBody2DSim + PenaltyImpactFrictionMap (rigidbody2d):
+                ``flow(dt)``, ``flow_with_weights(dt)``.
+* ``Hybrid``  - HybridGrains2DSim node-node step (hybridgrains2dnew).
+
+There is no CPU fallback: constructing any object loads the CUDA library and
+raises if it is missing or no GPU is present.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _capi
+from ._capi import HGError, check, load  # noqa: F401
+
+__all__ = ["Context", "MPM", "DEM", "Hybrid", "HGError", "load", "kernel_launch_count"]
+
+LINEAR, UGIMP = 0, 1
+FP64, MIXED = 0, 1
+
+
+def _d(a):
+    return None if a is None else a.ctypes.data_as(_capi._D)
+
+
+def _i32(a):
+    return None if a is None else a.ctypes.data_as(_capi._I32)
+
+
+def _u8(a):
+    return None if a is None else a.ctypes.data_as(_capi._U8)
+
+
+def _f64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+def kernel_launch_count():
+    """Kernels launched by libhg_gpu in this process so far."""
+    return int(load().hg_kernel_launch_count())
+
+
+class Context:
+    """A device and the CUDA stream all objects of the context run on."""
+
+    def __init__(self, device=0):
+        load()
+        h = ctypes.c_void_p()
+        check("hg_context_create", int(device), ctypes.byref(h))
+        self._h = h
+        self.device = device
+
+    def synchronize(self):
+        check("hg_context_synchronize", self._h)
+
+    def timer_begin(self):
+        check("hg_context_timer_begin", self._h)
+
+    def timer_end(self):
+        """Milliseconds on the context stream since timer_begin (synchronises)."""
+        ms = ctypes.c_double()
+        check("hg_context_timer_end", self._h, ctypes.byref(ms))
+        return ms.value
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _capi.load().hg_context_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class MPM:
+    """Material points + physics grid on the device (mpmgrains2d SimulationState).
+
+    planes: iterable of (x[2], n[2], sticking: bool, lower_bound) like
+    MPMStaticPlane. precision: MIXED (FP64 positions, FP32 elsewhere) or FP64.
+    """
+
+    def __init__(self, ctx, grid_min, grid_max, cell_width, shear_modulus, bulk_modulus,
+                 dp_alpha, flip_alpha, gravity=(0.0, -9.81), planes=(), basis=LINEAR,
+                 precision=MIXED, capacity=0):
+        self.ctx = ctx
+        d = _capi.MpmDesc()
+        d.grid_min[:] = list(map(float, grid_min))
+        d.grid_max[:] = list(map(float, grid_max))
+        d.cell_width = float(cell_width)
+        d.basis = int(basis)
+        d.precision = int(precision)
+        d.shear_modulus = float(shear_modulus)
+        d.bulk_modulus = float(bulk_modulus)
+        d.dp_alpha = float(dp_alpha)
+        d.flip_alpha = float(flip_alpha)
+        d.gravity[:] = list(map(float, gravity))
+        planes = list(planes)
+        d.num_planes = len(planes)
+        for k, pl in enumerate(planes):
+            x, n = pl[0], pl[1]
+            st = pl[2] if len(pl) > 2 else True
+            lb = pl[3] if len(pl) > 3 else -np.inf
+            d.planes[k].x[:] = list(map(float, x))
+            d.planes[k].n[:] = list(map(float, n))
+            d.planes[k].sticking = 1 if st else 0
+            d.planes[k].lower_bound = float(lb)
+        d.capacity = int(capacity)
+        h = ctypes.c_void_p()
+        check("hg_mpm_create", ctx._h, ctypes.byref(d), ctypes.byref(h))
+        self._h = h
+        self.precision = precision
+        self.basis = basis
+        gmin = np.zeros(2)
+        gmax = np.zeros(2)
+        cc = np.zeros(2, dtype=np.int32)
+        check("hg_mpm_grid_info", h, _d(gmin), _d(gmax), _i32(cc))
+        self.grid_min, self.grid_max = gmin, gmax
+        self.nx, self.ny = int(cc[0]), int(cc[1])
+        self.nnodes = (self.nx + 1) * (self.ny + 1)
+        self.n = 0
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _capi.load().hg_mpm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def seed_rectangle(self, rmin, rmax, density, samples_per_dim, vel=(0.0, 0.0), omega=0.0):
+        """InitialSimulationState rasterizeRectangle: returns particle arrays."""
+        cnt = ctypes.c_int64()
+        rmin, rmax, vel = _f64(rmin), _f64(rmax), _f64(vel)
+        check("hg_mpm_seed_rectangle", self._h, _d(rmin), _d(rmax), float(density),
+              int(samples_per_dim), _d(vel), float(omega), 0, None, None, None, None, None,
+              ctypes.byref(cnt))
+        n = cnt.value
+        q, v = np.zeros((n, 2)), np.zeros((n, 2))
+        m, vol, hl = np.zeros(n), np.zeros(n), np.zeros(n)
+        check("hg_mpm_seed_rectangle", self._h, _d(rmin), _d(rmax), float(density),
+              int(samples_per_dim), _d(vel), float(omega), n, _d(q), _d(v), _d(m), _d(vol),
+              _d(hl), ctypes.byref(cnt))
+        return dict(q=q, v=v, m=m, vol=vol, hl=hl)
+
+    def upload(self, q, v, m, vol, hl=None, be=None, J=None, jh=None, kin=None):
+        """MaterialPoints::setPoints. q, v: (N, 2); be: (N, 4) column-major."""
+        q, v, m, vol = _f64(q), _f64(v), _f64(m), _f64(vol)
+        hl, be, J = _f64(hl), _f64(be), _f64(J)
+        jh = None if jh is None else np.ascontiguousarray(jh, dtype=np.int32)
+        kin = None if kin is None else np.ascontiguousarray(kin, dtype=np.uint8)
+        n = len(m)
+        check("hg_mpm_upload", self._h, n, _d(q), _d(v), _d(m), _d(vol), _d(hl), _d(be), _d(J),
+              _i32(jh), _u8(kin))
+        self.n = n
+
+    def download(self):
+        n = self.n
+        q, v, be = np.zeros((n, 2)), np.zeros((n, 2)), np.zeros((n, 4))
+        J = np.zeros(n)
+        jh = np.zeros(n, dtype=np.int32)
+        check("hg_mpm_download", self._h, _d(q), _d(v), _d(be), _d(J), _i32(jh))
+        return dict(q=q, v=v, be=be, J=J, jh=jh)
+
+    def download_into(self, q=None, v=None, be=None, J=None, jh=None):
+        """Download into caller-provided (e.g. pinned) buffers."""
+        check("hg_mpm_download", self._h, _d(q), _d(v), _d(be), _d(J), _i32(jh))
+
+    def grid(self):
+        nn = self.nnodes
+        mass = np.zeros(nn)
+        vel, acc = np.zeros((nn, 2)), np.zeros((nn, 2))
+        if self.precision == FP64:
+            mom, mom_new, force = np.zeros((nn, 2)), np.zeros((nn, 2)), np.zeros((nn, 2))
+            check("hg_mpm_download_grid", self._h, _d(mass), _d(mom), _d(mom_new), _d(force),
+                  _d(vel), _d(acc))
+            return dict(mass=mass, mom=mom, mom_new=mom_new, force=force, vel=vel, acc=acc)
+        check("hg_mpm_download_grid", self._h, _d(mass), None, None, None, _d(vel), _d(acc))
+        return dict(mass=mass, vel=vel, acc=acc)
+
+    def cell_index(self):
+        cells = np.zeros((self.n, 2), dtype=np.int32)
+        check("hg_mpm_cell_index", self._h, _i32(cells))
+        return cells
+
+    # ExplicitIntegrator surface (mpmgrains2d/ExplicitIntegrator.h:8-20)
+    def flow(self, dt, nsteps=1):
+        check("hg_mpm_step", self._h, float(dt), int(nsteps))
+
+    step = flow
+
+    def flow_zero_phase(self):
+        check("hg_mpm_phase0", self._h)
+
+    def flow_first_phase(self, dt):
+        check("hg_mpm_phase1", self._h, float(dt))
+
+    def flow_second_phase(self, dt):
+        check("hg_mpm_phase2", self._h, float(dt))
+
+    def status(self):
+        w = ctypes.c_uint32()
+        check("hg_mpm_status", self._h, ctypes.byref(w))
+        return w.value
+
+    def clear_status(self):
+        check("hg_mpm_clear_status", self._h)
+
+    def profile(self, enable=True):
+        check("hg_mpm_profile", self._h, 1 if enable else 0)
+
+    def profile_read(self):
+        """(fused G2P/P2G ms, grid-update ms, steps) summed since profile(True)."""
+        a, b, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_int64()
+        check("hg_mpm_profile_read", self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(n))
+        return a.value, b.value, n.value
+
+    def rebin_count(self):
+        c = ctypes.c_int64()
+        check("hg_mpm_rebin_count", self._h, ctypes.byref(c))
+        return c.value
+
+
+class DEM:
+    """Circle bodies with the penalty impact-friction map (rigidbody2d)."""
+
+    def __init__(self, ctx, gravity, kn, kt, gamman, gammat, mu, planes=(), cell_scale=1.0,
+                 capacity=0, contact_capacity=0):
+        self.ctx = ctx
+        d = _capi.DemDesc()
+        d.gravity[:] = list(map(float, gravity))
+        d.kn, d.kt, d.gamman, d.gammat, d.mu = map(float, (kn, kt, gamman, gammat, mu))
+        d.cell_scale = float(cell_scale)
+        planes = list(planes)
+        d.num_planes = len(planes)
+        for k, (x, n) in enumerate(planes):
+            d.planes[k].x[:] = list(map(float, x))
+            d.planes[k].n[:] = list(map(float, n))
+        d.capacity = int(capacity)
+        d.contact_capacity = int(contact_capacity or 8 * max(capacity, 1))
+        h = ctypes.c_void_p()
+        check("hg_dem_create", ctx._h, ctypes.byref(d), ctypes.byref(h))
+        self._h = h
+        self.n = 0
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _capi.load().hg_dem_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, q, v, r, m, I, fixed=None):
+        """q, v: (N, 3) as (x, y, theta); m = rho pi r^2, I = m r^2 / 2."""
+        q, v, r, m, I = map(_f64, (q, v, r, m, I))
+        fx = None if fixed is None else np.ascontiguousarray(fixed, dtype=np.uint8)
+        n = len(r)
+        check("hg_dem_upload", self._h, n, _d(q), _d(v), _d(r), _d(m), _d(I), _u8(fx))
+        self.n = n
+
+    def set_weights(self, w):
+        check("hg_dem_set_weights", self._h, _d(_f64(w)))
+
+    def set_state(self, q=None, v=None):
+        check("hg_dem_set_state", self._h, _d(_f64(q)), _d(_f64(v)))
+
+    def download(self):
+        q, v = np.zeros((self.n, 3)), np.zeros((self.n, 3))
+        check("hg_dem_download", self._h, _d(q), _d(v))
+        return q, v
+
+    def flow(self, dt, nsteps=1):
+        check("hg_dem_step", self._h, float(dt), int(nsteps), 0)
+
+    def flow_with_weights(self, dt, nsteps=1):
+        check("hg_dem_step", self._h, float(dt), int(nsteps), 1)
+
+    def contacts(self):
+        cnt = ctypes.c_int64()
+        check("hg_dem_download_contacts", self._h, 0, None, ctypes.byref(cnt))
+        rec = np.zeros((max(cnt.value, 1), _capi.HG_DEM_RECORD_WIDTH))
+        check("hg_dem_download_contacts", self._h, cnt.value, _d(rec), ctypes.byref(cnt))
+        return rec[: cnt.value]
+
+    def status(self):
+        w = ctypes.c_uint32()
+        check("hg_dem_status", self._h, ctypes.byref(w))
+        return w.value
+
+
+def candidate_pairs(ctx, aabb_min, aabb_max):
+    """SpatialGrid::getPotentialOverlaps on the device: sorted (i, j), i < j."""
+    mn, mx = _f64(aabb_min), _f64(aabb_max)
+    n = mn.shape[0]
+    cnt = ctypes.c_int64()
+    check("hg_dem_candidate_pairs", ctx._h, n, _d(mn), _d(mx), 0, None, ctypes.byref(cnt))
+    pairs = np.zeros((max(cnt.value, 1), 2), dtype=np.int32)
+    check("hg_dem_candidate_pairs", ctx._h, n, _d(mn), _d(mx), cnt.value, _i32(pairs),
+          ctypes.byref(cnt))
+    return pairs[: cnt.value]
+
+
+class Hybrid:
+    """HybridGrains2DSim node-node step over an FP64 MPM and a DEM object."""
+
+    HOMOGENIZE_STRESS = 1
+    HOMOGENIZE_VELOCITY = 2
+
+    def __init__(self, ctx, mpm, dem):
+        self.ctx, self.mpm, self.dem = ctx, mpm, dem
+        h = ctypes.c_void_p()
+        check("hg_hybrid_create", ctx._h, mpm._h, dem._h, ctypes.byref(h))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _capi.load().hg_hybrid_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, dt, nsteps=1, homogenize_stress=False, homogenize_velocity=False):
+        flags = (1 if homogenize_stress else 0) | (2 if homogenize_velocity else 0)
+        check("hg_hybrid_step", self._h, float(dt), int(nsteps), flags)
+
+    def clear_homogenized(self):
+        check("hg_hybrid_clear_homogenized", self._h)
+
+    def coupling(self):
+        ng, nn_ = ctypes.c_int64(), ctypes.c_int64()
+        check("hg_hybrid_num_packed", self._h, ctypes.byref(ng), ctypes.byref(nn_))
+        nn = self.mpm.nnodes
+        pg = np.zeros(max(ng.value, 1), dtype=np.int32)
+        pn = np.zeros(max(nn_.value, 1), dtype=np.int32)
+        dm, dp = np.zeros(nn), np.zeros((nn, 2))
+        va, aa = np.zeros((nn, 2)), np.zeros((nn, 2))
+        hf, hs, hv = np.zeros(nn), np.zeros((nn, 4)), np.zeros((nn, 2))
+        check("hg_hybrid_download", self._h, _i32(pg), _i32(pn), _d(dm), _d(dp), _d(va), _d(aa),
+              _d(hf), _d(hs), _d(hv))
+        return dict(packed_dem=pg[: ng.value], packed_mpm=pn[: nn_.value], dem_mass_grid=dm,
+                    dem_mom_grid=dp, v_after=va, at_after=aa, homog_factor=hf, homog_stress=hs,
+                    homog_velocity=hv)

@@ -1,0 +1,87 @@
+"""Build recipe for libhg_gpu.so (the C-ABI CUDA library), in-tree.
+
+Each translation unit is compiled for sm_103a only, in parallel, and linked
+into ``libhybridgrains_gb300/_build/libhg_gpu.so``. Translation units that
+restate the reference's FP64 arithmetic are compiled with ``--fmad=false`` so
+that every multiply and add rounds separately, matching the operation order of
+the reference's expressions; the mixed-precision path keeps FMA contraction.
+"""
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+INCLUDE = os.path.join(ROOT, "include")
+OUT_DIR = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT_DIR, "libhg_gpu.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# (source, exact-FP64 translation unit)
+SOURCES = [
+    ("capi.cu", True),
+    ("scan.cu", False),
+    ("mpm_fp64.cu", True),
+    ("mpm_mixed.cu", False),
+    ("dem.cu", True),
+    ("coupling.cu", True),
+]
+HEADERS = ["hg_internal.cuh", "mpm_basis.cuh"]
+
+
+def _nvcc():
+    cand = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
+    return cand if os.path.exists(cand) else "nvcc"
+
+
+def _compile(src, exact, verbose):
+    obj = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
+    # -ffp-contract=off keeps the host-side seeding and grid set-up rounding
+    # identical on x86 and on Arm (where GCC would otherwise fuse a*b+c).
+    cmd = [_nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+           "-Xcompiler", "-ffp-contract=off",
+           "-I", INCLUDE, "-I", CSRC, "-c", os.path.join(CSRC, src), "-o", obj]
+    if exact:
+        cmd.insert(1, "--fmad=false")
+    if verbose:
+        cmd.insert(1, "-Xptxas=-v")
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc failed for %s:\n%s%s" % (src, r.stdout, r.stderr))
+    return obj, r.stderr
+
+
+def _stale():
+    if not os.path.exists(LIB):
+        return True
+    t = os.path.getmtime(LIB)
+    deps = [os.path.join(CSRC, s) for s, _ in SOURCES] + [os.path.join(CSRC, h) for h in HEADERS]
+    deps.append(os.path.join(INCLUDE, "hg_gpu.h"))
+    deps.append(os.path.abspath(__file__))
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(force=False, verbose=False):
+    """Compile and link libhg_gpu.so if any source is newer than it."""
+    if not force and not _stale():
+        return LIB
+    os.makedirs(OUT_DIR, exist_ok=True)
+    with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+        results = list(ex.map(lambda s: _compile(s[0], s[1], verbose), SOURCES))
+    if verbose:
+        for _, log in results:
+            sys.stderr.write(log)
+    objs = [o for o, _ in results]
+    tmp = LIB + ".tmp"
+    cmd = [_nvcc(), *ARCH, "-shared", "-o", tmp] + objs
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

@@ -1,0 +1,937 @@
+// extern "C" entry points of libhg_gpu (declared in include/hg_gpu.h):
+// argument validation, host<->device staging and dispatch to the kernels.
+#include "hg_internal.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <new>
+#include <string>
+#include <vector>
+
+namespace hg {
+
+std::atomic<int64_t> g_launches{0};
+
+namespace {
+thread_local std::string t_last_error;
+}
+
+void set_error(const std::string &msg) { t_last_error = msg; }
+
+hg_status fail(hg_status s, const std::string &msg) {
+  set_error(msg);
+  return s;
+}
+
+hg_status cuda_fail(cudaError_t e, const char *what) {
+  set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? HG_ERR_OUT_OF_MEMORY : HG_ERR_CUDA;
+}
+
+const char *last_error_cstr() { return t_last_error.c_str(); }
+
+void context_retain(hg_context *c) { ++c->refs; }
+
+void context_release(hg_context *c) {
+  if (--c->refs > 0) return;
+  int prev = -1;
+  cudaGetDevice(&prev);
+  if (prev != c->device) cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  cudaStreamDestroy(c->stream);
+  if (c->t0) cudaEventDestroy(c->t0);
+  if (c->t1) cudaEventDestroy(c->t1);
+  if (prev >= 0 && prev != c->device) cudaSetDevice(prev);
+  delete c;
+}
+
+} // namespace hg
+
+using namespace hg;
+
+namespace capi_impl {
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+bool finite_all(const double *a, int k) {
+  for (int i = 0; i < k; ++i)
+    if (!std::isfinite(a[i])) return false;
+  return true;
+}
+
+template <typename T>
+hg_status h2d(cudaStream_t s, T *dst, const T *src, size_t n) {
+  if (n == 0) return HG_OK;
+  HG_CUDA_TRY(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyHostToDevice, s));
+  return HG_OK;
+}
+
+template <typename T>
+hg_status d2h(cudaStream_t s, T *dst, const T *src, size_t n) {
+  if (n == 0 || dst == nullptr) return HG_OK;
+  HG_CUDA_TRY(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDeviceToHost, s));
+  return HG_OK;
+}
+
+__global__ void k_fill_d(double *a, int64_t n, double v, int stride, int comp) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) a[(int64_t)stride * i + comp] = v;
+}
+
+hg_status fill(cudaStream_t s, double *a, int64_t n, double v, int stride = 1, int comp = 0) {
+  if (n <= 0) return HG_OK;
+  HG_LAUNCH(k_fill_d, (int)((n + 255) / 256), 256, 0, s, a, n, v, stride, comp);
+  HG_CHECK_LAUNCH();
+  return HG_OK;
+}
+
+__global__ void k_cells_fp64(int64_t n, const double *__restrict__ q, double gx, double gy,
+                             double h, int32_t *cells) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  cells[2 * p] = (int32_t)floor((q[2 * p] - gx) / h);
+  cells[2 * p + 1] = (int32_t)floor((q[2 * p + 1] - gy) / h);
+}
+
+__global__ void k_cells_mixed(int64_t n, const double2 *__restrict__ u,
+                              const int32_t *__restrict__ id, int32_t *cells) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int64_t o = id[k];
+  const double2 uu = u[k];
+  cells[2 * o] = (int32_t)floor(uu.x);
+  cells[2 * o + 1] = (int32_t)floor(uu.y);
+}
+
+// PhysicsGrid::setDimensions (mpmgrains2d/PhysicsGrid.cpp:14-55).
+void set_dimensions(MpmParams &P, const double gmin[2], const double gmax[2], double h) {
+  const double cx = 0.5 * (gmin[0] + gmax[0]), cy = 0.5 * (gmin[1] + gmax[1]);
+  double wx = gmax[0] - gmin[0], wy = gmax[1] - gmin[1];
+  P.nx = (int)std::ceil(wx / h);
+  P.ny = (int)std::ceil(wy / h);
+  wx = (double)P.nx * h;
+  wy = (double)P.ny * h;
+  P.gmin[0] = cx - 0.5 * wx;
+  P.gmin[1] = cy - 0.5 * wy;
+  P.gmax[0] = cx + 0.5 * wx;
+  P.gmax[1] = cy + 0.5 * wy;
+  P.h = h;
+  P.inv_h = 1.0 / h;
+}
+
+} // namespace capi_impl
+
+using namespace capi_impl;
+
+extern "C" {
+
+const char *hg_status_string(hg_status s) {
+  switch (s) {
+  case HG_OK: return "ok";
+  case HG_ERR_INVALID_ARGUMENT: return "invalid argument";
+  case HG_ERR_CUDA: return "CUDA error";
+  case HG_ERR_OUT_OF_MEMORY: return "out of device memory";
+  case HG_ERR_CAPACITY: return "capacity exceeded";
+  case HG_ERR_UNSUPPORTED: return "unsupported";
+  case HG_ERR_DEVICE_STATUS: return "device status word set";
+  default: return "unknown status";
+  }
+}
+
+const char *hg_last_error(void) { return hg::last_error_cstr(); }
+
+int64_t hg_kernel_launch_count(void) { return g_launches.load(); }
+
+// ---- context --------------------------------------------------------------
+
+hg_status hg_context_create(int32_t device, hg_context **out) {
+  if (!out) return fail(HG_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  int count = 0;
+  HG_CUDA_TRY(cudaGetDeviceCount(&count));
+  if (device < 0 || device >= count)
+    return fail(HG_ERR_INVALID_ARGUMENT, "device index out of range");
+  DeviceGuard g(device);
+  hg_context *c = new (std::nothrow) hg_context();
+  if (!c) return fail(HG_ERR_OUT_OF_MEMORY, "host allocation failed");
+  c->device = device;
+  cudaError_t e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete c;
+    return cuda_fail(e, "context creation");
+  }
+  *out = c;
+  return HG_OK;
+}
+
+hg_status hg_context_destroy(hg_context *ctx) {
+  if (!ctx) return HG_OK;
+  context_release(ctx);
+  return HG_OK;
+}
+
+hg_status hg_context_timer_begin(hg_context *ctx) {
+  if (!ctx) return fail(HG_ERR_INVALID_ARGUMENT, "ctx is NULL");
+  DeviceGuard g(ctx->device);
+  if (!ctx->t0) HG_CUDA_TRY(cudaEventCreate(&ctx->t0));
+  if (!ctx->t1) HG_CUDA_TRY(cudaEventCreate(&ctx->t1));
+  HG_CUDA_TRY(cudaEventRecord(ctx->t0, ctx->stream));
+  return HG_OK;
+}
+
+hg_status hg_context_timer_end(hg_context *ctx, double *ms) {
+  if (!ctx || !ms) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (!ctx->t0) return fail(HG_ERR_INVALID_ARGUMENT, "timer not started");
+  DeviceGuard g(ctx->device);
+  HG_CUDA_TRY(cudaEventRecord(ctx->t1, ctx->stream));
+  HG_CUDA_TRY(cudaEventSynchronize(ctx->t1));
+  float f = 0.f;
+  HG_CUDA_TRY(cudaEventElapsedTime(&f, ctx->t0, ctx->t1));
+  *ms = f;
+  return HG_OK;
+}
+
+hg_status hg_context_synchronize(hg_context *ctx) {
+  if (!ctx) return fail(HG_ERR_INVALID_ARGUMENT, "ctx is NULL");
+  DeviceGuard g(ctx->device);
+  HG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return HG_OK;
+}
+
+// ---- MPM --------------------------------------------------------------------
+
+hg_status hg_mpm_create(hg_context *ctx, const hg_mpm_desc *d, hg_mpm **out) {
+  if (!ctx || !d || !out) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  *out = nullptr;
+  if (!(d->cell_width > 0.0) || !std::isfinite(d->cell_width))
+    return fail(HG_ERR_INVALID_ARGUMENT, "cell_width must be positive and finite");
+  if (!finite_all(d->grid_min, 2) || !finite_all(d->grid_max, 2) ||
+      !(d->grid_max[0] > d->grid_min[0]) || !(d->grid_max[1] > d->grid_min[1]))
+    return fail(HG_ERR_INVALID_ARGUMENT, "grid_max must exceed grid_min");
+  if (d->basis != HG_BASIS_LINEAR && d->basis != HG_BASIS_UGIMP)
+    return fail(HG_ERR_INVALID_ARGUMENT, "unknown basis");
+  if (d->precision != HG_PRECISION_FP64 && d->precision != HG_PRECISION_MIXED)
+    return fail(HG_ERR_INVALID_ARGUMENT, "unknown precision");
+  if (d->precision == HG_PRECISION_MIXED && d->basis != HG_BASIS_LINEAR)
+    return fail(HG_ERR_UNSUPPORTED, "MIXED precision supports the linear basis only");
+  if (d->num_planes < 0 || d->num_planes > HG_MAX_PLANES)
+    return fail(HG_ERR_INVALID_ARGUMENT, "num_planes out of range");
+  if (d->capacity < 0 || d->capacity > (int64_t)INT32_MAX)
+    return fail(HG_ERR_INVALID_ARGUMENT, "capacity out of range");
+  if (!finite_all(d->gravity, 2)) return fail(HG_ERR_INVALID_ARGUMENT, "gravity not finite");
+  const double cw = (d->grid_max[0] - d->grid_min[0]) / d->cell_width;
+  const double ch = (d->grid_max[1] - d->grid_min[1]) / d->cell_width;
+  if (cw > 1.0e6 || ch > 1.0e6) return fail(HG_ERR_INVALID_ARGUMENT, "grid too large");
+  DeviceGuard g(ctx->device);
+  hg_mpm *m = new (std::nothrow) hg_mpm();
+  if (!m) return fail(HG_ERR_OUT_OF_MEMORY, "host allocation failed");
+  m->ctx = ctx;
+  context_retain(ctx);
+  MpmParams &P = m->p;
+  set_dimensions(P, d->grid_min, d->grid_max, d->cell_width);
+  P.basis = d->basis;
+  P.precision = d->precision;
+  P.mu = d->shear_modulus;
+  P.kappa = d->bulk_modulus;
+  P.dp_alpha = d->dp_alpha;
+  P.flip_alpha = d->flip_alpha;
+  P.g[0] = d->gravity[0];
+  P.g[1] = d->gravity[1];
+  P.nplanes = d->num_planes;
+  for (int k = 0; k < d->num_planes; ++k) {
+    const hg_mpm_plane &pl = d->planes[k];
+    const double nn = std::sqrt(pl.n[0] * pl.n[0] + pl.n[1] * pl.n[1]);
+    if (!(nn > 0.0) || !finite_all(pl.x, 2) || std::isnan(pl.lower_bound)) {
+      hg_mpm_destroy(m);
+      return fail(HG_ERR_INVALID_ARGUMENT, "invalid plane");
+    }
+    MpmPlaneDev &q = P.planes[k];
+    q.x[0] = pl.x[0];
+    q.x[1] = pl.x[1];
+    q.n[0] = pl.n[0] / nn; // StaticPlane.cpp:6-12 normalises the normal
+    q.n[1] = pl.n[1] / nn;
+    q.sticking = pl.sticking ? 1 : 0;
+    q.lower_bound = pl.lower_bound;
+    q.ux[0] = (pl.x[0] - P.gmin[0]) / P.h;
+    q.ux[1] = (pl.x[1] - P.gmin[1]) / P.h;
+    q.ulb = (pl.lower_bound - P.gmin[1]) / P.h;
+    q.fux[0] = (float)q.ux[0];
+    q.fux[1] = (float)q.ux[1];
+    q.fulb = (float)q.ulb;
+  }
+  m->cap = d->capacity;
+  hg_status st = m->status.alloc(1);
+  if (st == HG_OK) {
+    cudaError_t e = cudaMemsetAsync(m->status.p, 0, sizeof(uint32_t), ctx->stream);
+    if (e != cudaSuccess) st = cuda_fail(e, "cudaMemsetAsync");
+  }
+  const int64_t nn = (int64_t)(P.nx + 1) * (P.ny + 1);
+  if (st == HG_OK && P.precision == HG_PRECISION_FP64) {
+    if ((st = m->q.alloc(2 * m->cap)) || (st = m->v.alloc(2 * m->cap)) ||
+        (st = m->m.alloc(m->cap)) || (st = m->vol.alloc(m->cap)) ||
+        (st = m->hl.alloc(m->cap)) || (st = m->be.alloc(4 * m->cap)) ||
+        (st = m->J.alloc(m->cap)) || (st = m->sigma.alloc(4 * m->cap)) ||
+        (st = m->jh.alloc(m->cap)) || (st = m->kin.alloc(m->cap)) ||
+        (st = m->g_mass.alloc(nn)) || (st = m->g_mom.alloc(2 * nn)) ||
+        (st = m->g_mom_new.alloc(2 * nn)) || (st = m->g_force.alloc(2 * nn)) ||
+        (st = m->g_vel.alloc(2 * nn)) || (st = m->g_acc.alloc(2 * nn)) ||
+        (st = m->g_cforce.alloc(2 * nn)) || (st = m->g_homog.alloc(nn)) ||
+        (st = m->g_hyb.alloc(nn))) {
+    } else {
+      cudaStream_t s = ctx->stream;
+      cudaMemsetAsync(m->g_cforce.p, 0, sizeof(double) * 2 * nn, s);
+      cudaMemsetAsync(m->g_hyb.p, 0, sizeof(int32_t) * nn, s);
+      cudaMemsetAsync(m->g_mass.p, 0, sizeof(double) * nn, s);
+      cudaMemsetAsync(m->g_mom.p, 0, sizeof(double) * 2 * nn, s);
+      cudaMemsetAsync(m->g_mom_new.p, 0, sizeof(double) * 2 * nn, s);
+      cudaMemsetAsync(m->g_force.p, 0, sizeof(double) * 2 * nn, s);
+      cudaMemsetAsync(m->g_vel.p, 0, sizeof(double) * 2 * nn, s);
+      cudaMemsetAsync(m->g_acc.p, 0, sizeof(double) * 2 * nn, s);
+      st = fill(s, m->g_homog.p, nn, 1.0);
+    }
+  } else if (st == HG_OK) {
+    st = mixed_alloc(m);
+  }
+  if (st == HG_OK) {
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) st = cuda_fail(e, "hg_mpm_create");
+  }
+  if (st != HG_OK) {
+    hg_mpm_destroy(m);
+    return st;
+  }
+  *out = m;
+  return HG_OK;
+}
+
+hg_status hg_mpm_destroy(hg_mpm *m) {
+  if (!m) return HG_OK;
+  hg_context *ctx = m->ctx;
+  {
+    DeviceGuard g(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    if (m->h_outside) cudaFreeHost(m->h_outside);
+    if (m->outside_ev) cudaEventDestroy(m->outside_ev);
+    for (cudaEvent_t e : m->prof_events) cudaEventDestroy(e);
+    delete m;
+  }
+  context_release(ctx);
+  return HG_OK;
+}
+
+hg_status hg_mpm_grid_info(hg_mpm *m, double gmin[2], double gmax[2], int32_t cc[2]) {
+  if (!m) return fail(HG_ERR_INVALID_ARGUMENT, "m is NULL");
+  if (gmin) {
+    gmin[0] = m->p.gmin[0];
+    gmin[1] = m->p.gmin[1];
+  }
+  if (gmax) {
+    gmax[0] = m->p.gmax[0];
+    gmax[1] = m->p.gmax[1];
+  }
+  if (cc) {
+    cc[0] = m->p.nx;
+    cc[1] = m->p.ny;
+  }
+  return HG_OK;
+}
+
+// InitialSimulationState.cpp:48-145
+hg_status hg_mpm_seed_rectangle(hg_mpm *m, const double rmin[2], const double rmax[2],
+                                double rho, int32_t npd, const double vel[2], double omega,
+                                int64_t cap, double *q, double *v, double *mass,
+                                double *volume, double *hl, int64_t *count) {
+  if (!m || !rmin || !rmax || !count) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (npd <= 0 || !(rho > 0.0)) return fail(HG_ERR_INVALID_ARGUMENT, "bad density or samples");
+  if (cap > 0 && (!q || !v || !mass || !volume || !hl))
+    return fail(HG_ERR_INVALID_ARGUMENT, "NULL output buffer");
+  const MpmParams &P = m->p;
+  if (rmin[0] < P.gmin[0] || rmin[1] < P.gmin[1])
+    return fail(HG_ERR_INVALID_ARGUMENT,
+                "initial rectangle region is below the simulation grid");
+  if (rmax[0] > P.gmax[0] || rmax[1] > P.gmax[1])
+    return fail(HG_ERR_INVALID_ARGUMENT,
+                "initial rectangle region is above the simulation grid");
+  const double v0x = vel ? vel[0] : 0.0, v0y = vel ? vel[1] : 0.0;
+  const unsigned bx0 = (unsigned)std::floor((rmin[0] - P.gmin[0]) / P.h);
+  const unsigned by0 = (unsigned)std::floor((rmin[1] - P.gmin[1]) / P.h);
+  const unsigned bx1 = (unsigned)std::ceil((rmax[0] - P.gmin[0]) / P.h);
+  const unsigned by1 = (unsigned)std::ceil((rmax[1] - P.gmin[1]) / P.h);
+  const double ctrx = 0.5 * (rmin[0] + rmax[0]), ctry = 0.5 * (rmin[1] + rmax[1]);
+  const double half = 0.5 * P.h / (double)npd;
+  const double pvol = half * half * 4.0;
+  const double pmass = rho * pvol;
+  int64_t k = 0;
+  for (unsigned gy = by0; gy < by1; ++gy)
+    for (unsigned gx = bx0; gx < bx1; ++gx)
+      for (int cy = 0; cy < npd; ++cy)
+        for (int cx = 0; cx < npd; ++cx) {
+          const double px = P.gmin[0] + P.h * ((double)gx + ((double)cx + 0.5) / (double)npd);
+          const double py = P.gmin[1] + P.h * ((double)gy + ((double)cy + 0.5) / (double)npd);
+          if (px < rmin[0] || py < rmin[1] || px > rmax[0] || py > rmax[1]) continue;
+          bool inside = false; // pointInsidePlane (InitialSimulationState.cpp:33-43)
+          for (int i = 0; i < P.nplanes; ++i) {
+            const MpmPlaneDev &pl = P.planes[i];
+            if (py < pl.lower_bound) break;
+            if (pl.n[0] * (px - pl.x[0]) + pl.n[1] * (py - pl.x[1]) < 0.0) {
+              inside = true;
+              break;
+            }
+          }
+          if (inside) continue;
+          if (k < cap) {
+            const double ax = px - ctrx, ay = py - ctry;
+            q[2 * k] = px;
+            q[2 * k + 1] = py;
+            v[2 * k] = v0x + omega * (-ay);
+            v[2 * k + 1] = v0y + omega * ax;
+            mass[k] = pmass;
+            volume[k] = pvol;
+            hl[k] = half;
+          }
+          ++k;
+        }
+  *count = k;
+  return HG_OK;
+}
+
+hg_status hg_mpm_upload(hg_mpm *m, int64_t n, const double *q, const double *v,
+                        const double *mass, const double *volume, const double *hl,
+                        const double *be, const double *J, const int32_t *jh,
+                        const uint8_t *kin) {
+  if (!m) return fail(HG_ERR_INVALID_ARGUMENT, "m is NULL");
+  if (n < 0) return fail(HG_ERR_INVALID_ARGUMENT, "negative particle count");
+  if (n > m->cap) return fail(HG_ERR_CAPACITY, "particle count exceeds capacity");
+  if (n > 0 && (!q || !v || !mass || !volume))
+    return fail(HG_ERR_INVALID_ARGUMENT, "q, v, mass and volume are required");
+  if (n > 0 && m->p.basis == HG_BASIS_UGIMP && !hl)
+    return fail(HG_ERR_INVALID_ARGUMENT, "hl is required for the uGIMP basis");
+  DeviceGuard g(m->ctx->device);
+  cudaStream_t s = m->ctx->stream;
+  m->n = n;
+  hg_status st = HG_OK;
+  if (m->p.precision == HG_PRECISION_FP64) {
+    if ((st = h2d(s, m->q.p, q, 2 * n)) || (st = h2d(s, m->v.p, v, 2 * n)) ||
+        (st = h2d(s, m->m.p, mass, n)) || (st = h2d(s, m->vol.p, volume, n)))
+      return st;
+    if (hl) {
+      if ((st = h2d(s, m->hl.p, hl, n))) return st;
+    } else if ((st = fill(s, m->hl.p, n, 0.0))) {
+      return st;
+    }
+    if (be) {
+      if ((st = h2d(s, m->be.p, be, 4 * n))) return st;
+    } else {
+      HG_CUDA_TRY(cudaMemsetAsync(m->be.p, 0, sizeof(double) * 4 * n, s));
+      if ((st = fill(s, m->be.p, n, 1.0, 4, 0)) || (st = fill(s, m->be.p, n, 1.0, 4, 3))) return st;
+    }
+    if (J) {
+      if ((st = h2d(s, m->J.p, J, n))) return st;
+    } else if ((st = fill(s, m->J.p, n, 1.0))) {
+      return st;
+    }
+    if (jh) {
+      if ((st = h2d(s, m->jh.p, jh, n))) return st;
+    } else {
+      HG_CUDA_TRY(cudaMemsetAsync(m->jh.p, 0, sizeof(int32_t) * n, s));
+    }
+    if (kin) {
+      if ((st = h2d(s, m->kin.p, kin, n))) return st;
+    } else {
+      HG_CUDA_TRY(cudaMemsetAsync(m->kin.p, 0, n, s));
+    }
+    HG_CUDA_TRY(cudaMemsetAsync(m->sigma.p, 0, sizeof(double) * 4 * n, s));
+  } else {
+    // stage in upload order, then convert and sort on the device
+    const int64_t nd = 11 * n;
+    if (m->stage_d.n < (size_t)nd && (st = m->stage_d.alloc(nd))) return st;
+    if (m->stage_i.n < (size_t)n && (st = m->stage_i.alloc(n))) return st;
+    if (m->stage_u8.n < (size_t)n && (st = m->stage_u8.alloc(n))) return st;
+    double *sq = m->stage_d.p, *sv = sq + 2 * n, *sm = sv + 2 * n, *svol = sm + n,
+           *sbe = svol + n, *sJ = sbe + 4 * n;
+    if ((st = h2d(s, sq, q, 2 * n)) || (st = h2d(s, sv, v, 2 * n)) ||
+        (st = h2d(s, sm, mass, n)) || (st = h2d(s, svol, volume, n)))
+      return st;
+    if (be) {
+      if ((st = h2d(s, sbe, be, 4 * n))) return st;
+    } else {
+      HG_CUDA_TRY(cudaMemsetAsync(sbe, 0, sizeof(double) * 4 * n, s));
+      if ((st = fill(s, sbe, n, 1.0, 4, 0)) || (st = fill(s, sbe, n, 1.0, 4, 3))) return st;
+    }
+    if (J) {
+      if ((st = h2d(s, sJ, J, n))) return st;
+    } else if ((st = fill(s, sJ, n, 1.0))) {
+      return st;
+    }
+    if (jh) {
+      if ((st = h2d(s, m->stage_i.p, jh, n))) return st;
+    } else {
+      HG_CUDA_TRY(cudaMemsetAsync(m->stage_i.p, 0, sizeof(int32_t) * n, s));
+    }
+    if (kin) {
+      if ((st = h2d(s, m->stage_u8.p, kin, n))) return st;
+    } else {
+      HG_CUDA_TRY(cudaMemsetAsync(m->stage_u8.p, 0, n, s));
+    }
+    m->primed = false;
+    if ((st = mixed_upload(m, sq, sv, sm, svol, sbe, sJ, m->stage_i.p, m->stage_u8.p)))
+      return st;
+  }
+  // the caller may reuse its buffers as soon as this returns
+  HG_CUDA_TRY(cudaStreamSynchronize(s));
+  return HG_OK;
+}
+
+hg_status hg_mpm_download(hg_mpm *m, double *q, double *v, double *be, double *J,
+                          int32_t *jh) {
+  if (!m) return fail(HG_ERR_INVALID_ARGUMENT, "m is NULL");
+  DeviceGuard g(m->ctx->device);
+  cudaStream_t s = m->ctx->stream;
+  const int64_t n = m->n;
+  hg_status st;
+  if (m->p.precision == HG_PRECISION_FP64) {
+    if ((st = d2h(s, q, m->q.p, 2 * n)) || (st = d2h(s, v, m->v.p, 2 * n)) ||
+        (st = d2h(s, be, m->be.p, 4 * n)) || (st = d2h(s, J, m->J.p, n)) ||
+        (st = d2h(s, jh, m->jh.p, n)))
+      return st;
+  } else {
+    const int64_t nd = 11 * n;
+    if (m->stage_d.n < (size_t)nd && (st = m->stage_d.alloc(nd))) return st;
+    if (m->stage_i.n < (size_t)n && (st = m->stage_i.alloc(n))) return st;
+    double *sq = m->stage_d.p, *sv = sq + 2 * n, *sbe = sv + 2 * n, *sJ = sbe + 4 * n;
+    if ((st = mixed_download(m, sq, sv, sbe, sJ, m->stage_i.p))) return st;
+    if ((st = d2h(s, q, sq, 2 * n)) || (st = d2h(s, v, sv, 2 * n)) ||
+        (st = d2h(s, be, sbe, 4 * n)) || (st = d2h(s, J, sJ, n)) ||
+        (st = d2h(s, jh, m->stage_i.p, n)))
+      return st;
+  }
+  HG_CUDA_TRY(cudaStreamSynchronize(s));
+  return HG_OK;
+}
+
+hg_status hg_mpm_num_particles(hg_mpm *m, int64_t *n) {
+  if (!m || !n) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  *n = m->n;
+  return HG_OK;
+}
+
+hg_status hg_mpm_step(hg_mpm *m, double dt, int32_t nsteps) {
+  if (!m) return fail(HG_ERR_INVALID_ARGUMENT, "m is NULL");
+  if (!(dt > 0.0) || !std::isfinite(dt)) return fail(HG_ERR_INVALID_ARGUMENT, "dt must be positive");
+  if (nsteps < 0) return fail(HG_ERR_INVALID_ARGUMENT, "negative step count");
+  DeviceGuard g(m->ctx->device);
+  if (m->p.precision == HG_PRECISION_MIXED) return mixed_step(m, dt, nsteps);
+  for (int k = 0; k < nsteps; ++k) {
+    hg_status st;
+    if ((st = mpm64_phase0(m)) || (st = mpm64_phase1(m, dt)) || (st = mpm64_phase2(m, dt)))
+      return st;
+  }
+  return HG_OK;
+}
+
+hg_status hg_mpm_phase0(hg_mpm *m) {
+  if (!m) return fail(HG_ERR_INVALID_ARGUMENT, "m is NULL");
+  if (m->p.precision != HG_PRECISION_FP64)
+    return fail(HG_ERR_UNSUPPORTED, "phase calls need FP64 precision");
+  DeviceGuard g(m->ctx->device);
+  return mpm64_phase0(m);
+}
+
+hg_status hg_mpm_phase1(hg_mpm *m, double dt) {
+  if (!m) return fail(HG_ERR_INVALID_ARGUMENT, "m is NULL");
+  if (m->p.precision != HG_PRECISION_FP64)
+    return fail(HG_ERR_UNSUPPORTED, "phase calls need FP64 precision");
+  if (!(dt > 0.0)) return fail(HG_ERR_INVALID_ARGUMENT, "dt must be positive");
+  DeviceGuard g(m->ctx->device);
+  return mpm64_phase1(m, dt);
+}
+
+hg_status hg_mpm_phase2(hg_mpm *m, double dt) {
+  if (!m) return fail(HG_ERR_INVALID_ARGUMENT, "m is NULL");
+  if (m->p.precision != HG_PRECISION_FP64)
+    return fail(HG_ERR_UNSUPPORTED, "phase calls need FP64 precision");
+  if (!(dt > 0.0)) return fail(HG_ERR_INVALID_ARGUMENT, "dt must be positive");
+  DeviceGuard g(m->ctx->device);
+  return mpm64_phase2(m, dt);
+}
+
+hg_status hg_mpm_download_grid(hg_mpm *m, double *mass, double *mom, double *mom_new,
+                               double *force, double *vel, double *acc) {
+  if (!m) return fail(HG_ERR_INVALID_ARGUMENT, "m is NULL");
+  DeviceGuard g(m->ctx->device);
+  cudaStream_t s = m->ctx->stream;
+  const int64_t nn = (int64_t)(m->p.nx + 1) * (m->p.ny + 1);
+  hg_status st;
+  if (m->p.precision == HG_PRECISION_FP64) {
+    if ((st = d2h(s, mass, m->g_mass.p, nn)) || (st = d2h(s, mom, m->g_mom.p, 2 * nn)) ||
+        (st = d2h(s, mom_new, m->g_mom_new.p, 2 * nn)) ||
+        (st = d2h(s, force, m->g_force.p, 2 * nn)) || (st = d2h(s, vel, m->g_vel.p, 2 * nn)) ||
+        (st = d2h(s, acc, m->g_acc.p, 2 * nn)))
+      return st;
+  } else {
+    if (mom || mom_new || force)
+      return fail(HG_ERR_UNSUPPORTED, "MIXED keeps mass, velocity and acceleration only");
+    if (m->stage_d.n < (size_t)(5 * nn) && (st = m->stage_d.alloc(5 * nn))) return st;
+    double *sm = m->stage_d.p, *sv = sm + nn, *sa = sv + 2 * nn;
+    if ((st = mixed_download_grid(m, sm, sv, sa))) return st;
+    if ((st = d2h(s, mass, sm, nn)) || (st = d2h(s, vel, sv, 2 * nn)) ||
+        (st = d2h(s, acc, sa, 2 * nn)))
+      return st;
+  }
+  HG_CUDA_TRY(cudaStreamSynchronize(s));
+  return HG_OK;
+}
+
+hg_status hg_mpm_cell_index(hg_mpm *m, int32_t *cells) {
+  if (!m || !cells) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  DeviceGuard g(m->ctx->device);
+  cudaStream_t s = m->ctx->stream;
+  const int64_t n = m->n;
+  if (n == 0) return HG_OK;
+  hg_status st;
+  if (m->stage_i.n < (size_t)(2 * n) && (st = m->stage_i.alloc(2 * n))) return st;
+  if (m->p.precision == HG_PRECISION_FP64) {
+    HG_LAUNCH(k_cells_fp64, (int)((n + 255) / 256), 256, 0, s, n, m->q.p, m->p.gmin[0],
+              m->p.gmin[1], m->p.h, m->stage_i.p);
+  } else {
+    HG_LAUNCH(k_cells_mixed, (int)((n + 255) / 256), 256, 0, s, n, m->mu_[m->cur].p,
+              m->mid_[m->cur].p, m->stage_i.p);
+  }
+  HG_CHECK_LAUNCH();
+  if ((st = d2h(s, cells, m->stage_i.p, 2 * n))) return st;
+  HG_CUDA_TRY(cudaStreamSynchronize(s));
+  return HG_OK;
+}
+
+hg_status hg_mpm_status(hg_mpm *m, uint32_t *word) {
+  if (!m || !word) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  DeviceGuard g(m->ctx->device);
+  HG_CUDA_TRY(cudaMemcpyAsync(word, m->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                              m->ctx->stream));
+  HG_CUDA_TRY(cudaStreamSynchronize(m->ctx->stream));
+  return HG_OK;
+}
+
+hg_status hg_mpm_clear_status(hg_mpm *m) {
+  if (!m) return fail(HG_ERR_INVALID_ARGUMENT, "m is NULL");
+  DeviceGuard g(m->ctx->device);
+  HG_CUDA_TRY(cudaMemsetAsync(m->status.p, 0, sizeof(uint32_t), m->ctx->stream));
+  return HG_OK;
+}
+
+hg_status hg_mpm_profile(hg_mpm *m, int32_t enable) {
+  if (!m) return fail(HG_ERR_INVALID_ARGUMENT, "m is NULL");
+  if (m->p.precision != HG_PRECISION_MIXED)
+    return fail(HG_ERR_UNSUPPORTED, "kernel profiling covers the MIXED path");
+  DeviceGuard g(m->ctx->device);
+  HG_CUDA_TRY(cudaStreamSynchronize(m->ctx->stream));
+  m->profile = enable != 0;
+  m->prof_used = 0;
+  return HG_OK;
+}
+
+hg_status hg_mpm_profile_read(hg_mpm *m, double *a, double *b, int64_t *steps) {
+  if (!m) return fail(HG_ERR_INVALID_ARGUMENT, "m is NULL");
+  DeviceGuard g(m->ctx->device);
+  return mixed_profile_read(m, a, b, steps);
+}
+
+hg_status hg_mpm_rebin_count(hg_mpm *m, int64_t *count) {
+  if (!m || !count) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  *count = m->rebins;
+  return HG_OK;
+}
+
+// ---- DEM ------------------------------------------------------------------------
+
+hg_status hg_dem_create(hg_context *ctx, const hg_dem_desc *d, hg_dem **out) {
+  if (!ctx || !d || !out) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  *out = nullptr;
+  if (d->num_planes < 0 || d->num_planes > HG_MAX_PLANES)
+    return fail(HG_ERR_INVALID_ARGUMENT, "num_planes out of range");
+  if (d->capacity < 0 || d->capacity > (int64_t)(1 << 30) || d->contact_capacity < 0 ||
+      d->contact_capacity > (int64_t)INT32_MAX)
+    return fail(HG_ERR_INVALID_ARGUMENT, "capacity out of range");
+  const double params[7] = {d->gravity[0], d->gravity[1], d->kn, d->kt, d->gamman,
+                            d->gammat, d->mu};
+  if (!finite_all(params, 7) || d->kn < 0 || d->kt < 0 || d->gamman < 0 || d->gammat < 0 ||
+      d->mu < 0)
+    return fail(HG_ERR_INVALID_ARGUMENT, "penalty parameters must be finite and >= 0");
+  DeviceGuard g(ctx->device);
+  hg_dem *dm = new (std::nothrow) hg_dem();
+  if (!dm) return fail(HG_ERR_OUT_OF_MEMORY, "host allocation failed");
+  dm->ctx = ctx;
+  context_retain(ctx);
+  DemParams &P = dm->p;
+  P.g[0] = d->gravity[0];
+  P.g[1] = d->gravity[1];
+  P.kn = d->kn;
+  P.kt = d->kt;
+  P.gn = d->gamman;
+  P.gt = d->gammat;
+  P.mu = d->mu;
+  P.cell_scale = d->cell_scale;
+  P.nplanes = d->num_planes;
+  for (int k = 0; k < d->num_planes; ++k) {
+    const hg_dem_plane &pl = d->planes[k];
+    // RigidBody2DSceneParser.cpp:264: planes are built with n.normalized()
+    const double n2 = pl.n[0] * pl.n[0] + pl.n[1] * pl.n[1];
+    if (!(n2 > 0.0) || !finite_all(pl.x, 2)) {
+      hg_dem_destroy(dm);
+      return fail(HG_ERR_INVALID_ARGUMENT, "invalid plane");
+    }
+    const double nn = std::sqrt(n2);
+    P.px[k][0] = pl.x[0];
+    P.px[k][1] = pl.x[1];
+    P.pn[k][0] = pl.n[0] / nn;
+    P.pn[k][1] = pl.n[1] / nn;
+  }
+  dm->cap = d->capacity;
+  dm->ccap = d->contact_capacity;
+  hg_status st = dem_alloc(dm);
+  if (st != HG_OK) {
+    hg_dem_destroy(dm);
+    return st;
+  }
+  *out = dm;
+  return HG_OK;
+}
+
+hg_status hg_dem_destroy(hg_dem *d) {
+  if (!d) return HG_OK;
+  hg_context *ctx = d->ctx;
+  {
+    DeviceGuard g(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    delete d;
+  }
+  context_release(ctx);
+  return HG_OK;
+}
+
+hg_status hg_dem_upload(hg_dem *d, int64_t n, const double *q, const double *v,
+                        const double *r, const double *mass, const double *inertia,
+                        const uint8_t *fixed) {
+  if (!d) return fail(HG_ERR_INVALID_ARGUMENT, "d is NULL");
+  if (n < 0) return fail(HG_ERR_INVALID_ARGUMENT, "negative body count");
+  if (n > d->cap) return fail(HG_ERR_CAPACITY, "body count exceeds capacity");
+  if (n > 0 && (!q || !v || !r || !mass || !inertia))
+    return fail(HG_ERR_INVALID_ARGUMENT, "q, v, radius, mass and inertia are required");
+  double rmax = 0.0;
+  for (int64_t i = 0; i < n; ++i) {
+    if (!(r[i] > 0.0) || !(mass[i] > 0.0) || !(inertia[i] > 0.0) || !std::isfinite(r[i]))
+      return fail(HG_ERR_INVALID_ARGUMENT, "radius, mass and inertia must be positive");
+    rmax = std::max(rmax, r[i]);
+  }
+  DeviceGuard g(d->ctx->device);
+  // Broadphase cell width: the widest disk AABB plus a relative margin, so a
+  // disk's partners lie in the 3x3 cells around the cell of its AABB minimum.
+  d->cell_h = 2.0 * rmax * (1.0 + 1.0e-6);
+  cudaStream_t s = d->ctx->stream;
+  d->n = n;
+  hg_status st;
+  if ((st = h2d(s, d->q.p, q, 3 * n)) || (st = h2d(s, d->v.p, v, 3 * n)) ||
+      (st = h2d(s, d->r.p, r, n)) || (st = h2d(s, d->m0.p, mass, n)) ||
+      (st = h2d(s, d->I0.p, inertia, n)))
+    return st;
+  if (fixed) {
+    if ((st = h2d(s, d->fixed.p, fixed, n))) return st;
+  } else {
+    HG_CUDA_TRY(cudaMemsetAsync(d->fixed.p, 0, n, s));
+  }
+  if ((st = fill(s, d->w.p, n, 1.0))) return st;
+  if ((st = dem_reset_history(d))) return st;
+  d->ncontacts_host = 0;
+  HG_CUDA_TRY(cudaStreamSynchronize(s));
+  return HG_OK;
+}
+
+hg_status hg_dem_set_weights(hg_dem *d, const double *w) {
+  if (!d || (!w && d->n > 0)) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  for (int64_t i = 0; i < d->n; ++i)
+    if (!(w[i] >= 0.0 && w[i] <= 1.0)) return fail(HG_ERR_INVALID_ARGUMENT, "weights must lie in [0, 1]");
+  DeviceGuard g(d->ctx->device);
+  hg_status st = h2d(d->ctx->stream, d->w.p, w, d->n);
+  if (st) return st;
+  HG_CUDA_TRY(cudaStreamSynchronize(d->ctx->stream));
+  return HG_OK;
+}
+
+hg_status hg_dem_set_state(hg_dem *d, const double *q, const double *v) {
+  if (!d) return fail(HG_ERR_INVALID_ARGUMENT, "d is NULL");
+  DeviceGuard g(d->ctx->device);
+  hg_status st;
+  if (q && (st = h2d(d->ctx->stream, d->q.p, q, 3 * d->n))) return st;
+  if (v && (st = h2d(d->ctx->stream, d->v.p, v, 3 * d->n))) return st;
+  HG_CUDA_TRY(cudaStreamSynchronize(d->ctx->stream));
+  return HG_OK;
+}
+
+hg_status hg_dem_download(hg_dem *d, double *q, double *v) {
+  if (!d) return fail(HG_ERR_INVALID_ARGUMENT, "d is NULL");
+  DeviceGuard g(d->ctx->device);
+  hg_status st;
+  if ((st = d2h(d->ctx->stream, q, d->q.p, 3 * d->n)) ||
+      (st = d2h(d->ctx->stream, v, d->v.p, 3 * d->n)))
+    return st;
+  HG_CUDA_TRY(cudaStreamSynchronize(d->ctx->stream));
+  return HG_OK;
+}
+
+hg_status hg_dem_step(hg_dem *d, double dt, int32_t nsteps, int32_t weighted) {
+  if (!d) return fail(HG_ERR_INVALID_ARGUMENT, "d is NULL");
+  if (!(dt > 0.0) || !std::isfinite(dt)) return fail(HG_ERR_INVALID_ARGUMENT, "dt must be positive");
+  if (nsteps < 0) return fail(HG_ERR_INVALID_ARGUMENT, "negative step count");
+  DeviceGuard g(d->ctx->device);
+  for (int k = 0; k < nsteps; ++k) {
+    hg_status st = dem_step(d, dt, weighted);
+    if (st != HG_OK) return st;
+  }
+  return HG_OK;
+}
+
+hg_status hg_dem_num_contacts(hg_dem *d, int64_t *n) {
+  if (!d || !n) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  DeviceGuard g(d->ctx->device);
+  int32_t c = 0;
+  if (d->history_valid) {
+    HG_CUDA_TRY(cudaMemcpyAsync(&c, d->c_count.p + d->cc, sizeof(int32_t),
+                                cudaMemcpyDeviceToHost, d->ctx->stream));
+    HG_CUDA_TRY(cudaStreamSynchronize(d->ctx->stream));
+  }
+  *n = c;
+  return HG_OK;
+}
+
+hg_status hg_dem_download_contacts(hg_dem *d, int64_t cap, double *rec, int64_t *count) {
+  if (!d || !count || (cap > 0 && !rec)) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  DeviceGuard g(d->ctx->device);
+  return dem_download_contacts(d, cap, rec, count);
+}
+
+hg_status hg_dem_status(hg_dem *d, uint32_t *word) {
+  if (!d || !word) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  DeviceGuard g(d->ctx->device);
+  HG_CUDA_TRY(cudaMemcpyAsync(word, d->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                              d->ctx->stream));
+  HG_CUDA_TRY(cudaStreamSynchronize(d->ctx->stream));
+  return HG_OK;
+}
+
+hg_status hg_dem_candidate_pairs(hg_context *ctx, int64_t n, const double *mn,
+                                 const double *mx, int64_t cap, int32_t *pairs,
+                                 int64_t *count) {
+  if (!ctx || !count || n < 0 || (n > 0 && (!mn || !mx)) || (cap > 0 && !pairs))
+    return fail(HG_ERR_INVALID_ARGUMENT, "bad argument");
+  if (n > (int64_t)(1 << 30)) return fail(HG_ERR_INVALID_ARGUMENT, "too many boxes");
+  for (int64_t i = 0; i < 2 * n; ++i)
+    if (!std::isfinite(mn[i]) || !std::isfinite(mx[i]) || !(mn[i] < mx[i]))
+      return fail(HG_ERR_INVALID_ARGUMENT, "boxes must be finite with min < max");
+  DeviceGuard g(ctx->device);
+  return dem_candidate_pairs(ctx, n, mn, mx, cap, pairs, count);
+}
+
+// ---- hybrid ---------------------------------------------------------------------
+
+hg_status hg_hybrid_create(hg_context *ctx, hg_mpm *m, hg_dem *d, hg_hybrid **out) {
+  if (!ctx || !m || !d || !out) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  *out = nullptr;
+  if (m->ctx != ctx || d->ctx != ctx)
+    return fail(HG_ERR_INVALID_ARGUMENT, "objects belong to another context");
+  if (m->p.precision != HG_PRECISION_FP64)
+    return fail(HG_ERR_UNSUPPORTED, "the hybrid step needs an FP64 MPM object");
+  DeviceGuard g(ctx->device);
+  hg_hybrid *h = new (std::nothrow) hg_hybrid();
+  if (!h) return fail(HG_ERR_OUT_OF_MEMORY, "host allocation failed");
+  h->ctx = ctx;
+  h->m = m;
+  h->d = d;
+  context_retain(ctx);
+  hg_status st = hybrid_alloc(h);
+  if (st != HG_OK) {
+    hg_hybrid_destroy(h);
+    return st;
+  }
+  *out = h;
+  return HG_OK;
+}
+
+hg_status hg_hybrid_destroy(hg_hybrid *h) {
+  if (!h) return HG_OK;
+  hg_context *ctx = h->ctx;
+  {
+    DeviceGuard g(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    delete h;
+  }
+  context_release(ctx);
+  return HG_OK;
+}
+
+hg_status hg_hybrid_step(hg_hybrid *h, double dt, int32_t nsteps, int32_t flags) {
+  if (!h) return fail(HG_ERR_INVALID_ARGUMENT, "h is NULL");
+  if (!(dt > 0.0) || !std::isfinite(dt)) return fail(HG_ERR_INVALID_ARGUMENT, "dt must be positive");
+  if (nsteps < 0) return fail(HG_ERR_INVALID_ARGUMENT, "negative step count");
+  if (h->m->n > 0 && h->m->cap < 1) return fail(HG_ERR_INVALID_ARGUMENT, "empty MPM object");
+  if (h->m->n == 0)
+    return fail(HG_ERR_INVALID_ARGUMENT, "the coupling needs at least one material point");
+  DeviceGuard g(h->ctx->device);
+  for (int k = 0; k < nsteps; ++k) {
+    hg_status st = hybrid_step(h, dt, flags);
+    if (st != HG_OK) return st;
+  }
+  return HG_OK;
+}
+
+hg_status hg_hybrid_clear_homogenized(hg_hybrid *h) {
+  if (!h) return fail(HG_ERR_INVALID_ARGUMENT, "h is NULL");
+  DeviceGuard g(h->ctx->device);
+  return hybrid_clear_homogenized(h);
+}
+
+hg_status hg_hybrid_num_packed(hg_hybrid *h, int64_t *ng, int64_t *nn) {
+  if (!h) return fail(HG_ERR_INVALID_ARGUMENT, "h is NULL");
+  DeviceGuard g(h->ctx->device);
+  int32_t c[2] = {0, 0};
+  HG_CUDA_TRY(cudaMemcpyAsync(c, h->counts.p, sizeof(c), cudaMemcpyDeviceToHost, h->ctx->stream));
+  HG_CUDA_TRY(cudaStreamSynchronize(h->ctx->stream));
+  if (ng) *ng = c[0];
+  if (nn) *nn = c[1];
+  return HG_OK;
+}
+
+hg_status hg_hybrid_download(hg_hybrid *h, int32_t *pg, int32_t *pn, double *dm, double *dp,
+                             double *va, double *aa, double *hf, double *hs, double *hv) {
+  if (!h) return fail(HG_ERR_INVALID_ARGUMENT, "h is NULL");
+  DeviceGuard g(h->ctx->device);
+  cudaStream_t s = h->ctx->stream;
+  int32_t c[2] = {0, 0};
+  HG_CUDA_TRY(cudaMemcpyAsync(c, h->counts.p, sizeof(c), cudaMemcpyDeviceToHost, s));
+  HG_CUDA_TRY(cudaStreamSynchronize(s));
+  const int64_t nn = (int64_t)(h->m->p.nx + 1) * (h->m->p.ny + 1);
+  hg_status st;
+  if ((st = d2h(s, pg, h->packed_dem.p, c[0])) || (st = d2h(s, pn, h->packed_mpm.p, c[1])) ||
+      (st = d2h(s, dm, h->dem_mass.p, nn)) || (st = d2h(s, dp, h->dem_mom.p, 2 * nn)) ||
+      (st = d2h(s, va, h->v_after.p, 2 * nn)) || (st = d2h(s, aa, h->a_after.p, 2 * nn)) ||
+      (st = d2h(s, hf, h->m->g_homog.p, nn)) || (st = d2h(s, hs, h->hstress.p, 4 * nn)) ||
+      (st = d2h(s, hv, h->hvel.p, 2 * nn)))
+    return st;
+  HG_CUDA_TRY(cudaStreamSynchronize(s));
+  return HG_OK;
+}
+
+} // extern "C"

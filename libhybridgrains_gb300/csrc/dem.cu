@@ -1,0 +1,772 @@
+// Penalty-DEM disk step (PenaltyImpactFrictionMap::flow / flowWithWeights,
+// rigidbody2d/PenaltyImpactFrictionMap.cpp:1083-1149) in FP64.
+//
+// Compiled with --fmad=false: every record and force is evaluated with the
+// operation order of the reference's Eigen expressions, and body forces are
+// summed in the reference's order (gravity, plane contacts, circle-circle
+// contacts in (first, second) order, kinematic contacts) by a per-body gather
+// instead of atomics. The step is therefore deterministic and matches a serial
+// FP64 evaluation of the reference bit for bit.
+//
+// Kernels per step:
+//   kd_home / kd_fill        broadphase: hash-grid counting sort of the disks
+//                            by the cell of their AABB minimum. The cell width
+//                            is 2 r_max (1 + 1e-6), so the partners of a disk
+//                            lie in 3x3 cells; the result is the reference's
+//                            candidate set {i < j : AABBs overlap}
+//                            (SpatialGrid.cpp:14-19, 90-118), independent of
+//                            the reference's own cell width.
+//   kd_pairs<EMIT>           narrow phase (RigidBody2DSim.cpp:270-336 with
+//                            q0 == q1, CollisionDetectionUtilities.cpp:3-101)
+//                            and body-plane tests (RigidBody2DSim.cpp:777-842);
+//                            count, then emit sorted per-body contact lists.
+//   kd_contacts              collision-cache update with tangential-spring
+//                            carry (PenaltyImpactFrictionMap.cpp:296-599) and
+//                            the penalty force with Coulomb projection
+//                            (616-1081, secondRootOfQuadratic 601-614).
+//   kd_in_count / kd_in_fill incoming circle-circle contact lists per body.
+//   kd_integrate             force gather, fixed-body zeroing and symplectic
+//                            Euler (PenaltyImpactFrictionMap.cpp:1101-1114).
+#include "hg_internal.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+namespace hg {
+
+namespace {
+
+constexpr int MAXP = 32; // partner list capacity per body and step
+enum { K_PLANE = 0, K_CC = 1, K_KIN = 2 };
+constexpr int RW = HG_DEM_RECORD_WIDTH;
+
+struct D2 {
+  double x, y;
+};
+__device__ __forceinline__ D2 dadd(D2 a, D2 b) { return {a.x + b.x, a.y + b.y}; }
+__device__ __forceinline__ D2 dsub(D2 a, D2 b) { return {a.x - b.x, a.y - b.y}; }
+__device__ __forceinline__ D2 dscl(double s, D2 a) { return {s * a.x, s * a.y}; }
+__device__ __forceinline__ double ddot(D2 a, D2 b) { return a.x * b.x + a.y * b.y; }
+__device__ __forceinline__ double dsq(D2 a) { return a.x * a.x + a.y * a.y; }
+__device__ __forceinline__ double dnorm(D2 a) { return sqrt(dsq(a)); }
+__device__ __forceinline__ D2 dnormalized(D2 a) {
+  const double n2 = dsq(a);
+  if (n2 > 0.0) {
+    const double n = sqrt(n2);
+    return {a.x / n, a.y / n};
+  }
+  return a;
+}
+__device__ __forceinline__ double dcross(D2 a, D2 b) { return a.x * b.y - a.y * b.x; }
+
+__device__ __forceinline__ uint32_t cell_hash(int cx, int cy, uint32_t mask) {
+  return ((uint32_t)cx * 73856093u ^ (uint32_t)cy * 19349663u) & mask;
+}
+
+__device__ __forceinline__ int64_t ckey(int kind, int a, int b) {
+  return ((int64_t)kind << 60) | ((int64_t)a << 30) | (int64_t)b;
+}
+
+struct BroadArgs {
+  int64_t n;
+  double H; // cell width
+  uint32_t mask;
+  const double *mn; // 2 per box (min x, min y)
+  const double *mx;
+};
+
+__global__ void kd_home(BroadArgs B, int2 *home, int32_t *bucket_count) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= B.n) return;
+  const int cx = (int)floor(B.mn[2 * i] / B.H), cy = (int)floor(B.mn[2 * i + 1] / B.H);
+  home[i] = make_int2(cx, cy);
+  atomicAdd(&bucket_count[cell_hash(cx, cy, B.mask)], 1);
+}
+
+__global__ void kd_fill(BroadArgs B, const int2 *__restrict__ home,
+                        const int32_t *__restrict__ bucket_start, int32_t *cursor,
+                        int32_t *items) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= B.n) return;
+  const int2 c = home[i];
+  const uint32_t b = cell_hash(c.x, c.y, B.mask);
+  items[bucket_start[b] + atomicAdd(&cursor[b], 1)] = (int32_t)i;
+}
+
+// AABB::overlaps (SpatialGrid.cpp:14-19), inclusive on every side.
+__device__ __forceinline__ bool box_overlap(const BroadArgs &B, int64_t i, int64_t j) {
+  return (B.mx[2 * i] >= B.mn[2 * j] && B.mx[2 * i + 1] >= B.mn[2 * j + 1]) &&
+         (B.mx[2 * j] >= B.mn[2 * i] && B.mx[2 * j + 1] >= B.mn[2 * i + 1]);
+}
+
+__device__ __forceinline__ void sort_small(int *keys, int n) {
+  for (int i = 1; i < n; ++i) {
+    const int k = keys[i];
+    int j = i - 1;
+    while (j >= 0 && keys[j] > k) {
+      keys[j + 1] = keys[j];
+      --j;
+    }
+    keys[j + 1] = k;
+  }
+}
+
+struct PairArgs {
+  BroadArgs B;
+  const int2 *home;
+  const int32_t *bucket_start;
+  const int32_t *bucket_count;
+  const int32_t *items;
+  const double *q;
+  const double *r;
+  const uint8_t *fixed;
+  int nplanes;
+  double px[HG_MAX_PLANES][2], pn[HG_MAX_PLANES][2];
+  int32_t *cnt;       // 3N counts [kind][body]
+  const int32_t *off; // 3N+1 offsets (emit pass)
+  int64_t *keys;      // emit pass output
+  int64_t ccap;
+  const int32_t *overflow; // emit pass: set when the contacts do not fit
+  uint32_t *status;
+};
+
+// Contact enumeration for body a as the first index: circle-circle with
+// b > a non-fixed, kinematic with b fixed (any index; the reference swaps the
+// fixed body into the second slot), and static planes. Fixed bodies emit none.
+template <bool EMIT> __global__ void kd_pairs(PairArgs A) {
+  const int64_t n = A.B.n;
+  const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (a >= n) return;
+  int ncc = 0, nkin = 0, npl = 0;
+  int cc[MAXP], kin[MAXP];
+  bool overflow = false;
+  if (!A.fixed[a]) {
+    const double xa = A.q[3 * a], ya = A.q[3 * a + 1], ra = A.r[a];
+    const int cx0 = (int)floor(A.B.mn[2 * a] / A.B.H) - 1;
+    const int cy0 = (int)floor(A.B.mn[2 * a + 1] / A.B.H) - 1;
+    const int cx1 = (int)floor(A.B.mx[2 * a] / A.B.H);
+    const int cy1 = (int)floor(A.B.mx[2 * a + 1] / A.B.H);
+    for (int cy = cy0; cy <= cy1; ++cy)
+      for (int cx = cx0; cx <= cx1; ++cx) {
+        const uint32_t bk = cell_hash(cx, cy, A.B.mask);
+        const int s = A.bucket_start[bk], e = s + A.bucket_count[bk];
+        for (int k = s; k < e; ++k) {
+          const int b = A.items[k];
+          if (b == a) continue;
+          const int2 hb = A.home[b];
+          if (hb.x != cx || hb.y != cy) continue; // bucket shared by another cell
+          const bool bf = A.fixed[b] != 0;
+          if (!(b > a || bf)) continue;
+          if (!box_overlap(A.B, a, b)) continue;
+          // ballBallCCDCollisionHappens with q0 == q1: active iff c0 <= 0
+          const double dx = xa - A.q[3 * b], dy = ya - A.q[3 * b + 1];
+          const double rb = A.r[b];
+          const double c0 = (dx * dx + dy * dy) - (ra + rb) * (ra + rb);
+          if (!(c0 <= 0.0)) continue;
+          if (!bf) {
+            if (ncc < MAXP) cc[ncc++] = b;
+            else overflow = true;
+          } else {
+            if (nkin < MAXP) kin[nkin++] = b;
+            else overflow = true;
+          }
+        }
+      }
+    // StaticPlaneCircleConstraint::isActive (StaticPlaneCircleConstraint.cpp:12-17)
+    for (int k = 0; k < A.nplanes; ++k) {
+      const double d = A.pn[k][0] * (xa - A.px[k][0]) + A.pn[k][1] * (ya - A.px[k][1]);
+      if (d <= ra) ++npl;
+    }
+  }
+  if (overflow) atomicOr(A.status, (uint32_t)HG_STATUS_CELL_OVERFLOW);
+  if (!EMIT) {
+    A.cnt[a] = npl;
+    A.cnt[n + a] = ncc;
+    A.cnt[2 * n + a] = nkin;
+    return;
+  }
+  if (npl + ncc + nkin == 0 || *A.overflow) return;
+  sort_small(cc, ncc);
+  sort_small(kin, nkin);
+  const int64_t o0 = A.off[a], o1 = A.off[n + a], o2 = A.off[2 * n + a];
+  if (o0 + npl > A.ccap || o1 + ncc > A.ccap || o2 + nkin > A.ccap) {
+    atomicOr(A.status, (uint32_t)HG_STATUS_CONTACT_OVERFLOW);
+    return;
+  }
+  const double xa = A.q[3 * a], ya = A.q[3 * a + 1], ra = A.r[a];
+  int j = 0;
+  for (int k = 0; k < A.nplanes; ++k) {
+    const double d = A.pn[k][0] * (xa - A.px[k][0]) + A.pn[k][1] * (ya - A.px[k][1]);
+    if (d <= ra) A.keys[o0 + j++] = ckey(K_PLANE, (int)a, k);
+  }
+  for (int k = 0; k < ncc; ++k) A.keys[o1 + k] = ckey(K_CC, (int)a, cc[k]);
+  for (int k = 0; k < nkin; ++k) A.keys[o2 + k] = ckey(K_KIN, (int)a, kin[k]);
+}
+
+// Capacity guard between the counting and the emission pass: when the total
+// exceeds the contact capacity the step keeps no contacts (and reports
+// HG_STATUS_CONTACT_OVERFLOW) instead of writing past the buffers.
+__global__ void kd_check_capacity(int64_t n, const int32_t *__restrict__ off, int64_t ccap,
+                                  int32_t *overflow, uint32_t *status) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const bool over = (int64_t)off[3 * n] > ccap;
+    *overflow = over ? 1 : 0;
+    if (over) atomicOr(status, (uint32_t)HG_STATUS_CONTACT_OVERFLOW);
+  }
+}
+
+__global__ void kd_drop_if_overflow(int64_t n, const int32_t *__restrict__ overflow,
+                                    int32_t *cnt, int32_t *off) {
+  if (!*overflow) return;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i <= 3 * n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    cnt[i] = 0;
+    off[i] = 0;
+  }
+}
+
+struct ContactArgs {
+  int64_t n;
+  double dt;
+  int weighted;
+  double kn, kt, gn, gt, mu;
+  int nplanes;
+  double px[HG_MAX_PLANES][2], pn[HG_MAX_PLANES][2];
+  const double *q, *v, *r, *w;
+  const int32_t *count; // device count (total contacts)
+  const int64_t *keys;
+  double *rec;
+  const int64_t *old_keys;
+  const double *old_rec;
+  const int32_t *old_count; // device count of the previous step's contacts
+  int64_t ccap;
+};
+
+__device__ __forceinline__ int find_old(const ContactArgs &C, int64_t key) {
+  int lo = 0, hi = min((int64_t)*C.old_count, C.ccap) - 1;
+  while (lo <= hi) {
+    const int mid = (lo + hi) >> 1;
+    const int64_t k = C.old_keys[mid];
+    if (k == key) return mid;
+    if (k < key) lo = mid + 1;
+    else hi = mid - 1;
+  }
+  return -1;
+}
+
+// secondRootOfQuadratic (PenaltyImpactFrictionMap.cpp:601-614)
+__device__ __forceinline__ double second_root(double a, double b, double c, double ds) {
+  if (b > 0.0) return (2.0 * c) / (-b - ds);
+  return (-b + ds) / (2.0 * a);
+}
+
+__global__ void kd_contacts(ContactArgs C) {
+  const int64_t total = min((int64_t)*C.count, C.ccap);
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t key = C.keys[k];
+    const int kind = (int)(key >> 60);
+    const int a = (int)((key >> 30) & 0x3FFFFFFF);
+    const int b = (int)(key & 0x3FFFFFFF);
+    const D2 qa{C.q[3 * a], C.q[3 * a + 1]};
+    const D2 va{C.v[3 * a], C.v[3 * a + 1]};
+    const double wa = C.v[3 * a + 2];
+    double depth, weight;
+    D2 n, cp{0.0, 0.0}, r0, r1{0.0, 0.0}, vrel;
+    const double ra = C.r[a];
+    if (kind == K_PLANE) { // PenaltyImpactFrictionMap.cpp:316-359
+      const D2 xp{C.px[b][0], C.px[b][1]};
+      n = D2{C.pn[b][0], C.pn[b][1]};
+      cp = dsub(qa, dscl(ra, n));
+      weight = C.weighted ? C.w[a] : 1.0;
+      depth = fmin(0.0, ddot(n, dsub(qa, xp)) - ra);
+      r0 = dscl(-ra, n);
+      const D2 t0{-r0.y, r0.x};
+      const D2 arm = dsub(cp, xp);
+      const D2 tp{-arm.y, arm.x};
+      const D2 vp{0.0 + 0.0 * tp.x, 0.0 + 0.0 * tp.y};
+      vrel = dsub(dadd(va, dscl(wa, t0)), vp);
+    } else {
+      const D2 qb{C.q[3 * b], C.q[3 * b + 1]};
+      const double rb = C.r[b];
+      n = dnormalized(dsub(qa, qb));
+      depth = fmin(0.0, dnorm(dsub(qa, qb)) - ra - rb);
+      const D2 vb{C.v[3 * b], C.v[3 * b + 1]};
+      const double wb = C.v[3 * b + 2];
+      if (kind == K_CC) { // CircleCircleConstraint.cpp:171-233
+        cp = dadd(qa, dscl(ra / (ra + rb), dsub(qb, qa)));
+        weight = C.weighted ? (C.w[a] + C.w[b]) * 0.5 : 1.0;
+        r0 = dsub(cp, qa);
+        r1 = dsub(cp, qb);
+        const D2 t0{-r0.y, r0.x}, t1{-r1.y, r1.x};
+        vrel = dsub(dsub(dadd(va, dscl(wa, t0)), vb), dscl(wb, t1));
+      } else { // KinematicObjectCircleConstraint.cpp
+        cp = dsub(qa, dscl(ra, n));
+        weight = C.weighted ? C.w[a] : 1.0;
+        r0 = dscl(-ra, n);
+        const D2 t{-r0.y, r0.x};
+        const D2 arm = dsub(cp, qb);
+        const D2 tk{-arm.y, arm.x};
+        const D2 vk = dadd(vb, dscl(wb, tk));
+        vrel = dsub(dadd(va, dscl(wa, t)), vk);
+      }
+    }
+    // tangential spring carry
+    D2 ds;
+    const int o = find_old(C, key);
+    if (o >= 0) {
+      ds = D2{C.old_rec[(int64_t)o * RW + 6], C.old_rec[(int64_t)o * RW + 7]};
+      ds = dadd(ds, dscl(C.dt, vrel));
+    } else {
+      ds = dscl(C.dt, vrel);
+    }
+    ds = dsub(ds, dscl(ddot(n, ds), n));
+    // penalty force (PenaltyImpactFrictionMap.cpp:616-1081)
+    const double w = weight;
+    const D2 vt = dsub(vrel, dscl(ddot(n, vrel), n));
+    const D2 vn = dsub(vrel, vt);
+    const D2 fn = dsub(dscl(-C.kn * w * depth, n), dscl(0.5 * C.gn * w, vn));
+    D2 ft = dsub(dscl(-C.kt * w, ds), dscl(0.5 * C.gt * w, vt));
+    const double mu_fn = C.mu * dnorm(fn);
+    const double ftn = dnorm(ft);
+    if (0.5 * C.gt * w * dnorm(vt) > mu_fn) {
+      ds = D2{0.0, 0.0};
+      ft = dscl(-0.5 * C.gt * w, vt);
+      ft = dnormalized(ft);
+      ft = dscl(mu_fn, ft);
+    } else if (ftn > mu_fn) {
+      const double qa_ = C.kt * w * C.kt * w * dsq(ds);
+      const double qb_ = C.kt * w * C.gt * w * ddot(ds, vt);
+      const double qc_ = 0.25 * C.gt * w * C.gt * w * ddot(vt, vt) - C.mu * C.mu * dsq(fn);
+      const double dscr = qb_ * qb_ - 4 * qa_ * qc_;
+      const double root1 = second_root(qa_, qb_, qc_, sqrt(dscr));
+      const D2 nds = dscl(root1, ds);
+      ft = dsub(dscl(-C.kt * w, nds), dscl(0.5 * C.gt * w, vt));
+      ds = nds;
+    }
+    double *o_ = C.rec + k * RW;
+    o_[0] = kind;
+    o_[1] = a;
+    o_[2] = b;
+    o_[3] = depth;
+    o_[4] = n.x;
+    o_[5] = n.y;
+    o_[6] = ds.x;
+    o_[7] = ds.y;
+    o_[8] = vrel.x;
+    o_[9] = vrel.y;
+    o_[10] = r0.x;
+    o_[11] = r0.y;
+    o_[12] = r1.x;
+    o_[13] = r1.y;
+    o_[14] = weight;
+    o_[15] = cp.x;
+    o_[16] = cp.y;
+    o_[17] = fn.x;
+    o_[18] = fn.y;
+    o_[19] = ft.x;
+    o_[20] = ft.y;
+    o_[21] = 0.0;
+  }
+}
+
+__global__ void kd_in_count(int64_t n, const int32_t *__restrict__ off,
+                            const int64_t *__restrict__ keys, int32_t *in_count) {
+  // circle-circle contacts occupy [off[n], off[2n])
+  const int s = off[n], e = off[2 * n];
+  for (int64_t k = s + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < e;
+       k += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(&in_count[keys[k] & 0x3FFFFFFF], 1);
+}
+
+__global__ void kd_in_fill(int64_t n, const int32_t *__restrict__ off,
+                           const int64_t *__restrict__ keys,
+                           const int32_t *__restrict__ in_off, int32_t *in_cursor,
+                           int32_t *in_list) {
+  const int s = off[n], e = off[2 * n];
+  for (int64_t k = s + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < e;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int b = (int)(keys[k] & 0x3FFFFFFF);
+    in_list[in_off[b] + atomicAdd(&in_cursor[b], 1)] = (int32_t)k;
+  }
+}
+
+__global__ void kd_integrate(int64_t n, double dt, double gx, double gy, double *q, double *v,
+                             const double *__restrict__ m0, const double *__restrict__ I0,
+                             const double *__restrict__ w, const uint8_t *__restrict__ fixed,
+                             const int32_t *__restrict__ cnt, const int32_t *__restrict__ off,
+                             const double *__restrict__ rec, const int32_t *__restrict__ in_count,
+                             const int32_t *__restrict__ in_off, int32_t *in_list,
+                             double *F_out, uint32_t *status) {
+  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  // RigidBody2DState::updateCurrentMassUsingMassWeights
+  const double M = m0[j] * w[j], Mi = I0[j] * w[j];
+  double Fx = 0.0 + M * gx, Fy = 0.0 + M * gy, T = 0.0;
+  auto total = [&](int64_t k, D2 &f) {
+    const double *r = rec + k * RW;
+    f = dadd(D2{r[17], r[18]}, D2{r[19], r[20]});
+  };
+  // circle vs plane
+  for (int64_t k = off[j], e = off[j] + cnt[j]; k < e; ++k) {
+    D2 f;
+    total(k, f);
+    Fx += f.x;
+    Fy += f.y;
+    T += dcross(D2{rec[k * RW + 10], rec[k * RW + 11]}, f);
+  }
+  // circle vs circle: contributions as the second body come from first
+  // indices below j, i.e. before j's own list in the reference's loop.
+  {
+    int *lst = in_list + in_off[j];
+    const int c = in_count[j];
+    for (int i = 1; i < c; ++i) { // contact indices sorted = first indices sorted
+      const int key = lst[i];
+      int t = i - 1;
+      while (t >= 0 && lst[t] > key) {
+        lst[t + 1] = lst[t];
+        --t;
+      }
+      lst[t + 1] = key;
+    }
+    for (int i = 0; i < c; ++i) {
+      const int64_t k = lst[i];
+      D2 f;
+      total(k, f);
+      Fx -= f.x;
+      Fy -= f.y;
+      T -= dcross(D2{rec[k * RW + 12], rec[k * RW + 13]}, f);
+    }
+  }
+  for (int64_t k = off[n + j], e = off[n + j] + cnt[n + j]; k < e; ++k) {
+    D2 f;
+    total(k, f);
+    Fx += f.x;
+    Fy += f.y;
+    T += dcross(D2{rec[k * RW + 10], rec[k * RW + 11]}, f);
+  }
+  // kinematic circle vs circle
+  for (int64_t k = off[2 * n + j], e = off[2 * n + j] + cnt[2 * n + j]; k < e; ++k) {
+    D2 f;
+    total(k, f);
+    Fx += f.x;
+    Fy += f.y;
+    T += dcross(D2{rec[k * RW + 10], rec[k * RW + 11]}, f);
+  }
+  if (fixed[j]) Fx = Fy = T = 0.0;
+  if (F_out) {
+    F_out[3 * j] = Fx;
+    F_out[3 * j + 1] = Fy;
+    F_out[3 * j + 2] = T;
+  }
+  // v1 = v0 + dt Minv F ; q1 = q0 + dt v1
+  const double v0 = v[3 * j] + (dt * (1.0 / M)) * Fx;
+  const double v1 = v[3 * j + 1] + (dt * (1.0 / M)) * Fy;
+  const double v2 = v[3 * j + 2] + (dt * (1.0 / Mi)) * T;
+  v[3 * j] = v0;
+  v[3 * j + 1] = v1;
+  v[3 * j + 2] = v2;
+  const double q0 = q[3 * j] + dt * v0, q1 = q[3 * j + 1] + dt * v1, q2 = q[3 * j + 2] + dt * v2;
+  q[3 * j] = q0;
+  q[3 * j + 1] = q1;
+  q[3 * j + 2] = q2;
+  if (!isfinite(q0) || !isfinite(q1) || !isfinite(v0) || !isfinite(v1))
+    atomicOr(status, (uint32_t)HG_STATUS_NONFINITE);
+}
+
+__global__ void kd_aabbs(int64_t n, const double *__restrict__ q, const double *__restrict__ r,
+                         double *mn, double *mx) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  // CircleGeometry::computeCollisionAABB (CircleGeometry.cpp:22-30), q0 == q1
+  const double x = q[3 * i], y = q[3 * i + 1], ri = r[i];
+  mn[2 * i] = x - ri;
+  mn[2 * i + 1] = y - ri;
+  mx[2 * i] = x + ri;
+  mx[2 * i + 1] = y + ri;
+}
+
+// Candidate pairs of explicit boxes (SpatialGrid::getPotentialOverlaps).
+template <bool EMIT>
+__global__ void kd_box_pairs(BroadArgs B, const int2 *__restrict__ home,
+                             const int32_t *__restrict__ bstart,
+                             const int32_t *__restrict__ bcount,
+                             const int32_t *__restrict__ items, int32_t *cnt,
+                             const int32_t *__restrict__ off, int32_t *pairs, int64_t cap,
+                             uint32_t *status) {
+  const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (a >= B.n) return;
+  int list[MAXP];
+  int np = 0;
+  bool overflow = false;
+  const int cx0 = (int)floor(B.mn[2 * a] / B.H) - 1, cy0 = (int)floor(B.mn[2 * a + 1] / B.H) - 1;
+  const int cx1 = (int)floor(B.mx[2 * a] / B.H), cy1 = (int)floor(B.mx[2 * a + 1] / B.H);
+  for (int cy = cy0; cy <= cy1; ++cy)
+    for (int cx = cx0; cx <= cx1; ++cx) {
+      const uint32_t bk = cell_hash(cx, cy, B.mask);
+      for (int k = bstart[bk], e = bstart[bk] + bcount[bk]; k < e; ++k) {
+        const int b = items[k];
+        if (b <= a) continue;
+        const int2 hb = home[b];
+        if (hb.x != cx || hb.y != cy) continue;
+        if (!box_overlap(B, a, b)) continue;
+        if (np < MAXP) list[np++] = b;
+        else overflow = true;
+      }
+    }
+  if (overflow) atomicOr(status, (uint32_t)HG_STATUS_CELL_OVERFLOW);
+  if (!EMIT) {
+    cnt[a] = np;
+    return;
+  }
+  sort_small(list, np);
+  const int64_t o = off[a];
+  for (int k = 0; k < np; ++k)
+    if (o + k < cap) {
+      pairs[2 * (o + k)] = (int32_t)a;
+      pairs[2 * (o + k) + 1] = list[k];
+    }
+}
+
+inline int blocks_for(int64_t n, int t) { return (int)std::max<int64_t>(1, (n + t - 1) / t); }
+
+uint32_t table_bits(int64_t n) {
+  uint32_t bits = 4;
+  while (((int64_t)1 << bits) < 2 * n && bits < 30) ++bits;
+  return bits;
+}
+
+// Broadphase tables for n boxes: bucket counts/starts, items and home cells.
+hg_status build_buckets(cudaStream_t s, BroadArgs &B, int32_t *bcount, int32_t *bstart,
+                        int32_t *cursor, int32_t *items, int2 *home, int32_t *scan_tmp) {
+  const int64_t T = (int64_t)B.mask + 1;
+  HG_CUDA_TRY(cudaMemsetAsync(bcount, 0, sizeof(int32_t) * T, s));
+  HG_CUDA_TRY(cudaMemsetAsync(cursor, 0, sizeof(int32_t) * T, s));
+  if (B.n == 0) return HG_OK;
+  HG_LAUNCH(kd_home, blocks_for(B.n, 256), 256, 0, s, B, home, bcount);
+  HG_CHECK_LAUNCH();
+  hg_status st = exclusive_scan_i32(bcount, bstart, T, scan_tmp, s);
+  if (st != HG_OK) return st;
+  HG_LAUNCH(kd_fill, blocks_for(B.n, 256), 256, 0, s, B, home, bstart, cursor, items);
+  HG_CHECK_LAUNCH();
+  return HG_OK;
+}
+
+
+} // namespace
+
+hg_status dem_alloc(hg_dem *d) {
+  const int64_t N = std::max<int64_t>(d->cap, 1);
+  const int64_t C = std::max<int64_t>(d->ccap, 1);
+  const uint32_t bits = table_bits(N);
+  d->mask = (1u << bits) - 1u;
+  const int64_t T = (int64_t)d->mask + 1;
+  int64_t tmp = std::max(scan_tmp_size(3 * N + 1), scan_tmp_size(T));
+  tmp = std::max(tmp, scan_tmp_size(N + 1));
+  hg_status st;
+  if ((st = d->status.alloc(1)) || (st = d->q.alloc(3 * N)) || (st = d->v.alloc(3 * N)) ||
+      (st = d->r.alloc(N)) || (st = d->m0.alloc(N)) || (st = d->I0.alloc(N)) ||
+      (st = d->w.alloc(N)) || (st = d->F.alloc(3 * N)) || (st = d->fixed.alloc(N)) ||
+      (st = d->aabb_mn.alloc(2 * N)) || (st = d->aabb_mx.alloc(2 * N)) ||
+      (st = d->home.alloc(N)) || (st = d->bcount.alloc(T)) || (st = d->bstart.alloc(T)) ||
+      (st = d->bcursor.alloc(T)) || (st = d->items.alloc(N)) || (st = d->scan_tmp.alloc(tmp)) ||
+      (st = d->c_count.alloc(2)) || (st = d->per_body.alloc(3 * N + 1)) ||
+      (st = d->per_body_off.alloc(3 * N + 1)) || (st = d->ckey[0].alloc(C)) ||
+      (st = d->ckey[1].alloc(C)) || (st = d->crec[0].alloc(C * RW)) ||
+      (st = d->crec[1].alloc(C * RW)) || (st = d->in_count.alloc(N + 1)) ||
+      (st = d->in_off.alloc(N + 1)) || (st = d->in_list.alloc(C)) ||
+      (st = d->in_cursor.alloc(N)) || (st = d->overflow.alloc(1)))
+    return st;
+  cudaStream_t s = d->ctx->stream;
+  HG_CUDA_TRY(cudaMemsetAsync(d->status.p, 0, sizeof(uint32_t), s));
+  HG_CUDA_TRY(cudaMemsetAsync(d->c_count.p, 0, 2 * sizeof(int32_t), s));
+  HG_CUDA_TRY(cudaStreamSynchronize(s));
+  return HG_OK;
+}
+
+hg_status dem_reset_history(hg_dem *d) {
+  HG_CUDA_TRY(cudaMemsetAsync(d->c_count.p, 0, 2 * sizeof(int32_t), d->ctx->stream));
+  d->history_valid = false;
+  return HG_OK;
+}
+
+hg_status dem_step(hg_dem *d, double dt, int weighted) {
+  cudaStream_t s = d->ctx->stream;
+  const int64_t n = d->n;
+  if (n == 0) return HG_OK;
+  hg_status st;
+  HG_LAUNCH(kd_aabbs, blocks_for(n, 256), 256, 0, s, n, d->q.p, d->r.p, d->aabb_mn.p,
+            d->aabb_mx.p);
+  HG_CHECK_LAUNCH();
+  BroadArgs B;
+  B.n = n;
+  B.H = d->cell_h;
+  B.mask = d->mask;
+  B.mn = d->aabb_mn.p;
+  B.mx = d->aabb_mx.p;
+  if ((st = build_buckets(s, B, d->bcount.p, d->bstart.p, d->bcursor.p, d->items.p, d->home.p,
+                          d->scan_tmp.p)))
+    return st;
+  PairArgs A;
+  A.B = B;
+  A.home = d->home.p;
+  A.bucket_start = d->bstart.p;
+  A.bucket_count = d->bcount.p;
+  A.items = d->items.p;
+  A.q = d->q.p;
+  A.r = d->r.p;
+  A.fixed = d->fixed.p;
+  A.nplanes = d->p.nplanes;
+  for (int k = 0; k < HG_MAX_PLANES; ++k)
+    for (int c = 0; c < 2; ++c) {
+      A.px[k][c] = d->p.px[k][c];
+      A.pn[k][c] = d->p.pn[k][c];
+    }
+  A.cnt = d->per_body.p;
+  A.off = d->per_body_off.p;
+  const int nb = 1 - d->cc; // buffer receiving this step's contacts
+  A.keys = d->ckey[nb].p;
+  A.ccap = d->ccap;
+  A.overflow = d->overflow.p;
+  A.status = d->status.p;
+  HG_CUDA_TRY(cudaMemsetAsync(d->per_body.p, 0, sizeof(int32_t) * (3 * n + 1), s));
+  HG_LAUNCH(kd_pairs<false>, blocks_for(n, 128), 128, 0, s, A);
+  HG_CHECK_LAUNCH();
+  if ((st = exclusive_scan_i32(d->per_body.p, d->per_body_off.p, 3 * n + 1, d->scan_tmp.p, s)))
+    return st;
+  HG_LAUNCH(kd_check_capacity, 1, 32, 0, s, n, d->per_body_off.p, d->ccap, d->overflow.p,
+            d->status.p);
+  HG_CHECK_LAUNCH();
+  HG_LAUNCH(kd_drop_if_overflow, blocks_for(3 * n + 1, 256), 256, 0, s, n, d->overflow.p,
+            d->per_body.p, d->per_body_off.p);
+  HG_CHECK_LAUNCH();
+  HG_LAUNCH(kd_pairs<true>, blocks_for(n, 128), 128, 0, s, A);
+  HG_CHECK_LAUNCH();
+  HG_CUDA_TRY(cudaMemcpyAsync(d->c_count.p + nb, d->per_body_off.p + 3 * n, sizeof(int32_t),
+                              cudaMemcpyDeviceToDevice, s));
+  ContactArgs Cg;
+  Cg.n = n;
+  Cg.dt = dt;
+  Cg.weighted = weighted;
+  Cg.kn = d->p.kn;
+  Cg.kt = d->p.kt;
+  Cg.gn = d->p.gn;
+  Cg.gt = d->p.gt;
+  Cg.mu = d->p.mu;
+  Cg.nplanes = d->p.nplanes;
+  for (int k = 0; k < HG_MAX_PLANES; ++k)
+    for (int c = 0; c < 2; ++c) {
+      Cg.px[k][c] = d->p.px[k][c];
+      Cg.pn[k][c] = d->p.pn[k][c];
+    }
+  Cg.q = d->q.p;
+  Cg.v = d->v.p;
+  Cg.r = d->r.p;
+  Cg.w = d->w.p;
+  Cg.count = d->c_count.p + nb;
+  Cg.keys = d->ckey[nb].p;
+  Cg.rec = d->crec[nb].p;
+  Cg.old_keys = d->ckey[d->cc].p;
+  Cg.old_rec = d->crec[d->cc].p;
+  Cg.old_count = d->c_count.p + d->cc;
+  Cg.ccap = d->ccap;
+  HG_LAUNCH(kd_contacts, d->ctx->num_sms * 4, 256, 0, s, Cg);
+  HG_CHECK_LAUNCH();
+  HG_CUDA_TRY(cudaMemsetAsync(d->in_count.p, 0, sizeof(int32_t) * (n + 1), s));
+  HG_CUDA_TRY(cudaMemsetAsync(d->in_cursor.p, 0, sizeof(int32_t) * n, s));
+  HG_LAUNCH(kd_in_count, d->ctx->num_sms * 2, 256, 0, s, n, d->per_body_off.p, d->ckey[nb].p,
+            d->in_count.p);
+  HG_CHECK_LAUNCH();
+  if ((st = exclusive_scan_i32(d->in_count.p, d->in_off.p, n + 1, d->scan_tmp.p, s))) return st;
+  HG_LAUNCH(kd_in_fill, d->ctx->num_sms * 2, 256, 0, s, n, d->per_body_off.p, d->ckey[nb].p,
+            d->in_off.p, d->in_cursor.p, d->in_list.p);
+  HG_CHECK_LAUNCH();
+  HG_LAUNCH(kd_integrate, blocks_for(n, 128), 128, 0, s, n, dt, d->p.g[0], d->p.g[1], d->q.p,
+            d->v.p, d->m0.p, d->I0.p, d->w.p, d->fixed.p, d->per_body.p, d->per_body_off.p,
+            d->crec[nb].p, d->in_count.p, d->in_off.p, d->in_list.p, d->F.p, d->status.p);
+  HG_CHECK_LAUNCH();
+  d->cc = nb;
+  d->history_valid = true;
+  return HG_OK;
+}
+
+hg_status dem_download_contacts(hg_dem *d, int64_t cap, double *rec, int64_t *count) {
+  cudaStream_t s = d->ctx->stream;
+  int32_t c = 0;
+  if (d->history_valid) {
+    HG_CUDA_TRY(cudaMemcpyAsync(&c, d->c_count.p + d->cc, sizeof(int32_t),
+                                cudaMemcpyDeviceToHost, s));
+    HG_CUDA_TRY(cudaStreamSynchronize(s));
+  }
+  const int64_t total = std::min<int64_t>(c, d->ccap);
+  *count = total;
+  const int64_t k = std::min<int64_t>(total, cap);
+  if (k > 0) {
+    HG_CUDA_TRY(cudaMemcpyAsync(rec, d->crec[d->cc].p, sizeof(double) * RW * k,
+                                cudaMemcpyDeviceToHost, s));
+    HG_CUDA_TRY(cudaStreamSynchronize(s));
+  }
+  return HG_OK;
+}
+
+hg_status dem_candidate_pairs(hg_context *ctx, int64_t n, const double *mn, const double *mx,
+                              int64_t cap, int32_t *pairs, int64_t *count) {
+  cudaStream_t s = ctx->stream;
+  *count = 0;
+  if (n == 0) return HG_OK;
+  double H = 0.0, amax = 0.0;
+  for (int64_t i = 0; i < 2 * n; ++i) {
+    H = std::max(H, mx[i] - mn[i]);
+    amax = std::max(amax, std::max(std::fabs(mn[i]), std::fabs(mx[i])));
+  }
+  H = H * (1.0 + 1.0e-6);
+  if (amax / H > 1.0e9) return fail(HG_ERR_INVALID_ARGUMENT, "boxes too small for their coordinates");
+  const uint32_t bits = table_bits(n);
+  const int64_t T = (int64_t)1 << bits;
+  DevBuf<double> dmn, dmx;
+  DevBuf<int2> home;
+  DevBuf<int32_t> bcount, bstart, bcursor, items, cnt, off, tmp, dpairs;
+  DevBuf<uint32_t> status;
+  hg_status st;
+  if ((st = dmn.alloc(2 * n)) || (st = dmx.alloc(2 * n)) || (st = home.alloc(n)) ||
+      (st = bcount.alloc(T)) || (st = bstart.alloc(T)) || (st = bcursor.alloc(T)) ||
+      (st = items.alloc(n)) || (st = cnt.alloc(n + 1)) || (st = off.alloc(n + 1)) ||
+      (st = tmp.alloc(std::max(scan_tmp_size(T), scan_tmp_size(n + 1)))) ||
+      (st = status.alloc(1)))
+    return st;
+  HG_CUDA_TRY(cudaMemcpyAsync(dmn.p, mn, sizeof(double) * 2 * n, cudaMemcpyHostToDevice, s));
+  HG_CUDA_TRY(cudaMemcpyAsync(dmx.p, mx, sizeof(double) * 2 * n, cudaMemcpyHostToDevice, s));
+  HG_CUDA_TRY(cudaMemsetAsync(status.p, 0, sizeof(uint32_t), s));
+  HG_CUDA_TRY(cudaMemsetAsync(cnt.p, 0, sizeof(int32_t) * (n + 1), s));
+  BroadArgs B;
+  B.n = n;
+  B.H = H;
+  B.mask = (uint32_t)(T - 1);
+  B.mn = dmn.p;
+  B.mx = dmx.p;
+  if ((st = build_buckets(s, B, bcount.p, bstart.p, bcursor.p, items.p, home.p, tmp.p))) return st;
+  HG_LAUNCH(kd_box_pairs<false>, blocks_for(n, 128), 128, 0, s, B, home.p, bstart.p, bcount.p,
+            items.p, cnt.p, off.p, nullptr, 0, status.p);
+  HG_CHECK_LAUNCH();
+  if ((st = exclusive_scan_i32(cnt.p, off.p, n + 1, tmp.p, s))) return st;
+  int32_t total = 0;
+  uint32_t word = 0;
+  HG_CUDA_TRY(cudaMemcpyAsync(&total, off.p + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  HG_CUDA_TRY(cudaMemcpyAsync(&word, status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  HG_CUDA_TRY(cudaStreamSynchronize(s));
+  if (word & HG_STATUS_CELL_OVERFLOW)
+    return fail(HG_ERR_CAPACITY, "more than 32 overlapping boxes for one box");
+  if ((st = dpairs.alloc(2 * (int64_t)std::max<int32_t>(total, 1)))) return st;
+  HG_LAUNCH(kd_box_pairs<true>, blocks_for(n, 128), 128, 0, s, B, home.p, bstart.p, bcount.p,
+            items.p, cnt.p, off.p, dpairs.p, (int64_t)total, status.p);
+  HG_CHECK_LAUNCH();
+  const int64_t k = std::min<int64_t>(total, cap);
+  if (k > 0)
+    HG_CUDA_TRY(cudaMemcpyAsync(pairs, dpairs.p, sizeof(int32_t) * 2 * k, cudaMemcpyDeviceToHost, s));
+  HG_CUDA_TRY(cudaStreamSynchronize(s));
+  *count = total;
+  return HG_OK;
+}
+
+} // namespace hg

@@ -1,0 +1,263 @@
+// Internal declarations shared by the CUDA translation units of libhg_gpu.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <string>
+#include <vector>
+
+#include "hg_gpu.h"
+
+namespace hg {
+
+// ---- error handling --------------------------------------------------------
+
+void set_error(const std::string &msg);
+hg_status fail(hg_status s, const std::string &msg);
+hg_status cuda_fail(cudaError_t e, const char *what);
+
+#define HG_CUDA_TRY(call)                                                     \
+  do {                                                                        \
+    cudaError_t e_ = (call);                                                  \
+    if (e_ != cudaSuccess) return ::hg::cuda_fail(e_, #call);                 \
+  } while (0)
+
+// Launch bookkeeping: every kernel launch goes through HG_LAUNCH so that the
+// number of library kernels launched is observable (hg_kernel_launch_count).
+extern std::atomic<int64_t> g_launches;
+
+#define HG_LAUNCH(kernel, grid, block, smem, stream, ...)                     \
+  do {                                                                        \
+    kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);               \
+    ::hg::g_launches.fetch_add(1, std::memory_order_relaxed);                 \
+  } while (0)
+
+#define HG_CHECK_LAUNCH()                                                     \
+  do {                                                                        \
+    cudaError_t e_ = cudaGetLastError();                                      \
+    if (e_ != cudaSuccess) return ::hg::cuda_fail(e_, "kernel launch");       \
+  } while (0)
+
+// ---- device buffers --------------------------------------------------------
+
+template <typename T> struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  hg_status alloc(size_t count) {
+    free();
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return cuda_fail(e, "cudaMalloc");
+    }
+    n = count;
+    return HG_OK;
+  }
+  void free() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  ~DevBuf() { free(); }
+};
+
+} // namespace hg
+
+// Reference-counted: every MPM/DEM/hybrid object holds a reference, so
+// destroying the context before its objects only drops the caller's reference.
+struct hg_context {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  int refs = 1;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+};
+
+namespace hg {
+void context_retain(hg_context *c);
+void context_release(hg_context *c);
+} // namespace hg
+
+namespace hg {
+
+// ---- MPM -------------------------------------------------------------------
+
+struct MpmPlaneDev {
+  double x[2], n[2];
+  double lower_bound;
+  int sticking;
+  // The same plane in grid units: u = (x - grid_min) / h.
+  double ux[2];
+  double ulb;
+  float fux[2], fulb;
+};
+
+struct MpmParams {
+  double gmin[2], gmax[2], h, inv_h;
+  int nx, ny; // cell counts; nodes are (nx+1) x (ny+1)
+  int basis;
+  int precision;
+  double mu, kappa, dp_alpha, flip_alpha;
+  double g[2];
+  int nplanes;
+  MpmPlaneDev planes[HG_MAX_PLANES];
+};
+
+// Bin (tile) geometry of the MIXED path: a tile is BIN x BIN cells; particles
+// are kept sorted by (tile, cell within tile). Tiles also partition the nodes
+// for the grid update: node (i, j) belongs to tile (i / BIN, j / BIN).
+constexpr int BIN = 16;
+constexpr int BIN_CELLS = BIN * BIN;
+// Particles may drift this many cells out of their tile before their next
+// re-sort and still use the tile's shared-memory windows.
+constexpr int DRIFT = 2;
+constexpr int VA_W = BIN + 2 * DRIFT + 1;  // G2P node window width
+constexpr int ACC_W = BIN + 2 * DRIFT + 3; // P2G node window width
+
+struct MixedParticles {
+  double2 *u;     // position in grid units, (x - grid_min) / h
+  float2 *v;      // velocity
+  float2 *mv;     // mass, volume
+  float4 *strain; // (J - 1, be_bar - I: xx, xy, yy)
+  uint8_t *flags; // bit0 just_homogenized, bit1 kinematically scripted
+  int32_t *id;    // upload index
+};
+
+} // namespace hg
+
+struct hg_mpm {
+  hg_context *ctx = nullptr;
+  hg::MpmParams p{};
+  int64_t cap = 0, n = 0;
+  hg::DevBuf<uint32_t> status;
+  // ---- FP64 state (reference layouts: q, v interleaved; be 4 per point) ----
+  hg::DevBuf<double> q, v, m, vol, hl, be, J, sigma;
+  hg::DevBuf<int32_t> jh;
+  hg::DevBuf<uint8_t> kin;
+  hg::DevBuf<double> g_mass, g_mom, g_mom_new, g_force, g_vel, g_acc, g_cforce,
+      g_homog;
+  hg::DevBuf<int32_t> g_hyb;
+  // ---- MIXED state ----
+  hg::DevBuf<double2> mu_[2];
+  hg::DevBuf<float2> mv_[2], mmv_[2];
+  hg::DevBuf<float4> mstrain_[2];
+  hg::DevBuf<uint8_t> mflags_[2];
+  hg::DevBuf<int32_t> mid_[2];
+  int cur = 0; // which buffer of the pairs above is live
+  hg::DevBuf<float4> acc4; // (px, py, fx, fy) accumulated for the next update
+  hg::DevBuf<float> accm;  // mass accumulated for the next update
+  hg::DevBuf<float4> va;   // (vx, vy, ax, ay) of the last update
+  hg::DevBuf<float> gm;    // mass of the last update
+  int ntx = 0, nty = 0;    // tiles in x, y
+  hg::DevBuf<int32_t> keys, counts, offsets, cursor, scan_tmp;
+  hg::DevBuf<int32_t> active_bins, active_tiles, nactive; // nactive[2]
+  hg::DevBuf<uint32_t> outside; // particles outside their window last step
+  uint32_t *h_outside = nullptr; // pinned mirror
+  cudaEvent_t outside_ev = nullptr;
+  bool outside_pending = false;
+  int64_t steps_since_rebin = 0;
+  int64_t rebins = 0;
+  bool primed = false;
+  // per-kernel event timing (hg_mpm_profile)
+  bool profile = false;
+  std::vector<cudaEvent_t> prof_events; // 3 per recorded step
+  size_t prof_used = 0;
+  // host-side staging for upload/download conversion
+  hg::DevBuf<double> stage_d;
+  hg::DevBuf<int32_t> stage_i;
+  hg::DevBuf<uint8_t> stage_u8;
+};
+
+namespace hg {
+
+hg_status mpm64_phase0(hg_mpm *m);
+hg_status mpm64_phase1(hg_mpm *m, double dt);
+hg_status mpm64_phase2(hg_mpm *m, double dt);
+
+hg_status mixed_alloc(hg_mpm *m);
+hg_status mixed_upload(hg_mpm *m, const double *q, const double *v,
+                       const double *mass, const double *vol,
+                       const double *be, const double *J, const int32_t *jh,
+                       const uint8_t *kin);
+hg_status mixed_download(hg_mpm *m, double *q, double *v, double *be,
+                         double *J, int32_t *jh);
+hg_status mixed_step(hg_mpm *m, double dt, int nsteps);
+hg_status mixed_download_grid(hg_mpm *m, double *mass, double *vel,
+                              double *acc);
+hg_status mixed_profile_read(hg_mpm *m, double *g2p2g_ms, double *update_ms,
+                             int64_t *steps);
+
+// ---- DEM ---------------------------------------------------------------------
+
+struct DemParams {
+  double g[2];
+  double kn, kt, gn, gt, mu;
+  double cell_scale;
+  int nplanes;
+  double px[HG_MAX_PLANES][2], pn[HG_MAX_PLANES][2];
+};
+
+} // namespace hg
+
+struct hg_dem {
+  hg_context *ctx = nullptr;
+  hg::DemParams p{};
+  int64_t cap = 0, ccap = 0, n = 0;
+  hg::DevBuf<uint32_t> status;
+  // bodies
+  hg::DevBuf<double> q, v, r, m0, I0, w, minv, mass, F;
+  hg::DevBuf<uint8_t> fixed;
+  // broadphase: hash grid of cell width H over the AABB minima
+  double cell_h = 0.0;
+  uint32_t mask = 0; // hash table size - 1
+  hg::DevBuf<double> aabb_mn, aabb_mx;
+  hg::DevBuf<int2> home;
+  hg::DevBuf<int32_t> bcount, bstart, bcursor, items;
+  hg::DevBuf<int32_t> scan_tmp;
+  // contacts: current and previous, sorted by (kind, first, second)
+  hg::DevBuf<int32_t> c_count; // contacts in ckey[0], ckey[1] (device)
+  hg::DevBuf<int32_t> overflow; // set when this step's contacts exceed ccap
+  hg::DevBuf<int32_t> per_body, per_body_off; // emission counts / offsets
+  hg::DevBuf<int64_t> ckey[2];                 // kind << 60 | first << 30 | second
+  hg::DevBuf<double> crec[2];                  // HG_DEM_RECORD_WIDTH per contact
+  int cc = 0;                                  // live contact buffer
+  int64_t ncontacts_host = 0;                  // count after the last step
+  bool history_valid = false;
+  // body gather lists for deterministic force accumulation
+  hg::DevBuf<int32_t> in_count, in_off, in_list, in_cursor;
+  hg::DevBuf<int32_t> out_off; // first contact index of each body
+};
+
+namespace hg {
+hg_status dem_alloc(hg_dem *d);
+hg_status dem_reset_history(hg_dem *d);
+hg_status dem_step(hg_dem *d, double dt, int weighted);
+hg_status dem_download_contacts(hg_dem *d, int64_t cap, double *rec,
+                                int64_t *count);
+hg_status dem_candidate_pairs(hg_context *ctx, int64_t n, const double *mn,
+                              const double *mx, int64_t cap, int32_t *pairs,
+                              int64_t *count);
+hg_status exclusive_scan_i32(const int32_t *in, int32_t *out, int64_t n,
+                             int32_t *tmp, cudaStream_t s);
+int64_t scan_tmp_size(int64_t n);
+} // namespace hg
+
+struct hg_hybrid {
+  hg_context *ctx = nullptr;
+  hg_mpm *m = nullptr;
+  hg_dem *d = nullptr;
+  hg::DevBuf<double> dem_mass, dem_mom, v_after, a_after, pos_before,
+      hstress, hvel, hmom, hmass;
+  hg::DevBuf<int32_t> coupled, packed_dem, packed_mpm, flag_tmp, scan_tmp,
+      node_flag, node_pos, counts; // counts[2]: packed sizes
+  int64_t n_packed_dem = 0, n_packed_mpm = 0;
+};
+
+namespace hg {
+hg_status hybrid_alloc(hg_hybrid *h);
+hg_status hybrid_step(hg_hybrid *h, double dt, int flags);
+hg_status hybrid_clear_homogenized(hg_hybrid *h);
+} // namespace hg

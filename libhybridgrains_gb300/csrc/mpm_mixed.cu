@@ -1,0 +1,845 @@
+// Mixed-precision MPM step (FP64 positions, FP32 everything else).
+//
+// One reference step (ExplicitIntegrator::flow, ExplicitIntegrator.cpp:63-67)
+// is executed as two kernels:
+//
+//   kx_grid_update  node part of computeForces (gravity, coupling force),
+//                   updateMomentum, PhysicsGrid::resolvePlaneCollisions and
+//                   lumpedMassVelocityAndAccelerationUpdate
+//                   (PhysicsGrid.cpp:459-673) over the active tiles only; it
+//                   consumes the accumulated (m, p, f) and zeroes it.
+//   kx_g2p2g        G2P of this step fused with P2G of the next one: per
+//                   material point computeVelGrad, elasticPrediction,
+//                   plasticCorrection, updateVelocities, updatePositions,
+//                   resolvePlaneCollisions (MaterialPoints.cpp:204-423), then
+//                   computeHyperelasticCauchyStress (183-202) at the new
+//                   state and the rasterisation of mass, momentum and
+//                   internal force (PhysicsGrid.cpp:168-471) for the next
+//                   step. Each particle is read once and written once per
+//                   step.
+//
+// Layout in HBM. Particles are SoA, sorted by (tile, cell within tile) with
+// 16x16-cell tiles: u = (x - grid_min)/h as double2, v float2, (m, V) float2,
+// strain float4 = (J - 1, be_bar - I [xx, xy, yy]) and a flag byte. Storing
+// J and be_bar as offsets from 1 and I keeps FP32's 24 bits on the strain
+// itself rather than on the leading 1. Grid fields are dense node-major
+// float4/float arrays; only tiles near particles are touched.
+//
+// P2G without float atomics on shared memory: for each pass of up to PASS
+// particles a CTA counting-sorts the particles of its tile by their new cell
+// (integer shared atomics), then one thread per node of the tile's window
+// gathers the contributions of the four adjacent cells. Window sums go to
+// global memory with one float4 + one float atomic per touched node.
+//
+// Re-sorting (counting sort by cell key) runs when a particle has drifted
+// out of its tile's window. Particles outside their window are still handled
+// exactly (G2P from global velocity, P2G with global atomics), so the re-sort
+// cadence affects speed only.
+#include "hg_internal.cuh"
+
+#include <cmath>
+
+namespace hg {
+
+namespace {
+
+constexpr int THREADS = 256;
+constexpr int PASS = 1024; // particles staged per pass
+constexpr int NC = ACC_W - 1; // cells per side of the P2G window
+constexpr int NCELL = NC * NC;
+
+struct MixedArgs {
+  int nx, ny, ntx, nty;
+  int64_t n;
+  float dt, inv_h, kappa, mu, dp_alpha, flip_alpha, gx, gy;
+  // Half-width (in cells) of the band around a plane in which the FP32
+  // plane test is redone exactly in FP64.
+  float pmargin;
+  int nplanes;
+  MpmPlaneDev planes[HG_MAX_PLANES];
+  const int32_t *offsets;
+  const int32_t *active;  // active bins or tiles
+  const int32_t *nactive; // device count
+  double2 *u;
+  float2 *v;
+  const float2 *mv;
+  float4 *strain;
+  uint8_t *flags;
+  const float4 *va;
+  float4 *acc4;
+  float *accm;
+  float *gm;
+  uint32_t *status;
+  uint32_t *outside;
+};
+
+// Exact floor(u) and the fraction u - floor(u) truncated to 24 bits, using
+// integer operations on the FP64 bit pattern (the FP64 pipe is ~1/64 of the
+// FP32 rate on this part). Valid for 0 <= u < 2^23; other values take the
+// FP64 path.
+__device__ __forceinline__ void split_u(double u, int &c, float &f) {
+  const long long b = __double_as_longlong(u);
+  const int e = (int)((b >> 52) & 0x7FF) - 1023;
+  if (e >= 0 && e < 23) {
+    const long long mant = (b & 0xFFFFFFFFFFFFFLL) | 0x10000000000000LL;
+    const int sh = 52 - e;
+    c = (int)(mant >> sh);
+    const long long fr = mant & ((1LL << sh) - 1);
+    f = (float)(int)(fr >> (sh - 24)) * (1.0f / 16777216.0f);
+  } else if (b >= 0 && e < 0) { // 0 <= u < 1
+    c = 0;
+    f = __double2float_rz(u);
+  } else {
+    const double fl = floor(u);
+    c = (int)fl;
+    f = __double2float_rz(u - fl);
+  }
+}
+
+__device__ __forceinline__ bool in_grid_cell(const MixedArgs &A, int cx, int cy) {
+  return cx >= 0 && cy >= 0 && cx < A.nx && cy < A.ny;
+}
+
+// Elastic prediction + Drucker-Prager plastic correction on offset-form
+// strain (ConstitutiveModel.cpp:19-81, MaterialPoints.cpp:324-369).
+// B = be - I; det(I + B) = 1 + t with t = tr B + det B.
+__device__ __forceinline__ void constitutive_update(float4 &s, int &jh, float Lxx,
+                                                    float Lxy, float Lyx, float Lyy,
+                                                    float dt, float kappa, float mu,
+                                                    float alpha) {
+  const float J = 1.0f + s.x;
+  float bxx = s.x + J * s.y, bxy = J * s.z, byy = s.x + J * s.w;
+  // be* = be + dt (L be + be L^T) with be = I + B
+  const float LBxx = Lxx * bxx + Lxy * bxy, LBxy = Lxx * bxy + Lxy * byy;
+  const float LByx = Lyx * bxx + Lyy * bxy, LByy = Lyx * bxy + Lyy * byy;
+  bxx += dt * (2.0f * Lxx + 2.0f * LBxx);
+  bxy += dt * ((Lxy + Lyx) + (LBxy + LByx));
+  byy += dt * (2.0f * Lyy + 2.0f * LByy);
+  float t = (bxx + byy) + (bxx * byy - bxy * bxy);
+  float dJ = t / (1.0f + sqrtf(1.0f + t));
+  if (jh != 0) {
+    if (dJ > 0.0f) { // J > 1: be = J I (ConstitutiveModel.cpp:28-35)
+      s = make_float4(dJ, 0.0f, 0.0f, 0.0f);
+      return;
+    }
+    jh = 0;
+  }
+  const float Js = 1.0f + dJ;
+  const float ys = fmaxf(0.0f, -0.5f * alpha * kappa * (2.0f + dJ) * dJ);
+  const float htr = 0.5f * (bxx + byy);
+  const float dxx = bxx - htr, dyy = byy - htr, dxy = bxy;
+  const float dn = sqrtf(dxx * dxx + 2.0f * dxy * dxy + dyy * dyy);
+  if (mu * dn > ys * Js) {
+    const float l2 = ys * Js / (mu * dn);
+    const float detdev = dxx * dyy - dxy * dxy;
+    const float l1sq_m1 = t - l2 * l2 * detdev;
+    const float l1m1 = l1sq_m1 / (1.0f + sqrtf(1.0f + l1sq_m1));
+    bxx = l1m1 + l2 * dxx;
+    byy = l1m1 + l2 * dyy;
+    bxy = l2 * dxy;
+    t = (bxx + byy) + (bxx * byy - bxy * bxy);
+    dJ = t / (1.0f + sqrtf(1.0f + t));
+  }
+  const float inv = 1.0f / (1.0f + dJ);
+  s = make_float4(dJ, (bxx - dJ) * inv, bxy * inv, (byy - dJ) * inv);
+}
+
+// Kirchhoff stress tau (ConstitutiveModel.cpp:83-97 via
+// MaterialPoints.cpp:183-202) scaled to the node force factor -V tau / h.
+__device__ __forceinline__ void stress_factor(const float4 s, int jh, float V,
+                                              float inv_h, float kappa, float mu,
+                                              float &s00, float &s01, float &s11) {
+  if (s.x > 0.0f || jh != 0) {
+    s00 = s01 = s11 = 0.0f;
+    return;
+  }
+  const float vol = kappa * 0.5f * (2.0f + s.x) * s.x;
+  const float dev = 0.5f * (s.y - s.w);
+  const float c = -V * inv_h;
+  s00 = c * (vol + mu * dev);
+  s11 = c * (vol - mu * dev);
+  s01 = c * (mu * s.z);
+}
+
+struct PRec {
+  float4 a; // fx, fy, m, m vx
+  float4 b; // m vy, s00, s01, s11
+};
+
+__device__ __forceinline__ void scatter_global(const MixedArgs &A, int cx, int cy,
+                                               const PRec &r) {
+  const int row = A.nx + 1;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int dx = k & 1, dy = k >> 1;
+    const int ix = cx + dx, iy = cy + dy;
+    const float wx = dx ? r.a.x : 1.0f - r.a.x;
+    const float wy = dy ? r.a.y : 1.0f - r.a.y;
+    const float w = wx * wy;
+    const float gx = dx ? wy : -wy, gy = dy ? wx : -wx;
+    float4 add = make_float4(w * r.a.w, w * r.b.x, 0.0f, 0.0f);
+    if (w != 0.0f) {
+      add.z = r.b.y * gx + r.b.z * gy;
+      add.w = r.b.z * gx + r.b.w * gy;
+    }
+    const int64_t node = (int64_t)iy * row + ix;
+    atomicAdd(&A.accm[node], w * r.a.z);
+    atomicAdd(&A.acc4[node], add);
+  }
+}
+
+template <bool PRIME>
+__global__ void __launch_bounds__(THREADS, 3) kx_g2p2g(MixedArgs A) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  float4 *s_va = reinterpret_cast<float4 *>(smem);              // VA_W^2
+  float4 *s_acc = s_va + VA_W * VA_W;                             // ACC_W^2
+  PRec *s_rec = reinterpret_cast<PRec *>(s_acc + ACC_W * ACC_W);  // PASS
+  float *s_accm = reinterpret_cast<float *>(s_rec + PASS);        // ACC_W^2
+  int *s_slot = reinterpret_cast<int *>(s_accm + ACC_W * ACC_W);  // PASS
+  int *s_sorted = s_slot + PASS;                                  // PASS
+  int *s_cnt = s_sorted + PASS;                                   // NCELL
+  int *s_start = s_cnt + NCELL;                                   // NCELL
+  __shared__ int s_warp[THREADS / 32];
+  __shared__ unsigned s_out;
+
+  const int tid = threadIdx.x;
+  const int nact = *A.nactive;
+  const int row = A.nx + 1;
+  for (int t = blockIdx.x; t < nact; t += gridDim.x) {
+    const int bin = A.active[t];
+    const int X0 = (bin % A.ntx) * BIN, Y0 = (bin / A.ntx) * BIN;
+    const int start = A.offsets[bin * BIN_CELLS];
+    const int end = A.offsets[(bin + 1) * BIN_CELLS];
+    const int WX = X0 - DRIFT - 1, WY = Y0 - DRIFT - 1; // P2G window origin (node)
+    if (!PRIME) {
+      for (int k = tid; k < VA_W * VA_W; k += THREADS) {
+        const int ix = X0 - DRIFT + k % VA_W, iy = Y0 - DRIFT + k / VA_W;
+        float4 val = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (ix >= 0 && iy >= 0 && ix <= A.nx && iy <= A.ny)
+          val = A.va[(int64_t)iy * row + ix];
+        s_va[k] = val;
+      }
+    }
+    for (int k = tid; k < ACC_W * ACC_W; k += THREADS) {
+      s_acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+      s_accm[k] = 0.f;
+    }
+    if (tid == 0) s_out = 0;
+    for (int base = start; base < end; base += PASS) {
+      for (int k = tid; k < NCELL; k += THREADS) s_cnt[k] = 0;
+      __syncthreads();
+      // ---- per-particle update (G2P of this step) ----
+      for (int sl = tid; sl < PASS; sl += THREADS) {
+        const int64_t p = (int64_t)base + sl;
+        int packed = -1;
+        if (p < end) {
+          const double2 u = A.u[p];
+          int cx, cy;
+          float fx, fy;
+          split_u(u.x, cx, fx);
+          split_u(u.y, cy, fy);
+          if (!in_grid_cell(A, cx, cy)) {
+            atomicOr(A.status, (uint32_t)HG_STATUS_OUT_OF_GRID);
+          } else {
+            const float2 mv = A.mv[p];
+            float2 vel = A.v[p];
+            float4 st = A.strain[p];
+            int fl = A.flags[p];
+            int jh = fl & 1;
+            int ncx = cx, ncy = cy;
+            float nfx = fx, nfy = fy;
+            if (!PRIME) {
+              float4 n00, n10, n01, n11;
+              const int gx = cx - (X0 - DRIFT), gy = cy - (Y0 - DRIFT);
+              if (gx >= 0 && gy >= 0 && gx <= VA_W - 2 && gy <= VA_W - 2) {
+                const int k0 = gy * VA_W + gx;
+                n00 = s_va[k0];
+                n10 = s_va[k0 + 1];
+                n01 = s_va[k0 + VA_W];
+                n11 = s_va[k0 + VA_W + 1];
+              } else {
+                const int64_t k0 = (int64_t)cy * row + cx;
+                n00 = A.va[k0];
+                n10 = A.va[k0 + 1];
+                n01 = A.va[k0 + row];
+                n11 = A.va[k0 + row + 1];
+              }
+              const float wx0 = 1.0f - fx, wx1 = fx, wy0 = 1.0f - fy, wy1 = fy;
+              const float w00 = wx0 * wy0, w10 = wx1 * wy0, w01 = wx0 * wy1,
+                          w11 = wx1 * wy1;
+              // grid-unit gradients of the four weights
+              const float ih = A.inv_h;
+              const float Lxx = (-wy0 * n00.x + wy0 * n10.x - wy1 * n01.x + wy1 * n11.x) * ih;
+              const float Lxy = (-wx0 * n00.x - wx1 * n10.x + wx0 * n01.x + wx1 * n11.x) * ih;
+              const float Lyx = (-wy0 * n00.y + wy0 * n10.y - wy1 * n01.y + wy1 * n11.y) * ih;
+              const float Lyy = (-wx0 * n00.y - wx1 * n10.y + wx0 * n01.y + wx1 * n11.y) * ih;
+              const float vpx = w00 * n00.x + w10 * n10.x + w01 * n01.x + w11 * n11.x;
+              const float vpy = w00 * n00.y + w10 * n10.y + w01 * n01.y + w11 * n11.y;
+              const float apx = w00 * n00.z + w10 * n10.z + w01 * n01.z + w11 * n11.z;
+              const float apy = w00 * n00.w + w10 * n10.w + w01 * n01.w + w11 * n11.w;
+              constitutive_update(st, jh, Lxx, Lxy, Lyx, Lyy, A.dt, A.kappa, A.mu,
+                                  A.dp_alpha);
+              float dux, duy;
+              const float dtih = A.dt * A.inv_h;
+              if (!(fl & 2)) {
+                const float a = A.flip_alpha;
+                dux = dtih * vpx;
+                duy = dtih * vpy;
+                vel.x = (1.0f - a) * vpx + a * (vel.x + A.dt * apx);
+                vel.y = (1.0f - a) * vpy + a * (vel.y + A.dt * apy);
+              } else {
+                dux = dtih * vel.x;
+                duy = dtih * vel.y;
+              }
+              double2 un = make_double2(u.x + (double)dux, u.y + (double)duy);
+              // new cell and fraction, FP32 carry of the old fraction
+              nfx = fx + dux;
+              nfy = fy + duy;
+              bool exact = !(fabsf(dux) < 1.0f && fabsf(duy) < 1.0f);
+              if (nfx >= 1.0f) { nfx -= 1.0f; ncx += 1; }
+              else if (nfx < 0.0f) { nfx += 1.0f; ncx -= 1; }
+              if (nfy >= 1.0f) { nfy -= 1.0f; ncy += 1; }
+              else if (nfy < 0.0f) { nfy += 1.0f; ncy -= 1; }
+              // MaterialPoints::resolvePlaneCollisions in grid units
+              const float ufx = (float)ncx + nfx, ufy = (float)ncy + nfy;
+              for (int k = 0; k < A.nplanes; ++k) {
+                const MpmPlaneDev &pl = A.planes[k];
+                if (ufy < pl.fulb - A.pmargin) continue;
+                const float dapprox = pl.n[0] * (ufx - pl.fux[0]) + pl.n[1] * (ufy - pl.fux[1]);
+                if (dapprox > A.pmargin) continue;
+                if (un.y < pl.ulb) continue;
+                const double d = pl.n[0] * (un.x - pl.ux[0]) + pl.n[1] * (un.y - pl.ux[1]);
+                if (d > 0.0) continue;
+                un.x += -d * pl.n[0];
+                un.y += -d * pl.n[1];
+                exact = true;
+                if (!pl.sticking) {
+                  const float vn = (float)pl.n[0] * vel.x + (float)pl.n[1] * vel.y;
+                  if (vn > 0.0f) continue;
+                  vel.x -= vn * (float)pl.n[0];
+                  vel.y -= vn * (float)pl.n[1];
+                } else {
+                  vel = make_float2(0.0f, 0.0f);
+                }
+              }
+              if (exact) {
+                split_u(un.x, ncx, nfx);
+                split_u(un.y, ncy, nfy);
+              }
+              if (!isfinite(un.x + un.y) || !isfinite(vel.x + vel.y) || !isfinite(st.x)) {
+                atomicOr(A.status, (uint32_t)HG_STATUS_NONFINITE);
+              }
+              A.u[p] = un;
+              A.v[p] = vel;
+              A.strain[p] = st;
+              A.flags[p] = (uint8_t)((fl & ~1) | jh);
+              // next step's G2P window test
+              const int ngx = ncx - (X0 - DRIFT), ngy = ncy - (Y0 - DRIFT);
+              if (ngx < 0 || ngy < 0 || ngx > VA_W - 2 || ngy > VA_W - 2)
+                atomicAdd(&s_out, 1u);
+            }
+            if (!in_grid_cell(A, ncx, ncy)) {
+              atomicOr(A.status, (uint32_t)HG_STATUS_OUT_OF_GRID);
+            } else {
+              // ---- P2G record for the next step ----
+              PRec r;
+              float s00, s01, s11;
+              stress_factor(st, jh, mv.y, A.inv_h, A.kappa, A.mu, s00, s01, s11);
+              r.a = make_float4(nfx, nfy, mv.x, mv.x * vel.x);
+              r.b = make_float4(mv.x * vel.y, s00, s01, s11);
+              const int lx = ncx - WX, ly = ncy - WY;
+              if (lx >= 0 && ly >= 0 && lx < NC && ly < NC) {
+                const int cell = ly * NC + lx;
+                const int rank = atomicAdd(&s_cnt[cell], 1);
+                s_rec[sl] = r;
+                packed = (cell << 11) | rank;
+              } else {
+                scatter_global(A, ncx, ncy, r);
+              }
+            }
+          }
+        }
+        s_slot[sl] = packed;
+      }
+      __syncthreads();
+      // ---- exclusive scan of the cell counts (NCELL <= 2 * THREADS) ----
+      {
+        const int c0 = 2 * tid, c1 = 2 * tid + 1;
+        const int v0 = c0 < NCELL ? s_cnt[c0] : 0;
+        const int v1 = c1 < NCELL ? s_cnt[c1] : 0;
+        int x = v0 + v1;
+        const int lane = tid & 31, wid = tid >> 5;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const int y = __shfl_up_sync(0xffffffffu, x, d);
+          if (lane >= d) x += y;
+        }
+        if (lane == 31) s_warp[wid] = x;
+        __syncthreads();
+        int off = 0;
+        for (int w = 0; w < wid; ++w) off += s_warp[w];
+        const int excl = off + x - (v0 + v1);
+        if (c0 < NCELL) s_start[c0] = excl;
+        if (c1 < NCELL) s_start[c1] = excl + v0;
+      }
+      __syncthreads();
+      for (int sl = tid; sl < PASS; sl += THREADS) {
+        const int pk = s_slot[sl];
+        if (pk >= 0) s_sorted[s_start[pk >> 11] + (pk & 2047)] = sl;
+      }
+      __syncthreads();
+      // ---- node gather over the four adjacent cells ----
+      for (int k = tid; k < ACC_W * ACC_W; k += THREADS) {
+        const int i = k % ACC_W, j = k / ACC_W;
+        float m = 0.f, px = 0.f, py = 0.f, fxs = 0.f, fys = 0.f;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int dx = (q & 1) ? 0 : 1; // node offset from the cell corner
+          const int dy = (q & 2) ? 0 : 1;
+          const int ci = i - dx, cj = j - dy;
+          if (ci < 0 || cj < 0 || ci >= NC || cj >= NC) continue;
+          const int cell = cj * NC + ci;
+          const int b0 = s_start[cell], cnt = s_cnt[cell];
+          for (int e = 0; e < cnt; ++e) {
+            const PRec r = s_rec[s_sorted[b0 + e]];
+            const float wx = dx ? r.a.x : 1.0f - r.a.x;
+            const float wy = dy ? r.a.y : 1.0f - r.a.y;
+            const float w = wx * wy;
+            m += w * r.a.z;
+            px += w * r.a.w;
+            py += w * r.b.x;
+            if (w != 0.0f) {
+              const float gx = dx ? wy : -wy, gy = dy ? wx : -wx;
+              fxs += r.b.y * gx + r.b.z * gy;
+              fys += r.b.z * gx + r.b.w * gy;
+            }
+          }
+        }
+        if (m != 0.f || px != 0.f || py != 0.f || fxs != 0.f || fys != 0.f) {
+          s_accm[k] += m;
+          float4 a = s_acc[k];
+          a.x += px;
+          a.y += py;
+          a.z += fxs;
+          a.w += fys;
+          s_acc[k] = a;
+        }
+      }
+      __syncthreads();
+    }
+    // ---- flush the window to the global accumulators ----
+    for (int k = tid; k < ACC_W * ACC_W; k += THREADS) {
+      const float m = s_accm[k];
+      const float4 a = s_acc[k];
+      if (m == 0.f && a.x == 0.f && a.y == 0.f && a.z == 0.f && a.w == 0.f) continue;
+      const int ix = WX + k % ACC_W, iy = WY + k / ACC_W;
+      if (ix < 0 || iy < 0 || ix > A.nx || iy > A.ny) continue;
+      const int64_t node = (int64_t)iy * row + ix;
+      atomicAdd(&A.accm[node], m);
+      atomicAdd(&A.acc4[node], a);
+    }
+    __syncthreads();
+    if (tid == 0 && s_out) atomicAdd(A.outside, s_out);
+  }
+}
+
+// Node update over active tiles; one thread per node of a 16x16 tile.
+__global__ void __launch_bounds__(THREADS) kx_grid_update(MixedArgs A, float4 *va) {
+  const int nact = *A.nactive;
+  const int row = A.nx + 1;
+  const int lx = threadIdx.x % BIN, ly = threadIdx.x / BIN;
+  for (int t = blockIdx.x; t < nact; t += gridDim.x) {
+    const int tile = A.active[t];
+    const int ix = (tile % A.ntx) * BIN + lx, iy = (tile / A.ntx) * BIN + ly;
+    if (ix > A.nx || iy > A.ny) continue;
+    const int64_t i = (int64_t)iy * row + ix;
+    const float m = A.accm[i];
+    const float4 acc = A.acc4[i];
+    float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (m > 0.0f) {
+      const float fx = acc.z + m * A.gx, fy = acc.w + m * A.gy;
+      // p_new - p, kept as an increment so FP32 keeps its bits on it
+      float dpx = A.dt * fx, dpy = A.dt * fy;
+      for (int k = 0; k < A.nplanes; ++k) {
+        const MpmPlaneDev &pl = A.planes[k];
+        const float fy_node = (float)iy;
+        if (fy_node < pl.fulb - A.pmargin) continue;
+        float d = pl.n[0] * ((float)ix - pl.fux[0]) + pl.n[1] * (fy_node - pl.fux[1]);
+        if (fabsf(d) < A.pmargin || fabsf(fy_node - pl.fulb) < A.pmargin) {
+          if ((double)iy < pl.ulb) continue;
+          const double dd = pl.n[0] * ((double)ix - pl.ux[0]) + pl.n[1] * ((double)iy - pl.ux[1]);
+          d = dd > 0.0 ? 1.0f : -1.0f;
+        }
+        if (d > 0.0f) continue;
+        if (!pl.sticking) {
+          const float vx = (acc.x + dpx) / m, vy = (acc.y + dpy) / m;
+          const float vn = (float)pl.n[0] * vx + (float)pl.n[1] * vy;
+          if (vn > 0.0f) continue;
+          dpx -= m * vn * (float)pl.n[0];
+          dpy -= m * vn * (float)pl.n[1];
+        } else {
+          dpx = -acc.x;
+          dpy = -acc.y;
+        }
+      }
+      const float inv_m = 1.0f / m;
+      out = make_float4((acc.x + dpx) * inv_m, (acc.y + dpy) * inv_m,
+                        dpx * inv_m / A.dt, dpy * inv_m / A.dt);
+    }
+    va[i] = out;
+    A.gm[i] = m;
+    A.accm[i] = 0.f;
+    A.acc4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+}
+
+// ---- re-sort -----------------------------------------------------------------
+
+__global__ void kx_keys(int64_t n, int nx, int ny, int ntx, const double2 *__restrict__ u,
+                        int32_t *keys, int32_t *counts, uint32_t *status) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  // Cell key floor((x - min)/h) in the reference's form (LinearBasisFunctions.
+  // cpp:53-59) is floor(u) here: u was computed with exactly that division.
+  const double2 up = u[p];
+  int cx = (int)floor(up.x), cy = (int)floor(up.y);
+  if (!(up.x >= 0.0 && up.y >= 0.0 && cx < nx && cy < ny)) {
+    atomicOr(status, (uint32_t)HG_STATUS_OUT_OF_GRID);
+    cx = min(max(cx, 0), nx - 1);
+    cy = min(max(cy, 0), ny - 1);
+  }
+  const int key = ((cy / BIN) * ntx + cx / BIN) * BIN_CELLS + (cy % BIN) * BIN + (cx % BIN);
+  keys[p] = key;
+  atomicAdd(&counts[key], 1);
+}
+
+__global__ void kx_scatter(int64_t n, const int32_t *__restrict__ keys,
+                           const int32_t *__restrict__ offsets, int32_t *cursor,
+                           MixedParticles src, MixedParticles dst) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const int key = keys[p];
+  const int64_t d = offsets[key] + atomicAdd(&cursor[key], 1);
+  dst.u[d] = src.u[p];
+  dst.v[d] = src.v[p];
+  dst.mv[d] = src.mv[p];
+  dst.strain[d] = src.strain[p];
+  dst.flags[d] = src.flags[p];
+  dst.id[d] = src.id[p];
+}
+
+__global__ void kx_active(int ntx, int nty, const int32_t *__restrict__ offsets,
+                          int32_t *bins, int32_t *tiles, int32_t *nactive) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= ntx * nty) return;
+  auto count = [&](int t) {
+    return offsets[(t + 1) * BIN_CELLS] - offsets[t * BIN_CELLS];
+  };
+  if (count(b) > 0) bins[atomicAdd(&nactive[0], 1)] = b;
+  const int tx = b % ntx, ty = b / ntx;
+  bool any = false;
+  for (int dy = -1; dy <= 1 && !any; ++dy)
+    for (int dx = -1; dx <= 1; ++dx) {
+      const int x = tx + dx, y = ty + dy;
+      if (x < 0 || y < 0 || x >= ntx || y >= nty) continue;
+      if (count(y * ntx + x) > 0) {
+        any = true;
+        break;
+      }
+    }
+  if (any) tiles[atomicAdd(&nactive[1], 1)] = b;
+}
+
+// ---- upload / download conversion -------------------------------------------
+
+__global__ void kx_upload(int64_t n, double gx, double gy, double h,
+                          const double *__restrict__ q, const double *__restrict__ v,
+                          const double *__restrict__ m, const double *__restrict__ vol,
+                          const double *__restrict__ be, const double *__restrict__ J,
+                          const int32_t *__restrict__ jh, const uint8_t *__restrict__ kin,
+                          MixedParticles dst) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  dst.u[p] = make_double2((q[2 * p] - gx) / h, (q[2 * p + 1] - gy) / h);
+  dst.v[p] = make_float2((float)v[2 * p], (float)v[2 * p + 1]);
+  dst.mv[p] = make_float2((float)m[p], (float)vol[p]);
+  const double b00 = be[4 * p], b10 = be[4 * p + 1], b01 = be[4 * p + 2], b11 = be[4 * p + 3];
+  dst.strain[p] = make_float4((float)(J[p] - 1.0), (float)(b00 - 1.0),
+                              (float)(0.5 * (b10 + b01)), (float)(b11 - 1.0));
+  dst.flags[p] = (uint8_t)((jh[p] != 0 ? 1 : 0) | (kin[p] != 0 ? 2 : 0));
+  dst.id[p] = (int32_t)p;
+}
+
+__global__ void kx_download(int64_t n, double gx, double gy, double h, MixedParticles src,
+                            double *q, double *v, double *be, double *J, int32_t *jh) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int64_t o = src.id[k];
+  const double2 u = src.u[k];
+  q[2 * o] = gx + u.x * h;
+  q[2 * o + 1] = gy + u.y * h;
+  const float2 vv = src.v[k];
+  v[2 * o] = vv.x;
+  v[2 * o + 1] = vv.y;
+  const float4 s = src.strain[k];
+  be[4 * o] = 1.0 + (double)s.y;
+  be[4 * o + 1] = (double)s.z;
+  be[4 * o + 2] = (double)s.z;
+  be[4 * o + 3] = 1.0 + (double)s.w;
+  J[o] = 1.0 + (double)s.x;
+  jh[o] = src.flags[k] & 1;
+}
+
+__global__ void kx_grid_download(int64_t nn, const float *__restrict__ gm,
+                                 const float4 *__restrict__ va, double *mass, double *vel,
+                                 double *acc) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nn) return;
+  const float4 a = va[i];
+  mass[i] = gm[i];
+  vel[2 * i] = a.x;
+  vel[2 * i + 1] = a.y;
+  acc[2 * i] = a.z;
+  acc[2 * i + 1] = a.w;
+}
+
+inline int blocks_for(int64_t n, int t) { return (int)((n + t - 1) / t); }
+
+MixedParticles parts(hg_mpm *m, int which) {
+  MixedParticles P;
+  P.u = m->mu_[which].p;
+  P.v = m->mv_[which].p;
+  P.mv = m->mmv_[which].p;
+  P.strain = m->mstrain_[which].p;
+  P.flags = m->mflags_[which].p;
+  P.id = m->mid_[which].p;
+  return P;
+}
+
+size_t fused_smem_bytes() {
+  return sizeof(float4) * VA_W * VA_W + sizeof(float4) * ACC_W * ACC_W +
+         sizeof(PRec) * PASS + sizeof(float) * ACC_W * ACC_W + sizeof(int) * PASS * 2 +
+         sizeof(int) * NCELL * 2;
+}
+
+MixedArgs make_args(hg_mpm *m, double dt, bool tiles) {
+  MixedArgs A;
+  const hg::MpmParams &P = m->p;
+  A.nx = P.nx;
+  A.ny = P.ny;
+  A.ntx = m->ntx;
+  A.nty = m->nty;
+  A.n = m->n;
+  A.dt = (float)dt;
+  A.inv_h = (float)P.inv_h;
+  A.kappa = (float)P.kappa;
+  A.mu = (float)P.mu;
+  A.dp_alpha = (float)P.dp_alpha;
+  A.flip_alpha = (float)P.flip_alpha;
+  A.gx = (float)P.g[0];
+  A.gy = (float)P.g[1];
+  A.pmargin = 0.01f + 4.0e-7f * (float)(P.nx + P.ny);
+  A.nplanes = P.nplanes;
+  for (int k = 0; k < HG_MAX_PLANES; ++k) A.planes[k] = P.planes[k];
+  A.offsets = m->offsets.p;
+  A.active = tiles ? m->active_tiles.p : m->active_bins.p;
+  A.nactive = tiles ? m->nactive.p + 1 : m->nactive.p;
+  MixedParticles cur = parts(m, m->cur);
+  A.u = cur.u;
+  A.v = cur.v;
+  A.mv = cur.mv;
+  A.strain = cur.strain;
+  A.flags = cur.flags;
+  A.va = m->va.p;
+  A.acc4 = m->acc4.p;
+  A.accm = m->accm.p;
+  A.gm = m->gm.p;
+  A.status = m->status.p;
+  A.outside = m->outside.p;
+  return A;
+}
+
+hg_status rebin(hg_mpm *m) {
+  cudaStream_t s = m->ctx->stream;
+  const int64_t nkeys = (int64_t)m->ntx * m->nty * BIN_CELLS;
+  HG_CUDA_TRY(cudaMemsetAsync(m->counts.p, 0, sizeof(int32_t) * (nkeys + 1), s));
+  HG_CUDA_TRY(cudaMemsetAsync(m->cursor.p, 0, sizeof(int32_t) * nkeys, s));
+  HG_CUDA_TRY(cudaMemsetAsync(m->nactive.p, 0, sizeof(int32_t) * 2, s));
+  HG_CUDA_TRY(cudaMemsetAsync(m->outside.p, 0, sizeof(uint32_t), s));
+  if (m->n > 0) {
+    HG_LAUNCH(kx_keys, blocks_for(m->n, 256), 256, 0, s, m->n, m->p.nx, m->p.ny, m->ntx,
+              m->mu_[m->cur].p, m->keys.p, m->counts.p, m->status.p);
+    HG_CHECK_LAUNCH();
+  }
+  hg_status st = exclusive_scan_i32(m->counts.p, m->offsets.p, nkeys + 1, m->scan_tmp.p, s);
+  if (st != HG_OK) return st;
+  if (m->n > 0) {
+    HG_LAUNCH(kx_scatter, blocks_for(m->n, 256), 256, 0, s, m->n, m->keys.p, m->offsets.p,
+              m->cursor.p, parts(m, m->cur), parts(m, 1 - m->cur));
+    HG_CHECK_LAUNCH();
+  }
+  m->cur = 1 - m->cur;
+  HG_LAUNCH(kx_active, blocks_for((int64_t)m->ntx * m->nty, 256), 256, 0, s, m->ntx, m->nty,
+            m->offsets.p, m->active_bins.p, m->active_tiles.p, m->nactive.p);
+  HG_CHECK_LAUNCH();
+  m->steps_since_rebin = 0;
+  m->outside_pending = false;
+  m->rebins++;
+  return HG_OK;
+}
+
+int fused_blocks(hg_mpm *m) { return m->ctx->num_sms * 3; }
+int update_blocks(hg_mpm *m) { return m->ctx->num_sms * 8; }
+
+hg_status prime(hg_mpm *m) {
+  cudaStream_t s = m->ctx->stream;
+  const int64_t nn = (int64_t)(m->p.nx + 1) * (m->p.ny + 1);
+  HG_CUDA_TRY(cudaMemsetAsync(m->accm.p, 0, sizeof(float) * nn, s));
+  HG_CUDA_TRY(cudaMemsetAsync(m->acc4.p, 0, sizeof(float4) * nn, s));
+  hg_status st = rebin(m);
+  if (st != HG_OK) return st;
+  MixedArgs A = make_args(m, 0.0, false);
+  HG_LAUNCH(kx_g2p2g<true>, fused_blocks(m), THREADS, fused_smem_bytes(), s, A);
+  HG_CHECK_LAUNCH();
+  m->primed = true;
+  return HG_OK;
+}
+
+} // namespace
+
+hg_status mixed_alloc(hg_mpm *m) {
+  const int64_t nn = (int64_t)(m->p.nx + 1) * (m->p.ny + 1);
+  m->ntx = (m->p.nx + 1 + BIN - 1) / BIN;
+  m->nty = (m->p.ny + 1 + BIN - 1) / BIN;
+  const int64_t nkeys = (int64_t)m->ntx * m->nty * BIN_CELLS;
+  if (nkeys + 1 > (int64_t)INT32_MAX / 2)
+    return fail(HG_ERR_INVALID_ARGUMENT, "grid too large for the MIXED path");
+  for (int b = 0; b < 2; ++b) {
+    hg_status st;
+    if ((st = m->mu_[b].alloc(m->cap)) || (st = m->mv_[b].alloc(m->cap)) ||
+        (st = m->mmv_[b].alloc(m->cap)) || (st = m->mstrain_[b].alloc(m->cap)) ||
+        (st = m->mflags_[b].alloc(m->cap)) || (st = m->mid_[b].alloc(m->cap)))
+      return st;
+  }
+  hg_status st;
+  if ((st = m->acc4.alloc(nn)) || (st = m->accm.alloc(nn)) || (st = m->va.alloc(nn)) ||
+      (st = m->gm.alloc(nn)) || (st = m->keys.alloc(m->cap)) ||
+      (st = m->counts.alloc(nkeys + 1)) || (st = m->offsets.alloc(nkeys + 1)) ||
+      (st = m->cursor.alloc(nkeys)) || (st = m->scan_tmp.alloc(scan_tmp_size(nkeys + 1))) ||
+      (st = m->active_bins.alloc((int64_t)m->ntx * m->nty)) ||
+      (st = m->active_tiles.alloc((int64_t)m->ntx * m->nty)) ||
+      (st = m->nactive.alloc(2)) || (st = m->outside.alloc(1)))
+    return st;
+  cudaStream_t s = m->ctx->stream;
+  HG_CUDA_TRY(cudaMemsetAsync(m->acc4.p, 0, sizeof(float4) * nn, s));
+  HG_CUDA_TRY(cudaMemsetAsync(m->accm.p, 0, sizeof(float) * nn, s));
+  HG_CUDA_TRY(cudaMemsetAsync(m->va.p, 0, sizeof(float4) * nn, s));
+  HG_CUDA_TRY(cudaMemsetAsync(m->gm.p, 0, sizeof(float) * nn, s));
+  HG_CUDA_TRY(cudaMemsetAsync(m->nactive.p, 0, sizeof(int32_t) * 2, s));
+  HG_CUDA_TRY(cudaMallocHost(&m->h_outside, sizeof(uint32_t)));
+  HG_CUDA_TRY(cudaEventCreateWithFlags(&m->outside_ev, cudaEventDisableTiming));
+  HG_CUDA_TRY(cudaFuncSetAttribute(kx_g2p2g<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)fused_smem_bytes()));
+  HG_CUDA_TRY(cudaFuncSetAttribute(kx_g2p2g<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)fused_smem_bytes()));
+  return HG_OK;
+}
+
+hg_status mixed_upload(hg_mpm *m, const double *q, const double *v, const double *mass,
+                       const double *vol, const double *be, const double *J,
+                       const int32_t *jh, const uint8_t *kin) {
+  cudaStream_t s = m->ctx->stream;
+  const int64_t n = m->n;
+  if (n > 0) {
+    HG_LAUNCH(kx_upload, blocks_for(n, 256), 256, 0, s, n, m->p.gmin[0], m->p.gmin[1], m->p.h,
+              q, v, mass, vol, be, J, jh, kin, parts(m, m->cur));
+    HG_CHECK_LAUNCH();
+  }
+  return prime(m);
+}
+
+hg_status mixed_download(hg_mpm *m, double *q, double *v, double *be, double *J, int32_t *jh) {
+  if (m->n <= 0) return HG_OK;
+  HG_LAUNCH(kx_download, blocks_for(m->n, 256), 256, 0, m->ctx->stream, m->n, m->p.gmin[0],
+            m->p.gmin[1], m->p.h, parts(m, m->cur), q, v, be, J, jh);
+  HG_CHECK_LAUNCH();
+  return HG_OK;
+}
+
+hg_status mixed_download_grid(hg_mpm *m, double *mass, double *vel, double *acc) {
+  const int64_t nn = (int64_t)(m->p.nx + 1) * (m->p.ny + 1);
+  HG_LAUNCH(kx_grid_download, blocks_for(nn, 256), 256, 0, m->ctx->stream, nn, m->gm.p,
+            m->va.p, mass, vel, acc);
+  HG_CHECK_LAUNCH();
+  return HG_OK;
+}
+
+// Maximum number of steps between two re-sorts. Particles outside their
+// window are exact but slow; this bound keeps every particle well inside the
+// dilated tile set that the grid update covers.
+constexpr int64_t MAX_STEPS_BETWEEN_REBINS = 64;
+
+hg_status mixed_profile_read(hg_mpm *m, double *g2p2g_ms, double *update_ms, int64_t *steps) {
+  double a = 0.0, b = 0.0;
+  if (m->prof_used > 0) HG_CUDA_TRY(cudaEventSynchronize(m->prof_events[m->prof_used - 1]));
+  for (size_t k = 0; k + 2 < m->prof_used; k += 3) {
+    float t01 = 0.f, t12 = 0.f;
+    HG_CUDA_TRY(cudaEventElapsedTime(&t01, m->prof_events[k], m->prof_events[k + 1]));
+    HG_CUDA_TRY(cudaEventElapsedTime(&t12, m->prof_events[k + 1], m->prof_events[k + 2]));
+    b += t01;
+    a += t12;
+  }
+  if (g2p2g_ms) *g2p2g_ms = a;
+  if (update_ms) *update_ms = b;
+  if (steps) *steps = (int64_t)(m->prof_used / 3);
+  return HG_OK;
+}
+
+hg_status mixed_step(hg_mpm *m, double dt, int nsteps) {
+  cudaStream_t s = m->ctx->stream;
+  if (!m->primed) {
+    hg_status st = prime(m);
+    if (st != HG_OK) return st;
+  }
+  const size_t smem = fused_smem_bytes();
+  for (int k = 0; k < nsteps; ++k) {
+    bool need = m->steps_since_rebin >= MAX_STEPS_BETWEEN_REBINS;
+    if (!need && m->outside_pending && cudaEventQuery(m->outside_ev) == cudaSuccess) {
+      m->outside_pending = false;
+      need = *m->h_outside > 0;
+    }
+    if (need) {
+      hg_status st = rebin(m);
+      if (st != HG_OK) return st;
+    }
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    if (m->profile) {
+      while (m->prof_events.size() < m->prof_used + 3) {
+        cudaEvent_t e;
+        HG_CUDA_TRY(cudaEventCreate(&e));
+        m->prof_events.push_back(e);
+      }
+      for (int j = 0; j < 3; ++j) ev[j] = m->prof_events[m->prof_used + j];
+      m->prof_used += 3;
+      HG_CUDA_TRY(cudaEventRecord(ev[0], s));
+    }
+    MixedArgs At = make_args(m, dt, true);
+    HG_LAUNCH(kx_grid_update, update_blocks(m), THREADS, 0, s, At, m->va.p);
+    HG_CHECK_LAUNCH();
+    if (m->profile) HG_CUDA_TRY(cudaEventRecord(ev[1], s));
+    MixedArgs Ab = make_args(m, dt, false);
+    HG_LAUNCH(kx_g2p2g<false>, fused_blocks(m), THREADS, smem, s, Ab);
+    HG_CHECK_LAUNCH();
+    if (m->profile) HG_CUDA_TRY(cudaEventRecord(ev[2], s));
+    m->steps_since_rebin++;
+    if (!m->outside_pending) {
+      HG_CUDA_TRY(cudaMemcpyAsync(m->h_outside, m->outside.p, sizeof(uint32_t),
+                                  cudaMemcpyDeviceToHost, s));
+      HG_CUDA_TRY(cudaEventRecord(m->outside_ev, s));
+      m->outside_pending = true;
+    }
+  }
+  return HG_OK;
+}
+
+} // namespace hg

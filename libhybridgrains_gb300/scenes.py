@@ -1,0 +1,153 @@
+"""Synthetic scenes with the shapes of the benchmark configurations.
+
+* ``mpm_column``   - granular column on a floor between walls (MPM configs:
+                     1.0 x 0.5 m domain at h = 5 mm with a 0.2 x 0.4 m column,
+                     12,800 points; or 2048 x 1024 cells at h = 1 mm with a
+                     1.0 x 0.5 m column, 2,000,000 points).
+* ``dem_column``   - disks on a jittered hex lattice (10,000 disks, radii
+                     U[0.9, 1.1] mm, pitch 2.2 mm, 100 per row).
+
+Material constants follow the configuration text: E = 1e6 Pa, nu = 0.3,
+rho = 1550 kg/m^3, friction angle 30 deg. The Drucker-Prager coefficient used
+for a friction angle phi is alpha = sqrt(2/3) * 2 sin(phi) / (3 - sin(phi))
+(the reference takes alpha directly as a material input, so this mapping is a
+choice of this project). PIC/FLIP alpha = 0.999 as in the reference assets.
+Random numbers come from splitmix64 with the stated seed.
+"""
+import math
+
+import numpy as np
+
+GRAVITY = (0.0, -9.81)
+
+
+def elastic_moduli(E, nu):
+    """(shear, bulk) moduli of a plane-strain solid."""
+    return E / (2.0 * (1.0 + nu)), E / (3.0 * (1.0 - 2.0 * nu))
+
+
+def dp_alpha(phi_deg):
+    s = math.sin(math.radians(phi_deg))
+    return math.sqrt(2.0 / 3.0) * 2.0 * s / (3.0 - s)
+
+
+def splitmix64(seed, n):
+    """n uniform doubles in [0, 1) from splitmix64 (53-bit mantissas)."""
+    out = np.empty(n, dtype=np.float64)
+    x = seed & 0xFFFFFFFFFFFFFFFF
+    mask = 0xFFFFFFFFFFFFFFFF
+    for i in range(n):
+        x = (x + 0x9E3779B97F4A7C15) & mask
+        z = x
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & mask
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & mask
+        z = z ^ (z >> 31)
+        out[i] = (z >> 11) * (1.0 / 9007199254740992.0)
+    return out
+
+
+MPM_CONFIGS = {
+    # 12,800 points: 1.0 x 0.5 m domain, h = 5 mm, column 0.2 x 0.4 m at x = 0.1
+    "column_12800": dict(grid_min=(0.0, 0.0), grid_max=(1.0, 0.5), h=5.0e-3,
+                         rect_min=(0.1, 0.0), rect_max=(0.3, 0.4), dt=1.0e-5, steps=1000),
+    # 2,000,000 points: 2048 x 1024 cells at h = 1 mm, column 1.0 x 0.5 m
+    "column_2M": dict(grid_min=(0.0, 0.0), grid_max=(2.048, 1.024), h=1.0e-3,
+                      rect_min=(0.0, 0.0), rect_max=(1.0, 0.5), dt=2.0e-6, steps=500),
+}
+
+
+def mpm_material(E=1.0e6, nu=0.3, phi_deg=30.0, rho=1550.0):
+    mu, kappa = elastic_moduli(E, nu)
+    return dict(shear_modulus=mu, bulk_modulus=kappa, dp_alpha=dp_alpha(phi_deg),
+                flip_alpha=0.999, rho=rho)
+
+
+def mpm_planes(grid_min, grid_max):
+    """Sticking floor and walls (MPMStaticPlane STICKING)."""
+    return [((grid_min[0], grid_min[1]), (0.0, 1.0), True, -np.inf),
+            ((grid_min[0], grid_min[1]), (1.0, 0.0), True, -np.inf),
+            ((grid_max[0], grid_min[1]), (-1.0, 0.0), True, -np.inf)]
+
+
+def mpm_column(name="column_12800", **overrides):
+    """Configuration dict for an MPM column scene (geometry, material, planes)."""
+    cfg = dict(MPM_CONFIGS[name])
+    cfg.update(mpm_material())
+    cfg.update(overrides)
+    cfg["planes"] = mpm_planes(cfg["grid_min"], cfg["grid_max"])
+    cfg["samples_per_dim"] = 2
+    return cfg
+
+
+def seed_column_points(cfg):
+    """rasterizeRectangle (mpmgrains2d/InitialSimulationState.cpp:48-145) in numpy.
+
+    Same formula and filters as the reference (and as hg_mpm_seed_rectangle),
+    for hosts that build scenes without a device.
+    """
+    gmin, gmax, h = cfg["grid_min"], cfg["grid_max"], cfg["h"]
+    # PhysicsGrid::setDimensions
+    cx, cy = 0.5 * (gmin[0] + gmax[0]), 0.5 * (gmin[1] + gmax[1])
+    nx, ny = math.ceil((gmax[0] - gmin[0]) / h), math.ceil((gmax[1] - gmin[1]) / h)
+    g0 = (cx - 0.5 * (nx * h), cy - 0.5 * (ny * h))
+    rmin, rmax, npd = cfg["rect_min"], cfg["rect_max"], cfg["samples_per_dim"]
+    bx0, by0 = math.floor((rmin[0] - g0[0]) / h), math.floor((rmin[1] - g0[1]) / h)
+    bx1, by1 = math.ceil((rmax[0] - g0[0]) / h), math.ceil((rmax[1] - g0[1]) / h)
+    gx = np.arange(bx0, bx1, dtype=np.float64)
+    gy = np.arange(by0, by1, dtype=np.float64)
+    off = (np.arange(npd, dtype=np.float64) + 0.5) / float(npd)
+    # loop order gy, gx, cy, cx
+    px = g0[0] + h * (gx[None, :, None, None] + off[None, None, None, :])
+    py = g0[1] + h * (gy[:, None, None, None] + off[None, None, :, None])
+    px, py = np.broadcast_arrays(px, py)
+    px, py = px.ravel(), py.ravel()
+    keep = (px >= rmin[0]) & (py >= rmin[1]) & (px <= rmax[0]) & (py <= rmax[1])
+    for (x, n, _st, lb) in cfg["planes"]:
+        nn = math.hypot(n[0], n[1])
+        d = (n[0] / nn) * (px - x[0]) + (n[1] / nn) * (py - x[1])
+        # pointInsidePlane is evaluated plane by plane with early exits; with
+        # -inf lower bounds it reduces to "strictly behind any plane".
+        keep &= ~((py >= lb) & (d < 0.0))
+    px, py = px[keep], py[keep]
+    half = 0.5 * h / float(npd)
+    vol = half * half * 4.0
+    n = px.size
+    return dict(q=np.stack([px, py], axis=1), v=np.zeros((n, 2)),
+                m=np.full(n, cfg["rho"] * vol), vol=np.full(n, vol), hl=np.full(n, half))
+
+
+# ---- DEM ------------------------------------------------------------------------
+
+def dem_column(n=10000, per_row=100, pitch=2.2e-3, rmin=0.9e-3, rmax=1.1e-3, jitter=0.05e-3,
+               rho=2600.0, seed=12345, x0=0.0, y0=0.0):
+    """Disks on a hex lattice with seeded radius and position jitter.
+
+    Returns q, v as (N, 3), radii, masses (rho pi r^2) and inertias (m r^2 / 2,
+    rigidbody2d/CircleGeometry.cpp:44-48).
+    """
+    u = splitmix64(seed, 3 * n)
+    r = rmin + (rmax - rmin) * u[:n]
+    k = np.arange(n)
+    row, col = k // per_row, k % per_row
+    x = x0 + pitch * (col + 0.5 + 0.5 * (row % 2)) + jitter * (2.0 * u[n:2 * n] - 1.0)
+    y = y0 + pitch * (0.5 + row * math.sqrt(3.0) / 2.0) + jitter * (2.0 * u[2 * n:] - 1.0)
+    q = np.stack([x, y, np.zeros(n)], axis=1)
+    v = np.zeros((n, 3))
+    m = rho * math.pi * r * r
+    I = 0.5 * m * r * r
+    return dict(q=q, v=v, r=r, m=m, I=I, fixed=np.zeros(n, dtype=np.uint8))
+
+
+def dem_params(kn=1.0e5, mu=0.5, restitution=0.5, r_mean=1.0e-3, rho=2600.0):
+    """Penalty parameters: restitution-matched normal damping for the mean disk.
+
+    The reference applies 0.5 * gamma in the force law
+    (PenaltyImpactFrictionMap.cpp:641-645), so gamma_n = 2 c with
+    c = 2 sqrt(m_eff k) ln(1/e) / sqrt(pi^2 + ln(e)^2), m_eff = m / 2.
+    kt = 2/7 kn, gamma_t = gamma_n.
+    """
+    m = rho * math.pi * r_mean * r_mean
+    le = math.log(restitution)
+    c = 2.0 * math.sqrt(0.5 * m * kn) * (-le) / math.sqrt(math.pi ** 2 + le * le)
+    gn = 2.0 * c
+    return dict(kn=kn, kt=2.0 / 7.0 * kn, gamman=gn, gammat=gn, mu=mu)
