@@ -269,6 +269,8 @@ hg_status hg_mpm_create(hg_context *ctx, const hg_mpm_desc *d, hg_mpm **out) {
     q.ux[0] = (pl.x[0] - P.gmin[0]) / P.h;
     q.ux[1] = (pl.x[1] - P.gmin[1]) / P.h;
     q.ulb = (pl.lower_bound - P.gmin[1]) / P.h;
+    q.fn[0] = (float)q.n[0];
+    q.fn[1] = (float)q.n[1];
     q.fux[0] = (float)q.ux[0];
     q.fux[1] = (float)q.ux[1];
     q.fulb = (float)q.ulb;

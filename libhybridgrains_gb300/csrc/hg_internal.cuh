@@ -93,6 +93,7 @@ struct MpmPlaneDev {
   double ux[2];
   double ulb;
   float fux[2], fulb;
+  float fn[2]; // the normal in FP32 for the mixed-precision kernels
 };
 
 struct MpmParams {

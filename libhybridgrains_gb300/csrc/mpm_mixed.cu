@@ -25,16 +25,17 @@
 // itself rather than on the leading 1. Grid fields are dense node-major
 // float4/float arrays; only tiles near particles are touched.
 //
-// P2G without float atomics on shared memory: for each pass of up to PASS
-// particles a CTA counting-sorts the particles of its tile by their new cell
-// (integer shared atomics), then one thread per node of the tile's window
-// gathers the contributions of the four adjacent cells. Window sums go to
-// global memory with one float4 + one float atomic per touched node.
+// P2G is cell-major: one thread per cell accumulates the contributions of the
+// points sorted into its cell in registers (no atomics); points that left
+// their cell since the last re-sort use shared-memory atomics on the tile's
+// node window. Window sums go to global memory with one float4 + one float
+// atomic per touched node.
 //
-// Re-sorting (counting sort by cell key) runs when a particle has drifted
-// out of its tile's window. Particles outside their window are still handled
-// exactly (G2P from global velocity, P2G with global atomics), so the re-sort
-// cadence affects speed only.
+// Re-sorting (counting sort by cell key) runs when a point has drifted out of
+// its tile's window, when more than 1/32 of the points have left their sorted
+// cell, and at least every MAX_STEPS_BETWEEN_REBINS steps. Points outside
+// their window are still handled exactly (G2P from global velocity, P2G with
+// global atomics), so the re-sort cadence affects speed only.
 #include "hg_internal.cuh"
 
 #include <cmath>
@@ -44,9 +45,6 @@ namespace hg {
 namespace {
 
 constexpr int THREADS = 256;
-constexpr int PASS = 1024; // particles staged per pass
-constexpr int NC = ACC_W - 1; // cells per side of the P2G window
-constexpr int NCELL = NC * NC;
 
 struct MixedArgs {
   int nx, ny, ntx, nty;
@@ -188,28 +186,69 @@ __device__ __forceinline__ void scatter_global(const MixedArgs &A, int cx, int c
   }
 }
 
+// Adds the P2G contribution of one material point at cell (cx, cy) with
+// fractions (fx, fy) to 4 corner accumulators a[corner * 5 + {m, px, py, fx, fy}]
+// (corner = dx + 2 dy). The internal force is skipped where the weight is
+// zero, like PhysicsGrid::computeForces (PhysicsGrid.cpp:439-441).
+__device__ __forceinline__ void p2g_corners(const PRec &r, float *a) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int dx = k & 1, dy = k >> 1;
+    const float wx = dx ? r.a.x : 1.0f - r.a.x;
+    const float wy = dy ? r.a.y : 1.0f - r.a.y;
+    const float w = wx * wy;
+    a[5 * k + 0] += w * r.a.z;
+    a[5 * k + 1] += w * r.a.w;
+    a[5 * k + 2] += w * r.b.x;
+    if (w != 0.0f) {
+      const float gx = dx ? wy : -wy, gy = dy ? wx : -wx;
+      a[5 * k + 3] += r.b.y * gx + r.b.z * gy;
+      a[5 * k + 4] += r.b.z * gx + r.b.w * gy;
+    }
+  }
+}
+
+// Exact float -> double widening with integer operations (keeps the FP64 pipe
+// free). Zero and subnormal inputs give 0; they are below the resolution of
+// any position they are added to.
+__device__ __forceinline__ double widen(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xFFu;
+  if (e == 0u) return 0.0;
+  if (e == 0xFFu) return (double)f;
+  const unsigned long long bits = ((unsigned long long)(b >> 31) << 63) |
+                                  ((unsigned long long)(e + 896u) << 52) |
+                                  ((unsigned long long)(b & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+
+__device__ __forceinline__ bool finite_d(double x) {
+  return ((__double_as_longlong(x) >> 52) & 0x7FF) != 0x7FF;
+}
+
+// Cell-major fused kernel. A CTA owns one tile of BIN x BIN cells at a time
+// and one thread owns one cell: it updates the material points sorted into
+// that cell (G2P of this step) and accumulates their P2G contributions for the
+// next step in registers, per corner node of the cell. Points that have left
+// their cell since the last re-sort go through shared-memory atomics on the
+// tile's node window (or global atomics outside it). Corner sums are combined
+// per node through shared memory and flushed with one global atomic per node
+// and field.
 template <bool PRIME>
-__global__ void __launch_bounds__(THREADS, 3) kx_g2p2g(MixedArgs A) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  float4 *s_va = reinterpret_cast<float4 *>(smem);              // VA_W^2
-  float4 *s_acc = s_va + VA_W * VA_W;                             // ACC_W^2
-  PRec *s_rec = reinterpret_cast<PRec *>(s_acc + ACC_W * ACC_W);  // PASS
-  float *s_accm = reinterpret_cast<float *>(s_rec + PASS);        // ACC_W^2
-  int *s_slot = reinterpret_cast<int *>(s_accm + ACC_W * ACC_W);  // PASS
-  int *s_sorted = s_slot + PASS;                                  // PASS
-  int *s_cnt = s_sorted + PASS;                                   // NCELL
-  int *s_start = s_cnt + NCELL;                                   // NCELL
-  __shared__ int s_warp[THREADS / 32];
-  __shared__ unsigned s_out;
+__global__ void __launch_bounds__(THREADS, 2) kx_g2p2g(MixedArgs A) {
+  static_assert(THREADS == BIN_CELLS, "one thread per cell of a tile");
+  __shared__ float4 s_va[VA_W * VA_W];
+  __shared__ float s_slow[5][ACC_W * ACC_W];
+  __shared__ float s_corner[20][BIN_CELLS];
+  __shared__ unsigned s_out[2]; // left the tile window / left the sorted cell
 
   const int tid = threadIdx.x;
   const int nact = *A.nactive;
   const int row = A.nx + 1;
+  const int lcx = tid % BIN, lcy = tid / BIN;
   for (int t = blockIdx.x; t < nact; t += gridDim.x) {
     const int bin = A.active[t];
     const int X0 = (bin % A.ntx) * BIN, Y0 = (bin / A.ntx) * BIN;
-    const int start = A.offsets[bin * BIN_CELLS];
-    const int end = A.offsets[(bin + 1) * BIN_CELLS];
     const int WX = X0 - DRIFT - 1, WY = Y0 - DRIFT - 1; // P2G window origin (node)
     if (!PRIME) {
       for (int k = tid; k < VA_W * VA_W; k += THREADS) {
@@ -221,225 +260,219 @@ __global__ void __launch_bounds__(THREADS, 3) kx_g2p2g(MixedArgs A) {
       }
     }
     for (int k = tid; k < ACC_W * ACC_W; k += THREADS) {
-      s_acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-      s_accm[k] = 0.f;
-    }
-    if (tid == 0) s_out = 0;
-    for (int base = start; base < end; base += PASS) {
-      for (int k = tid; k < NCELL; k += THREADS) s_cnt[k] = 0;
-      __syncthreads();
-      // ---- per-particle update (G2P of this step) ----
-      for (int sl = tid; sl < PASS; sl += THREADS) {
-        const int64_t p = (int64_t)base + sl;
-        int packed = -1;
-        if (p < end) {
-          const double2 u = A.u[p];
-          int cx, cy;
-          float fx, fy;
-          split_u(u.x, cx, fx);
-          split_u(u.y, cy, fy);
-          if (!in_grid_cell(A, cx, cy)) {
-            atomicOr(A.status, (uint32_t)HG_STATUS_OUT_OF_GRID);
-          } else {
-            const float2 mv = A.mv[p];
-            float2 vel = A.v[p];
-            float4 st = A.strain[p];
-            int fl = A.flags[p];
-            int jh = fl & 1;
-            int ncx = cx, ncy = cy;
-            float nfx = fx, nfy = fy;
-            if (!PRIME) {
-              float4 n00, n10, n01, n11;
-              const int gx = cx - (X0 - DRIFT), gy = cy - (Y0 - DRIFT);
-              if (gx >= 0 && gy >= 0 && gx <= VA_W - 2 && gy <= VA_W - 2) {
-                const int k0 = gy * VA_W + gx;
-                n00 = s_va[k0];
-                n10 = s_va[k0 + 1];
-                n01 = s_va[k0 + VA_W];
-                n11 = s_va[k0 + VA_W + 1];
-              } else {
-                const int64_t k0 = (int64_t)cy * row + cx;
-                n00 = A.va[k0];
-                n10 = A.va[k0 + 1];
-                n01 = A.va[k0 + row];
-                n11 = A.va[k0 + row + 1];
-              }
-              const float wx0 = 1.0f - fx, wx1 = fx, wy0 = 1.0f - fy, wy1 = fy;
-              const float w00 = wx0 * wy0, w10 = wx1 * wy0, w01 = wx0 * wy1,
-                          w11 = wx1 * wy1;
-              // grid-unit gradients of the four weights
-              const float ih = A.inv_h;
-              const float Lxx = (-wy0 * n00.x + wy0 * n10.x - wy1 * n01.x + wy1 * n11.x) * ih;
-              const float Lxy = (-wx0 * n00.x - wx1 * n10.x + wx0 * n01.x + wx1 * n11.x) * ih;
-              const float Lyx = (-wy0 * n00.y + wy0 * n10.y - wy1 * n01.y + wy1 * n11.y) * ih;
-              const float Lyy = (-wx0 * n00.y - wx1 * n10.y + wx0 * n01.y + wx1 * n11.y) * ih;
-              const float vpx = w00 * n00.x + w10 * n10.x + w01 * n01.x + w11 * n11.x;
-              const float vpy = w00 * n00.y + w10 * n10.y + w01 * n01.y + w11 * n11.y;
-              const float apx = w00 * n00.z + w10 * n10.z + w01 * n01.z + w11 * n11.z;
-              const float apy = w00 * n00.w + w10 * n10.w + w01 * n01.w + w11 * n11.w;
-              constitutive_update(st, jh, Lxx, Lxy, Lyx, Lyy, A.dt, A.kappa, A.mu,
-                                  A.dp_alpha);
-              float dux, duy;
-              const float dtih = A.dt * A.inv_h;
-              if (!(fl & 2)) {
-                const float a = A.flip_alpha;
-                dux = dtih * vpx;
-                duy = dtih * vpy;
-                vel.x = (1.0f - a) * vpx + a * (vel.x + A.dt * apx);
-                vel.y = (1.0f - a) * vpy + a * (vel.y + A.dt * apy);
-              } else {
-                dux = dtih * vel.x;
-                duy = dtih * vel.y;
-              }
-              double2 un = make_double2(u.x + (double)dux, u.y + (double)duy);
-              // new cell and fraction, FP32 carry of the old fraction
-              nfx = fx + dux;
-              nfy = fy + duy;
-              bool exact = !(fabsf(dux) < 1.0f && fabsf(duy) < 1.0f);
-              if (nfx >= 1.0f) { nfx -= 1.0f; ncx += 1; }
-              else if (nfx < 0.0f) { nfx += 1.0f; ncx -= 1; }
-              if (nfy >= 1.0f) { nfy -= 1.0f; ncy += 1; }
-              else if (nfy < 0.0f) { nfy += 1.0f; ncy -= 1; }
-              // MaterialPoints::resolvePlaneCollisions in grid units
-              const float ufx = (float)ncx + nfx, ufy = (float)ncy + nfy;
-              for (int k = 0; k < A.nplanes; ++k) {
-                const MpmPlaneDev &pl = A.planes[k];
-                if (ufy < pl.fulb - A.pmargin) continue;
-                const float dapprox = pl.n[0] * (ufx - pl.fux[0]) + pl.n[1] * (ufy - pl.fux[1]);
-                if (dapprox > A.pmargin) continue;
-                if (un.y < pl.ulb) continue;
-                const double d = pl.n[0] * (un.x - pl.ux[0]) + pl.n[1] * (un.y - pl.ux[1]);
-                if (d > 0.0) continue;
-                un.x += -d * pl.n[0];
-                un.y += -d * pl.n[1];
-                exact = true;
-                if (!pl.sticking) {
-                  const float vn = (float)pl.n[0] * vel.x + (float)pl.n[1] * vel.y;
-                  if (vn > 0.0f) continue;
-                  vel.x -= vn * (float)pl.n[0];
-                  vel.y -= vn * (float)pl.n[1];
-                } else {
-                  vel = make_float2(0.0f, 0.0f);
-                }
-              }
-              if (exact) {
-                split_u(un.x, ncx, nfx);
-                split_u(un.y, ncy, nfy);
-              }
-              if (!isfinite(un.x + un.y) || !isfinite(vel.x + vel.y) || !isfinite(st.x)) {
-                atomicOr(A.status, (uint32_t)HG_STATUS_NONFINITE);
-              }
-              A.u[p] = un;
-              A.v[p] = vel;
-              A.strain[p] = st;
-              A.flags[p] = (uint8_t)((fl & ~1) | jh);
-              // next step's G2P window test
-              const int ngx = ncx - (X0 - DRIFT), ngy = ncy - (Y0 - DRIFT);
-              if (ngx < 0 || ngy < 0 || ngx > VA_W - 2 || ngy > VA_W - 2)
-                atomicAdd(&s_out, 1u);
-            }
-            if (!in_grid_cell(A, ncx, ncy)) {
-              atomicOr(A.status, (uint32_t)HG_STATUS_OUT_OF_GRID);
-            } else {
-              // ---- P2G record for the next step ----
-              PRec r;
-              float s00, s01, s11;
-              stress_factor(st, jh, mv.y, A.inv_h, A.kappa, A.mu, s00, s01, s11);
-              r.a = make_float4(nfx, nfy, mv.x, mv.x * vel.x);
-              r.b = make_float4(mv.x * vel.y, s00, s01, s11);
-              const int lx = ncx - WX, ly = ncy - WY;
-              if (lx >= 0 && ly >= 0 && lx < NC && ly < NC) {
-                const int cell = ly * NC + lx;
-                const int rank = atomicAdd(&s_cnt[cell], 1);
-                s_rec[sl] = r;
-                packed = (cell << 11) | rank;
-              } else {
-                scatter_global(A, ncx, ncy, r);
-              }
-            }
-          }
-        }
-        s_slot[sl] = packed;
-      }
-      __syncthreads();
-      // ---- exclusive scan of the cell counts (NCELL <= 2 * THREADS) ----
-      {
-        const int c0 = 2 * tid, c1 = 2 * tid + 1;
-        const int v0 = c0 < NCELL ? s_cnt[c0] : 0;
-        const int v1 = c1 < NCELL ? s_cnt[c1] : 0;
-        int x = v0 + v1;
-        const int lane = tid & 31, wid = tid >> 5;
 #pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-          const int y = __shfl_up_sync(0xffffffffu, x, d);
-          if (lane >= d) x += y;
-        }
-        if (lane == 31) s_warp[wid] = x;
-        __syncthreads();
-        int off = 0;
-        for (int w = 0; w < wid; ++w) off += s_warp[w];
-        const int excl = off + x - (v0 + v1);
-        if (c0 < NCELL) s_start[c0] = excl;
-        if (c1 < NCELL) s_start[c1] = excl + v0;
-      }
-      __syncthreads();
-      for (int sl = tid; sl < PASS; sl += THREADS) {
-        const int pk = s_slot[sl];
-        if (pk >= 0) s_sorted[s_start[pk >> 11] + (pk & 2047)] = sl;
-      }
-      __syncthreads();
-      // ---- node gather over the four adjacent cells ----
-      for (int k = tid; k < ACC_W * ACC_W; k += THREADS) {
-        const int i = k % ACC_W, j = k / ACC_W;
-        float m = 0.f, px = 0.f, py = 0.f, fxs = 0.f, fys = 0.f;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int dx = (q & 1) ? 0 : 1; // node offset from the cell corner
-          const int dy = (q & 2) ? 0 : 1;
-          const int ci = i - dx, cj = j - dy;
-          if (ci < 0 || cj < 0 || ci >= NC || cj >= NC) continue;
-          const int cell = cj * NC + ci;
-          const int b0 = s_start[cell], cnt = s_cnt[cell];
-          for (int e = 0; e < cnt; ++e) {
-            const PRec r = s_rec[s_sorted[b0 + e]];
-            const float wx = dx ? r.a.x : 1.0f - r.a.x;
-            const float wy = dy ? r.a.y : 1.0f - r.a.y;
-            const float w = wx * wy;
-            m += w * r.a.z;
-            px += w * r.a.w;
-            py += w * r.b.x;
-            if (w != 0.0f) {
-              const float gx = dx ? wy : -wy, gy = dy ? wx : -wx;
-              fxs += r.b.y * gx + r.b.z * gy;
-              fys += r.b.z * gx + r.b.w * gy;
-            }
-          }
-        }
-        if (m != 0.f || px != 0.f || py != 0.f || fxs != 0.f || fys != 0.f) {
-          s_accm[k] += m;
-          float4 a = s_acc[k];
-          a.x += px;
-          a.y += py;
-          a.z += fxs;
-          a.w += fys;
-          s_acc[k] = a;
-        }
-      }
-      __syncthreads();
+      for (int c = 0; c < 5; ++c) s_slow[c][k] = 0.f;
     }
-    // ---- flush the window to the global accumulators ----
-    for (int k = tid; k < ACC_W * ACC_W; k += THREADS) {
-      const float m = s_accm[k];
-      const float4 a = s_acc[k];
-      if (m == 0.f && a.x == 0.f && a.y == 0.f && a.z == 0.f && a.w == 0.f) continue;
-      const int ix = WX + k % ACC_W, iy = WY + k / ACC_W;
-      if (ix < 0 || iy < 0 || ix > A.nx || iy > A.ny) continue;
-      const int64_t node = (int64_t)iy * row + ix;
-      atomicAdd(&A.accm[node], m);
-      atomicAdd(&A.acc4[node], a);
+    if (tid < 2) s_out[tid] = 0;
+    const int ps = A.offsets[bin * BIN_CELLS + tid];
+    const int pe = A.offsets[bin * BIN_CELLS + tid + 1];
+    const int gcx = X0 + lcx, gcy = Y0 + lcy;
+    // Planes that can touch a point of this tile's window: the window corners
+    // bound every position a point of the tile can take this step.
+    unsigned plane_mask = 0;
+    for (int k = 0; k < A.nplanes; ++k) {
+      const MpmPlaneDev &pl = A.planes[k];
+      const float x0 = (float)WX, y0 = (float)WY;
+      const float x1 = (float)(WX + ACC_W), y1 = (float)(WY + ACC_W);
+      float dmin = fminf(fminf(pl.fn[0] * (x0 - pl.fux[0]) + pl.fn[1] * (y0 - pl.fux[1]),
+                               pl.fn[0] * (x1 - pl.fux[0]) + pl.fn[1] * (y0 - pl.fux[1])),
+                         fminf(pl.fn[0] * (x0 - pl.fux[0]) + pl.fn[1] * (y1 - pl.fux[1]),
+                               pl.fn[0] * (x1 - pl.fux[0]) + pl.fn[1] * (y1 - pl.fux[1])));
+      if (dmin <= 2.0f * A.pmargin && y1 >= pl.fulb - A.pmargin) plane_mask |= 1u << k;
     }
     __syncthreads();
-    if (tid == 0 && s_out) atomicAdd(A.outside, s_out);
+    float acc[20];
+#pragma unroll
+    for (int k = 0; k < 20; ++k) acc[k] = 0.f;
+    // the next point's state is loaded while the current one is processed
+    double2 nu = make_double2(0.0, 0.0);
+    float2 nmv = make_float2(0.f, 0.f), nvel = make_float2(0.f, 0.f);
+    float4 nst = make_float4(0.f, 0.f, 0.f, 0.f);
+    int nfl = 0;
+    if (ps < pe) {
+      nu = A.u[ps];
+      nmv = A.mv[ps];
+      nvel = A.v[ps];
+      nst = A.strain[ps];
+      nfl = A.flags[ps];
+    }
+    for (int p = ps; p < pe; ++p) {
+      const double2 u = nu;
+      const float2 mv = nmv;
+      float2 vel = nvel;
+      float4 st = nst;
+      const int fl = nfl;
+      if (p + 1 < pe) {
+        nu = A.u[p + 1];
+        nmv = A.mv[p + 1];
+        nvel = A.v[p + 1];
+        nst = A.strain[p + 1];
+        nfl = A.flags[p + 1];
+      }
+      int cx, cy;
+      float fx, fy;
+      split_u(u.x, cx, fx);
+      split_u(u.y, cy, fy);
+      if (!in_grid_cell(A, cx, cy)) {
+        atomicOr(A.status, (uint32_t)HG_STATUS_OUT_OF_GRID);
+        continue;
+      }
+      int jh = fl & 1;
+      int ncx = cx, ncy = cy;
+      float nfx = fx, nfy = fy;
+      if (!PRIME) {
+        float4 n00, n10, n01, n11;
+        const int gx = cx - (X0 - DRIFT), gy = cy - (Y0 - DRIFT);
+        const bool in_window = gx >= 0 && gy >= 0 && gx <= VA_W - 2 && gy <= VA_W - 2;
+        if (in_window) {
+          const int k0 = gy * VA_W + gx;
+          n00 = s_va[k0];
+          n10 = s_va[k0 + 1];
+          n01 = s_va[k0 + VA_W];
+          n11 = s_va[k0 + VA_W + 1];
+        } else {
+          const int64_t k0 = (int64_t)cy * row + cx;
+          n00 = A.va[k0];
+          n10 = A.va[k0 + 1];
+          n01 = A.va[k0 + row];
+          n11 = A.va[k0 + row + 1];
+        }
+        const float wx0 = 1.0f - fx, wx1 = fx, wy0 = 1.0f - fy, wy1 = fy;
+        const float w00 = wx0 * wy0, w10 = wx1 * wy0, w01 = wx0 * wy1, w11 = wx1 * wy1;
+        // velocity gradient from the grid-unit weight gradients
+        const float ih = A.inv_h;
+        const float Lxx = (-wy0 * n00.x + wy0 * n10.x - wy1 * n01.x + wy1 * n11.x) * ih;
+        const float Lxy = (-wx0 * n00.x - wx1 * n10.x + wx0 * n01.x + wx1 * n11.x) * ih;
+        const float Lyx = (-wy0 * n00.y + wy0 * n10.y - wy1 * n01.y + wy1 * n11.y) * ih;
+        const float Lyy = (-wx0 * n00.y - wx1 * n10.y + wx0 * n01.y + wx1 * n11.y) * ih;
+        const float vpx = w00 * n00.x + w10 * n10.x + w01 * n01.x + w11 * n11.x;
+        const float vpy = w00 * n00.y + w10 * n10.y + w01 * n01.y + w11 * n11.y;
+        const float apx = w00 * n00.z + w10 * n10.z + w01 * n01.z + w11 * n11.z;
+        const float apy = w00 * n00.w + w10 * n10.w + w01 * n01.w + w11 * n11.w;
+        constitutive_update(st, jh, Lxx, Lxy, Lyx, Lyy, A.dt, A.kappa, A.mu, A.dp_alpha);
+        float dux, duy;
+        const float dtih = A.dt * A.inv_h;
+        if (!(fl & 2)) {
+          const float a = A.flip_alpha;
+          dux = dtih * vpx;
+          duy = dtih * vpy;
+          vel.x = (1.0f - a) * vpx + a * (vel.x + A.dt * apx);
+          vel.y = (1.0f - a) * vpy + a * (vel.y + A.dt * apy);
+        } else {
+          dux = dtih * vel.x;
+          duy = dtih * vel.y;
+        }
+        double2 un = make_double2(u.x + widen(dux), u.y + widen(duy));
+        // new cell and fraction by FP32 carry of the old fraction
+        nfx = fx + dux;
+        nfy = fy + duy;
+        bool exact = !(fabsf(dux) < 1.0f && fabsf(duy) < 1.0f);
+        // the tile's plane mask bounds points that start in the window and
+        // move less than a cell; any other point tests every plane
+        const unsigned pmask = (in_window && !exact) ? plane_mask : (1u << A.nplanes) - 1u;
+        if (nfx >= 1.0f) { nfx -= 1.0f; ncx += 1; }
+        else if (nfx < 0.0f) { nfx += 1.0f; ncx -= 1; }
+        if (nfy >= 1.0f) { nfy -= 1.0f; ncy += 1; }
+        else if (nfy < 0.0f) { nfy += 1.0f; ncy -= 1; }
+        // MaterialPoints::resolvePlaneCollisions in grid units; FP32 test
+        // first, FP64 where the point is within pmargin cells of a plane
+        const float ufx = (float)ncx + nfx, ufy = (float)ncy + nfy;
+        for (unsigned mk = pmask; mk; mk &= mk - 1) {
+          const MpmPlaneDev &pl = A.planes[__ffs(mk) - 1];
+          if (ufy < pl.fulb - A.pmargin) continue;
+          const float dapprox = pl.fn[0] * (ufx - pl.fux[0]) + pl.fn[1] * (ufy - pl.fux[1]);
+          if (dapprox > A.pmargin) continue;
+          if (un.y < pl.ulb) continue;
+          const double d = pl.n[0] * (un.x - pl.ux[0]) + pl.n[1] * (un.y - pl.ux[1]);
+          if (d > 0.0) continue;
+          un.x += -d * pl.n[0];
+          un.y += -d * pl.n[1];
+          exact = true;
+          if (!pl.sticking) {
+            const float vn = pl.fn[0] * vel.x + pl.fn[1] * vel.y;
+            if (vn > 0.0f) continue;
+            vel.x -= vn * pl.fn[0];
+            vel.y -= vn * pl.fn[1];
+          } else {
+            vel = make_float2(0.0f, 0.0f);
+          }
+        }
+        if (exact) {
+          split_u(un.x, ncx, nfx);
+          split_u(un.y, ncy, nfy);
+        }
+        if (!finite_d(un.x) || !finite_d(un.y) || !isfinite(vel.x + vel.y) ||
+            !isfinite(st.x))
+          atomicOr(A.status, (uint32_t)HG_STATUS_NONFINITE);
+        A.u[p] = un;
+        A.v[p] = vel;
+        A.strain[p] = st;
+        A.flags[p] = (uint8_t)((fl & ~1) | jh);
+        const int ngx = ncx - (X0 - DRIFT), ngy = ncy - (Y0 - DRIFT);
+        if (ngx < 0 || ngy < 0 || ngx > VA_W - 2 || ngy > VA_W - 2) atomicAdd(&s_out[0], 1u);
+        if (ncx != gcx || ncy != gcy) atomicAdd(&s_out[1], 1u);
+      }
+      if (!in_grid_cell(A, ncx, ncy)) {
+        atomicOr(A.status, (uint32_t)HG_STATUS_OUT_OF_GRID);
+        continue;
+      }
+      // ---- P2G contribution for the next step ----
+      PRec r;
+      float s00, s01, s11;
+      stress_factor(st, jh, mv.y, A.inv_h, A.kappa, A.mu, s00, s01, s11);
+      r.a = make_float4(nfx, nfy, mv.x, mv.x * vel.x);
+      r.b = make_float4(mv.x * vel.y, s00, s01, s11);
+      if (ncx == gcx && ncy == gcy) {
+        p2g_corners(r, acc);
+      } else {
+        const int lx = ncx - WX, ly = ncy - WY;
+        if (lx >= 0 && ly >= 0 && lx <= ACC_W - 2 && ly <= ACC_W - 2) {
+          float part[20];
+#pragma unroll
+          for (int k = 0; k < 20; ++k) part[k] = 0.f;
+          p2g_corners(r, part);
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const int node = (ly + (k >> 1)) * ACC_W + lx + (k & 1);
+#pragma unroll
+            for (int c = 0; c < 5; ++c) atomicAdd(&s_slow[c][node], part[5 * k + c]);
+          }
+        } else {
+          scatter_global(A, ncx, ncy, r);
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 20; ++k) s_corner[k][tid] = acc[k];
+    __syncthreads();
+    // ---- node sums of the tile window, flushed to the global accumulators ----
+    for (int k = tid; k < ACC_W * ACC_W; k += THREADS) {
+      const int i = k % ACC_W, j = k / ACC_W;
+      float sum[5];
+#pragma unroll
+      for (int c = 0; c < 5; ++c) sum[c] = s_slow[c][k];
+      const int bi = i - (DRIFT + 1), bj = j - (DRIFT + 1); // node index within the tile
+      if (bi >= 0 && bj >= 0 && bi <= BIN && bj <= BIN) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int dx = q & 1, dy = q >> 1;
+          const int ci = bi - dx, cj = bj - dy;
+          if (ci < 0 || cj < 0 || ci >= BIN || cj >= BIN) continue;
+          const int cell = cj * BIN + ci;
+#pragma unroll
+          for (int c = 0; c < 5; ++c) sum[c] += s_corner[5 * q + c][cell];
+        }
+      }
+      if (sum[0] == 0.f && sum[1] == 0.f && sum[2] == 0.f && sum[3] == 0.f && sum[4] == 0.f)
+        continue;
+      const int ix = WX + i, iy = WY + j;
+      if (ix < 0 || iy < 0 || ix > A.nx || iy > A.ny) continue;
+      const int64_t node = (int64_t)iy * row + ix;
+      atomicAdd(&A.accm[node], sum[0]);
+      atomicAdd(&A.acc4[node], make_float4(sum[1], sum[2], sum[3], sum[4]));
+    }
+    __syncthreads();
+    if (tid < 2 && s_out[tid]) atomicAdd(&A.outside[tid], s_out[tid]);
   }
 }
 
@@ -464,7 +497,7 @@ __global__ void __launch_bounds__(THREADS) kx_grid_update(MixedArgs A, float4 *v
         const MpmPlaneDev &pl = A.planes[k];
         const float fy_node = (float)iy;
         if (fy_node < pl.fulb - A.pmargin) continue;
-        float d = pl.n[0] * ((float)ix - pl.fux[0]) + pl.n[1] * (fy_node - pl.fux[1]);
+        float d = pl.fn[0] * ((float)ix - pl.fux[0]) + pl.fn[1] * (fy_node - pl.fux[1]);
         if (fabsf(d) < A.pmargin || fabsf(fy_node - pl.fulb) < A.pmargin) {
           if ((double)iy < pl.ulb) continue;
           const double dd = pl.n[0] * ((double)ix - pl.ux[0]) + pl.n[1] * ((double)iy - pl.ux[1]);
@@ -473,10 +506,10 @@ __global__ void __launch_bounds__(THREADS) kx_grid_update(MixedArgs A, float4 *v
         if (d > 0.0f) continue;
         if (!pl.sticking) {
           const float vx = (acc.x + dpx) / m, vy = (acc.y + dpy) / m;
-          const float vn = (float)pl.n[0] * vx + (float)pl.n[1] * vy;
+          const float vn = pl.fn[0] * vx + pl.fn[1] * vy;
           if (vn > 0.0f) continue;
-          dpx -= m * vn * (float)pl.n[0];
-          dpy -= m * vn * (float)pl.n[1];
+          dpx -= m * vn * pl.fn[0];
+          dpy -= m * vn * pl.fn[1];
         } else {
           dpx = -acc.x;
           dpy = -acc.y;
@@ -616,11 +649,7 @@ MixedParticles parts(hg_mpm *m, int which) {
   return P;
 }
 
-size_t fused_smem_bytes() {
-  return sizeof(float4) * VA_W * VA_W + sizeof(float4) * ACC_W * ACC_W +
-         sizeof(PRec) * PASS + sizeof(float) * ACC_W * ACC_W + sizeof(int) * PASS * 2 +
-         sizeof(int) * NCELL * 2;
-}
+size_t fused_smem_bytes() { return 0; } // static shared memory only
 
 MixedArgs make_args(hg_mpm *m, double dt, bool tiles) {
   MixedArgs A;
@@ -665,7 +694,7 @@ hg_status rebin(hg_mpm *m) {
   HG_CUDA_TRY(cudaMemsetAsync(m->counts.p, 0, sizeof(int32_t) * (nkeys + 1), s));
   HG_CUDA_TRY(cudaMemsetAsync(m->cursor.p, 0, sizeof(int32_t) * nkeys, s));
   HG_CUDA_TRY(cudaMemsetAsync(m->nactive.p, 0, sizeof(int32_t) * 2, s));
-  HG_CUDA_TRY(cudaMemsetAsync(m->outside.p, 0, sizeof(uint32_t), s));
+  HG_CUDA_TRY(cudaMemsetAsync(m->outside.p, 0, 2 * sizeof(uint32_t), s));
   if (m->n > 0) {
     HG_LAUNCH(kx_keys, blocks_for(m->n, 256), 256, 0, s, m->n, m->p.nx, m->p.ny, m->ntx,
               m->mu_[m->cur].p, m->keys.p, m->counts.p, m->status.p);
@@ -688,7 +717,7 @@ hg_status rebin(hg_mpm *m) {
   return HG_OK;
 }
 
-int fused_blocks(hg_mpm *m) { return m->ctx->num_sms * 3; }
+int fused_blocks(hg_mpm *m) { return m->ctx->num_sms * 2; }
 int update_blocks(hg_mpm *m) { return m->ctx->num_sms * 8; }
 
 hg_status prime(hg_mpm *m) {
@@ -728,7 +757,7 @@ hg_status mixed_alloc(hg_mpm *m) {
       (st = m->cursor.alloc(nkeys)) || (st = m->scan_tmp.alloc(scan_tmp_size(nkeys + 1))) ||
       (st = m->active_bins.alloc((int64_t)m->ntx * m->nty)) ||
       (st = m->active_tiles.alloc((int64_t)m->ntx * m->nty)) ||
-      (st = m->nactive.alloc(2)) || (st = m->outside.alloc(1)))
+      (st = m->nactive.alloc(2)) || (st = m->outside.alloc(2)))
     return st;
   cudaStream_t s = m->ctx->stream;
   HG_CUDA_TRY(cudaMemsetAsync(m->acc4.p, 0, sizeof(float4) * nn, s));
@@ -736,12 +765,9 @@ hg_status mixed_alloc(hg_mpm *m) {
   HG_CUDA_TRY(cudaMemsetAsync(m->va.p, 0, sizeof(float4) * nn, s));
   HG_CUDA_TRY(cudaMemsetAsync(m->gm.p, 0, sizeof(float) * nn, s));
   HG_CUDA_TRY(cudaMemsetAsync(m->nactive.p, 0, sizeof(int32_t) * 2, s));
-  HG_CUDA_TRY(cudaMallocHost(&m->h_outside, sizeof(uint32_t)));
+  HG_CUDA_TRY(cudaMallocHost(&m->h_outside, 2 * sizeof(uint32_t)));
+  m->h_outside[0] = m->h_outside[1] = 0;
   HG_CUDA_TRY(cudaEventCreateWithFlags(&m->outside_ev, cudaEventDisableTiming));
-  HG_CUDA_TRY(cudaFuncSetAttribute(kx_g2p2g<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)fused_smem_bytes()));
-  HG_CUDA_TRY(cudaFuncSetAttribute(kx_g2p2g<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)fused_smem_bytes()));
   return HG_OK;
 }
 
@@ -806,7 +832,7 @@ hg_status mixed_step(hg_mpm *m, double dt, int nsteps) {
     bool need = m->steps_since_rebin >= MAX_STEPS_BETWEEN_REBINS;
     if (!need && m->outside_pending && cudaEventQuery(m->outside_ev) == cudaSuccess) {
       m->outside_pending = false;
-      need = *m->h_outside > 0;
+      need = m->h_outside[0] > 0 || (int64_t)m->h_outside[1] * 32 > m->n;
     }
     if (need) {
       hg_status st = rebin(m);
@@ -833,7 +859,7 @@ hg_status mixed_step(hg_mpm *m, double dt, int nsteps) {
     if (m->profile) HG_CUDA_TRY(cudaEventRecord(ev[2], s));
     m->steps_since_rebin++;
     if (!m->outside_pending) {
-      HG_CUDA_TRY(cudaMemcpyAsync(m->h_outside, m->outside.p, sizeof(uint32_t),
+      HG_CUDA_TRY(cudaMemcpyAsync(m->h_outside, m->outside.p, 2 * sizeof(uint32_t),
                                   cudaMemcpyDeviceToHost, s));
       HG_CUDA_TRY(cudaEventRecord(m->outside_ev, s));
       m->outside_pending = true;

@@ -44,7 +44,7 @@ def test_candidate_pairs_bit_exact(ctx):
 def column_scene(n=600, per_row=30, fall=True):
     sc = scenes.dem_column(n=n, per_row=per_row)
     if fall:
-        sc["v"][:, 1] = -0.5
+        sc["v"][:, 1] = -2.0  # rows close their 0.2 mm gaps within the run
     return sc
 
 
@@ -53,7 +53,8 @@ def test_dem_step_bit_exact(ctx, weighted):
     sc = column_scene()
     p = scenes.dem_params()
     fixed = np.zeros(len(sc["r"]), dtype=np.uint8)
-    fixed[: 30] = 1  # a kinematic bottom row
+    fixed[: 30] = 1  # a kinematic bottom row, at rest (fixed bodies keep their velocity)
+    sc["v"][: 30] = 0.0
     # the left wall touches part of the first column of disks
     planes = [((0.15e-3, 0.0), (1.0, 0.0)), ((0.0, 0.0), (0.0, 1.0))]
     g, c = build_pair(ctx, sc, p, planes, fixed=fixed)

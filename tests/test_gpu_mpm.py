@@ -175,8 +175,8 @@ def test_mixed_fast_particles_resort(ctx):
     g.flow(dt, 40)
     c.step(dt, 40)
     P, Q = g.download(), c.particles()
-    # FP32 displacements of 0.2 cells per step over 40 steps
-    assert np.abs(P["q"] - Q["q"]).max() <= 5e-9
+    # FP32 velocities integrated over 40 steps of 0.2 cells each
+    assert np.abs(P["q"] - Q["q"]).max() <= 2e-8
     assert g.rebin_count() >= 2
     assert g.status() == 0
 
