@@ -19,12 +19,14 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libhg_gpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-# (source, exact-FP64 translation unit)
+# (source, exact-FP64 translation unit). The mixed-precision unit is built
+# with fast FP32 division and square root: its FP32 results are checked
+# against the FP64 oracle with a stated tolerance, not bit for bit.
 SOURCES = [
     ("capi.cu", True),
     ("scan.cu", False),
     ("mpm_fp64.cu", True),
-    ("mpm_mixed.cu", False),
+    ("mpm_mixed.cu", None),
     ("dem.cu", True),
     ("coupling.cu", True),
 ]
@@ -45,6 +47,8 @@ def _compile(src, exact, verbose):
            "-I", INCLUDE, "-I", CSRC, "-c", os.path.join(CSRC, src), "-o", obj]
     if exact:
         cmd.insert(1, "--fmad=false")
+    elif exact is None:
+        cmd.insert(1, "--use_fast_math")
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)

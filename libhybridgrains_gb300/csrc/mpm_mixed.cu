@@ -75,22 +75,26 @@ struct MixedArgs {
 // integer operations on the FP64 bit pattern (the FP64 pipe is ~1/64 of the
 // FP32 rate on this part). Valid for 0 <= u < 2^23; other values take the
 // FP64 path.
+// Rare cases (u < 1, negative, huge or non-finite) are kept out of line so
+// that the common path does not carry predicated FP64 instructions.
+__device__ __noinline__ void split_u_slow(double u, int &c, float &f) {
+  const double fl = floor(u);
+  c = (int)fl;
+  f = __double2float_rz(u - fl);
+}
+
 __device__ __forceinline__ void split_u(double u, int &c, float &f) {
-  const long long b = __double_as_longlong(u);
-  const int e = (int)((b >> 52) & 0x7FF) - 1023;
+  // 32-bit word operations only: hi = sign | exponent | mantissa[51:32]
+  const unsigned hi = (unsigned)__double2hiint(u), lo = (unsigned)__double2loint(u);
+  const int e = (int)(hi >> 20) - 1023; // sign bit set gives e >= 1025
   if (e >= 0 && e < 23) {
-    const long long mant = (b & 0xFFFFFFFFFFFFFLL) | 0x10000000000000LL;
-    const int sh = 52 - e;
-    c = (int)(mant >> sh);
-    const long long fr = mant & ((1LL << sh) - 1);
-    f = (float)(int)(fr >> (sh - 24)) * (1.0f / 16777216.0f);
-  } else if (b >= 0 && e < 0) { // 0 <= u < 1
-    c = 0;
-    f = __double2float_rz(u);
+    const unsigned hf = (hi & 0xFFFFFu) | 0x100000u; // 21 leading mantissa bits
+    const int sh = 52 - e;                            // 30..52
+    c = sh >= 32 ? (int)(hf >> (sh - 32)) : (int)__funnelshift_r(lo, hf, sh);
+    const unsigned f24 = __funnelshift_r(lo, hf, sh - 24) & 0xFFFFFFu;
+    f = (float)f24 * (1.0f / 16777216.0f);
   } else {
-    const double fl = floor(u);
-    c = (int)fl;
-    f = __double2float_rz(u - fl);
+    split_u_slow(u, c, f);
   }
 }
 
@@ -211,19 +215,20 @@ __device__ __forceinline__ void p2g_corners(const PRec &r, float *a) {
 // Exact float -> double widening with integer operations (keeps the FP64 pipe
 // free). Zero and subnormal inputs give 0; they are below the resolution of
 // any position they are added to.
+__device__ __noinline__ double widen_slow(float f) { return (double)f; }
+
 __device__ __forceinline__ double widen(float f) {
   const unsigned b = __float_as_uint(f);
   const unsigned e = (b >> 23) & 0xFFu;
   if (e == 0u) return 0.0;
-  if (e == 0xFFu) return (double)f;
-  const unsigned long long bits = ((unsigned long long)(b >> 31) << 63) |
-                                  ((unsigned long long)(e + 896u) << 52) |
-                                  ((unsigned long long)(b & 0x7FFFFFu) << 29);
-  return __longlong_as_double((long long)bits);
+  if (e == 0xFFu) return widen_slow(f);
+  const unsigned m = b & 0x7FFFFFu;
+  const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | (m >> 3);
+  return __hiloint2double((int)hi, (int)(m << 29));
 }
 
 __device__ __forceinline__ bool finite_d(double x) {
-  return ((__double_as_longlong(x) >> 52) & 0x7FF) != 0x7FF;
+  return ((unsigned)__double2hiint(x) & 0x7FF00000u) != 0x7FF00000u;
 }
 
 // Cell-major fused kernel. A CTA owns one tile of BIN x BIN cells at a time
@@ -235,7 +240,7 @@ __device__ __forceinline__ bool finite_d(double x) {
 // per node through shared memory and flushed with one global atomic per node
 // and field.
 template <bool PRIME>
-__global__ void __launch_bounds__(THREADS, 2) kx_g2p2g(MixedArgs A) {
+__global__ void __launch_bounds__(THREADS, 3) kx_g2p2g(MixedArgs A) {
   static_assert(THREADS == BIN_CELLS, "one thread per cell of a tile");
   __shared__ float4 s_va[VA_W * VA_W];
   __shared__ float s_slow[5][ACC_W * ACC_W];
@@ -717,7 +722,7 @@ hg_status rebin(hg_mpm *m) {
   return HG_OK;
 }
 
-int fused_blocks(hg_mpm *m) { return m->ctx->num_sms * 2; }
+int fused_blocks(hg_mpm *m) { return m->ctx->num_sms * 3; }
 int update_blocks(hg_mpm *m) { return m->ctx->num_sms * 8; }
 
 hg_status prime(hg_mpm *m) {
