@@ -232,6 +232,27 @@ hg_status hg_dem_candidate_pairs(hg_context *ctx, int64_t n,
                                  const double *aabb_min, const double *aabb_max,
                                  int64_t cap, int32_t *pairs, int64_t *count);
 
+/* Allocation-free variant of hg_dem_candidate_pairs. No counterpart in the
+ * reference. For callers that cannot allocate device memory on the calling
+ * path: cudaMalloc synchronises the device and may be forbidden by a
+ * host application that sets a fixed device-memory budget at start-up, and
+ * some callers run the broadphase from a loop whose timing must not include
+ * allocation. All device temporaries live in one fixed array inside the
+ * library (about 3.4 MB, held by every GPU that loads the library until the
+ * process exits), so the call takes at most HG_STATIC_PAIRS_MAX_BOXES boxes
+ * and returns at most HG_STATIC_PAIRS_MAX_PAIRS pairs; larger inputs are
+ * rejected with HG_ERR_CAPACITY. It allocates nothing: no cudaMalloc, no
+ * cudaFree. The first call on each device looks up the array's device
+ * address; make that first call before any stream capture. Calls share the
+ * array: calls that overlap on the GPU (from several threads or contexts on
+ * one device) race, so serialise them. Same inputs, outputs and results as
+ * hg_dem_candidate_pairs. */
+enum { HG_STATIC_PAIRS_MAX_BOXES = 16384, HG_STATIC_PAIRS_MAX_PAIRS = 262144 };
+hg_status hg_dem_candidate_pairs_static(hg_context *ctx, int64_t n,
+                                        const double *aabb_min,
+                                        const double *aabb_max, int64_t cap,
+                                        int32_t *pairs, int64_t *count);
+
 /* ---- hybrid node-node coupling (hybridgrains2dnew) ------------------------ */
 
 enum {

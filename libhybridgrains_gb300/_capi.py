@@ -11,6 +11,8 @@ LIB_PATH = os.path.join(HERE, "_build", "libhg_gpu.so")
 
 HG_MAX_PLANES = 8
 HG_DEM_RECORD_WIDTH = 22
+HG_STATIC_PAIRS_MAX_BOXES = 16384
+HG_STATIC_PAIRS_MAX_PAIRS = 262144
 
 STATUS = {0: "HG_OK", 1: "HG_ERR_INVALID_ARGUMENT", 2: "HG_ERR_CUDA", 3: "HG_ERR_OUT_OF_MEMORY",
           4: "HG_ERR_CAPACITY", 5: "HG_ERR_UNSUPPORTED", 6: "HG_ERR_DEVICE_STATUS"}
@@ -100,6 +102,7 @@ SIGNATURES = {
     "hg_dem_download_contacts": [_P, _i64, _D, _I64],
     "hg_dem_status": [_P, _U32],
     "hg_dem_candidate_pairs": [_P, _i64, _D, _D, _i64, _I32, _I64],
+    "hg_dem_candidate_pairs_static": [_P, _i64, _D, _D, _i64, _I32, _I64],
     "hg_hybrid_create": [_P, _P, _P, _PP],
     "hg_hybrid_destroy": [_P],
     "hg_hybrid_step": [_P, _dbl, _i32, _i32],

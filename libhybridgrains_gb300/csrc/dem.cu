@@ -31,6 +31,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
+#include <string>
 #include <vector>
 
 namespace hg {
@@ -770,3 +772,154 @@ hg_status dem_candidate_pairs(hg_context *ctx, int64_t n, const double *mn, cons
 }
 
 } // namespace hg
+
+// ---- allocation-free candidate-pair search -------------------------------------
+//
+// The same broadphase as hg_dem_candidate_pairs, with every device temporary
+// placed in one file-scope __device__ array instead of cudaMalloc'd buffers.
+
+namespace hg {
+namespace {
+
+constexpr int64_t SP_MAX_BOXES = HG_STATIC_PAIRS_MAX_BOXES;
+constexpr int64_t SP_MAX_PAIRS = HG_STATIC_PAIRS_MAX_PAIRS;
+constexpr uint32_t SP_TABLE_BITS = 15; // 32768 buckets >= 2 * SP_MAX_BOXES
+constexpr int64_t SP_TABLE = (int64_t)1 << SP_TABLE_BITS;
+static_assert(SP_TABLE >= 2 * SP_MAX_BOXES, "hash table too small");
+
+constexpr size_t sp_align(size_t b) { return (b + 255) & ~(size_t)255; }
+// Byte offsets of the regions inside the scratch array.
+constexpr size_t SP_MN = 0;
+constexpr size_t SP_MX = SP_MN + sp_align(sizeof(double) * 2 * SP_MAX_BOXES);
+constexpr size_t SP_HOME = SP_MX + sp_align(sizeof(double) * 2 * SP_MAX_BOXES);
+constexpr size_t SP_BCOUNT = SP_HOME + sp_align(sizeof(int2) * SP_MAX_BOXES);
+constexpr size_t SP_BSTART = SP_BCOUNT + sp_align(sizeof(int32_t) * SP_TABLE);
+constexpr size_t SP_BCURSOR = SP_BSTART + sp_align(sizeof(int32_t) * SP_TABLE);
+constexpr size_t SP_ITEMS = SP_BCURSOR + sp_align(sizeof(int32_t) * SP_TABLE);
+constexpr size_t SP_CNT = SP_ITEMS + sp_align(sizeof(int32_t) * SP_MAX_BOXES);
+constexpr size_t SP_OFF = SP_CNT + sp_align(sizeof(int32_t) * (SP_MAX_BOXES + 1));
+constexpr size_t SP_TMP = SP_OFF + sp_align(sizeof(int32_t) * (SP_MAX_BOXES + 1));
+constexpr size_t SP_TMP_INTS = 256; // >= scan_tmp_size(max(SP_TABLE, SP_MAX_BOXES + 1))
+constexpr size_t SP_PAIRS = SP_TMP + sp_align(sizeof(int32_t) * SP_TMP_INTS);
+constexpr size_t SP_STATUS = SP_PAIRS + sp_align(sizeof(int32_t) * 2 * SP_MAX_PAIRS);
+constexpr size_t SP_BYTES = SP_STATUS + 256;
+
+} // namespace
+} // namespace hg
+
+// Every GPU that loads the library holds this array (about 3.4 MB) until the
+// process exits. Host code must not pass its name to a kernel: on the host
+// the name is a stand-in, not a device address; the device address comes from
+// cudaGetSymbolAddress below.
+static __device__ __align__(256) unsigned char g_pairs_scratch[hg::SP_BYTES];
+
+namespace hg {
+namespace {
+
+std::mutex g_sp_mutex;
+unsigned char *g_sp_ptr[256] = {};
+
+// Device address of g_pairs_scratch on the current device, looked up once per
+// device (the lookup initialises the module on that device).
+hg_status static_scratch(int device, unsigned char **out) {
+  if (device < 0 || device >= 256) return fail(HG_ERR_INVALID_ARGUMENT, "device index out of range");
+  std::lock_guard<std::mutex> lock(g_sp_mutex);
+  if (!g_sp_ptr[device]) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_pairs_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_pairs_scratch)");
+    g_sp_ptr[device] = static_cast<unsigned char *>(p);
+  }
+  *out = g_sp_ptr[device];
+  return HG_OK;
+}
+
+} // namespace
+} // namespace hg
+
+extern "C" hg_status hg_dem_candidate_pairs_static(hg_context *ctx, int64_t n,
+                                                   const double *aabb_min,
+                                                   const double *aabb_max, int64_t cap,
+                                                   int32_t *pairs, int64_t *count) {
+  using namespace hg;
+  if (!ctx || !count || n < 0 || (n > 0 && (!aabb_min || !aabb_max)) || (cap > 0 && !pairs) ||
+      cap < 0)
+    return fail(HG_ERR_INVALID_ARGUMENT, "bad argument");
+  if (n > SP_MAX_BOXES)
+    return fail(HG_ERR_CAPACITY, "hg_dem_candidate_pairs_static takes at most " +
+                                     std::to_string(SP_MAX_BOXES) + " boxes, got " +
+                                     std::to_string(n));
+  *count = 0;
+  double H = 0.0, amax = 0.0;
+  for (int64_t i = 0; i < 2 * n; ++i) {
+    if (!std::isfinite(aabb_min[i]) || !std::isfinite(aabb_max[i]) || !(aabb_min[i] < aabb_max[i]))
+      return fail(HG_ERR_INVALID_ARGUMENT, "boxes must be finite with min < max");
+    H = std::max(H, aabb_max[i] - aabb_min[i]);
+    amax = std::max(amax, std::max(std::fabs(aabb_min[i]), std::fabs(aabb_max[i])));
+  }
+  if (n == 0) return HG_OK;
+  H = H * (1.0 + 1.0e-6);
+  if (amax / H > 1.0e9) return fail(HG_ERR_INVALID_ARGUMENT, "boxes too small for their coordinates");
+  int prev = -1;
+  cudaGetDevice(&prev);
+  if (prev != ctx->device) cudaSetDevice(ctx->device);
+  struct Restore {
+    int dev;
+    ~Restore() {
+      if (dev >= 0) cudaSetDevice(dev);
+    }
+  } restore{prev != ctx->device ? prev : -1};
+  unsigned char *base = nullptr;
+  hg_status st = static_scratch(ctx->device, &base);
+  if (st != HG_OK) return st;
+  cudaStream_t s = ctx->stream;
+  double *dmn = reinterpret_cast<double *>(base + SP_MN);
+  double *dmx = reinterpret_cast<double *>(base + SP_MX);
+  int2 *home = reinterpret_cast<int2 *>(base + SP_HOME);
+  int32_t *bcount = reinterpret_cast<int32_t *>(base + SP_BCOUNT);
+  int32_t *bstart = reinterpret_cast<int32_t *>(base + SP_BSTART);
+  int32_t *bcursor = reinterpret_cast<int32_t *>(base + SP_BCURSOR);
+  int32_t *items = reinterpret_cast<int32_t *>(base + SP_ITEMS);
+  int32_t *cnt = reinterpret_cast<int32_t *>(base + SP_CNT);
+  int32_t *off = reinterpret_cast<int32_t *>(base + SP_OFF);
+  int32_t *tmp = reinterpret_cast<int32_t *>(base + SP_TMP);
+  int32_t *dpairs = reinterpret_cast<int32_t *>(base + SP_PAIRS);
+  uint32_t *status = reinterpret_cast<uint32_t *>(base + SP_STATUS);
+  // Inputs in, counters cleared: the array keeps the previous call's contents.
+  HG_CUDA_TRY(cudaMemcpyAsync(dmn, aabb_min, sizeof(double) * 2 * n, cudaMemcpyHostToDevice, s));
+  HG_CUDA_TRY(cudaMemcpyAsync(dmx, aabb_max, sizeof(double) * 2 * n, cudaMemcpyHostToDevice, s));
+  HG_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(uint32_t), s));
+  HG_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (n + 1), s));
+  const uint32_t bits = std::min<uint32_t>(table_bits(n), SP_TABLE_BITS);
+  BroadArgs B;
+  B.n = n;
+  B.H = H;
+  B.mask = (1u << bits) - 1u;
+  B.mn = dmn;
+  B.mx = dmx;
+  if ((st = build_buckets(s, B, bcount, bstart, bcursor, items, home, tmp))) return st;
+  HG_LAUNCH(kd_box_pairs<false>, blocks_for(n, 128), 128, 0, s, B, home, bstart, bcount, items,
+            cnt, off, nullptr, 0, status);
+  HG_CHECK_LAUNCH();
+  if ((st = exclusive_scan_i32(cnt, off, n + 1, tmp, s))) return st;
+  int32_t total = 0;
+  uint32_t word = 0;
+  HG_CUDA_TRY(cudaMemcpyAsync(&total, off + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  HG_CUDA_TRY(cudaMemcpyAsync(&word, status, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  HG_CUDA_TRY(cudaStreamSynchronize(s));
+  if (word & HG_STATUS_CELL_OVERFLOW)
+    return fail(HG_ERR_CAPACITY, "more than 32 overlapping boxes for one box");
+  if (total > SP_MAX_PAIRS)
+    return fail(HG_ERR_CAPACITY, "hg_dem_candidate_pairs_static holds at most " +
+                                     std::to_string(SP_MAX_PAIRS) + " pairs, found " +
+                                     std::to_string(total));
+  HG_LAUNCH(kd_box_pairs<true>, blocks_for(n, 128), 128, 0, s, B, home, bstart, bcount, items,
+            cnt, off, dpairs, (int64_t)total, status);
+  HG_CHECK_LAUNCH();
+  const int64_t k = std::min<int64_t>(total, cap);
+  if (k > 0)
+    HG_CUDA_TRY(cudaMemcpyAsync(pairs, dpairs, sizeof(int32_t) * 2 * k, cudaMemcpyDeviceToHost, s));
+  HG_CUDA_TRY(cudaStreamSynchronize(s));
+  *count = total;
+  return HG_OK;
+}
