@@ -36,13 +36,17 @@ sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s mixed vs FP64 GPU at stated error; batched p50/p99 latency"
 UNIT = "particle-steps/s"
-# Algorithmic bytes of the fused G2P/P2G kernel: each persistent particle
-# field read once (u 16 + v 8 + m,V 8 + strain 16 + flags 1 = 49 B) and the
-# updated ones written once (u 16 + v 8 + strain 16 + flags 1 = 41 B); per
-# active node the grid velocity/acceleration read (16 B) and the accumulated
-# mass/momentum/force written (20 B).
-BYTES_PER_PARTICLE = 90
-BYTES_PER_ACTIVE_NODE = 36
+# Algorithmic bytes of one fused G2P/P2G launch, with the per-unit figures of
+# the reference algorithm's two particle passes: P2G reads 48 B per point
+# (position 16, velocity 8, mass 4, volume 4, J 4, be_bar 12) and writes 20 B
+# per active node (mass, momentum, force); G2P reads 40 B and writes 40 B per
+# point and reads 16 B per active node (velocity, acceleration). The fused
+# kernel reads each point once, so it moves fewer bytes than this
+# (FUSED_MIN_* below, and the ncu DRAM traffic in profiles/).
+BYTES_PER_PARTICLE = 48 + 80
+BYTES_PER_ACTIVE_NODE = 20 + 16
+FUSED_MIN_BYTES_PER_PARTICLE = 90  # u 16+16, v 8+8, (m, V) 8, strain 16+16, flags 1+1
+FUSED_MIN_BYTES_PER_ACTIVE_NODE = 36
 
 
 def dist_env():
@@ -319,6 +323,8 @@ def run_ours(args, rank, world, local):
         "roofline": {"bound": "hbm", "kernel": "kx_g2p2g", "achieved": achieved, "peak": peak,
                      "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "algorithmic_bytes": alg_bytes,
+                     "fused_min_bytes": n * FUSED_MIN_BYTES_PER_PARTICLE
+                                        + n_active * FUSED_MIN_BYTES_PER_ACTIVE_NODE,
                      "kernel_ms": per_launch_s * 1e3,
                      "grid_update_ms": update_ms / max(prof_steps, 1)},
         "cpu_baseline": cpu,

@@ -260,7 +260,7 @@ __global__ void __launch_bounds__(THREADS, 3) kx_g2p2g(MixedArgs A) {
         const int ix = X0 - DRIFT + k % VA_W, iy = Y0 - DRIFT + k / VA_W;
         float4 val = make_float4(0.f, 0.f, 0.f, 0.f);
         if (ix >= 0 && iy >= 0 && ix <= A.nx && iy <= A.ny)
-          val = A.va[(int64_t)iy * row + ix];
+          val = A.va[iy * row + ix]; // MIXED grids have < 2^30 nodes
         s_va[k] = val;
       }
     }
@@ -336,7 +336,7 @@ __global__ void __launch_bounds__(THREADS, 3) kx_g2p2g(MixedArgs A) {
           n01 = s_va[k0 + VA_W];
           n11 = s_va[k0 + VA_W + 1];
         } else {
-          const int64_t k0 = (int64_t)cy * row + cx;
+          const int k0 = cy * row + cx;
           n00 = A.va[k0];
           n10 = A.va[k0 + 1];
           n01 = A.va[k0 + row];
@@ -472,7 +472,7 @@ __global__ void __launch_bounds__(THREADS, 3) kx_g2p2g(MixedArgs A) {
         continue;
       const int ix = WX + i, iy = WY + j;
       if (ix < 0 || iy < 0 || ix > A.nx || iy > A.ny) continue;
-      const int64_t node = (int64_t)iy * row + ix;
+      const int node = iy * row + ix;
       atomicAdd(&A.accm[node], sum[0]);
       atomicAdd(&A.acc4[node], make_float4(sum[1], sum[2], sum[3], sum[4]));
     }
@@ -490,7 +490,7 @@ __global__ void __launch_bounds__(THREADS) kx_grid_update(MixedArgs A, float4 *v
     const int tile = A.active[t];
     const int ix = (tile % A.ntx) * BIN + lx, iy = (tile / A.ntx) * BIN + ly;
     if (ix > A.nx || iy > A.ny) continue;
-    const int64_t i = (int64_t)iy * row + ix;
+    const int i = iy * row + ix;
     const float m = A.accm[i];
     const float4 acc = A.acc4[i];
     float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
