@@ -296,11 +296,14 @@ def run_ours(args, rank, world, local):
     alg_bytes = n * BYTES_PER_PARTICLE + n_active * BYTES_PER_ACTIVE_NODE
     per_launch_s = (g2p2g_ms * 1e-3) / max(prof_steps, 1)
     achieved = alg_bytes / per_launch_s / 1e9
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "kx_g2p2g_column_2M.traffic")
+    traffic = None  # DRAM bytes per launch from the committed ncu summary
+    tpath = os.path.join(ROOT, "profiles", "kx_g2p2g_column_2M.md")
     if os.path.exists(tpath):
+        import re
         with open(tpath) as f:
-            traffic = float(f.read().split()[0])
+            mt = re.search(r"traffic_bytes_per_launch = (\d+)", f.read())
+        if mt:
+            traffic = int(mt.group(1))
 
     cpu = None
     if world == 1 and args.cpu_steps > 0:
