@@ -176,6 +176,25 @@ hg_status hg_mpm_profile(hg_mpm *m, int32_t enable);
 hg_status hg_mpm_profile_read(hg_mpm *m, double *g2p2g_ms,
                               double *grid_update_ms, int64_t *steps);
 
+/* ---- batches of independent MIXED MPM scenes -------------------------------
+ * No counterpart in the reference (it steps one scene per process). A batch
+ * steps every member scene with one grid-update launch and one fused G2P/P2G
+ * launch whose CTAs drain (scene, tile) work items, so many small scenes share
+ * the GPU the way one large scene does. Members are MIXED MPM objects of the
+ * batch's context; each keeps its own state, dt and parameters, and stepping
+ * a member alone or in a batch gives the same result up to the order of FP32
+ * atomic additions. Members may join and leave between steps; remove a
+ * member before destroying it, and destroy a batch before its context. */
+typedef struct hg_batch hg_batch;
+enum { HG_MAX_BATCH = 1024 };
+hg_status hg_batch_create(hg_context *ctx, int32_t max_members, hg_batch **out);
+hg_status hg_batch_destroy(hg_batch *b);
+hg_status hg_batch_add(hg_batch *b, hg_mpm *m, double dt);
+hg_status hg_batch_remove(hg_batch *b, hg_mpm *m);
+hg_status hg_batch_size(hg_batch *b, int32_t *n);
+/* nsteps steps of every member (ExplicitIntegrator::flow per member). */
+hg_status hg_batch_step(hg_batch *b, int32_t nsteps);
+
 /* ---- DEM (rigidbody2d, penalty map) --------------------------------------- */
 
 /* RigidBody2DStaticPlane, static (v = 0, omega = 0). */

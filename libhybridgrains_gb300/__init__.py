@@ -360,3 +360,44 @@ class Hybrid:
         return dict(packed_dem=pg[: ng.value], packed_mpm=pn[: nn_.value], dem_mass_grid=dm,
                     dem_mom_grid=dp, v_after=va, at_after=aa, homog_factor=hf, homog_stress=hs,
                     homog_velocity=hv)
+
+
+class Batch:
+    """Independent MIXED MPM scenes stepped together: one grid-update and one
+    fused G2P/P2G launch per step for all members (no counterpart in the
+    reference, which runs one scene per process)."""
+
+    def __init__(self, ctx, max_members=64):
+        self.ctx = ctx
+        h = ctypes.c_void_p()
+        check("hg_batch_create", ctx._h, int(max_members), ctypes.byref(h))
+        self._h = h
+        self._members = {}
+
+    def add(self, mpm, dt):
+        check("hg_batch_add", self._h, mpm._h, float(dt))
+        self._members[id(mpm)] = mpm
+
+    def remove(self, mpm):
+        check("hg_batch_remove", self._h, mpm._h)
+        self._members.pop(id(mpm), None)
+
+    def __len__(self):
+        n = ctypes.c_int32()
+        check("hg_batch_size", self._h, ctypes.byref(n))
+        return n.value
+
+    def step(self, nsteps=1):
+        check("hg_batch_step", self._h, int(nsteps))
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _capi.load().hg_batch_destroy(self._h)
+            self._h = None
+        self._members = {}
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

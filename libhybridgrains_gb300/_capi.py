@@ -13,6 +13,7 @@ HG_MAX_PLANES = 8
 HG_DEM_RECORD_WIDTH = 22
 HG_STATIC_PAIRS_MAX_BOXES = 16384
 HG_STATIC_PAIRS_MAX_PAIRS = 262144
+HG_MAX_BATCH = 1024
 
 STATUS = {0: "HG_OK", 1: "HG_ERR_INVALID_ARGUMENT", 2: "HG_ERR_CUDA", 3: "HG_ERR_OUT_OF_MEMORY",
           4: "HG_ERR_CAPACITY", 5: "HG_ERR_UNSUPPORTED", 6: "HG_ERR_DEVICE_STATUS"}
@@ -91,6 +92,12 @@ SIGNATURES = {
     "hg_mpm_rebin_count": [_P, _I64],
     "hg_mpm_profile": [_P, _i32],
     "hg_mpm_profile_read": [_P, _D, _D, _I64],
+    "hg_batch_create": [_P, _i32, _PP],
+    "hg_batch_destroy": [_P],
+    "hg_batch_add": [_P, _P, _dbl],
+    "hg_batch_remove": [_P, _P],
+    "hg_batch_size": [_P, _I32],
+    "hg_batch_step": [_P, _i32],
     "hg_dem_create": [_P, ctypes.POINTER(DemDesc), _PP],
     "hg_dem_destroy": [_P],
     "hg_dem_upload": [_P, _i64, _D, _D, _D, _D, _D, _U8],

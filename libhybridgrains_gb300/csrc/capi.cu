@@ -658,6 +658,82 @@ hg_status hg_mpm_rebin_count(hg_mpm *m, int64_t *count) {
   return HG_OK;
 }
 
+// ---- batches ------------------------------------------------------------------------
+
+hg_status hg_batch_create(hg_context *ctx, int32_t max_members, hg_batch **out) {
+  if (!ctx || !out) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  *out = nullptr;
+  if (max_members < 1 || max_members > HG_MAX_BATCH)
+    return fail(HG_ERR_INVALID_ARGUMENT, "max_members must lie in [1, HG_MAX_BATCH]");
+  DeviceGuard g(ctx->device);
+  hg_batch *b = new (std::nothrow) hg_batch();
+  if (!b) return fail(HG_ERR_OUT_OF_MEMORY, "host allocation failed");
+  b->ctx = ctx;
+  b->max_members = max_members;
+  context_retain(ctx);
+  hg_status st = batch_alloc(b);
+  if (st != HG_OK) {
+    hg_batch_destroy(b);
+    return st;
+  }
+  *out = b;
+  return HG_OK;
+}
+
+hg_status hg_batch_destroy(hg_batch *b) {
+  if (!b) return HG_OK;
+  hg_context *ctx = b->ctx;
+  {
+    DeviceGuard g(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    batch_free(b);
+    delete b;
+  }
+  context_release(ctx);
+  return HG_OK;
+}
+
+hg_status hg_batch_add(hg_batch *b, hg_mpm *m, double dt) {
+  if (!b || !m) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (m->ctx != b->ctx) return fail(HG_ERR_INVALID_ARGUMENT, "member of another context");
+  if (m->p.precision != HG_PRECISION_MIXED)
+    return fail(HG_ERR_UNSUPPORTED, "batches hold MIXED precision MPM objects");
+  if (!(dt > 0.0) || !std::isfinite(dt)) return fail(HG_ERR_INVALID_ARGUMENT, "dt must be positive");
+  for (hg_mpm *x : b->members)
+    if (x == m) return fail(HG_ERR_INVALID_ARGUMENT, "already a member");
+  if ((int)b->members.size() >= b->max_members) return fail(HG_ERR_CAPACITY, "batch is full");
+  b->members.push_back(m);
+  b->dts.push_back(dt);
+  return HG_OK;
+}
+
+hg_status hg_batch_remove(hg_batch *b, hg_mpm *m) {
+  if (!b || !m) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  for (size_t i = 0; i < b->members.size(); ++i)
+    if (b->members[i] == m) {
+      b->members.erase(b->members.begin() + i);
+      b->dts.erase(b->dts.begin() + i);
+      // its counters may still be in flight: forget the object, keep the slot
+      for (hg_mpm *&x : b->out_members)
+        if (x == m) x = nullptr;
+      return HG_OK;
+    }
+  return fail(HG_ERR_INVALID_ARGUMENT, "not a member");
+}
+
+hg_status hg_batch_size(hg_batch *b, int32_t *n) {
+  if (!b || !n) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  *n = (int32_t)b->members.size();
+  return HG_OK;
+}
+
+hg_status hg_batch_step(hg_batch *b, int32_t nsteps) {
+  if (!b) return fail(HG_ERR_INVALID_ARGUMENT, "b is NULL");
+  if (nsteps < 0) return fail(HG_ERR_INVALID_ARGUMENT, "negative step count");
+  DeviceGuard g(b->ctx->device);
+  return batch_step(b, nsteps);
+}
+
 // ---- DEM ------------------------------------------------------------------------
 
 hg_status hg_dem_create(hg_context *ctx, const hg_dem_desc *d, hg_dem **out) {

@@ -191,6 +191,29 @@ hg_status mixed_download_grid(hg_mpm *m, double *mass, double *vel,
 hg_status mixed_profile_read(hg_mpm *m, double *g2p2g_ms, double *update_ms,
                              int64_t *steps);
 
+} // namespace hg
+
+struct hg_batch {
+  hg_context *ctx = nullptr;
+  int max_members = 0;
+  std::vector<hg_mpm *> members;
+  std::vector<double> dts;
+  hg::DevBuf<unsigned char> table; // [bins | tiles] per-scene argument tables
+  unsigned char *h_table[2] = {nullptr, nullptr}; // pinned, double-buffered
+  cudaEvent_t table_ev[2] = {nullptr, nullptr};
+  int tb = 0;
+  hg::DevBuf<uint32_t> outside; // 2 counters per member
+  uint32_t *h_outside = nullptr;
+  cudaEvent_t out_ev = nullptr;
+  bool out_pending = false;
+  std::vector<hg_mpm *> out_members; // members whose counters are in flight
+};
+
+namespace hg {
+hg_status batch_alloc(hg_batch *b);
+void batch_free(hg_batch *b);
+hg_status batch_step(hg_batch *b, int nsteps);
+
 // ---- DEM ---------------------------------------------------------------------
 
 struct DemParams {

@@ -45,6 +45,7 @@ namespace hg {
 namespace {
 
 constexpr int THREADS = 256;
+constexpr int MAX_BATCH = HG_MAX_BATCH; // scenes per batched launch
 
 struct MixedArgs {
   int nx, ny, ntx, nty;
@@ -64,6 +65,7 @@ struct MixedArgs {
   float4 *strain;
   uint8_t *flags;
   const float4 *va;
+  float4 *va_out; // the same array, written by the grid update
   float4 *acc4;
   float *accm;
   float *gm;
@@ -239,20 +241,25 @@ __device__ __forceinline__ bool finite_d(double x) {
 // tile's node window (or global atomics outside it). Corner sums are combined
 // per node through shared memory and flushed with one global atomic per node
 // and field.
-template <bool PRIME>
-__global__ void __launch_bounds__(THREADS, 3) kx_g2p2g(MixedArgs A) {
-  static_assert(THREADS == BIN_CELLS, "one thread per cell of a tile");
-  __shared__ float4 s_va[VA_W * VA_W];
-  __shared__ float s_slow[5][ACC_W * ACC_W];
-  __shared__ float s_corner[20][BIN_CELLS];
-  __shared__ unsigned s_out[2]; // left the tile window / left the sorted cell
+struct FusedSmem {
+  float4 va[VA_W * VA_W];
+  float slow[5][ACC_W * ACC_W];
+  float corner[20][BIN_CELLS];
+  unsigned out[2]; // left the tile window / left the sorted cell
+};
 
+// One tile of one scene; A lives in shared memory.
+template <bool PRIME>
+__device__ __forceinline__ void fused_tile(const MixedArgs &A, const int bin, FusedSmem &S) {
+  static_assert(THREADS == BIN_CELLS, "one thread per cell of a tile");
+  float4 *s_va = S.va;
+  float(&s_slow)[5][ACC_W * ACC_W] = S.slow;
+  float(&s_corner)[20][BIN_CELLS] = S.corner;
+  unsigned *s_out = S.out;
   const int tid = threadIdx.x;
-  const int nact = *A.nactive;
   const int row = A.nx + 1;
   const int lcx = tid % BIN, lcy = tid / BIN;
-  for (int t = blockIdx.x; t < nact; t += gridDim.x) {
-    const int bin = A.active[t];
+  {
     const int X0 = (bin % A.ntx) * BIN, Y0 = (bin / A.ntx) * BIN;
     const int WX = X0 - DRIFT - 1, WY = Y0 - DRIFT - 1; // P2G window origin (node)
     if (!PRIME) {
@@ -481,15 +488,88 @@ __global__ void __launch_bounds__(THREADS, 3) kx_g2p2g(MixedArgs A) {
   }
 }
 
-// Node update over active tiles; one thread per node of a 16x16 tile.
-__global__ void __launch_bounds__(THREADS) kx_grid_update(MixedArgs A, float4 *va) {
+template <bool PRIME>
+__global__ void __launch_bounds__(THREADS, 3) kx_g2p2g(const __grid_constant__ MixedArgs A) {
+  // the arguments stay in the constant bank: operands need no registers
+  __shared__ FusedSmem S;
   const int nact = *A.nactive;
+  for (int t = blockIdx.x; t < nact; t += gridDim.x) fused_tile<PRIME>(A, A.active[t], S);
+}
+
+// Exclusive prefix of the scenes' work-item counts, in shared memory
+// (nslots <= MAX_BATCH). Item k of the launch is tile (k - prefix[s]) of
+// scene s with prefix[s] <= k < prefix[s + 1].
+__device__ __forceinline__ void batch_prefix(const MixedArgs *slots, int nslots, int *prefix) {
+  __shared__ int warp_tot[THREADS / 32];
+  constexpr int PER = (MAX_BATCH + THREADS - 1) / THREADS;
+  int v[PER];
+  int sum = 0;
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    const int s = threadIdx.x * PER + j;
+    v[j] = s < nslots ? *slots[s].nactive : 0;
+    sum += v[j];
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int x = sum;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, d);
+    if (lane >= d) x += y;
+  }
+  if (lane == 31) warp_tot[wid] = x;
+  __syncthreads();
+  int off = 0;
+  for (int w = 0; w < wid; ++w) off += warp_tot[w];
+  int run = off + x - sum;
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    const int s = threadIdx.x * PER + j;
+    if (s <= MAX_BATCH) prefix[s] = run;
+    run += v[j];
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ int batch_slot(const int *prefix, int nslots, int item) {
+  int lo = 0, hi = nslots - 1;
+  while (lo < hi) { // largest s with prefix[s] <= item
+    const int mid = (lo + hi + 1) >> 1;
+    if (prefix[mid] <= item) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// All scenes of a batch in one launch: the CTAs drain (scene, tile) items.
+__global__ void __launch_bounds__(THREADS, 3) kb_g2p2g(const MixedArgs *__restrict__ slots,
+                                                     int nslots) {
+  __shared__ FusedSmem S;
+  __shared__ MixedArgs A;
+  __shared__ int prefix[MAX_BATCH + 1];
+  batch_prefix(slots, nslots, prefix);
+  const int total = prefix[nslots];
+  int cur = -1;
+  for (int item = blockIdx.x; item < total; item += gridDim.x) {
+    const int s = batch_slot(prefix, nslots, item);
+    if (s != cur) {
+      __syncthreads();
+      if (threadIdx.x == 0) A = slots[s];
+      __syncthreads();
+      cur = s;
+    }
+    fused_tile<false>(A, A.active[item - prefix[s]], S);
+  }
+}
+
+// Node update of one tile; one thread per node of the 16x16 tile.
+__device__ __forceinline__ void update_tile(const MixedArgs &A, const int tile) {
+  float4 *va = A.va_out;
   const int row = A.nx + 1;
   const int lx = threadIdx.x % BIN, ly = threadIdx.x / BIN;
-  for (int t = blockIdx.x; t < nact; t += gridDim.x) {
-    const int tile = A.active[t];
+  {
     const int ix = (tile % A.ntx) * BIN + lx, iy = (tile / A.ntx) * BIN + ly;
-    if (ix > A.nx || iy > A.ny) continue;
+    if (ix > A.nx || iy > A.ny) return;
     const int i = iy * row + ix;
     const float m = A.accm[i];
     const float4 acc = A.acc4[i];
@@ -529,6 +609,40 @@ __global__ void __launch_bounds__(THREADS) kx_grid_update(MixedArgs A, float4 *v
     A.accm[i] = 0.f;
     A.acc4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
+}
+
+__global__ void __launch_bounds__(THREADS) kx_grid_update(const __grid_constant__ MixedArgs A) {
+  const int nact = *A.nactive;
+  for (int t = blockIdx.x; t < nact; t += gridDim.x) update_tile(A, A.active[t]);
+}
+
+__global__ void __launch_bounds__(THREADS) kb_grid_update(const MixedArgs *__restrict__ slots,
+                                                          int nslots) {
+  __shared__ MixedArgs A;
+  __shared__ int prefix[MAX_BATCH + 1];
+  batch_prefix(slots, nslots, prefix);
+  const int total = prefix[nslots];
+  int cur = -1;
+  for (int item = blockIdx.x; item < total; item += gridDim.x) {
+    const int s = batch_slot(prefix, nslots, item);
+    if (s != cur) {
+      __syncthreads();
+      if (threadIdx.x == 0) A = slots[s];
+      __syncthreads();
+      cur = s;
+    }
+    update_tile(A, A.active[item - prefix[s]]);
+  }
+}
+
+// Copies every member's out-of-window counters into one array, for a single
+// asynchronous read-back per batch step.
+__global__ void kb_gather_outside(const MixedArgs *__restrict__ slots, int nslots,
+                                  uint32_t *out) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nslots) return;
+  out[2 * s] = slots[s].outside[0];
+  out[2 * s + 1] = slots[s].outside[1];
 }
 
 // ---- re-sort -----------------------------------------------------------------
@@ -685,6 +799,7 @@ MixedArgs make_args(hg_mpm *m, double dt, bool tiles) {
   A.strain = cur.strain;
   A.flags = cur.flags;
   A.va = m->va.p;
+  A.va_out = m->va.p;
   A.acc4 = m->acc4.p;
   A.accm = m->accm.p;
   A.gm = m->gm.p;
@@ -855,7 +970,7 @@ hg_status mixed_step(hg_mpm *m, double dt, int nsteps) {
       HG_CUDA_TRY(cudaEventRecord(ev[0], s));
     }
     MixedArgs At = make_args(m, dt, true);
-    HG_LAUNCH(kx_grid_update, update_blocks(m), THREADS, 0, s, At, m->va.p);
+    HG_LAUNCH(kx_grid_update, update_blocks(m), THREADS, 0, s, At);
     HG_CHECK_LAUNCH();
     if (m->profile) HG_CUDA_TRY(cudaEventRecord(ev[1], s));
     MixedArgs Ab = make_args(m, dt, false);
@@ -868,6 +983,95 @@ hg_status mixed_step(hg_mpm *m, double dt, int nsteps) {
                                   cudaMemcpyDeviceToHost, s));
       HG_CUDA_TRY(cudaEventRecord(m->outside_ev, s));
       m->outside_pending = true;
+    }
+  }
+  return HG_OK;
+}
+
+} // namespace hg
+
+// ---- batches ---------------------------------------------------------------------
+
+namespace hg {
+
+hg_status batch_alloc(hg_batch *b) {
+  const size_t tsz = 2 * (size_t)b->max_members * sizeof(MixedArgs);
+  hg_status st;
+  if ((st = b->table.alloc(tsz)) || (st = b->outside.alloc(2 * (size_t)b->max_members)))
+    return st;
+  for (int k = 0; k < 2; ++k) {
+    HG_CUDA_TRY(cudaMallocHost(&b->h_table[k], tsz));
+    HG_CUDA_TRY(cudaEventCreateWithFlags(&b->table_ev[k], cudaEventDisableTiming));
+  }
+  HG_CUDA_TRY(cudaMallocHost(&b->h_outside, 2 * sizeof(uint32_t) * b->max_members));
+  HG_CUDA_TRY(cudaEventCreateWithFlags(&b->out_ev, cudaEventDisableTiming));
+  return HG_OK;
+}
+
+void batch_free(hg_batch *b) {
+  for (int k = 0; k < 2; ++k) {
+    if (b->h_table[k]) cudaFreeHost(b->h_table[k]);
+    if (b->table_ev[k]) cudaEventDestroy(b->table_ev[k]);
+  }
+  if (b->h_outside) cudaFreeHost(b->h_outside);
+  if (b->out_ev) cudaEventDestroy(b->out_ev);
+}
+
+hg_status batch_step(hg_batch *b, int nsteps) {
+  cudaStream_t s = b->ctx->stream;
+  const int S = (int)b->members.size();
+  if (S == 0) return HG_OK;
+  const size_t half = (size_t)b->max_members * sizeof(MixedArgs);
+  for (int k = 0; k < nsteps; ++k) {
+    // re-sort members whose points left their windows (counters read back
+    // asynchronously one step late), members due for a periodic re-sort and
+    // members not yet primed
+    if (b->out_pending && cudaEventQuery(b->out_ev) == cudaSuccess) {
+      b->out_pending = false;
+      for (size_t i = 0; i < b->out_members.size(); ++i) {
+        hg_mpm *m = b->out_members[i];
+        if (!m) continue;
+        if (b->h_outside[2 * i] > 0 || (int64_t)b->h_outside[2 * i + 1] * 32 > m->n)
+          m->steps_since_rebin = MAX_STEPS_BETWEEN_REBINS;
+      }
+    }
+    for (hg_mpm *m : b->members) {
+      hg_status st = HG_OK;
+      if (!m->primed) st = prime(m);
+      else if (m->steps_since_rebin >= MAX_STEPS_BETWEEN_REBINS) st = rebin(m);
+      if (st != HG_OK) return st;
+    }
+    // per-scene argument tables (buffer pointers change with every re-sort)
+    const int tb = b->tb;
+    b->tb = 1 - b->tb;
+    HG_CUDA_TRY(cudaEventSynchronize(b->table_ev[tb]));
+    MixedArgs *hb = reinterpret_cast<MixedArgs *>(b->h_table[tb]);
+    MixedArgs *ht = reinterpret_cast<MixedArgs *>(b->h_table[tb] + half);
+    for (int i = 0; i < S; ++i) {
+      hb[i] = make_args(b->members[i], b->dts[i], false);
+      ht[i] = make_args(b->members[i], b->dts[i], true);
+    }
+    // the device table is read by the previous step's kernels; the copy is
+    // ordered after them on the stream
+    HG_CUDA_TRY(cudaMemcpyAsync(b->table.p, b->h_table[tb], half + sizeof(MixedArgs) * S,
+                                cudaMemcpyHostToDevice, s));
+    HG_CUDA_TRY(cudaEventRecord(b->table_ev[tb], s));
+    const MixedArgs *db = reinterpret_cast<const MixedArgs *>(b->table.p);
+    const MixedArgs *dt = reinterpret_cast<const MixedArgs *>(b->table.p + half);
+    const int nsm = b->ctx->num_sms;
+    HG_LAUNCH(kb_grid_update, nsm * 8, THREADS, 0, s, dt, S);
+    HG_CHECK_LAUNCH();
+    HG_LAUNCH(kb_g2p2g, nsm * 3, THREADS, 0, s, db, S);
+    HG_CHECK_LAUNCH();
+    for (hg_mpm *m : b->members) m->steps_since_rebin++;
+    if (!b->out_pending) {
+      HG_LAUNCH(kb_gather_outside, (S + 127) / 128, 128, 0, s, db, S, b->outside.p);
+      HG_CHECK_LAUNCH();
+      HG_CUDA_TRY(cudaMemcpyAsync(b->h_outside, b->outside.p, 2 * sizeof(uint32_t) * S,
+                                  cudaMemcpyDeviceToHost, s));
+      HG_CUDA_TRY(cudaEventRecord(b->out_ev, s));
+      b->out_members = b->members;
+      b->out_pending = true;
     }
   }
   return HG_OK;

@@ -151,3 +151,19 @@ def dem_params(kn=1.0e5, mu=0.5, restitution=0.5, r_mean=1.0e-3, rho=2600.0):
     c = 2.0 * math.sqrt(0.5 * m * kn) * (-le) / math.sqrt(math.pi ** 2 + le * le)
     gn = 2.0 * c
     return dict(kn=kn, kt=2.0 / 7.0 * kn, gamman=gn, gammat=gn, mu=mu)
+
+
+def serving_column(npoints, aspect, phi_deg, h=5.0e-3):
+    """A granular-column collapse of about npoints material points (2 x 2 per
+    cell) whose height/width ratio is aspect, on a domain long enough for the
+    run-out; friction angle phi_deg. Used for mixes of many small scenes."""
+    cells = max(npoints / 4.0, 4.0)
+    wc = max(int(round(math.sqrt(cells / aspect))), 2)
+    hc = max(int(round(cells / wc)), 2)
+    nx, ny = wc + 2 * hc + 8, hc + 8
+    cfg = dict(grid_min=(0.0, 0.0), grid_max=(nx * h, ny * h), h=h,
+               rect_min=(2 * h, 0.0), rect_max=((2 + wc) * h, hc * h), dt=1.0e-5)
+    cfg.update(mpm_material(phi_deg=phi_deg))
+    cfg["planes"] = mpm_planes(cfg["grid_min"], cfg["grid_max"])
+    cfg["samples_per_dim"] = 2
+    return cfg
