@@ -287,6 +287,10 @@ def run_ours(args, rank, world, local):
                "steps": args.e2e_steps, "ms_per_step": 1e3 * e2e_s / args.e2e_steps}
         del e2
 
+    serve = None
+    if args.serve_requests > 0:
+        serve = run_serving(args, ctx)
+
     if rank != 0:
         return
     peaks = measured_peaks()
@@ -332,11 +336,66 @@ def run_ours(args, rank, world, local):
                      "grid_update_ms": update_ms / max(prof_steps, 1)},
         "cpu_baseline": cpu,
         "e2e": e2e,
+        "serving": serve,
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "status_word": status,
     }
     print(json.dumps(line), flush=True)
+
+
+def run_serving(args, ctx):
+    """Batched serving of column-collapse requests: Poisson arrivals with
+    continuous batching (latency), the same requests all queued at once
+    (saturated throughput) and served one scene at a time (baseline)."""
+    from libhybridgrains_gb300 import serving
+
+    def copies(reqs, at_once=False):
+        return [serving.Request(r.rid, 0.0 if at_once else r.arrival, r.cfg, r.npoints, r.steps,
+                                r.frame_every, r.dt) for r in reqs]
+
+    budget = int(args.serve_budget_gb * 2**30)
+    reqs = serving.column_requests(n=args.serve_requests, rate=args.serve_rate,
+                                   steps=args.serve_steps, seed=2024)
+    be = serving.DeviceBackend(ctx, max_members=min(256, args.serve_requests))
+    # warm-up: a few short requests (library load, pools)
+    serving.Server(be, budget).run(copies(serving.column_requests(n=8, rate=1e3, steps=200,
+                                                                   seed=7)))
+    launches0 = __import__("libhybridgrains_gb300").kernel_launch_count()
+    srv = serving.Server(be, budget, max_members=min(256, args.serve_requests))
+    live = srv.run(copies(reqs))
+    poisson = serving.summary(live, srv.makespan)
+    launches = __import__("libhybridgrains_gb300").kernel_launch_count() - launches0
+    srv2 = serving.Server(be, budget, max_members=min(256, args.serve_requests))
+    sat_reqs = srv2.run(copies(reqs, at_once=True))
+    saturated = serving.summary(sat_reqs, srv2.makespan)
+    be.shutdown()
+    alone = copies(reqs)
+    alone_s = serving.run_one_at_a_time(ctx, alone)
+    psteps = float(sum(r.npoints * r.steps for r in reqs))
+    diff = max(abs(a[1] - b[1]) for r1, r2 in zip(live, alone) for a, b in zip(r1.frames, r2.frames))
+    return {
+        "workload": "%d column-collapse requests, Poisson arrivals %.0f/s (seed 2024), points "
+                    "log-U[2e3,2e5], aspect U[0.5,4], friction angle U[20,40] deg, %d steps, "
+                    "a frame (positions) every 100 steps, MPM only" %
+                    (len(reqs), args.serve_rate, args.serve_steps),
+        "p50_latency_s": poisson["p50_latency_s"], "p99_latency_s": poisson["p99_latency_s"],
+        "max_latency_s": poisson["max_latency_s"],
+        "p99_admission_wait_s": poisson["p99_admission_wait_s"],
+        "makespan_s": poisson["makespan_s"],
+        "particle_steps_per_s": poisson["particle_steps_per_s"],
+        "peak_members": srv.peak_members, "peak_resident_bytes": srv.peak_resident,
+        "hbm_budget_bytes": budget, "gpu_launches": launches,
+        "saturated": {"particle_steps_per_s": saturated["particle_steps_per_s"],
+                      "requests_per_s": saturated["requests_per_s"],
+                      "p50_latency_s": saturated["p50_latency_s"],
+                      "p99_latency_s": saturated["p99_latency_s"],
+                      "makespan_s": saturated["makespan_s"]},
+        "one_at_a_time": {"particle_steps_per_s": psteps / alone_s,
+                          "requests_per_s": len(reqs) / alone_s, "seconds": alone_s},
+        "batched_over_one_at_a_time": saturated["particle_steps_per_s"] * alone_s / psteps,
+        "max_frame_runout_diff_m": diff,
+    }
 
 
 def main():
@@ -348,6 +407,10 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-steps", type=int, default=10)
     ap.add_argument("--fp64-steps", type=int, default=10)
+    ap.add_argument("--serve-requests", type=int, default=256)
+    ap.add_argument("--serve-rate", type=float, default=50.0)
+    ap.add_argument("--serve-steps", type=int, default=2000)
+    ap.add_argument("--serve-budget-gb", type=float, default=64.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()

@@ -73,6 +73,23 @@ int64_t hg_kernel_launch_count(void);
 hg_status hg_context_timer_begin(hg_context *ctx);
 hg_status hg_context_timer_end(hg_context *ctx, double *ms);
 
+/* Fences and page-locked memory, for callers that keep work queued while
+ * they handle results (no counterpart in the reference, which steps
+ * synchronously). A fence marks the point of the context's stream reached by
+ * the calls made so far; it is done once the device has finished them.
+ * Fence ids increase by one per call; only the latest 256 fences are
+ * tracked exactly, and an older one may report "not done" until a later one
+ * is done. */
+hg_status hg_context_fence(hg_context *ctx, int64_t *fence);
+hg_status hg_context_fence_done(hg_context *ctx, int64_t fence, int32_t *done);
+hg_status hg_context_fence_wait(hg_context *ctx, int64_t fence);
+/* Device bytes held by this process's objects (all contexts on the device). */
+hg_status hg_context_device_bytes(hg_context *ctx, int64_t *bytes);
+/* Page-locked host memory: asynchronous copies from and to it overlap with
+ * queued work. */
+hg_status hg_host_alloc(int64_t bytes, void **out);
+hg_status hg_host_free(void *p);
+
 /* ---- MPM (mpmgrains2d) ------------------------------------------------------ */
 
 enum { HG_BASIS_LINEAR = 0, HG_BASIS_UGIMP = 1 };
@@ -135,6 +152,25 @@ hg_status hg_mpm_upload(hg_mpm *m, int64_t n, const double *q, const double *v,
                         const double *hl, const double *be_bar,
                         const double *J, const int32_t *just_homogenized,
                         const uint8_t *kinematic);
+/* hg_mpm_upload without waiting: the copies are queued on the context's
+ * stream, and the caller keeps the arrays unchanged until a fence taken
+ * after this call is done. From page-locked memory (hg_host_alloc) the host
+ * does not wait for queued steps. No counterpart in the reference. */
+hg_status hg_mpm_upload_async(hg_mpm *m, int64_t n, const double *q, const double *v,
+                              const double *mass, const double *volume,
+                              const double *hl, const double *be_bar,
+                              const double *J, const int32_t *just_homogenized,
+                              const uint8_t *kinematic);
+/* Positions and velocities (2 x N each, upload order; either may be NULL)
+ * copied to host memory behind the steps queued so far, without waiting: the
+ * arrays hold the frame once a fence taken after this call is done. Use
+ * page-locked memory for the copy to overlap. A frame of the reference's
+ * output loop (mpmgrains2d_cli.cpp) taken without stopping the device. */
+hg_status hg_mpm_frame_async(hg_mpm *m, double *q, double *v);
+/* Device bytes hg_mpm_create plus an upload and a download of capacity
+ * points allocate for this description (admission control for many
+ * resident scenes; no counterpart in the reference). */
+hg_status hg_mpm_estimate_bytes(const hg_mpm_desc *desc, int64_t *bytes);
 /* Material point state in upload order; any pointer may be NULL. */
 hg_status hg_mpm_download(hg_mpm *m, double *q, double *v, double *be_bar,
                           double *J, int32_t *just_homogenized);
@@ -194,6 +230,10 @@ hg_status hg_batch_remove(hg_batch *b, hg_mpm *m);
 hg_status hg_batch_size(hg_batch *b, int32_t *n);
 /* nsteps steps of every member (ExplicitIntegrator::flow per member). */
 hg_status hg_batch_step(hg_batch *b, int32_t nsteps);
+/* Counters since creation: member-steps queued, member re-sorts, batch
+ * steps, and host milliseconds spent inside hg_batch_step. */
+hg_status hg_batch_stats(hg_batch *b, int64_t *member_steps, int64_t *resorts,
+                         int64_t *steps, double *host_ms);
 
 /* ---- DEM (rigidbody2d, penalty map) --------------------------------------- */
 

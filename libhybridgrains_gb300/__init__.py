@@ -15,13 +15,15 @@ There is no CPU fallback: constructing any object loads the CUDA library and
 raises if it is missing or no GPU is present.
 """
 import ctypes
+import weakref
 
 import numpy as np
 
 from . import _capi
 from ._capi import HGError, check, load  # noqa: F401
 
-__all__ = ["Context", "MPM", "DEM", "Hybrid", "HGError", "load", "kernel_launch_count"]
+__all__ = ["Context", "MPM", "DEM", "Hybrid", "Batch", "HGError", "load",
+           "kernel_launch_count", "pinned"]
 
 LINEAR, UGIMP = 0, 1
 FP64, MIXED = 0, 1
@@ -41,6 +43,21 @@ def _u8(a):
 
 def _f64(a):
     return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+def pinned(shape, dtype=np.float64):
+    """A numpy array in page-locked host memory (hg_host_alloc), freed when
+    the array is garbage collected. Asynchronous copies to and from it
+    overlap with queued device work."""
+    dt = np.dtype(dtype)
+    count = int(np.prod(shape)) if np.ndim(shape) else int(shape)
+    nbytes = max(count * dt.itemsize, 1)
+    p = ctypes.c_void_p()
+    check("hg_host_alloc", nbytes, ctypes.byref(p))
+    buf = (ctypes.c_char * nbytes).from_address(p.value)
+    arr = np.frombuffer(buf, dtype=dt, count=count).reshape(shape)
+    weakref.finalize(buf, _capi.load().hg_host_free, ctypes.c_void_p(p.value))
+    return arr
 
 
 def kernel_launch_count():
@@ -70,6 +87,25 @@ class Context:
         check("hg_context_timer_end", self._h, ctypes.byref(ms))
         return ms.value
 
+    def fence(self):
+        """Marks the calls queued so far; see fence_done / fence_wait."""
+        f = ctypes.c_int64()
+        check("hg_context_fence", self._h, ctypes.byref(f))
+        return f.value
+
+    def fence_done(self, fence):
+        d = ctypes.c_int32()
+        check("hg_context_fence_done", self._h, int(fence), ctypes.byref(d))
+        return bool(d.value)
+
+    def fence_wait(self, fence):
+        check("hg_context_fence_wait", self._h, int(fence))
+
+    def device_bytes(self):
+        b = ctypes.c_int64()
+        check("hg_context_device_bytes", self._h, ctypes.byref(b))
+        return b.value
+
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:
             _capi.load().hg_context_destroy(self._h)
@@ -80,6 +116,43 @@ class Context:
             self.close()
         except Exception:
             pass
+
+
+def _mpm_desc(grid_min, grid_max, cell_width, shear_modulus, bulk_modulus, dp_alpha,
+              flip_alpha, gravity, planes, basis, precision, capacity):
+    d = _capi.MpmDesc()
+    d.grid_min[:] = list(map(float, grid_min))
+    d.grid_max[:] = list(map(float, grid_max))
+    d.cell_width = float(cell_width)
+    d.basis = int(basis)
+    d.precision = int(precision)
+    d.shear_modulus = float(shear_modulus)
+    d.bulk_modulus = float(bulk_modulus)
+    d.dp_alpha = float(dp_alpha)
+    d.flip_alpha = float(flip_alpha)
+    d.gravity[:] = list(map(float, gravity))
+    planes = list(planes)
+    d.num_planes = len(planes)
+    for k, pl in enumerate(planes):
+        x, n = pl[0], pl[1]
+        st = pl[2] if len(pl) > 2 else True
+        lb = pl[3] if len(pl) > 3 else -np.inf
+        d.planes[k].x[:] = list(map(float, x))
+        d.planes[k].n[:] = list(map(float, n))
+        d.planes[k].sticking = 1 if st else 0
+        d.planes[k].lower_bound = float(lb)
+    d.capacity = int(capacity)
+    return d
+
+
+def mpm_estimate_bytes(grid_min, grid_max, cell_width, capacity, precision=MIXED,
+                       basis=LINEAR):
+    """Device bytes an MPM object of this size holds (hg_mpm_estimate_bytes)."""
+    d = _mpm_desc(grid_min, grid_max, cell_width, 1.0, 1.0, 0.0, 1.0, (0.0, 0.0), (), basis,
+                  precision, capacity)
+    b = ctypes.c_int64()
+    check("hg_mpm_estimate_bytes", ctypes.byref(d), ctypes.byref(b))
+    return b.value
 
 
 class MPM:
@@ -93,28 +166,8 @@ class MPM:
                  dp_alpha, flip_alpha, gravity=(0.0, -9.81), planes=(), basis=LINEAR,
                  precision=MIXED, capacity=0):
         self.ctx = ctx
-        d = _capi.MpmDesc()
-        d.grid_min[:] = list(map(float, grid_min))
-        d.grid_max[:] = list(map(float, grid_max))
-        d.cell_width = float(cell_width)
-        d.basis = int(basis)
-        d.precision = int(precision)
-        d.shear_modulus = float(shear_modulus)
-        d.bulk_modulus = float(bulk_modulus)
-        d.dp_alpha = float(dp_alpha)
-        d.flip_alpha = float(flip_alpha)
-        d.gravity[:] = list(map(float, gravity))
-        planes = list(planes)
-        d.num_planes = len(planes)
-        for k, pl in enumerate(planes):
-            x, n = pl[0], pl[1]
-            st = pl[2] if len(pl) > 2 else True
-            lb = pl[3] if len(pl) > 3 else -np.inf
-            d.planes[k].x[:] = list(map(float, x))
-            d.planes[k].n[:] = list(map(float, n))
-            d.planes[k].sticking = 1 if st else 0
-            d.planes[k].lower_bound = float(lb)
-        d.capacity = int(capacity)
+        d = _mpm_desc(grid_min, grid_max, cell_width, shear_modulus, bulk_modulus, dp_alpha,
+                      flip_alpha, gravity, planes, basis, precision, capacity)
         h = ctypes.c_void_p()
         check("hg_mpm_create", ctx._h, ctypes.byref(d), ctypes.byref(h))
         self._h = h
@@ -165,6 +218,23 @@ class MPM:
         check("hg_mpm_upload", self._h, n, _d(q), _d(v), _d(m), _d(vol), _d(hl), _d(be), _d(J),
               _i32(jh), _u8(kin))
         self.n = n
+
+    def upload_async(self, q, v, m, vol, hl=None):
+        """hg_mpm_upload_async: the arrays (float64, C order; page-locked for
+        the copy to overlap) must stay alive and unchanged until a fence
+        taken after this call is done."""
+        for a in (q, v, m, vol) + (() if hl is None else (hl,)):
+            if a.dtype != np.float64 or not a.flags.c_contiguous:
+                raise ValueError("upload_async takes C-contiguous float64 arrays")
+        n = len(m)
+        check("hg_mpm_upload_async", self._h, n, _d(q), _d(v), _d(m), _d(vol), _d(hl), None,
+              None, None, None)
+        self.n = n
+
+    def frame_async(self, q=None, v=None):
+        """Queue a copy of positions / velocities ((N, 2) float64 arrays) to
+        the host; valid once a later fence is done."""
+        check("hg_mpm_frame_async", self._h, _d(q), _d(v))
 
     def download(self):
         n = self.n
@@ -389,6 +459,14 @@ class Batch:
 
     def step(self, nsteps=1):
         check("hg_batch_step", self._h, int(nsteps))
+
+    def stats(self):
+        """(member-steps, re-sorts, batch steps, host ms inside hg_batch_step)."""
+        a, r, s = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        h = ctypes.c_double()
+        check("hg_batch_stats", self._h, ctypes.byref(a), ctypes.byref(r), ctypes.byref(s),
+              ctypes.byref(h))
+        return a.value, r.value, s.value, h.value
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:

@@ -92,12 +92,22 @@ SIGNATURES = {
     "hg_mpm_rebin_count": [_P, _I64],
     "hg_mpm_profile": [_P, _i32],
     "hg_mpm_profile_read": [_P, _D, _D, _I64],
+    "hg_context_fence": [_P, _I64],
+    "hg_context_fence_done": [_P, _i64, _I32],
+    "hg_context_fence_wait": [_P, _i64],
+    "hg_context_device_bytes": [_P, _I64],
+    "hg_host_alloc": [_i64, _PP],
+    "hg_host_free": [_P],
+    "hg_mpm_upload_async": [_P, _i64, _D, _D, _D, _D, _D, _D, _D, _I32, _U8],
+    "hg_mpm_frame_async": [_P, _D, _D],
+    "hg_mpm_estimate_bytes": [ctypes.POINTER(MpmDesc), _I64],
     "hg_batch_create": [_P, _i32, _PP],
     "hg_batch_destroy": [_P],
     "hg_batch_add": [_P, _P, _dbl],
     "hg_batch_remove": [_P, _P],
     "hg_batch_size": [_P, _I32],
     "hg_batch_step": [_P, _i32],
+    "hg_batch_stats": [_P, _I64, _I64, _I64, _D],
     "hg_dem_create": [_P, ctypes.POINTER(DemDesc), _PP],
     "hg_dem_destroy": [_P],
     "hg_dem_upload": [_P, _i64, _D, _D, _D, _D, _D, _U8],

@@ -3,6 +3,7 @@
 #include "hg_internal.cuh"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -13,6 +14,7 @@
 namespace hg {
 
 std::atomic<int64_t> g_launches{0};
+thread_local cudaStream_t t_alloc_stream = nullptr;
 
 namespace {
 thread_local std::string t_last_error;
@@ -43,8 +45,29 @@ void context_release(hg_context *c) {
   cudaStreamDestroy(c->stream);
   if (c->t0) cudaEventDestroy(c->t0);
   if (c->t1) cudaEventDestroy(c->t1);
+  for (cudaEvent_t e : c->fences)
+    if (e) cudaEventDestroy(e);
+  for (uint32_t *p : c->pinned_chunks) cudaFreeHost(p);
   if (prev >= 0 && prev != c->device) cudaSetDevice(prev);
   delete c;
+}
+
+uint32_t *context_pinned_pair(hg_context *c) {
+  constexpr int PAIRS_PER_CHUNK = 4096;
+  if (c->pinned_free.empty()) {
+    uint32_t *chunk = nullptr;
+    if (cudaMallocHost(&chunk, 2 * sizeof(uint32_t) * PAIRS_PER_CHUNK) != cudaSuccess)
+      return nullptr;
+    c->pinned_chunks.push_back(chunk);
+    for (int k = PAIRS_PER_CHUNK - 1; k >= 0; --k) c->pinned_free.push_back(chunk + 2 * k);
+  }
+  uint32_t *p = c->pinned_free.back();
+  c->pinned_free.pop_back();
+  return p;
+}
+
+void context_return_pair(hg_context *c, uint32_t *p) {
+  if (p) c->pinned_free.push_back(p);
 }
 
 } // namespace hg
@@ -53,9 +76,14 @@ using namespace hg;
 
 namespace capi_impl {
 
+// Selects the context's device and makes device buffers allocated in the
+// scope stream-ordered on the context's stream.
 struct DeviceGuard {
   int prev = -1;
-  explicit DeviceGuard(int dev) {
+  AllocScope scope;
+  explicit DeviceGuard(int dev) : scope(nullptr) { select(dev); }
+  explicit DeviceGuard(const hg_context *c) : scope(c->stream) { select(c->device); }
+  void select(int dev) {
     cudaGetDevice(&prev);
     if (prev != dev) cudaSetDevice(dev);
   }
@@ -174,6 +202,15 @@ hg_status hg_context_create(int32_t device, hg_context **out) {
     delete c;
     return cuda_fail(e, "context creation");
   }
+  // Objects allocate stream-ordered from the device's default pool; keep
+  // freed blocks in the pool (this process only) so that scenes created and
+  // destroyed while others run reuse memory without returning it to the
+  // driver at every synchronisation.
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
   *out = c;
   return HG_OK;
 }
@@ -186,7 +223,7 @@ hg_status hg_context_destroy(hg_context *ctx) {
 
 hg_status hg_context_timer_begin(hg_context *ctx) {
   if (!ctx) return fail(HG_ERR_INVALID_ARGUMENT, "ctx is NULL");
-  DeviceGuard g(ctx->device);
+  DeviceGuard g(ctx);
   if (!ctx->t0) HG_CUDA_TRY(cudaEventCreate(&ctx->t0));
   if (!ctx->t1) HG_CUDA_TRY(cudaEventCreate(&ctx->t1));
   HG_CUDA_TRY(cudaEventRecord(ctx->t0, ctx->stream));
@@ -196,7 +233,7 @@ hg_status hg_context_timer_begin(hg_context *ctx) {
 hg_status hg_context_timer_end(hg_context *ctx, double *ms) {
   if (!ctx || !ms) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
   if (!ctx->t0) return fail(HG_ERR_INVALID_ARGUMENT, "timer not started");
-  DeviceGuard g(ctx->device);
+  DeviceGuard g(ctx);
   HG_CUDA_TRY(cudaEventRecord(ctx->t1, ctx->stream));
   HG_CUDA_TRY(cudaEventSynchronize(ctx->t1));
   float f = 0.f;
@@ -207,16 +244,73 @@ hg_status hg_context_timer_end(hg_context *ctx, double *ms) {
 
 hg_status hg_context_synchronize(hg_context *ctx) {
   if (!ctx) return fail(HG_ERR_INVALID_ARGUMENT, "ctx is NULL");
-  DeviceGuard g(ctx->device);
+  DeviceGuard g(ctx);
   HG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return HG_OK;
+}
+
+static constexpr int FENCE_RING = 256;
+
+hg_status hg_context_fence(hg_context *ctx, int64_t *fence) {
+  if (!ctx || !fence) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  DeviceGuard g(ctx);
+  if (ctx->fences.empty()) ctx->fences.assign(FENCE_RING, nullptr);
+  const int64_t id = ctx->next_fence;
+  cudaEvent_t &e = ctx->fences[id % FENCE_RING];
+  if (!e) HG_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  HG_CUDA_TRY(cudaEventRecord(e, ctx->stream));
+  ctx->next_fence = id + 1;
+  *fence = id;
+  return HG_OK;
+}
+
+hg_status hg_context_fence_done(hg_context *ctx, int64_t fence, int32_t *done) {
+  if (!ctx || !done) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (fence < 0 || fence >= ctx->next_fence) return fail(HG_ERR_INVALID_ARGUMENT, "unknown fence");
+  DeviceGuard g(ctx);
+  // a slot reused by a later fence answers for that one: done then implies
+  // done for this one (same stream), not-done is conservative
+  const cudaError_t q = cudaEventQuery(ctx->fences[fence % FENCE_RING]);
+  if (q != cudaSuccess && q != cudaErrorNotReady) return cuda_fail(q, "fence query");
+  *done = q == cudaSuccess ? 1 : 0;
+  return HG_OK;
+}
+
+hg_status hg_context_fence_wait(hg_context *ctx, int64_t fence) {
+  if (!ctx) return fail(HG_ERR_INVALID_ARGUMENT, "ctx is NULL");
+  if (fence < 0 || fence >= ctx->next_fence) return fail(HG_ERR_INVALID_ARGUMENT, "unknown fence");
+  DeviceGuard g(ctx);
+  HG_CUDA_TRY(cudaEventSynchronize(ctx->fences[fence % FENCE_RING]));
+  return HG_OK;
+}
+
+hg_status hg_context_device_bytes(hg_context *ctx, int64_t *bytes) {
+  if (!ctx || !bytes) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  DeviceGuard g(ctx);
+  cudaMemPool_t pool;
+  HG_CUDA_TRY(cudaDeviceGetDefaultMemPool(&pool, ctx->device));
+  uint64_t used = 0;
+  HG_CUDA_TRY(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used));
+  *bytes = (int64_t)used;
+  return HG_OK;
+}
+
+hg_status hg_host_alloc(int64_t bytes, void **out) {
+  if (!out) return fail(HG_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  if (bytes <= 0) return fail(HG_ERR_INVALID_ARGUMENT, "bytes must be positive");
+  HG_CUDA_TRY(cudaMallocHost(out, (size_t)bytes));
+  return HG_OK;
+}
+
+hg_status hg_host_free(void *p) {
+  if (p) HG_CUDA_TRY(cudaFreeHost(p));
   return HG_OK;
 }
 
 // ---- MPM --------------------------------------------------------------------
 
-hg_status hg_mpm_create(hg_context *ctx, const hg_mpm_desc *d, hg_mpm **out) {
-  if (!ctx || !d || !out) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
-  *out = nullptr;
+static hg_status validate_desc(const hg_mpm_desc *d) {
   if (!(d->cell_width > 0.0) || !std::isfinite(d->cell_width))
     return fail(HG_ERR_INVALID_ARGUMENT, "cell_width must be positive and finite");
   if (!finite_all(d->grid_min, 2) || !finite_all(d->grid_max, 2) ||
@@ -236,7 +330,15 @@ hg_status hg_mpm_create(hg_context *ctx, const hg_mpm_desc *d, hg_mpm **out) {
   const double cw = (d->grid_max[0] - d->grid_min[0]) / d->cell_width;
   const double ch = (d->grid_max[1] - d->grid_min[1]) / d->cell_width;
   if (cw > 1.0e6 || ch > 1.0e6) return fail(HG_ERR_INVALID_ARGUMENT, "grid too large");
-  DeviceGuard g(ctx->device);
+  return HG_OK;
+}
+
+hg_status hg_mpm_create(hg_context *ctx, const hg_mpm_desc *d, hg_mpm **out) {
+  if (!ctx || !d || !out) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  *out = nullptr;
+  hg_status vst = validate_desc(d);
+  if (vst != HG_OK) return vst;
+  DeviceGuard g(ctx);
   hg_mpm *m = new (std::nothrow) hg_mpm();
   if (!m) return fail(HG_ERR_OUT_OF_MEMORY, "host allocation failed");
   m->ctx = ctx;
@@ -309,7 +411,9 @@ hg_status hg_mpm_create(hg_context *ctx, const hg_mpm_desc *d, hg_mpm **out) {
     st = mixed_alloc(m);
   }
   if (st == HG_OK) {
-    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    // no wait for the queued memsets: creating a scene while others step
+    // must not drain the stream; errors surface at the next synchronising call
+    cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) st = cuda_fail(e, "hg_mpm_create");
   }
   if (st != HG_OK) {
@@ -324,9 +428,10 @@ hg_status hg_mpm_destroy(hg_mpm *m) {
   if (!m) return HG_OK;
   hg_context *ctx = m->ctx;
   {
-    DeviceGuard g(ctx->device);
-    cudaStreamSynchronize(ctx->stream);
-    if (m->h_outside) cudaFreeHost(m->h_outside);
+    DeviceGuard g(ctx);
+    // buffers are released stream-ordered behind the queued work; the
+    // read-back slot goes back to the context's pool for later work
+    context_return_pair(ctx, m->h_outside);
     if (m->outside_ev) cudaEventDestroy(m->outside_ev);
     for (cudaEvent_t e : m->prof_events) cudaEventDestroy(e);
     delete m;
@@ -411,10 +516,10 @@ hg_status hg_mpm_seed_rectangle(hg_mpm *m, const double rmin[2], const double rm
   return HG_OK;
 }
 
-hg_status hg_mpm_upload(hg_mpm *m, int64_t n, const double *q, const double *v,
-                        const double *mass, const double *volume, const double *hl,
-                        const double *be, const double *J, const int32_t *jh,
-                        const uint8_t *kin) {
+static hg_status upload_impl(hg_mpm *m, int64_t n, const double *q, const double *v,
+                             const double *mass, const double *volume, const double *hl,
+                             const double *be, const double *J, const int32_t *jh,
+                             const uint8_t *kin, bool wait) {
   if (!m) return fail(HG_ERR_INVALID_ARGUMENT, "m is NULL");
   if (n < 0) return fail(HG_ERR_INVALID_ARGUMENT, "negative particle count");
   if (n > m->cap) return fail(HG_ERR_CAPACITY, "particle count exceeds capacity");
@@ -422,7 +527,7 @@ hg_status hg_mpm_upload(hg_mpm *m, int64_t n, const double *q, const double *v,
     return fail(HG_ERR_INVALID_ARGUMENT, "q, v, mass and volume are required");
   if (n > 0 && m->p.basis == HG_BASIS_UGIMP && !hl)
     return fail(HG_ERR_INVALID_ARGUMENT, "hl is required for the uGIMP basis");
-  DeviceGuard g(m->ctx->device);
+  DeviceGuard g(m->ctx);
   cudaStream_t s = m->ctx->stream;
   m->n = n;
   hg_status st = HG_OK;
@@ -494,14 +599,66 @@ hg_status hg_mpm_upload(hg_mpm *m, int64_t n, const double *q, const double *v,
       return st;
   }
   // the caller may reuse its buffers as soon as this returns
-  HG_CUDA_TRY(cudaStreamSynchronize(s));
+  if (wait) HG_CUDA_TRY(cudaStreamSynchronize(s));
+  return HG_OK;
+}
+
+hg_status hg_mpm_upload(hg_mpm *m, int64_t n, const double *q, const double *v,
+                        const double *mass, const double *volume, const double *hl,
+                        const double *be, const double *J, const int32_t *jh,
+                        const uint8_t *kin) {
+  return upload_impl(m, n, q, v, mass, volume, hl, be, J, jh, kin, true);
+}
+
+hg_status hg_mpm_upload_async(hg_mpm *m, int64_t n, const double *q, const double *v,
+                              const double *mass, const double *volume, const double *hl,
+                              const double *be, const double *J, const int32_t *jh,
+                              const uint8_t *kin) {
+  return upload_impl(m, n, q, v, mass, volume, hl, be, J, jh, kin, false);
+}
+
+hg_status hg_mpm_frame_async(hg_mpm *m, double *q, double *v) {
+  if (!m) return fail(HG_ERR_INVALID_ARGUMENT, "m is NULL");
+  DeviceGuard g(m->ctx);
+  cudaStream_t s = m->ctx->stream;
+  const int64_t n = m->n;
+  if (n == 0 || (!q && !v)) return HG_OK;
+  hg_status st;
+  if (m->p.precision == HG_PRECISION_FP64) {
+    if ((st = d2h(s, q, m->q.p, 2 * n)) || (st = d2h(s, v, m->v.p, 2 * n))) return st;
+    return HG_OK;
+  }
+  if (m->stage_d.n < (size_t)(4 * n) && (st = m->stage_d.alloc(4 * n))) return st;
+  double *sq = m->stage_d.p, *sv = sq + 2 * n;
+  if ((st = mixed_download(m, sq, sv, nullptr, nullptr, nullptr))) return st;
+  if ((st = d2h(s, q, sq, 2 * n)) || (st = d2h(s, v, sv, 2 * n))) return st;
+  return HG_OK;
+}
+
+hg_status hg_mpm_estimate_bytes(const hg_mpm_desc *d, int64_t *bytes) {
+  if (!d || !bytes) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  hg_status st = validate_desc(d);
+  if (st != HG_OK) return st;
+  MpmParams P{};
+  set_dimensions(P, d->grid_min, d->grid_max, d->cell_width);
+  const int64_t nn = (int64_t)(P.nx + 1) * (P.ny + 1), cap = d->capacity;
+  int64_t b = 4; // status word
+  if (d->precision == HG_PRECISION_FP64) {
+    b += cap * (2 * 16 + 3 * 8 + 32 + 8 + 32 + 4 + 1); // q v | m vol hl | be | J | sigma | jh | kin
+    b += nn * (8 + 6 * 16 + 8 + 4);                    // grid fields
+  } else {
+    b += mixed_device_bytes(P.nx, P.ny, cap);
+    b += 8 * std::max<int64_t>(11 * cap, 5 * nn) + cap; // upload / download staging
+  }
+  b += 4 * 2 * cap; // int staging (upload, cell index)
+  *bytes = b;
   return HG_OK;
 }
 
 hg_status hg_mpm_download(hg_mpm *m, double *q, double *v, double *be, double *J,
                           int32_t *jh) {
   if (!m) return fail(HG_ERR_INVALID_ARGUMENT, "m is NULL");
-  DeviceGuard g(m->ctx->device);
+  DeviceGuard g(m->ctx);
   cudaStream_t s = m->ctx->stream;
   const int64_t n = m->n;
   hg_status st;
@@ -535,7 +692,7 @@ hg_status hg_mpm_step(hg_mpm *m, double dt, int32_t nsteps) {
   if (!m) return fail(HG_ERR_INVALID_ARGUMENT, "m is NULL");
   if (!(dt > 0.0) || !std::isfinite(dt)) return fail(HG_ERR_INVALID_ARGUMENT, "dt must be positive");
   if (nsteps < 0) return fail(HG_ERR_INVALID_ARGUMENT, "negative step count");
-  DeviceGuard g(m->ctx->device);
+  DeviceGuard g(m->ctx);
   if (m->p.precision == HG_PRECISION_MIXED) return mixed_step(m, dt, nsteps);
   for (int k = 0; k < nsteps; ++k) {
     hg_status st;
@@ -549,7 +706,7 @@ hg_status hg_mpm_phase0(hg_mpm *m) {
   if (!m) return fail(HG_ERR_INVALID_ARGUMENT, "m is NULL");
   if (m->p.precision != HG_PRECISION_FP64)
     return fail(HG_ERR_UNSUPPORTED, "phase calls need FP64 precision");
-  DeviceGuard g(m->ctx->device);
+  DeviceGuard g(m->ctx);
   return mpm64_phase0(m);
 }
 
@@ -558,7 +715,7 @@ hg_status hg_mpm_phase1(hg_mpm *m, double dt) {
   if (m->p.precision != HG_PRECISION_FP64)
     return fail(HG_ERR_UNSUPPORTED, "phase calls need FP64 precision");
   if (!(dt > 0.0)) return fail(HG_ERR_INVALID_ARGUMENT, "dt must be positive");
-  DeviceGuard g(m->ctx->device);
+  DeviceGuard g(m->ctx);
   return mpm64_phase1(m, dt);
 }
 
@@ -567,14 +724,14 @@ hg_status hg_mpm_phase2(hg_mpm *m, double dt) {
   if (m->p.precision != HG_PRECISION_FP64)
     return fail(HG_ERR_UNSUPPORTED, "phase calls need FP64 precision");
   if (!(dt > 0.0)) return fail(HG_ERR_INVALID_ARGUMENT, "dt must be positive");
-  DeviceGuard g(m->ctx->device);
+  DeviceGuard g(m->ctx);
   return mpm64_phase2(m, dt);
 }
 
 hg_status hg_mpm_download_grid(hg_mpm *m, double *mass, double *mom, double *mom_new,
                                double *force, double *vel, double *acc) {
   if (!m) return fail(HG_ERR_INVALID_ARGUMENT, "m is NULL");
-  DeviceGuard g(m->ctx->device);
+  DeviceGuard g(m->ctx);
   cudaStream_t s = m->ctx->stream;
   const int64_t nn = (int64_t)(m->p.nx + 1) * (m->p.ny + 1);
   hg_status st;
@@ -600,7 +757,7 @@ hg_status hg_mpm_download_grid(hg_mpm *m, double *mass, double *mom, double *mom
 
 hg_status hg_mpm_cell_index(hg_mpm *m, int32_t *cells) {
   if (!m || !cells) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
-  DeviceGuard g(m->ctx->device);
+  DeviceGuard g(m->ctx);
   cudaStream_t s = m->ctx->stream;
   const int64_t n = m->n;
   if (n == 0) return HG_OK;
@@ -621,7 +778,7 @@ hg_status hg_mpm_cell_index(hg_mpm *m, int32_t *cells) {
 
 hg_status hg_mpm_status(hg_mpm *m, uint32_t *word) {
   if (!m || !word) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
-  DeviceGuard g(m->ctx->device);
+  DeviceGuard g(m->ctx);
   HG_CUDA_TRY(cudaMemcpyAsync(word, m->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost,
                               m->ctx->stream));
   HG_CUDA_TRY(cudaStreamSynchronize(m->ctx->stream));
@@ -630,7 +787,7 @@ hg_status hg_mpm_status(hg_mpm *m, uint32_t *word) {
 
 hg_status hg_mpm_clear_status(hg_mpm *m) {
   if (!m) return fail(HG_ERR_INVALID_ARGUMENT, "m is NULL");
-  DeviceGuard g(m->ctx->device);
+  DeviceGuard g(m->ctx);
   HG_CUDA_TRY(cudaMemsetAsync(m->status.p, 0, sizeof(uint32_t), m->ctx->stream));
   return HG_OK;
 }
@@ -639,7 +796,7 @@ hg_status hg_mpm_profile(hg_mpm *m, int32_t enable) {
   if (!m) return fail(HG_ERR_INVALID_ARGUMENT, "m is NULL");
   if (m->p.precision != HG_PRECISION_MIXED)
     return fail(HG_ERR_UNSUPPORTED, "kernel profiling covers the MIXED path");
-  DeviceGuard g(m->ctx->device);
+  DeviceGuard g(m->ctx);
   HG_CUDA_TRY(cudaStreamSynchronize(m->ctx->stream));
   m->profile = enable != 0;
   m->prof_used = 0;
@@ -648,7 +805,7 @@ hg_status hg_mpm_profile(hg_mpm *m, int32_t enable) {
 
 hg_status hg_mpm_profile_read(hg_mpm *m, double *a, double *b, int64_t *steps) {
   if (!m) return fail(HG_ERR_INVALID_ARGUMENT, "m is NULL");
-  DeviceGuard g(m->ctx->device);
+  DeviceGuard g(m->ctx);
   return mixed_profile_read(m, a, b, steps);
 }
 
@@ -665,7 +822,7 @@ hg_status hg_batch_create(hg_context *ctx, int32_t max_members, hg_batch **out) 
   *out = nullptr;
   if (max_members < 1 || max_members > HG_MAX_BATCH)
     return fail(HG_ERR_INVALID_ARGUMENT, "max_members must lie in [1, HG_MAX_BATCH]");
-  DeviceGuard g(ctx->device);
+  DeviceGuard g(ctx);
   hg_batch *b = new (std::nothrow) hg_batch();
   if (!b) return fail(HG_ERR_OUT_OF_MEMORY, "host allocation failed");
   b->ctx = ctx;
@@ -684,7 +841,7 @@ hg_status hg_batch_destroy(hg_batch *b) {
   if (!b) return HG_OK;
   hg_context *ctx = b->ctx;
   {
-    DeviceGuard g(ctx->device);
+    DeviceGuard g(ctx);
     cudaStreamSynchronize(ctx->stream);
     batch_free(b);
     delete b;
@@ -730,8 +887,21 @@ hg_status hg_batch_size(hg_batch *b, int32_t *n) {
 hg_status hg_batch_step(hg_batch *b, int32_t nsteps) {
   if (!b) return fail(HG_ERR_INVALID_ARGUMENT, "b is NULL");
   if (nsteps < 0) return fail(HG_ERR_INVALID_ARGUMENT, "negative step count");
-  DeviceGuard g(b->ctx->device);
-  return batch_step(b, nsteps);
+  DeviceGuard g(b->ctx);
+  const auto t0 = std::chrono::steady_clock::now();
+  const hg_status st = batch_step(b, nsteps);
+  b->host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return st;
+}
+
+hg_status hg_batch_stats(hg_batch *b, int64_t *member_steps, int64_t *resorts, int64_t *steps,
+                         double *host_ms) {
+  if (!b) return fail(HG_ERR_INVALID_ARGUMENT, "b is NULL");
+  if (member_steps) *member_steps = b->member_steps;
+  if (resorts) *resorts = b->resorts;
+  if (steps) *steps = b->steps;
+  if (host_ms) *host_ms = b->host_ms;
+  return HG_OK;
 }
 
 // ---- DEM ------------------------------------------------------------------------
@@ -749,7 +919,7 @@ hg_status hg_dem_create(hg_context *ctx, const hg_dem_desc *d, hg_dem **out) {
   if (!finite_all(params, 7) || d->kn < 0 || d->kt < 0 || d->gamman < 0 || d->gammat < 0 ||
       d->mu < 0)
     return fail(HG_ERR_INVALID_ARGUMENT, "penalty parameters must be finite and >= 0");
-  DeviceGuard g(ctx->device);
+  DeviceGuard g(ctx);
   hg_dem *dm = new (std::nothrow) hg_dem();
   if (!dm) return fail(HG_ERR_OUT_OF_MEMORY, "host allocation failed");
   dm->ctx = ctx;
@@ -793,7 +963,7 @@ hg_status hg_dem_destroy(hg_dem *d) {
   if (!d) return HG_OK;
   hg_context *ctx = d->ctx;
   {
-    DeviceGuard g(ctx->device);
+    DeviceGuard g(ctx);
     cudaStreamSynchronize(ctx->stream);
     delete d;
   }
@@ -815,7 +985,7 @@ hg_status hg_dem_upload(hg_dem *d, int64_t n, const double *q, const double *v,
       return fail(HG_ERR_INVALID_ARGUMENT, "radius, mass and inertia must be positive");
     rmax = std::max(rmax, r[i]);
   }
-  DeviceGuard g(d->ctx->device);
+  DeviceGuard g(d->ctx);
   // Broadphase cell width: the widest disk AABB plus a relative margin, so a
   // disk's partners lie in the 3x3 cells around the cell of its AABB minimum.
   d->cell_h = 2.0 * rmax * (1.0 + 1.0e-6);
@@ -842,7 +1012,7 @@ hg_status hg_dem_set_weights(hg_dem *d, const double *w) {
   if (!d || (!w && d->n > 0)) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
   for (int64_t i = 0; i < d->n; ++i)
     if (!(w[i] >= 0.0 && w[i] <= 1.0)) return fail(HG_ERR_INVALID_ARGUMENT, "weights must lie in [0, 1]");
-  DeviceGuard g(d->ctx->device);
+  DeviceGuard g(d->ctx);
   hg_status st = h2d(d->ctx->stream, d->w.p, w, d->n);
   if (st) return st;
   HG_CUDA_TRY(cudaStreamSynchronize(d->ctx->stream));
@@ -851,7 +1021,7 @@ hg_status hg_dem_set_weights(hg_dem *d, const double *w) {
 
 hg_status hg_dem_set_state(hg_dem *d, const double *q, const double *v) {
   if (!d) return fail(HG_ERR_INVALID_ARGUMENT, "d is NULL");
-  DeviceGuard g(d->ctx->device);
+  DeviceGuard g(d->ctx);
   hg_status st;
   if (q && (st = h2d(d->ctx->stream, d->q.p, q, 3 * d->n))) return st;
   if (v && (st = h2d(d->ctx->stream, d->v.p, v, 3 * d->n))) return st;
@@ -861,7 +1031,7 @@ hg_status hg_dem_set_state(hg_dem *d, const double *q, const double *v) {
 
 hg_status hg_dem_download(hg_dem *d, double *q, double *v) {
   if (!d) return fail(HG_ERR_INVALID_ARGUMENT, "d is NULL");
-  DeviceGuard g(d->ctx->device);
+  DeviceGuard g(d->ctx);
   hg_status st;
   if ((st = d2h(d->ctx->stream, q, d->q.p, 3 * d->n)) ||
       (st = d2h(d->ctx->stream, v, d->v.p, 3 * d->n)))
@@ -874,7 +1044,7 @@ hg_status hg_dem_step(hg_dem *d, double dt, int32_t nsteps, int32_t weighted) {
   if (!d) return fail(HG_ERR_INVALID_ARGUMENT, "d is NULL");
   if (!(dt > 0.0) || !std::isfinite(dt)) return fail(HG_ERR_INVALID_ARGUMENT, "dt must be positive");
   if (nsteps < 0) return fail(HG_ERR_INVALID_ARGUMENT, "negative step count");
-  DeviceGuard g(d->ctx->device);
+  DeviceGuard g(d->ctx);
   for (int k = 0; k < nsteps; ++k) {
     hg_status st = dem_step(d, dt, weighted);
     if (st != HG_OK) return st;
@@ -884,7 +1054,7 @@ hg_status hg_dem_step(hg_dem *d, double dt, int32_t nsteps, int32_t weighted) {
 
 hg_status hg_dem_num_contacts(hg_dem *d, int64_t *n) {
   if (!d || !n) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
-  DeviceGuard g(d->ctx->device);
+  DeviceGuard g(d->ctx);
   int32_t c = 0;
   if (d->history_valid) {
     HG_CUDA_TRY(cudaMemcpyAsync(&c, d->c_count.p + d->cc, sizeof(int32_t),
@@ -897,13 +1067,13 @@ hg_status hg_dem_num_contacts(hg_dem *d, int64_t *n) {
 
 hg_status hg_dem_download_contacts(hg_dem *d, int64_t cap, double *rec, int64_t *count) {
   if (!d || !count || (cap > 0 && !rec)) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
-  DeviceGuard g(d->ctx->device);
+  DeviceGuard g(d->ctx);
   return dem_download_contacts(d, cap, rec, count);
 }
 
 hg_status hg_dem_status(hg_dem *d, uint32_t *word) {
   if (!d || !word) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
-  DeviceGuard g(d->ctx->device);
+  DeviceGuard g(d->ctx);
   HG_CUDA_TRY(cudaMemcpyAsync(word, d->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost,
                               d->ctx->stream));
   HG_CUDA_TRY(cudaStreamSynchronize(d->ctx->stream));
@@ -919,7 +1089,7 @@ hg_status hg_dem_candidate_pairs(hg_context *ctx, int64_t n, const double *mn,
   for (int64_t i = 0; i < 2 * n; ++i)
     if (!std::isfinite(mn[i]) || !std::isfinite(mx[i]) || !(mn[i] < mx[i]))
       return fail(HG_ERR_INVALID_ARGUMENT, "boxes must be finite with min < max");
-  DeviceGuard g(ctx->device);
+  DeviceGuard g(ctx);
   return dem_candidate_pairs(ctx, n, mn, mx, cap, pairs, count);
 }
 
@@ -932,7 +1102,7 @@ hg_status hg_hybrid_create(hg_context *ctx, hg_mpm *m, hg_dem *d, hg_hybrid **ou
     return fail(HG_ERR_INVALID_ARGUMENT, "objects belong to another context");
   if (m->p.precision != HG_PRECISION_FP64)
     return fail(HG_ERR_UNSUPPORTED, "the hybrid step needs an FP64 MPM object");
-  DeviceGuard g(ctx->device);
+  DeviceGuard g(ctx);
   hg_hybrid *h = new (std::nothrow) hg_hybrid();
   if (!h) return fail(HG_ERR_OUT_OF_MEMORY, "host allocation failed");
   h->ctx = ctx;
@@ -952,7 +1122,7 @@ hg_status hg_hybrid_destroy(hg_hybrid *h) {
   if (!h) return HG_OK;
   hg_context *ctx = h->ctx;
   {
-    DeviceGuard g(ctx->device);
+    DeviceGuard g(ctx);
     cudaStreamSynchronize(ctx->stream);
     delete h;
   }
@@ -967,7 +1137,7 @@ hg_status hg_hybrid_step(hg_hybrid *h, double dt, int32_t nsteps, int32_t flags)
   if (h->m->n > 0 && h->m->cap < 1) return fail(HG_ERR_INVALID_ARGUMENT, "empty MPM object");
   if (h->m->n == 0)
     return fail(HG_ERR_INVALID_ARGUMENT, "the coupling needs at least one material point");
-  DeviceGuard g(h->ctx->device);
+  DeviceGuard g(h->ctx);
   for (int k = 0; k < nsteps; ++k) {
     hg_status st = hybrid_step(h, dt, flags);
     if (st != HG_OK) return st;
@@ -977,13 +1147,13 @@ hg_status hg_hybrid_step(hg_hybrid *h, double dt, int32_t nsteps, int32_t flags)
 
 hg_status hg_hybrid_clear_homogenized(hg_hybrid *h) {
   if (!h) return fail(HG_ERR_INVALID_ARGUMENT, "h is NULL");
-  DeviceGuard g(h->ctx->device);
+  DeviceGuard g(h->ctx);
   return hybrid_clear_homogenized(h);
 }
 
 hg_status hg_hybrid_num_packed(hg_hybrid *h, int64_t *ng, int64_t *nn) {
   if (!h) return fail(HG_ERR_INVALID_ARGUMENT, "h is NULL");
-  DeviceGuard g(h->ctx->device);
+  DeviceGuard g(h->ctx);
   int32_t c[2] = {0, 0};
   HG_CUDA_TRY(cudaMemcpyAsync(c, h->counts.p, sizeof(c), cudaMemcpyDeviceToHost, h->ctx->stream));
   HG_CUDA_TRY(cudaStreamSynchronize(h->ctx->stream));
@@ -995,7 +1165,7 @@ hg_status hg_hybrid_num_packed(hg_hybrid *h, int64_t *ng, int64_t *nn) {
 hg_status hg_hybrid_download(hg_hybrid *h, int32_t *pg, int32_t *pn, double *dm, double *dp,
                              double *va, double *aa, double *hf, double *hs, double *hv) {
   if (!h) return fail(HG_ERR_INVALID_ARGUMENT, "h is NULL");
-  DeviceGuard g(h->ctx->device);
+  DeviceGuard g(h->ctx);
   cudaStream_t s = h->ctx->stream;
   int32_t c[2] = {0, 0};
   HG_CUDA_TRY(cudaMemcpyAsync(c, h->counts.p, sizeof(c), cudaMemcpyDeviceToHost, s));

@@ -42,24 +42,49 @@ extern std::atomic<int64_t> g_launches;
 
 // ---- device buffers --------------------------------------------------------
 
+// Stream-ordered allocation. While an AllocScope is active on the calling
+// thread, DevBuf allocates with cudaMallocAsync on the scope's stream and
+// frees with cudaFreeAsync on the same stream, so creating and destroying
+// objects neither waits for queued work nor lets a buffer be reused while a
+// queued kernel still reads it. Without a scope it uses cudaMalloc/cudaFree.
+extern thread_local cudaStream_t t_alloc_stream;
+
+struct AllocScope {
+  cudaStream_t prev;
+  explicit AllocScope(cudaStream_t s) : prev(t_alloc_stream) { t_alloc_stream = s; }
+  ~AllocScope() { t_alloc_stream = prev; }
+};
+
 template <typename T> struct DevBuf {
   T *p = nullptr;
   size_t n = 0;
+  cudaStream_t s = nullptr; // stream of a stream-ordered allocation
   hg_status alloc(size_t count) {
     free();
     if (count == 0) count = 1;
-    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    cudaError_t e;
+    if (t_alloc_stream) {
+      e = cudaMallocAsync(reinterpret_cast<void **>(&p), count * sizeof(T), t_alloc_stream);
+      s = t_alloc_stream;
+    } else {
+      e = cudaMalloc(&p, count * sizeof(T));
+      s = nullptr;
+    }
     if (e != cudaSuccess) {
       p = nullptr;
-      return cuda_fail(e, "cudaMalloc");
+      return cuda_fail(e, "device allocation");
     }
     n = count;
     return HG_OK;
   }
   void free() {
-    if (p) cudaFree(p);
+    if (p) {
+      if (s) cudaFreeAsync(p, s);
+      else cudaFree(p);
+    }
     p = nullptr;
     n = 0;
+    s = nullptr;
   }
   ~DevBuf() { free(); }
 };
@@ -74,11 +99,21 @@ struct hg_context {
   cudaStream_t stream = nullptr;
   int refs = 1;
   cudaEvent_t t0 = nullptr, t1 = nullptr;
+  // fences: a ring of events recorded on the stream (hg_context_fence)
+  std::vector<cudaEvent_t> fences;
+  int64_t next_fence = 0;
+  // page-locked 8-byte slots for small asynchronous read-backs; a slot is
+  // reused only by later work on the same stream, after the earlier copy
+  std::vector<uint32_t *> pinned_chunks;
+  std::vector<uint32_t *> pinned_free;
 };
 
 namespace hg {
 void context_retain(hg_context *c);
 void context_release(hg_context *c);
+// two page-locked uint32 words; NULL when page-locked memory is exhausted
+uint32_t *context_pinned_pair(hg_context *c);
+void context_return_pair(hg_context *c, uint32_t *p);
 } // namespace hg
 
 namespace hg {
@@ -188,6 +223,8 @@ hg_status mixed_download(hg_mpm *m, double *q, double *v, double *be,
 hg_status mixed_step(hg_mpm *m, double dt, int nsteps);
 hg_status mixed_download_grid(hg_mpm *m, double *mass, double *vel,
                               double *acc);
+// device bytes mixed_alloc plus the staging of an upload allocate
+int64_t mixed_device_bytes(int nx, int ny, int64_t cap);
 hg_status mixed_profile_read(hg_mpm *m, double *g2p2g_ms, double *update_ms,
                              int64_t *steps);
 
@@ -207,6 +244,8 @@ struct hg_batch {
   cudaEvent_t out_ev = nullptr;
   bool out_pending = false;
   std::vector<hg_mpm *> out_members; // members whose counters are in flight
+  int64_t member_steps = 0, resorts = 0, steps = 0;
+  double host_ms = 0.0;
 };
 
 namespace hg {

@@ -733,6 +733,7 @@ __global__ void kx_download(int64_t n, double gx, double gy, double h, MixedPart
   const float2 vv = src.v[k];
   v[2 * o] = vv.x;
   v[2 * o + 1] = vv.y;
+  if (!be) return; // frames: positions and velocities only
   const float4 s = src.strain[k];
   be[4 * o] = 1.0 + (double)s.y;
   be[4 * o + 1] = (double)s.z;
@@ -885,10 +886,23 @@ hg_status mixed_alloc(hg_mpm *m) {
   HG_CUDA_TRY(cudaMemsetAsync(m->va.p, 0, sizeof(float4) * nn, s));
   HG_CUDA_TRY(cudaMemsetAsync(m->gm.p, 0, sizeof(float) * nn, s));
   HG_CUDA_TRY(cudaMemsetAsync(m->nactive.p, 0, sizeof(int32_t) * 2, s));
-  HG_CUDA_TRY(cudaMallocHost(&m->h_outside, 2 * sizeof(uint32_t)));
+  m->h_outside = context_pinned_pair(m->ctx);
+  if (!m->h_outside) return fail(HG_ERR_OUT_OF_MEMORY, "page-locked host memory");
   m->h_outside[0] = m->h_outside[1] = 0;
   HG_CUDA_TRY(cudaEventCreateWithFlags(&m->outside_ev, cudaEventDisableTiming));
   return HG_OK;
+}
+
+int64_t mixed_device_bytes(int nx, int ny, int64_t cap) {
+  const int64_t nn = (int64_t)(nx + 1) * (ny + 1);
+  const int64_t ntx = (nx + 1 + BIN - 1) / BIN, nty = (ny + 1 + BIN - 1) / BIN;
+  const int64_t nkeys = ntx * nty * BIN_CELLS;
+  const int64_t per_point = sizeof(double2) + 2 * sizeof(float2) + sizeof(float4) + 1 + 4;
+  int64_t b = 2 * cap * per_point + cap * 4;                 // particle pairs, keys
+  b += nn * (2 * sizeof(float4) + 2 * sizeof(float));       // acc4, va, accm, gm
+  b += 4 * (3 * nkeys + 2 + scan_tmp_size(nkeys + 1));      // counts, offsets, cursor
+  b += 4 * (2 * ntx * nty + 4);                             // active lists, counters
+  return b;
 }
 
 hg_status mixed_upload(hg_mpm *m, const double *q, const double *v, const double *mass,
@@ -1038,7 +1052,10 @@ hg_status batch_step(hg_batch *b, int nsteps) {
     for (hg_mpm *m : b->members) {
       hg_status st = HG_OK;
       if (!m->primed) st = prime(m);
-      else if (m->steps_since_rebin >= MAX_STEPS_BETWEEN_REBINS) st = rebin(m);
+      else if (m->steps_since_rebin >= MAX_STEPS_BETWEEN_REBINS) {
+        st = rebin(m);
+        b->resorts++;
+      }
       if (st != HG_OK) return st;
     }
     // per-scene argument tables (buffer pointers change with every re-sort)
@@ -1064,6 +1081,8 @@ hg_status batch_step(hg_batch *b, int nsteps) {
     HG_LAUNCH(kb_g2p2g, nsm * 3, THREADS, 0, s, db, S);
     HG_CHECK_LAUNCH();
     for (hg_mpm *m : b->members) m->steps_since_rebin++;
+    b->member_steps += S;
+    b->steps++;
     if (!b->out_pending) {
       HG_LAUNCH(kb_gather_outside, (S + 127) / 128, 128, 0, s, db, S, b->outside.p);
       HG_CHECK_LAUNCH();

@@ -1,0 +1,87 @@
+"""Asynchronous pieces of the serving path and the serving loop on the GPU.
+
+* fences and frames: a frame copied without waiting equals the synchronous
+  download bit for bit (the same conversion kernel);
+* admission estimate: hg_mpm_estimate_bytes bounds the device bytes an MPM
+  object really holds after upload and downloads, within 10% + 1 MiB;
+* continuous batching: every request's frames (front run-out per 100 steps)
+  equal those of the same scene served alone within 1e-9 m (FP32 atomic
+  summation order is the only difference).
+"""
+import numpy as np
+import pytest
+
+import libhybridgrains_gb300 as hg
+from libhybridgrains_gb300 import scenes, serving
+
+pytestmark = pytest.mark.gpu
+
+
+def build(ctx, cfg, n):
+    return hg.MPM(ctx, cfg["grid_min"], cfg["grid_max"], cfg["h"], cfg["shear_modulus"],
+                  cfg["bulk_modulus"], cfg["dp_alpha"], cfg["flip_alpha"], scenes.GRAVITY,
+                  cfg["planes"], capacity=n)
+
+
+def test_async_upload_and_frame_match_sync_download(ctx):
+    cfg = scenes.serving_column(20000, 2.0, 30.0)
+    p = scenes.seed_column_points(cfg)
+    n = len(p["m"])
+    host = {k: hg.pinned(p[k].shape) for k in ("q", "v", "m", "vol")}
+    for k in host:
+        host[k][...] = p[k]
+    m = build(ctx, cfg, n)
+    m.upload_async(host["q"], host["v"], host["m"], host["vol"])
+    f0 = ctx.fence()
+    m.flow(cfg["dt"], 50)
+    q, v = hg.pinned((n, 2)), hg.pinned((n, 2))
+    m.frame_async(q, v)
+    f1 = ctx.fence()
+    assert f1 == f0 + 1
+    ctx.fence_wait(f1)
+    assert ctx.fence_done(f0) and ctx.fence_done(f1)
+    ref = m.download()
+    assert np.array_equal(q, ref["q"]) and np.array_equal(v, ref["v"])
+    assert np.abs(ref["q"] - p["q"]).max() > 0  # it moved
+    with pytest.raises(hg.HGError):
+        ctx.fence_done(f1 + 5)
+
+
+def test_estimate_bounds_device_bytes(ctx):
+    cfg = scenes.serving_column(100000, 1.0, 30.0)
+    p = scenes.seed_column_points(cfg)
+    n = len(p["m"])
+    ctx.synchronize()
+    b0 = ctx.device_bytes()
+    m = build(ctx, cfg, n)
+    m.upload(p["q"], p["v"], p["m"], p["vol"])
+    m.flow(cfg["dt"], 2)
+    m.download()
+    m.grid()
+    ctx.synchronize()
+    used = ctx.device_bytes() - b0
+    est = hg.mpm_estimate_bytes(cfg["grid_min"], cfg["grid_max"], cfg["h"], n)
+    assert used > 0
+    assert est >= used, (est, used)
+    assert est <= 1.1 * used + 2**20, (est, used)
+    m.close()
+
+
+def test_serving_results_match_scenes_served_alone(ctx):
+    reqs = serving.column_requests(n=6, rate=400.0, seed=11, steps=300, nmax=3.0e4)
+    for r, t in zip(reqs, (0.0, 0.0, 0.0, 0.002, 0.004, 0.006)):
+        r.arrival = t  # three at once, three while those run
+    alone = [serving.Request(r.rid, r.arrival, r.cfg, r.npoints, r.steps, r.frame_every, r.dt)
+             for r in reqs]
+    be = serving.DeviceBackend(ctx, max_members=8)
+    srv = serving.Server(be, 2**33, max_members=8)
+    srv.run(reqs)
+    be.shutdown()
+    serving.run_one_at_a_time(ctx, alone)
+    assert srv.peak_members >= 2  # they overlapped on the device
+    for a, b in zip(reqs, alone):
+        assert [s for s, _ in a.frames] == [100, 200, 300]
+        assert [s for s, _ in b.frames] == [100, 200, 300]
+        for (_, x), (_, y) in zip(a.frames, b.frames):
+            assert abs(x - y) <= 1e-9
+        assert a.finished >= a.admitted >= a.arrival
