@@ -144,6 +144,17 @@ hg_status hg_mpm_seed_rectangle(hg_mpm *m, const double rmin[2],
                                 double *mass, double *volume, double *hl,
                                 int64_t *count);
 
+/* hg_mpm_seed_rectangle followed by hg_mpm_upload_async of its points
+ * (be_bar = I, J = 1), with the points generated on the device: bit-identical
+ * to the host version and queued without host data or waiting. *count gets
+ * the number of points; more than the capacity is HG_ERR_CAPACITY and
+ * changes nothing. For scenes described by their geometry (many small
+ * scenes admitted while others step); no counterpart in the reference. */
+hg_status hg_mpm_seed_rectangle_device(hg_mpm *m, const double rmin[2],
+                                       const double rmax[2], double density,
+                                       int32_t samples_per_dim, const double vel[2],
+                                       double omega, int64_t *count);
+
 /* MaterialPoints::setPoints (mpmgrains2d/MaterialPoints.cpp). Optional
  * arrays may be NULL: be_bar = I, J = 1, just_homogenized = 0,
  * kinematic = 0. */
@@ -231,9 +242,17 @@ hg_status hg_batch_size(hg_batch *b, int32_t *n);
 /* nsteps steps of every member (ExplicitIntegrator::flow per member). */
 hg_status hg_batch_step(hg_batch *b, int32_t nsteps);
 /* Counters since creation: member-steps queued, member re-sorts, batch
- * steps, and host milliseconds spent inside hg_batch_step. */
+ * steps, host milliseconds spent inside hg_batch_step and, of those, the
+ * milliseconds it waited for the device (argument tables in use). */
 hg_status hg_batch_stats(hg_batch *b, int64_t *member_steps, int64_t *resorts,
-                         int64_t *steps, double *host_ms);
+                         int64_t *steps, double *host_ms, double *wait_ms);
+/* Measurement hooks: CUDA events around each phase of every batch step
+ * while enabled (enabling clears earlier records); _read synchronises and
+ * returns the summed milliseconds of re-sorts, argument-table copies, grid
+ * updates and fused launches, and the number of steps recorded. */
+hg_status hg_batch_profile(hg_batch *b, int32_t enable);
+hg_status hg_batch_profile_read(hg_batch *b, double *resort_ms, double *table_ms,
+                                double *update_ms, double *fused_ms, int64_t *steps);
 
 /* ---- DEM (rigidbody2d, penalty map) --------------------------------------- */
 

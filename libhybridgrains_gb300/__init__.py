@@ -208,6 +208,17 @@ class MPM:
               _d(hl), ctypes.byref(cnt))
         return dict(q=q, v=v, m=m, vol=vol, hl=hl)
 
+    def seed_rectangle_device(self, rmin, rmax, density, samples_per_dim, vel=(0.0, 0.0),
+                              omega=0.0):
+        """seed_rectangle + upload with the points generated on the device
+        (hg_mpm_seed_rectangle_device); returns the point count."""
+        cnt = ctypes.c_int64()
+        rmin, rmax, vel = _f64(rmin), _f64(rmax), _f64(vel)
+        check("hg_mpm_seed_rectangle_device", self._h, _d(rmin), _d(rmax), float(density),
+              int(samples_per_dim), _d(vel), float(omega), ctypes.byref(cnt))
+        self.n = cnt.value
+        return self.n
+
     def upload(self, q, v, m, vol, hl=None, be=None, J=None, jh=None, kin=None):
         """MaterialPoints::setPoints. q, v: (N, 2); be: (N, 4) column-major."""
         q, v, m, vol = _f64(q), _f64(v), _f64(m), _f64(vol)
@@ -461,12 +472,24 @@ class Batch:
         check("hg_batch_step", self._h, int(nsteps))
 
     def stats(self):
-        """(member-steps, re-sorts, batch steps, host ms inside hg_batch_step)."""
+        """(member-steps, re-sorts, batch steps, host ms inside hg_batch_step,
+        of which ms waiting for the device)."""
         a, r, s = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
-        h = ctypes.c_double()
+        h, w = ctypes.c_double(), ctypes.c_double()
         check("hg_batch_stats", self._h, ctypes.byref(a), ctypes.byref(r), ctypes.byref(s),
-              ctypes.byref(h))
-        return a.value, r.value, s.value, h.value
+              ctypes.byref(h), ctypes.byref(w))
+        return a.value, r.value, s.value, h.value, w.value
+
+    def profile(self, enable=True):
+        check("hg_batch_profile", self._h, 1 if enable else 0)
+
+    def profile_read(self):
+        """dict of summed ms per phase (resort, table, update, fused) and steps."""
+        v = [ctypes.c_double() for _ in range(4)]
+        n = ctypes.c_int64()
+        check("hg_batch_profile_read", self._h, *[ctypes.byref(x) for x in v], ctypes.byref(n))
+        return dict(resort_ms=v[0].value, table_ms=v[1].value, update_ms=v[2].value,
+                    fused_ms=v[3].value, steps=n.value)
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:

@@ -98,6 +98,7 @@ SIGNATURES = {
     "hg_context_device_bytes": [_P, _I64],
     "hg_host_alloc": [_i64, _PP],
     "hg_host_free": [_P],
+    "hg_mpm_seed_rectangle_device": [_P, _D, _D, _dbl, _i32, _D, _dbl, _I64],
     "hg_mpm_upload_async": [_P, _i64, _D, _D, _D, _D, _D, _D, _D, _I32, _U8],
     "hg_mpm_frame_async": [_P, _D, _D],
     "hg_mpm_estimate_bytes": [ctypes.POINTER(MpmDesc), _I64],
@@ -107,7 +108,9 @@ SIGNATURES = {
     "hg_batch_remove": [_P, _P],
     "hg_batch_size": [_P, _I32],
     "hg_batch_step": [_P, _i32],
-    "hg_batch_stats": [_P, _I64, _I64, _I64, _D],
+    "hg_batch_stats": [_P, _I64, _I64, _I64, _D, _D],
+    "hg_batch_profile": [_P, _i32],
+    "hg_batch_profile_read": [_P, _D, _D, _D, _D, _I64],
     "hg_dem_create": [_P, ctypes.POINTER(DemDesc), _PP],
     "hg_dem_destroy": [_P],
     "hg_dem_upload": [_P, _i64, _D, _D, _D, _D, _D, _U8],

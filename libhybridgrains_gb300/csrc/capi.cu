@@ -103,7 +103,8 @@ bool finite_all(const double *a, int k) {
 template <typename T>
 hg_status h2d(cudaStream_t s, T *dst, const T *src, size_t n) {
   if (n == 0) return HG_OK;
-  HG_CUDA_TRY(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyHostToDevice, s));
+  // cudaMemcpyDefault: the source may be host or device memory
+  HG_CUDA_TRY(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDefault, s));
   return HG_OK;
 }
 
@@ -145,6 +146,60 @@ __global__ void k_cells_mixed(int64_t n, const double2 *__restrict__ u,
 }
 
 // PhysicsGrid::setDimensions (mpmgrains2d/PhysicsGrid.cpp:14-55).
+// Device version of the rasterizeRectangle lattice (InitialSimulationState.
+// cpp:48-145): lattice point k = ((gy * nbx + gx) * npd + cy) * npd + cx in
+// the host loop order, with the same FP64 expressions (this file is compiled
+// without FMA contraction, like the host code), so positions are
+// bit-identical to hg_mpm_seed_rectangle.
+struct SeedLattice {
+  double rmin[2], rmax[2], vel[2], omega, ctr[2], pmass, pvol, half;
+  unsigned bx0, by0, nbx, nby;
+  int npd;
+};
+
+__device__ __forceinline__ bool seed_point(const MpmParams &P, const SeedLattice &L, int64_t k,
+                                           double &px, double &py) {
+  const int npd = L.npd;
+  const int cx = (int)(k % npd), cy = (int)((k / npd) % npd);
+  const int64_t cell = k / ((int64_t)npd * npd);
+  const unsigned gx = L.bx0 + (unsigned)(cell % L.nbx), gy = L.by0 + (unsigned)(cell / L.nbx);
+  px = P.gmin[0] + P.h * ((double)gx + ((double)cx + 0.5) / (double)npd);
+  py = P.gmin[1] + P.h * ((double)gy + ((double)cy + 0.5) / (double)npd);
+  if (px < L.rmin[0] || py < L.rmin[1] || px > L.rmax[0] || py > L.rmax[1]) return false;
+  for (int i = 0; i < P.nplanes; ++i) { // pointInsidePlane
+    const MpmPlaneDev &pl = P.planes[i];
+    if (py < pl.lower_bound) break;
+    if (pl.n[0] * (px - pl.x[0]) + pl.n[1] * (py - pl.x[1]) < 0.0) return false;
+  }
+  return true;
+}
+
+__global__ void k_seed_keep(MpmParams P, SeedLattice L, int64_t total, int32_t *keep) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k > total) return;
+  double px, py;
+  keep[k] = k < total && seed_point(P, L, k, px, py) ? 1 : 0;
+}
+
+__global__ void k_seed_write(MpmParams P, SeedLattice L, int64_t total, int64_t count,
+                             const int32_t *__restrict__ keep, const int32_t *__restrict__ off,
+                             double *q, double *v, double *mass, double *vol, double *hl) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= total || !keep[k]) return;
+  const int64_t o = off[k];
+  if (o >= count) return;
+  double px, py;
+  seed_point(P, L, k, px, py);
+  const double ax = px - L.ctr[0], ay = py - L.ctr[1];
+  q[2 * o] = px;
+  q[2 * o + 1] = py;
+  v[2 * o] = L.vel[0] + L.omega * (-ay);
+  v[2 * o + 1] = L.vel[1] + L.omega * ax;
+  mass[o] = L.pmass;
+  vol[o] = L.pvol;
+  hl[o] = L.half;
+}
+
 void set_dimensions(MpmParams &P, const double gmin[2], const double gmax[2], double h) {
   const double cx = 0.5 * (gmin[0] + gmax[0]), cy = 0.5 * (gmin[1] + gmax[1]);
   double wx = gmax[0] - gmin[0], wy = gmax[1] - gmin[1];
@@ -519,6 +574,64 @@ hg_status hg_mpm_seed_rectangle(hg_mpm *m, const double rmin[2], const double rm
 static hg_status upload_impl(hg_mpm *m, int64_t n, const double *q, const double *v,
                              const double *mass, const double *volume, const double *hl,
                              const double *be, const double *J, const int32_t *jh,
+                             const uint8_t *kin, bool wait);
+
+hg_status hg_mpm_seed_rectangle_device(hg_mpm *m, const double rmin[2], const double rmax[2],
+                                       double rho, int32_t npd, const double vel[2],
+                                       double omega, int64_t *count) {
+  if (!m || !rmin || !rmax || !count) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  // the count, and the argument checks, of the host version
+  hg_status st = hg_mpm_seed_rectangle(m, rmin, rmax, rho, npd, vel, omega, 0, nullptr,
+                                       nullptr, nullptr, nullptr, nullptr, count);
+  if (st != HG_OK) return st;
+  const int64_t n = *count;
+  if (n > m->cap) return fail(HG_ERR_CAPACITY, "seeded points exceed the capacity");
+  const MpmParams &P = m->p;
+  SeedLattice L{};
+  L.rmin[0] = rmin[0];
+  L.rmin[1] = rmin[1];
+  L.rmax[0] = rmax[0];
+  L.rmax[1] = rmax[1];
+  L.vel[0] = vel ? vel[0] : 0.0;
+  L.vel[1] = vel ? vel[1] : 0.0;
+  L.omega = omega;
+  L.ctr[0] = 0.5 * (rmin[0] + rmax[0]);
+  L.ctr[1] = 0.5 * (rmin[1] + rmax[1]);
+  L.half = 0.5 * P.h / (double)npd;
+  L.pvol = L.half * L.half * 4.0;
+  L.pmass = rho * L.pvol;
+  L.bx0 = (unsigned)std::floor((rmin[0] - P.gmin[0]) / P.h);
+  L.by0 = (unsigned)std::floor((rmin[1] - P.gmin[1]) / P.h);
+  const unsigned bx1 = (unsigned)std::ceil((rmax[0] - P.gmin[0]) / P.h);
+  const unsigned by1 = (unsigned)std::ceil((rmax[1] - P.gmin[1]) / P.h);
+  L.nbx = bx1 > L.bx0 ? bx1 - L.bx0 : 0;
+  L.nby = by1 > L.by0 ? by1 - L.by0 : 0;
+  L.npd = npd;
+  const int64_t total = (int64_t)L.nbx * L.nby * npd * npd;
+  if (total + 1 > (int64_t)INT32_MAX) return fail(HG_ERR_INVALID_ARGUMENT, "rectangle too large");
+  DeviceGuard g(m->ctx);
+  cudaStream_t s = m->ctx->stream;
+  DevBuf<int32_t> keep, off, tmp;
+  DevBuf<double> pts;
+  if ((st = keep.alloc(total + 1)) || (st = off.alloc(total + 1)) ||
+      (st = tmp.alloc(scan_tmp_size(total + 1))) || (st = pts.alloc(7 * std::max<int64_t>(n, 1))))
+    return st;
+  HG_LAUNCH(k_seed_keep, (int)((total + 256) / 256), 256, 0, s, P, L, total, keep.p);
+  HG_CHECK_LAUNCH();
+  if ((st = exclusive_scan_i32(keep.p, off.p, total + 1, tmp.p, s))) return st;
+  double *q = pts.p, *v = q + 2 * n, *ms = v + 2 * n, *vol = ms + n, *hl = vol + n;
+  if (total > 0) {
+    HG_LAUNCH(k_seed_write, (int)((total + 255) / 256), 256, 0, s, P, L, total, n, keep.p,
+              off.p, q, v, ms, vol, hl);
+    HG_CHECK_LAUNCH();
+  }
+  // scratch is released stream-ordered after the upload's copies
+  return upload_impl(m, n, q, v, ms, vol, hl, nullptr, nullptr, nullptr, nullptr, false);
+}
+
+static hg_status upload_impl(hg_mpm *m, int64_t n, const double *q, const double *v,
+                             const double *mass, const double *volume, const double *hl,
+                             const double *be, const double *J, const int32_t *jh,
                              const uint8_t *kin, bool wait) {
   if (!m) return fail(HG_ERR_INVALID_ARGUMENT, "m is NULL");
   if (n < 0) return fail(HG_ERR_INVALID_ARGUMENT, "negative particle count");
@@ -861,6 +974,7 @@ hg_status hg_batch_add(hg_batch *b, hg_mpm *m, double dt) {
   if ((int)b->members.size() >= b->max_members) return fail(HG_ERR_CAPACITY, "batch is full");
   b->members.push_back(m);
   b->dts.push_back(dt);
+  b->dirty = true;
   return HG_OK;
 }
 
@@ -870,6 +984,7 @@ hg_status hg_batch_remove(hg_batch *b, hg_mpm *m) {
     if (b->members[i] == m) {
       b->members.erase(b->members.begin() + i);
       b->dts.erase(b->dts.begin() + i);
+      b->dirty = true;
       // its counters may still be in flight: forget the object, keep the slot
       for (hg_mpm *&x : b->out_members)
         if (x == m) x = nullptr;
@@ -894,13 +1009,35 @@ hg_status hg_batch_step(hg_batch *b, int32_t nsteps) {
   return st;
 }
 
+hg_status hg_batch_profile(hg_batch *b, int32_t enable) {
+  if (!b) return fail(HG_ERR_INVALID_ARGUMENT, "b is NULL");
+  b->profile = enable != 0;
+  if (b->profile) b->prof_used = 0;
+  return HG_OK;
+}
+
+hg_status hg_batch_profile_read(hg_batch *b, double *resort_ms, double *table_ms,
+                                double *update_ms, double *fused_ms, int64_t *steps) {
+  if (!b) return fail(HG_ERR_INVALID_ARGUMENT, "b is NULL");
+  DeviceGuard g(b->ctx);
+  double ms[hg_batch::PROF_PHASES];
+  hg_status st = batch_profile_read(b, ms, steps);
+  if (st != HG_OK) return st;
+  if (resort_ms) *resort_ms = ms[0];
+  if (table_ms) *table_ms = ms[1];
+  if (update_ms) *update_ms = ms[2];
+  if (fused_ms) *fused_ms = ms[3];
+  return HG_OK;
+}
+
 hg_status hg_batch_stats(hg_batch *b, int64_t *member_steps, int64_t *resorts, int64_t *steps,
-                         double *host_ms) {
+                         double *host_ms, double *wait_ms) {
   if (!b) return fail(HG_ERR_INVALID_ARGUMENT, "b is NULL");
   if (member_steps) *member_steps = b->member_steps;
   if (resorts) *resorts = b->resorts;
   if (steps) *steps = b->steps;
   if (host_ms) *host_ms = b->host_ms;
+  if (wait_ms) *wait_ms = b->wait_ms;
   return HG_OK;
 }
 

@@ -231,27 +231,53 @@ hg_status mixed_profile_read(hg_mpm *m, double *g2p2g_ms, double *update_ms,
 } // namespace hg
 
 struct hg_batch {
+  static constexpr int NBUF = 4;        // page-locked argument tables in flight
+  static constexpr int PROF_PHASES = 4; // re-sorts, table copy, grid update, fused
+  struct Sig { // what an argument-table entry depends on
+    hg_mpm *m = nullptr;
+    int cur = -1;
+    int64_t n = -1;
+    double dt = 0.0;
+    bool operator==(const Sig &o) const {
+      return m == o.m && cur == o.cur && n == o.n && dt == o.dt;
+    }
+  };
   hg_context *ctx = nullptr;
   int max_members = 0;
   std::vector<hg_mpm *> members;
   std::vector<double> dts;
-  hg::DevBuf<unsigned char> table; // [bins | tiles] per-scene argument tables
-  unsigned char *h_table[2] = {nullptr, nullptr}; // pinned, double-buffered
-  cudaEvent_t table_ev[2] = {nullptr, nullptr};
+  std::vector<Sig> sigs;
+  std::vector<unsigned char> args; // host copy of the argument table
+  bool dirty = true;
+  hg::DevBuf<unsigned char> table; // [update args | fused args] per member
+  unsigned char *h_table[NBUF] = {};
+  cudaEvent_t table_ev[NBUF] = {};
   int tb = 0;
+  // batched re-sort: members due this step and their argument tables
+  std::vector<hg_mpm *> due;
+  hg::DevBuf<unsigned char> rtable;
+  unsigned char *h_rtable[NBUF] = {};
+  cudaEvent_t rtable_ev[NBUF] = {};
+  int rb = 0;
   hg::DevBuf<uint32_t> outside; // 2 counters per member
   uint32_t *h_outside = nullptr;
   cudaEvent_t out_ev = nullptr;
   bool out_pending = false;
   std::vector<hg_mpm *> out_members; // members whose counters are in flight
   int64_t member_steps = 0, resorts = 0, steps = 0;
-  double host_ms = 0.0;
+  double host_ms = 0.0, wait_ms = 0.0; // wait: host blocked on the device
+  bool profile = false;
+  std::vector<cudaEvent_t> prof_events; // PROF_PHASES + 1 per step
+  size_t prof_used = 0;
 };
 
 namespace hg {
 hg_status batch_alloc(hg_batch *b);
 void batch_free(hg_batch *b);
 hg_status batch_step(hg_batch *b, int nsteps);
+// per-phase milliseconds [re-sorts, table copy, grid update, fused] summed
+// over the profiled steps
+hg_status batch_profile_read(hg_batch *b, double *ms, int64_t *steps);
 
 // ---- DEM ---------------------------------------------------------------------
 

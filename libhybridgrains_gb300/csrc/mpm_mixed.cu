@@ -37,6 +37,11 @@
 // their window are still handled exactly (G2P from global velocity, P2G with
 // global atomics), so the re-sort cadence affects speed only.
 #include "hg_internal.cuh"
+#include "scan_block.cuh"
+
+#include <chrono>
+#include <cstddef>
+#include <cstring>
 
 #include <cmath>
 
@@ -47,7 +52,7 @@ namespace {
 constexpr int THREADS = 256;
 constexpr int MAX_BATCH = HG_MAX_BATCH; // scenes per batched launch
 
-struct MixedArgs {
+struct alignas(16) MixedArgs {
   int nx, ny, ntx, nty;
   int64_t n;
   float dt, inv_h, kappa, mu, dp_alpha, flip_alpha, gx, gy;
@@ -55,7 +60,6 @@ struct MixedArgs {
   // plane test is redone exactly in FP64.
   float pmargin;
   int nplanes;
-  MpmPlaneDev planes[HG_MAX_PLANES];
   const int32_t *offsets;
   const int32_t *active;  // active bins or tiles
   const int32_t *nactive; // device count
@@ -71,6 +75,8 @@ struct MixedArgs {
   float *gm;
   uint32_t *status;
   uint32_t *outside;
+  // last, so that a batched kernel copies only the nplanes planes in use
+  MpmPlaneDev planes[HG_MAX_PLANES];
 };
 
 // Exact floor(u) and the fraction u - floor(u) truncated to 24 bits, using
@@ -524,11 +530,32 @@ __device__ __forceinline__ void batch_prefix(const MixedArgs *slots, int nslots,
   int run = off + x - sum;
 #pragma unroll
   for (int j = 0; j < PER; ++j) {
-    const int s = threadIdx.x * PER + j;
-    if (s <= MAX_BATCH) prefix[s] = run;
+    prefix[threadIdx.x * PER + j] = run;
     run += v[j];
   }
+  if (threadIdx.x == THREADS - 1) prefix[THREADS * PER] = run;
   __syncthreads();
+}
+
+constexpr int PREFIX_LEN = ((MAX_BATCH + THREADS - 1) / THREADS) * THREADS + 1;
+
+// Copies slot s's arguments into shared memory with all threads, up to the
+// planes in use (the arguments end with the plane array).
+__device__ __forceinline__ void load_slot(const MixedArgs *slots, int s, MixedArgs &A) {
+  __syncthreads(); // the previous tile is done with A
+  const int words = (int)((offsetof(MixedArgs, planes) +
+                           (size_t)slots[s].nplanes * sizeof(MpmPlaneDev) + 15) / 16);
+  const int4 *src = reinterpret_cast<const int4 *>(slots + s);
+  int4 *dst = reinterpret_cast<int4 *>(&A);
+  for (int w = threadIdx.x; w < words; w += blockDim.x) dst[w] = src[w];
+  __syncthreads();
+}
+
+// This CTA's contiguous share [begin, end) of the batch's work items, so
+// that a CTA crosses few scene boundaries.
+__device__ __forceinline__ void cta_range(int total, int &begin, int &end) {
+  begin = (int)((int64_t)total * blockIdx.x / gridDim.x);
+  end = (int)((int64_t)total * (blockIdx.x + 1) / gridDim.x);
 }
 
 __device__ __forceinline__ int batch_slot(const int *prefix, int nslots, int item) {
@@ -546,17 +573,17 @@ __global__ void __launch_bounds__(THREADS, 3) kb_g2p2g(const MixedArgs *__restri
                                                      int nslots) {
   __shared__ FusedSmem S;
   __shared__ MixedArgs A;
-  __shared__ int prefix[MAX_BATCH + 1];
+  __shared__ int prefix[PREFIX_LEN];
   batch_prefix(slots, nslots, prefix);
-  const int total = prefix[nslots];
-  int cur = -1;
-  for (int item = blockIdx.x; item < total; item += gridDim.x) {
-    const int s = batch_slot(prefix, nslots, item);
-    if (s != cur) {
-      __syncthreads();
-      if (threadIdx.x == 0) A = slots[s];
-      __syncthreads();
-      cur = s;
+  int begin, end;
+  cta_range(prefix[nslots], begin, end);
+  if (begin >= end) return;
+  int s = batch_slot(prefix, nslots, begin);
+  load_slot(slots, s, A);
+  for (int item = begin; item < end; ++item) {
+    if (item >= prefix[s + 1]) {
+      do ++s; while (item >= prefix[s + 1]);
+      load_slot(slots, s, A);
     }
     fused_tile<false>(A, A.active[item - prefix[s]], S);
   }
@@ -619,17 +646,17 @@ __global__ void __launch_bounds__(THREADS) kx_grid_update(const __grid_constant_
 __global__ void __launch_bounds__(THREADS) kb_grid_update(const MixedArgs *__restrict__ slots,
                                                           int nslots) {
   __shared__ MixedArgs A;
-  __shared__ int prefix[MAX_BATCH + 1];
+  __shared__ int prefix[PREFIX_LEN];
   batch_prefix(slots, nslots, prefix);
-  const int total = prefix[nslots];
-  int cur = -1;
-  for (int item = blockIdx.x; item < total; item += gridDim.x) {
-    const int s = batch_slot(prefix, nslots, item);
-    if (s != cur) {
-      __syncthreads();
-      if (threadIdx.x == 0) A = slots[s];
-      __syncthreads();
-      cur = s;
+  int begin, end;
+  cta_range(prefix[nslots], begin, end);
+  if (begin >= end) return;
+  int s = batch_slot(prefix, nslots, begin);
+  load_slot(slots, s, A);
+  for (int item = begin; item < end; ++item) {
+    if (item >= prefix[s + 1]) {
+      do ++s; while (item >= prefix[s + 1]);
+      load_slot(slots, s, A);
     }
     update_tile(A, A.active[item - prefix[s]]);
   }
@@ -700,6 +727,187 @@ __global__ void kx_active(int ntx, int nty, const int32_t *__restrict__ offsets,
       }
     }
   if (any) tiles[atomicAdd(&nactive[1], 1)] = b;
+}
+
+// ---- batched re-sort -------------------------------------------------------------
+//
+// The re-sort of every batch member that needs one in a step, in six launches
+// whatever their number: the same counting sort as above, over (member, item)
+// work items. The host lays out, per member, the item counts of each pass as
+// prefix sums (points, keys, scan chunks, bins); a thread finds its member by
+// binary search over them.
+
+struct RebinArgs {
+  int64_t n;
+  int nx, ny, ntx, nty;
+  MixedParticles src, dst;
+  int32_t *keys, *counts, *offsets, *cursor, *bins, *tiles, *nactive, *chunk_sums;
+  uint32_t *status, *outside;
+};
+
+struct RebinPrefix {
+  const int64_t *pts, *keys, *chunks, *bins; // nmem + 1 each
+  int nmem;
+};
+
+constexpr int RB_CHUNK = 2048; // elements per scan chunk (256 threads x 8)
+
+__device__ __forceinline__ int member_of(const int64_t *pre, int nmem, int64_t item) {
+  int lo = 0, hi = nmem - 1;
+  while (lo < hi) { // largest m with pre[m] <= item
+    const int mid = (lo + hi + 1) >> 1;
+    if (pre[mid] <= item) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void kr_clear(const RebinArgs *__restrict__ R, RebinPrefix P) {
+  const int64_t total = P.keys[P.nmem];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int m = member_of(P.keys, P.nmem, i);
+    const int64_t j = i - P.keys[m]; // 0 .. nkeys
+    const RebinArgs &a = R[m];
+    a.counts[j] = 0;
+    const int64_t nkeys = P.keys[m + 1] - P.keys[m] - 1;
+    if (j < nkeys) a.cursor[j] = 0;
+    if (j < 2) {
+      a.nactive[j] = 0;
+      a.outside[j] = 0;
+    }
+  }
+}
+
+__global__ void kr_keys(const RebinArgs *__restrict__ R, RebinPrefix P) {
+  const int64_t total = P.pts[P.nmem];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int m = member_of(P.pts, P.nmem, i);
+    const int64_t p = i - P.pts[m];
+    const RebinArgs &a = R[m];
+    // the cell key of kx_keys
+    const double2 up = a.src.u[p];
+    int cx = (int)floor(up.x), cy = (int)floor(up.y);
+    if (!(up.x >= 0.0 && up.y >= 0.0 && cx < a.nx && cy < a.ny)) {
+      atomicOr(a.status, (uint32_t)HG_STATUS_OUT_OF_GRID);
+      cx = min(max(cx, 0), a.nx - 1);
+      cy = min(max(cy, 0), a.ny - 1);
+    }
+    const int key = ((cy / BIN) * a.ntx + cx / BIN) * BIN_CELLS + (cy % BIN) * BIN + (cx % BIN);
+    a.keys[p] = key;
+    atomicAdd(&a.counts[key], 1);
+  }
+}
+
+// One CTA per (member, chunk): the chunk's sum of counts.
+__global__ void __launch_bounds__(THREADS) kr_chunk_sums(const RebinArgs *__restrict__ R,
+                                                         RebinPrefix P) {
+  const int64_t total = P.chunks[P.nmem];
+  for (int64_t blk = blockIdx.x; blk < total; blk += gridDim.x) {
+    const int m = member_of(P.chunks, P.nmem, blk);
+    const int64_t c = blk - P.chunks[m];
+    const int64_t n = P.keys[m + 1] - P.keys[m]; // nkeys + 1
+    const RebinArgs &a = R[m];
+    int s = 0;
+    for (int k = 0; k < RB_CHUNK / THREADS; ++k) {
+      const int64_t i = c * RB_CHUNK + k * THREADS + threadIdx.x;
+      if (i < n) s += a.counts[i];
+    }
+    int tot;
+    block_excl_scan<THREADS>(s, &tot);
+    if (threadIdx.x == 0) a.chunk_sums[c] = tot;
+  }
+}
+
+// One CTA per member: exclusive scan of its chunk sums, in place.
+__global__ void __launch_bounds__(THREADS) kr_chunk_scan(const RebinArgs *__restrict__ R,
+                                                         RebinPrefix P) {
+  for (int m = blockIdx.x; m < P.nmem; m += gridDim.x) {
+    const int64_t nch = P.chunks[m + 1] - P.chunks[m];
+    int32_t *cs = R[m].chunk_sums;
+    int carry = 0;
+    for (int64_t base = 0; base < nch; base += THREADS) {
+      const int64_t i = base + threadIdx.x;
+      const int v = i < nch ? cs[i] : 0;
+      int tot;
+      const int ex = block_excl_scan<THREADS>(v, &tot);
+      if (i < nch) cs[i] = carry + ex;
+      carry += tot;
+    }
+  }
+}
+
+// One CTA per (member, chunk): offsets = exclusive scan of counts.
+__global__ void __launch_bounds__(THREADS) kr_chunk_scan_apply(const RebinArgs *__restrict__ R,
+                                                               RebinPrefix P) {
+  constexpr int ITEMS = RB_CHUNK / THREADS;
+  const int64_t total = P.chunks[P.nmem];
+  for (int64_t blk = blockIdx.x; blk < total; blk += gridDim.x) {
+    const int m = member_of(P.chunks, P.nmem, blk);
+    const int64_t c = blk - P.chunks[m];
+    const int64_t n = P.keys[m + 1] - P.keys[m];
+    const RebinArgs &a = R[m];
+    int v[ITEMS];
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) {
+      const int64_t i = c * RB_CHUNK + (int64_t)threadIdx.x * ITEMS + k;
+      v[k] = i < n ? a.counts[i] : 0;
+      s += v[k];
+    }
+    int tot;
+    int run = block_excl_scan<THREADS>(s, &tot) + a.chunk_sums[c];
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) {
+      const int64_t i = c * RB_CHUNK + (int64_t)threadIdx.x * ITEMS + k;
+      if (i < n) a.offsets[i] = run;
+      run += v[k];
+    }
+  }
+}
+
+__global__ void kr_scatter(const RebinArgs *__restrict__ R, RebinPrefix P) {
+  const int64_t total = P.pts[P.nmem];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int m = member_of(P.pts, P.nmem, i);
+    const int64_t p = i - P.pts[m];
+    const RebinArgs &a = R[m];
+    const int key = a.keys[p];
+    const int64_t d = a.offsets[key] + atomicAdd(&a.cursor[key], 1);
+    a.dst.u[d] = a.src.u[p];
+    a.dst.v[d] = a.src.v[p];
+    a.dst.mv[d] = a.src.mv[p];
+    a.dst.strain[d] = a.src.strain[p];
+    a.dst.flags[d] = a.src.flags[p];
+    a.dst.id[d] = a.src.id[p];
+  }
+}
+
+__global__ void kr_active(const RebinArgs *__restrict__ R, RebinPrefix P) {
+  const int64_t total = P.bins[P.nmem];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int m = member_of(P.bins, P.nmem, i);
+    const int b = (int)(i - P.bins[m]);
+    const RebinArgs &a = R[m];
+    const int32_t *off = a.offsets;
+    auto count = [&](int t) { return off[(t + 1) * BIN_CELLS] - off[t * BIN_CELLS]; };
+    if (count(b) > 0) a.bins[atomicAdd(&a.nactive[0], 1)] = b;
+    const int tx = b % a.ntx, ty = b / a.ntx;
+    bool any = false;
+    for (int dy = -1; dy <= 1 && !any; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        const int x = tx + dx, y = ty + dy;
+        if (x < 0 || y < 0 || x >= a.ntx || y >= a.nty) continue;
+        if (count(y * a.ntx + x) > 0) {
+          any = true;
+          break;
+        }
+      }
+    if (any) a.tiles[atomicAdd(&a.nactive[1], 1)] = b;
+  }
 }
 
 // ---- upload / download conversion -------------------------------------------
@@ -835,6 +1043,82 @@ hg_status rebin(hg_mpm *m) {
   m->steps_since_rebin = 0;
   m->outside_pending = false;
   m->rebins++;
+  return HG_OK;
+}
+
+// Space for the batched re-sort's argument table of up to nmax members.
+size_t rebin_table_bytes(int nmax) {
+  return (size_t)nmax * sizeof(RebinArgs) + 4 * (size_t)(nmax + 1) * sizeof(int64_t);
+}
+
+// Re-sorts the given members in six launches. table: page-locked host staging
+// (rebin_table_bytes), dtable: its device copy; both free to overwrite.
+hg_status rebin_batch(hg_context *ctx, const std::vector<hg_mpm *> &R, unsigned char *table,
+                      unsigned char *dtable) {
+  cudaStream_t s = ctx->stream;
+  const int nm = (int)R.size();
+  RebinArgs *args = reinterpret_cast<RebinArgs *>(table);
+  int64_t *pre = reinterpret_cast<int64_t *>(table + (size_t)nm * sizeof(RebinArgs));
+  int64_t *pp = pre, *pk = pre + (nm + 1), *pc = pre + 2 * (nm + 1), *pb = pre + 3 * (nm + 1);
+  pp[0] = pk[0] = pc[0] = pb[0] = 0;
+  int64_t max_items = 0;
+  for (int i = 0; i < nm; ++i) {
+    hg_mpm *m = R[i];
+    const int64_t nkeys = (int64_t)m->ntx * m->nty * BIN_CELLS;
+    RebinArgs &a = args[i];
+    a.n = m->n;
+    a.nx = m->p.nx;
+    a.ny = m->p.ny;
+    a.ntx = m->ntx;
+    a.nty = m->nty;
+    a.src = parts(m, m->cur);
+    a.dst = parts(m, 1 - m->cur);
+    a.keys = m->keys.p;
+    a.counts = m->counts.p;
+    a.offsets = m->offsets.p;
+    a.cursor = m->cursor.p;
+    a.bins = m->active_bins.p;
+    a.tiles = m->active_tiles.p;
+    a.nactive = m->nactive.p;
+    a.chunk_sums = m->scan_tmp.p;
+    a.status = m->status.p;
+    a.outside = m->outside.p;
+    pp[i + 1] = pp[i] + m->n;
+    pk[i + 1] = pk[i] + nkeys + 1;
+    pc[i + 1] = pc[i] + (nkeys + 1 + RB_CHUNK - 1) / RB_CHUNK;
+    pb[i + 1] = pb[i] + (int64_t)m->ntx * m->nty;
+    max_items = std::max(max_items, std::max(pp[i + 1], pk[i + 1]));
+  }
+  const size_t bytes = (size_t)nm * sizeof(RebinArgs) + 4 * (size_t)(nm + 1) * sizeof(int64_t);
+  HG_CUDA_TRY(cudaMemcpyAsync(dtable, table, bytes, cudaMemcpyHostToDevice, s));
+  const RebinArgs *dR = reinterpret_cast<const RebinArgs *>(dtable);
+  const int64_t *dpre = reinterpret_cast<const int64_t *>(dtable + (size_t)nm * sizeof(RebinArgs));
+  RebinPrefix P{dpre, dpre + (nm + 1), dpre + 2 * (nm + 1), dpre + 3 * (nm + 1), nm};
+  const int cap = ctx->num_sms * 8;
+  auto grid = [&](int64_t items) {
+    return (int)std::max<int64_t>(1, std::min<int64_t>(cap, (items + 255) / 256));
+  };
+  HG_LAUNCH(kr_clear, grid(pk[nm]), 256, 0, s, dR, P);
+  HG_CHECK_LAUNCH();
+  HG_LAUNCH(kr_keys, grid(pp[nm]), 256, 0, s, dR, P);
+  HG_CHECK_LAUNCH();
+  const int cgrid = (int)std::min<int64_t>(pc[nm], (int64_t)ctx->num_sms * 8);
+  HG_LAUNCH(kr_chunk_sums, cgrid, THREADS, 0, s, dR, P);
+  HG_CHECK_LAUNCH();
+  HG_LAUNCH(kr_chunk_scan, nm, THREADS, 0, s, dR, P);
+  HG_CHECK_LAUNCH();
+  HG_LAUNCH(kr_chunk_scan_apply, cgrid, THREADS, 0, s, dR, P);
+  HG_CHECK_LAUNCH();
+  HG_LAUNCH(kr_scatter, grid(pp[nm]), 256, 0, s, dR, P);
+  HG_CHECK_LAUNCH();
+  HG_LAUNCH(kr_active, grid(pb[nm]), 256, 0, s, dR, P);
+  HG_CHECK_LAUNCH();
+  for (hg_mpm *m : R) {
+    m->cur = 1 - m->cur;
+    m->steps_since_rebin = 0;
+    m->outside_pending = false;
+    m->rebins++;
+  }
   return HG_OK;
 }
 
@@ -1013,9 +1297,16 @@ hg_status batch_alloc(hg_batch *b) {
   hg_status st;
   if ((st = b->table.alloc(tsz)) || (st = b->outside.alloc(2 * (size_t)b->max_members)))
     return st;
-  for (int k = 0; k < 2; ++k) {
+  for (int k = 0; k < hg_batch::NBUF; ++k) {
     HG_CUDA_TRY(cudaMallocHost(&b->h_table[k], tsz));
     HG_CUDA_TRY(cudaEventCreateWithFlags(&b->table_ev[k], cudaEventDisableTiming));
+  }
+  b->args.resize(2 * (size_t)b->max_members * sizeof(MixedArgs));
+  const size_t rsz = rebin_table_bytes(b->max_members);
+  if ((st = b->rtable.alloc(rsz))) return st;
+  for (int k = 0; k < hg_batch::NBUF; ++k) {
+    HG_CUDA_TRY(cudaMallocHost(&b->h_rtable[k], rsz));
+    HG_CUDA_TRY(cudaEventCreateWithFlags(&b->rtable_ev[k], cudaEventDisableTiming));
   }
   HG_CUDA_TRY(cudaMallocHost(&b->h_outside, 2 * sizeof(uint32_t) * b->max_members));
   HG_CUDA_TRY(cudaEventCreateWithFlags(&b->out_ev, cudaEventDisableTiming));
@@ -1023,19 +1314,41 @@ hg_status batch_alloc(hg_batch *b) {
 }
 
 void batch_free(hg_batch *b) {
-  for (int k = 0; k < 2; ++k) {
+  for (int k = 0; k < hg_batch::NBUF; ++k) {
     if (b->h_table[k]) cudaFreeHost(b->h_table[k]);
     if (b->table_ev[k]) cudaEventDestroy(b->table_ev[k]);
+    if (b->h_rtable[k]) cudaFreeHost(b->h_rtable[k]);
+    if (b->rtable_ev[k]) cudaEventDestroy(b->rtable_ev[k]);
   }
   if (b->h_outside) cudaFreeHost(b->h_outside);
   if (b->out_ev) cudaEventDestroy(b->out_ev);
+  for (cudaEvent_t e : b->prof_events) cudaEventDestroy(e);
+}
+
+hg_status batch_profile_read(hg_batch *b, double *ms, int64_t *steps) {
+  double acc[hg_batch::PROF_PHASES] = {0.0};
+  const size_t per = hg_batch::PROF_PHASES + 1;
+  if (b->prof_used > 0) HG_CUDA_TRY(cudaEventSynchronize(b->prof_events[b->prof_used - 1]));
+  for (size_t k = 0; k + per <= b->prof_used; k += per)
+    for (int j = 0; j < hg_batch::PROF_PHASES; ++j) {
+      float t = 0.f;
+      HG_CUDA_TRY(cudaEventElapsedTime(&t, b->prof_events[k + j], b->prof_events[k + j + 1]));
+      acc[j] += t;
+    }
+  for (int j = 0; j < hg_batch::PROF_PHASES; ++j) ms[j] = acc[j];
+  if (steps) *steps = (int64_t)(b->prof_used / per);
+  return HG_OK;
 }
 
 hg_status batch_step(hg_batch *b, int nsteps) {
   cudaStream_t s = b->ctx->stream;
   const int S = (int)b->members.size();
   if (S == 0) return HG_OK;
-  const size_t half = (size_t)b->max_members * sizeof(MixedArgs);
+  MixedArgs *cache = reinterpret_cast<MixedArgs *>(b->args.data());
+  if ((int)b->sigs.size() != S) {
+    b->sigs.assign(S, hg_batch::Sig{});
+    b->dirty = true;
+  }
   for (int k = 0; k < nsteps; ++k) {
     // re-sort members whose points left their windows (counters read back
     // asynchronously one step late), members due for a periodic re-sort and
@@ -1049,37 +1362,79 @@ hg_status batch_step(hg_batch *b, int nsteps) {
           m->steps_since_rebin = MAX_STEPS_BETWEEN_REBINS;
       }
     }
-    for (hg_mpm *m : b->members) {
-      hg_status st = HG_OK;
-      if (!m->primed) st = prime(m);
-      else if (m->steps_since_rebin >= MAX_STEPS_BETWEEN_REBINS) {
-        st = rebin(m);
-        b->resorts++;
+    cudaEvent_t ev[hg_batch::PROF_PHASES + 1] = {};
+    if (b->profile) {
+      while (b->prof_events.size() < b->prof_used + hg_batch::PROF_PHASES + 1) {
+        cudaEvent_t e;
+        HG_CUDA_TRY(cudaEventCreate(&e));
+        b->prof_events.push_back(e);
       }
+      for (int j = 0; j <= hg_batch::PROF_PHASES; ++j) ev[j] = b->prof_events[b->prof_used + j];
+      b->prof_used += hg_batch::PROF_PHASES + 1;
+      HG_CUDA_TRY(cudaEventRecord(ev[0], s));
+    }
+    b->due.clear();
+    for (hg_mpm *m : b->members) {
+      if (!m->primed) {
+        const hg_status st = prime(m);
+        if (st != HG_OK) return st;
+      } else if (m->steps_since_rebin >= MAX_STEPS_BETWEEN_REBINS) {
+        b->due.push_back(m);
+      }
+    }
+    if (!b->due.empty()) {
+      // the staging buffer last used NBUF re-sorts ago must have been copied
+      const int rb = b->rb;
+      b->rb = (b->rb + 1) % hg_batch::NBUF;
+      const auto w0 = std::chrono::steady_clock::now();
+      HG_CUDA_TRY(cudaEventSynchronize(b->rtable_ev[rb]));
+      b->wait_ms +=
+          std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
+      // the device table is reused: its previous copy was read by kernels
+      // that precede this copy on the stream
+      const hg_status st = rebin_batch(b->ctx, b->due, b->h_rtable[rb], b->rtable.p);
       if (st != HG_OK) return st;
+      HG_CUDA_TRY(cudaEventRecord(b->rtable_ev[rb], s));
+      b->resorts += (int64_t)b->due.size();
     }
-    // per-scene argument tables (buffer pointers change with every re-sort)
-    const int tb = b->tb;
-    b->tb = 1 - b->tb;
-    HG_CUDA_TRY(cudaEventSynchronize(b->table_ev[tb]));
-    MixedArgs *hb = reinterpret_cast<MixedArgs *>(b->h_table[tb]);
-    MixedArgs *ht = reinterpret_cast<MixedArgs *>(b->h_table[tb] + half);
+    if (b->profile) HG_CUDA_TRY(cudaEventRecord(ev[1], s));
+    // per-scene argument tables [update args of S scenes | fused args of S
+    // scenes]; an entry changes when its scene re-sorts (buffer swap), is
+    // re-uploaded or changes dt, and the table is copied only then
     for (int i = 0; i < S; ++i) {
-      hb[i] = make_args(b->members[i], b->dts[i], false);
-      ht[i] = make_args(b->members[i], b->dts[i], true);
+      hg_mpm *m = b->members[i];
+      const hg_batch::Sig sg{m, m->cur, m->n, b->dts[i]};
+      if (b->dirty || !(sg == b->sigs[i])) {
+        b->sigs[i] = sg;
+        cache[i] = make_args(m, b->dts[i], true);
+        cache[S + i] = make_args(m, b->dts[i], false);
+        b->dirty = true;
+      }
     }
-    // the device table is read by the previous step's kernels; the copy is
-    // ordered after them on the stream
-    HG_CUDA_TRY(cudaMemcpyAsync(b->table.p, b->h_table[tb], half + sizeof(MixedArgs) * S,
-                                cudaMemcpyHostToDevice, s));
-    HG_CUDA_TRY(cudaEventRecord(b->table_ev[tb], s));
-    const MixedArgs *db = reinterpret_cast<const MixedArgs *>(b->table.p);
-    const MixedArgs *dt = reinterpret_cast<const MixedArgs *>(b->table.p + half);
+    if (b->dirty) {
+      const int tb = b->tb;
+      b->tb = (b->tb + 1) % hg_batch::NBUF;
+      const auto w0 = std::chrono::steady_clock::now();
+      HG_CUDA_TRY(cudaEventSynchronize(b->table_ev[tb]));
+      b->wait_ms +=
+          std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
+      const size_t bytes = 2 * (size_t)S * sizeof(MixedArgs);
+      std::memcpy(b->h_table[tb], cache, bytes);
+      // ordered after the previous step's kernels, which read the table
+      HG_CUDA_TRY(cudaMemcpyAsync(b->table.p, b->h_table[tb], bytes, cudaMemcpyHostToDevice, s));
+      HG_CUDA_TRY(cudaEventRecord(b->table_ev[tb], s));
+      b->dirty = false;
+    }
+    if (b->profile) HG_CUDA_TRY(cudaEventRecord(ev[2], s));
+    const MixedArgs *dt = reinterpret_cast<const MixedArgs *>(b->table.p);
+    const MixedArgs *db = dt + S;
     const int nsm = b->ctx->num_sms;
     HG_LAUNCH(kb_grid_update, nsm * 8, THREADS, 0, s, dt, S);
     HG_CHECK_LAUNCH();
+    if (b->profile) HG_CUDA_TRY(cudaEventRecord(ev[3], s));
     HG_LAUNCH(kb_g2p2g, nsm * 3, THREADS, 0, s, db, S);
     HG_CHECK_LAUNCH();
+    if (b->profile) HG_CUDA_TRY(cudaEventRecord(ev[4], s));
     for (hg_mpm *m : b->members) m->steps_since_rebin++;
     b->member_steps += S;
     b->steps++;

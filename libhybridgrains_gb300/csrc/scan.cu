@@ -6,6 +6,7 @@
 // are read with coalesced 32-bit loads; the whole pass streams the counts
 // twice, which is the floor for a scan that does not fuse into its producer.
 #include "hg_internal.cuh"
+#include "scan_block.cuh"
 
 namespace hg {
 
@@ -14,36 +15,6 @@ namespace {
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 8;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
-
-__device__ __forceinline__ int warp_incl_scan(int x) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const int y = __shfl_up_sync(0xffffffffu, x, d);
-    if (lane >= d) x += y;
-  }
-  return x;
-}
-
-// Exclusive scan of one value per thread across the block; returns the
-// exclusive prefix and writes the block total to *total.
-__device__ __forceinline__ int block_excl_scan(int x, int *total) {
-  __shared__ int s_warp[SCAN_THREADS / 32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int inc = warp_incl_scan(x);
-  if (lane == 31) s_warp[wid] = inc;
-  __syncthreads();
-  if (wid == 0) {
-    int w = lane < SCAN_THREADS / 32 ? s_warp[lane] : 0;
-    w = warp_incl_scan(w);
-    if (lane < SCAN_THREADS / 32) s_warp[lane] = w;
-  }
-  __syncthreads();
-  const int warp_off = wid > 0 ? s_warp[wid - 1] : 0;
-  *total = s_warp[SCAN_THREADS / 32 - 1];
-  __syncthreads();
-  return warp_off + inc - x;
-}
 
 __global__ void k_tile_sums(const int32_t *__restrict__ in, int64_t n,
                             int32_t *__restrict__ sums) {
@@ -55,7 +26,7 @@ __global__ void k_tile_sums(const int32_t *__restrict__ in, int64_t n,
     if (i < n) s += in[i];
   }
   int total;
-  block_excl_scan(s, &total);
+  block_excl_scan<SCAN_THREADS>(s, &total);
   if (threadIdx.x == 0) sums[blockIdx.x] = total;
 }
 
@@ -73,7 +44,7 @@ __global__ void k_tile_scan(const int32_t *__restrict__ in, int64_t n,
     s += v[k];
   }
   int total;
-  int run = block_excl_scan(s, &total) + (tile_off ? tile_off[blockIdx.x] : 0);
+  int run = block_excl_scan<SCAN_THREADS>(s, &total) + (tile_off ? tile_off[blockIdx.x] : 0);
 #pragma unroll
   for (int k = 0; k < SCAN_ITEMS; ++k) {
     const int64_t i = base + (int64_t)threadIdx.x * SCAN_ITEMS + k;

@@ -7,10 +7,13 @@ a frame every ``frame_every`` steps. The loop
 * admits arrived requests first come, first served while their device
   footprint (``hg_mpm_estimate_bytes``) fits the budget and a batch slot is
   free; a request that does not fit waits at the head of the queue;
-* keeps every admitted scene resident and steps all of them together
+* creates each admitted scene on the device from its geometry (no host
+  point data) and keeps it resident;
+* steps all resident scenes together
   (``hg_batch_step``: one grid-update and one fused G2P/P2G launch per step);
-* admits new requests at chunk boundaries (every ``frame_every`` steps), so
-  work that arrives while others run joins the running batch;
+* admits new requests at chunk boundaries (every ``frame_every`` steps), at
+  most ``admit_per_chunk`` per chunk, so work that arrives while others run
+  joins the running batch;
 * queues each frame's copy to page-locked host memory and a fence behind the
   chunk, and hands frames over once the fence is done, keeping at most
   ``depth`` chunks queued on the device;
@@ -77,7 +80,7 @@ class Backend:
     def footprint(self, req):
         raise NotImplementedError
 
-    def open(self, req):  # create, seed, queue the upload, join the batch
+    def open(self, req):  # create the scene and join the batch
         raise NotImplementedError
 
     def step(self, nsteps):
@@ -106,12 +109,15 @@ class Backend:
 
 
 class Server:
-    def __init__(self, backend, budget_bytes, max_members=256, depth=3, clock=time.perf_counter,
-                 sleep=time.sleep):
+    def __init__(self, backend, budget_bytes, max_members=256, depth=3, admit_per_chunk=16,
+                 clock=time.perf_counter, sleep=time.sleep):
         self.b = backend
         self.budget = int(budget_bytes)
         self.max_members = max_members
         self.depth = depth
+        # scenes created per chunk: creation overlaps with the chunks queued
+        # on the device instead of delaying the first one
+        self.admit_per_chunk = admit_per_chunk
         self.clock = clock
         self.sleep = sleep
         self.resident = 0
@@ -140,8 +146,10 @@ class Server:
             while pending and pending[-1].arrival <= now:
                 waiting.append(pending.pop())
             # admission: FIFO, by footprint and free slots
-            while waiting and len(active) < self.max_members and \
-                    self.resident + waiting[0].footprint <= self.budget:
+            admitted = 0
+            while waiting and len(active) < self.max_members and admitted < self.admit_per_chunk \
+                    and self.resident + waiting[0].footprint <= self.budget:
+                admitted += 1
                 r = waiting.popleft()
                 self.b.open(r)
                 r.admitted = self.clock() - t0
@@ -262,17 +270,11 @@ class DeviceBackend(Backend):
         m = MPM(self.ctx, c["grid_min"], c["grid_max"], c["h"], c["shear_modulus"],
                 c["bulk_modulus"], c["dp_alpha"], c["flip_alpha"], scenes.GRAVITY,
                 c["planes"], capacity=req.npoints)
-        p = scenes.seed_column_points(c)
-        n = len(p["m"])
-        up = dict(q=self._buf((n, 2)), v=self._buf((n, 2)), m=self._buf((n,)),
-                  vol=self._buf((n,)))
-        for k in up:
-            up[k][...] = p[k]
-        m.upload_async(up["q"], up["v"], up["m"], up["vol"])
-        frames = [self._buf((n, 2)) for _ in range(self.depth + 1)]
+        # points generated on the device from the request's geometry
+        m.seed_rectangle_device(c["rect_min"], c["rect_max"], c["rho"], c["samples_per_dim"])
+        frames = [self._buf((req.npoints, 2)) for _ in range(self.depth + 1)]
         self.batch.add(m, req.dt)
-        # upload staging is returned once a fence behind the upload is done
-        self.state[req.rid] = dict(m=m, up=up, up_fence=self.ctx.fence(), frames=frames)
+        self.state[req.rid] = dict(m=m, frames=frames)
 
     def step(self, nsteps):
         self.batch.step(nsteps)
@@ -285,13 +287,7 @@ class DeviceBackend(Backend):
         self.batch.remove(self.state[req.rid]["m"])
 
     def fence(self):
-        f = self.ctx.fence()
-        for s in self.state.values():
-            if s["up"] is not None and self.ctx.fence_done(s["up_fence"]):
-                for a in s["up"].values():
-                    self._give(a)
-                s["up"] = None
-        return f
+        return self.ctx.fence()
 
     def fence_done(self, f):
         return self.ctx.fence_done(f)
@@ -306,10 +302,6 @@ class DeviceBackend(Backend):
     def close(self, req):
         s = self.state.pop(req.rid)
         s["m"].close()
-        if s["up"] is not None:
-            self.ctx.fence_wait(s["up_fence"])
-            for a in s["up"].values():
-                self._give(a)
         for a in s["frames"]:
             self._give(a)
 
@@ -328,8 +320,7 @@ def run_one_at_a_time(ctx, requests):
         m = MPM(ctx, c["grid_min"], c["grid_max"], c["h"], c["shear_modulus"],
                 c["bulk_modulus"], c["dp_alpha"], c["flip_alpha"], scenes.GRAVITY,
                 c["planes"], capacity=r.npoints)
-        p = scenes.seed_column_points(c)
-        m.upload(p["q"], p["v"], p["m"], p["vol"])
+        m.seed_rectangle_device(c["rect_min"], c["rect_max"], c["rho"], c["samples_per_dim"])
         q = np.zeros((r.npoints, 2))
         for k in range(r.steps // r.frame_every):
             m.flow(r.dt, r.frame_every)

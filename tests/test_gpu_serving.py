@@ -47,6 +47,34 @@ def test_async_upload_and_frame_match_sync_download(ctx):
         ctx.fence_done(f1 + 5)
 
 
+@pytest.mark.parametrize("precision", [hg.FP64, hg.MIXED])
+def test_device_seed_is_host_seed_bit_for_bit(ctx, precision):
+    cfg = scenes.serving_column(30000, 1.5, 30.0)
+    n_host = len(scenes.seed_column_points(cfg)["m"])
+    a = hg.MPM(ctx, cfg["grid_min"], cfg["grid_max"], cfg["h"], cfg["shear_modulus"],
+               cfg["bulk_modulus"], cfg["dp_alpha"], cfg["flip_alpha"], scenes.GRAVITY,
+               cfg["planes"], precision=precision, capacity=3 * n_host)
+    b = hg.MPM(ctx, cfg["grid_min"], cfg["grid_max"], cfg["h"], cfg["shear_modulus"],
+               cfg["bulk_modulus"], cfg["dp_alpha"], cfg["flip_alpha"], scenes.GRAVITY,
+               cfg["planes"], precision=precision, capacity=3 * n_host)
+    lo, hi = (cfg["rect_min"][0] + 0.3 * cfg["h"], 0.0), cfg["rect_max"]  # ragged edge
+    p = a.seed_rectangle(lo, hi, 1550.0, 3, vel=(0.5, -0.25), omega=2.0)
+    a.upload(p["q"], p["v"], p["m"], p["vol"], p["hl"])
+    n = b.seed_rectangle_device(lo, hi, 1550.0, 3, vel=(0.5, -0.25), omega=2.0)
+    assert n == len(p["m"]) > 0
+    A, B = a.download(), b.download()
+    for k in ("q", "v", "be", "J", "jh"):
+        assert np.array_equal(A[k], B[k]), k
+    # stepping from the two states agrees up to the order of atomic sums
+    # (FP64 atomics: 1e-12 m; FP32 atomics of the MIXED path: 1e-9 m)
+    a.flow(cfg["dt"], 3)
+    b.flow(cfg["dt"], 3)
+    tol = 1e-12 if precision == hg.FP64 else 1e-9
+    assert np.abs(a.download()["q"] - b.download()["q"]).max() <= tol
+    with pytest.raises(hg.HGError):  # more points than the capacity
+        b.seed_rectangle_device(lo, hi, 1550.0, 4)
+
+
 def test_estimate_bounds_device_bytes(ctx):
     cfg = scenes.serving_column(100000, 1.0, 30.0)
     p = scenes.seed_column_points(cfg)
