@@ -254,6 +254,74 @@ hg_status hg_batch_profile(hg_batch *b, int32_t enable);
 hg_status hg_batch_profile_read(hg_batch *b, double *resort_ms, double *table_ms,
                                 double *update_ms, double *fused_ms, int64_t *steps);
 
+/* ---- zone labels (hybridgrains2dnew ZoneTools), host code ----------------
+ * Runs on the host at the resampling interval on positions copied from the
+ * device (HybridGrains2DSim::updateHybridStates_poorman,
+ * HybridGrains2DSim.cpp:301-326). Labels are bit-exact restatements of the
+ * reference's FP64 arithmetic. */
+enum { HG_ZONE_CONTINUUM = 0, HG_ZONE_DISCRETE = 1, HG_ZONE_HYBRID = 2 };
+enum {
+  HG_ZONES_RECONCILIATION = 0,    /* getRZones / getRZoneIndices */
+  HG_ZONES_DIRECT_TRANSITION = 1, /* getDirectTransitionZonesFromDiscreteToContinuum */
+  HG_ZONES_INNER_CONTINUUM = 2,   /* identifyInnerContinuumRegion */
+  HG_ZONES_INNER_CONTINUUM_EXCLUDING_DIRECT = 3,
+  HG_ZONES_LEVEL_SET_HYBRID = 4   /* hybrid cells of the level-set grid */
+};
+enum { HG_ZONES_MPM = 0, HG_ZONES_DEM = 1 };
+typedef struct hg_zones hg_zones;
+typedef struct {
+  double mpm_grid_min[2];   /* PhysicsGrid::min after setDimensions */
+  double mpm_cell_width;
+  int32_t mpm_cells[2];     /* PhysicsGrid::cell_count */
+  double level_set_cell_width;
+  int32_t allow_direct_transitions;
+  int32_t phi_samples_per_cell_side;
+  double phi_window_size;
+  double phi_threshold;
+  double rzone_level_set;
+  double rzone_half_thickness;
+} hg_zones_desc;
+/* ZoneTools::init (ZoneTools.cpp:6-64); a level-set cell wider than an MPM
+ * cell is HG_ERR_INVALID_ARGUMENT (the reference exits). */
+hg_status hg_zones_create(const hg_zones_desc *desc, hg_zones **out);
+hg_status hg_zones_destroy(hg_zones *z);
+/* updatePackingFraction + updateDistanceField + computeRZones
+ * (ZoneTools.cpp:186-672). q: 3 x n_disks (x, y, theta), radius, fixed
+ * (NULL: none fixed; fixed disks are ignored as in
+ * getAllNonFixedCircleBodies); points: 2 x n_points MPM positions. */
+hg_status hg_zones_update(hg_zones *z, int64_t n_disks, const double *q,
+                          const double *radius, const uint8_t *fixed,
+                          int64_t n_points, const double *points);
+hg_status hg_zones_grid_info(hg_zones *z, int32_t level_set_cells[2],
+                             int32_t mpm_cells[2]);
+/* Packing fraction per level-set cell, signed distance per level-set grid
+ * point ((nx+1) x (ny+1)), level-set cell labels, MPM cell labels; any
+ * pointer may be NULL. */
+hg_status hg_zones_fields(hg_zones *z, double *packing_fraction, double *distance,
+                          int32_t *level_set_labels, int32_t *mpm_labels);
+/* Replaces the MPM cell labels (the previous labels of the next update). */
+hg_status hg_zones_set_labels(hg_zones *z, const int32_t *mpm_labels);
+/* A zone list (HG_ZONES_*): boxes (x0, y0, x1, y1) and cell indices (i, j),
+ * at most cap of each; *count gets the list's length. */
+hg_status hg_zones_list(hg_zones *z, int32_t which, int64_t cap, double *boxes,
+                        int32_t *cells, int64_t *count);
+/* determineMPMParticlesToDelete (kind HG_ZONES_MPM) /
+ * determineDEMGrainsToDelete (HG_ZONES_DEM) (ZoneTools.cpp:674-731): ids in
+ * increasing order; x holds positions with the given stride in doubles (2
+ * for MPM q, 3 for DEM q). */
+hg_status hg_zones_to_delete(hg_zones *z, int32_t kind, int64_t n, const double *x,
+                             int32_t stride, const uint8_t *fixed, int64_t cap,
+                             int32_t *ids, int64_t *count);
+/* demWeight / mpmWeight (ZoneTools.cpp:123-147) for n positions. */
+hg_status hg_zones_weights(hg_zones *z, int32_t kind, int64_t n, const double *x,
+                           int32_t stride, double *w);
+/* Number of edge samples of the last distance field. */
+hg_status hg_zones_boundary_samples(hg_zones *z, int64_t *count);
+/* Area of the intersection of a disk with an axis-aligned box
+ * (circleRectangleIntersectionArea, CircleRectangleIntersection.cpp:70-82). */
+double hg_zones_disk_box_area(double x0, double x1, double y0, double y1,
+                              double cx, double cy, double r);
+
 /* ---- DEM (rigidbody2d, penalty map) --------------------------------------- */
 
 /* RigidBody2DStaticPlane, static (v = 0, omega = 0). */

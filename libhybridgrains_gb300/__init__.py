@@ -502,3 +502,101 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+CONTINUUM, DISCRETE, HYBRID = 0, 1, 2
+(ZONES_RECONCILIATION, ZONES_DIRECT_TRANSITION, ZONES_INNER_CONTINUUM,
+ ZONES_INNER_CONTINUUM_EXCLUDING_DIRECT, ZONES_LEVEL_SET_HYBRID) = range(5)
+ZONES_MPM, ZONES_DEM = 0, 1
+
+
+class Zones:
+    """Zone labels of the hybrid method (ZoneTools), host code of libhg_gpu
+    run at the resampling interval on positions copied from the device."""
+
+    def __init__(self, mpm_grid_min, mpm_cell_width, mpm_cells, level_set_cell_width,
+                 phi_window_size, phi_samples_per_cell_side, phi_threshold, rzone_level_set,
+                 rzone_half_thickness, allow_direct_transitions=False):
+        d = _capi.ZonesDesc()
+        d.mpm_grid_min[:] = list(map(float, mpm_grid_min))
+        d.mpm_cell_width = float(mpm_cell_width)
+        d.mpm_cells[:] = [int(mpm_cells[0]), int(mpm_cells[1])]
+        d.level_set_cell_width = float(level_set_cell_width)
+        d.allow_direct_transitions = 1 if allow_direct_transitions else 0
+        d.phi_samples_per_cell_side = int(phi_samples_per_cell_side)
+        d.phi_window_size = float(phi_window_size)
+        d.phi_threshold = float(phi_threshold)
+        d.rzone_level_set = float(rzone_level_set)
+        d.rzone_half_thickness = float(rzone_half_thickness)
+        h = ctypes.c_void_p()
+        check("hg_zones_create", ctypes.byref(d), ctypes.byref(h))
+        self._h = h
+        ls, mc = np.zeros(2, dtype=np.int32), np.zeros(2, dtype=np.int32)
+        check("hg_zones_grid_info", h, _i32(ls), _i32(mc))
+        self.level_set_cells = (int(ls[0]), int(ls[1]))
+        self.mpm_cells = (int(mc[0]), int(mc[1]))
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _capi.load().hg_zones_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def update(self, q, radius, fixed=None, points=None):
+        """q: (n, 3) disk states (x, y, theta); points: (m, 2) MPM positions."""
+        q, radius = _f64(q), _f64(radius)
+        fixed = None if fixed is None else np.ascontiguousarray(fixed, dtype=np.uint8)
+        points = None if points is None else _f64(points)
+        check("hg_zones_update", self._h, len(radius), _d(q), _d(radius), _u8(fixed),
+              0 if points is None else len(points), _d(points))
+
+    def fields(self):
+        nx, ny = self.level_set_cells
+        phi, dist = np.zeros(nx * ny), np.zeros((nx + 1) * (ny + 1))
+        ls = np.zeros(nx * ny, dtype=np.int32)
+        mpm = np.zeros(self.mpm_cells[0] * self.mpm_cells[1], dtype=np.int32)
+        check("hg_zones_fields", self._h, _d(phi), _d(dist), _i32(ls), _i32(mpm))
+        return dict(phi=phi, dist=dist, ls=ls, mpm=mpm)
+
+    def set_labels(self, mpm):
+        check("hg_zones_set_labels", self._h, _i32(np.ascontiguousarray(mpm, dtype=np.int32)))
+
+    def zone_list(self, which):
+        n = ctypes.c_int64()
+        check("hg_zones_list", self._h, int(which), 0, None, None, ctypes.byref(n))
+        boxes, cells = np.zeros((n.value, 4)), np.zeros((n.value, 2), dtype=np.int32)
+        check("hg_zones_list", self._h, int(which), n.value, _d(boxes), _i32(cells),
+              ctypes.byref(n))
+        return boxes, cells
+
+    def to_delete(self, kind, x, stride, fixed=None):
+        x = _f64(x)
+        n = x.size // stride
+        ids = np.zeros(max(n, 1), dtype=np.int32)
+        c = ctypes.c_int64()
+        fx = None if fixed is None else np.ascontiguousarray(fixed, dtype=np.uint8)
+        check("hg_zones_to_delete", self._h, int(kind), n, _d(x), int(stride), _u8(fx), n,
+              _i32(ids), ctypes.byref(c))
+        return ids[:c.value]
+
+    def weights(self, kind, x, stride):
+        x = _f64(x)
+        n = x.size // stride
+        w = np.zeros(n)
+        check("hg_zones_weights", self._h, int(kind), n, _d(x), int(stride), _d(w))
+        return w
+
+    def boundary_samples(self):
+        c = ctypes.c_int64()
+        check("hg_zones_boundary_samples", self._h, ctypes.byref(c))
+        return c.value
+
+
+def disk_box_area(x0, x1, y0, y1, cx, cy, r):
+    """Area of a disk inside an axis-aligned box (hg_zones_disk_box_area)."""
+    return _capi.load().hg_zones_disk_box_area(x0, x1, y0, y1, cx, cy, r)

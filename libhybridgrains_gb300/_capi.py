@@ -44,6 +44,15 @@ class DemPlane(ctypes.Structure):
     _fields_ = [("x", ctypes.c_double * 2), ("n", ctypes.c_double * 2)]
 
 
+class ZonesDesc(ctypes.Structure):
+    _fields_ = [("mpm_grid_min", ctypes.c_double * 2), ("mpm_cell_width", ctypes.c_double),
+                ("mpm_cells", ctypes.c_int32 * 2), ("level_set_cell_width", ctypes.c_double),
+                ("allow_direct_transitions", ctypes.c_int32),
+                ("phi_samples_per_cell_side", ctypes.c_int32), ("phi_window_size", ctypes.c_double),
+                ("phi_threshold", ctypes.c_double), ("rzone_level_set", ctypes.c_double),
+                ("rzone_half_thickness", ctypes.c_double)]
+
+
 class DemDesc(ctypes.Structure):
     _fields_ = [("gravity", ctypes.c_double * 2), ("kn", ctypes.c_double),
                 ("kt", ctypes.c_double), ("gamman", ctypes.c_double),
@@ -111,6 +120,17 @@ SIGNATURES = {
     "hg_batch_stats": [_P, _I64, _I64, _I64, _D, _D],
     "hg_batch_profile": [_P, _i32],
     "hg_batch_profile_read": [_P, _D, _D, _D, _D, _I64],
+    "hg_zones_create": [ctypes.POINTER(ZonesDesc), _PP],
+    "hg_zones_destroy": [_P],
+    "hg_zones_update": [_P, _i64, _D, _D, _U8, _i64, _D],
+    "hg_zones_grid_info": [_P, _I32, _I32],
+    "hg_zones_fields": [_P, _D, _D, _I32, _I32],
+    "hg_zones_set_labels": [_P, _I32],
+    "hg_zones_list": [_P, _i32, _i64, _D, _I32, _I64],
+    "hg_zones_to_delete": [_P, _i32, _i64, _D, _i32, _U8, _i64, _I32, _I64],
+    "hg_zones_weights": [_P, _i32, _i64, _D, _i32, _D],
+    "hg_zones_boundary_samples": [_P, _I64],
+    "hg_zones_disk_box_area": [_dbl, _dbl, _dbl, _dbl, _dbl, _dbl, _dbl],
     "hg_dem_create": [_P, ctypes.POINTER(DemDesc), _PP],
     "hg_dem_destroy": [_P],
     "hg_dem_upload": [_P, _i64, _D, _D, _D, _D, _D, _U8],
@@ -131,6 +151,7 @@ SIGNATURES = {
     "hg_hybrid_download": [_P, _I32, _I32, _D, _D, _D, _D, _D, _D, _D],
 }
 _RET = {"hg_status_string": ctypes.c_char_p, "hg_last_error": ctypes.c_char_p,
+        "hg_zones_disk_box_area": ctypes.c_double,
         "hg_kernel_launch_count": ctypes.c_int64}
 
 _lib = None

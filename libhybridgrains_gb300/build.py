@@ -29,8 +29,9 @@ SOURCES = [
     ("mpm_mixed.cu", None),
     ("dem.cu", True),
     ("coupling.cu", True),
+    ("zones.cu", True),  # host code (zone labels)
 ]
-HEADERS = ["hg_internal.cuh", "mpm_basis.cuh"]
+HEADERS = ["hg_internal.cuh", "mpm_basis.cuh", "scan_block.cuh"]
 
 
 def _nvcc():

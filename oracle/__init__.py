@@ -73,13 +73,57 @@ def _sig(lib):
     f.hgo_hybrid_get.argtypes = [_P, _I, _I, _D, _D, _D, _D, _D, _D, _D]
 
 
+def _zones_sig(f):
+    f.hgo_zones_create.restype = _P
+    f.hgo_zones_create.argtypes = [_D, ctypes.c_double, _I, ctypes.c_double, ctypes.c_int]
+    f.hgo_zones_destroy.argtypes = [_P]
+    f.hgo_zones_packing.argtypes = [_P, ctypes.c_int, _D, _D, _U8, ctypes.c_int, _D,
+                                    ctypes.c_double, ctypes.c_int]
+    f.hgo_zones_distance.argtypes = [_P, ctypes.c_double]
+    f.hgo_zones_labels.argtypes = [_P, ctypes.c_double, ctypes.c_double]
+    f.hgo_zones_get.argtypes = [_P, _D, _D, _I, _I]
+    f.hgo_zones_nsamples.restype = ctypes.c_int
+    f.hgo_zones_nsamples.argtypes = [_P]
+    f.hgo_zones_list.restype = ctypes.c_int
+    f.hgo_zones_list.argtypes = [_P, ctypes.c_int, _D, _I]
+    f.hgo_zones_to_delete.restype = ctypes.c_int
+    f.hgo_zones_to_delete.argtypes = [_P, ctypes.c_int, ctypes.c_int, _D, ctypes.c_int, _U8, _I]
+    f.hgo_zones_weights.argtypes = [_P, ctypes.c_int, ctypes.c_int, _D, ctypes.c_int, _D]
+    f.hgo_zones_set_labels.argtypes = [_P, _I]
+    f.hgo_disk_box_area.restype = ctypes.c_double
+    f.hgo_disk_box_area.argtypes = [ctypes.c_double] * 7
+
+
 def lib():
     global _lib
     if _lib is None:
         path = _build.build()
         _lib = ctypes.CDLL(path)
         _sig(_lib)
+        _zones_sig(_lib)
     return _lib
+
+
+_ref = None
+
+
+def reference_lib():
+    """The reference's own standalone sources (circle/box area, MT19937)
+    built by oracle/build_ref.py, or None where the reference checkout is
+    absent."""
+    global _ref
+    if _ref is None:
+        from . import build_ref
+        path = build_ref.build()
+        if path is None:
+            return None
+        _ref = ctypes.CDLL(path)
+        _ref.hgr_circle_rectangle_area.restype = ctypes.c_double
+        _ref.hgr_circle_rectangle_area.argtypes = [ctypes.c_double] * 7
+        _ref.seedMT.argtypes = [ctypes.c_uint32]
+        _ref.randomMT.restype = ctypes.c_float
+        _ref.randomMT_i.restype = ctypes.c_uint32
+    return _ref
 
 
 def _d(a):
@@ -298,3 +342,76 @@ class Hybrid:
                     dem_mom_grid=dp.reshape(-1, 2), v_after=va.reshape(-1, 2),
                     at_after=aa.reshape(-1, 2), homog_factor=hf, homog_stress=hs.reshape(-1, 4),
                     homog_velocity=hv.reshape(-1, 2))
+
+
+class Zones:
+    """ZoneTools restated (zones_oracle.cpp)."""
+
+    def __init__(self, mpm_min, mpm_cell_width, mpm_cells, level_set_cell_width,
+                 allow_direct=False):
+        self.cells = (int(mpm_cells[0]), int(mpm_cells[1]))
+        self.N = tuple(int(np.ceil(c * mpm_cell_width / level_set_cell_width)) for c in mpm_cells)
+        self._h = lib().hgo_zones_create(_d(_f64(mpm_min)), float(mpm_cell_width),
+                                         (ctypes.c_int * 2)(*self.cells),
+                                         float(level_set_cell_width), int(allow_direct))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().hgo_zones_destroy(self._h)
+            self._h = None
+
+    def update(self, q3, r, fixed, points, window, samples, threshold, level, half):
+        q3 = _f64(q3)
+        r = _f64(r)
+        fixed = None if fixed is None else np.ascontiguousarray(fixed, dtype=np.uint8)
+        points = _f64(points) if points is not None else None
+        L = lib()
+        L.hgo_zones_packing(self._h, len(r), _d(q3), _d(r),
+                            None if fixed is None else fixed.ctypes.data_as(_U8),
+                            0 if points is None else len(points), _d(points), float(window),
+                            int(samples))
+        L.hgo_zones_distance(self._h, float(threshold))
+        L.hgo_zones_labels(self._h, float(level), float(half))
+
+    def fields(self):
+        nx, ny = self.N
+        pf = np.zeros(nx * ny)
+        dist = np.zeros((nx + 1) * (ny + 1))
+        ls = np.zeros(nx * ny, dtype=np.int32)
+        mpm = np.zeros(self.cells[0] * self.cells[1], dtype=np.int32)
+        lib().hgo_zones_get(self._h, _d(pf), _d(dist), _i(ls), _i(mpm))
+        return dict(phi=pf, dist=dist, ls=ls, mpm=mpm)
+
+    def samples(self):
+        return lib().hgo_zones_nsamples(self._h)
+
+    def zone_list(self, which):
+        n = lib().hgo_zones_list(self._h, int(which), None, None)
+        boxes = np.zeros((n, 4))
+        cells = np.zeros((n, 2), dtype=np.int32)
+        lib().hgo_zones_list(self._h, int(which), _d(boxes), _i(cells))
+        return boxes, cells
+
+    def to_delete(self, kind, x, stride, fixed=None):
+        x = _f64(x)
+        n = len(x.reshape(-1)) // stride
+        ids = np.zeros(max(n, 1), dtype=np.int32)
+        fx = None if fixed is None else np.ascontiguousarray(fixed, dtype=np.uint8)
+        c = lib().hgo_zones_to_delete(self._h, int(kind), n, _d(x), int(stride),
+                                      None if fx is None else fx.ctypes.data_as(_U8), _i(ids))
+        return ids[:c]
+
+    def weights(self, kind, x, stride):
+        x = _f64(x)
+        n = len(x.reshape(-1)) // stride
+        w = np.zeros(n)
+        lib().hgo_zones_weights(self._h, int(kind), n, _d(x), int(stride), _d(w))
+        return w
+
+    def set_labels(self, mpm):
+        mpm = np.ascontiguousarray(mpm, dtype=np.int32)
+        lib().hgo_zones_set_labels(self._h, _i(mpm))
+
+
+def disk_box_area(x0, x1, y0, y1, cx, cy, r):
+    return lib().hgo_disk_box_area(x0, x1, y0, y1, cx, cy, r)

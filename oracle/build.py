@@ -10,7 +10,7 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SOURCES = ["mpm_oracle.cpp", "dem_oracle.cpp", "coupling_oracle.cpp"]
+SOURCES = ["mpm_oracle.cpp", "dem_oracle.cpp", "coupling_oracle.cpp", "zones_oracle.cpp"]
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libhg_oracle.so")
 
