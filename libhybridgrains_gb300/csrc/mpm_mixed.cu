@@ -85,10 +85,12 @@ struct alignas(16) MixedArgs {
 // FP64 path.
 // Rare cases (u < 1, negative, huge or non-finite) are kept out of line so
 // that the common path does not carry predicated FP64 instructions.
-__device__ __noinline__ void split_u_slow(double u, int &c, float &f) {
+// Returned by value (cell, fraction bits): reference parameters would take
+// the callers' variables' addresses and keep them in local memory on every
+// path.
+__device__ __noinline__ int2 split_u_slow(double u) {
   const double fl = floor(u);
-  c = (int)fl;
-  f = __double2float_rz(u - fl);
+  return make_int2((int)fl, __float_as_int(__double2float_rz(u - fl)));
 }
 
 __device__ __forceinline__ void split_u(double u, int &c, float &f) {
@@ -102,7 +104,9 @@ __device__ __forceinline__ void split_u(double u, int &c, float &f) {
     const unsigned f24 = __funnelshift_r(lo, hf, sh - 24) & 0xFFFFFFu;
     f = (float)f24 * (1.0f / 16777216.0f);
   } else {
-    split_u_slow(u, c, f);
+    const int2 s = split_u_slow(u);
+    c = s.x;
+    f = __int_as_float(s.y);
   }
 }
 
@@ -277,10 +281,8 @@ __device__ __forceinline__ void fused_tile(const MixedArgs &A, const int bin, Fu
         s_va[k] = val;
       }
     }
-    for (int k = tid; k < ACC_W * ACC_W; k += THREADS) {
-#pragma unroll
-      for (int c = 0; c < 5; ++c) s_slow[c][k] = 0.f;
-    }
+    // s_slow is zero here: zeroed at kernel start and by the previous
+    // tile's flush
     if (tid < 2) s_out[tid] = 0;
     const int ps = A.offsets[bin * BIN_CELLS + tid];
     const int pe = A.offsets[bin * BIN_CELLS + tid + 1];
@@ -298,11 +300,8 @@ __device__ __forceinline__ void fused_tile(const MixedArgs &A, const int bin, Fu
                                pl.fn[0] * (x1 - pl.fux[0]) + pl.fn[1] * (y1 - pl.fux[1])));
       if (dmin <= 2.0f * A.pmargin && y1 >= pl.fulb - A.pmargin) plane_mask |= 1u << k;
     }
-    __syncthreads();
-    float acc[20];
-#pragma unroll
-    for (int k = 0; k < 20; ++k) acc[k] = 0.f;
-    // the next point's state is loaded while the current one is processed
+    // the next point's state is loaded while the current one is processed;
+    // the first one before the barrier, under the window loads
     double2 nu = make_double2(0.0, 0.0);
     float2 nmv = make_float2(0.f, 0.f), nvel = make_float2(0.f, 0.f);
     float4 nst = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -314,6 +313,10 @@ __device__ __forceinline__ void fused_tile(const MixedArgs &A, const int bin, Fu
       nst = A.strain[ps];
       nfl = A.flags[ps];
     }
+    __syncthreads();
+    float acc[20];
+#pragma unroll
+    for (int k = 0; k < 20; ++k) acc[k] = 0.f;
     for (int p = ps; p < pe; ++p) {
       const double2 u = nu;
       const float2 mv = nmv;
@@ -468,7 +471,10 @@ __device__ __forceinline__ void fused_tile(const MixedArgs &A, const int bin, Fu
       const int i = k % ACC_W, j = k / ACC_W;
       float sum[5];
 #pragma unroll
-      for (int c = 0; c < 5; ++c) sum[c] = s_slow[c][k];
+      for (int c = 0; c < 5; ++c) {
+        sum[c] = s_slow[c][k];
+        s_slow[c][k] = 0.f; // ready for the next tile
+      }
       const int bi = i - (DRIFT + 1), bj = j - (DRIFT + 1); // node index within the tile
       if (bi >= 0 && bj >= 0 && bi <= BIN && bj <= BIN) {
 #pragma unroll
@@ -494,10 +500,18 @@ __device__ __forceinline__ void fused_tile(const MixedArgs &A, const int bin, Fu
   }
 }
 
+// fused_tile expects the moved-point window to be zero on entry (it leaves
+// it zero); the first tile's barrier orders this against its use.
+__device__ __forceinline__ void zero_slow(FusedSmem &S) {
+  float *s = &S.slow[0][0];
+  for (int k = threadIdx.x; k < 5 * ACC_W * ACC_W; k += THREADS) s[k] = 0.f;
+}
+
 template <bool PRIME>
 __global__ void __launch_bounds__(THREADS, 3) kx_g2p2g(const __grid_constant__ MixedArgs A) {
   // the arguments stay in the constant bank: operands need no registers
   __shared__ FusedSmem S;
+  zero_slow(S);
   const int nact = *A.nactive;
   for (int t = blockIdx.x; t < nact; t += gridDim.x) fused_tile<PRIME>(A, A.active[t], S);
 }
@@ -574,6 +588,7 @@ __global__ void __launch_bounds__(THREADS, 3) kb_g2p2g(const MixedArgs *__restri
   __shared__ FusedSmem S;
   __shared__ MixedArgs A;
   __shared__ int prefix[PREFIX_LEN];
+  zero_slow(S);
   batch_prefix(slots, nslots, prefix);
   int begin, end;
   cta_range(prefix[nslots], begin, end);
