@@ -216,11 +216,11 @@ __device__ __forceinline__ void p2g_corners(const PRec &r, float *a) {
     a[5 * k + 0] += w * r.a.z;
     a[5 * k + 1] += w * r.a.w;
     a[5 * k + 2] += w * r.b.x;
-    if (w != 0.0f) {
-      const float gx = dx ? wy : -wy, gy = dy ? wx : -wx;
-      a[5 * k + 3] += r.b.y * gx + r.b.z * gy;
-      a[5 * k + 4] += r.b.z * gx + r.b.w * gy;
-    }
+    // nodes of zero weight get no force (PhysicsGrid.cpp:443-445)
+    const bool on = w != 0.0f;
+    const float gx = on ? (dx ? wy : -wy) : 0.0f, gy = on ? (dy ? wx : -wx) : 0.0f;
+    a[5 * k + 3] += r.b.y * gx + r.b.z * gy;
+    a[5 * k + 4] += r.b.z * gx + r.b.w * gy;
   }
 }
 
@@ -317,13 +317,16 @@ __device__ __forceinline__ void fused_tile(const MixedArgs &A, const int bin, Fu
     float acc[20];
 #pragma unroll
     for (int k = 0; k < 20; ++k) acc[k] = 0.f;
+    // per-thread counters and flags, published once after the loop
+    unsigned left_window = 0, left_cell = 0;
+    bool nonfinite = false;
     for (int p = ps; p < pe; ++p) {
       const double2 u = nu;
       const float2 mv = nmv;
       float2 vel = nvel;
       float4 st = nst;
       const int fl = nfl;
-      if (p + 1 < pe) {
+      if (p + 1 < pe) { // (an unconditional reload of the last point was slower)
         nu = A.u[p + 1];
         nmv = A.mv[p + 1];
         nvel = A.v[p + 1];
@@ -371,17 +374,17 @@ __device__ __forceinline__ void fused_tile(const MixedArgs &A, const int bin, Fu
         const float apx = w00 * n00.z + w10 * n10.z + w01 * n01.z + w11 * n11.z;
         const float apy = w00 * n00.w + w10 * n10.w + w01 * n01.w + w11 * n11.w;
         constitutive_update(st, jh, Lxx, Lxy, Lyx, Lyy, A.dt, A.kappa, A.mu, A.dp_alpha);
-        float dux, duy;
+        // kinematically scripted points move with their own velocity
+        const bool kin = (fl & 2) != 0;
         const float dtih = A.dt * A.inv_h;
-        if (!(fl & 2)) {
+        const float dux = dtih * (kin ? vel.x : vpx);
+        const float duy = dtih * (kin ? vel.y : vpy);
+        {
           const float a = A.flip_alpha;
-          dux = dtih * vpx;
-          duy = dtih * vpy;
-          vel.x = (1.0f - a) * vpx + a * (vel.x + A.dt * apx);
-          vel.y = (1.0f - a) * vpy + a * (vel.y + A.dt * apy);
-        } else {
-          dux = dtih * vel.x;
-          duy = dtih * vel.y;
+          const float fvx = (1.0f - a) * vpx + a * (vel.x + A.dt * apx);
+          const float fvy = (1.0f - a) * vpy + a * (vel.y + A.dt * apy);
+          vel.x = kin ? vel.x : fvx;
+          vel.y = kin ? vel.y : fvy;
         }
         double2 un = make_double2(u.x + widen(dux), u.y + widen(duy));
         // new cell and fraction by FP32 carry of the old fraction
@@ -391,10 +394,13 @@ __device__ __forceinline__ void fused_tile(const MixedArgs &A, const int bin, Fu
         // the tile's plane mask bounds points that start in the window and
         // move less than a cell; any other point tests every plane
         const unsigned pmask = (in_window && !exact) ? plane_mask : (1u << A.nplanes) - 1u;
-        if (nfx >= 1.0f) { nfx -= 1.0f; ncx += 1; }
-        else if (nfx < 0.0f) { nfx += 1.0f; ncx -= 1; }
-        if (nfy >= 1.0f) { nfy -= 1.0f; ncy += 1; }
-        else if (nfy < 0.0f) { nfy += 1.0f; ncy -= 1; }
+        {
+          const float cx1 = floorf(nfx), cy1 = floorf(nfy); // -1, 0 or 1
+          ncx += (int)cx1;
+          ncy += (int)cy1;
+          nfx -= cx1;
+          nfy -= cy1;
+        }
         // MaterialPoints::resolvePlaneCollisions in grid units; FP32 test
         // first, FP64 where the point is within pmargin cells of a plane
         const float ufx = (float)ncx + nfx, ufy = (float)ncy + nfy;
@@ -422,16 +428,15 @@ __device__ __forceinline__ void fused_tile(const MixedArgs &A, const int bin, Fu
           split_u(un.x, ncx, nfx);
           split_u(un.y, ncy, nfy);
         }
-        if (!finite_d(un.x) || !finite_d(un.y) || !isfinite(vel.x + vel.y) ||
-            !isfinite(st.x))
-          atomicOr(A.status, (uint32_t)HG_STATUS_NONFINITE);
+        nonfinite |= !finite_d(un.x) | !finite_d(un.y) | !isfinite(vel.x + vel.y) |
+                     !isfinite(st.x);
         A.u[p] = un;
         A.v[p] = vel;
         A.strain[p] = st;
         A.flags[p] = (uint8_t)((fl & ~1) | jh);
         const int ngx = ncx - (X0 - DRIFT), ngy = ncy - (Y0 - DRIFT);
-        if (ngx < 0 || ngy < 0 || ngx > VA_W - 2 || ngy > VA_W - 2) atomicAdd(&s_out[0], 1u);
-        if (ncx != gcx || ncy != gcy) atomicAdd(&s_out[1], 1u);
+        left_window += (ngx < 0) | (ngy < 0) | (ngx > VA_W - 2) | (ngy > VA_W - 2);
+        left_cell += (ncx != gcx) | (ncy != gcy);
       }
       if (!in_grid_cell(A, ncx, ncy)) {
         atomicOr(A.status, (uint32_t)HG_STATUS_OUT_OF_GRID);
@@ -463,6 +468,9 @@ __device__ __forceinline__ void fused_tile(const MixedArgs &A, const int bin, Fu
         }
       }
     }
+    if (nonfinite) atomicOr(A.status, (uint32_t)HG_STATUS_NONFINITE);
+    if (left_window) atomicAdd(&s_out[0], left_window);
+    if (left_cell) atomicAdd(&s_out[1], left_cell);
 #pragma unroll
     for (int k = 0; k < 20; ++k) s_corner[k][tid] = acc[k];
     __syncthreads();
