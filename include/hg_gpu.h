@@ -322,6 +322,73 @@ hg_status hg_zones_boundary_samples(hg_zones *z, int64_t *count);
 double hg_zones_disk_box_area(double x0, double x1, double y0, double y1,
                               double cx, double cy, double r);
 
+/* ---- resampling (hybridgrains2dnew ResamplingTools), host code -----------
+ * The resampling step of HybridGrains2DSim::updateHybridStates_poorman
+ * (HybridGrains2DSim.cpp:327-536) after the zone labels are updated: grain
+ * and point insertion in the reconciliation (and direct-transition) zones
+ * and the inner continuum zones (CAvoidAVoid, AvoidAvoid.cpp:103-183), the
+ * inserted bodies' quantities, deletion by zone, and mass weights. Runs on the
+ * host on state copied from the device; bit-exact restatement of the
+ * reference's FP64 arithmetic and random streams (MT19937 of random.c,
+ * std::default_random_engine + std::normal_distribution for radii). */
+typedef struct hg_resampler hg_resampler;
+typedef struct {
+  hg_zones_desc zones;              /* the MPM grid and zone settings */
+  double mpm_grid_max[2];           /* PhysicsGrid::max after setDimensions */
+  int32_t basis;                    /* HG_BASIS_* of the MPM scene */
+  int32_t newly_inserted_continuum_stress_free;
+  double initial_particle_size;     /* cell width / samples per dimension */
+  double material_density;
+  double dem_r_mean, dem_r_std;     /* demRMean, demRStd (mean < 0: unset) */
+  double rho_dem;
+  double kappa, mu;                 /* bulk and shear modulus */
+  int32_t homogenize_stress, homogenize_velocity;
+} hg_resampler_desc;
+typedef struct {
+  int64_t points_inserted, grains_inserted, points_deleted, grains_deleted;
+} hg_resampler_stats;
+hg_status hg_resampler_create(const hg_resampler_desc *desc, hg_resampler **out);
+hg_status hg_resampler_destroy(hg_resampler *r);
+/* MaterialPoints arrays: q0, q, v 2 x n; m, volume, m0, volume0, hl, J n;
+ * be_bar 4 per point (column-major); just_homogenized, kinematic may be
+ * NULL (0). */
+hg_status hg_resampler_set_points(hg_resampler *r, int64_t n, const double *q0,
+                                  const double *q, const double *v, const double *m,
+                                  const double *volume, const double *m0,
+                                  const double *volume0, const double *hl,
+                                  const double *be_bar, const double *J,
+                                  const int32_t *just_homogenized,
+                                  const uint8_t *kinematic);
+/* RigidBody2DState: q0, q, v 3 x n; radius n; M0 3 x n (m, m, I); fixed
+ * may be NULL. */
+hg_status hg_resampler_set_grains(hg_resampler *r, int64_t n, const double *q0,
+                                  const double *q, const double *v, const double *radius,
+                                  const double *M0, const uint8_t *fixed);
+/* Finalised homogenised stress (4 per node, column-major) and velocity (2
+ * per node) of the MPM grid; NULL: zero. */
+hg_status hg_resampler_set_homogenized(hg_resampler *r, const double *stress,
+                                       const double *velocity);
+/* The resampling step with the labels of z (updated by hg_zones_update). */
+hg_status hg_resampler_run(hg_resampler *r, hg_zones *z);
+hg_status hg_resampler_counts(hg_resampler *r, int64_t *points, int64_t *grains,
+                              hg_resampler_stats *stats);
+/* The state after the step, in the layouts of the setters; w: mass weights.
+ * old_to_new maps the grains after insertion (before deletion) to their new
+ * index or -1 (hg_resampler_dem_map_size entries), for the contact history. */
+hg_status hg_resampler_get_points(hg_resampler *r, double *q0, double *q, double *v,
+                                  double *m, double *volume, double *m0,
+                                  double *volume0, double *w, double *hl,
+                                  double *be_bar, double *J, int32_t *just_homogenized,
+                                  uint8_t *kinematic);
+hg_status hg_resampler_get_grains(hg_resampler *r, double *q0, double *q, double *v,
+                                  double *radius, double *M0, double *w, uint8_t *fixed,
+                                  int32_t *old_to_new);
+hg_status hg_resampler_dem_map_size(hg_resampler *r, int64_t *n);
+/* The resampler's random streams, advanced by one draw (for tests). */
+uint32_t hg_resampler_random_u32(hg_resampler *r);
+float hg_resampler_random_f32(hg_resampler *r);
+double hg_resampler_random_radius(hg_resampler *r);
+
 /* ---- DEM (rigidbody2d, penalty map) --------------------------------------- */
 
 /* RigidBody2DStaticPlane, static (v = 0, omega = 0). */

@@ -600,3 +600,109 @@ class Zones:
 def disk_box_area(x0, x1, y0, y1, cx, cy, r):
     """Area of a disk inside an axis-aligned box (hg_zones_disk_box_area)."""
     return _capi.load().hg_zones_disk_box_area(x0, x1, y0, y1, cx, cy, r)
+
+
+class Resampler:
+    """The hybrid method's resampling step (ResamplingTools), host code of
+    libhg_gpu run at the resampling interval after Zones.update."""
+
+    def __init__(self, zones_desc_args, mpm_grid_max, basis, initial_particle_size,
+                 material_density, dem_r_mean, dem_r_std, rho_dem, kappa, mu,
+                 newly_inserted_continuum_stress_free=False, homogenize_stress=False,
+                 homogenize_velocity=False):
+        d = _capi.ResamplerDesc()
+        z = d.zones
+        (gmin, cw, cells, ls_cw, window, samples, thr, level, half, direct) = zones_desc_args
+        z.mpm_grid_min[:] = list(map(float, gmin))
+        z.mpm_cell_width = float(cw)
+        z.mpm_cells[:] = [int(cells[0]), int(cells[1])]
+        z.level_set_cell_width = float(ls_cw)
+        z.phi_window_size = float(window)
+        z.phi_samples_per_cell_side = int(samples)
+        z.phi_threshold = float(thr)
+        z.rzone_level_set = float(level)
+        z.rzone_half_thickness = float(half)
+        z.allow_direct_transitions = 1 if direct else 0
+        d.mpm_grid_max[:] = list(map(float, mpm_grid_max))
+        d.basis = int(basis)
+        d.newly_inserted_continuum_stress_free = 1 if newly_inserted_continuum_stress_free else 0
+        d.initial_particle_size = float(initial_particle_size)
+        d.material_density = float(material_density)
+        d.dem_r_mean, d.dem_r_std, d.rho_dem = float(dem_r_mean), float(dem_r_std), float(rho_dem)
+        d.kappa, d.mu = float(kappa), float(mu)
+        d.homogenize_stress = 1 if homogenize_stress else 0
+        d.homogenize_velocity = 1 if homogenize_velocity else 0
+        h = ctypes.c_void_p()
+        check("hg_resampler_create", ctypes.byref(d), ctypes.byref(h))
+        self._h = h
+        self.nodes = (int(cells[0]) + 1) * (int(cells[1]) + 1)
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _capi.load().hg_resampler_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_points(self, q0, q, v, m, vol, m0, vol0, hl, be, J, jh=None, kin=None):
+        a = [_f64(x) for x in (q0, q, v, m, vol, m0, vol0, hl, be, J)]
+        jh = None if jh is None else np.ascontiguousarray(jh, dtype=np.int32)
+        kin = None if kin is None else np.ascontiguousarray(kin, dtype=np.uint8)
+        check("hg_resampler_set_points", self._h, len(a[3]), *[_d(x) for x in a], _i32(jh),
+              _u8(kin))
+
+    def set_grains(self, q0, q, v, radius, M0, fixed=None):
+        a = [_f64(x) for x in (q0, q, v, radius, M0)]
+        fixed = None if fixed is None else np.ascontiguousarray(fixed, dtype=np.uint8)
+        check("hg_resampler_set_grains", self._h, len(a[3]), *[_d(x) for x in a], _u8(fixed))
+
+    def set_homogenized(self, stress=None, velocity=None):
+        check("hg_resampler_set_homogenized", self._h, _d(_f64(stress) if stress is not None else None),
+              _d(_f64(velocity) if velocity is not None else None))
+
+    def run(self, zones):
+        check("hg_resampler_run", self._h, zones._h)
+
+    def stats(self):
+        n, g = ctypes.c_int64(), ctypes.c_int64()
+        s = _capi.ResamplerStats()
+        check("hg_resampler_counts", self._h, ctypes.byref(n), ctypes.byref(g), ctypes.byref(s))
+        return n.value, g.value, dict(points_inserted=s.points_inserted,
+                                      grains_inserted=s.grains_inserted,
+                                      points_deleted=s.points_deleted,
+                                      grains_deleted=s.grains_deleted)
+
+    def points(self):
+        n, _, _ = self.stats()
+        out = dict(q0=np.zeros((n, 2)), q=np.zeros((n, 2)), v=np.zeros((n, 2)), m=np.zeros(n),
+                   vol=np.zeros(n), m0=np.zeros(n), vol0=np.zeros(n), w=np.zeros(n),
+                   hl=np.zeros(n), be=np.zeros((n, 4)), J=np.zeros(n),
+                   jh=np.zeros(n, dtype=np.int32), kin=np.zeros(n, dtype=np.uint8))
+        check("hg_resampler_get_points", self._h, *[_d(out[k]) for k in
+              ("q0", "q", "v", "m", "vol", "m0", "vol0", "w", "hl", "be", "J")],
+              _i32(out["jh"]), _u8(out["kin"]))
+        return out
+
+    def grains(self):
+        _, g, _ = self.stats()
+        k = ctypes.c_int64()
+        check("hg_resampler_dem_map_size", self._h, ctypes.byref(k))
+        out = dict(q0=np.zeros((g, 3)), q=np.zeros((g, 3)), v=np.zeros((g, 3)), r=np.zeros(g),
+                   M0=np.zeros((g, 3)), w=np.zeros(g), fixed=np.zeros(g, dtype=np.uint8),
+                   old_to_new=np.zeros(k.value, dtype=np.int32))
+        check("hg_resampler_get_grains", self._h, *[_d(out[x]) for x in
+              ("q0", "q", "v", "r", "M0", "w")], _u8(out["fixed"]), _i32(out["old_to_new"]))
+        return out
+
+    def random_u32(self):
+        return _capi.load().hg_resampler_random_u32(self._h)
+
+    def random_f32(self):
+        return _capi.load().hg_resampler_random_f32(self._h)
+
+    def random_radius(self):
+        return _capi.load().hg_resampler_random_radius(self._h)

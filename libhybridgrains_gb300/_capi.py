@@ -53,6 +53,20 @@ class ZonesDesc(ctypes.Structure):
                 ("rzone_half_thickness", ctypes.c_double)]
 
 
+class ResamplerDesc(ctypes.Structure):
+    _fields_ = [("zones", ZonesDesc), ("mpm_grid_max", ctypes.c_double * 2),
+                ("basis", ctypes.c_int32), ("newly_inserted_continuum_stress_free", ctypes.c_int32),
+                ("initial_particle_size", ctypes.c_double), ("material_density", ctypes.c_double),
+                ("dem_r_mean", ctypes.c_double), ("dem_r_std", ctypes.c_double),
+                ("rho_dem", ctypes.c_double), ("kappa", ctypes.c_double), ("mu", ctypes.c_double),
+                ("homogenize_stress", ctypes.c_int32), ("homogenize_velocity", ctypes.c_int32)]
+
+
+class ResamplerStats(ctypes.Structure):
+    _fields_ = [("points_inserted", ctypes.c_int64), ("grains_inserted", ctypes.c_int64),
+                ("points_deleted", ctypes.c_int64), ("grains_deleted", ctypes.c_int64)]
+
+
 class DemDesc(ctypes.Structure):
     _fields_ = [("gravity", ctypes.c_double * 2), ("kn", ctypes.c_double),
                 ("kt", ctypes.c_double), ("gamman", ctypes.c_double),
@@ -131,6 +145,19 @@ SIGNATURES = {
     "hg_zones_weights": [_P, _i32, _i64, _D, _i32, _D],
     "hg_zones_boundary_samples": [_P, _I64],
     "hg_zones_disk_box_area": [_dbl, _dbl, _dbl, _dbl, _dbl, _dbl, _dbl],
+    "hg_resampler_create": [ctypes.POINTER(ResamplerDesc), _PP],
+    "hg_resampler_destroy": [_P],
+    "hg_resampler_set_points": [_P, _i64, _D, _D, _D, _D, _D, _D, _D, _D, _D, _D, _I32, _U8],
+    "hg_resampler_set_grains": [_P, _i64, _D, _D, _D, _D, _D, _U8],
+    "hg_resampler_set_homogenized": [_P, _D, _D],
+    "hg_resampler_run": [_P, _P],
+    "hg_resampler_counts": [_P, _I64, _I64, ctypes.POINTER(ResamplerStats)],
+    "hg_resampler_get_points": [_P, _D, _D, _D, _D, _D, _D, _D, _D, _D, _D, _D, _I32, _U8],
+    "hg_resampler_get_grains": [_P, _D, _D, _D, _D, _D, _D, _U8, _I32],
+    "hg_resampler_dem_map_size": [_P, _I64],
+    "hg_resampler_random_u32": [_P],
+    "hg_resampler_random_f32": [_P],
+    "hg_resampler_random_radius": [_P],
     "hg_dem_create": [_P, ctypes.POINTER(DemDesc), _PP],
     "hg_dem_destroy": [_P],
     "hg_dem_upload": [_P, _i64, _D, _D, _D, _D, _D, _U8],
@@ -152,6 +179,8 @@ SIGNATURES = {
 }
 _RET = {"hg_status_string": ctypes.c_char_p, "hg_last_error": ctypes.c_char_p,
         "hg_zones_disk_box_area": ctypes.c_double,
+        "hg_resampler_random_u32": ctypes.c_uint32, "hg_resampler_random_f32": ctypes.c_float,
+        "hg_resampler_random_radius": ctypes.c_double,
         "hg_kernel_launch_count": ctypes.c_int64}
 
 _lib = None

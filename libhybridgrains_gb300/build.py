@@ -30,8 +30,9 @@ SOURCES = [
     ("dem.cu", True),
     ("coupling.cu", True),
     ("zones.cu", True),  # host code (zone labels)
+    ("resampling.cu", True),  # host code (resampling)
 ]
-HEADERS = ["hg_internal.cuh", "mpm_basis.cuh", "scan_block.cuh"]
+HEADERS = ["hg_internal.cuh", "mpm_basis.cuh", "scan_block.cuh", "zones_internal.cuh"]
 
 
 def _nvcc():

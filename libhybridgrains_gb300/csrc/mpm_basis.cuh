@@ -1,4 +1,4 @@
-// FP64 MPM basis functions on the device (linear and uGIMP linear), with the
+// FP64 MPM basis functions (linear and uGIMP linear), device and host, with the
 // reference's operation order. Included by translation units compiled with
 // --fmad=false.
 #pragma once
@@ -6,17 +6,17 @@
 namespace hg {
 
 // LinearBasisFunctions.cpp:6-13
-__device__ __forceinline__ double linear_n(double x) {
+__host__ __device__ __forceinline__ double linear_n(double x) {
   const double a = fabs(x);
   return a < 1.0 ? 1.0 - a : 0.0;
 }
 // LinearBasisFunctions.cpp:16-22
-__device__ __forceinline__ double linear_dn(double x) {
+__host__ __device__ __forceinline__ double linear_dn(double x) {
   if (fabs(x) <= 1.0) return (x >= 0.0) ? -1.0 : 1.0;
   return 0.0;
 }
 // uGIMPLinearBasisFunctions.cpp:6-22
-__device__ __forceinline__ double lin_integral(double xp, double hl, double xi,
+__host__ __device__ __forceinline__ double lin_integral(double xp, double hl, double xi,
                                                double w) {
   const double diff = fabs(xp - xi);
   if (diff >= w + hl) return 0.0;
@@ -25,7 +25,7 @@ __device__ __forceinline__ double lin_integral(double xp, double hl, double xi,
   return 2.0 * hl - (hl * hl + diff * diff) / w;
 }
 // uGIMPLinearBasisFunctions.cpp:24-42
-__device__ __forceinline__ double lin_integral_grad(double xp, double hl,
+__host__ __device__ __forceinline__ double lin_integral_grad(double xp, double hl,
                                                     double xi, double w) {
   const double diff = fabs(xp - xi);
   const double sgn = (xp - xi) >= 0.0 ? 1.0 : -1.0;
@@ -37,7 +37,7 @@ __device__ __forceinline__ double lin_integral_grad(double xp, double hl,
 
 // LinearBasisFunctions.cpp:49-62 / uGIMPLinearBasisFunctions.cpp:71-94.
 // Inclusive node range; negative or too-large values mean out of grid.
-__device__ __forceinline__ void stencil64(int basis, double x, double y,
+__host__ __device__ __forceinline__ void stencil64(int basis, double x, double y,
                                           double hl, double gx, double gy,
                                           double h, int &x0, int &y0, int &x1,
                                           int &y1) {
@@ -55,7 +55,7 @@ __device__ __forceinline__ void stencil64(int basis, double x, double y,
 }
 
 // LinearBasisFunctions.cpp:81-97 / uGIMPLinearBasisFunctions.cpp:110-123
-__device__ __forceinline__ double weight64(int basis, double x, double y,
+__host__ __device__ __forceinline__ double weight64(int basis, double x, double y,
                                            double hl, int ix, int iy, double gx,
                                            double gy, double h) {
   if (basis == HG_BASIS_LINEAR) {
@@ -70,7 +70,7 @@ __device__ __forceinline__ double weight64(int basis, double x, double y,
 }
 
 // LinearBasisFunctions.cpp:115-136 / uGIMPLinearBasisFunctions.cpp:139-156
-__device__ __forceinline__ void weight_grad64(int basis, double x, double y,
+__host__ __device__ __forceinline__ void weight_grad64(int basis, double x, double y,
                                               double hl, int ix, int iy,
                                               double gx, double gy, double h,
                                               double &ox, double &oy) {

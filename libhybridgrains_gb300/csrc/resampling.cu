@@ -1,0 +1,860 @@
+// Resampling of the hybrid method (ResamplingTools + CAvoidAVoid,
+// hybridgrains2dnew/ResamplingTools.cpp and AvoidAvoid.cpp), host code run
+// at the resampling interval on state copied from the device, after the
+// zone labels (zones.cu) are updated. One call does what
+// HybridGrains2DSim::updateHybridStates_poorman does between computeRZones
+// and the mass-weight update (HybridGrains2DSim.cpp:327-536):
+//
+//   1. new grains in the reconciliation zones and new material points in the
+//      reconciliation (and direct-transition) zones and in the inner
+//      continuum zones, by random insertion without overlap;
+//   2. their quantities: masses/volumes per hybrid cell, Gaussian-weighted
+//      neighbour averages of J, be_bar, velocity and reference position
+//      (or the homogenised stress and velocity), mass-weighted grid fields
+//      for inner continuum points, and the mass/volume shared with their
+//      neighbours;
+//   3. deletion of points in discrete cells and of grains in continuum
+//      cells (and of anything outside the MPM grid);
+//   4. the DEM and MPM mass weights (1, 0.5 or 0 by zone) and the masses.
+//
+// The random stream is MT19937 in the form of hybridgrains2dnew/random.c
+// (Knuth's 69069 seeding, default seed 4357, float outputs) for positions,
+// and std::default_random_engine + std::normal_distribution for grain radii,
+// as the reference uses them. Everything runs in the reference's order, with
+// FP64 expressions in its evaluation order (this file is compiled without
+// FMA contraction); results are bit-exact against the oracle.
+#include "hg_internal.cuh"
+#include "mpm_basis.cuh"
+#include "zones_internal.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <new>
+#include <random>
+#include <vector>
+
+namespace {
+
+// MT19937 (Matsumoto and Nishimura, 1998), with the 1998 reference code's
+// seeding and single-precision output in [0, 1).
+struct Mt19937 {
+  static constexpr int N = 624, M = 397;
+  uint32_t s[N];
+  int i = N + 1; // not seeded
+  void seed(uint32_t v) {
+    s[0] = v;
+    for (i = 1; i < N; ++i) s[i] = 69069u * s[i - 1];
+  }
+  uint32_t next() {
+    if (i >= N) {
+      if (i == N + 1) seed(4357u);
+      for (int k = 0; k < N; ++k) {
+        const uint32_t y = (s[k] & 0x80000000u) | (s[(k + 1) % N] & 0x7fffffffu);
+        s[k] = s[(k + M) % N] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+      }
+      i = 0;
+    }
+    uint32_t y = s[i++];
+    y ^= y >> 11;
+    y ^= (y << 7) & 0x9d2c5680u;
+    y ^= (y << 15) & 0xefc60000u;
+    y ^= y >> 18;
+    return y;
+  }
+  float uniform() { return (float)next() * 2.3283064365386963e-10f; }
+};
+
+inline double dist2d(double ax, double ay, double bx, double by) {
+  const double dx = ax - bx, dy = ay - by;
+  return std::sqrt(dx * dx + dy * dy);
+}
+
+// CUniformGridH2D (uniformgrid.cpp) with growable per-cell id lists.
+struct CellLists {
+  double mn[2] = {0, 0}, cw = 1.0;
+  unsigned res[2] = {1, 1};
+  std::vector<std::vector<int>> ids;
+  void reset(double x0, double y0, unsigned rx, unsigned ry, double w) {
+    mn[0] = x0;
+    mn[1] = y0;
+    res[0] = std::max(rx, 1u);
+    res[1] = std::max(ry, 1u);
+    cw = w;
+    ids.assign((size_t)res[0] * res[1], {});
+  }
+  void cell(double x, double y, unsigned &i, unsigned &j) const {
+    const double u = (x - mn[0]) / cw, v = (y - mn[1]) / cw;
+    i = (unsigned)std::max<int>(0, std::min<int>((int)res[0] - 1, (int)std::floor(u)));
+    j = (unsigned)std::max<int>(0, std::min<int>((int)res[1] - 1, (int)std::floor(v)));
+  }
+  void add_box(double x0, double y0, double x1, double y1, int id) {
+    unsigned i0, j0, i1, j1;
+    cell(x0, y0, i0, j0);
+    cell(x1, y1, i1, j1);
+    for (unsigned j = j0; j <= j1; ++j)
+      for (unsigned i = i0; i <= i1; ++i) ids[(size_t)j * res[0] + i].push_back(id);
+  }
+  void add_point(double x, double y, int id) {
+    unsigned i, j;
+    cell(x, y, i, j);
+    ids[(size_t)j * res[0] + i].push_back(id);
+  }
+  const std::vector<int> &at(unsigned i, unsigned j) const {
+    static const std::vector<int> none;
+    if (i >= res[0] || j >= res[1]) return none;
+    return ids[(size_t)j * res[0] + i];
+  }
+};
+
+} // namespace
+
+struct hg_resampler {
+  hg_resampler_desc d{};
+  double grid_h = 0.0; // cell width of the interpolation grids, (max - min) / n
+  Mt19937 mt;
+  std::default_random_engine gen;
+  std::normal_distribution<double> radius_dist;
+  int test_id = 100;
+  // MPM points (MaterialPoints)
+  std::vector<double> q0, q, v, m, vol, m0, vol0, w, hl, be, J;
+  std::vector<int32_t> jh;
+  std::vector<uint8_t> kin;
+  // DEM bodies (RigidBody2DState)
+  std::vector<double> dq0, dq, dv, dr, M0, dw;
+  std::vector<uint8_t> fixed;
+  std::vector<int32_t> dem_map; // old (after insertion) -> new index, -1 deleted
+  // homogenised fields per node: stress 4 (column-major), velocity 2
+  std::vector<double> hs, hv;
+  hg_resampler_stats stats{};
+};
+
+namespace {
+
+using Box = hg_zones::Box;
+
+size_t npoints(const hg_resampler &r) { return r.m.size(); }
+size_t nbodies(const hg_resampler &r) { return r.dr.size(); }
+
+// CAvoidAVoid::avoidAVoid with randomFillRegion (AvoidAvoid.cpp:103-183):
+// bodies (px, py, rad) grow by the accepted samples.
+template <typename Sampler>
+hg_status fill_regions(hg_resampler &R, const std::vector<Box> &regions, double mean_r,
+                       std::vector<double> &px, std::vector<double> &py,
+                       std::vector<double> &rad, Sampler sampler) {
+  if (regions.empty()) return HG_OK;
+  double lo[2] = {regions[0].b[0], regions[0].b[1]}, up[2] = {regions[0].b[2], regions[0].b[3]};
+  for (size_t k = 1; k < regions.size(); ++k) {
+    lo[0] = std::min(lo[0], regions[k].b[0]);
+    lo[1] = std::min(lo[1], regions[k].b[1]);
+    up[0] = std::max(up[0], regions[k].b[2]);
+    up[1] = std::max(up[1], regions[k].b[3]);
+  }
+  const double g0x = lo[0] - 6.0 * mean_r, g0y = lo[1] - 6.0 * mean_r;
+  const double g1x = up[0] + 6.0 * mean_r, g1y = up[1] + 6.0 * mean_r;
+  const double cw = 4.0 * mean_r;
+  CellLists grid;
+  grid.reset(g0x, g0y, (unsigned)std::ceil((g1x - g0x) / cw), (unsigned)std::ceil((g1y - g0y) / cw),
+             cw);
+  std::vector<int> mail(px.size(), 0);
+  for (size_t b = 0; b < px.size(); ++b)
+    grid.add_box(px[b] - rad[b], py[b] - rad[b], px[b] + rad[b], py[b] + rad[b], (int)b);
+  auto next_test = [&]() {
+    if (++R.test_id == 0) R.test_id = 1;
+  };
+  auto conflict = [&](double x, double y, double r) {
+    const int t = R.test_id;
+    unsigned i0, j0, i1, j1;
+    grid.cell(x - r, y - r, i0, j0);
+    grid.cell(x + r, y + r, i1, j1);
+    for (unsigned j = j0; j <= j1; ++j)
+      for (unsigned i = i0; i <= i1; ++i)
+        for (int id : grid.at(i, j)) {
+          if (mail[id] == t) continue;
+          mail[id] = t;
+          if (dist2d(px[id], py[id], x, y) < (rad[id] + r) * 0.97) {
+            next_test();
+            return true;
+          }
+        }
+    next_test();
+    return false;
+  };
+  for (const Box &reg : regions) {
+    const double dx = reg.b[2] - reg.b[0], dy = reg.b[3] - reg.b[1];
+    for (int trial = 0; trial < 16; ++trial) {
+      const double x = (double)R.mt.uniform() * dx + reg.b[0];
+      const double y = (double)R.mt.uniform() * dy + reg.b[1];
+      double r;
+      const hg_status st = sampler(r);
+      if (st != HG_OK) return st;
+      if (conflict(x, y, r)) continue;
+      const int id = (int)px.size();
+      px.push_back(x);
+      py.push_back(y);
+      rad.push_back(r);
+      mail.push_back(0);
+      grid.add_box(x - r, y - r, x + r, y + r, id);
+    }
+  }
+  return HG_OK;
+}
+
+// avoidAVoidMPMparticlesInsideZonesWithTentativeQuantities
+// (ResamplingTools.cpp:58-104): returns the count before insertion.
+hg_status insert_points(hg_resampler &R, const std::vector<Box> &zones, int64_t &before) {
+  const double rp = 0.5 * R.d.initial_particle_size;
+  const size_t n = npoints(R);
+  before = (int64_t)n;
+  std::vector<double> px(n), py(n), rad(n, rp);
+  for (size_t p = 0; p < n; ++p) {
+    px[p] = R.q[2 * p];
+    py[p] = R.q[2 * p + 1];
+  }
+  const hg_status st = fill_regions(R, zones, rp, px, py, rad, [&](double &r) -> hg_status {
+    r = rp;
+    return HG_OK;
+  });
+  if (st != HG_OK) return st;
+  const double hl0 = R.d.initial_particle_size * 0.5;
+  for (size_t p = n; p < px.size(); ++p) { // addMaterialPoint, MaterialPoints.cpp:439-467
+    R.q0.push_back(px[p]);
+    R.q0.push_back(py[p]);
+    R.q.push_back(px[p]);
+    R.q.push_back(py[p]);
+    R.v.push_back(0.0);
+    R.v.push_back(0.0);
+    R.m.push_back(0.0);
+    R.vol.push_back(0.0);
+    R.m0.push_back(0.0);
+    R.vol0.push_back(0.0);
+    R.w.push_back(1.0);
+    R.hl.push_back(hl0);
+    const double I4[4] = {1.0, 0.0, 0.0, 1.0};
+    R.be.insert(R.be.end(), I4, I4 + 4);
+    R.J.push_back(1.0);
+    R.jh.push_back(0);
+    R.kin.push_back(0);
+  }
+  R.stats.points_inserted += (int64_t)(px.size() - n);
+  return HG_OK;
+}
+
+// avoidAVoidDEMparticlesInsideZonesWithTentativeQuantities
+// (ResamplingTools.cpp:106-196) with randomRadiusSampler (:19-26).
+hg_status insert_grains(hg_resampler &R, const std::vector<Box> &zones, int64_t &before) {
+  const size_t n = nbodies(R);
+  before = (int64_t)n;
+  std::vector<double> px(n), py(n), rad(R.dr);
+  for (size_t b = 0; b < n; ++b) {
+    px[b] = R.dq[3 * b];
+    py[b] = R.dq[3 * b + 1];
+  }
+  double r_mean = R.d.dem_r_mean;
+  const double lo = R.d.dem_r_mean - 2.0 * R.d.dem_r_std, hi = R.d.dem_r_mean + 2.0 * R.d.dem_r_std;
+  bool unset = false;
+  if (R.d.dem_r_mean < 0.0) { // the first radius, without spread
+    if (n == 0) return hg::fail(HG_ERR_INVALID_ARGUMENT, "no grain radius to sample from");
+    r_mean = rad[0];
+    R.radius_dist = std::normal_distribution<double>(rad[0], 0.0);
+    unset = true;
+  }
+  const hg_status st = fill_regions(R, zones, r_mean, px, py, rad, [&](double &r) -> hg_status {
+    if (unset) {
+      // the reference's rejection bounds stay at the unset mean and would
+      // never accept: take the sampled radius as is
+      r = R.radius_dist(R.gen);
+      return HG_OK;
+    }
+    r = -1.0e33;
+    for (int k = 0; r < lo || r > hi; ++k) {
+      if (k == 1000000) return hg::fail(HG_ERR_INVALID_ARGUMENT, "grain radius sampler does not accept");
+      r = R.radius_dist(R.gen);
+    }
+    return HG_OK;
+  });
+  if (st != HG_OK) return st;
+  const double pi = 3.14159265358979323846;
+  for (size_t b = n; b < px.size(); ++b) { // RigidBody2DState::addBodies
+    const double r = rad[b];
+    const double m = R.d.rho_dem * pi * r * r; // CircleGeometry::massAndInertia
+    const double I = 0.5 * m * r * r;
+    const double q3[3] = {px[b], py[b], 0.0}, z3[3] = {0.0, 0.0, 0.0}, m3[3] = {m, m, I};
+    R.dq.insert(R.dq.end(), q3, q3 + 3);
+    R.dq0.insert(R.dq0.end(), q3, q3 + 3);
+    R.dv.insert(R.dv.end(), z3, z3 + 3);
+    R.dr.push_back(r);
+    R.M0.insert(R.M0.end(), m3, m3 + 3);
+    R.dw.push_back(1.0);
+    R.fixed.push_back(0);
+  }
+  R.stats.grains_inserted += (int64_t)(px.size() - n);
+  return HG_OK;
+}
+
+// Uniform grids over the MPM cells with points and grains as points
+// (ZoneTools::setupUniformGridElementsAsPoints, ZoneTools.cpp:800-827).
+void point_grids(const hg_resampler &R, CellLists &cont, CellLists &disc) {
+  const hg_zones_desc &zd = R.d.zones;
+  cont.reset(zd.mpm_grid_min[0], zd.mpm_grid_min[1], zd.mpm_cells[0], zd.mpm_cells[1],
+             zd.mpm_cell_width);
+  disc.reset(zd.mpm_grid_min[0], zd.mpm_grid_min[1], zd.mpm_cells[0], zd.mpm_cells[1],
+             zd.mpm_cell_width);
+  for (size_t p = 0; p < npoints(R); ++p) cont.add_point(R.q[2 * p], R.q[2 * p + 1], (int)p);
+  for (size_t b = 0; b < nbodies(R); ++b) disc.add_point(R.dq[3 * b], R.dq[3 * b + 1], (int)b);
+}
+
+template <typename F>
+void for_range(const CellLists &g, double x0, double y0, double x1, double y1, F f) {
+  unsigned i0, j0, i1, j1;
+  g.cell(x0, y0, i0, j0);
+  g.cell(x1, y1, i1, j1);
+  for (unsigned j = j0; j <= j1; ++j)
+    for (unsigned i = i0; i <= i1; ++i)
+      for (int id : g.at(i, j)) f(id);
+}
+
+// Node range of a stencil as the reference iterates it: its bounds are cast
+// to unsigned, so a stencil starting left of or below the grid (x - hl <
+// grid min for uGIMP) runs no iteration at all; nodes past the last one are
+// skipped (the reference would read past its arrays there).
+inline bool stencil_range(int a0, int a1, int last, int &b0, int &b1) {
+  if (a0 < 0) return false;
+  b0 = a0;
+  b1 = std::min(a1, last);
+  return b0 <= b1;
+}
+
+// Interpolation of a node field with the MPM basis at half width hl
+// (computeStencil / weight over the physics grid).
+void interp_nodes(const hg_resampler &R, double x, double y, double hl, double gmin_x,
+                  double gmin_y, double h, int nx, const std::vector<double> &field, int len,
+                  double *out) {
+  for (int c = 0; c < len; ++c) out[c] = 0.0;
+  const int ny = R.d.zones.mpm_cells[1];
+  int x0, y0, x1, y1, i0, i1, j0, j1;
+  hg::stencil64(R.d.basis, x, y, hl, gmin_x, gmin_y, h, x0, y0, x1, y1);
+  if (!stencil_range(y0, y1, ny, j0, j1) || !stencil_range(x0, x1, nx, i0, i1)) return;
+  for (int iy = j0; iy <= j1; ++iy)
+    for (int ix = i0; ix <= i1; ++ix) {
+      const double wgt = hg::weight64(R.d.basis, x, y, hl, ix, iy, gmin_x, gmin_y, h);
+      const size_t node = (size_t)iy * (nx + 1) + ix;
+      for (int c = 0; c < len; ++c) out[c] += wgt * field[node * len + c];
+    }
+}
+
+// 2x2 determinant in column-major storage (a00, a10, a01, a11)
+inline double det2(const double *a) { return a[0] * a[3] - a[1] * a[2]; }
+
+// ConstitutiveModel::computeStrainFromCauchyStress (ConstitutiveModel.cpp:99-117)
+void strain_from_stress(const double *s, double kappa, double mu, double &J, double *be) {
+  const double T = s[0] + s[3];
+  J = 0.5 * (T / kappa + std::sqrt((T * T) / (kappa * kappa) + 4.0));
+  double dev[4] = {s[0] - T * 1.0 / 2.0, s[1] - T * 0.0 / 2.0, s[2] - T * 0.0 / 2.0,
+                   s[3] - T * 1.0 / 2.0};
+  for (int c = 0; c < 4; ++c) dev[c] = J * dev[c] / mu;
+  const double t = std::sqrt(1.0 - det2(dev));
+  be[0] = dev[0] + t * 1.0;
+  be[1] = dev[1] + t * 0.0;
+  be[2] = dev[2] + t * 0.0;
+  be[3] = dev[3] + t * 1.0;
+}
+
+// determineMPMQuantitiesForHybridZones (ResamplingTools.cpp:616-639) with
+// reassignMassAndVolumesForHybridAndNewlyGeneratedContinuumZone (:379-400)
+// and reassignJVelAndBebarForHybridMaterialPoint (:402-612).
+void hybrid_point_quantities(hg_resampler &R, const std::vector<Box> &zones, int64_t before,
+                             int64_t after, int64_t grains_before, const CellLists &cont,
+                             const CellLists &disc) {
+  const hg_zones_desc &zd = R.d.zones;
+  const double cell_volume = zd.mpm_cell_width * zd.mpm_cell_width;
+  const double mass_per_cell = R.d.material_density * cell_volume;
+  for (const Box &z : zones) {
+    const std::vector<int> &ids = cont.at((unsigned)z.c[0], (unsigned)z.c[1]);
+    const int n = (int)ids.size();
+    for (int id : ids) {
+      R.m0[id] = mass_per_cell / n;
+      R.vol0[id] = cell_volume / n;
+    }
+  }
+  const double size = R.d.initial_particle_size;
+  const double sigma = 0.5 * size, max_dist = 3.0 * size;
+  const double hh = zd.mpm_cell_width * 0.25;
+  for (int64_t p = before; p < after; ++p) {
+    const double x = R.q[2 * p], y = R.q[2 * p + 1];
+    double vs[2] = {0, 0}, q0s[2] = {0, 0}, Js = 0.0, bes[4] = {0, 0, 0, 0}, ws = 0.0;
+    int nn = 0;
+    for_range(cont, x - max_dist, y - max_dist, x + max_dist, y + max_dist, [&](int id) {
+      if (id >= before) return;
+      const double d = dist2d(R.q[2 * id], R.q[2 * id + 1], x, y);
+      if (d <= max_dist) {
+        const double wgt = std::exp(-(d * d) / (2.0 * sigma * sigma));
+        vs[0] += R.v[2 * id] * wgt;
+        vs[1] += R.v[2 * id + 1] * wgt;
+        q0s[0] += R.q0[2 * id] * wgt;
+        q0s[1] += R.q0[2 * id + 1] * wgt;
+        Js += R.J[id] * wgt;
+        for (int c = 0; c < 4; ++c) bes[c] += R.be[4 * id + c] * wgt;
+        ws += wgt;
+        ++nn;
+      }
+    });
+    double stress[4] = {0, 0, 0, 0}, hvel[2] = {0, 0};
+    if (R.d.homogenize_stress)
+      interp_nodes(R, x, y, hh, zd.mpm_grid_min[0], zd.mpm_grid_min[1], zd.mpm_cell_width,
+                   zd.mpm_cells[0], R.hs, 4, stress);
+    if (R.d.homogenize_velocity)
+      interp_nodes(R, x, y, hh, zd.mpm_grid_min[0], zd.mpm_grid_min[1], zd.mpm_cell_width,
+                   zd.mpm_cells[0], R.hv, 2, hvel);
+    double Jn, ben[4];
+    if (nn == 0) {
+      Jn = 1.0;
+      ben[0] = 1.0, ben[1] = 0.0, ben[2] = 0.0, ben[3] = 1.0;
+    } else {
+      Jn = Js / ws;
+      for (int c = 0; c < 4; ++c) ben[c] = bes[c] / ws;
+      const double sd = std::sqrt(det2(ben));
+      for (int c = 0; c < 4; ++c) ben[c] = ben[c] / sd;
+    }
+    for_range(disc, x - max_dist, y - max_dist, x + max_dist, y + max_dist, [&](int id) {
+      if (id >= grains_before) return;
+      const double d = dist2d(R.dq[3 * id], R.dq[3 * id + 1], x, y);
+      if (d <= max_dist) {
+        const double wgt = std::exp(-(d * d) / (2.0 * sigma * sigma));
+        vs[0] += R.dv[3 * id] * wgt;
+        vs[1] += R.dv[3 * id + 1] * wgt;
+        q0s[0] += R.dq0[3 * id] * wgt;
+        q0s[1] += R.dq0[3 * id + 1] * wgt;
+        ws += wgt;
+      }
+    });
+    double vn[2], q0n[2];
+    if (ws == 0.0) {
+      vn[0] = vn[1] = 0.0;
+      q0n[0] = x;
+      q0n[1] = y;
+    } else {
+      vn[0] = vs[0] / ws;
+      vn[1] = vs[1] / ws;
+      q0n[0] = q0s[0] / ws;
+      q0n[1] = q0s[1] / ws;
+    }
+    R.q0[2 * p] = q0n[0];
+    R.q0[2 * p + 1] = q0n[1];
+    R.v[2 * p] = R.d.homogenize_velocity ? hvel[0] : vn[0];
+    R.v[2 * p + 1] = R.d.homogenize_velocity ? hvel[1] : vn[1];
+    if (R.d.homogenize_stress) {
+      strain_from_stress(stress, R.d.kappa, R.d.mu, Jn, ben);
+      R.J[p] = Jn;
+    } else {
+      R.J[p] = R.d.newly_inserted_continuum_stress_free ? 1.0 : Jn;
+    }
+    for (int c = 0; c < 4; ++c) R.be[4 * p + c] = ben[c];
+  }
+}
+
+// determineDEMQuantitiesForHybridZones (ResamplingTools.cpp:646-725)
+void grain_quantities(hg_resampler &R, int64_t before, int64_t after, int64_t points_before,
+                      const CellLists &cont, const CellLists &disc) {
+  const double sigma = R.d.dem_r_mean, max_dist = 6.0 * R.d.dem_r_mean;
+  for (int64_t b = before; b < after; ++b) {
+    const double x = R.dq[3 * b], y = R.dq[3 * b + 1];
+    double vs[3] = {0, 0, 0}, q0s[3] = {0, 0, 0}, ws = 0.0;
+    for_range(disc, x - max_dist, y - max_dist, x + max_dist, y + max_dist, [&](int id) {
+      if (id >= before) return;
+      const double d = dist2d(R.dq[3 * id], R.dq[3 * id + 1], x, y);
+      if (d <= max_dist) {
+        const double wgt = std::exp(-(d * d) / (2.0 * sigma * sigma));
+        for (int c = 0; c < 3; ++c) {
+          vs[c] += R.dv[3 * id + c] * wgt;
+          q0s[c] += R.dq0[3 * id + c] * wgt;
+        }
+        ws += wgt;
+      }
+    });
+    for_range(cont, x - max_dist, y - max_dist, x + max_dist, y + max_dist, [&](int id) {
+      if (id >= points_before) return;
+      const double d = dist2d(R.q[2 * id], R.q[2 * id + 1], x, y);
+      if (d <= max_dist) {
+        const double wgt = std::exp(-(d * d) / (2.0 * sigma * sigma));
+        vs[0] += R.v[2 * id] * wgt;
+        vs[1] += R.v[2 * id + 1] * wgt;
+        vs[2] += 0.0 * wgt;
+        q0s[0] += R.q0[2 * id] * wgt;
+        q0s[1] += R.q0[2 * id + 1] * wgt;
+        q0s[2] += 0.0 * wgt;
+        ws += wgt;
+      }
+    });
+    if (ws == 0.0) {
+      for (int c = 0; c < 3; ++c) R.dv[3 * b + c] = 0.0;
+      R.dq0[3 * b] = x;
+      R.dq0[3 * b + 1] = y;
+      R.dq0[3 * b + 2] = 0.0;
+    } else {
+      for (int c = 0; c < 3; ++c) {
+        R.dv[3 * b + c] = vs[c] / ws;
+        R.dq0[3 * b + c] = q0s[c] / ws;
+      }
+    }
+  }
+}
+
+// Mass-weighted node field of the first n points (Grid::rasterizeMass +
+// rasterizeMassWeightedValues* + normalizationByMass, Grid.cpp:148-348).
+void mass_weighted_field(const hg_resampler &R, int64_t n, int len, const std::vector<double> &vals,
+                         const double *dflt, std::vector<double> &out) {
+  const hg_zones_desc &zd = R.d.zones;
+  const int nx = zd.mpm_cells[0], ny = zd.mpm_cells[1];
+  const size_t nn = (size_t)(nx + 1) * (ny + 1);
+  std::vector<double> mass(nn, 0.0);
+  out.assign(nn * len, 0.0);
+  const double h1 = R.hl.empty() ? 0.0 : R.hl[0];
+  for (int64_t p = 0; p < n; ++p) {
+    const double x = R.q[2 * p], y = R.q[2 * p + 1];
+    int x0, y0, x1, y1, i0, i1, j0, j1;
+    hg::stencil64(R.d.basis, x, y, h1, zd.mpm_grid_min[0], zd.mpm_grid_min[1], R.grid_h, x0, y0,
+                  x1, y1);
+    if (!stencil_range(y0, y1, ny, j0, j1) || !stencil_range(x0, x1, nx, i0, i1)) continue;
+    for (int iy = j0; iy <= j1; ++iy)
+      for (int ix = i0; ix <= i1; ++ix) {
+        const double wgt = hg::weight64(R.d.basis, x, y, h1, ix, iy, zd.mpm_grid_min[0],
+                                        zd.mpm_grid_min[1], R.grid_h);
+        const size_t node = (size_t)iy * (nx + 1) + ix;
+        mass[node] += wgt * R.m[p];
+        for (int c = 0; c < len; ++c) out[node * len + c] += wgt * R.m[p] * vals[(size_t)p * len + c];
+      }
+  }
+  for (size_t node = 0; node < nn; ++node) {
+    if (mass[node] > 0.0) {
+      for (int c = 0; c < len; ++c) out[node * len + c] /= mass[node];
+    } else {
+      for (int c = 0; c < len; ++c) out[node * len + c] = dflt[c];
+    }
+  }
+}
+
+// determineMPMQuantitiesForInnerContinuumZones (ResamplingTools.cpp:353-377)
+// with computeFieldsForInterpolation (:276-333), gatherMassAndVolume
+// (:198-274) and reassignJVelAndBebarForInternalMaterialPoint (:335-366).
+void inner_point_quantities(hg_resampler &R, int64_t before, int64_t after, const CellLists &cont) {
+  const hg_zones_desc &zd = R.d.zones;
+  std::vector<double> fJ, fv, fb;
+  const double dJ[1] = {1.0}, dv[2] = {0.0, 0.0}, db[4] = {1.0, 0.0, 0.0, 1.0};
+  mass_weighted_field(R, before, 1, R.J, dJ, fJ);
+  mass_weighted_field(R, before, 2, R.v, dv, fv);
+  mass_weighted_field(R, before, 4, R.be, db, fb);
+  const double size = R.d.initial_particle_size;
+  const double sigma = 0.5 * size, rr = 2.0 * size;
+  for (int64_t i = before; i < after; ++i) { // gatherMassAndVolume
+    const double x = R.q[2 * i], y = R.q[2 * i + 1];
+    double tm = 0.0, tv = 0.0, ws = 0.0, q0s[2] = {0, 0};
+    std::vector<int> nb;
+    for_range(cont, x - rr, y - rr, x + rr, y + rr, [&](int id) {
+      if (id >= i) return;
+      const double ex = x - R.q[2 * id], ey = y - R.q[2 * id + 1];
+      const double d2 = ex * ex + ey * ey;
+      if (d2 < rr * rr) {
+        const double wgt = std::exp(-(d2 * d2) / (2.0 * sigma * sigma));
+        ws += wgt;
+        q0s[0] += wgt * R.q0[2 * id];
+        q0s[1] += wgt * R.q0[2 * id + 1];
+        nb.push_back(id);
+        tm += R.m0[id];
+        tv += R.vol0[id];
+      }
+    });
+    const int count = (int)nb.size();
+    // with no neighbour the reference leaves 0/0 here
+    R.q0[2 * i] = q0s[0] / ws;
+    R.q0[2 * i + 1] = q0s[1] / ws;
+    R.m0[i] = tm / (count + 1.0);
+    R.vol0[i] = tv / (count + 1.0);
+    const double factor = (double)count / (double)(count + 1.0);
+    for (int id : nb) {
+      R.m0[id] *= factor;
+      R.vol0[id] *= factor;
+    }
+  }
+  const double h1 = R.hl.empty() ? 0.0 : R.hl[0];
+  for (int64_t p = before; p < after; ++p) {
+    const double x = R.q[2 * p], y = R.q[2 * p + 1];
+    double Jv[1], be[4], vel[2];
+    interp_nodes(R, x, y, h1, zd.mpm_grid_min[0], zd.mpm_grid_min[1], R.grid_h, zd.mpm_cells[0],
+                 fJ, 1, Jv);
+    interp_nodes(R, x, y, h1, zd.mpm_grid_min[0], zd.mpm_grid_min[1], R.grid_h, zd.mpm_cells[0],
+                 fb, 4, be);
+    const double sd = std::sqrt(det2(be));
+    for (int c = 0; c < 4; ++c) be[c] /= sd;
+    interp_nodes(R, x, y, h1, zd.mpm_grid_min[0], zd.mpm_grid_min[1], R.grid_h, zd.mpm_cells[0],
+                 fv, 2, vel);
+    R.v[2 * p] = vel[0];
+    R.v[2 * p + 1] = vel[1];
+    if (R.d.newly_inserted_continuum_stress_free) {
+      R.J[p] = 1.0;
+      be[0] = 1.0, be[1] = 0.0, be[2] = 0.0, be[3] = 1.0;
+    } else {
+      R.J[p] = Jv[0];
+    }
+    for (int c = 0; c < 4; ++c) R.be[4 * p + c] = be[c];
+  }
+}
+
+template <typename T> void compact(std::vector<T> &a, const std::vector<uint8_t> &keep, int width) {
+  size_t to = 0;
+  for (size_t i = 0; i < keep.size(); ++i) {
+    if (!keep[i]) continue;
+    if (to != i)
+      for (int c = 0; c < width; ++c) a[to * width + c] = a[i * width + c];
+    ++to;
+  }
+  a.resize(to * width);
+}
+
+// deleteParticlesUsingZoneIndicators (ResamplingTools.cpp:28-56) with
+// MaterialPoints::deleteMaterialPoint and RigidBody2DState::removeBodies.
+void delete_by_zone(hg_resampler &R, const hg_zones &z) {
+  const size_t n = npoints(R);
+  std::vector<uint8_t> keep(n, 1);
+  for (size_t p = 0; p < n; ++p) {
+    const int32_t l = hg::zone_label_at(z, R.q[2 * p], R.q[2 * p + 1]);
+    if (l < 0 || l == HG_ZONE_DISCRETE) keep[p] = 0;
+  }
+  R.stats.points_deleted += (int64_t)std::count(keep.begin(), keep.end(), 0);
+  compact(R.q0, keep, 2);
+  compact(R.q, keep, 2);
+  compact(R.v, keep, 2);
+  compact(R.m, keep, 1);
+  compact(R.vol, keep, 1);
+  compact(R.m0, keep, 1);
+  compact(R.vol0, keep, 1);
+  compact(R.w, keep, 1);
+  compact(R.hl, keep, 1);
+  compact(R.be, keep, 4);
+  compact(R.J, keep, 1);
+  compact(R.jh, keep, 1);
+  compact(R.kin, keep, 1);
+  const size_t nb = nbodies(R);
+  std::vector<uint8_t> keepb(nb, 1);
+  for (size_t b = 0; b < nb; ++b) {
+    if (R.fixed[b]) continue;
+    const int32_t l = hg::zone_label_at(z, R.dq[3 * b], R.dq[3 * b + 1]);
+    if (l < 0 || l == HG_ZONE_CONTINUUM) keepb[b] = 0;
+  }
+  R.dem_map.assign(nb, -1);
+  int32_t next = 0;
+  for (size_t b = 0; b < nb; ++b)
+    if (keepb[b]) R.dem_map[b] = next++;
+  R.stats.grains_deleted += (int64_t)(nb - (size_t)next);
+  compact(R.dq0, keepb, 3);
+  compact(R.dq, keepb, 3);
+  compact(R.dv, keepb, 3);
+  compact(R.dr, keepb, 1);
+  compact(R.M0, keepb, 3);
+  compact(R.dw, keepb, 1);
+  compact(R.fixed, keepb, 1);
+}
+
+// demWeight / mpmWeight with updateMassWeights / updateWeights
+// (HybridGrains2DSim.cpp:512-528)
+void update_weights(hg_resampler &R, const hg_zones &z) {
+  for (size_t b = 0; b < nbodies(R); ++b) {
+    const int32_t l = hg::zone_label_at(z, R.dq[3 * b], R.dq[3 * b + 1]);
+    R.dw[b] = l == HG_ZONE_HYBRID ? 0.5 : (l == HG_ZONE_DISCRETE ? 1.0 : 0.0);
+  }
+  for (size_t p = 0; p < npoints(R); ++p) {
+    const int32_t l = hg::zone_label_at(z, R.q[2 * p], R.q[2 * p + 1]);
+    R.w[p] = l == HG_ZONE_HYBRID ? 0.5 : (l == HG_ZONE_CONTINUUM ? 1.0 : 0.0);
+    R.m[p] = R.m0[p] * R.w[p];
+    R.vol[p] = R.vol0[p] * R.w[p];
+  }
+}
+
+hg_status run(hg_resampler &R, const hg_zones &z) {
+  R.stats = hg_resampler_stats{};
+  const bool direct = z.d.allow_direct_transitions != 0;
+  hg_status st;
+  int64_t g_before = 0, p_before = 0, p_after = 0, p_mid = 0, dummy = 0;
+  if ((st = insert_grains(R, z.rzones, g_before))) return st;
+  const int64_t g_after = (int64_t)nbodies(R);
+  if ((st = insert_points(R, z.rzones, p_before))) return st;
+  p_mid = (int64_t)npoints(R);
+  if (direct && (st = insert_points(R, z.direct, dummy))) return st;
+  p_after = (int64_t)npoints(R);
+  std::vector<Box> inner;
+  hg::zone_inner_continuum(z, direct, inner);
+  int64_t i_before = p_after, i_after = p_after;
+  if (!inner.empty()) {
+    if ((st = insert_points(R, inner, i_before))) return st;
+    i_after = (int64_t)npoints(R);
+  }
+  CellLists cont, disc;
+  point_grids(R, cont, disc);
+  if (direct) {
+    hybrid_point_quantities(R, z.rzones, p_before, p_mid, g_before, cont, disc);
+    hybrid_point_quantities(R, z.direct, p_mid, p_after, g_before, cont, disc);
+  } else {
+    hybrid_point_quantities(R, z.rzones, p_before, p_after, g_before, cont, disc);
+  }
+  grain_quantities(R, g_before, g_after, p_before, cont, disc);
+  inner_point_quantities(R, i_before, i_after, cont);
+  delete_by_zone(R, z);
+  update_weights(R, z);
+  return HG_OK;
+}
+
+} // namespace
+
+using hg::fail;
+
+extern "C" {
+
+hg_status hg_resampler_create(const hg_resampler_desc *d, hg_resampler **out) {
+  if (!d || !out) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  *out = nullptr;
+  if (!(d->initial_particle_size > 0.0) || d->zones.mpm_cells[0] <= 0 || d->zones.mpm_cells[1] <= 0 ||
+      !(d->zones.mpm_cell_width > 0.0) || !(d->mpm_grid_max[0] > d->zones.mpm_grid_min[0]))
+    return fail(HG_ERR_INVALID_ARGUMENT, "invalid resampler description");
+  if (d->basis != HG_BASIS_LINEAR && d->basis != HG_BASIS_UGIMP)
+    return fail(HG_ERR_INVALID_ARGUMENT, "unknown basis");
+  hg_resampler *r = new (std::nothrow) hg_resampler();
+  if (!r) return fail(HG_ERR_OUT_OF_MEMORY, "host allocation failed");
+  r->d = *d;
+  // Grid::computeCellWidth (Grid.cpp:5-10): (max - min) / count along x
+  r->grid_h = (d->mpm_grid_max[0] - d->zones.mpm_grid_min[0]) / (double)d->zones.mpm_cells[0];
+  r->radius_dist = std::normal_distribution<double>(d->dem_r_mean, d->dem_r_std);
+  *out = r;
+  return HG_OK;
+}
+
+hg_status hg_resampler_destroy(hg_resampler *r) {
+  delete r;
+  return HG_OK;
+}
+
+hg_status hg_resampler_set_points(hg_resampler *r, int64_t n, const double *q0, const double *q,
+                                  const double *v, const double *m, const double *vol,
+                                  const double *m0, const double *vol0, const double *hl,
+                                  const double *be, const double *J, const int32_t *jh,
+                                  const uint8_t *kin) {
+  if (!r || n < 0) return fail(HG_ERR_INVALID_ARGUMENT, "invalid argument");
+  if (n > 0 && (!q0 || !q || !v || !m || !vol || !m0 || !vol0 || !hl || !be || !J))
+    return fail(HG_ERR_INVALID_ARGUMENT, "NULL array");
+  const size_t k = (size_t)n;
+  r->q0.assign(q0, q0 + 2 * k);
+  r->q.assign(q, q + 2 * k);
+  r->v.assign(v, v + 2 * k);
+  r->m.assign(m, m + k);
+  r->vol.assign(vol, vol + k);
+  r->m0.assign(m0, m0 + k);
+  r->vol0.assign(vol0, vol0 + k);
+  r->w.assign(k, 1.0);
+  r->hl.assign(hl, hl + k);
+  r->be.assign(be, be + 4 * k);
+  r->J.assign(J, J + k);
+  if (jh) r->jh.assign(jh, jh + k);
+  else r->jh.assign(k, 0);
+  if (kin) r->kin.assign(kin, kin + k);
+  else r->kin.assign(k, 0);
+  return HG_OK;
+}
+
+hg_status hg_resampler_set_grains(hg_resampler *r, int64_t n, const double *q0, const double *q,
+                                  const double *v, const double *radius, const double *M0,
+                                  const uint8_t *fixed) {
+  if (!r || n < 0) return fail(HG_ERR_INVALID_ARGUMENT, "invalid argument");
+  if (n > 0 && (!q0 || !q || !v || !radius || !M0)) return fail(HG_ERR_INVALID_ARGUMENT, "NULL array");
+  const size_t k = (size_t)n;
+  r->dq0.assign(q0, q0 + 3 * k);
+  r->dq.assign(q, q + 3 * k);
+  r->dv.assign(v, v + 3 * k);
+  r->dr.assign(radius, radius + k);
+  r->M0.assign(M0, M0 + 3 * k);
+  r->dw.assign(k, 1.0);
+  if (fixed) r->fixed.assign(fixed, fixed + k);
+  else r->fixed.assign(k, 0);
+  r->dem_map.clear();
+  return HG_OK;
+}
+
+hg_status hg_resampler_set_homogenized(hg_resampler *r, const double *stress, const double *velocity) {
+  if (!r) return fail(HG_ERR_INVALID_ARGUMENT, "r is NULL");
+  const size_t nn = (size_t)(r->d.zones.mpm_cells[0] + 1) * (r->d.zones.mpm_cells[1] + 1);
+  if (stress) r->hs.assign(stress, stress + 4 * nn);
+  else r->hs.assign(4 * nn, 0.0);
+  if (velocity) r->hv.assign(velocity, velocity + 2 * nn);
+  else r->hv.assign(2 * nn, 0.0);
+  return HG_OK;
+}
+
+hg_status hg_resampler_run(hg_resampler *r, hg_zones *z) {
+  if (!r || !z) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  const hg_zones_desc &a = r->d.zones, &b = z->d;
+  if (a.mpm_cells[0] != b.mpm_cells[0] || a.mpm_cells[1] != b.mpm_cells[1] ||
+      a.mpm_cell_width != b.mpm_cell_width || a.mpm_grid_min[0] != b.mpm_grid_min[0] ||
+      a.mpm_grid_min[1] != b.mpm_grid_min[1])
+    return fail(HG_ERR_INVALID_ARGUMENT, "zone labels of another grid");
+  if ((r->d.homogenize_stress || r->d.homogenize_velocity) && r->hs.empty())
+    hg_resampler_set_homogenized(r, nullptr, nullptr);
+  return run(*r, *z);
+}
+
+hg_status hg_resampler_counts(hg_resampler *r, int64_t *points, int64_t *grains,
+                              hg_resampler_stats *stats) {
+  if (!r) return fail(HG_ERR_INVALID_ARGUMENT, "r is NULL");
+  if (points) *points = (int64_t)npoints(*r);
+  if (grains) *grains = (int64_t)nbodies(*r);
+  if (stats) *stats = r->stats;
+  return HG_OK;
+}
+
+hg_status hg_resampler_get_points(hg_resampler *r, double *q0, double *q, double *v, double *m,
+                                  double *vol, double *m0, double *vol0, double *w, double *hl,
+                                  double *be, double *J, int32_t *jh, uint8_t *kin) {
+  if (!r) return fail(HG_ERR_INVALID_ARGUMENT, "r is NULL");
+  auto put = [](const auto &src, auto *dst) {
+    if (dst) std::copy(src.begin(), src.end(), dst);
+  };
+  put(r->q0, q0);
+  put(r->q, q);
+  put(r->v, v);
+  put(r->m, m);
+  put(r->vol, vol);
+  put(r->m0, m0);
+  put(r->vol0, vol0);
+  put(r->w, w);
+  put(r->hl, hl);
+  put(r->be, be);
+  put(r->J, J);
+  put(r->jh, jh);
+  put(r->kin, kin);
+  return HG_OK;
+}
+
+hg_status hg_resampler_get_grains(hg_resampler *r, double *q0, double *q, double *v, double *radius,
+                                  double *M0, double *w, uint8_t *fixed, int32_t *old_to_new) {
+  if (!r) return fail(HG_ERR_INVALID_ARGUMENT, "r is NULL");
+  auto put = [](const auto &src, auto *dst) {
+    if (dst) std::copy(src.begin(), src.end(), dst);
+  };
+  put(r->dq0, q0);
+  put(r->dq, q);
+  put(r->dv, v);
+  put(r->dr, radius);
+  put(r->M0, M0);
+  put(r->dw, w);
+  put(r->fixed, fixed);
+  put(r->dem_map, old_to_new);
+  return HG_OK;
+}
+
+hg_status hg_resampler_dem_map_size(hg_resampler *r, int64_t *n) {
+  if (!r || !n) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  *n = (int64_t)r->dem_map.size();
+  return HG_OK;
+}
+
+uint32_t hg_resampler_random_u32(hg_resampler *r) { return r ? r->mt.next() : 0u; }
+float hg_resampler_random_f32(hg_resampler *r) { return r ? r->mt.uniform() : 0.0f; }
+double hg_resampler_random_radius(hg_resampler *r) { return r ? r->radius_dist(r->gen) : 0.0; }
+
+} // extern "C"

@@ -25,6 +25,7 @@
 // the packing-fraction grid are computed by worker threads (each cell's sum
 // is independent of the others, so the result does not depend on them).
 #include "hg_internal.cuh"
+#include "zones_internal.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -66,22 +67,6 @@ double disk_box_area(double x0, double x1, double y0, double y1, double cx, doub
 
 } // namespace
 
-struct hg_zones {
-  hg_zones_desc d{};
-  // level-set grid
-  unsigned N[2] = {0, 0};
-  double ls_min[2] = {0, 0}, ls_max[2] = {0, 0}, ls_h = 0.0;
-  std::vector<double> phi;      // packing fraction per level-set cell
-  std::vector<double> dist;     // signed distance per level-set grid point
-  std::vector<int32_t> ls_label;
-  std::vector<int32_t> label, prev; // per MPM cell
-  struct Box {
-    double b[4];
-    int32_t c[2];
-  };
-  std::vector<Box> rzones, direct, ls_rzones;
-  int64_t n_boundary_samples = 0;
-};
 
 namespace {
 
@@ -354,12 +339,6 @@ void labels(hg_zones &z) {
     }
 }
 
-inline int32_t mpm_label_at(const hg_zones &z, double x, double y) {
-  const int i = (int)std::floor((x - z.d.mpm_grid_min[0]) / z.d.mpm_cell_width);
-  const int j = (int)std::floor((y - z.d.mpm_grid_min[1]) / z.d.mpm_cell_width);
-  if (i < 0 || j < 0 || i >= z.d.mpm_cells[0] || j >= z.d.mpm_cells[1]) return -1;
-  return z.label[(size_t)j * z.d.mpm_cells[0] + i];
-}
 
 } // namespace
 
@@ -451,22 +430,10 @@ hg_status hg_zones_list(hg_zones *z, int32_t which, int64_t cap, double *boxes, 
   case HG_ZONES_DIRECT_TRANSITION: src = &z->direct; break;
   case HG_ZONES_LEVEL_SET_HYBRID: src = &z->ls_rzones; break;
   case HG_ZONES_INNER_CONTINUUM:
-  case HG_ZONES_INNER_CONTINUUM_EXCLUDING_DIRECT: {
-    // identifyInnerContinuumRegion[ExcludingDirectTransitionZones]
-    const int mx = z->d.mpm_cells[0], my = z->d.mpm_cells[1];
-    const double cw = z->d.mpm_cell_width;
-    for (int j = 0; j < my; ++j)
-      for (int i = 0; i < mx; ++i) {
-        const size_t f = (size_t)j * mx + i;
-        if (z->label[f] != ZC) continue;
-        if (which == HG_ZONES_INNER_CONTINUUM_EXCLUDING_DIRECT && z->prev[f] == ZD) continue;
-        tmp.push_back({{z->d.mpm_grid_min[0] + i * cw, z->d.mpm_grid_min[1] + j * cw,
-                        z->d.mpm_grid_min[0] + (i + 1) * cw, z->d.mpm_grid_min[1] + (j + 1) * cw},
-                       {i, j}});
-      }
+  case HG_ZONES_INNER_CONTINUUM_EXCLUDING_DIRECT:
+    hg::zone_inner_continuum(*z, which == HG_ZONES_INNER_CONTINUUM_EXCLUDING_DIRECT, tmp);
     src = &tmp;
     break;
-  }
   default: return fail(HG_ERR_INVALID_ARGUMENT, "unknown zone list");
   }
   *count = (int64_t)src->size();
@@ -494,7 +461,7 @@ hg_status hg_zones_to_delete(hg_zones *z, int32_t kind, int64_t n, const double 
   int64_t c = 0;
   for (int64_t p = 0; p < n; ++p) {
     if (kind == HG_ZONES_DEM && fixed && fixed[p]) continue;
-    const int32_t l = mpm_label_at(*z, x[(size_t)stride * p], x[(size_t)stride * p + 1]);
+    const int32_t l = hg::zone_label_at(*z, x[(size_t)stride * p], x[(size_t)stride * p + 1]);
     if (l < 0 || l == gone) {
       if (ids && c < cap) ids[c] = (int32_t)p;
       ++c;
@@ -512,7 +479,7 @@ hg_status hg_zones_weights(hg_zones *z, int32_t kind, int64_t n, const double *x
   // demWeight / mpmWeight (ZoneTools.cpp:123-147)
   const int32_t own = kind == HG_ZONES_MPM ? ZC : ZD;
   for (int64_t p = 0; p < n; ++p) {
-    const int32_t l = mpm_label_at(*z, x[(size_t)stride * p], x[(size_t)stride * p + 1]);
+    const int32_t l = hg::zone_label_at(*z, x[(size_t)stride * p], x[(size_t)stride * p + 1]);
     w[p] = l == ZH ? 0.5 : (l == own ? 1.0 : 0.0);
   }
   return HG_OK;
