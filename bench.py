@@ -290,6 +290,12 @@ def run_ours(args, rank, world, local):
     serve = None
     if args.serve_requests > 0:
         serve = run_serving(args, ctx)
+    dem = None
+    if args.dem_steps > 0:
+        dem = run_dem(args, ctx)
+    hyb = None
+    if args.hybrid_steps > 0:
+        hyb = run_hybrid(args, ctx)
 
     if rank != 0:
         return
@@ -337,11 +343,96 @@ def run_ours(args, rank, world, local):
         "cpu_baseline": cpu,
         "e2e": e2e,
         "serving": serve,
+        "dem": dem,
+        "hybrid": hyb,
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "status_word": status,
     }
     print(json.dumps(line), flush=True)
+
+
+def run_dem(args, ctx):
+    """DEM column (10,000 disks, hex pitch 2.2 mm, r U[0.9, 1.1] mm, seed
+    12345, rho 2600, kn 1e5, mu 0.5, floor plane, dt 1e-6 s): disk-steps/s on
+    the GPU (FP64, bit-exact with the oracle) and the oracle on one host core
+    (the reference's penalty map is serial)."""
+    import libhybridgrains_gb300 as hg
+    import oracle
+    from libhybridgrains_gb300 import scenes
+    sc = scenes.dem_column()
+    dp = scenes.dem_params()
+    planes = [((0.0, 0.0), (0.0, 1.0))]
+    n = len(sc["r"])
+    d = hg.DEM(ctx, scenes.GRAVITY, dp["kn"], dp["kt"], dp["gamman"], dp["gammat"], dp["mu"],
+               planes, capacity=n)
+    d.upload(sc["q"], sc["v"], sc["r"], sc["m"], sc["I"], sc["fixed"])
+    dt = 1.0e-6
+    d.flow(dt, 20)
+    ctx.synchronize()
+    l0 = hg.kernel_launch_count()
+    ctx.timer_begin()
+    d.flow(dt, args.dem_steps)
+    ms = ctx.timer_end()
+    launches = hg.kernel_launch_count() - l0
+    contacts = d.num_contacts()
+    o = oracle.DEM(sc["q"], sc["v"], sc["r"], sc["m"], sc["I"], sc["fixed"], scenes.GRAVITY,
+                   dp["kn"], dp["kt"], dp["gamman"], dp["gammat"], dp["mu"], 1.0)
+    for (x, nn) in planes:
+        o.add_plane(x, nn)
+    o.step(dt, 1)
+    t0 = time.perf_counter()
+    csteps = max(1, args.dem_cpu_steps)
+    o.step(dt, csteps)
+    cs = time.perf_counter() - t0
+    gpu_rate = n * args.dem_steps / (ms * 1e-3)
+    # per disk-step 128 B, per contact 40 B (FP64 figures of the scope table)
+    alg = n * 128 + contacts * 40
+    return {"workload": "DEM column: 10,000 disks, hex pitch 2.2 mm, r U[0.9,1.1] mm, dt 1e-6 s, "
+                        "FP64 penalty contacts with friction history",
+            "disk_steps_per_s": gpu_rate, "us_per_step": 1e3 * ms / args.dem_steps,
+            "steps": args.dem_steps, "contacts": contacts,
+            "launches_per_step": launches / args.dem_steps,
+            "algorithmic_bytes_per_step": alg,
+            "achieved_gbs": alg / (ms * 1e-3 / args.dem_steps) / 1e9,
+            "cpu_baseline": {"value": n * csteps / cs, "unit": "disk-steps/s", "cores": 1,
+                             "kind": "port", "sample": "%d steps of the same column (%.1f s)" %
+                             (csteps, cs)}}
+
+
+def run_hybrid(args, ctx):
+    """Hybrid column (100,000 material points under 20,000 disks, FP64,
+    uGIMP, node-node coupling, resampling every 200 steps on the host):
+    steps/s of the whole loop, with the share of the host resampling."""
+    from libhybridgrains_gb300 import hybrid, scenes
+    scene = scenes.hybrid_column()
+    sim = hybrid.HybridSim(ctx, scene)
+    sim.step(1)  # initial resampling and one step
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    import libhybridgrains_gb300 as hg
+    rs0 = sim.resamplings
+    host = [0.0]
+    orig = sim._resample
+
+    def timed():
+        ctx.synchronize()
+        t = time.perf_counter()
+        orig()
+        host[0] += time.perf_counter() - t
+    sim._resample = timed
+    sim.step(args.hybrid_steps)
+    ctx.synchronize()
+    wall = time.perf_counter() - t0
+    n, nd = sim.counts()
+    return {"workload": "hybrid column: 100,000 MPM points (h 2.5 mm, uGIMP, FP64) under 20,000 "
+                        "disks, node-node coupling, homogenised stress and velocity, resampling "
+                        "every 200 steps, dt 1e-6 s",
+            "steps": args.hybrid_steps, "steps_per_s": args.hybrid_steps / wall,
+            "ms_per_step": 1e3 * wall / args.hybrid_steps,
+            "resamplings": sim.resamplings - rs0, "resampling_host_s": host[0],
+            "points": n, "disks": nd,
+            "status": [sim.mpm.status(), sim.dem.status()]}
 
 
 def run_serving(args, ctx):
@@ -407,6 +498,9 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-steps", type=int, default=10)
     ap.add_argument("--fp64-steps", type=int, default=10)
+    ap.add_argument("--dem-steps", type=int, default=2000)
+    ap.add_argument("--hybrid-steps", type=int, default=1000)
+    ap.add_argument("--dem-cpu-steps", type=int, default=200)
     ap.add_argument("--serve-requests", type=int, default=256)
     ap.add_argument("--serve-rate", type=float, default=50.0)
     ap.add_argument("--serve-steps", type=int, default=2000)

@@ -418,6 +418,15 @@ hg_status hg_dem_destroy(hg_dem *d);
 hg_status hg_dem_upload(hg_dem *d, int64_t n, const double *q, const double *v,
                         const double *radius, const double *mass,
                         const double *inertia, const uint8_t *fixed);
+/* hg_dem_upload after bodies were added and removed (the resampling step):
+ * the contact history is kept, with the contacts of removed bodies dropped
+ * and the others renumbered by old_to_new (n_old entries, -1: removed;
+ * PenaltyImpactFrictionMap::deleteCacheEntries, PenaltyImpactFrictionMap.cpp:
+ * 1199-1278). Added bodies start without contacts. */
+hg_status hg_dem_upload_relabel(hg_dem *d, int64_t n, const double *q, const double *v,
+                                const double *radius, const double *mass,
+                                const double *inertia, const uint8_t *fixed,
+                                int64_t n_old, const int32_t *old_to_new);
 /* RigidBody2DState::updateCurrentMassUsingMassWeights
  * (RigidBody2DState.cpp:1182-1200). */
 hg_status hg_dem_set_weights(hg_dem *d, const double *w);

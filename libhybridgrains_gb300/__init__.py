@@ -355,6 +355,16 @@ class DEM:
         check("hg_dem_upload", self._h, n, _d(q), _d(v), _d(r), _d(m), _d(I), _u8(fx))
         self.n = n
 
+    def upload_relabel(self, q, v, r, m, I, fixed, old_to_new):
+        """Upload after a resampling step, keeping the contact history
+        renumbered by old_to_new (-1 for removed bodies)."""
+        q, v, r, m, I = _f64(q), _f64(v), _f64(r), _f64(m), _f64(I)
+        fx = np.ascontiguousarray(fixed, dtype=np.uint8)
+        mp = np.ascontiguousarray(old_to_new, dtype=np.int32)
+        check("hg_dem_upload_relabel", self._h, len(r), _d(q), _d(v), _d(r), _d(m), _d(I),
+              _u8(fx), len(mp), _i32(mp))
+        self.n = len(r)
+
     def set_weights(self, w):
         check("hg_dem_set_weights", self._h, _d(_f64(w)))
 
@@ -371,6 +381,11 @@ class DEM:
 
     def flow_with_weights(self, dt, nsteps=1):
         check("hg_dem_step", self._h, float(dt), int(nsteps), 1)
+
+    def num_contacts(self):
+        n = ctypes.c_int64()
+        check("hg_dem_num_contacts", self._h, ctypes.byref(n))
+        return n.value
 
     def contacts(self):
         cnt = ctypes.c_int64()

@@ -159,6 +159,7 @@ SIGNATURES = {
     "hg_resampler_random_f32": [_P],
     "hg_resampler_random_radius": [_P],
     "hg_dem_create": [_P, ctypes.POINTER(DemDesc), _PP],
+    "hg_dem_upload_relabel": [_P, _i64, _D, _D, _D, _D, _D, _U8, _i64, _I32],
     "hg_dem_destroy": [_P],
     "hg_dem_upload": [_P, _i64, _D, _D, _D, _D, _D, _U8],
     "hg_dem_set_weights": [_P, _D],

@@ -1108,9 +1108,29 @@ hg_status hg_dem_destroy(hg_dem *d) {
   return HG_OK;
 }
 
+static hg_status dem_upload_impl(hg_dem *d, int64_t n, const double *q, const double *v,
+                                 const double *r, const double *mass, const double *inertia,
+                                 const uint8_t *fixed, int64_t nmap, const int32_t *old_to_new);
+
 hg_status hg_dem_upload(hg_dem *d, int64_t n, const double *q, const double *v,
                         const double *r, const double *mass, const double *inertia,
                         const uint8_t *fixed) {
+  return dem_upload_impl(d, n, q, v, r, mass, inertia, fixed, -1, nullptr);
+}
+
+hg_status hg_dem_upload_relabel(hg_dem *d, int64_t n, const double *q, const double *v,
+                                const double *r, const double *mass, const double *inertia,
+                                const uint8_t *fixed, int64_t n_old, const int32_t *old_to_new) {
+  if (n_old < 0 || (n_old > 0 && !old_to_new))
+    return fail(HG_ERR_INVALID_ARGUMENT, "invalid body map");
+  for (int64_t i = 0; i < n_old; ++i)
+    if (old_to_new[i] >= n) return fail(HG_ERR_INVALID_ARGUMENT, "body map points past n");
+  return dem_upload_impl(d, n, q, v, r, mass, inertia, fixed, n_old, old_to_new);
+}
+
+static hg_status dem_upload_impl(hg_dem *d, int64_t n, const double *q, const double *v,
+                                 const double *r, const double *mass, const double *inertia,
+                                 const uint8_t *fixed, int64_t nmap, const int32_t *old_to_new) {
   if (!d) return fail(HG_ERR_INVALID_ARGUMENT, "d is NULL");
   if (n < 0) return fail(HG_ERR_INVALID_ARGUMENT, "negative body count");
   if (n > d->cap) return fail(HG_ERR_CAPACITY, "body count exceeds capacity");
@@ -1139,7 +1159,11 @@ hg_status hg_dem_upload(hg_dem *d, int64_t n, const double *q, const double *v,
     HG_CUDA_TRY(cudaMemsetAsync(d->fixed.p, 0, n, s));
   }
   if ((st = fill(s, d->w.p, n, 1.0))) return st;
-  if ((st = dem_reset_history(d))) return st;
+  if (nmap < 0) {
+    if ((st = dem_reset_history(d))) return st;
+  } else if ((st = dem_relabel(d, old_to_new, nmap))) {
+    return st;
+  }
   d->ncontacts_host = 0;
   HG_CUDA_TRY(cudaStreamSynchronize(s));
   return HG_OK;

@@ -693,6 +693,83 @@ hg_status dem_step(hg_dem *d, double dt, int weighted) {
   return HG_OK;
 }
 
+// ---- contact history after bodies are removed -------------------------------
+//
+// PenaltyImpactFrictionMap::deleteCacheEntries / relabelEntries
+// (PenaltyImpactFrictionMap.cpp:1199-1278): contacts of removed bodies are
+// dropped and the others renumbered. The map is monotone, so the list stays
+// sorted by (kind, first, second) and a stable compaction keeps it valid for
+// the next step's history lookup.
+namespace {
+
+__device__ __forceinline__ bool relabel_one(int64_t key, const int32_t *map, int64_t nmap,
+                                            int64_t &out, int32_t &a2, int32_t &b2) {
+  const int64_t kind = key >> 60;
+  const int64_t a = (key >> 30) & 0x3FFFFFFF, b = key & 0x3FFFFFFF;
+  a2 = a < nmap ? map[a] : -1;
+  b2 = kind == 0 ? (int32_t)b : (b < nmap ? map[b] : -1); // kind 0: plane index
+  out = (kind << 60) | ((int64_t)a2 << 30) | (int64_t)b2;
+  return a2 >= 0 && b2 >= 0;
+}
+
+__global__ void kd_relabel_keep(int64_t ccap, const int32_t *__restrict__ count,
+                                const int64_t *__restrict__ keys, const int32_t *__restrict__ map,
+                                int64_t nmap, int32_t *keep) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k > ccap) return;
+  const int64_t c = min((int64_t)*count, ccap);
+  int64_t nk;
+  int32_t a2, b2;
+  keep[k] = (k < c && relabel_one(keys[k], map, nmap, nk, a2, b2)) ? 1 : 0;
+}
+
+__global__ void kd_relabel_move(int64_t ccap, const int32_t *__restrict__ count,
+                                const int64_t *__restrict__ keys, const double *__restrict__ rec,
+                                const int32_t *__restrict__ map, int64_t nmap,
+                                const int32_t *__restrict__ off, int64_t *okeys, double *orec,
+                                int32_t *ocount) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t c = min((int64_t)*count, ccap);
+  if (k == 0) *ocount = off[c];
+  if (k >= c) return;
+  int64_t nk;
+  int32_t a2, b2;
+  if (!relabel_one(keys[k], map, nmap, nk, a2, b2)) return;
+  const int64_t o = off[k];
+  okeys[o] = nk;
+  for (int j = 0; j < RW; ++j) orec[o * RW + j] = rec[k * RW + j];
+  orec[o * RW + 1] = (double)a2;
+  orec[o * RW + 2] = (double)b2;
+}
+
+} // namespace
+
+hg_status dem_relabel(hg_dem *d, const int32_t *map_host, int64_t nmap) {
+  if (!d->history_valid) return HG_OK;
+  cudaStream_t s = d->ctx->stream;
+  const int64_t C = d->ccap;
+  DevBuf<int32_t> map, keep, off, tmp;
+  hg_status st;
+  if ((st = map.alloc(std::max<int64_t>(nmap, 1))) || (st = keep.alloc(C + 1)) ||
+      (st = off.alloc(C + 1)) || (st = tmp.alloc(scan_tmp_size(C + 1))))
+    return st;
+  if (nmap > 0)
+    HG_CUDA_TRY(cudaMemcpyAsync(map.p, map_host, sizeof(int32_t) * nmap, cudaMemcpyHostToDevice, s));
+  const int nb = 1 - d->cc;
+  HG_LAUNCH(kd_relabel_keep, blocks_for(C + 1, 256), 256, 0, s, C, d->c_count.p + d->cc,
+            d->ckey[d->cc].p, map.p, nmap, keep.p);
+  HG_CHECK_LAUNCH();
+  if ((st = exclusive_scan_i32(keep.p, off.p, C + 1, tmp.p, s))) return st;
+  HG_LAUNCH(kd_relabel_move, blocks_for(C + 1, 256), 256, 0, s, C, d->c_count.p + d->cc,
+            d->ckey[d->cc].p, d->crec[d->cc].p, map.p, nmap, off.p, d->ckey[nb].p,
+            d->crec[nb].p, d->c_count.p + nb);
+  HG_CHECK_LAUNCH();
+  d->cc = nb;
+  // the map was copied from the caller's memory: it may go once this returns
+  HG_CUDA_TRY(cudaStreamSynchronize(s));
+  return HG_OK;
+}
+
 hg_status dem_download_contacts(hg_dem *d, int64_t cap, double *rec, int64_t *count) {
   cudaStream_t s = d->ctx->stream;
   int32_t c = 0;

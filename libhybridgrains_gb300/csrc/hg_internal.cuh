@@ -323,6 +323,8 @@ struct hg_dem {
 namespace hg {
 hg_status dem_alloc(hg_dem *d);
 hg_status dem_reset_history(hg_dem *d);
+// renumber the contact history by old_to_new (-1: removed) of nmap bodies
+hg_status dem_relabel(hg_dem *d, const int32_t *old_to_new, int64_t nmap);
 hg_status dem_step(hg_dem *d, double dt, int weighted);
 hg_status dem_download_contacts(hg_dem *d, int64_t cap, double *rec,
                                 int64_t *count);

@@ -1,0 +1,140 @@
+"""Hybrid MPM/DEM simulation with the resampling interval (HybridGrains2DSim).
+
+The node-node step runs on the device (``Hybrid.step``); the zone labels and
+the resampling step run on the host every ``avoid_a_void_freq + 1`` steps on
+state copied from the device, and the result is copied back
+(HybridGrains2DSim.cpp:116-227 and 301-559):
+
+* before the first step, the resampling runs once (the reference calls its
+  update twice; the second call only counts), from labels seeded by where
+  the material points are (see _seed_labels);
+* after every step the counter advances; when it wraps, the device
+  accumulation of the homogenised stress and velocity is finalised (1/freq),
+  the zones and the resampling step run, points and grains are uploaded (the
+  DEM contact history renumbered), and the accumulators are cleared.
+
+Host copies kept between intervals: reference positions q0, initial masses
+and volumes (m0, volume0) and half widths of the points; reference
+positions, radii and initial masses of the grains.
+
+The homogenised fields are accumulated once per device step, so at a
+resampling step the finalised field has one term less than the reference's,
+which accumulates the current step a second time inside the branch.
+"""
+import numpy as np
+
+from . import DEM, FP64, MPM, Hybrid, Resampler, Zones, scenes
+
+
+class HybridSim:
+    def __init__(self, ctx, scene, basis=1, point_headroom=2.0, grain_headroom=3.0):
+        cfg, sc, dp = scene["mpm"], scene["dem"], scene["dem_params"]
+        zs, rs = scene["zones"], scene["resampling"]
+        self.ctx, self.cfg, self.dt = ctx, cfg, cfg["dt"]
+        p = scenes.seed_column_points(cfg)
+        n, nd = len(p["m"]), len(sc["r"])
+        self.mpm = MPM(ctx, cfg["grid_min"], cfg["grid_max"], cfg["h"], cfg["shear_modulus"],
+                       cfg["bulk_modulus"], cfg["dp_alpha"], cfg["flip_alpha"], scenes.GRAVITY,
+                       cfg["planes"], basis=basis, precision=FP64,
+                       capacity=int(point_headroom * n) + 1024)
+        self.mpm.upload(p["q"], p["v"], p["m"], p["vol"], p["hl"])
+        planes = [(pl[0], pl[1]) for pl in cfg["planes"]]  # the same walls for the grains
+        self.dem = DEM(ctx, scenes.GRAVITY, dp["kn"], dp["kt"], dp["gamman"], dp["gammat"],
+                       dp["mu"], planes, capacity=int(grain_headroom * nd) + 1024)
+        self.dem.upload(sc["q"], sc["v"], sc["r"], sc["m"], sc["I"], sc["fixed"])
+        self.hyb = Hybrid(ctx, self.mpm, self.dem)
+        g = self.mpm
+        zargs = (g.grid_min, cfg["h"], (g.nx, g.ny), zs["level_set_cell_width"],
+                 zs["phi_window_size"], zs["phi_samples_per_cell_side"], zs["phi_threshold"],
+                 zs["rzone_level_set"], zs["rzone_half_thickness"],
+                 zs["allow_direct_transitions"])
+        self.zones = Zones(*zargs[:-1], allow_direct_transitions=zargs[-1])
+        self.res = Resampler(zargs, g.grid_max, basis, cfg["h"] / cfg["samples_per_dim"],
+                             cfg["rho"], rs["dem_r_mean"], rs["dem_r_std"], rs["rho_dem"],
+                             cfg["bulk_modulus"], cfg["shear_modulus"],
+                             rs["newly_inserted_continuum_stress_free"],
+                             rs["homogenize_stress"], rs["homogenize_velocity"])
+        self.freq = rs["avoid_a_void_freq"]
+        self.hom = (rs["homogenize_stress"], rs["homogenize_velocity"])
+        # host-side state kept between intervals
+        self.P = dict(q0=p["q"].copy(), m0=p["m"].copy(), vol0=p["vol"].copy(), hl=p["hl"].copy(),
+                      w=np.ones(n))
+        self.G = dict(q0=sc["q"].copy(), r=sc["r"].copy(),
+                      M0=np.stack([sc["m"], sc["m"], sc["I"]], axis=1), fixed=sc["fixed"].copy(),
+                      w=np.ones(nd))
+        self.counter = 0
+        self.started = False
+        self.resamplings = 0
+        self.steps = 0
+        self.stats = []
+
+    def _resample(self):
+        st = self.mpm.download()
+        q3, v3 = self.dem.download()
+        P, G = self.P, self.G
+        nn = self.mpm.nnodes
+        hs, hv = np.zeros((nn, 4)), np.zeros((nn, 2))
+        if self.hom[0] or self.hom[1]:
+            c = self.hyb.coupling()
+            hs, hv = c["homog_stress"] / self.freq, c["homog_velocity"] / self.freq
+        self.zones.update(q3, G["r"], G["fixed"], st["q"])
+        self.res.set_points(P["q0"], st["q"], st["v"], P["m0"] * P["w"], P["vol0"] * P["w"],
+                            P["m0"], P["vol0"], P["hl"], st["be"], st["J"], st["jh"])
+        self.res.set_grains(G["q0"], q3, v3, G["r"], G["M0"], G["fixed"])
+        self.res.set_homogenized(hs, hv)
+        self.res.run(self.zones)
+        a, b = self.res.points(), self.res.grains()
+        self.mpm.upload(a["q"], a["v"], a["m"], a["vol"], a["hl"], a["be"], a["J"], a["jh"])
+        self.dem.upload_relabel(b["q"], b["v"], b["r"], b["M0"][:, 0], b["M0"][:, 2], b["fixed"],
+                                b["old_to_new"])
+        self.dem.set_weights(b["w"])
+        self.P = dict(q0=a["q0"], m0=a["m0"], vol0=a["vol0"], hl=a["hl"], w=a["w"])
+        self.G = dict(q0=b["q0"], r=b["r"], M0=b["M0"], fixed=b["fixed"], w=b["w"])
+        self.hyb.clear_homogenized()
+        self.resamplings += 1
+        self.stats.append(self.res.stats()[2])
+
+    def _update(self):
+        """updateHybridStates_poorman's counter (HybridGrains2DSim.cpp:301-559)."""
+        if self.counter == 0:
+            self._resample()
+        elif self.counter >= self.freq:
+            self.counter = -1
+        self.counter += 1
+
+    def _seed_labels(self):
+        """Both methods are seeded (the reference discards the material
+        points at initialisation and grows the continuum from the grains by
+        resampling, HybridGrains2DSim.cpp:55): cells holding material points
+        start as continuum and the others as discrete, so the first update's
+        hysteresis keeps the bulk continuous and the grains discrete."""
+        from . import CONTINUUM, DISCRETE
+        g = self.mpm
+        q = g.download()["q"]
+        i = np.floor((q[:, 0] - g.grid_min[0]) / self.cfg["h"]).astype(np.int64)
+        j = np.floor((q[:, 1] - g.grid_min[1]) / self.cfg["h"]).astype(np.int64)
+        ok = (i >= 0) & (j >= 0) & (i < g.nx) & (j < g.ny)
+        labels = np.full(g.nx * g.ny, DISCRETE, dtype=np.int32)
+        labels[j[ok] * g.nx + i[ok]] = CONTINUUM
+        self.zones.set_labels(labels)
+
+    def step(self, nsteps):
+        if not self.started:  # the initial resampling (HybridGrains2DSim.cpp:120-128)
+            self._seed_labels()
+            self._update()
+            self._update()
+            self.started = True
+        done = 0
+        while done < nsteps:
+            # device steps up to the next resampling call
+            run = 1 if self.counter == 0 else min(nsteps - done, self.freq + 1 - self.counter)
+            run = max(run, 1)
+            self.hyb.step(self.dt, run, *self.hom)
+            for _ in range(run - 1):
+                self.counter += 1  # calls that only count
+            self._update()
+            done += run
+            self.steps += run
+
+    def counts(self):
+        return self.mpm.n, self.dem.n

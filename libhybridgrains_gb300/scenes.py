@@ -167,3 +167,42 @@ def serving_column(npoints, aspect, phi_deg, h=5.0e-3):
     cfg["planes"] = mpm_planes(cfg["grid_min"], cfg["grid_max"])
     cfg["samples_per_dim"] = 2
     return cfg
+
+
+def hybrid_column(scale=1.0, seed=12345):
+    """The hybrid column collapse (MPM bulk under a DEM layer).
+
+    scale=1: 100,000 material points (h = 2.5 mm, 2 x 2 per cell, a column
+    0.25 m wide and 0.625 m tall) under 20,000 disks (r U[0.9, 1.1] mm, hex
+    pitch 2.2 mm, 113 per row) that start 10 mm (four cells) below the top
+    of the bulk, so the coupling band is four cells wide; resampling every
+    200 steps, dt = 1e-6 s. The disk count does not fit a 10 mm band on this
+    column, so the layer is as tall as the count needs (about 0.34 m). scale
+    < 1 shrinks both counts (column and layer widths by sqrt(scale)) for
+    tests. Zone settings are the reference's column-collapse ones in units
+    of the cell width and mean radius."""
+    h = 2.5e-3
+    wc = max(int(round(100 * math.sqrt(scale))), 8)
+    hc = max(int(round(250 * math.sqrt(scale))), 8)
+    # the grid extends four cells past the floor and the left wall: uGIMP
+    # stencils of points within half a sample of a wall then stay on the grid
+    nx, ny = 404, 404
+    cfg = dict(grid_min=(-4 * h, -4 * h), grid_max=(400 * h, 400 * h), h=h,
+               rect_min=(0.0, 0.0), rect_max=(wc * h, hc * h), dt=1.0e-6)
+    cfg.update(mpm_material())
+    cfg["planes"] = [((0.0, 0.0), (0.0, 1.0), True, -np.inf),
+                     ((0.0, 0.0), (1.0, 0.0), True, -np.inf),
+                     ((396 * h, 0.0), (-1.0, 0.0), True, -np.inf)]
+    cfg["samples_per_dim"] = 2
+    per_row = max(int((wc * h) / 2.2e-3), 4)
+    n_disks = int(round(20000 * scale))
+    sc = dem_column(n=n_disks, per_row=per_row, pitch=2.2e-3, seed=seed, x0=0.0,
+                    y0=hc * h - 4 * h)
+    dp = dem_params()
+    zones = dict(level_set_cell_width=h, phi_window_size=4.35e-3, phi_samples_per_cell_side=1,
+                 phi_threshold=0.3, rzone_level_set=6.25 * h, rzone_half_thickness=0.5 * h,
+                 allow_direct_transitions=False)
+    res = dict(dem_r_mean=1.0e-3, dem_r_std=0.1e-3, rho_dem=2600.0, avoid_a_void_freq=200,
+               homogenize_stress=True, homogenize_velocity=True,
+               newly_inserted_continuum_stress_free=False)
+    return dict(mpm=cfg, dem=sc, dem_params=dp, zones=zones, resampling=res)

@@ -89,3 +89,40 @@ def test_contact_capacity_overflow_is_reported(ctx):
     assert g.status() & 4  # HG_STATUS_CONTACT_OVERFLOW
     q, v = g.download()
     assert np.isfinite(q).all() and np.isfinite(v).all()
+
+
+def test_upload_relabel_keeps_renumbered_history(ctx):
+    """After bodies are removed (the resampling step), the contact history
+    keeps the surviving contacts, renumbered, with their tangential springs
+    (PenaltyImpactFrictionMap::deleteCacheEntries); bit-exact bookkeeping."""
+    sc = scenes.dem_column(n=2000, per_row=50)
+    dp = scenes.dem_params()
+    d = hg.DEM(ctx, scenes.GRAVITY, dp["kn"], dp["kt"], dp["gamman"], dp["gammat"], dp["mu"],
+               [((0.0, 0.0), (0.0, 1.0))], capacity=2100)
+    d.upload(sc["q"], sc["v"], sc["r"], sc["m"], sc["I"], sc["fixed"])
+    d.flow(1e-6, 200)
+    before = d.contacts()
+    q, v = d.download()
+    n = len(sc["r"])
+    keep = np.ones(n, dtype=bool)
+    keep[::7] = False
+    old_to_new = np.where(keep, np.cumsum(keep) - 1, -1).astype(np.int32)
+    # two bodies appended after the survivors, as the resampling step does
+    extra_q = np.array([[0.5, 0.5, 0.0], [0.6, 0.5, 0.0]])
+    nq = np.concatenate([q[keep], extra_q])
+    nv = np.concatenate([v[keep], np.zeros((2, 3))])
+    nr = np.concatenate([sc["r"][keep], [1e-3, 1e-3]])
+    nm = np.concatenate([sc["m"][keep], sc["m"][:2]])
+    nI = np.concatenate([sc["I"][keep], sc["I"][:2]])
+    d.upload_relabel(nq, nv, nr, nm, nI, np.zeros(len(nr), dtype=np.uint8), old_to_new)
+    after = d.contacts()
+    kind, a, b = before[:, 0].astype(int), before[:, 1].astype(int), before[:, 2].astype(int)
+    alive = keep[a] & ((kind == 0) | keep[np.where(kind == 0, 0, b)])
+    exp = before[alive].copy()
+    exp[:, 1] = old_to_new[a[alive]]
+    nb = b[alive]
+    exp[:, 2] = np.where(kind[alive] == 0, nb, old_to_new[np.where(kind[alive] == 0, 0, nb)])
+    assert len(exp) > 20 and len(exp) < len(before)
+    assert np.array_equal(after, exp)
+    d.flow(1e-6, 10)
+    assert d.status() == 0

@@ -2,20 +2,27 @@
 is chaotic, so point states diverge; the shape of the collapse must not.
 
 The 12,800-point column (0.2 m x 0.4 m, E = 1e6 Pa, friction angle 30 deg)
-collapses for 0.3 s (30,000 steps of 1e-5 s). Compared, against the FP64
-oracle's run (``tests/golden/column_12800_30k.json``, made by
-``tests/golden/make_long_horizon.py``) and between the MIXED and FP64 GPU
+collapses for 0.5 s (50,000 steps of 1e-5 s); the shape is compared at 0.3 s
+and at 0.5 s (by then the front has reached the far wall of the 1 m domain,
+so the run-out is bounded and the height profile carries the comparison),
+against the FP64 oracle's run (``tests/golden/column_12800_50k.json``, made
+by ``tests/golden/make_long_horizon.py``) and between the MIXED and FP64 GPU
 paths:
 
 * run-out length: front position (largest x of the points) minus the
   column's initial right edge, within 2%;
-* free-surface height profile: the highest point in each 1 cm strip, within
-  2% of the initial height, from x = 5 cm to the front. The first 5 cm are
-  excluded: the column's left side slides against the sticking wall at
-  x = 0, where points stop at whatever height they touch it. Two FP64 GPU
-  runs of the same scene, differing only in the order of atomic sums, end up
-  to 9 cm apart there, but within 1.7 mm (0.4%) everywhere from 5 cm on and
-  within 0.3% in run-out.
+* free-surface height profile: per 1 cm strip, the 95th percentile of the
+  strip's point heights, within 2% of the initial height up to x = 95 cm
+  from x = 5 cm at 0.3 s and from x = 10 cm at 0.5 s. The strips next to
+  the walls are left out, and a percentile is
+  used rather than the highest point, because material sticks to the walls
+  (MPM planes are sticking) at whatever height it reaches them and comes off
+  as clumps later: runs of the same scene that differ only in the order of
+  atomic sums end up tens of millimetres apart there and in the single
+  highest points. Measured over five GPU runs (two MIXED, three FP64)
+  against the oracle: at 0.3 s within 2.2 mm from 5 cm, at 0.5 s within
+  3.4 mm from 10 cm (but up to 7 mm between 5 and 10 cm); run-out within
+  0.5%.
 """
 import json
 import os
@@ -30,37 +37,50 @@ pytestmark = pytest.mark.gpu
 
 X_EDGE = 0.3  # initial right edge of the column (m)
 H0 = 0.4      # initial height (m)
-FIRST = 5     # first compared strip (x >= 5 cm)
-STEPS = 30000
-GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "column_12800_30k.json")
+# compared strips: from 5 cm at 0.3 s and from 10 cm at 0.5 s (the region the
+# left wall's clumps reach grows with time) to 95 cm
+FIRST = {30000: 5, 50000: 10}
+LAST = 95
+CHECKPOINTS = (30000, 50000)
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "column_12800_50k.json")
 
 
-def profile(q, width=0.01, xmax=1.0):
+def profile(q, width=0.01, xmax=1.0, pct=95.0, nmin=10):
+    """Free-surface height per strip: the 95th percentile of the strip's point
+    heights (strips with fewer than 10 points: 0)."""
     bins = np.floor(q[:, 0] / width).astype(int)
     prof = np.zeros(int(round(xmax / width)))
-    np.maximum.at(prof, np.clip(bins, 0, len(prof) - 1), q[:, 1])
+    for k in range(len(prof)):
+        y = q[bins == k, 1]
+        if len(y) >= nmin:
+            prof[k] = np.percentile(y, pct)
     return prof
 
 
-def compare(front_a, prof_a, front_b, prof_b):
+def compare(front_a, prof_a, front_b, prof_b, first):
     ra, rb = front_a - X_EDGE, front_b - X_EDGE
     assert rb > 0.1, rb  # the column has collapsed
     assert abs(ra - rb) <= 0.02 * rb, (ra, rb)
-    d = np.abs(prof_a[FIRST:] - prof_b[FIRST:])
-    assert d.max() <= 0.02 * H0, (d.max(), int(d.argmax()) + FIRST)
+    d = np.abs(prof_a[first:LAST] - prof_b[first:LAST])
+    assert d.max() <= 0.02 * H0, (d.max(), int(d.argmax()) + first)
 
 
 def run(ctx, precision):
+    """Positions after each checkpoint."""
     cfg = scenes.mpm_column("column_12800")
     p = scenes.seed_column_points(cfg)
     m = hg.MPM(ctx, cfg["grid_min"], cfg["grid_max"], cfg["h"], cfg["shear_modulus"],
                cfg["bulk_modulus"], cfg["dp_alpha"], cfg["flip_alpha"], scenes.GRAVITY,
                cfg["planes"], precision=precision, capacity=len(p["m"]))
     m.upload(p["q"], p["v"], p["m"], p["vol"], p["hl"])
-    for _ in range(STEPS // 1000):
-        m.flow(cfg["dt"], 1000)
-    assert m.status() == 0
-    return m.download()["q"]
+    out, done = {}, 0
+    for steps in CHECKPOINTS:
+        while done < steps:
+            m.flow(cfg["dt"], 1000)
+            done += 1000
+        assert m.status() == 0
+        out[steps] = m.download()["q"]
+    return out
 
 
 @pytest.fixture(scope="module")
@@ -68,15 +88,21 @@ def finals(ctx):
     return {"mixed": run(ctx, hg.MIXED), "fp64": run(ctx, hg.FP64)}
 
 
-@pytest.mark.parametrize("path", ["mixed", "fp64"])
-def test_collapse_shape_matches_the_oracle_after_30000_steps(finals, path):
+@pytest.fixture(scope="module")
+def golden():
     with open(GOLDEN) as f:
-        g = json.load(f)
-    assert g["steps"] == STEPS
-    q = finals[path]
-    compare(q[:, 0].max(), profile(q), g["front_x_m"], np.array(g["profile_top_y_m"]))
+        return {c["steps"]: c for c in json.load(f)["checkpoints"]}
 
 
-def test_mixed_collapse_shape_matches_fp64_after_30000_steps(finals):
-    a, b = finals["mixed"], finals["fp64"]
-    compare(a[:, 0].max(), profile(a), b[:, 0].max(), profile(b))
+@pytest.mark.parametrize("steps", CHECKPOINTS)
+@pytest.mark.parametrize("path", ["mixed", "fp64"])
+def test_collapse_shape_matches_the_oracle(finals, golden, path, steps):
+    q, g = finals[path][steps], golden[steps]
+    compare(q[:, 0].max(), profile(q), g["front_x_m"], np.array(g["profile_p95_y_m"]),
+            FIRST[steps])
+
+
+@pytest.mark.parametrize("steps", CHECKPOINTS)
+def test_mixed_collapse_shape_matches_fp64(finals, steps):
+    a, b = finals["mixed"][steps], finals["fp64"][steps]
+    compare(a[:, 0].max(), profile(a), b[:, 0].max(), profile(b), FIRST[steps])
