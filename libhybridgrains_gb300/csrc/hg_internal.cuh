@@ -318,6 +318,13 @@ struct hg_dem {
   // body gather lists for deterministic force accumulation
   hg::DevBuf<int32_t> in_count, in_off, in_list, in_cursor;
   hg::DevBuf<int32_t> out_off; // first contact index of each body
+  // two steps captured as a CUDA graph (the contact buffers alternate, so a
+  // pair of steps returns to the same pointers); rebuilt when n, dt, the
+  // weighting, the live buffer or the broadphase cell change
+  cudaGraphExec_t pair_exec = nullptr;
+  int64_t pair_n = -1, pair_launches = 0;
+  double pair_dt = 0.0, pair_cell = 0.0;
+  int pair_weighted = -1, pair_cc = -1;
 };
 
 namespace hg {
