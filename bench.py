@@ -442,8 +442,7 @@ def run_serving(args, ctx):
     from libhybridgrains_gb300 import serving
 
     def copies(reqs, at_once=False):
-        return [serving.Request(r.rid, 0.0 if at_once else r.arrival, r.cfg, r.npoints, r.steps,
-                                r.frame_every, r.dt) for r in reqs]
+        return [r.copy(0.0 if at_once else None) for r in reqs]
 
     budget = int(args.serve_budget_gb * 2**30)
     reqs = serving.column_requests(n=args.serve_requests, rate=args.serve_rate,
@@ -464,28 +463,34 @@ def run_serving(args, ctx):
     alone = copies(reqs)
     alone_s = serving.run_one_at_a_time(ctx, alone)
     psteps = float(sum(r.npoints * r.steps for r in reqs))
-    diff = max(abs(a[1] - b[1]) for r1, r2 in zip(live, alone) for a, b in zip(r1.frames, r2.frames))
+    dsteps = float(sum(r.ndisks * r.steps for r in reqs))
+    diff = max(serving.frame_diff(a[1], b[1])
+               for r1, r2 in zip(live, alone) for a, b in zip(r1.frames, r2.frames))
     return {
         "workload": "%d column-collapse requests, Poisson arrivals %.0f/s (seed 2024), points "
-                    "log-U[2e3,2e5], aspect U[0.5,4], friction angle U[20,40] deg, %d steps, "
-                    "a frame (positions) every 100 steps, MPM only" %
-                    (len(reqs), args.serve_rate, args.serve_steps),
+                    "log-U[2e3,2e5], aspect U[0.5,4], friction angle U[20,40] deg, a DEM pile "
+                    "of U[0,0.2] x the point count in disks, %d steps, a frame (positions) "
+                    "every 100 steps" % (len(reqs), args.serve_rate, args.serve_steps),
+        "disks": int(sum(r.ndisks for r in reqs)),
         "p50_latency_s": poisson["p50_latency_s"], "p99_latency_s": poisson["p99_latency_s"],
         "max_latency_s": poisson["max_latency_s"],
         "p99_admission_wait_s": poisson["p99_admission_wait_s"],
         "makespan_s": poisson["makespan_s"],
         "particle_steps_per_s": poisson["particle_steps_per_s"],
+        "disk_steps_per_s": poisson["disk_steps_per_s"],
         "peak_members": srv.peak_members, "peak_resident_bytes": srv.peak_resident,
         "hbm_budget_bytes": budget, "gpu_launches": launches,
         "saturated": {"particle_steps_per_s": saturated["particle_steps_per_s"],
+                      "disk_steps_per_s": saturated["disk_steps_per_s"],
                       "requests_per_s": saturated["requests_per_s"],
                       "p50_latency_s": saturated["p50_latency_s"],
                       "p99_latency_s": saturated["p99_latency_s"],
                       "makespan_s": saturated["makespan_s"]},
         "one_at_a_time": {"particle_steps_per_s": psteps / alone_s,
+                          "disk_steps_per_s": dsteps / alone_s,
                           "requests_per_s": len(reqs) / alone_s, "seconds": alone_s},
         "batched_over_one_at_a_time": saturated["particle_steps_per_s"] * alone_s / psteps,
-        "max_frame_runout_diff_m": diff,
+        "max_frame_front_diff_m": diff,
     }
 
 

@@ -427,6 +427,22 @@ hg_status hg_dem_upload_relabel(hg_dem *d, int64_t n, const double *q, const dou
                                 const double *radius, const double *mass,
                                 const double *inertia, const uint8_t *fixed,
                                 int64_t n_old, const int32_t *old_to_new);
+/* Removes and adds bodies on the device, without a round trip to the host:
+ * body i of the current n_old moves to old_to_new[i] (-1: removed; kept
+ * bodies keep their order and fill 0 .. kept-1), then n_add bodies from the
+ * arrays (q, v 3 x n_add) are appended with weight 1; the contact history is
+ * renumbered. Queued without waiting: the arrays stay valid and unchanged
+ * until a fence taken after this call is done (page-locked for the copies to
+ * overlap). For many independent scenes in one object; no counterpart in the
+ * reference. */
+hg_status hg_dem_edit_async(hg_dem *d, int64_t n_old, const int32_t *old_to_new,
+                            int64_t n_add, const double *q, const double *v,
+                            const double *radius, const double *mass,
+                            const double *inertia, const uint8_t *fixed);
+/* q, v (3 x N each; either may be NULL) copied to host memory behind the
+ * queued steps, without waiting (valid once a later fence is done). */
+hg_status hg_dem_frame_async(hg_dem *d, double *q, double *v);
+hg_status hg_dem_num_bodies(hg_dem *d, int64_t *n);
 /* RigidBody2DState::updateCurrentMassUsingMassWeights
  * (RigidBody2DState.cpp:1182-1200). */
 hg_status hg_dem_set_weights(hg_dem *d, const double *w);

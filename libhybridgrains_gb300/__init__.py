@@ -365,6 +365,24 @@ class DEM:
               _u8(fx), len(mp), _i32(mp))
         self.n = len(r)
 
+    def edit_async(self, old_to_new, q=None, v=None, r=None, m=None, I=None, fixed=None):
+        """hg_dem_edit_async: arrays (float64 C order, page-locked for overlap)
+        must stay alive until a later fence is done."""
+        mp = np.ascontiguousarray(old_to_new, dtype=np.int32)
+        n_add = 0 if r is None else len(r)
+        q, v, r, m, I = (None if a is None else _f64(a) for a in (q, v, r, m, I))
+        if fixed is not None:
+            fixed = np.ascontiguousarray(fixed, dtype=np.uint8)
+        check("hg_dem_edit_async", self._h, len(mp), _i32(mp), n_add, _d(q), _d(v), _d(r),
+              _d(m), _d(I), _u8(fixed))
+        c = ctypes.c_int64()
+        check("hg_dem_num_bodies", self._h, ctypes.byref(c))
+        self.n = c.value
+        return mp
+
+    def frame_async(self, q=None, v=None):
+        check("hg_dem_frame_async", self._h, _d(q), _d(v))
+
     def set_weights(self, w):
         check("hg_dem_set_weights", self._h, _d(_f64(w)))
 

@@ -160,6 +160,9 @@ SIGNATURES = {
     "hg_resampler_random_radius": [_P],
     "hg_dem_create": [_P, ctypes.POINTER(DemDesc), _PP],
     "hg_dem_upload_relabel": [_P, _i64, _D, _D, _D, _D, _D, _U8, _i64, _I32],
+    "hg_dem_edit_async": [_P, _i64, _I32, _i64, _D, _D, _D, _D, _D, _U8],
+    "hg_dem_frame_async": [_P, _D, _D],
+    "hg_dem_num_bodies": [_P, _I64],
     "hg_dem_destroy": [_P],
     "hg_dem_upload": [_P, _i64, _D, _D, _D, _D, _D, _U8],
     "hg_dem_set_weights": [_P, _D],

@@ -1170,6 +1170,48 @@ static hg_status dem_upload_impl(hg_dem *d, int64_t n, const double *q, const do
   return HG_OK;
 }
 
+hg_status hg_dem_edit_async(hg_dem *d, int64_t n_old, const int32_t *old_to_new, int64_t n_add,
+                            const double *q, const double *v, const double *r,
+                            const double *mass, const double *inertia, const uint8_t *fixed) {
+  if (!d) return fail(HG_ERR_INVALID_ARGUMENT, "d is NULL");
+  if (n_old != d->n) return fail(HG_ERR_INVALID_ARGUMENT, "n_old must be the current body count");
+  if (n_add < 0 || (n_old > 0 && !old_to_new)) return fail(HG_ERR_INVALID_ARGUMENT, "invalid edit");
+  if (n_add > 0 && (!q || !v || !r || !mass || !inertia))
+    return fail(HG_ERR_INVALID_ARGUMENT, "q, v, radius, mass and inertia are required");
+  int64_t keep = 0;
+  for (int64_t i = 0; i < n_old; ++i) {
+    if (old_to_new[i] < 0) continue;
+    if (old_to_new[i] != keep) return fail(HG_ERR_INVALID_ARGUMENT, "kept bodies must keep their order");
+    ++keep;
+  }
+  if (keep + n_add > d->cap) return fail(HG_ERR_CAPACITY, "body count exceeds capacity");
+  double rmax = 0.0;
+  for (int64_t i = 0; i < n_add; ++i) {
+    if (!(r[i] > 0.0) || !(mass[i] > 0.0) || !(inertia[i] > 0.0) || !std::isfinite(r[i]))
+      return fail(HG_ERR_INVALID_ARGUMENT, "radius, mass and inertia must be positive");
+    rmax = std::max(rmax, r[i]);
+  }
+  DeviceGuard g(d->ctx);
+  // the broadphase cell only grows: the candidate set does not depend on it
+  d->cell_h = std::max(d->cell_h, 2.0 * rmax * (1.0 + 1.0e-6));
+  return dem_edit(d, n_old, old_to_new, keep, n_add, q, v, r, mass, inertia, fixed);
+}
+
+hg_status hg_dem_frame_async(hg_dem *d, double *q, double *v) {
+  if (!d) return fail(HG_ERR_INVALID_ARGUMENT, "d is NULL");
+  DeviceGuard g(d->ctx);
+  hg_status st;
+  if ((st = d2h(d->ctx->stream, q, d->q.p, 3 * d->n)) || (st = d2h(d->ctx->stream, v, d->v.p, 3 * d->n)))
+    return st;
+  return HG_OK;
+}
+
+hg_status hg_dem_num_bodies(hg_dem *d, int64_t *n) {
+  if (!d || !n) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  *n = d->n;
+  return HG_OK;
+}
+
 hg_status hg_dem_set_weights(hg_dem *d, const double *w) {
   if (!d || (!w && d->n > 0)) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
   for (int64_t i = 0; i < d->n; ++i)

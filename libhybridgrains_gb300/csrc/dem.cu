@@ -744,31 +744,122 @@ __global__ void kd_relabel_move(int64_t ccap, const int32_t *__restrict__ count,
 
 } // namespace
 
-hg_status dem_relabel(hg_dem *d, const int32_t *map_host, int64_t nmap) {
+hg_status dem_relabel_device(hg_dem *d, const int32_t *map, int64_t nmap) {
   if (!d->history_valid) return HG_OK;
   cudaStream_t s = d->ctx->stream;
   const int64_t C = d->ccap;
-  DevBuf<int32_t> map, keep, off, tmp;
+  DevBuf<int32_t> keep, off, tmp;
   hg_status st;
-  if ((st = map.alloc(std::max<int64_t>(nmap, 1))) || (st = keep.alloc(C + 1)) ||
-      (st = off.alloc(C + 1)) || (st = tmp.alloc(scan_tmp_size(C + 1))))
+  if ((st = keep.alloc(C + 1)) || (st = off.alloc(C + 1)) || (st = tmp.alloc(scan_tmp_size(C + 1))))
     return st;
-  if (nmap > 0)
-    HG_CUDA_TRY(cudaMemcpyAsync(map.p, map_host, sizeof(int32_t) * nmap, cudaMemcpyHostToDevice, s));
   const int nb = 1 - d->cc;
   HG_LAUNCH(kd_relabel_keep, blocks_for(C + 1, 256), 256, 0, s, C, d->c_count.p + d->cc,
-            d->ckey[d->cc].p, map.p, nmap, keep.p);
+            d->ckey[d->cc].p, map, nmap, keep.p);
   HG_CHECK_LAUNCH();
   if ((st = exclusive_scan_i32(keep.p, off.p, C + 1, tmp.p, s))) return st;
   HG_LAUNCH(kd_relabel_move, blocks_for(C + 1, 256), 256, 0, s, C, d->c_count.p + d->cc,
-            d->ckey[d->cc].p, d->crec[d->cc].p, map.p, nmap, off.p, d->ckey[nb].p,
+            d->ckey[d->cc].p, d->crec[d->cc].p, map, nmap, off.p, d->ckey[nb].p,
             d->crec[nb].p, d->c_count.p + nb);
   HG_CHECK_LAUNCH();
   d->cc = nb;
+  return HG_OK;
+}
+
+hg_status dem_relabel(hg_dem *d, const int32_t *map_host, int64_t nmap) {
+  if (!d->history_valid) return HG_OK;
+  cudaStream_t s = d->ctx->stream;
+  DevBuf<int32_t> map;
+  hg_status st;
+  if ((st = map.alloc(std::max<int64_t>(nmap, 1)))) return st;
+  if (nmap > 0)
+    HG_CUDA_TRY(cudaMemcpyAsync(map.p, map_host, sizeof(int32_t) * nmap, cudaMemcpyHostToDevice, s));
+  if ((st = dem_relabel_device(d, map.p, nmap))) return st;
   // the map was copied from the caller's memory: it may go once this returns
   HG_CUDA_TRY(cudaStreamSynchronize(s));
   return HG_OK;
 }
+
+namespace {
+
+// Moves kept bodies to their new slots (old_to_new, monotone) in scratch
+// arrays; the caller copies the scratch back.
+__global__ void kd_compact_bodies(int64_t n_old, const int32_t *__restrict__ map,
+                                  const double *__restrict__ q, const double *__restrict__ v,
+                                  const double *__restrict__ r, const double *__restrict__ m0,
+                                  const double *__restrict__ I0, const double *__restrict__ w,
+                                  const uint8_t *__restrict__ fixed, double *tq, double *tv,
+                                  double *tr, double *tm, double *tI, double *tw, uint8_t *tf) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n_old) return;
+  const int32_t j = map[i];
+  if (j < 0) return;
+  for (int c = 0; c < 3; ++c) {
+    tq[3 * (int64_t)j + c] = q[3 * i + c];
+    tv[3 * (int64_t)j + c] = v[3 * i + c];
+  }
+  tr[j] = r[i];
+  tm[j] = m0[i];
+  tI[j] = I0[i];
+  tw[j] = w[i];
+  tf[j] = fixed[i];
+}
+
+__global__ void kd_ones(double *a, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) a[i] = 1.0;
+}
+
+} // namespace
+
+hg_status dem_edit(hg_dem *d, int64_t n_old, const int32_t *map_host, int64_t n_keep,
+                   int64_t n_add, const double *q, const double *v, const double *r,
+                   const double *m, const double *I, const uint8_t *fixed) {
+  cudaStream_t s = d->ctx->stream;
+  hg_status st;
+  DevBuf<int32_t> map;
+  if (n_old > 0) {
+    DevBuf<double> tq, tv, tr, tm, tI, tw;
+    DevBuf<uint8_t> tf;
+    const int64_t k = std::max<int64_t>(n_keep, 1);
+    if ((st = map.alloc(n_old)) || (st = tq.alloc(3 * k)) || (st = tv.alloc(3 * k)) ||
+        (st = tr.alloc(k)) || (st = tm.alloc(k)) || (st = tI.alloc(k)) || (st = tw.alloc(k)) ||
+        (st = tf.alloc(k)))
+      return st;
+    HG_CUDA_TRY(cudaMemcpyAsync(map.p, map_host, sizeof(int32_t) * n_old, cudaMemcpyHostToDevice, s));
+    HG_LAUNCH(kd_compact_bodies, blocks_for(n_old, 256), 256, 0, s, n_old, map.p, d->q.p, d->v.p,
+              d->r.p, d->m0.p, d->I0.p, d->w.p, d->fixed.p, tq.p, tv.p, tr.p, tm.p, tI.p, tw.p,
+              tf.p);
+    HG_CHECK_LAUNCH();
+    if (n_keep > 0) {
+      HG_CUDA_TRY(cudaMemcpyAsync(d->q.p, tq.p, sizeof(double) * 3 * n_keep, cudaMemcpyDeviceToDevice, s));
+      HG_CUDA_TRY(cudaMemcpyAsync(d->v.p, tv.p, sizeof(double) * 3 * n_keep, cudaMemcpyDeviceToDevice, s));
+      HG_CUDA_TRY(cudaMemcpyAsync(d->r.p, tr.p, sizeof(double) * n_keep, cudaMemcpyDeviceToDevice, s));
+      HG_CUDA_TRY(cudaMemcpyAsync(d->m0.p, tm.p, sizeof(double) * n_keep, cudaMemcpyDeviceToDevice, s));
+      HG_CUDA_TRY(cudaMemcpyAsync(d->I0.p, tI.p, sizeof(double) * n_keep, cudaMemcpyDeviceToDevice, s));
+      HG_CUDA_TRY(cudaMemcpyAsync(d->w.p, tw.p, sizeof(double) * n_keep, cudaMemcpyDeviceToDevice, s));
+      HG_CUDA_TRY(cudaMemcpyAsync(d->fixed.p, tf.p, n_keep, cudaMemcpyDeviceToDevice, s));
+    }
+    if ((st = dem_relabel_device(d, map.p, n_old))) return st;
+  }
+  if (n_add > 0) {
+    const int64_t o = n_keep;
+    HG_CUDA_TRY(cudaMemcpyAsync(d->q.p + 3 * o, q, sizeof(double) * 3 * n_add, cudaMemcpyHostToDevice, s));
+    HG_CUDA_TRY(cudaMemcpyAsync(d->v.p + 3 * o, v, sizeof(double) * 3 * n_add, cudaMemcpyHostToDevice, s));
+    HG_CUDA_TRY(cudaMemcpyAsync(d->r.p + o, r, sizeof(double) * n_add, cudaMemcpyHostToDevice, s));
+    HG_CUDA_TRY(cudaMemcpyAsync(d->m0.p + o, m, sizeof(double) * n_add, cudaMemcpyHostToDevice, s));
+    HG_CUDA_TRY(cudaMemcpyAsync(d->I0.p + o, I, sizeof(double) * n_add, cudaMemcpyHostToDevice, s));
+    if (fixed) {
+      HG_CUDA_TRY(cudaMemcpyAsync(d->fixed.p + o, fixed, n_add, cudaMemcpyHostToDevice, s));
+    } else {
+      HG_CUDA_TRY(cudaMemsetAsync(d->fixed.p + o, 0, n_add, s));
+    }
+    HG_LAUNCH(kd_ones, blocks_for(n_add, 256), 256, 0, s, d->w.p + o, n_add);
+    HG_CHECK_LAUNCH();
+  }
+  d->n = n_keep + n_add;
+  return HG_OK;
+}
+
 
 hg_status dem_download_contacts(hg_dem *d, int64_t cap, double *rec, int64_t *count) {
   cudaStream_t s = d->ctx->stream;

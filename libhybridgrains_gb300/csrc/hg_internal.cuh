@@ -332,6 +332,11 @@ hg_status dem_alloc(hg_dem *d);
 hg_status dem_reset_history(hg_dem *d);
 // renumber the contact history by old_to_new (-1: removed) of nmap bodies
 hg_status dem_relabel(hg_dem *d, const int32_t *old_to_new, int64_t nmap);
+hg_status dem_relabel_device(hg_dem *d, const int32_t *old_to_new, int64_t nmap);
+// remove bodies by old_to_new and append n_add bodies, on the device, queued
+hg_status dem_edit(hg_dem *d, int64_t n_old, const int32_t *old_to_new, int64_t n_keep,
+                   int64_t n_add, const double *q, const double *v, const double *r,
+                   const double *m, const double *I, const uint8_t *fixed);
 hg_status dem_step(hg_dem *d, double dt, int weighted);
 hg_status dem_download_contacts(hg_dem *d, int64_t cap, double *rec,
                                 int64_t *count);

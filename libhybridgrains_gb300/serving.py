@@ -19,6 +19,15 @@ a frame every ``frame_every`` steps. The loop
   ``depth`` chunks queued on the device;
 * records for each request its arrival, admission and completion times.
 
+A request may carry a DEM pile (disks of the rigidbody2d penalty map) beside
+its MPM column. The piles of all resident requests share one DEM object, each
+in its own lane (shifted LANE metres along x, so that piles never meet and the
+broadphase hash keeps them apart); a request's disks are a contiguous range of
+bodies. Piles join and leave at chunk boundaries through one edit of the DEM
+object per chunk (stable compaction of the remaining bodies, which renumbers
+their contact history, then the new piles appended), and the whole body array
+is copied once per chunk for the frames.
+
 The scheduling is separate from the device (``Backend``) so that admission
 and ordering can be tested without a GPU.
 """
@@ -33,9 +42,10 @@ from . import scenes
 
 class Request:
     __slots__ = ("rid", "arrival", "cfg", "npoints", "steps", "frame_every", "dt",
-                 "admitted", "finished", "frames", "footprint", "issued")
+                 "admitted", "finished", "frames", "footprint", "issued", "ndisks", "aspect")
 
-    def __init__(self, rid, arrival, cfg, npoints, steps=2000, frame_every=100, dt=1.0e-5):
+    def __init__(self, rid, arrival, cfg, npoints, steps=2000, frame_every=100, dt=1.0e-5,
+                 ndisks=0, aspect=1.0):
         self.rid = rid
         self.arrival = arrival
         self.cfg = cfg
@@ -45,9 +55,19 @@ class Request:
         self.dt = dt
         self.admitted = None
         self.finished = None
-        self.frames = []  # per frame: (step, run-out x of the front)
+        # per frame: (step, (front x of the column, front x of the pile in its
+        # lane or None without disks))
+        self.frames = []
         self.footprint = 0
         self.issued = 0   # frames queued on the device
+        self.ndisks = ndisks  # disks of the request's DEM pile
+        self.aspect = aspect
+
+    def copy(self, arrival=None):
+        """A fresh request for the same scene (no frames or times)."""
+        return Request(self.rid, self.arrival if arrival is None else arrival, self.cfg,
+                       self.npoints, self.steps, self.frame_every, self.dt, self.ndisks,
+                       self.aspect)
 
     @property
     def latency(self):
@@ -55,10 +75,11 @@ class Request:
 
 
 def column_requests(n=256, rate=50.0, seed=2024, steps=2000, frame_every=100,
-                    nmin=2.0e3, nmax=2.0e5):
+                    nmin=2.0e3, nmax=2.0e5, dem_max=0.2):
     """Seeded request stream: exponential inter-arrival gaps at ``rate``/s,
     aspect ratio U[0.5, 4], point count log-uniform in [nmin, nmax],
-    friction angle U[20, 40] degrees."""
+    friction angle U[20, 40] degrees, and a DEM pile of U[0, dem_max] times
+    the point count in disks."""
     rng = np.random.default_rng(seed)
     gaps = rng.exponential(1.0 / rate, size=n)
     arrivals = np.cumsum(gaps) - gaps[0]
@@ -67,11 +88,43 @@ def column_requests(n=256, rate=50.0, seed=2024, steps=2000, frame_every=100,
         aspect = rng.uniform(0.5, 4.0)
         npts = math.exp(rng.uniform(math.log(nmin), math.log(nmax)))
         phi = rng.uniform(20.0, 40.0)
+        frac = rng.uniform(0.0, dem_max)
         cfg = scenes.serving_column(npts, aspect, phi)
         npoints = len(scenes.seed_column_points(cfg)["m"])
         out.append(Request(i, float(arrivals[i]), cfg, npoints, steps, frame_every,
-                           cfg["dt"]))
+                           cfg["dt"], int(round(frac * npoints)), aspect))
     return out
+
+
+LANE = 10.0  # m between the DEM piles of the scenes sharing one DEM object
+
+
+def dem_pile(req, lane):
+    """The request's DEM pile (the DEM column's disks: r U[0.9, 1.1] mm, hex
+    pitch 2.2 mm, rho 2600) on the floor with the request's aspect ratio,
+    shifted to its lane."""
+    per_row = max(4, int(round(math.sqrt(max(req.ndisks, 1) / req.aspect))))
+    return scenes.dem_column(n=req.ndisks, per_row=per_row, seed=1000 + req.rid,
+                             x0=lane * LANE)
+
+
+def dem_for_piles(ctx, capacity):
+    """A DEM object for piles: the penalty parameters of the DEM column and
+    the floor (y = 0) as the only plane."""
+    from . import DEM
+    p = scenes.dem_params()
+    return DEM(ctx, scenes.GRAVITY, p["kn"], p["kt"], p["gamman"], p["gammat"], p["mu"],
+               [((0.0, 0.0), (0.0, 1.0))], capacity=capacity,
+               contact_capacity=4 * max(capacity, 1))
+
+
+def frame_diff(a, b):
+    """Largest difference of the fronts of two frames (column and pile)."""
+    (ma, da), (mb, db) = a, b
+    d = abs(ma - mb)
+    if da is not None or db is not None:
+        d = max(d, abs(da - db))
+    return d
 
 
 class Backend:
@@ -79,6 +132,9 @@ class Backend:
 
     def footprint(self, req):
         raise NotImplementedError
+
+    def can_open(self, req):  # room for the request besides its footprint
+        return True
 
     def open(self, req):  # create the scene and join the batch
         raise NotImplementedError
@@ -148,7 +204,8 @@ class Server:
             # admission: FIFO, by footprint and free slots
             admitted = 0
             while waiting and len(active) < self.max_members and admitted < self.admit_per_chunk \
-                    and self.resident + waiting[0].footprint <= self.budget:
+                    and self.resident + waiting[0].footprint <= self.budget \
+                    and self.b.can_open(waiting[0]):
                 admitted += 1
                 r = waiting.popleft()
                 self.b.open(r)
@@ -220,6 +277,7 @@ def summary(requests, makespan):
     lat = np.array([r.latency for r in requests])
     wait = np.array([r.admitted - r.arrival for r in requests])
     psteps = float(sum(r.npoints * r.steps for r in requests))
+    dsteps = float(sum(r.ndisks * r.steps for r in requests))
     return dict(requests=len(requests), p50_latency_s=float(np.percentile(lat, 50)),
                 p99_latency_s=float(np.percentile(lat, 99)),
                 max_latency_s=float(lat.max()),
@@ -227,13 +285,16 @@ def summary(requests, makespan):
                 p99_admission_wait_s=float(np.percentile(wait, 99)),
                 makespan_s=makespan, particle_steps=psteps,
                 particle_steps_per_s=psteps / makespan,
+                disk_steps=dsteps, disk_steps_per_s=dsteps / makespan,
                 requests_per_s=len(requests) / makespan)
 
 
 class DeviceBackend(Backend):
-    """The loop on one GPU: MIXED MPM scenes in one hg_batch."""
+    """The loop on one GPU: MIXED MPM scenes in one hg_batch, and their DEM
+    piles in one DEM object of ``dem_capacity`` bodies (a fixed pool outside
+    the HBM budget; a request waits while its pile does not fit)."""
 
-    def __init__(self, ctx, max_members=256, depth=3):
+    def __init__(self, ctx, max_members=256, depth=3, dem_capacity=1 << 21):
         from . import Batch  # noqa: WPS433 (package import cycle)
         self.ctx = ctx
         self.batch = Batch(ctx, max_members)
@@ -241,6 +302,18 @@ class DeviceBackend(Backend):
         self.state = {}
         self.pool = collections.defaultdict(list)  # page-locked buffers by size class
         self.owner = {}
+        # DEM piles
+        self.dem = None
+        self.dem_capacity = int(dem_capacity)
+        self.dem_dt = None
+        self.free_lanes = list(range(max_members - 1, -1, -1))  # pop() gives the lowest
+        self.order = []        # requests with disks in the DEM object, in body order
+        self.adds = []         # piles opened since the last step
+        self.drops = set()     # rids of piles that leave at the next step
+        self.disks = 0         # disks in the DEM object and opened since
+        self.staging = []      # (fence, page-locked buffer) of edits in flight
+        self.chunk = 0
+        self.dem_frames = {}   # chunk -> [buffer, {rid: (start, count, x0)}, readers]
 
     def _buf(self, shape):
         """A page-locked view of the given shape, from a pool of buffers whose
@@ -261,8 +334,14 @@ class DeviceBackend(Backend):
 
     def footprint(self, req):
         from . import mpm_estimate_bytes
+        if req.ndisks > self.dem_capacity:
+            raise ValueError(f"request {req.rid} has {req.ndisks} disks, over the DEM "
+                             f"capacity of {self.dem_capacity}")
         c = req.cfg
         return mpm_estimate_bytes(c["grid_min"], c["grid_max"], c["h"], req.npoints)
+
+    def can_open(self, req):
+        return self.disks + req.ndisks <= self.dem_capacity
 
     def open(self, req):
         from . import MPM
@@ -274,17 +353,82 @@ class DeviceBackend(Backend):
         m.seed_rectangle_device(c["rect_min"], c["rect_max"], c["rho"], c["samples_per_dim"])
         frames = [self._buf((req.npoints, 2)) for _ in range(self.depth + 1)]
         self.batch.add(m, req.dt)
-        self.state[req.rid] = dict(m=m, frames=frames)
+        st = dict(m=m, frames=frames, dem_chunk=[None] * (self.depth + 1))
+        if req.ndisks > 0:
+            if self.dem_dt is None:
+                self.dem_dt = req.dt
+            elif req.dt != self.dem_dt:
+                raise ValueError("the DEM piles of one backend share a time step")
+            st["lane"] = self.free_lanes.pop()
+            self.adds.append((req, dem_pile(req, st["lane"])))
+            self.disks += req.ndisks
+        self.state[req.rid] = st
+
+    def _edit_piles(self):
+        """One DEM edit: drop the piles that left, append the opened ones."""
+        if self.dem is None:
+            self.dem = dem_for_piles(self.ctx, self.dem_capacity)
+        n_old = sum(r.ndisks for r in self.order)
+        old_to_new = np.full(n_old, -1, dtype=np.int32)
+        keep, o, k = [], 0, 0
+        for r in self.order:
+            if r.rid not in self.drops:
+                old_to_new[o:o + r.ndisks] = np.arange(k, k + r.ndisks, dtype=np.int32)
+                k += r.ndisks
+                keep.append(r)
+            o += r.ndisks
+        n_add = sum(r.ndisks for r, _ in self.adds)
+        arrays = {}
+        if n_add:
+            # one page-locked staging buffer: q, v (3 per disk), radius, mass, inertia
+            buf = self._buf((9 * n_add,))
+            names = (("q", 3), ("v", 3), ("r", 1), ("m", 1), ("I", 1))
+            o = 0
+            for name, w in names:
+                a = buf[o:o + w * n_add]
+                arrays[name] = a.reshape(n_add, w) if w > 1 else a
+                o += w * n_add
+            o = 0
+            for r, pile in self.adds:
+                for name, _ in names:
+                    arrays[name][o:o + r.ndisks] = pile[name]
+                o += r.ndisks
+        self.dem.edit_async(old_to_new, **arrays)
+        if n_add:
+            self.staging.append((self.ctx.fence(), buf))
+        self.order = keep + [r for r, _ in self.adds]
+        self.adds, self.drops = [], set()
 
     def step(self, nsteps):
+        while self.staging and self.ctx.fence_done(self.staging[0][0]):
+            self._give(self.staging.pop(0)[1])
+        if self.adds or self.drops:
+            self._edit_piles()
         self.batch.step(nsteps)
+        if self.dem is not None and self.dem.n > 0:
+            self.dem.flow(self.dem_dt, nsteps)
+        self.chunk += 1
 
     def frame(self, req, slot):
         s = self.state[req.rid]
         s["m"].frame_async(s["frames"][slot], None)
+        if req.ndisks > 0:
+            fr = self.dem_frames.get(self.chunk)
+            if fr is None:  # the chunk's first frame copies all bodies
+                buf = self._buf((self.dem.n, 3))
+                self.dem.frame_async(buf)
+                ranges, o = {}, 0
+                for r in self.order:
+                    ranges[r.rid] = (o, r.ndisks, self.state[r.rid]["lane"] * LANE)
+                    o += r.ndisks
+                fr = self.dem_frames[self.chunk] = [buf, ranges, 0]
+            fr[2] += 1
+            s["dem_chunk"][slot] = self.chunk
 
     def leave(self, req):
         self.batch.remove(self.state[req.rid]["m"])
+        if req.ndisks > 0:
+            self.drops.add(req.rid)
 
     def fence(self):
         return self.ctx.fence()
@@ -296,23 +440,40 @@ class DeviceBackend(Backend):
         self.ctx.fence_wait(f)
 
     def read_frame(self, req, slot):
-        q = self.state[req.rid]["frames"][slot]
-        return float(q[:, 0].max())  # run-out: front position
+        s = self.state[req.rid]
+        q = s["frames"][slot]
+        pile = None
+        if req.ndisks > 0:
+            c = s["dem_chunk"][slot]
+            fr = self.dem_frames[c]
+            o, n, x0 = fr[1][req.rid]
+            pile = float(fr[0][o:o + n, 0].max() - x0)
+            fr[2] -= 1
+            if fr[2] == 0:
+                self._give(fr[0])
+                del self.dem_frames[c]
+        return float(q[:, 0].max()), pile  # run-outs: front positions
 
     def close(self, req):
         s = self.state.pop(req.rid)
         s["m"].close()
         for a in s["frames"]:
             self._give(a)
+        if req.ndisks > 0:
+            self.free_lanes.append(s["lane"])
+            self.free_lanes.sort(reverse=True)
+            self.disks -= req.ndisks
 
     def shutdown(self):
         self.batch.close()
+        if self.dem is not None:
+            self.dem.close()
 
 
 def run_one_at_a_time(ctx, requests):
     """The same requests served one after another, each scene alone
-    (hg_mpm_step per frame interval, frame read synchronously); returns
-    wall seconds."""
+    (hg_mpm_step and, with disks, hg_dem_step of its own DEM object per frame
+    interval, frames read synchronously); returns wall seconds."""
     from . import MPM
     t0 = time.perf_counter()
     for r in requests:
@@ -321,11 +482,20 @@ def run_one_at_a_time(ctx, requests):
                 c["bulk_modulus"], c["dp_alpha"], c["flip_alpha"], scenes.GRAVITY,
                 c["planes"], capacity=r.npoints)
         m.seed_rectangle_device(c["rect_min"], c["rect_max"], c["rho"], c["samples_per_dim"])
+        d = None
+        if r.ndisks > 0:
+            p = dem_pile(r, 0)
+            d = dem_for_piles(ctx, r.ndisks)
+            d.upload(p["q"], p["v"], p["r"], p["m"], p["I"], p["fixed"])
         q = np.zeros((r.npoints, 2))
         for k in range(r.steps // r.frame_every):
             m.flow(r.dt, r.frame_every)
+            if d is not None:
+                d.flow(r.dt, r.frame_every)
             m.download_into(q=q)
-            r.frames.append(((k + 1) * r.frame_every, float(q[:, 0].max())))
+            pile = None if d is None else float(d.download()[0][:, 0].max())
+            r.frames.append(((k + 1) * r.frame_every, (float(q[:, 0].max()), pile)))
         m.close()
+        if d is not None:
+            d.close()
     return time.perf_counter() - t0
-

@@ -126,3 +126,58 @@ def test_upload_relabel_keeps_renumbered_history(ctx):
     assert np.array_equal(after, exp)
     d.flow(1e-6, 10)
     assert d.status() == 0
+
+
+def test_edit_async_matches_the_scene_without_the_removed_pile(ctx):
+    """hg_dem_edit_async (bodies removed by a stable compaction, new ones
+    appended, all on the device): three piles A, B, C step together, B leaves
+    and D joins; a second object that never held B (A and C, then D appended)
+    gives the same positions, velocities and collision cache bit for bit,
+    so the compaction renumbered the contact history of A and C exactly."""
+    from libhybridgrains_gb300 import serving
+
+    def pile(rid, n, lane):
+        return serving.dem_pile(serving.Request(rid, 0.0, None, 0, ndisks=n, aspect=1.5), lane)
+
+    A, B, C, D = pile(1, 700, 0), pile(2, 500, 1), pile(3, 900, 2), pile(4, 400, 3)
+
+    def cat(*ps):
+        return {k: np.concatenate([p[k] for p in ps]) for k in ("q", "v", "r", "m", "I")}
+
+    x = serving.dem_for_piles(ctx, 3000)
+    y = serving.dem_for_piles(ctx, 3000)
+    for d, s in ((x, cat(A, B, C)), (y, cat(A, C))):
+        d.edit_async(np.zeros(0, dtype=np.int32), **s)
+    x.flow(1e-5, 1000)  # 10 ms: the piles settle into contact
+    y.flow(1e-5, 1000)
+    nA, nB, nC = 700, 500, 900
+    assert x.n == nA + nB + nC and y.n == nA + nC
+    drop = np.concatenate([np.arange(nA), np.full(nB, -1), nA + np.arange(nC)]).astype(np.int32)
+    x.edit_async(drop, **D)
+    y.edit_async(np.arange(nA + nC, dtype=np.int32), **D)
+    assert x.n == y.n == nA + nC + 400
+    x.flow(1e-5, 1001)  # graph replays and one plain step
+    y.flow(1e-5, 1001)
+    qx, vx = x.download()
+    qy, vy = y.download()
+    assert np.array_equal(qx, qy) and np.array_equal(vx, vy)
+    cx, cy = x.contacts(), y.contacts()
+    assert len(cx) > 500 and np.array_equal(cx, cy)
+    assert np.abs(cx[:, 6:8]).max() > 0  # tangential springs carried over
+    assert x.status() == 0 and y.status() == 0
+    # everything removed, then refilled
+    x.edit_async(np.full(x.n, -1, dtype=np.int32))
+    assert x.n == 0
+    x.flow(1e-5, 5)
+    x.edit_async(np.zeros(0, dtype=np.int32), **A)
+    x.flow(1e-5, 5)
+    assert x.n == nA and np.isfinite(x.download()[0]).all()
+    # host-side checks: capacity, order of the kept bodies
+    with pytest.raises(hg.HGError):
+        x.edit_async(np.arange(nA, dtype=np.int32), **cat(B, C, D, D, D, D))
+    bad = np.arange(nA, dtype=np.int32)
+    bad[[0, 1]] = bad[[1, 0]]
+    with pytest.raises(hg.HGError):
+        x.edit_async(bad)
+    x.close()
+    y.close()

@@ -4,9 +4,12 @@
   download bit for bit (the same conversion kernel);
 * admission estimate: hg_mpm_estimate_bytes bounds the device bytes an MPM
   object really holds after upload and downloads, within 10% + 1 MiB;
-* continuous batching: every request's frames (front run-out per 100 steps)
-  equal those of the same scene served alone within 1e-9 m (FP32 atomic
-  summation order is the only difference).
+* continuous batching: every request's frames (the column's front and its
+  DEM pile's front per 100 steps) equal those of the same scene served alone
+  within 1e-9 m. For the columns FP32 atomic summation order is the only
+  difference; the piles share one DEM object in the mix, shifted by their
+  lane, where alone each sits at x = 0, so their FP64 positions round
+  differently.
 """
 import numpy as np
 import pytest
@@ -99,8 +102,8 @@ def test_serving_results_match_scenes_served_alone(ctx):
     reqs = serving.column_requests(n=6, rate=400.0, seed=11, steps=300, nmax=3.0e4)
     for r, t in zip(reqs, (0.0, 0.0, 0.0, 0.002, 0.004, 0.006)):
         r.arrival = t  # three at once, three while those run
-    alone = [serving.Request(r.rid, r.arrival, r.cfg, r.npoints, r.steps, r.frame_every, r.dt)
-             for r in reqs]
+    assert sum(r.ndisks > 0 for r in reqs) >= 4
+    alone = [r.copy() for r in reqs]
     be = serving.DeviceBackend(ctx, max_members=8)
     srv = serving.Server(be, 2**33, max_members=8)
     srv.run(reqs)
@@ -111,5 +114,6 @@ def test_serving_results_match_scenes_served_alone(ctx):
         assert [s for s, _ in a.frames] == [100, 200, 300]
         assert [s for s, _ in b.frames] == [100, 200, 300]
         for (_, x), (_, y) in zip(a.frames, b.frames):
-            assert abs(x - y) <= 1e-9
+            assert (x[1] is None) == (a.ndisks == 0) and (y[1] is None) == (a.ndisks == 0)
+            assert serving.frame_diff(x, y) <= 1e-9, (a.rid, x, y)
         assert a.finished >= a.admitted >= a.arrival
