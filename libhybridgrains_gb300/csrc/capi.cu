@@ -1149,6 +1149,7 @@ static hg_status dem_upload_impl(hg_dem *d, int64_t n, const double *q, const do
   d->cell_h = 2.0 * rmax * (1.0 + 1.0e-6);
   cudaStream_t s = d->ctx->stream;
   d->n = n;
+  d->inv_valid = false;
   hg_status st;
   if ((st = h2d(s, d->q.p, q, 3 * n)) || (st = h2d(s, d->v.p, v, 3 * n)) ||
       (st = h2d(s, d->r.p, r, n)) || (st = h2d(s, d->m0.p, mass, n)) ||
@@ -1219,6 +1220,7 @@ hg_status hg_dem_set_weights(hg_dem *d, const double *w) {
   DeviceGuard g(d->ctx);
   hg_status st = h2d(d->ctx->stream, d->w.p, w, d->n);
   if (st) return st;
+  d->inv_valid = false;
   HG_CUDA_TRY(cudaStreamSynchronize(d->ctx->stream));
   return HG_OK;
 }
@@ -1299,7 +1301,8 @@ hg_status hg_dem_step(hg_dem *d, double dt, int32_t nsteps, int32_t weighted) {
   if (nsteps >= 4 && d->n > 0) {
     // Repeated steps replay a captured pair of steps: one graph launch in
     // place of about 40 kernel launches and memsets.
-    hg_status st = dem_pair_graph(d, dt, weighted);
+    hg_status st = dem_prepare(d);
+    if (st == HG_OK) st = dem_pair_graph(d, dt, weighted);
     if (st != HG_OK) return st;
     for (; k + 2 <= nsteps; k += 2) {
       HG_CUDA_TRY(cudaGraphLaunch(d->pair_exec, d->ctx->stream));

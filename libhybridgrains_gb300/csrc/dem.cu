@@ -9,17 +9,22 @@
 // FP64 evaluation of the reference bit for bit.
 //
 // Kernels per step:
-//   kd_home / kd_fill        broadphase: hash-grid counting sort of the disks
+//   kd_bodies_home / kd_fill broadphase: hash-grid counting sort of the disks
 //                            by the cell of their AABB minimum. The cell width
 //                            is 2 r_max (1 + 1e-6), so the partners of a disk
 //                            lie in 3x3 cells; the result is the reference's
 //                            candidate set {i < j : AABBs overlap}
 //                            (SpatialGrid.cpp:14-19, 90-118), independent of
 //                            the reference's own cell width.
-//   kd_pairs<EMIT>           narrow phase (RigidBody2DSim.cpp:270-336 with
+//   kd_pairs_count / _emit   narrow phase (RigidBody2DSim.cpp:270-336 with
 //                            q0 == q1, CollisionDetectionUtilities.cpp:3-101)
 //                            and body-plane tests (RigidBody2DSim.cpp:777-842);
-//                            count, then emit sorted per-body contact lists.
+//                            count (keeping short partner lists), then emit
+//                            sorted per-body contact lists. Candidates are
+//                            filtered in FP32 on cell-relative offsets before
+//                            the exact FP64 tests: FP64 runs at 1/64 of the
+//                            FP32 rate on this part, and the filter leaves
+//                            about one FP64 test per contact.
 //   kd_contacts              collision-cache update with tangential-spring
 //                            carry (PenaltyImpactFrictionMap.cpp:296-599) and
 //                            the penalty force with Coulomb projection
@@ -61,6 +66,10 @@ __device__ __forceinline__ D2 dnormalized(D2 a) {
   return a;
 }
 __device__ __forceinline__ double dcross(D2 a, D2 b) { return a.x * b.y - a.y * b.x; }
+// isfinite on the bit pattern (integer pipe; FP64 compares are scarce here)
+__device__ __forceinline__ bool finite_bits(double x) {
+  return ((__double_as_longlong(x) >> 52) & 0x7FF) != 0x7FF;
+}
 
 __device__ __forceinline__ uint32_t cell_hash(int cx, int cy, uint32_t mask) {
   return ((uint32_t)cx * 73856093u ^ (uint32_t)cy * 19349663u) & mask;
@@ -114,18 +123,86 @@ __device__ __forceinline__ void sort_small(int *keys, int n) {
   }
 }
 
+// Per body, for the pair search: the home cell (the cell of the AABB
+// minimum) and, in FP32, the offset of the centre from the home cell's
+// corner and the radius, with the fixed flag and the active static planes
+// (StaticPlaneCircleConstraint::isActive, StaticPlaneCircleConstraint.cpp:
+// 12-17, in FP64) as bits. The FP64 arithmetic per body is a few operations;
+// per candidate pair the search needs FP32 only, except for the exact tests
+// of the pairs that survive the FP32 filter. The home cell only has to be a
+// consistent binning (the search covers the neighbouring cells), so it is
+// floor(x_min / H) computed as x_min * (1 / H).
+struct HomeArgs {
+  int64_t n;
+  double H, invH;
+  uint32_t mask;
+  int nplanes;
+  double px[HG_MAX_PLANES][2], pn[HG_MAX_PLANES][2];
+  const double *q, *r;
+  const uint8_t *fixed;
+  float4 *rec; // 2 per body: (offset x, offset y, radius, flags), (home cell x, y)
+  int32_t *bucket_count;
+};
+
+enum : uint32_t { REL_FIXED = 1u, REL_PLANE0 = 2u };
+
+__global__ void kd_bodies_home(HomeArgs A) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= A.n) return;
+  // CircleGeometry::computeCollisionAABB (CircleGeometry.cpp:22-30), q0 == q1
+  const double x = A.q[3 * i], y = A.q[3 * i + 1], ri = A.r[i];
+  const int cx = (int)floor((x - ri) * A.invH), cy = (int)floor((y - ri) * A.invH);
+  uint32_t flags = A.fixed[i] ? REL_FIXED : 0u;
+  for (int k = 0; k < A.nplanes; ++k) {
+    const double d = A.pn[k][0] * (x - A.px[k][0]) + A.pn[k][1] * (y - A.px[k][1]);
+    if (d <= ri) flags |= REL_PLANE0 << k;
+  }
+  // one 32-byte record: the FP32 part, then the home cell
+  A.rec[2 * i] = make_float4((float)(x - (double)cx * A.H), (float)(y - (double)cy * A.H),
+                             (float)ri, __uint_as_float(flags));
+  A.rec[2 * i + 1] = make_float4(__int_as_float(cx), __int_as_float(cy), 0.0f, 0.0f);
+  atomicAdd(&A.bucket_count[cell_hash(cx, cy, A.mask)], 1);
+}
+
+// Places each body in its bucket. bucket_pos holds the bucket starts and
+// ends up holding the bucket ends (start + count).
+__global__ void kd_fill_ends(int64_t n, uint32_t mask, const float4 *__restrict__ rec,
+                             int32_t *bucket_pos, int32_t *items) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 h = rec[2 * i + 1];
+  items[atomicAdd(&bucket_pos[cell_hash(__float_as_int(h.x), __float_as_int(h.y), mask)], 1)] =
+      (int32_t)i;
+}
+
+// 1 / (m0 w) and 1 / (I0 w): the inverse masses of kd_integrate
+// (RigidBody2DState::updateCurrentMassUsingMassWeights), recomputed when
+// masses or weights change.
+__global__ void kd_inverse_masses(int64_t n, const double *__restrict__ m0,
+                                  const double *__restrict__ I0, const double *__restrict__ w,
+                                  double *inv) {
+  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  inv[2 * j] = 1.0 / (m0[j] * w[j]);
+  inv[2 * j + 1] = 1.0 / (I0[j] * w[j]);
+}
+
+constexpr int PW = 8; // partners per body kept by the counting pass
+
 struct PairArgs {
-  BroadArgs B;
-  const int2 *home;
-  const int32_t *bucket_start;
+  int64_t n;
+  uint32_t mask;
+  const float4 *rec; // body records of kd_bodies_home
+  float Hf;  // cell width in FP32
+  float tol; // FP32 filter slack
+  const int32_t *bucket_end;
   const int32_t *bucket_count;
   const int32_t *items;
   const double *q;
   const double *r;
-  const uint8_t *fixed;
   int nplanes;
-  double px[HG_MAX_PLANES][2], pn[HG_MAX_PLANES][2];
   int32_t *cnt;       // 3N counts [kind][body]
+  uint32_t *plist;    // PW partners per body (fixed partners flagged by bit 31)
   const int32_t *off; // 3N+1 offsets (emit pass)
   int64_t *keys;      // emit pass output
   int64_t ccap;
@@ -135,75 +212,139 @@ struct PairArgs {
 
 // Contact enumeration for body a as the first index: circle-circle with
 // b > a non-fixed, kinematic with b fixed (any index; the reference swaps the
-// fixed body into the second slot), and static planes. Fixed bodies emit none.
-template <bool EMIT> __global__ void kd_pairs(PairArgs A) {
-  const int64_t n = A.B.n;
-  const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (a >= n) return;
-  int ncc = 0, nkin = 0, npl = 0;
-  int cc[MAXP], kin[MAXP];
-  bool overflow = false;
-  if (!A.fixed[a]) {
-    const double xa = A.q[3 * a], ya = A.q[3 * a + 1], ra = A.r[a];
-    const int cx0 = (int)floor(A.B.mn[2 * a] / A.B.H) - 1;
-    const int cy0 = (int)floor(A.B.mn[2 * a + 1] / A.B.H) - 1;
-    const int cx1 = (int)floor(A.B.mx[2 * a] / A.B.H);
-    const int cy1 = (int)floor(A.B.mx[2 * a + 1] / A.B.H);
-    for (int cy = cy0; cy <= cy1; ++cy)
-      for (int cx = cx0; cx <= cx1; ++cx) {
-        const uint32_t bk = cell_hash(cx, cy, A.B.mask);
-        const int s = A.bucket_start[bk], e = s + A.bucket_count[bk];
-        for (int k = s; k < e; ++k) {
-          const int b = A.items[k];
-          if (b == a) continue;
-          const int2 hb = A.home[b];
-          if (hb.x != cx || hb.y != cy) continue; // bucket shared by another cell
-          const bool bf = A.fixed[b] != 0;
-          if (!(b > a || bf)) continue;
-          if (!box_overlap(A.B, a, b)) continue;
-          // ballBallCCDCollisionHappens with q0 == q1: active iff c0 <= 0
-          const double dx = xa - A.q[3 * b], dy = ya - A.q[3 * b + 1];
-          const double rb = A.r[b];
-          const double c0 = (dx * dx + dy * dy) - (ra + rb) * (ra + rb);
-          if (!(c0 <= 0.0)) continue;
-          if (!bf) {
-            if (ncc < MAXP) cc[ncc++] = b;
-            else overflow = true;
-          } else {
-            if (nkin < MAXP) kin[nkin++] = b;
-            else overflow = true;
-          }
-        }
-      }
-    // StaticPlaneCircleConstraint::isActive (StaticPlaneCircleConstraint.cpp:12-17)
-    for (int k = 0; k < A.nplanes; ++k) {
-      const double d = A.pn[k][0] * (xa - A.px[k][0]) + A.pn[k][1] * (ya - A.px[k][1]);
-      if (d <= ra) ++npl;
+// fixed body into the second slot). Fixed bodies emit none.
+//
+// A partner b overlapping a's AABB has its home cell within one cell of a's
+// (the cell width is at least every AABB's width), so the 3x3 cells around
+// a's home cell hold every candidate. The FP32 filter passes b when the
+// centres lie within ra + rb (plus slack) of each other; the offsets are
+// exact to about 1e-7 of a cell and the slack is 1e-4 of a cell, so every
+// pair that is a contact in FP64 passes. The survivors take the reference's
+// FP64 tests: AABB overlap (SpatialGrid.cpp:14-19, with the AABB corners
+// x -+ r evaluated as CircleGeometry.cpp:22-30 does) and
+// ballBallCCDCollisionHappens with q0 == q1 (active iff c0 <= 0).
+template <class F>
+__device__ __forceinline__ void for_each_partner(const PairArgs &A, int a, F &&found) {
+  const float4 pa = A.rec[2 * a], ca = A.rec[2 * a + 1];
+  const int2 ha = make_int2(__float_as_int(ca.x), __float_as_int(ca.y));
+  const double xa = A.q[3 * a], ya = A.q[3 * a + 1], ra = A.r[a];
+  // the nine bucket ranges first: independent loads instead of a chain
+  int bs[9], be[9];
+#pragma unroll
+  for (int c = 0; c < 9; ++c) {
+    const uint32_t bk = cell_hash(ha.x + c % 3 - 1, ha.y + c / 3 - 1, A.mask);
+    be[c] = A.bucket_end[bk];
+    bs[c] = be[c] - A.bucket_count[bk];
+  }
+#pragma unroll
+  for (int c = 0; c < 9; ++c) {
+    const int dx = c % 3 - 1, dy = c / 3 - 1;
+    const int cx = ha.x + dx, cy = ha.y + dy;
+    for (int k = bs[c]; k < be[c]; ++k) {
+      const int b = A.items[k];
+      if (b == a) continue;
+      const float4 pb = A.rec[2 * b], cb = A.rec[2 * b + 1];
+      if (__float_as_int(cb.x) != cx || __float_as_int(cb.y) != cy)
+        continue; // bucket shared by another cell
+      const bool bf = (__float_as_uint(pb.w) & REL_FIXED) != 0u;
+      if (!(b > a || bf)) continue;
+      const float reach = pa.z + pb.z + A.tol;
+      const float ex = (float)dx * A.Hf + (pb.x - pa.x);
+      const float ey = (float)dy * A.Hf + (pb.y - pa.y);
+      if (ex * ex + ey * ey > reach * reach) continue;
+      const double xb = A.q[3 * b], yb = A.q[3 * b + 1], rb = A.r[b];
+      if (!((xa + ra >= xb - rb && ya + ra >= yb - rb) &&
+            (xb + rb >= xa - ra && yb + rb >= ya - ra)))
+        continue;
+      const double ddx = xa - xb, ddy = ya - yb;
+      const double c0 = (ddx * ddx + ddy * ddy) - (ra + rb) * (ra + rb);
+      if (!(c0 <= 0.0)) continue;
+      found(b, bf);
     }
   }
-  if (overflow) atomicOr(A.status, (uint32_t)HG_STATUS_CELL_OVERFLOW);
-  if (!EMIT) {
-    A.cnt[a] = npl;
-    A.cnt[n + a] = ncc;
-    A.cnt[2 * n + a] = nkin;
-    return;
+}
+
+// Counting pass: per-kind counts, and the first PW partners in plist.
+__global__ void kd_pairs_count(PairArgs A) {
+  const int64_t n = A.n;
+  const int a = (int)(blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+  if (a >= n) return;
+  int ncc = 0, nkin = 0, npl = 0;
+  bool overflow = false;
+  const uint32_t flags = __float_as_uint(A.rec[2 * a].w);
+  if (!(flags & REL_FIXED)) {
+    uint32_t *lst = A.plist + (int64_t)a * PW;
+    for_each_partner(A, a, [&](int b, bool bf) {
+      int &c = bf ? nkin : ncc;
+      if (c >= MAXP) {
+        overflow = true;
+        return;
+      }
+      const int t = ncc + nkin;
+      if (t < PW) lst[t] = (uint32_t)b | (bf ? 0x80000000u : 0u);
+      ++c;
+    });
+    npl = __popc(flags >> 1);
   }
+  if (overflow) atomicOr(A.status, (uint32_t)HG_STATUS_CELL_OVERFLOW);
+  A.cnt[a] = npl;
+  A.cnt[n + a] = ncc;
+  A.cnt[2 * n + a] = nkin;
+}
+
+// Emission pass: sorted per-body contact keys at the scanned offsets. Lists
+// of at most PW partners come from the counting pass; longer ones are
+// searched again (the same partners, the first MAXP of each kind).
+__global__ void kd_pairs_emit(PairArgs A) {
+  const int64_t n = A.n;
+  const int a = (int)(blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+  if (a >= n) return;
+  const int npl = A.cnt[a], ncc = A.cnt[n + a], nkin = A.cnt[2 * n + a];
   if (npl + ncc + nkin == 0 || *A.overflow) return;
-  sort_small(cc, ncc);
-  sort_small(kin, nkin);
   const int64_t o0 = A.off[a], o1 = A.off[n + a], o2 = A.off[2 * n + a];
   if (o0 + npl > A.ccap || o1 + ncc > A.ccap || o2 + nkin > A.ccap) {
     atomicOr(A.status, (uint32_t)HG_STATUS_CONTACT_OVERFLOW);
     return;
   }
-  const double xa = A.q[3 * a], ya = A.q[3 * a + 1], ra = A.r[a];
+  const uint32_t flags = __float_as_uint(A.rec[2 * a].w);
   int j = 0;
-  for (int k = 0; k < A.nplanes; ++k) {
-    const double d = A.pn[k][0] * (xa - A.px[k][0]) + A.pn[k][1] * (ya - A.px[k][1]);
-    if (d <= ra) A.keys[o0 + j++] = ckey(K_PLANE, (int)a, k);
+  for (int k = 0; k < A.nplanes; ++k)
+    if (flags & (REL_PLANE0 << k)) A.keys[o0 + j++] = ckey(K_PLANE, a, k);
+  if (ncc + nkin <= PW) {
+    // odd-even transposition sort of the flagged indices: circle-circle
+    // partners ascending, then the fixed ones ascending
+    uint32_t L[PW];
+    const uint32_t *lst = A.plist + (int64_t)a * PW;
+#pragma unroll
+    for (int k = 0; k < PW; ++k) L[k] = k < ncc + nkin ? lst[k] : 0xFFFFFFFFu;
+#pragma unroll
+    for (int p = 0; p < PW; ++p)
+#pragma unroll
+      for (int i = p & 1; i + 1 < PW; i += 2) {
+        const uint32_t lo = min(L[i], L[i + 1]), hi = max(L[i], L[i + 1]);
+        L[i] = lo;
+        L[i + 1] = hi;
+      }
+#pragma unroll
+    for (int k = 0; k < PW; ++k) {
+      if (k < ncc) A.keys[o1 + k] = ckey(K_CC, a, (int)L[k]);
+      else if (k < ncc + nkin) A.keys[o2 + (k - ncc)] = ckey(K_KIN, a, (int)(L[k] & 0x7FFFFFFFu));
+    }
+    return;
   }
-  for (int k = 0; k < ncc; ++k) A.keys[o1 + k] = ckey(K_CC, (int)a, cc[k]);
-  for (int k = 0; k < nkin; ++k) A.keys[o2 + k] = ckey(K_KIN, (int)a, kin[k]);
+  int cc[MAXP], kin[MAXP];
+  int mc = 0, mk = 0;
+  for_each_partner(A, a, [&](int b, bool bf) {
+    if (bf) {
+      if (mk < MAXP) kin[mk++] = b;
+    } else if (mc < MAXP) {
+      cc[mc++] = b;
+    }
+  });
+  sort_small(cc, mc);
+  sort_small(kin, mk);
+  for (int k = 0; k < mc; ++k) A.keys[o1 + k] = ckey(K_CC, a, cc[k]);
+  for (int k = 0; k < mk; ++k) A.keys[o2 + k] = ckey(K_KIN, a, kin[k]);
 }
 
 // Capacity guard between the counting and the emission pass: when the total
@@ -395,16 +536,18 @@ __global__ void kd_in_fill(int64_t n, const int32_t *__restrict__ off,
 }
 
 __global__ void kd_integrate(int64_t n, double dt, double gx, double gy, double *q, double *v,
-                             const double *__restrict__ m0, const double *__restrict__ I0,
-                             const double *__restrict__ w, const uint8_t *__restrict__ fixed,
+                             const double *__restrict__ m0, const double *__restrict__ w,
+                             const double *__restrict__ inv_mass,
+                             const uint8_t *__restrict__ fixed,
                              const int32_t *__restrict__ cnt, const int32_t *__restrict__ off,
                              const double *__restrict__ rec, const int32_t *__restrict__ in_count,
                              const int32_t *__restrict__ in_off, int32_t *in_list,
-                             double *F_out, uint32_t *status) {
+                             uint32_t *status) {
   const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (j >= n) return;
-  // RigidBody2DState::updateCurrentMassUsingMassWeights
-  const double M = m0[j] * w[j], Mi = I0[j] * w[j];
+  // RigidBody2DState::updateCurrentMassUsingMassWeights; 1 / M and 1 / Mi
+  // come from kd_inverse_masses
+  const double M = m0[j] * w[j];
   double Fx = 0.0 + M * gx, Fy = 0.0 + M * gy, T = 0.0;
   auto total = [&](int64_t k, D2 &f) {
     const double *r = rec + k * RW;
@@ -457,15 +600,11 @@ __global__ void kd_integrate(int64_t n, double dt, double gx, double gy, double 
     T += dcross(D2{rec[k * RW + 10], rec[k * RW + 11]}, f);
   }
   if (fixed[j]) Fx = Fy = T = 0.0;
-  if (F_out) {
-    F_out[3 * j] = Fx;
-    F_out[3 * j + 1] = Fy;
-    F_out[3 * j + 2] = T;
-  }
   // v1 = v0 + dt Minv F ; q1 = q0 + dt v1
-  const double v0 = v[3 * j] + (dt * (1.0 / M)) * Fx;
-  const double v1 = v[3 * j + 1] + (dt * (1.0 / M)) * Fy;
-  const double v2 = v[3 * j + 2] + (dt * (1.0 / Mi)) * T;
+  const double im = inv_mass[2 * j], iI = inv_mass[2 * j + 1];
+  const double v0 = v[3 * j] + (dt * im) * Fx;
+  const double v1 = v[3 * j + 1] + (dt * im) * Fy;
+  const double v2 = v[3 * j + 2] + (dt * iI) * T;
   v[3 * j] = v0;
   v[3 * j + 1] = v1;
   v[3 * j + 2] = v2;
@@ -473,20 +612,8 @@ __global__ void kd_integrate(int64_t n, double dt, double gx, double gy, double 
   q[3 * j] = q0;
   q[3 * j + 1] = q1;
   q[3 * j + 2] = q2;
-  if (!isfinite(q0) || !isfinite(q1) || !isfinite(v0) || !isfinite(v1))
+  if (!finite_bits(q0) || !finite_bits(q1) || !finite_bits(v0) || !finite_bits(v1))
     atomicOr(status, (uint32_t)HG_STATUS_NONFINITE);
-}
-
-__global__ void kd_aabbs(int64_t n, const double *__restrict__ q, const double *__restrict__ r,
-                         double *mn, double *mx) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  // CircleGeometry::computeCollisionAABB (CircleGeometry.cpp:22-30), q0 == q1
-  const double x = q[3 * i], y = q[3 * i + 1], ri = r[i];
-  mn[2 * i] = x - ri;
-  mn[2 * i + 1] = y - ri;
-  mx[2 * i] = x + ri;
-  mx[2 * i + 1] = y + ri;
 }
 
 // Candidate pairs of explicit boxes (SpatialGrid::getPotentialOverlaps).
@@ -569,10 +696,10 @@ hg_status dem_alloc(hg_dem *d) {
   hg_status st;
   if ((st = d->status.alloc(1)) || (st = d->q.alloc(3 * N)) || (st = d->v.alloc(3 * N)) ||
       (st = d->r.alloc(N)) || (st = d->m0.alloc(N)) || (st = d->I0.alloc(N)) ||
-      (st = d->w.alloc(N)) || (st = d->F.alloc(3 * N)) || (st = d->fixed.alloc(N)) ||
-      (st = d->aabb_mn.alloc(2 * N)) || (st = d->aabb_mx.alloc(2 * N)) ||
-      (st = d->home.alloc(N)) || (st = d->bcount.alloc(T)) || (st = d->bstart.alloc(T)) ||
-      (st = d->bcursor.alloc(T)) || (st = d->items.alloc(N)) || (st = d->scan_tmp.alloc(tmp)) ||
+      (st = d->w.alloc(N)) || (st = d->minv.alloc(2 * N)) || (st = d->fixed.alloc(N)) ||
+      (st = d->brec.alloc(2 * N)) || (st = d->plist.alloc(PW * N)) ||
+      (st = d->bcount.alloc(T)) || (st = d->bstart.alloc(T)) ||
+      (st = d->items.alloc(N)) || (st = d->scan_tmp.alloc(tmp)) ||
       (st = d->c_count.alloc(2)) || (st = d->per_body.alloc(3 * N + 1)) ||
       (st = d->per_body_off.alloc(3 * N + 1)) || (st = d->ckey[0].alloc(C)) ||
       (st = d->ckey[1].alloc(C)) || (st = d->crec[0].alloc(C * RW)) ||
@@ -593,38 +720,63 @@ hg_status dem_reset_history(hg_dem *d) {
   return HG_OK;
 }
 
+hg_status dem_prepare(hg_dem *d) {
+  if (d->inv_valid || d->n == 0) return HG_OK;
+  HG_LAUNCH(kd_inverse_masses, blocks_for(d->n, 256), 256, 0, d->ctx->stream, d->n, d->m0.p,
+            d->I0.p, d->w.p, d->minv.p);
+  HG_CHECK_LAUNCH();
+  d->inv_valid = true;
+  return HG_OK;
+}
+
 hg_status dem_step(hg_dem *d, double dt, int weighted) {
   cudaStream_t s = d->ctx->stream;
   const int64_t n = d->n;
   if (n == 0) return HG_OK;
   hg_status st;
-  HG_LAUNCH(kd_aabbs, blocks_for(n, 256), 256, 0, s, n, d->q.p, d->r.p, d->aabb_mn.p,
-            d->aabb_mx.p);
-  HG_CHECK_LAUNCH();
-  BroadArgs B;
-  B.n = n;
-  B.H = d->cell_h;
-  B.mask = d->mask;
-  B.mn = d->aabb_mn.p;
-  B.mx = d->aabb_mx.p;
-  if ((st = build_buckets(s, B, d->bcount.p, d->bstart.p, d->bcursor.p, d->items.p, d->home.p,
-                          d->scan_tmp.p)))
-    return st;
+  if ((st = dem_prepare(d))) return st;
+  // the hash table grows with the live body count (at most the capacity's)
+  const uint32_t mask = (1u << table_bits(n)) - 1u;
+  {
+    // hash-grid counting sort of the bodies by home cell
+    const int64_t T = (int64_t)mask + 1;
+    HG_CUDA_TRY(cudaMemsetAsync(d->bcount.p, 0, sizeof(int32_t) * T, s));
+    HomeArgs H;
+    H.n = n;
+    H.H = d->cell_h;
+    H.invH = 1.0 / d->cell_h;
+    H.mask = mask;
+    H.nplanes = d->p.nplanes;
+    for (int k = 0; k < HG_MAX_PLANES; ++k)
+      for (int c = 0; c < 2; ++c) {
+        H.px[k][c] = d->p.px[k][c];
+        H.pn[k][c] = d->p.pn[k][c];
+      }
+    H.q = d->q.p;
+    H.r = d->r.p;
+    H.fixed = d->fixed.p;
+    H.rec = d->brec.p;
+    H.bucket_count = d->bcount.p;
+    HG_LAUNCH(kd_bodies_home, blocks_for(n, 256), 256, 0, s, H);
+    HG_CHECK_LAUNCH();
+    if ((st = exclusive_scan_i32(d->bcount.p, d->bstart.p, T, d->scan_tmp.p, s))) return st;
+    HG_LAUNCH(kd_fill_ends, blocks_for(n, 256), 256, 0, s, n, mask, d->brec.p, d->bstart.p,
+              d->items.p);
+    HG_CHECK_LAUNCH();
+  }
   PairArgs A;
-  A.B = B;
-  A.home = d->home.p;
-  A.bucket_start = d->bstart.p;
+  A.n = n;
+  A.mask = mask;
+  A.rec = d->brec.p;
+  A.Hf = (float)d->cell_h;
+  A.tol = (float)(1.0e-4 * d->cell_h);
+  A.plist = d->plist.p;
+  A.bucket_end = d->bstart.p;
   A.bucket_count = d->bcount.p;
   A.items = d->items.p;
   A.q = d->q.p;
   A.r = d->r.p;
-  A.fixed = d->fixed.p;
   A.nplanes = d->p.nplanes;
-  for (int k = 0; k < HG_MAX_PLANES; ++k)
-    for (int c = 0; c < 2; ++c) {
-      A.px[k][c] = d->p.px[k][c];
-      A.pn[k][c] = d->p.pn[k][c];
-    }
   A.cnt = d->per_body.p;
   A.off = d->per_body_off.p;
   const int nb = 1 - d->cc; // buffer receiving this step's contacts
@@ -632,8 +784,8 @@ hg_status dem_step(hg_dem *d, double dt, int weighted) {
   A.ccap = d->ccap;
   A.overflow = d->overflow.p;
   A.status = d->status.p;
-  HG_CUDA_TRY(cudaMemsetAsync(d->per_body.p, 0, sizeof(int32_t) * (3 * n + 1), s));
-  HG_LAUNCH(kd_pairs<false>, blocks_for(n, 128), 128, 0, s, A);
+  HG_CUDA_TRY(cudaMemsetAsync(d->per_body.p + 3 * n, 0, sizeof(int32_t), s));
+  HG_LAUNCH(kd_pairs_count, blocks_for(n, 128), 128, 0, s, A);
   HG_CHECK_LAUNCH();
   if ((st = exclusive_scan_i32(d->per_body.p, d->per_body_off.p, 3 * n + 1, d->scan_tmp.p, s)))
     return st;
@@ -643,7 +795,7 @@ hg_status dem_step(hg_dem *d, double dt, int weighted) {
   HG_LAUNCH(kd_drop_if_overflow, blocks_for(3 * n + 1, 256), 256, 0, s, n, d->overflow.p,
             d->per_body.p, d->per_body_off.p);
   HG_CHECK_LAUNCH();
-  HG_LAUNCH(kd_pairs<true>, blocks_for(n, 128), 128, 0, s, A);
+  HG_LAUNCH(kd_pairs_emit, blocks_for(n, 128), 128, 0, s, A);
   HG_CHECK_LAUNCH();
   HG_CUDA_TRY(cudaMemcpyAsync(d->c_count.p + nb, d->per_body_off.p + 3 * n, sizeof(int32_t),
                               cudaMemcpyDeviceToDevice, s));
@@ -685,8 +837,8 @@ hg_status dem_step(hg_dem *d, double dt, int weighted) {
             d->in_off.p, d->in_cursor.p, d->in_list.p);
   HG_CHECK_LAUNCH();
   HG_LAUNCH(kd_integrate, blocks_for(n, 128), 128, 0, s, n, dt, d->p.g[0], d->p.g[1], d->q.p,
-            d->v.p, d->m0.p, d->I0.p, d->w.p, d->fixed.p, d->per_body.p, d->per_body_off.p,
-            d->crec[nb].p, d->in_count.p, d->in_off.p, d->in_list.p, d->F.p, d->status.p);
+            d->v.p, d->m0.p, d->w.p, d->minv.p, d->fixed.p, d->per_body.p, d->per_body_off.p,
+            d->crec[nb].p, d->in_count.p, d->in_off.p, d->in_list.p, d->status.p);
   HG_CHECK_LAUNCH();
   d->cc = nb;
   d->history_valid = true;
@@ -857,6 +1009,7 @@ hg_status dem_edit(hg_dem *d, int64_t n_old, const int32_t *map_host, int64_t n_
     HG_CHECK_LAUNCH();
   }
   d->n = n_keep + n_add;
+  d->inv_valid = false;
   return HG_OK;
 }
 

@@ -297,14 +297,17 @@ struct hg_dem {
   int64_t cap = 0, ccap = 0, n = 0;
   hg::DevBuf<uint32_t> status;
   // bodies
-  hg::DevBuf<double> q, v, r, m0, I0, w, minv, mass, F;
+  hg::DevBuf<double> q, v, r, m0, I0, w;
+  hg::DevBuf<double> minv; // 1 / (m0 w), 1 / (I0 w) per body
+  bool inv_valid = false;  // minv matches m0, I0 and w
   hg::DevBuf<uint8_t> fixed;
   // broadphase: hash grid of cell width H over the AABB minima
   double cell_h = 0.0;
-  uint32_t mask = 0; // hash table size - 1
-  hg::DevBuf<double> aabb_mn, aabb_mx;
-  hg::DevBuf<int2> home;
-  hg::DevBuf<int32_t> bcount, bstart, bcursor, items;
+  uint32_t mask = 0; // hash table size - 1 at the capacity
+  // per body, 32 bytes: FP32 offset from the home cell, radius, flags; home cell
+  hg::DevBuf<float4> brec;
+  hg::DevBuf<uint32_t> plist;  // partners kept by the counting pass
+  hg::DevBuf<int32_t> bcount, bstart, items; // bstart holds bucket ends after the fill
   hg::DevBuf<int32_t> scan_tmp;
   // contacts: current and previous, sorted by (kind, first, second)
   hg::DevBuf<int32_t> c_count; // contacts in ckey[0], ckey[1] (device)
@@ -338,6 +341,9 @@ hg_status dem_edit(hg_dem *d, int64_t n_old, const int32_t *old_to_new, int64_t 
                    int64_t n_add, const double *q, const double *v, const double *r,
                    const double *m, const double *I, const uint8_t *fixed);
 hg_status dem_step(hg_dem *d, double dt, int weighted);
+// per-body data that dem_step needs and that only changes with the bodies
+// (inverse masses); called before a step is captured into a graph
+hg_status dem_prepare(hg_dem *d);
 hg_status dem_download_contacts(hg_dem *d, int64_t cap, double *rec,
                                 int64_t *count);
 hg_status dem_candidate_pairs(hg_context *ctx, int64_t n, const double *mn,
