@@ -388,6 +388,25 @@ def run_dem(args, ctx):
     gpu_rate = n * args.dem_steps / (ms * 1e-3)
     # per disk-step 128 B, per contact 40 B (FP64 figures of the scope table)
     alg = n * 128 + contacts * 40
+    large = None
+    if args.dem_large_disks > 0:
+        # the same lattice at a size where the step is no longer launch-bound
+        nl = args.dem_large_disks
+        sl = scenes.dem_column(n=nl, per_row=1000)
+        dl = hg.DEM(ctx, scenes.GRAVITY, dp["kn"], dp["kt"], dp["gamman"], dp["gammat"],
+                    dp["mu"], planes, capacity=nl, contact_capacity=4 * nl)
+        dl.upload(sl["q"], sl["v"], sl["r"], sl["m"], sl["I"], sl["fixed"])
+        dl.flow(1.0e-5, 200)
+        ctx.synchronize()
+        ctx.timer_begin()
+        dl.flow(1.0e-5, args.dem_large_steps)
+        msl = ctx.timer_end()
+        large = {"workload": "%d disks, the same lattice 1000 per row, dt 1e-5 s" % nl,
+                 "disk_steps_per_s": nl * args.dem_large_steps / (msl * 1e-3),
+                 "us_per_step": 1e3 * msl / args.dem_large_steps,
+                 "steps": args.dem_large_steps, "contacts": dl.num_contacts(),
+                 "status": dl.status()}
+        dl.close()
     return {"workload": "DEM column: 10,000 disks, hex pitch 2.2 mm, r U[0.9,1.1] mm, dt 1e-6 s, "
                         "FP64 penalty contacts with friction history",
             "disk_steps_per_s": gpu_rate, "us_per_step": 1e3 * ms / args.dem_steps,
@@ -397,7 +416,8 @@ def run_dem(args, ctx):
             "achieved_gbs": alg / (ms * 1e-3 / args.dem_steps) / 1e9,
             "cpu_baseline": {"value": n * csteps / cs, "unit": "disk-steps/s", "cores": 1,
                              "kind": "port", "sample": "%d steps of the same column (%.1f s)" %
-                             (csteps, cs)}}
+                             (csteps, cs)},
+            "large": large}
 
 
 def run_hybrid(args, ctx):
@@ -506,6 +526,8 @@ def main():
     ap.add_argument("--dem-steps", type=int, default=2000)
     ap.add_argument("--hybrid-steps", type=int, default=1000)
     ap.add_argument("--dem-cpu-steps", type=int, default=200)
+    ap.add_argument("--dem-large-disks", type=int, default=1000000)
+    ap.add_argument("--dem-large-steps", type=int, default=200)
     ap.add_argument("--serve-requests", type=int, default=256)
     ap.add_argument("--serve-rate", type=float, default=50.0)
     ap.add_argument("--serve-steps", type=int, default=2000)

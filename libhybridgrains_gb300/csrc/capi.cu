@@ -488,6 +488,8 @@ hg_status hg_mpm_destroy(hg_mpm *m) {
     // read-back slot goes back to the context's pool for later work
     context_return_pair(ctx, m->h_outside);
     if (m->outside_ev) cudaEventDestroy(m->outside_ev);
+    for (cudaGraphExec_t &e : m->chunk_exec)
+      if (e) cudaGraphExecDestroy(e);
     for (cudaEvent_t e : m->prof_events) cudaEventDestroy(e);
     delete m;
   }

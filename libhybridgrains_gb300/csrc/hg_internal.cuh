@@ -197,6 +197,12 @@ struct hg_mpm {
   int64_t steps_since_rebin = 0;
   int64_t rebins = 0;
   bool primed = false;
+  // CHUNK_STEPS steps captured as a CUDA graph, one per live buffer; rebuilt
+  // when dt or the point count changes
+  cudaGraphExec_t chunk_exec[2] = {nullptr, nullptr};
+  double chunk_dt[2] = {0.0, 0.0};
+  int64_t chunk_n[2] = {-1, -1};
+  int64_t chunk_launches = 0;
   // per-kernel event timing (hg_mpm_profile)
   bool profile = false;
   std::vector<cudaEvent_t> prof_events; // 3 per recorded step
@@ -264,6 +270,12 @@ struct hg_batch {
   cudaEvent_t out_ev = nullptr;
   bool out_pending = false;
   std::vector<hg_mpm *> out_members; // members whose counters are in flight
+  // CHUNK_STEPS steps of all members captured as a CUDA graph (kernels read
+  // the argument table through a fixed pointer, so only the member count
+  // keys it)
+  cudaGraphExec_t chunk_exec = nullptr;
+  int chunk_members = -1;
+  int64_t chunk_launches = 0;
   int64_t member_steps = 0, resorts = 0, steps = 0;
   double host_ms = 0.0, wait_ms = 0.0; // wait: host blocked on the device
   bool profile = false;

@@ -1262,6 +1262,69 @@ hg_status mixed_profile_read(hg_mpm *m, double *g2p2g_ms, double *update_ms, int
   return HG_OK;
 }
 
+// Steps per captured chunk. Re-sort decisions are taken between chunks; the
+// cadence only affects speed (points outside their window stay exact), and
+// at a CFL number below 1 no point crosses a tile within a chunk.
+constexpr int CHUNK_STEPS = 16;
+
+// Ends a capture begun on s, restoring the launch counter that the captured
+// launches advanced; instantiates the graph into *exec and returns the
+// number of kernel launches one replay performs.
+hg_status end_chunk_capture(cudaStream_t s, hg_status st, int64_t l0, cudaGraphExec_t *exec,
+                            int64_t *launches) {
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(s, &graph);
+  *launches = g_launches.load() - l0;
+  g_launches.fetch_sub(*launches, std::memory_order_relaxed);
+  if (st != HG_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return st;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+  const cudaError_t ei = cudaGraphInstantiate(exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ei != cudaSuccess) {
+    *exec = nullptr;
+    return cuda_fail(ei, "cudaGraphInstantiate");
+  }
+  return HG_OK;
+}
+
+// The graph of CHUNK_STEPS steps of one scene for its live buffer: the two
+// kernels per step, then the read-back of the out-of-window counters.
+hg_status mixed_chunk_graph(hg_mpm *m, double dt) {
+  const int c = m->cur;
+  if (m->chunk_exec[c] && m->chunk_dt[c] == dt && m->chunk_n[c] == m->n) return HG_OK;
+  if (m->chunk_exec[c]) {
+    cudaGraphExecDestroy(m->chunk_exec[c]);
+    m->chunk_exec[c] = nullptr;
+  }
+  cudaStream_t s = m->ctx->stream;
+  const size_t smem = fused_smem_bytes();
+  const MixedArgs At = make_args(m, dt, true), Ab = make_args(m, dt, false);
+  const int64_t l0 = g_launches.load();
+  HG_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  hg_status st = HG_OK;
+  for (int k = 0; k < CHUNK_STEPS && st == HG_OK; ++k) {
+    HG_LAUNCH(kx_grid_update, update_blocks(m), THREADS, 0, s, At);
+    HG_LAUNCH(kx_g2p2g<false>, fused_blocks(m), THREADS, smem, s, Ab);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) st = cuda_fail(e, "kernel launch");
+  }
+  if (st == HG_OK) {
+    const cudaError_t e = cudaMemcpyAsync(m->h_outside, m->outside.p, 2 * sizeof(uint32_t),
+                                          cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) st = cuda_fail(e, "cudaMemcpyAsync");
+  }
+  int64_t launches = 0;
+  st = end_chunk_capture(s, st, l0, &m->chunk_exec[c], &launches);
+  if (st != HG_OK) return st;
+  m->chunk_dt[c] = dt;
+  m->chunk_n[c] = m->n;
+  m->chunk_launches = launches;
+  return HG_OK;
+}
+
 hg_status mixed_step(hg_mpm *m, double dt, int nsteps) {
   cudaStream_t s = m->ctx->stream;
   if (!m->primed) {
@@ -1269,7 +1332,29 @@ hg_status mixed_step(hg_mpm *m, double dt, int nsteps) {
     if (st != HG_OK) return st;
   }
   const size_t smem = fused_smem_bytes();
-  for (int k = 0; k < nsteps; ++k) {
+  int k = 0;
+  // whole chunks replay a captured graph (one launch for 2 x CHUNK_STEPS
+  // kernels); event timing needs the per-step path
+  while (!m->profile && nsteps - k >= CHUNK_STEPS) {
+    bool need = m->steps_since_rebin >= MAX_STEPS_BETWEEN_REBINS;
+    if (!need && m->outside_pending && cudaEventQuery(m->outside_ev) == cudaSuccess) {
+      m->outside_pending = false;
+      need = m->h_outside[0] > 0 || (int64_t)m->h_outside[1] * 32 > m->n;
+    }
+    if (need) {
+      hg_status st = rebin(m);
+      if (st != HG_OK) return st;
+    }
+    hg_status st = mixed_chunk_graph(m, dt);
+    if (st != HG_OK) return st;
+    HG_CUDA_TRY(cudaGraphLaunch(m->chunk_exec[m->cur], s));
+    g_launches.fetch_add(m->chunk_launches, std::memory_order_relaxed);
+    HG_CUDA_TRY(cudaEventRecord(m->outside_ev, s));
+    m->outside_pending = true;
+    m->steps_since_rebin += CHUNK_STEPS;
+    k += CHUNK_STEPS;
+  }
+  for (; k < nsteps; ++k) {
     bool need = m->steps_since_rebin >= MAX_STEPS_BETWEEN_REBINS;
     if (!need && m->outside_pending && cudaEventQuery(m->outside_ev) == cudaSuccess) {
       m->outside_pending = false;
@@ -1345,6 +1430,7 @@ void batch_free(hg_batch *b) {
   }
   if (b->h_outside) cudaFreeHost(b->h_outside);
   if (b->out_ev) cudaEventDestroy(b->out_ev);
+  if (b->chunk_exec) cudaGraphExecDestroy(b->chunk_exec);
   for (cudaEvent_t e : b->prof_events) cudaEventDestroy(e);
 }
 
@@ -1363,6 +1449,43 @@ hg_status batch_profile_read(hg_batch *b, double *ms, int64_t *steps) {
   return HG_OK;
 }
 
+// The graph of CHUNK_STEPS steps of all S members: the two batched kernels
+// per step, then the gather and read-back of the out-of-window counters.
+hg_status batch_chunk_graph(hg_batch *b, int S) {
+  if (b->chunk_exec && b->chunk_members == S) return HG_OK;
+  if (b->chunk_exec) {
+    cudaGraphExecDestroy(b->chunk_exec);
+    b->chunk_exec = nullptr;
+  }
+  cudaStream_t s = b->ctx->stream;
+  const MixedArgs *dt = reinterpret_cast<const MixedArgs *>(b->table.p);
+  const MixedArgs *db = dt + S;
+  const int nsm = b->ctx->num_sms;
+  const int64_t l0 = g_launches.load();
+  HG_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  hg_status st = HG_OK;
+  for (int k = 0; k < CHUNK_STEPS && st == HG_OK; ++k) {
+    HG_LAUNCH(kb_grid_update, nsm * 8, THREADS, 0, s, dt, S);
+    HG_LAUNCH(kb_g2p2g, nsm * 3, THREADS, 0, s, db, S);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) st = cuda_fail(e, "kernel launch");
+  }
+  if (st == HG_OK) {
+    HG_LAUNCH(kb_gather_outside, (S + 127) / 128, 128, 0, s, db, S, b->outside.p);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(b->h_outside, b->outside.p, 2 * sizeof(uint32_t) * S,
+                          cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) st = cuda_fail(e, "chunk capture");
+  }
+  int64_t launches = 0;
+  st = end_chunk_capture(s, st, l0, &b->chunk_exec, &launches);
+  if (st != HG_OK) return st;
+  b->chunk_members = S;
+  b->chunk_launches = launches;
+  return HG_OK;
+}
+
 hg_status batch_step(hg_batch *b, int nsteps) {
   cudaStream_t s = b->ctx->stream;
   const int S = (int)b->members.size();
@@ -1372,10 +1495,11 @@ hg_status batch_step(hg_batch *b, int nsteps) {
     b->sigs.assign(S, hg_batch::Sig{});
     b->dirty = true;
   }
-  for (int k = 0; k < nsteps; ++k) {
-    // re-sort members whose points left their windows (counters read back
-    // asynchronously one step late), members due for a periodic re-sort and
-    // members not yet primed
+  // Host work ahead of a step (or of a captured chunk of steps): re-sort
+  // members whose points left their windows (counters read back
+  // asynchronously), members due for a periodic re-sort and members not yet
+  // primed; then bring the argument table up to date.
+  auto prepare = [&](cudaEvent_t ev1, cudaEvent_t ev2) -> hg_status {
     if (b->out_pending && cudaEventQuery(b->out_ev) == cudaSuccess) {
       b->out_pending = false;
       for (size_t i = 0; i < b->out_members.size(); ++i) {
@@ -1384,17 +1508,6 @@ hg_status batch_step(hg_batch *b, int nsteps) {
         if (b->h_outside[2 * i] > 0 || (int64_t)b->h_outside[2 * i + 1] * 32 > m->n)
           m->steps_since_rebin = MAX_STEPS_BETWEEN_REBINS;
       }
-    }
-    cudaEvent_t ev[hg_batch::PROF_PHASES + 1] = {};
-    if (b->profile) {
-      while (b->prof_events.size() < b->prof_used + hg_batch::PROF_PHASES + 1) {
-        cudaEvent_t e;
-        HG_CUDA_TRY(cudaEventCreate(&e));
-        b->prof_events.push_back(e);
-      }
-      for (int j = 0; j <= hg_batch::PROF_PHASES; ++j) ev[j] = b->prof_events[b->prof_used + j];
-      b->prof_used += hg_batch::PROF_PHASES + 1;
-      HG_CUDA_TRY(cudaEventRecord(ev[0], s));
     }
     b->due.clear();
     for (hg_mpm *m : b->members) {
@@ -1420,7 +1533,7 @@ hg_status batch_step(hg_batch *b, int nsteps) {
       HG_CUDA_TRY(cudaEventRecord(b->rtable_ev[rb], s));
       b->resorts += (int64_t)b->due.size();
     }
-    if (b->profile) HG_CUDA_TRY(cudaEventRecord(ev[1], s));
+    if (ev1) HG_CUDA_TRY(cudaEventRecord(ev1, s));
     // per-scene argument tables [update args of S scenes | fused args of S
     // scenes]; an entry changes when its scene re-sorts (buffer swap), is
     // re-uploaded or changes dt, and the table is copied only then
@@ -1448,7 +1561,39 @@ hg_status batch_step(hg_batch *b, int nsteps) {
       HG_CUDA_TRY(cudaEventRecord(b->table_ev[tb], s));
       b->dirty = false;
     }
-    if (b->profile) HG_CUDA_TRY(cudaEventRecord(ev[2], s));
+    if (ev2) HG_CUDA_TRY(cudaEventRecord(ev2, s));
+    return HG_OK;
+  };
+  int k = 0;
+  // whole chunks replay a captured graph; event timing needs the per-step path
+  while (!b->profile && nsteps - k >= CHUNK_STEPS) {
+    hg_status st = prepare(nullptr, nullptr);
+    if (st == HG_OK) st = batch_chunk_graph(b, S);
+    if (st != HG_OK) return st;
+    HG_CUDA_TRY(cudaGraphLaunch(b->chunk_exec, s));
+    g_launches.fetch_add(b->chunk_launches, std::memory_order_relaxed);
+    HG_CUDA_TRY(cudaEventRecord(b->out_ev, s));
+    b->out_members = b->members;
+    b->out_pending = true;
+    for (hg_mpm *m : b->members) m->steps_since_rebin += CHUNK_STEPS;
+    b->member_steps += (int64_t)S * CHUNK_STEPS;
+    b->steps += CHUNK_STEPS;
+    k += CHUNK_STEPS;
+  }
+  for (; k < nsteps; ++k) {
+    cudaEvent_t ev[hg_batch::PROF_PHASES + 1] = {};
+    if (b->profile) {
+      while (b->prof_events.size() < b->prof_used + hg_batch::PROF_PHASES + 1) {
+        cudaEvent_t e;
+        HG_CUDA_TRY(cudaEventCreate(&e));
+        b->prof_events.push_back(e);
+      }
+      for (int j = 0; j <= hg_batch::PROF_PHASES; ++j) ev[j] = b->prof_events[b->prof_used + j];
+      b->prof_used += hg_batch::PROF_PHASES + 1;
+      HG_CUDA_TRY(cudaEventRecord(ev[0], s));
+    }
+    hg_status st = prepare(ev[1], ev[2]);
+    if (st != HG_OK) return st;
     const MixedArgs *dt = reinterpret_cast<const MixedArgs *>(b->table.p);
     const MixedArgs *db = dt + S;
     const int nsm = b->ctx->num_sms;

@@ -155,7 +155,10 @@ def test_mixed_multi_step_tracks_oracle(ctx, cfg0):
 
 def test_mixed_fast_particles_resort(ctx):
     """Isolated points crossing several tiles: exercises the out-of-window
-    path and the re-sort; results follow the FP64 oracle."""
+    path and the re-sort, stepping both per step (calls of fewer steps than a
+    captured chunk, re-sort decisions every step) and through the graph of
+    captured chunks (decisions between chunks); results follow the FP64
+    oracle either way."""
     # no elastic stiffness: at 0.2 cells per step the elastic CFL limit of the
     # column material would be exceeded, so these points carry no stress
     cfg = scenes.mpm_column("column_12800", shear_modulus=0.0, bulk_modulus=0.0)
@@ -168,17 +171,22 @@ def test_mixed_fast_particles_resort(ctx):
     vol = np.full(n, 1e-6)
     hl = np.full(n, 1.25e-3)
     g = gpu_mpm(ctx, cfg, hg.MIXED)
+    gc = gpu_mpm(ctx, cfg, hg.MIXED)
     c = cpu_mpm(cfg)
     g.upload(q, v, m, vol, hl)
+    gc.upload(q, v, m, vol, hl)
     c.set_particles(q, v, m, vol, hl)
     dt = 5e-4  # 0.2 cells per step
-    g.flow(dt, 40)
+    for _ in range(5):
+        g.flow(dt, 8)
+    gc.flow(dt, 40)
     c.step(dt, 40)
-    P, Q = g.download(), c.particles()
-    # FP32 velocities integrated over 40 steps of 0.2 cells each
-    assert np.abs(P["q"] - Q["q"]).max() <= 2e-8
+    Q = c.particles()
+    for x in (g, gc):
+        # FP32 velocities integrated over 40 steps of 0.2 cells each
+        assert np.abs(x.download()["q"] - Q["q"]).max() <= 2e-8
+        assert x.status() == 0
     assert g.rebin_count() >= 2
-    assert g.status() == 0
 
 
 @pytest.mark.parametrize("precision", [0, 1])
