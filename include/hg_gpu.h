@@ -254,6 +254,43 @@ hg_status hg_batch_profile(hg_batch *b, int32_t enable);
 hg_status hg_batch_profile_read(hg_batch *b, double *resort_ms, double *table_ms,
                                 double *update_ms, double *fused_ms, int64_t *steps);
 
+/* ---- launch-shape autotuning (no reference counterpart) -------------------
+ * The MIXED kernels run as grids of CTAs that walk the active tiles (single
+ * scene) or contiguous shares of the (scene, tile) items (batch). A launch
+ * shape gives the CTAs per SM of the fused G2P/P2G kernel and of the grid
+ * update; 0 keeps the built-in choice (3 and 8). The autotuner times
+ * HG_TUNE_CANDIDATES shapes on the live object with CUDA events, each for
+ * steps_per_candidate steps (the scene advances by all of them: a shape only
+ * changes the order of FP32 atomic sums), keeps the fastest for each kernel,
+ * and records the result in a process-wide table under the object's size
+ * class: the device's SM count, the tile count (single scenes) and the point
+ * count, both rounded up to powers of two. MIXED objects and batches look up
+ * their class before their first step. The table can be saved to and merged
+ * from a text file. */
+enum { HG_TUNE_CANDIDATES = 4 };
+typedef struct hg_launch_shape {
+  int32_t fused_ctas_per_sm;
+  int32_t update_ctas_per_sm;
+} hg_launch_shape;
+typedef struct hg_tune_report {
+  int32_t candidates;
+  hg_launch_shape tried[HG_TUNE_CANDIDATES];
+  double fused_ms[HG_TUNE_CANDIDATES];  /* mean per step */
+  double update_ms[HG_TUNE_CANDIDATES]; /* mean per step */
+  hg_launch_shape chosen;
+} hg_tune_report;
+hg_status hg_mpm_autotune(hg_mpm *m, double dt, int32_t steps_per_candidate,
+                          hg_tune_report *report);
+hg_status hg_mpm_launch_shape(hg_mpm *m, hg_launch_shape *shape);
+hg_status hg_mpm_set_launch_shape(hg_mpm *m, const hg_launch_shape *shape);
+hg_status hg_batch_autotune(hg_batch *b, int32_t steps_per_candidate, hg_tune_report *report);
+hg_status hg_batch_launch_shape(hg_batch *b, hg_launch_shape *shape);
+/* One line per entry: "kind sms tiles points fused update" (kind 0: single
+ * scene, 1: batch). */
+hg_status hg_tune_save(const char *path);
+hg_status hg_tune_load(const char *path);
+hg_status hg_tune_clear(void);
+
 /* ---- zone labels (hybridgrains2dnew ZoneTools), host code ----------------
  * Runs on the host at the resampling interval on positions copied from the
  * device (HybridGrains2DSim::updateHybridStates_poorman,

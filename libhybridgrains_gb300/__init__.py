@@ -15,6 +15,7 @@ There is no CPU fallback: constructing any object loads the CUDA library and
 raises if it is missing or no GPU is present.
 """
 import ctypes
+import os
 import weakref
 
 import numpy as np
@@ -58,6 +59,29 @@ def pinned(shape, dtype=np.float64):
     arr = np.frombuffer(buf, dtype=dt, count=count).reshape(shape)
     weakref.finalize(buf, _capi.load().hg_host_free, ctypes.c_void_p(p.value))
     return arr
+
+
+def _report(r):
+    k = r.candidates
+    return dict(tried=[(r.tried[i].fused_ctas_per_sm, r.tried[i].update_ctas_per_sm)
+                       for i in range(k)],
+                fused_ms=[r.fused_ms[i] for i in range(k)],
+                update_ms=[r.update_ms[i] for i in range(k)],
+                chosen=(r.chosen.fused_ctas_per_sm, r.chosen.update_ctas_per_sm))
+
+
+def tune_save(path):
+    """Writes the process-wide launch-shape table (hg_tune_save)."""
+    check("hg_tune_save", os.fsencode(path))
+
+
+def tune_load(path):
+    """Merges a saved launch-shape table (hg_tune_load)."""
+    check("hg_tune_load", os.fsencode(path))
+
+
+def tune_clear():
+    check("hg_tune_clear")
 
 
 def kernel_launch_count():
@@ -313,6 +337,22 @@ class MPM:
         check("hg_mpm_rebin_count", self._h, ctypes.byref(c))
         return c.value
 
+    def autotune(self, dt, steps_per_candidate=20):
+        """hg_mpm_autotune: times the candidate launch shapes on this scene
+        (which advances by all the timed steps) and keeps the fastest."""
+        r = _capi.TuneReport()
+        check("hg_mpm_autotune", self._h, float(dt), int(steps_per_candidate), ctypes.byref(r))
+        return _report(r)
+
+    def launch_shape(self):
+        s = _capi.LaunchShape()
+        check("hg_mpm_launch_shape", self._h, ctypes.byref(s))
+        return s.fused_ctas_per_sm, s.update_ctas_per_sm
+
+    def set_launch_shape(self, fused_ctas_per_sm, update_ctas_per_sm):
+        s = _capi.LaunchShape(int(fused_ctas_per_sm), int(update_ctas_per_sm))
+        check("hg_mpm_set_launch_shape", self._h, ctypes.byref(s))
+
 
 class DEM:
     """Circle bodies with the penalty impact-friction map (rigidbody2d)."""
@@ -515,6 +555,18 @@ class Batch:
 
     def profile(self, enable=True):
         check("hg_batch_profile", self._h, 1 if enable else 0)
+
+    def autotune(self, steps_per_candidate=20):
+        """hg_batch_autotune: times the candidate launch shapes on the
+        current members (which advance) and records the fastest."""
+        r = _capi.TuneReport()
+        check("hg_batch_autotune", self._h, int(steps_per_candidate), ctypes.byref(r))
+        return _report(r)
+
+    def launch_shape(self):
+        s = _capi.LaunchShape()
+        check("hg_batch_launch_shape", self._h, ctypes.byref(s))
+        return s.fused_ctas_per_sm, s.update_ctas_per_sm
 
     def profile_read(self):
         """dict of summed ms per phase (resort, table, update, fused) and steps."""

@@ -67,6 +67,19 @@ class ResamplerStats(ctypes.Structure):
                 ("points_deleted", ctypes.c_int64), ("grains_deleted", ctypes.c_int64)]
 
 
+HG_TUNE_CANDIDATES = 4
+
+
+class LaunchShape(ctypes.Structure):
+    _fields_ = [("fused_ctas_per_sm", ctypes.c_int32), ("update_ctas_per_sm", ctypes.c_int32)]
+
+
+class TuneReport(ctypes.Structure):
+    _fields_ = [("candidates", ctypes.c_int32), ("tried", LaunchShape * HG_TUNE_CANDIDATES),
+                ("fused_ms", ctypes.c_double * HG_TUNE_CANDIDATES),
+                ("update_ms", ctypes.c_double * HG_TUNE_CANDIDATES), ("chosen", LaunchShape)]
+
+
 class DemDesc(ctypes.Structure):
     _fields_ = [("gravity", ctypes.c_double * 2), ("kn", ctypes.c_double),
                 ("kt", ctypes.c_double), ("gamman", ctypes.c_double),
@@ -134,6 +147,14 @@ SIGNATURES = {
     "hg_batch_stats": [_P, _I64, _I64, _I64, _D, _D],
     "hg_batch_profile": [_P, _i32],
     "hg_batch_profile_read": [_P, _D, _D, _D, _D, _I64],
+    "hg_mpm_autotune": [_P, _dbl, _i32, ctypes.POINTER(TuneReport)],
+    "hg_mpm_launch_shape": [_P, ctypes.POINTER(LaunchShape)],
+    "hg_mpm_set_launch_shape": [_P, ctypes.POINTER(LaunchShape)],
+    "hg_batch_autotune": [_P, _i32, ctypes.POINTER(TuneReport)],
+    "hg_batch_launch_shape": [_P, ctypes.POINTER(LaunchShape)],
+    "hg_tune_save": [ctypes.c_char_p],
+    "hg_tune_load": [ctypes.c_char_p],
+    "hg_tune_clear": [],
     "hg_zones_create": [ctypes.POINTER(ZonesDesc), _PP],
     "hg_zones_destroy": [_P],
     "hg_zones_update": [_P, _i64, _D, _D, _U8, _i64, _D],

@@ -924,6 +924,52 @@ hg_status hg_mpm_profile_read(hg_mpm *m, double *a, double *b, int64_t *steps) {
   return mixed_profile_read(m, a, b, steps);
 }
 
+hg_status hg_mpm_autotune(hg_mpm *m, double dt, int32_t steps_per_candidate,
+                          hg_tune_report *report) {
+  if (!m) return fail(HG_ERR_INVALID_ARGUMENT, "m is NULL");
+  if (m->p.precision != HG_PRECISION_MIXED)
+    return fail(HG_ERR_UNSUPPORTED, "launch shapes apply to the MIXED path");
+  if (!(dt > 0.0) || !std::isfinite(dt)) return fail(HG_ERR_INVALID_ARGUMENT, "dt must be positive");
+  if (steps_per_candidate < 1 || steps_per_candidate > 100000)
+    return fail(HG_ERR_INVALID_ARGUMENT, "steps_per_candidate must lie in [1, 100000]");
+  DeviceGuard g(m->ctx);
+  return mixed_autotune(m, dt, steps_per_candidate, report);
+}
+
+static bool valid_shape(const hg_launch_shape &s) {
+  return s.fused_ctas_per_sm >= 0 && s.fused_ctas_per_sm <= 64 && s.update_ctas_per_sm >= 0 &&
+         s.update_ctas_per_sm <= 64;
+}
+
+hg_status hg_mpm_launch_shape(hg_mpm *m, hg_launch_shape *shape) {
+  if (!m || !shape) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  *shape = m->shape;
+  return HG_OK;
+}
+
+hg_status hg_mpm_set_launch_shape(hg_mpm *m, const hg_launch_shape *shape) {
+  if (!m || !shape) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (!valid_shape(*shape)) return fail(HG_ERR_INVALID_ARGUMENT, "CTAs per SM must lie in [0, 64]");
+  m->shape = *shape;
+  m->shape_set = true;
+  return HG_OK;
+}
+
+hg_status hg_tune_save(const char *path) {
+  if (!path) return fail(HG_ERR_INVALID_ARGUMENT, "path is NULL");
+  return tune_save(path);
+}
+
+hg_status hg_tune_load(const char *path) {
+  if (!path) return fail(HG_ERR_INVALID_ARGUMENT, "path is NULL");
+  return tune_load(path);
+}
+
+hg_status hg_tune_clear(void) {
+  tune_clear();
+  return HG_OK;
+}
+
 hg_status hg_mpm_rebin_count(hg_mpm *m, int64_t *count) {
   if (!m || !count) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
   *count = m->rebins;
@@ -1009,6 +1055,21 @@ hg_status hg_batch_step(hg_batch *b, int32_t nsteps) {
   const hg_status st = batch_step(b, nsteps);
   b->host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return st;
+}
+
+hg_status hg_batch_autotune(hg_batch *b, int32_t steps_per_candidate, hg_tune_report *report) {
+  if (!b) return fail(HG_ERR_INVALID_ARGUMENT, "b is NULL");
+  if (steps_per_candidate < 1 || steps_per_candidate > 100000)
+    return fail(HG_ERR_INVALID_ARGUMENT, "steps_per_candidate must lie in [1, 100000]");
+  if (b->members.empty()) return fail(HG_ERR_INVALID_ARGUMENT, "the batch has no members");
+  DeviceGuard g(b->ctx);
+  return batch_autotune(b, steps_per_candidate, report);
+}
+
+hg_status hg_batch_launch_shape(hg_batch *b, hg_launch_shape *shape) {
+  if (!b || !shape) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  *shape = b->shape;
+  return HG_OK;
 }
 
 hg_status hg_batch_profile(hg_batch *b, int32_t enable) {

@@ -197,11 +197,16 @@ struct hg_mpm {
   int64_t steps_since_rebin = 0;
   int64_t rebins = 0;
   bool primed = false;
+  // launch shape of the MIXED kernels (0: built-in); set explicitly or by
+  // the autotuner, else looked up in the tuning table at priming
+  hg_launch_shape shape{0, 0};
+  bool shape_set = false;
   // CHUNK_STEPS steps captured as a CUDA graph, one per live buffer; rebuilt
-  // when dt or the point count changes
+  // when dt, the point count or the launch shape changes
   cudaGraphExec_t chunk_exec[2] = {nullptr, nullptr};
   double chunk_dt[2] = {0.0, 0.0};
   int64_t chunk_n[2] = {-1, -1};
+  hg_launch_shape chunk_shape[2] = {{-1, -1}, {-1, -1}};
   int64_t chunk_launches = 0;
   // per-kernel event timing (hg_mpm_profile)
   bool profile = false;
@@ -231,6 +236,11 @@ hg_status mixed_download_grid(hg_mpm *m, double *mass, double *vel,
                               double *acc);
 // device bytes mixed_alloc plus the staging of an upload allocate
 int64_t mixed_device_bytes(int nx, int ny, int64_t cap);
+hg_status mixed_autotune(hg_mpm *m, double dt, int steps, hg_tune_report *report);
+hg_status batch_autotune(hg_batch *b, int steps, hg_tune_report *report);
+hg_status tune_save(const char *path);
+hg_status tune_load(const char *path);
+void tune_clear();
 hg_status mixed_profile_read(hg_mpm *m, double *g2p2g_ms, double *update_ms,
                              int64_t *steps);
 
@@ -275,7 +285,13 @@ struct hg_batch {
   // keys it)
   cudaGraphExec_t chunk_exec = nullptr;
   int chunk_members = -1;
+  hg_launch_shape chunk_shape{-1, -1};
   int64_t chunk_launches = 0;
+  // launch shape of the batched kernels and the size class it was looked
+  // up for (the total point count changes as members come and go)
+  hg_launch_shape shape{0, 0};
+  bool shape_set = false;
+  int64_t shape_class = -1;
   int64_t member_steps = 0, resorts = 0, steps = 0;
   double host_ms = 0.0, wait_ms = 0.0; // wait: host blocked on the device
   bool profile = false;

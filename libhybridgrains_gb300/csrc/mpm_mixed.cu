@@ -39,9 +39,15 @@
 #include "hg_internal.cuh"
 #include "scan_block.cuh"
 
+#include <algorithm>
+#include <array>
 #include <chrono>
 #include <cstddef>
+#include <cstdio>
 #include <cstring>
+#include <limits>
+#include <map>
+#include <mutex>
 
 #include <cmath>
 
@@ -1145,11 +1151,62 @@ hg_status rebin_batch(hg_context *ctx, const std::vector<hg_mpm *> &R, unsigned 
   return HG_OK;
 }
 
-int fused_blocks(hg_mpm *m) { return m->ctx->num_sms * 3; }
-int update_blocks(hg_mpm *m) { return m->ctx->num_sms * 8; }
+// CTAs per SM of the two kernels: the launch shape, else 3 (the fused
+// kernel's occupancy at 80 registers) and 8
+constexpr int DEFAULT_FUSED_CTAS = 3, DEFAULT_UPDATE_CTAS = 8;
+int fused_per_sm(const hg_launch_shape &s) {
+  return s.fused_ctas_per_sm > 0 ? s.fused_ctas_per_sm : DEFAULT_FUSED_CTAS;
+}
+int update_per_sm(const hg_launch_shape &s) {
+  return s.update_ctas_per_sm > 0 ? s.update_ctas_per_sm : DEFAULT_UPDATE_CTAS;
+}
+int fused_blocks(hg_mpm *m) { return m->ctx->num_sms * fused_per_sm(m->shape); }
+int update_blocks(hg_mpm *m) { return m->ctx->num_sms * update_per_sm(m->shape); }
+bool same_shape(const hg_launch_shape &a, const hg_launch_shape &b) {
+  return a.fused_ctas_per_sm == b.fused_ctas_per_sm &&
+         a.update_ctas_per_sm == b.update_ctas_per_sm;
+}
+
+// ---- the tuning table -------------------------------------------------------
+//
+// Keyed by (kind, SMs, tiles, points), tiles and points rounded up to powers
+// of two: kind 0 is a single scene, kind 1 a batch (tiles 0).
+using TuneKey = std::array<int64_t, 4>;
+std::mutex g_tune_mu;
+std::map<TuneKey, hg_launch_shape> g_tune;
+
+int64_t ceil_pow2(int64_t x) {
+  int64_t p = 1;
+  while (p < x) p <<= 1;
+  return p;
+}
+TuneKey mixed_key(const hg_mpm *m) {
+  return {0, m->ctx->num_sms, ceil_pow2((int64_t)m->ntx * m->nty), ceil_pow2(std::max<int64_t>(m->n, 1))};
+}
+TuneKey batch_key(const hg_batch *b, int64_t points) {
+  return {1, b->ctx->num_sms, 0, ceil_pow2(std::max<int64_t>(points, 1))};
+}
+bool tune_lookup(const TuneKey &k, hg_launch_shape *out) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  auto it = g_tune.find(k);
+  if (it == g_tune.end()) return false;
+  *out = it->second;
+  return true;
+}
+void tune_store(const TuneKey &k, const hg_launch_shape &s) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tune[k] = s;
+}
+// CTAs per SM tried for (fused, update): fewer, the default, and more CTAs
+// than are resident (finer shares of the tiles, later ones fill in behind
+// the first wave)
+constexpr hg_launch_shape TUNE_CANDIDATES[HG_TUNE_CANDIDATES] = {{2, 4}, {3, 8}, {6, 16},
+                                                                 {12, 32}};
+static_assert(HG_TUNE_CANDIDATES == 4, "candidate list");
 
 hg_status prime(hg_mpm *m) {
   cudaStream_t s = m->ctx->stream;
+  if (!m->shape_set && !tune_lookup(mixed_key(m), &m->shape)) m->shape = hg_launch_shape{0, 0};
   const int64_t nn = (int64_t)(m->p.nx + 1) * (m->p.ny + 1);
   HG_CUDA_TRY(cudaMemsetAsync(m->accm.p, 0, sizeof(float) * nn, s));
   HG_CUDA_TRY(cudaMemsetAsync(m->acc4.p, 0, sizeof(float4) * nn, s));
@@ -1294,7 +1351,9 @@ hg_status end_chunk_capture(cudaStream_t s, hg_status st, int64_t l0, cudaGraphE
 // kernels per step, then the read-back of the out-of-window counters.
 hg_status mixed_chunk_graph(hg_mpm *m, double dt) {
   const int c = m->cur;
-  if (m->chunk_exec[c] && m->chunk_dt[c] == dt && m->chunk_n[c] == m->n) return HG_OK;
+  if (m->chunk_exec[c] && m->chunk_dt[c] == dt && m->chunk_n[c] == m->n &&
+      same_shape(m->chunk_shape[c], m->shape))
+    return HG_OK;
   if (m->chunk_exec[c]) {
     cudaGraphExecDestroy(m->chunk_exec[c]);
     m->chunk_exec[c] = nullptr;
@@ -1321,6 +1380,7 @@ hg_status mixed_chunk_graph(hg_mpm *m, double dt) {
   if (st != HG_OK) return st;
   m->chunk_dt[c] = dt;
   m->chunk_n[c] = m->n;
+  m->chunk_shape[c] = m->shape;
   m->chunk_launches = launches;
   return HG_OK;
 }
@@ -1452,7 +1512,8 @@ hg_status batch_profile_read(hg_batch *b, double *ms, int64_t *steps) {
 // The graph of CHUNK_STEPS steps of all S members: the two batched kernels
 // per step, then the gather and read-back of the out-of-window counters.
 hg_status batch_chunk_graph(hg_batch *b, int S) {
-  if (b->chunk_exec && b->chunk_members == S) return HG_OK;
+  if (b->chunk_exec && b->chunk_members == S && same_shape(b->chunk_shape, b->shape))
+    return HG_OK;
   if (b->chunk_exec) {
     cudaGraphExecDestroy(b->chunk_exec);
     b->chunk_exec = nullptr;
@@ -1461,12 +1522,13 @@ hg_status batch_chunk_graph(hg_batch *b, int S) {
   const MixedArgs *dt = reinterpret_cast<const MixedArgs *>(b->table.p);
   const MixedArgs *db = dt + S;
   const int nsm = b->ctx->num_sms;
+  const int gu = nsm * update_per_sm(b->shape), gf = nsm * fused_per_sm(b->shape);
   const int64_t l0 = g_launches.load();
   HG_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   hg_status st = HG_OK;
   for (int k = 0; k < CHUNK_STEPS && st == HG_OK; ++k) {
-    HG_LAUNCH(kb_grid_update, nsm * 8, THREADS, 0, s, dt, S);
-    HG_LAUNCH(kb_g2p2g, nsm * 3, THREADS, 0, s, db, S);
+    HG_LAUNCH(kb_grid_update, gu, THREADS, 0, s, dt, S);
+    HG_LAUNCH(kb_g2p2g, gf, THREADS, 0, s, db, S);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) st = cuda_fail(e, "kernel launch");
   }
@@ -1482,6 +1544,7 @@ hg_status batch_chunk_graph(hg_batch *b, int S) {
   st = end_chunk_capture(s, st, l0, &b->chunk_exec, &launches);
   if (st != HG_OK) return st;
   b->chunk_members = S;
+  b->chunk_shape = b->shape;
   b->chunk_launches = launches;
   return HG_OK;
 }
@@ -1494,6 +1557,15 @@ hg_status batch_step(hg_batch *b, int nsteps) {
   if ((int)b->sigs.size() != S) {
     b->sigs.assign(S, hg_batch::Sig{});
     b->dirty = true;
+  }
+  if (!b->shape_set) {
+    int64_t points = 0;
+    for (hg_mpm *m : b->members) points += m->n;
+    const TuneKey key = batch_key(b, points);
+    if (key[3] != b->shape_class) {
+      b->shape_class = key[3];
+      if (!tune_lookup(key, &b->shape)) b->shape = hg_launch_shape{0, 0};
+    }
   }
   // Host work ahead of a step (or of a captured chunk of steps): re-sort
   // members whose points left their windows (counters read back
@@ -1597,10 +1669,10 @@ hg_status batch_step(hg_batch *b, int nsteps) {
     const MixedArgs *dt = reinterpret_cast<const MixedArgs *>(b->table.p);
     const MixedArgs *db = dt + S;
     const int nsm = b->ctx->num_sms;
-    HG_LAUNCH(kb_grid_update, nsm * 8, THREADS, 0, s, dt, S);
+    HG_LAUNCH(kb_grid_update, nsm * update_per_sm(b->shape), THREADS, 0, s, dt, S);
     HG_CHECK_LAUNCH();
     if (b->profile) HG_CUDA_TRY(cudaEventRecord(ev[3], s));
-    HG_LAUNCH(kb_g2p2g, nsm * 3, THREADS, 0, s, db, S);
+    HG_LAUNCH(kb_g2p2g, nsm * fused_per_sm(b->shape), THREADS, 0, s, db, S);
     HG_CHECK_LAUNCH();
     if (b->profile) HG_CUDA_TRY(cudaEventRecord(ev[4], s));
     for (hg_mpm *m : b->members) m->steps_since_rebin++;
@@ -1617,6 +1689,135 @@ hg_status batch_step(hg_batch *b, int nsteps) {
     }
   }
   return HG_OK;
+}
+
+// ---- autotuning -------------------------------------------------------------
+
+namespace {
+
+// Picks, per kernel, the candidate with the least mean time per step.
+void pick(hg_tune_report &r) {
+  int bf = 0, bu = 0;
+  for (int i = 1; i < r.candidates; ++i) {
+    if (r.fused_ms[i] < r.fused_ms[bf]) bf = i;
+    if (r.update_ms[i] < r.update_ms[bu]) bu = i;
+  }
+  r.chosen = hg_launch_shape{r.tried[bf].fused_ctas_per_sm, r.tried[bu].update_ctas_per_sm};
+}
+
+} // namespace
+
+hg_status mixed_autotune(hg_mpm *m, double dt, int steps, hg_tune_report *report) {
+  hg_tune_report r{};
+  r.candidates = HG_TUNE_CANDIDATES;
+  const bool prof0 = m->profile;
+  hg_status st = HG_OK;
+  if (!m->primed) st = prime(m);
+  for (int i = 0; i < HG_TUNE_CANDIDATES && st == HG_OK; ++i) {
+    r.tried[i] = TUNE_CANDIDATES[i];
+    m->shape = TUNE_CANDIDATES[i];
+    // one untimed step with the shape, then steps timed per kernel
+    m->profile = false;
+    st = mixed_step(m, dt, 1);
+    if (st != HG_OK) break;
+    m->profile = true;
+    m->prof_used = 0;
+    st = mixed_step(m, dt, steps);
+    double g2p2g = 0.0, update = 0.0;
+    int64_t n = 0;
+    if (st == HG_OK) st = mixed_profile_read(m, &g2p2g, &update, &n);
+    r.fused_ms[i] = n > 0 ? g2p2g / n : std::numeric_limits<double>::infinity();
+    r.update_ms[i] = n > 0 ? update / n : std::numeric_limits<double>::infinity();
+  }
+  m->profile = prof0;
+  m->prof_used = 0;
+  if (st != HG_OK) {
+    m->shape = hg_launch_shape{0, 0};
+    return st;
+  }
+  pick(r);
+  m->shape = r.chosen;
+  m->shape_set = true;
+  tune_store(mixed_key(m), r.chosen);
+  if (report) *report = r;
+  return HG_OK;
+}
+
+hg_status batch_autotune(hg_batch *b, int steps, hg_tune_report *report) {
+  hg_tune_report r{};
+  r.candidates = HG_TUNE_CANDIDATES;
+  const bool prof0 = b->profile;
+  int64_t points = 0;
+  for (hg_mpm *m : b->members) points += m->n;
+  b->shape_set = true; // the candidates, not the table, during the timing
+  hg_status st = HG_OK;
+  for (int i = 0; i < HG_TUNE_CANDIDATES && st == HG_OK; ++i) {
+    r.tried[i] = TUNE_CANDIDATES[i];
+    b->shape = TUNE_CANDIDATES[i];
+    b->profile = false;
+    st = batch_step(b, 1);
+    if (st != HG_OK) break;
+    b->profile = true;
+    b->prof_used = 0;
+    st = batch_step(b, steps);
+    double ms[hg_batch::PROF_PHASES] = {0.0};
+    int64_t n = 0;
+    if (st == HG_OK) st = batch_profile_read(b, ms, &n);
+    r.update_ms[i] = n > 0 ? ms[2] / n : std::numeric_limits<double>::infinity();
+    r.fused_ms[i] = n > 0 ? ms[3] / n : std::numeric_limits<double>::infinity();
+  }
+  b->profile = prof0;
+  b->prof_used = 0;
+  if (st != HG_OK) {
+    b->shape = hg_launch_shape{0, 0};
+    b->shape_set = false;
+    b->shape_class = -1;
+    return st;
+  }
+  pick(r);
+  b->shape = r.chosen;
+  b->shape_class = batch_key(b, points)[3];
+  tune_store(batch_key(b, points), r.chosen);
+  // later steps follow the table again as the member mix changes
+  b->shape_set = false;
+  if (report) *report = r;
+  return HG_OK;
+}
+
+hg_status tune_save(const char *path) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  FILE *f = std::fopen(path, "w");
+  if (!f) return fail(HG_ERR_INVALID_ARGUMENT, "cannot open the tuning file for writing");
+  for (const auto &e : g_tune)
+    std::fprintf(f, "%lld %lld %lld %lld %d %d\n", (long long)e.first[0], (long long)e.first[1],
+                 (long long)e.first[2], (long long)e.first[3], e.second.fused_ctas_per_sm,
+                 e.second.update_ctas_per_sm);
+  const bool ok = std::fclose(f) == 0;
+  return ok ? HG_OK : fail(HG_ERR_INVALID_ARGUMENT, "writing the tuning file failed");
+}
+
+hg_status tune_load(const char *path) {
+  FILE *f = std::fopen(path, "r");
+  if (!f) return fail(HG_ERR_INVALID_ARGUMENT, "cannot open the tuning file");
+  std::map<TuneKey, hg_launch_shape> add;
+  long long k0, k1, k2, k3;
+  int fu, up;
+  int got;
+  while ((got = std::fscanf(f, "%lld %lld %lld %lld %d %d", &k0, &k1, &k2, &k3, &fu, &up)) == 6) {
+    if (fu < 0 || fu > 64 || up < 0 || up > 64) break;
+    add[TuneKey{k0, k1, k2, k3}] = hg_launch_shape{fu, up};
+  }
+  const bool clean = got == EOF;
+  std::fclose(f);
+  if (!clean) return fail(HG_ERR_INVALID_ARGUMENT, "malformed tuning file");
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  for (const auto &e : add) g_tune[e.first] = e.second;
+  return HG_OK;
+}
+
+void tune_clear() {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tune.clear();
 }
 
 } // namespace hg

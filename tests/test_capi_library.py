@@ -70,3 +70,28 @@ def test_no_gpu_fails_loudly(lib):
         pytest.skip("a GPU is present")
     assert st in (1, 2)
     assert lib.hg_last_error()
+
+
+def test_tuning_table_round_trip(lib, tmp_path):
+    """The launch-shape table (host only): save, merge, clear, and a
+    malformed file is refused without touching the table."""
+    import libhybridgrains_gb300 as hg
+    hg.tune_clear()
+    p = tmp_path / "shapes.txt"
+    p.write_text("0 152 8192 2097152 2 16\n1 152 0 16777216 3 8\n")
+    hg.tune_load(str(p))
+    q = tmp_path / "out.txt"
+    hg.tune_save(str(q))
+    assert q.read_text() == p.read_text()
+    bad = tmp_path / "bad.txt"
+    bad.write_text("0 152 8192\n")
+    with pytest.raises(hg.HGError):
+        hg.tune_load(str(bad))
+    bad.write_text("0 152 8192 2097152 99 16\n")  # CTAs per SM out of range
+    with pytest.raises(hg.HGError):
+        hg.tune_load(str(bad))
+    hg.tune_save(str(q))
+    assert q.read_text() == p.read_text()
+    hg.tune_clear()
+    hg.tune_save(str(q))
+    assert q.read_text() == ""
