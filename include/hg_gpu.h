@@ -285,6 +285,28 @@ hg_status hg_mpm_launch_shape(hg_mpm *m, hg_launch_shape *shape);
 hg_status hg_mpm_set_launch_shape(hg_mpm *m, const hg_launch_shape *shape);
 hg_status hg_batch_autotune(hg_batch *b, int32_t steps_per_candidate, hg_tune_report *report);
 hg_status hg_batch_launch_shape(hg_batch *b, hg_launch_shape *shape);
+/* ---- checkpoint / resume (no reference counterpart: the reference's
+ * mpmgrains2d snapshot, mpmgrains2d_cli.cpp:154-247, holds host arrays, and
+ * its hybrid and penalty-map serialization exit) --------------------------
+ * An object's device state as one host blob in this library's own versioned
+ * format ("HGSTATE" header, then tagged segments): for MIXED MPM the sorted
+ * particle records, the next step's P2G accumulators and the sort tables; for
+ * FP64 MPM the particle and grid arrays; for DEM the bodies and the live
+ * contact history (keys and records); for a hybrid coupling the homogenised
+ * stress and velocity accumulated in the current interval. A blob loads into
+ * an object created with the same grid (MPM) and a capacity that holds it;
+ * the loaded object continues as the saved one would. *_state_bytes gives the
+ * size a save needs. */
+hg_status hg_mpm_state_bytes(hg_mpm *m, int64_t *bytes);
+hg_status hg_mpm_state_save(hg_mpm *m, void *dst, int64_t bytes);
+hg_status hg_mpm_state_load(hg_mpm *m, const void *src, int64_t bytes);
+hg_status hg_dem_state_bytes(hg_dem *d, int64_t *bytes);
+hg_status hg_dem_state_save(hg_dem *d, void *dst, int64_t bytes);
+hg_status hg_dem_state_load(hg_dem *d, const void *src, int64_t bytes);
+hg_status hg_hybrid_state_bytes(hg_hybrid *h, int64_t *bytes);
+hg_status hg_hybrid_state_save(hg_hybrid *h, void *dst, int64_t bytes);
+hg_status hg_hybrid_state_load(hg_hybrid *h, const void *src, int64_t bytes);
+
 /* One line per entry: "kind sms tiles points fused update" (kind 0: single
  * scene, 1: batch). */
 hg_status hg_tune_save(const char *path);
@@ -425,6 +447,12 @@ hg_status hg_resampler_dem_map_size(hg_resampler *r, int64_t *n);
 uint32_t hg_resampler_random_u32(hg_resampler *r);
 float hg_resampler_random_f32(hg_resampler *r);
 double hg_resampler_random_radius(hg_resampler *r);
+/* The random streams' state (the insertion MT19937, the radius engine and
+ * its normal distribution, the next test id) as a host blob, for checkpoint
+ * and resume of a hybrid simulation. */
+hg_status hg_resampler_rng_bytes(hg_resampler *r, int64_t *bytes);
+hg_status hg_resampler_rng_save(hg_resampler *r, void *dst, int64_t bytes);
+hg_status hg_resampler_rng_load(hg_resampler *r, const void *src, int64_t bytes);
 
 /* ---- DEM (rigidbody2d, penalty map) --------------------------------------- */
 

@@ -61,6 +61,20 @@ def pinned(shape, dtype=np.float64):
     return arr
 
 
+def _save_blob(prefix, h):
+    """The object's state blob (hg_*_state_save) as a uint8 array."""
+    n = ctypes.c_int64()
+    check(prefix + "_bytes", h, ctypes.byref(n))
+    buf = np.zeros(n.value, dtype=np.uint8)
+    check(prefix + "_save", h, buf.ctypes.data_as(ctypes.c_void_p), n.value)
+    return buf
+
+
+def _load_blob(prefix, h, blob):
+    blob = np.ascontiguousarray(blob, dtype=np.uint8)
+    check(prefix + "_load", h, blob.ctypes.data_as(ctypes.c_void_p), len(blob))
+
+
 def _report(r):
     k = r.candidates
     return dict(tried=[(r.tried[i].fused_ctas_per_sm, r.tried[i].update_ctas_per_sm)
@@ -337,6 +351,17 @@ class MPM:
         check("hg_mpm_rebin_count", self._h, ctypes.byref(c))
         return c.value
 
+    def state(self):
+        """The device state as a blob (hg_mpm_state_save) for checkpoints."""
+        return _save_blob("hg_mpm_state", self._h)
+
+    def load_state(self, blob):
+        """Restores a blob saved from an object with the same grid."""
+        _load_blob("hg_mpm_state", self._h, blob)
+        c = ctypes.c_int64()
+        check("hg_mpm_num_particles", self._h, ctypes.byref(c))
+        self.n = c.value
+
     def autotune(self, dt, steps_per_candidate=20):
         """hg_mpm_autotune: times the candidate launch shapes on this scene
         (which advances by all the timed steps) and keeps the fastest."""
@@ -423,6 +448,16 @@ class DEM:
     def frame_async(self, q=None, v=None):
         check("hg_dem_frame_async", self._h, _d(q), _d(v))
 
+    def state(self):
+        """Bodies and contact history as a blob (hg_dem_state_save)."""
+        return _save_blob("hg_dem_state", self._h)
+
+    def load_state(self, blob):
+        _load_blob("hg_dem_state", self._h, blob)
+        c = ctypes.c_int64()
+        check("hg_dem_num_bodies", self._h, ctypes.byref(c))
+        self.n = c.value
+
     def set_weights(self, w):
         check("hg_dem_set_weights", self._h, _d(_f64(w)))
 
@@ -496,6 +531,13 @@ class Hybrid:
     def step(self, dt, nsteps=1, homogenize_stress=False, homogenize_velocity=False):
         flags = (1 if homogenize_stress else 0) | (2 if homogenize_velocity else 0)
         check("hg_hybrid_step", self._h, float(dt), int(nsteps), flags)
+
+    def state(self):
+        """Homogenised accumulators of the interval (hg_hybrid_state_save)."""
+        return _save_blob("hg_hybrid_state", self._h)
+
+    def load_state(self, blob):
+        _load_blob("hg_hybrid_state", self._h, blob)
 
     def clear_homogenized(self):
         check("hg_hybrid_clear_homogenized", self._h)
@@ -782,6 +824,13 @@ class Resampler:
         check("hg_resampler_get_grains", self._h, *[_d(out[x]) for x in
               ("q0", "q", "v", "r", "M0", "w")], _u8(out["fixed"]), _i32(out["old_to_new"]))
         return out
+
+    def rng_state(self):
+        """The random streams' state (hg_resampler_rng_save)."""
+        return _save_blob("hg_resampler_rng", self._h)
+
+    def load_rng_state(self, blob):
+        _load_blob("hg_resampler_rng", self._h, blob)
 
     def random_u32(self):
         return _capi.load().hg_resampler_random_u32(self._h)

@@ -155,6 +155,18 @@ SIGNATURES = {
     "hg_tune_save": [ctypes.c_char_p],
     "hg_tune_load": [ctypes.c_char_p],
     "hg_tune_clear": [],
+    "hg_mpm_state_bytes": [_P, _I64],
+    "hg_mpm_state_save": [_P, _P, _i64],
+    "hg_mpm_state_load": [_P, _P, _i64],
+    "hg_dem_state_bytes": [_P, _I64],
+    "hg_dem_state_save": [_P, _P, _i64],
+    "hg_dem_state_load": [_P, _P, _i64],
+    "hg_hybrid_state_bytes": [_P, _I64],
+    "hg_hybrid_state_save": [_P, _P, _i64],
+    "hg_hybrid_state_load": [_P, _P, _i64],
+    "hg_resampler_rng_bytes": [_P, _I64],
+    "hg_resampler_rng_save": [_P, _P, _i64],
+    "hg_resampler_rng_load": [_P, _P, _i64],
     "hg_zones_create": [ctypes.POINTER(ZonesDesc), _PP],
     "hg_zones_destroy": [_P],
     "hg_zones_update": [_P, _i64, _D, _D, _U8, _i64, _D],

@@ -31,6 +31,7 @@ SOURCES = [
     ("coupling.cu", True),
     ("zones.cu", True),  # host code (zone labels)
     ("resampling.cu", True),  # host code (resampling)
+    ("state.cu", False),  # checkpoint / resume blobs
 ]
 HEADERS = ["hg_internal.cuh", "mpm_basis.cuh", "scan_block.cuh", "zones_internal.cuh"]
 

@@ -722,6 +722,7 @@ hg_status hg_mpm_upload(hg_mpm *m, int64_t n, const double *q, const double *v,
                         const double *mass, const double *volume, const double *hl,
                         const double *be, const double *J, const int32_t *jh,
                         const uint8_t *kin) {
+  HG_TRACE("hg_mpm_upload");
   return upload_impl(m, n, q, v, mass, volume, hl, be, J, jh, kin, true);
 }
 
@@ -772,6 +773,7 @@ hg_status hg_mpm_estimate_bytes(const hg_mpm_desc *d, int64_t *bytes) {
 
 hg_status hg_mpm_download(hg_mpm *m, double *q, double *v, double *be, double *J,
                           int32_t *jh) {
+  HG_TRACE("hg_mpm_download");
   if (!m) return fail(HG_ERR_INVALID_ARGUMENT, "m is NULL");
   DeviceGuard g(m->ctx);
   cudaStream_t s = m->ctx->stream;
@@ -804,6 +806,7 @@ hg_status hg_mpm_num_particles(hg_mpm *m, int64_t *n) {
 }
 
 hg_status hg_mpm_step(hg_mpm *m, double dt, int32_t nsteps) {
+  HG_TRACE("hg_mpm_step");
   if (!m) return fail(HG_ERR_INVALID_ARGUMENT, "m is NULL");
   if (!(dt > 0.0) || !std::isfinite(dt)) return fail(HG_ERR_INVALID_ARGUMENT, "dt must be positive");
   if (nsteps < 0) return fail(HG_ERR_INVALID_ARGUMENT, "negative step count");
@@ -926,6 +929,7 @@ hg_status hg_mpm_profile_read(hg_mpm *m, double *a, double *b, int64_t *steps) {
 
 hg_status hg_mpm_autotune(hg_mpm *m, double dt, int32_t steps_per_candidate,
                           hg_tune_report *report) {
+  HG_TRACE("hg_mpm_autotune");
   if (!m) return fail(HG_ERR_INVALID_ARGUMENT, "m is NULL");
   if (m->p.precision != HG_PRECISION_MIXED)
     return fail(HG_ERR_UNSUPPORTED, "launch shapes apply to the MIXED path");
@@ -954,6 +958,31 @@ hg_status hg_mpm_set_launch_shape(hg_mpm *m, const hg_launch_shape *shape) {
   m->shape_set = true;
   return HG_OK;
 }
+
+// ---- checkpoint / resume ------------------------------------------------------------
+
+#define HG_STATE_API(T, obj, name)                                                          \
+  hg_status hg_##name##_state_bytes(T *o, int64_t *bytes) {                                 \
+    if (!o || !bytes) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");                \
+    DeviceGuard g(o->ctx);                                                                  \
+    return name##_state_bytes(o, bytes);                                                    \
+  }                                                                                         \
+  hg_status hg_##name##_state_save(T *o, void *dst, int64_t bytes) {                        \
+    if (!o || !dst) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");                  \
+    HG_TRACE("hg_" #name "_state_save");                                                    \
+    DeviceGuard g(o->ctx);                                                                  \
+    return name##_state_save(o, dst, bytes);                                                \
+  }                                                                                         \
+  hg_status hg_##name##_state_load(T *o, const void *src, int64_t bytes) {                  \
+    if (!o || !src) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");                  \
+    HG_TRACE("hg_" #name "_state_load");                                                    \
+    DeviceGuard g(o->ctx);                                                                  \
+    return name##_state_load(o, src, bytes);                                                \
+  }
+
+HG_STATE_API(hg_mpm, m, mpm)
+HG_STATE_API(hg_dem, d, dem)
+HG_STATE_API(hg_hybrid, h, hybrid)
 
 hg_status hg_tune_save(const char *path) {
   if (!path) return fail(HG_ERR_INVALID_ARGUMENT, "path is NULL");
@@ -1048,6 +1077,7 @@ hg_status hg_batch_size(hg_batch *b, int32_t *n) {
 }
 
 hg_status hg_batch_step(hg_batch *b, int32_t nsteps) {
+  HG_TRACE("hg_batch_step");
   if (!b) return fail(HG_ERR_INVALID_ARGUMENT, "b is NULL");
   if (nsteps < 0) return fail(HG_ERR_INVALID_ARGUMENT, "negative step count");
   DeviceGuard g(b->ctx);
@@ -1058,6 +1088,7 @@ hg_status hg_batch_step(hg_batch *b, int32_t nsteps) {
 }
 
 hg_status hg_batch_autotune(hg_batch *b, int32_t steps_per_candidate, hg_tune_report *report) {
+  HG_TRACE("hg_batch_autotune");
   if (!b) return fail(HG_ERR_INVALID_ARGUMENT, "b is NULL");
   if (steps_per_candidate < 1 || steps_per_candidate > 100000)
     return fail(HG_ERR_INVALID_ARGUMENT, "steps_per_candidate must lie in [1, 100000]");
@@ -1237,6 +1268,7 @@ static hg_status dem_upload_impl(hg_dem *d, int64_t n, const double *q, const do
 hg_status hg_dem_edit_async(hg_dem *d, int64_t n_old, const int32_t *old_to_new, int64_t n_add,
                             const double *q, const double *v, const double *r,
                             const double *mass, const double *inertia, const uint8_t *fixed) {
+  HG_TRACE("hg_dem_edit_async");
   if (!d) return fail(HG_ERR_INVALID_ARGUMENT, "d is NULL");
   if (n_old != d->n) return fail(HG_ERR_INVALID_ARGUMENT, "n_old must be the current body count");
   if (n_add < 0 || (n_old > 0 && !old_to_new)) return fail(HG_ERR_INVALID_ARGUMENT, "invalid edit");
@@ -1356,6 +1388,7 @@ static hg_status dem_pair_graph(hg_dem *d, double dt, int weighted) {
 }
 
 hg_status hg_dem_step(hg_dem *d, double dt, int32_t nsteps, int32_t weighted) {
+  HG_TRACE("hg_dem_step");
   if (!d) return fail(HG_ERR_INVALID_ARGUMENT, "d is NULL");
   if (!(dt > 0.0) || !std::isfinite(dt)) return fail(HG_ERR_INVALID_ARGUMENT, "dt must be positive");
   if (nsteps < 0) return fail(HG_ERR_INVALID_ARGUMENT, "negative step count");
@@ -1458,6 +1491,7 @@ hg_status hg_hybrid_destroy(hg_hybrid *h) {
 }
 
 hg_status hg_hybrid_step(hg_hybrid *h, double dt, int32_t nsteps, int32_t flags) {
+  HG_TRACE("hg_hybrid_step");
   if (!h) return fail(HG_ERR_INVALID_ARGUMENT, "h is NULL");
   if (!(dt > 0.0) || !std::isfinite(dt)) return fail(HG_ERR_INVALID_ARGUMENT, "dt must be positive");
   if (nsteps < 0) return fail(HG_ERR_INVALID_ARGUMENT, "negative step count");

@@ -8,6 +8,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "hg_gpu.h"
 
 namespace hg {
@@ -27,6 +29,16 @@ hg_status cuda_fail(cudaError_t e, const char *what);
 // Launch bookkeeping: every kernel launch goes through HG_LAUNCH so that the
 // number of library kernels launched is observable (hg_kernel_launch_count).
 extern std::atomic<int64_t> g_launches;
+// An NVTX range over a C-ABI call, for timelines of profiling tools (a no-op
+// when no tool is attached).
+struct TraceRange {
+  explicit TraceRange(const char *name) { nvtxRangePushA(name); }
+  ~TraceRange() { nvtxRangePop(); }
+  TraceRange(const TraceRange &) = delete;
+  TraceRange &operator=(const TraceRange &) = delete;
+};
+
+#define HG_TRACE(name) ::hg::TraceRange hg_trace_range_(name)
 
 #define HG_LAUNCH(kernel, grid, block, smem, stream, ...)                     \
   do {                                                                        \
@@ -238,6 +250,15 @@ hg_status mixed_download_grid(hg_mpm *m, double *mass, double *vel,
 int64_t mixed_device_bytes(int nx, int ny, int64_t cap);
 hg_status mixed_autotune(hg_mpm *m, double dt, int steps, hg_tune_report *report);
 hg_status batch_autotune(hg_batch *b, int steps, hg_tune_report *report);
+hg_status mpm_state_bytes(hg_mpm *m, int64_t *bytes);
+hg_status mpm_state_save(hg_mpm *m, void *dst, int64_t bytes);
+hg_status mpm_state_load(hg_mpm *m, const void *src, int64_t bytes);
+hg_status dem_state_bytes(hg_dem *d, int64_t *bytes);
+hg_status dem_state_save(hg_dem *d, void *dst, int64_t bytes);
+hg_status dem_state_load(hg_dem *d, const void *src, int64_t bytes);
+hg_status hybrid_state_bytes(hg_hybrid *h, int64_t *bytes);
+hg_status hybrid_state_save(hg_hybrid *h, void *dst, int64_t bytes);
+hg_status hybrid_state_load(hg_hybrid *h, const void *src, int64_t bytes);
 hg_status tune_save(const char *path);
 hg_status tune_load(const char *path);
 void tune_clear();

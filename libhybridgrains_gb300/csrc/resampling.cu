@@ -29,8 +29,11 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <new>
 #include <random>
+#include <sstream>
+#include <string>
 #include <vector>
 
 namespace {
@@ -726,6 +729,92 @@ hg_status hg_resampler_create(const hg_resampler_desc *d, hg_resampler **out) {
   return HG_OK;
 }
 
+namespace {
+
+// RNG blob: magic, MT19937 position and words, next test id, then the text
+// forms (operator<<) of the radius engine and distribution, each length-
+// prefixed.
+constexpr char RNG_MAGIC[8] = {'H', 'G', 'R', 'N', 'G', '\0', '\0', '\1'};
+
+std::string rng_text(const hg_resampler *r, int which) {
+  std::ostringstream o;
+  if (which == 0) o << r->gen;
+  else o << r->radius_dist;
+  return o.str();
+}
+
+int64_t rng_size(const hg_resampler *r) {
+  return 8 + 4 + 4 * Mt19937::N + 4 + 8 + (int64_t)rng_text(r, 0).size() + 8 +
+         (int64_t)rng_text(r, 1).size();
+}
+
+} // namespace
+
+hg_status hg_resampler_rng_bytes(hg_resampler *r, int64_t *bytes) {
+  if (!r || !bytes) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  *bytes = rng_size(r);
+  return HG_OK;
+}
+
+hg_status hg_resampler_rng_save(hg_resampler *r, void *dst, int64_t bytes) {
+  if (!r || !dst) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (bytes < rng_size(r)) return fail(HG_ERR_CAPACITY, "RNG buffer too small");
+  unsigned char *o = static_cast<unsigned char *>(dst);
+  auto put = [&](const void *p, size_t n) {
+    std::memcpy(o, p, n);
+    o += n;
+  };
+  put(RNG_MAGIC, 8);
+  const int32_t pos = r->mt.i, tid = r->test_id;
+  put(&pos, 4);
+  put(r->mt.s, 4 * Mt19937::N);
+  put(&tid, 4);
+  for (int w = 0; w < 2; ++w) {
+    const std::string t = rng_text(r, w);
+    const int64_t len = (int64_t)t.size();
+    put(&len, 8);
+    put(t.data(), t.size());
+  }
+  return HG_OK;
+}
+
+hg_status hg_resampler_rng_load(hg_resampler *r, const void *src, int64_t bytes) {
+  if (!r || !src) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
+  const unsigned char *p = static_cast<const unsigned char *>(src), *end = p + bytes;
+  auto get = [&](void *d, size_t n) {
+    if (p + n > end) return false;
+    std::memcpy(d, p, n);
+    p += n;
+    return true;
+  };
+  char magic[8];
+  int32_t pos = 0, tid = 0;
+  Mt19937 mt;
+  if (!get(magic, 8) || std::memcmp(magic, RNG_MAGIC, 8) != 0 || !get(&pos, 4) ||
+      !get(mt.s, 4 * Mt19937::N) || !get(&tid, 4) || pos < 0 || pos > Mt19937::N + 1)
+    return fail(HG_ERR_INVALID_ARGUMENT, "not a resampler RNG blob");
+  std::string text[2];
+  for (int w = 0; w < 2; ++w) {
+    int64_t len = 0;
+    if (!get(&len, 8) || len < 0 || p + len > end)
+      return fail(HG_ERR_INVALID_ARGUMENT, "truncated resampler RNG blob");
+    text[w].assign(reinterpret_cast<const char *>(p), (size_t)len);
+    p += len;
+  }
+  std::default_random_engine gen;
+  std::normal_distribution<double> dist;
+  std::istringstream a(text[0]), b(text[1]);
+  a >> gen;
+  b >> dist;
+  if (a.fail() || b.fail()) return fail(HG_ERR_INVALID_ARGUMENT, "malformed resampler RNG blob");
+  mt.i = pos;
+  r->mt = mt;
+  r->gen = gen;
+  r->radius_dist = dist;
+  r->test_id = tid;
+  return HG_OK;
+}
+
 hg_status hg_resampler_destroy(hg_resampler *r) {
   delete r;
   return HG_OK;
@@ -787,6 +876,7 @@ hg_status hg_resampler_set_homogenized(hg_resampler *r, const double *stress, co
 }
 
 hg_status hg_resampler_run(hg_resampler *r, hg_zones *z) {
+  HG_TRACE("hg_resampler_run");
   if (!r || !z) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
   const hg_zones_desc &a = r->d.zones, &b = z->d;
   if (a.mpm_cells[0] != b.mpm_cells[0] || a.mpm_cells[1] != b.mpm_cells[1] ||

@@ -381,6 +381,7 @@ hg_status hg_zones_destroy(hg_zones *z) {
 
 hg_status hg_zones_update(hg_zones *z, int64_t n_disks, const double *q, const double *radius,
                           const uint8_t *fixed, int64_t n_points, const double *points) {
+  HG_TRACE("hg_zones_update");
   if (!z) return fail(HG_ERR_INVALID_ARGUMENT, "z is NULL");
   if (n_disks < 0 || n_points < 0) return fail(HG_ERR_INVALID_ARGUMENT, "negative count");
   if ((n_disks > 0 && (!q || !radius)) || (n_points > 0 && !points))

@@ -138,3 +138,34 @@ class HybridSim:
 
     def counts(self):
         return self.mpm.n, self.dem.n
+
+    def save(self, path):
+        """Checkpoint: the device objects' state, the zone labels, the
+        resampler's random streams and the host arrays of the interval."""
+        from . import checkpoint
+        arrays = dict(mpm=self.mpm.state(), dem=self.dem.state(), hybrid=self.hyb.state(),
+                      rng=self.res.rng_state(), labels=self.zones.fields()["mpm"])
+        for k, v in self.P.items():
+            arrays["P." + k] = v
+        for k, v in self.G.items():
+            arrays["G." + k] = v
+        meta = dict(counter=self.counter, started=self.started, resamplings=self.resamplings,
+                    steps=self.steps, stats=self.stats)
+        checkpoint.write(path, arrays, meta)
+
+    def restore(self, path):
+        """Resumes from ``save`` into a simulation built from the same scene."""
+        from . import checkpoint
+        arrays, meta = checkpoint.read(path)
+        self.mpm.load_state(arrays["mpm"])
+        self.dem.load_state(arrays["dem"])
+        self.hyb.load_state(arrays["hybrid"])
+        self.res.load_rng_state(arrays["rng"])
+        self.zones.set_labels(arrays["labels"])
+        self.P = {k[2:]: v for k, v in arrays.items() if k.startswith("P.")}
+        self.G = {k[2:]: v for k, v in arrays.items() if k.startswith("G.")}
+        self.counter = meta["counter"]
+        self.started = meta["started"]
+        self.resamplings = meta["resamplings"]
+        self.steps = meta["steps"]
+        self.stats = list(meta["stats"])
