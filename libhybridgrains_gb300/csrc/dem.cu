@@ -203,6 +203,7 @@ struct PairArgs {
   int nplanes;
   int32_t *cnt;       // 3N counts [kind][body]
   uint32_t *plist;    // PW partners per body (fixed partners flagged by bit 31)
+  int32_t *pfill;     // partners credited to each body (counting pass)
   const int32_t *off; // 3N+1 offsets (emit pass)
   int64_t *keys;      // emit pass output
   int64_t ccap;
@@ -264,32 +265,77 @@ __device__ __forceinline__ void for_each_partner(const PairArgs &A, int a, F &&f
   }
 }
 
-// Counting pass: per-kind counts, and the first PW partners in plist.
+// Counting pass over half of each neighbourhood: the home cell and the four
+// cells after it in (dy, dx) order. A pair of bodies in different cells is
+// met from exactly one of them (the offset from one home cell to the other is
+// in the half, its negative is not); a pair within one cell is met from both
+// and kept from the lower index. Each contact is credited to its first body
+// (the lower index of two free bodies, the free body of a free-fixed pair,
+// none for two fixed bodies) with atomics: per-kind counts, capped at MAXP,
+// and the first PW partners in plist (in no particular order; the emission
+// pass sorts them). The survivors of the FP32 filter take the same FP64 tests
+// as the full search, which are symmetric in the two bodies.
+__constant__ int HALF_CELLS[5][2] = {{0, 0}, {1, 0}, {-1, 1}, {0, 1}, {1, 1}};
+
+__device__ __forceinline__ void credit(const PairArgs &A, int first, int second, bool kin,
+                                       bool &overflow) {
+  int32_t *c = A.cnt + (kin ? 2 : 1) * A.n + first;
+  if (atomicAdd(c, 1) >= MAXP) {
+    atomicSub(c, 1);
+    overflow = true;
+    return;
+  }
+  const int slot = atomicAdd(A.pfill + first, 1);
+  if (slot < PW) A.plist[(int64_t)first * PW + slot] = (uint32_t)second | (kin ? 0x80000000u : 0u);
+}
+
 __global__ void kd_pairs_count(PairArgs A) {
   const int64_t n = A.n;
   const int a = (int)(blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
   if (a >= n) return;
-  int ncc = 0, nkin = 0, npl = 0;
+  const float4 pa = A.rec[2 * a], ca = A.rec[2 * a + 1];
+  const uint32_t flags = __float_as_uint(pa.w);
+  const bool af = (flags & REL_FIXED) != 0u;
+  if (!af) A.cnt[a] = __popc(flags >> 1); // static planes
+  const int2 ha = make_int2(__float_as_int(ca.x), __float_as_int(ca.y));
+  const double xa = A.q[3 * a], ya = A.q[3 * a + 1], ra = A.r[a];
+  int bs[5], be[5];
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    const uint32_t bk = cell_hash(ha.x + HALF_CELLS[c][0], ha.y + HALF_CELLS[c][1], A.mask);
+    be[c] = A.bucket_end[bk];
+    bs[c] = be[c] - A.bucket_count[bk];
+  }
   bool overflow = false;
-  const uint32_t flags = __float_as_uint(A.rec[2 * a].w);
-  if (!(flags & REL_FIXED)) {
-    uint32_t *lst = A.plist + (int64_t)a * PW;
-    for_each_partner(A, a, [&](int b, bool bf) {
-      int &c = bf ? nkin : ncc;
-      if (c >= MAXP) {
-        overflow = true;
-        return;
-      }
-      const int t = ncc + nkin;
-      if (t < PW) lst[t] = (uint32_t)b | (bf ? 0x80000000u : 0u);
-      ++c;
-    });
-    npl = __popc(flags >> 1);
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    const int dx = HALF_CELLS[c][0], dy = HALF_CELLS[c][1];
+    const int cx = ha.x + dx, cy = ha.y + dy;
+    for (int k = bs[c]; k < be[c]; ++k) {
+      const int b = A.items[k];
+      if (b == a || (c == 0 && b < a)) continue;
+      const float4 pb = A.rec[2 * b], cb = A.rec[2 * b + 1];
+      if (__float_as_int(cb.x) != cx || __float_as_int(cb.y) != cy)
+        continue; // bucket shared by another cell
+      const bool bf = (__float_as_uint(pb.w) & REL_FIXED) != 0u;
+      if (af && bf) continue;
+      const float reach = pa.z + pb.z + A.tol;
+      const float ex = (float)dx * A.Hf + (pb.x - pa.x);
+      const float ey = (float)dy * A.Hf + (pb.y - pa.y);
+      if (ex * ex + ey * ey > reach * reach) continue;
+      const double xb = A.q[3 * b], yb = A.q[3 * b + 1], rb = A.r[b];
+      if (!((xa + ra >= xb - rb && ya + ra >= yb - rb) &&
+            (xb + rb >= xa - ra && yb + rb >= ya - ra)))
+        continue;
+      const double ddx = xa - xb, ddy = ya - yb;
+      const double c0 = (ddx * ddx + ddy * ddy) - (ra + rb) * (ra + rb);
+      if (!(c0 <= 0.0)) continue;
+      if (af) credit(A, b, a, true, overflow);
+      else if (bf) credit(A, a, b, true, overflow);
+      else credit(A, min(a, b), max(a, b), false, overflow);
+    }
   }
   if (overflow) atomicOr(A.status, (uint32_t)HG_STATUS_CELL_OVERFLOW);
-  A.cnt[a] = npl;
-  A.cnt[n + a] = ncc;
-  A.cnt[2 * n + a] = nkin;
 }
 
 // Emission pass: sorted per-body contact keys at the scanned offsets. Lists
@@ -697,7 +743,7 @@ hg_status dem_alloc(hg_dem *d) {
   if ((st = d->status.alloc(1)) || (st = d->q.alloc(3 * N)) || (st = d->v.alloc(3 * N)) ||
       (st = d->r.alloc(N)) || (st = d->m0.alloc(N)) || (st = d->I0.alloc(N)) ||
       (st = d->w.alloc(N)) || (st = d->minv.alloc(2 * N)) || (st = d->fixed.alloc(N)) ||
-      (st = d->brec.alloc(2 * N)) || (st = d->plist.alloc(PW * N)) ||
+      (st = d->brec.alloc(2 * N)) || (st = d->pfill.alloc(N)) || (st = d->plist.alloc(PW * N)) ||
       (st = d->bcount.alloc(T)) || (st = d->bstart.alloc(T)) ||
       (st = d->items.alloc(N)) || (st = d->scan_tmp.alloc(tmp)) ||
       (st = d->c_count.alloc(2)) || (st = d->per_body.alloc(3 * N + 1)) ||
@@ -784,7 +830,9 @@ hg_status dem_step(hg_dem *d, double dt, int weighted) {
   A.ccap = d->ccap;
   A.overflow = d->overflow.p;
   A.status = d->status.p;
-  HG_CUDA_TRY(cudaMemsetAsync(d->per_body.p + 3 * n, 0, sizeof(int32_t), s));
+  A.pfill = d->pfill.p;
+  HG_CUDA_TRY(cudaMemsetAsync(d->per_body.p, 0, sizeof(int32_t) * (3 * n + 1), s));
+  HG_CUDA_TRY(cudaMemsetAsync(d->pfill.p, 0, sizeof(int32_t) * n, s));
   HG_LAUNCH(kd_pairs_count, blocks_for(n, 128), 128, 0, s, A);
   HG_CHECK_LAUNCH();
   if ((st = exclusive_scan_i32(d->per_body.p, d->per_body_off.p, 3 * n + 1, d->scan_tmp.p, s)))

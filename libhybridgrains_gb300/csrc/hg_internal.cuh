@@ -356,6 +356,7 @@ struct hg_dem {
   // per body, 32 bytes: FP32 offset from the home cell, radius, flags; home cell
   hg::DevBuf<float4> brec;
   hg::DevBuf<uint32_t> plist;  // partners kept by the counting pass
+  hg::DevBuf<int32_t> pfill;   // partners credited per body in the counting pass
   hg::DevBuf<int32_t> bcount, bstart, items; // bstart holds bucket ends after the fill
   hg::DevBuf<int32_t> scan_tmp;
   // contacts: current and previous, sorted by (kind, first, second)
