@@ -1397,7 +1397,7 @@ hg_status hg_dem_step(hg_dem *d, double dt, int32_t nsteps, int32_t weighted) {
   if (nsteps >= 4 && d->n > 0) {
     // Repeated steps replay a captured pair of steps: one graph launch in
     // place of about 40 kernel launches and memsets.
-    hg_status st = dem_prepare(d);
+    hg_status st = dem_prepare(d, dt);
     if (st == HG_OK) st = dem_pair_graph(d, dt, weighted);
     if (st != HG_OK) return st;
     for (; k + 2 <= nsteps; k += 2) {

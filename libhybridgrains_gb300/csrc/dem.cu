@@ -175,16 +175,18 @@ __global__ void kd_fill_ends(int64_t n, uint32_t mask, const float4 *__restrict_
       (int32_t)i;
 }
 
-// 1 / (m0 w) and 1 / (I0 w): the inverse masses of kd_integrate
-// (RigidBody2DState::updateCurrentMassUsingMassWeights), recomputed when
-// masses or weights change.
-__global__ void kd_inverse_masses(int64_t n, const double *__restrict__ m0,
-                                  const double *__restrict__ I0, const double *__restrict__ w,
-                                  double *inv) {
+// The per-body terms of kd_integrate that change only with the masses, the
+// weights or the time step, with kd_integrate's operations: the gravity
+// force 0 + M g (NearEarthGravityForce::computeForce) and dt / M, dt / Mi
+// written as dt * (1 / M) (M = m0 w, Mi = I0 w:
+// RigidBody2DState::updateCurrentMassUsingMassWeights).
+__global__ void kd_body_terms(int64_t n, double dt, double gx, double gy,
+                              const double *__restrict__ m0, const double *__restrict__ I0,
+                              const double *__restrict__ w, double4 *terms) {
   const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (j >= n) return;
-  inv[2 * j] = 1.0 / (m0[j] * w[j]);
-  inv[2 * j + 1] = 1.0 / (I0[j] * w[j]);
+  const double M = m0[j] * w[j], Mi = I0[j] * w[j];
+  terms[j] = make_double4(0.0 + M * gx, 0.0 + M * gy, dt * (1.0 / M), dt * (1.0 / Mi));
 }
 
 constexpr int PW = 8; // partners per body kept by the counting pass
@@ -581,9 +583,8 @@ __global__ void kd_in_fill(int64_t n, const int32_t *__restrict__ off,
   }
 }
 
-__global__ void kd_integrate(int64_t n, double dt, double gx, double gy, double *q, double *v,
-                             const double *__restrict__ m0, const double *__restrict__ w,
-                             const double *__restrict__ inv_mass,
+__global__ void kd_integrate(int64_t n, double dt, double *q, double *v,
+                             const double4 *__restrict__ terms,
                              const uint8_t *__restrict__ fixed,
                              const int32_t *__restrict__ cnt, const int32_t *__restrict__ off,
                              const double *__restrict__ rec, const int32_t *__restrict__ in_count,
@@ -591,10 +592,9 @@ __global__ void kd_integrate(int64_t n, double dt, double gx, double gy, double 
                              uint32_t *status) {
   const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (j >= n) return;
-  // RigidBody2DState::updateCurrentMassUsingMassWeights; 1 / M and 1 / Mi
-  // come from kd_inverse_masses
-  const double M = m0[j] * w[j];
-  double Fx = 0.0 + M * gx, Fy = 0.0 + M * gy, T = 0.0;
+  // gravity and dt / M, dt / Mi from kd_body_terms
+  const double4 bt = terms[j];
+  double Fx = bt.x, Fy = bt.y, T = 0.0;
   auto total = [&](int64_t k, D2 &f) {
     const double *r = rec + k * RW;
     f = dadd(D2{r[17], r[18]}, D2{r[19], r[20]});
@@ -647,10 +647,9 @@ __global__ void kd_integrate(int64_t n, double dt, double gx, double gy, double 
   }
   if (fixed[j]) Fx = Fy = T = 0.0;
   // v1 = v0 + dt Minv F ; q1 = q0 + dt v1
-  const double im = inv_mass[2 * j], iI = inv_mass[2 * j + 1];
-  const double v0 = v[3 * j] + (dt * im) * Fx;
-  const double v1 = v[3 * j + 1] + (dt * im) * Fy;
-  const double v2 = v[3 * j + 2] + (dt * iI) * T;
+  const double v0 = v[3 * j] + bt.z * Fx;
+  const double v1 = v[3 * j + 1] + bt.z * Fy;
+  const double v2 = v[3 * j + 2] + bt.w * T;
   v[3 * j] = v0;
   v[3 * j + 1] = v1;
   v[3 * j + 2] = v2;
@@ -742,7 +741,7 @@ hg_status dem_alloc(hg_dem *d) {
   hg_status st;
   if ((st = d->status.alloc(1)) || (st = d->q.alloc(3 * N)) || (st = d->v.alloc(3 * N)) ||
       (st = d->r.alloc(N)) || (st = d->m0.alloc(N)) || (st = d->I0.alloc(N)) ||
-      (st = d->w.alloc(N)) || (st = d->minv.alloc(2 * N)) || (st = d->fixed.alloc(N)) ||
+      (st = d->w.alloc(N)) || (st = d->minv.alloc(4 * N)) || (st = d->fixed.alloc(N)) ||
       (st = d->brec.alloc(2 * N)) || (st = d->pfill.alloc(N)) || (st = d->plist.alloc(PW * N)) ||
       (st = d->bcount.alloc(T)) || (st = d->bstart.alloc(T)) ||
       (st = d->items.alloc(N)) || (st = d->scan_tmp.alloc(tmp)) ||
@@ -766,12 +765,13 @@ hg_status dem_reset_history(hg_dem *d) {
   return HG_OK;
 }
 
-hg_status dem_prepare(hg_dem *d) {
-  if (d->inv_valid || d->n == 0) return HG_OK;
-  HG_LAUNCH(kd_inverse_masses, blocks_for(d->n, 256), 256, 0, d->ctx->stream, d->n, d->m0.p,
-            d->I0.p, d->w.p, d->minv.p);
+hg_status dem_prepare(hg_dem *d, double dt) {
+  if ((d->inv_valid && d->terms_dt == dt) || d->n == 0) return HG_OK;
+  HG_LAUNCH(kd_body_terms, blocks_for(d->n, 256), 256, 0, d->ctx->stream, d->n, dt, d->p.g[0],
+            d->p.g[1], d->m0.p, d->I0.p, d->w.p, reinterpret_cast<double4 *>(d->minv.p));
   HG_CHECK_LAUNCH();
   d->inv_valid = true;
+  d->terms_dt = dt;
   return HG_OK;
 }
 
@@ -780,7 +780,7 @@ hg_status dem_step(hg_dem *d, double dt, int weighted) {
   const int64_t n = d->n;
   if (n == 0) return HG_OK;
   hg_status st;
-  if ((st = dem_prepare(d))) return st;
+  if ((st = dem_prepare(d, dt))) return st;
   // the hash table grows with the live body count (at most the capacity's)
   const uint32_t mask = (1u << table_bits(n)) - 1u;
   {
@@ -884,8 +884,9 @@ hg_status dem_step(hg_dem *d, double dt, int weighted) {
   HG_LAUNCH(kd_in_fill, d->ctx->num_sms * 2, 256, 0, s, n, d->per_body_off.p, d->ckey[nb].p,
             d->in_off.p, d->in_cursor.p, d->in_list.p);
   HG_CHECK_LAUNCH();
-  HG_LAUNCH(kd_integrate, blocks_for(n, 128), 128, 0, s, n, dt, d->p.g[0], d->p.g[1], d->q.p,
-            d->v.p, d->m0.p, d->w.p, d->minv.p, d->fixed.p, d->per_body.p, d->per_body_off.p,
+  HG_LAUNCH(kd_integrate, blocks_for(n, 128), 128, 0, s, n, dt, d->q.p, d->v.p,
+            reinterpret_cast<const double4 *>(d->minv.p), d->fixed.p, d->per_body.p,
+            d->per_body_off.p,
             d->crec[nb].p, d->in_count.p, d->in_off.p, d->in_list.p, d->status.p);
   HG_CHECK_LAUNCH();
   d->cc = nb;

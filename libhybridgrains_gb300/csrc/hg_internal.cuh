@@ -347,8 +347,10 @@ struct hg_dem {
   hg::DevBuf<uint32_t> status;
   // bodies
   hg::DevBuf<double> q, v, r, m0, I0, w;
-  hg::DevBuf<double> minv; // 1 / (m0 w), 1 / (I0 w) per body
-  bool inv_valid = false;  // minv matches m0, I0 and w
+  // per body (as double4): gravity force x, y; dt / M; dt / Mi
+  hg::DevBuf<double> minv;
+  bool inv_valid = false;  // minv matches m0, I0, w and terms_dt
+  double terms_dt = 0.0;
   hg::DevBuf<uint8_t> fixed;
   // broadphase: hash grid of cell width H over the AABB minima
   double cell_h = 0.0;
@@ -391,9 +393,9 @@ hg_status dem_edit(hg_dem *d, int64_t n_old, const int32_t *old_to_new, int64_t 
                    int64_t n_add, const double *q, const double *v, const double *r,
                    const double *m, const double *I, const uint8_t *fixed);
 hg_status dem_step(hg_dem *d, double dt, int weighted);
-// per-body data that dem_step needs and that only changes with the bodies
-// (inverse masses); called before a step is captured into a graph
-hg_status dem_prepare(hg_dem *d);
+// per-body terms that dem_step needs and that only change with the bodies
+// or the time step; called before a step is captured into a graph
+hg_status dem_prepare(hg_dem *d, double dt);
 hg_status dem_download_contacts(hg_dem *d, int64_t cap, double *rec,
                                 int64_t *count);
 hg_status dem_candidate_pairs(hg_context *ctx, int64_t n, const double *mn,
