@@ -91,4 +91,55 @@ __host__ __device__ __forceinline__ void weight_grad64(int basis, double x, doub
   oy = wx * lin_integral_grad(y, hl, xiy, h) / Vp;
 }
 
+// Per-axis factors over a stencil of at most STENCIL_AXIS nodes from i0: a
+// is the 1-D weight and b its derivative factor (linear: N(d) and dN(d) of
+// d = ((x - h i) - g) / h; uGIMP: lin_integral and lin_integral_grad at
+// x_i = h i + g). The 2-D weight and gradient are products of these in the
+// order weight64 and weight_grad64 use, so they come out bit for bit the same
+// while each 1-D factor is evaluated once per axis instead of once per node.
+constexpr int STENCIL_AXIS = 4;
+
+__host__ __device__ __forceinline__ void axis_factors(int basis, double x, double hl, int i0,
+                                                      int count, double g, double h,
+                                                      double a[STENCIL_AXIS],
+                                                      double b[STENCIL_AXIS]) {
+#pragma unroll
+  for (int k = 0; k < STENCIL_AXIS; ++k) {
+    a[k] = 0.0;
+    b[k] = 0.0;
+    if (k >= count) continue;
+    const int i = i0 + k;
+    if (basis == HG_BASIS_LINEAR) {
+      const double d = ((x - h * (double)i) - g) / h;
+      a[k] = linear_n(d);
+      b[k] = linear_dn(d);
+    } else {
+      const double xi = h * (double)i + g;
+      a[k] = lin_integral(x, hl, xi, h);
+      b[k] = lin_integral_grad(x, hl, xi, h);
+    }
+  }
+}
+
+// weight64 from the axis factors
+__host__ __device__ __forceinline__ double weight_ax(int basis, double ax, double ay, double hl) {
+  if (basis == HG_BASIS_LINEAR) return ax * ay;
+  const double Vp = 4.0 * hl * hl;
+  return ax * ay / Vp;
+}
+
+// weight_grad64 from the axis factors
+__host__ __device__ __forceinline__ void grad_ax(int basis, double ax, double bx, double ay,
+                                                 double by, double hl, double h, double &ox,
+                                                 double &oy) {
+  if (basis == HG_BASIS_LINEAR) {
+    ox = (ay * bx) / h;
+    oy = (ax * by) / h;
+    return;
+  }
+  const double Vp = 4.0 * hl * hl;
+  ox = ay * bx / Vp;
+  oy = ax * by / Vp;
+}
+
 } // namespace hg

@@ -131,20 +131,40 @@ __global__ void k64_p2g(MpmParams P, int64_t n, const double *__restrict__ q,
   const double mp = m[p];
   const double pmx = mp * v[2 * p], pmy = mp * v[2 * p + 1];
   const double c = -vol[p] * Jp;
+  auto node = [&](int ix, int iy, double w, double gx, double gy) {
+    const int64_t i = (int64_t)iy * (P.nx + 1) + ix;
+    atomicAdd(&g_mass[i], w * mp);
+    atomicAdd(&g_mom[2 * i], w * pmx);
+    atomicAdd(&g_mom[2 * i + 1], w * pmy);
+    if (w == 0.0) return;
+    const double swx = sg.a00 * gx + sg.a01 * gy;
+    const double swy = sg.a10 * gx + sg.a11 * gy;
+    atomicAdd(&g_force[2 * i], c * swx);
+    atomicAdd(&g_force[2 * i + 1], c * swy);
+  };
+  const int nxs = x1 - x0 + 1, nys = y1 - y0 + 1;
+  if (nxs <= STENCIL_AXIS && nys <= STENCIL_AXIS) {
+    double ax[STENCIL_AXIS], bx[STENCIL_AXIS], ay[STENCIL_AXIS], by[STENCIL_AXIS];
+    axis_factors(P.basis, x, h, x0, nxs, P.gmin[0], P.h, ax, bx);
+    axis_factors(P.basis, y, h, y0, nys, P.gmin[1], P.h, ay, by);
+#pragma unroll
+    for (int ky = 0; ky < STENCIL_AXIS; ++ky) {
+      if (ky >= nys) break;
+#pragma unroll
+      for (int kx = 0; kx < STENCIL_AXIS; ++kx) {
+        if (kx >= nxs) break;
+        double gx, gy;
+        grad_ax(P.basis, ax[kx], bx[kx], ay[ky], by[ky], h, P.h, gx, gy);
+        node(x0 + kx, y0 + ky, weight_ax(P.basis, ax[kx], ay[ky], h), gx, gy);
+      }
+    }
+    return;
+  }
   for (int iy = y0; iy <= y1; ++iy)
     for (int ix = x0; ix <= x1; ++ix) {
-      const double w = weight64(P.basis, x, y, h, ix, iy, P.gmin[0], P.gmin[1], P.h);
-      const int64_t i = (int64_t)iy * (P.nx + 1) + ix;
-      atomicAdd(&g_mass[i], w * mp);
-      atomicAdd(&g_mom[2 * i], w * pmx);
-      atomicAdd(&g_mom[2 * i + 1], w * pmy);
-      if (w == 0.0) continue;
       double gx, gy;
       weight_grad64(P.basis, x, y, h, ix, iy, P.gmin[0], P.gmin[1], P.h, gx, gy);
-      const double swx = sg.a00 * gx + sg.a01 * gy;
-      const double swy = sg.a10 * gx + sg.a11 * gy;
-      atomicAdd(&g_force[2 * i], c * swx);
-      atomicAdd(&g_force[2 * i + 1], c * swy);
+      node(ix, iy, weight64(P.basis, x, y, h, ix, iy, P.gmin[0], P.gmin[1], P.h), gx, gy);
     }
 }
 
@@ -241,16 +261,46 @@ __global__ void k64_g2p(MpmParams P, double dt, int64_t n, double *q, double *v,
     return;
   }
   const int64_t row = P.nx + 1;
+  // axis factors of the start-of-step position (when the stencil fits)
+  const int nxs = x1 - x0 + 1, nys = y1 - y0 + 1;
+  const bool fits = nxs <= STENCIL_AXIS && nys <= STENCIL_AXIS;
+  double ax[STENCIL_AXIS], bx[STENCIL_AXIS], ay[STENCIL_AXIS], by[STENCIL_AXIS];
+  if (fits) {
+    axis_factors(P.basis, x, h, x0, nxs, P.gmin[0], P.h, ax, bx);
+    axis_factors(P.basis, y, h, y0, nys, P.gmin[1], P.h, ay, by);
+  }
+  // visits the stencil's nodes in the reference's order with their weight
+  // and weight gradient
+  auto each_node = [&](auto &&f) {
+    if (fits) {
+#pragma unroll
+      for (int ky = 0; ky < STENCIL_AXIS; ++ky) {
+        if (ky >= nys) break;
+#pragma unroll
+        for (int kx = 0; kx < STENCIL_AXIS; ++kx) {
+          if (kx >= nxs) break;
+          double gx, gy;
+          grad_ax(P.basis, ax[kx], bx[kx], ay[ky], by[ky], h, P.h, gx, gy);
+          f((int64_t)(y0 + ky) * row + (x0 + kx), weight_ax(P.basis, ax[kx], ay[ky], h), gx,
+            gy);
+        }
+      }
+      return;
+    }
+    for (int iy = y0; iy <= y1; ++iy)
+      for (int ix = x0; ix <= x1; ++ix) {
+        double gx, gy;
+        weight_grad64(P.basis, x, y, h, ix, iy, P.gmin[0], P.gmin[1], P.h, gx, gy);
+        f((int64_t)iy * row + ix, weight64(P.basis, x, y, h, ix, iy, P.gmin[0], P.gmin[1], P.h),
+          gx, gy);
+      }
+  };
   // computeVelGrad (MaterialPoints.cpp:296-322)
   M2d L{0.0, 0.0, 0.0, 0.0};
-  for (int iy = y0; iy <= y1; ++iy)
-    for (int ix = x0; ix <= x1; ++ix) {
-      double gx, gy;
-      weight_grad64(P.basis, x, y, h, ix, iy, P.gmin[0], P.gmin[1], P.h, gx, gy);
-      const int64_t i = iy * row + ix;
-      const double vx = g_vel[2 * i], vy = g_vel[2 * i + 1];
-      L = m_add(L, M2d{vx * gx, vy * gx, vx * gy, vy * gy});
-    }
+  each_node([&](int64_t i, double, double gx, double gy) {
+    const double vx = g_vel[2 * i], vy = g_vel[2 * i + 1];
+    L = m_add(L, M2d{vx * gx, vy * gx, vx * gy, vy * gy});
+  });
   // elasticPrediction (MaterialPoints.cpp:324-348, ConstitutiveModel.cpp:19-22)
   double Jp = J[p];
   M2d bb = load_m(be, p);
@@ -270,15 +320,12 @@ __global__ void k64_g2p(MpmParams P, double dt, int64_t n, double *q, double *v,
   // updateVelocities (MaterialPoints.cpp:204-245) and updatePositions
   // (247-288); both read the grid at the start-of-step position.
   double vpx = 0.0, vpy = 0.0, apx = 0.0, apy = 0.0, gvx = 0.0, gvy = 0.0;
-  for (int iy = y0; iy <= y1; ++iy)
-    for (int ix = x0; ix <= x1; ++ix) {
-      const double w = weight64(P.basis, x, y, h, ix, iy, P.gmin[0], P.gmin[1], P.h);
-      const int64_t i = iy * row + ix;
-      vpx = vpx + w * g_vel[2 * i];
-      vpy = vpy + w * g_vel[2 * i + 1];
-      apx = apx + w * g_acc[2 * i];
-      apy = apy + w * g_acc[2 * i + 1];
-    }
+  each_node([&](int64_t i, double w, double, double) {
+    vpx = vpx + w * g_vel[2 * i];
+    vpy = vpy + w * g_vel[2 * i + 1];
+    apx = apx + w * g_acc[2 * i];
+    apy = apy + w * g_acc[2 * i + 1];
+  });
   gvx = vpx;
   gvy = vpy;
   double vx = v[2 * p], vy = v[2 * p + 1];

@@ -120,6 +120,17 @@ __device__ __forceinline__ bool in_grid_cell(const MixedArgs &A, int cx, int cy)
   return cx >= 0 && cy >= 0 && cx < A.nx && cy < A.ny;
 }
 
+// A point exactly on the grid's far edge (where a plane at the grid bound
+// projects it) is taken as the last cell at fraction 1: the same weights and
+// no node beyond the grid (the reference's stencil would reach one node past
+// its arrays there, with weight 0).
+__device__ __forceinline__ void far_edge(int n, int &c, float &f) {
+  if (c == n && f == 0.0f) {
+    c = n - 1;
+    f = 1.0f;
+  }
+}
+
 // Elastic prediction + Drucker-Prager plastic correction on offset-form
 // strain (ConstitutiveModel.cpp:19-81, MaterialPoints.cpp:324-369).
 // B = be - I; det(I + B) = 1 + t with t = tr B + det B.
@@ -343,6 +354,8 @@ __device__ __forceinline__ void fused_tile(const MixedArgs &A, const int bin, Fu
       float fx, fy;
       split_u(u.x, cx, fx);
       split_u(u.y, cy, fy);
+      far_edge(A.nx, cx, fx);
+      far_edge(A.ny, cy, fy);
       if (!in_grid_cell(A, cx, cy)) {
         atomicOr(A.status, (uint32_t)HG_STATUS_OUT_OF_GRID);
         continue;
@@ -430,10 +443,15 @@ __device__ __forceinline__ void fused_tile(const MixedArgs &A, const int bin, Fu
             vel = make_float2(0.0f, 0.0f);
           }
         }
-        if (exact) {
+        if (exact || !in_grid_cell(A, ncx, ncy)) {
+          // (also when the FP32 carry put a point just inside the low edge in
+          // cell -1, its fraction rounded down and its step rounded up: the
+          // FP64 position decides)
           split_u(un.x, ncx, nfx);
           split_u(un.y, ncy, nfy);
         }
+        far_edge(A.nx, ncx, nfx);
+        far_edge(A.ny, ncy, nfy);
         nonfinite |= !finite_d(un.x) | !finite_d(un.y) | !isfinite(vel.x + vel.y) |
                      !isfinite(st.x);
         A.u[p] = un;
@@ -711,6 +729,9 @@ __global__ void kx_keys(int64_t n, int nx, int ny, int ntx, const double2 *__res
   // cpp:53-59) is floor(u) here: u was computed with exactly that division.
   const double2 up = u[p];
   int cx = (int)floor(up.x), cy = (int)floor(up.y);
+  // a point exactly on the far edge belongs to the last cell
+  if (up.x == (double)nx) cx = nx - 1;
+  if (up.y == (double)ny) cy = ny - 1;
   if (!(up.x >= 0.0 && up.y >= 0.0 && cx < nx && cy < ny)) {
     atomicOr(status, (uint32_t)HG_STATUS_OUT_OF_GRID);
     cx = min(max(cx, 0), nx - 1);
