@@ -62,12 +62,11 @@ __global__ void kc_grain_mass(GridGeom G, int64_t nb, const double *__restrict__
   if (!all_pos) return;
   coupled[b] = 1;
   const double pm = m0[b] * w[b]; // RigidBody2DState::getTotalMass
-  for (int iy = y0; iy <= y1; ++iy)
-    for (int ix = x0; ix <= x1; ++ix) {
-      if (!node_ok(G, ix, iy)) continue;
-      const double wt = weight64(G.basis, x, y, hl, ix, iy, G.gx, G.gy, G.h);
-      atomicAdd(&dem_mass[(int64_t)iy * (G.nx + 1) + ix], wt * pm);
-    }
+  for_stencil_weights(G.basis, x, y, hl, x0, y0, x1, y1, G.gx, G.gy, G.h,
+                      [&](int ix, int iy, double wt) {
+                        if (!node_ok(G, ix, iy)) return;
+                        atomicAdd(&dem_mass[(int64_t)iy * (G.nx + 1) + ix], wt * pm);
+                      });
 }
 
 __global__ void kc_flag_nodes(int64_t nn, const double *__restrict__ dem_mass, int32_t *flag) {
@@ -104,14 +103,13 @@ __global__ void kc_grain_mom(GridGeom G, const int32_t *__restrict__ count,
     stencil64(G.basis, x, y, hl, G.gx, G.gy, G.h, x0, y0, x1, y1);
     const double pm = m0[b] * w[b];
     const double px = pm * v[3 * b], py = pm * v[3 * b + 1];
-    for (int iy = y0; iy <= y1; ++iy)
-      for (int ix = x0; ix <= x1; ++ix) {
-        if (!node_ok(G, ix, iy)) continue;
-        const double wt = weight64(G.basis, x, y, hl, ix, iy, G.gx, G.gy, G.h);
-        const int64_t i = (int64_t)iy * (G.nx + 1) + ix;
-        atomicAdd(&dem_mom[2 * i], wt * px);
-        atomicAdd(&dem_mom[2 * i + 1], wt * py);
-      }
+    for_stencil_weights(G.basis, x, y, hl, x0, y0, x1, y1, G.gx, G.gy, G.h,
+                        [&](int ix, int iy, double wt) {
+                          if (!node_ok(G, ix, iy)) return;
+                          const int64_t i = (int64_t)iy * (G.nx + 1) + ix;
+                          atomicAdd(&dem_mom[2 * i], wt * px);
+                          atomicAdd(&dem_mom[2 * i + 1], wt * py);
+                        });
   }
 }
 
@@ -162,16 +160,15 @@ __global__ void kc_transfer(GridGeom G, const int32_t *__restrict__ count,
     int x0, y0, x1, y1;
     stencil64(G.basis, x, y, hl, G.gx, G.gy, G.h, x0, y0, x1, y1);
     double vpx = 0.0, vpy = 0.0, atx = 0.0, aty = 0.0;
-    for (int iy = y0; iy <= y1; ++iy)
-      for (int ix = x0; ix <= x1; ++ix) {
-        if (!node_ok(G, ix, iy)) continue;
-        const double wt = weight64(G.basis, x, y, hl, ix, iy, G.gx, G.gy, G.h);
-        const int64_t i = (int64_t)iy * (G.nx + 1) + ix;
-        vpx = vpx + wt * v_after[2 * i];
-        vpy = vpy + wt * v_after[2 * i + 1];
-        atx = atx + wt * a_after[2 * i];
-        aty = aty + wt * a_after[2 * i + 1];
-      }
+    for_stencil_weights(G.basis, x, y, hl, x0, y0, x1, y1, G.gx, G.gy, G.h,
+                        [&](int ix, int iy, double wt) {
+                          if (!node_ok(G, ix, iy)) return;
+                          const int64_t i = (int64_t)iy * (G.nx + 1) + ix;
+                          vpx = vpx + wt * v_after[2 * i];
+                          vpy = vpy + wt * v_after[2 * i + 1];
+                          atx = atx + wt * a_after[2 * i];
+                          aty = aty + wt * a_after[2 * i + 1];
+                        });
     const double fx = v[3 * b] + atx, fy = v[3 * b + 1] + aty;
     v[3 * b] = vpx * (1.0 - alpha) + fx * alpha;
     v[3 * b + 1] = vpy * (1.0 - alpha) + fy * alpha;
@@ -212,16 +209,15 @@ __global__ void kc_hstress(GridGeom G, int64_t nb, const int32_t *__restrict__ o
     const double s11 = -0.5 * (fy * ry + ry * fy);
     int x0, y0, x1, y1;
     stencil64(G.basis, px, py, hl, G.gx, G.gy, G.h, x0, y0, x1, y1);
-    for (int iy = y0; iy <= y1; ++iy)
-      for (int ix = x0; ix <= x1; ++ix) {
-        if (!node_ok(G, ix, iy)) continue;
-        const double wt = weight64(G.basis, px, py, hl, ix, iy, G.gx, G.gy, G.h);
-        const int64_t i = (int64_t)iy * (G.nx + 1) + ix;
-        atomicAdd(&hs[4 * i], wt * s00 / area);
-        atomicAdd(&hs[4 * i + 1], wt * s10 / area);
-        atomicAdd(&hs[4 * i + 2], wt * s01 / area);
-        atomicAdd(&hs[4 * i + 3], wt * s11 / area);
-      }
+    for_stencil_weights(G.basis, px, py, hl, x0, y0, x1, y1, G.gx, G.gy, G.h,
+                        [&](int ix, int iy, double wt) {
+                          if (!node_ok(G, ix, iy)) return;
+                          const int64_t i = (int64_t)iy * (G.nx + 1) + ix;
+                          atomicAdd(&hs[4 * i], wt * s00 / area);
+                          atomicAdd(&hs[4 * i + 1], wt * s10 / area);
+                          atomicAdd(&hs[4 * i + 2], wt * s01 / area);
+                          atomicAdd(&hs[4 * i + 3], wt * s11 / area);
+                        });
   }
 }
 
@@ -237,15 +233,14 @@ __global__ void kc_hvel_scatter(GridGeom G, int64_t nb, const double *__restrict
   const double x = q[3 * b], y = q[3 * b + 1];
   int x0, y0, x1, y1;
   stencil64(G.basis, x, y, hl, G.gx, G.gy, G.h, x0, y0, x1, y1);
-  for (int iy = y0; iy <= y1; ++iy)
-    for (int ix = x0; ix <= x1; ++ix) {
-      if (!node_ok(G, ix, iy)) continue;
-      const double wt = weight64(G.basis, x, y, hl, ix, iy, G.gx, G.gy, G.h);
-      const int64_t i = (int64_t)iy * (G.nx + 1) + ix;
-      atomicAdd(&hmom[2 * i], wt * mass * vx);
-      atomicAdd(&hmom[2 * i + 1], wt * mass * vy);
-      atomicAdd(&hmass[i], wt * mass);
-    }
+  for_stencil_weights(G.basis, x, y, hl, x0, y0, x1, y1, G.gx, G.gy, G.h,
+                      [&](int ix, int iy, double wt) {
+                        if (!node_ok(G, ix, iy)) return;
+                        const int64_t i = (int64_t)iy * (G.nx + 1) + ix;
+                        atomicAdd(&hmom[2 * i], wt * mass * vx);
+                        atomicAdd(&hmom[2 * i + 1], wt * mass * vy);
+                        atomicAdd(&hmass[i], wt * mass);
+                      });
 }
 
 __global__ void kc_hvel_finish(int64_t nn, const double *__restrict__ hmom,

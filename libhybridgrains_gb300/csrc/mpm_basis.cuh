@@ -121,6 +121,23 @@ __host__ __device__ __forceinline__ void axis_factors(int basis, double x, doubl
   }
 }
 
+// The 1-D weights alone (the a of axis_factors).
+__host__ __device__ __forceinline__ void axis_weights(int basis, double x, double hl, int i0,
+                                                      int count, double g, double h,
+                                                      double a[STENCIL_AXIS]) {
+#pragma unroll
+  for (int k = 0; k < STENCIL_AXIS; ++k) {
+    a[k] = 0.0;
+    if (k >= count) continue;
+    const int i = i0 + k;
+    if (basis == HG_BASIS_LINEAR) {
+      a[k] = linear_n(((x - h * (double)i) - g) / h);
+    } else {
+      a[k] = lin_integral(x, hl, h * (double)i + g, h);
+    }
+  }
+}
+
 // weight64 from the axis factors
 __host__ __device__ __forceinline__ double weight_ax(int basis, double ax, double ay, double hl) {
   if (basis == HG_BASIS_LINEAR) return ax * ay;
@@ -140,6 +157,33 @@ __host__ __device__ __forceinline__ void grad_ax(int basis, double ax, double bx
   const double Vp = 4.0 * hl * hl;
   ox = ay * bx / Vp;
   oy = ax * by / Vp;
+}
+
+// Visits the stencil's nodes in the reference's order (y outer, x inner) with
+// weight64 of each, the 1-D factors evaluated once per axis when the stencil
+// has at most STENCIL_AXIS nodes per axis.
+template <class F>
+__device__ __forceinline__ void for_stencil_weights(int basis, double x, double y, double hl,
+                                                    int x0, int y0, int x1, int y1, double gx,
+                                                    double gy, double h, F &&f) {
+  const int nxs = x1 - x0 + 1, nys = y1 - y0 + 1;
+  if (nxs <= STENCIL_AXIS && nys <= STENCIL_AXIS) {
+    double ax[STENCIL_AXIS], ay[STENCIL_AXIS];
+    axis_weights(basis, x, hl, x0, nxs, gx, h, ax);
+    axis_weights(basis, y, hl, y0, nys, gy, h, ay);
+#pragma unroll
+    for (int ky = 0; ky < STENCIL_AXIS; ++ky) {
+      if (ky >= nys) break;
+#pragma unroll
+      for (int kx = 0; kx < STENCIL_AXIS; ++kx) {
+        if (kx >= nxs) break;
+        f(x0 + kx, y0 + ky, weight_ax(basis, ax[kx], ay[ky], hl));
+      }
+    }
+    return;
+  }
+  for (int iy = y0; iy <= y1; ++iy)
+    for (int ix = x0; ix <= x1; ++ix) f(ix, iy, weight64(basis, x, y, hl, ix, iy, gx, gy, h));
 }
 
 } // namespace hg
