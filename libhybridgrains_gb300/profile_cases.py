@@ -1,0 +1,70 @@
+"""Small fixed workloads for kernel profilers (ncu launch lists and captures).
+
+    python -m libhybridgrains_gb300.profile_cases dem --disks 1000000 --steps 12
+    python -m libhybridgrains_gb300.profile_cases hybrid --steps 6
+    python -m libhybridgrains_gb300.profile_cases column --steps 8
+
+Each case builds its scene, runs one warm-up step, then ``--steps`` steps one
+call per step (so that every kernel is a separate launch a profiler can
+select), synchronises and prints the wall time per step and the status words.
+The DEM case is the DEM column's lattice at 1000 disks per row (dt 1e-5 s);
+the hybrid case is the hybrid column (100,000 points under 20,000 disks)
+after its initial resampling; the column case is the 2,000,000-point MIXED
+column.
+"""
+import argparse
+import time
+
+
+def main(argv=None):
+    import libhybridgrains_gb300 as hg
+    from libhybridgrains_gb300 import scenes, serving
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("case", choices=["dem", "hybrid", "column"])
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--disks", type=int, default=1000000)
+    args = ap.parse_args(argv)
+    ctx = hg.Context(0)
+    if args.case == "dem":
+        sc = scenes.dem_column(n=args.disks, per_row=1000)
+        obj = serving.dem_for_piles(ctx, args.disks)
+        obj.upload(sc["q"], sc["v"], sc["r"], sc["m"], sc["I"], sc["fixed"])
+
+        def step():
+            obj.flow(1.0e-5, 1)
+        status = obj.status
+    elif args.case == "hybrid":
+        from libhybridgrains_gb300.hybrid import HybridSim
+        sim = HybridSim(ctx, scenes.hybrid_column())
+        sim.step(1)
+
+        def step():
+            sim.hyb.step(sim.dt, 1, *sim.hom)
+
+        def status():
+            return sim.mpm.status(), sim.dem.status()
+    else:
+        cfg = scenes.mpm_column("column_2M")
+        p = scenes.seed_column_points(cfg)
+        obj = hg.MPM(ctx, cfg["grid_min"], cfg["grid_max"], cfg["h"], cfg["shear_modulus"],
+                     cfg["bulk_modulus"], cfg["dp_alpha"], cfg["flip_alpha"], scenes.GRAVITY,
+                     cfg["planes"], capacity=len(p["m"]))
+        obj.upload(p["q"], p["v"], p["m"], p["vol"], p["hl"])
+
+        def step():
+            obj.flow(cfg["dt"], 1)
+        status = obj.status
+    step()
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    ctx.synchronize()
+    ms = 1e3 * (time.perf_counter() - t0) / max(args.steps, 1)
+    print("%s: %d steps, %.3f ms/step (one call per step), status %s" %
+          (args.case, args.steps, ms, status()))
+
+
+if __name__ == "__main__":
+    main()
