@@ -473,6 +473,12 @@ typedef struct {
   hg_dem_plane planes[HG_MAX_PLANES];
   int64_t capacity;         /* bodies */
   int64_t contact_capacity; /* active contacts */
+  /* HG_PRECISION_FP64: the reference's FP64 arithmetic, bit for bit.
+   * HG_PRECISION_MIXED: contact law and integration in FP32; positions, the
+   * pairwise position difference, contact points and the position update in
+   * FP64 (velocities and records keep FP64 storage holding FP32 values). */
+  int32_t precision;
+  int32_t pad2_;
 } hg_dem_desc;
 
 hg_status hg_dem_create(hg_context *ctx, const hg_dem_desc *desc, hg_dem **out);

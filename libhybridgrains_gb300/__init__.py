@@ -383,7 +383,7 @@ class DEM:
     """Circle bodies with the penalty impact-friction map (rigidbody2d)."""
 
     def __init__(self, ctx, gravity, kn, kt, gamman, gammat, mu, planes=(), cell_scale=1.0,
-                 capacity=0, contact_capacity=0):
+                 capacity=0, contact_capacity=0, precision=0):
         self.ctx = ctx
         d = _capi.DemDesc()
         d.gravity[:] = list(map(float, gravity))
@@ -396,6 +396,8 @@ class DEM:
             d.planes[k].n[:] = list(map(float, n))
         d.capacity = int(capacity)
         d.contact_capacity = int(contact_capacity or 8 * max(capacity, 1))
+        d.precision = int(precision)
+        self.precision = int(precision)
         h = ctypes.c_void_p()
         check("hg_dem_create", ctx._h, ctypes.byref(d), ctypes.byref(h))
         self._h = h

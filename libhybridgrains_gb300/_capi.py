@@ -86,7 +86,8 @@ class DemDesc(ctypes.Structure):
                 ("gammat", ctypes.c_double), ("mu", ctypes.c_double),
                 ("cell_scale", ctypes.c_double), ("num_planes", ctypes.c_int32),
                 ("pad_", ctypes.c_int32), ("planes", DemPlane * HG_MAX_PLANES),
-                ("capacity", ctypes.c_int64), ("contact_capacity", ctypes.c_int64)]
+                ("capacity", ctypes.c_int64), ("contact_capacity", ctypes.c_int64),
+                ("precision", ctypes.c_int32), ("pad2_", ctypes.c_int32)]
 
 
 _P = ctypes.c_void_p

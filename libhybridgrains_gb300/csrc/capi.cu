@@ -1164,6 +1164,11 @@ hg_status hg_dem_create(hg_context *ctx, const hg_dem_desc *d, hg_dem **out) {
   P.gt = d->gammat;
   P.mu = d->mu;
   P.cell_scale = d->cell_scale;
+  if (d->precision != HG_PRECISION_FP64 && d->precision != HG_PRECISION_MIXED) {
+    hg_dem_destroy(dm);
+    return fail(HG_ERR_INVALID_ARGUMENT, "precision must be HG_PRECISION_FP64 or HG_PRECISION_MIXED");
+  }
+  P.precision = d->precision;
   P.nplanes = d->num_planes;
   for (int k = 0; k < d->num_planes; ++k) {
     const hg_dem_plane &pl = d->planes[k];

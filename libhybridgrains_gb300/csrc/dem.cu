@@ -661,6 +661,198 @@ __global__ void kd_integrate(int64_t n, double dt, double *q, double *v,
     atomicOr(status, (uint32_t)HG_STATUS_NONFINITE);
 }
 
+// ---- mixed precision: the same contact law and integration with FP32
+// arithmetic; positions, the pairwise position difference, the contact point
+// and the position update stay FP64 (a millimetre overlap taken from
+// metre-scale coordinates in FP32 would be lost to cancellation). Records and
+// velocities keep the FP64 storage of the FP64 path, holding FP32 values, so
+// the broadphase, history relabelling, collision-cache export, coupling and
+// checkpoints are shared.
+struct F2 {
+  float x, y;
+};
+__device__ __forceinline__ F2 fadd(F2 a, F2 b) { return {a.x + b.x, a.y + b.y}; }
+__device__ __forceinline__ F2 fsub(F2 a, F2 b) { return {a.x - b.x, a.y - b.y}; }
+__device__ __forceinline__ F2 fscl(float s, F2 a) { return {s * a.x, s * a.y}; }
+__device__ __forceinline__ float fdot(F2 a, F2 b) { return a.x * b.x + a.y * b.y; }
+__device__ __forceinline__ float fnrm(F2 a) { return sqrtf(fdot(a, a)); }
+__device__ __forceinline__ F2 fnormalized(F2 a) {
+  const float n2 = fdot(a, a);
+  if (n2 > 0.0f) {
+    const float n = sqrtf(n2);
+    return {a.x / n, a.y / n};
+  }
+  return a;
+}
+__device__ __forceinline__ float fcross(F2 a, F2 b) { return a.x * b.y - a.y * b.x; }
+
+__global__ void kdx_contacts(ContactArgs C) {
+  const int64_t total = min((int64_t)*C.count, C.ccap);
+  const float dt = (float)C.dt, kn = (float)C.kn, kt = (float)C.kt, gn = (float)C.gn,
+              gt = (float)C.gt, mu = (float)C.mu;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t key = C.keys[k];
+    const int kind = (int)(key >> 60);
+    const int a = (int)((key >> 30) & 0x3FFFFFFF);
+    const int b = (int)(key & 0x3FFFFFFF);
+    const double qax = C.q[3 * a], qay = C.q[3 * a + 1];
+    const F2 va{(float)C.v[3 * a], (float)C.v[3 * a + 1]};
+    const float wa = (float)C.v[3 * a + 2];
+    const float ra = (float)C.r[a];
+    float depth, weight;
+    F2 n, r0, r1{0.0f, 0.0f}, vrel;
+    double cpx, cpy;
+    if (kind == K_PLANE) { // PenaltyImpactFrictionMap.cpp:316-359
+      n = F2{(float)C.pn[b][0], (float)C.pn[b][1]};
+      // penetration from FP64 positions (a difference of nearly equal terms)
+      const double dist = C.pn[b][0] * (qax - C.px[b][0]) + C.pn[b][1] * (qay - C.px[b][1]);
+      depth = (float)fmin(0.0, dist - C.r[a]);
+      weight = C.weighted ? (float)C.w[a] : 1.0f;
+      r0 = fscl(-ra, n);
+      cpx = qax + (double)r0.x;
+      cpy = qay + (double)r0.y;
+      vrel = fadd(va, fscl(wa, F2{-r0.y, r0.x})); // the plane is static
+    } else {
+      const double qbx = C.q[3 * b], qby = C.q[3 * b + 1];
+      const float rb = (float)C.r[b];
+      const double dx = qax - qbx, dy = qay - qby; // FP64 difference
+      const F2 d{(float)dx, (float)dy};
+      n = fnormalized(d);
+      // |d| - (ra + rb) as (|d|^2 - (ra + rb)^2) / (|d| + ra + rb): the
+      // cancelling difference in FP64, the rest in FP32
+      const double rs = C.r[a] + C.r[b];
+      const double g2 = (dx * dx + dy * dy) - rs * rs;
+      depth = g2 < 0.0 ? (float)g2 / (fnrm(d) + (float)rs) : 0.0f;
+      const F2 vb{(float)C.v[3 * b], (float)C.v[3 * b + 1]};
+      const float wb = (float)C.v[3 * b + 2];
+      if (kind == K_CC) { // CircleCircleConstraint.cpp:171-233
+        weight = C.weighted ? (float)((C.w[a] + C.w[b]) * 0.5) : 1.0f;
+        r0 = fscl(-(ra / (ra + rb)), d); // p - xa = ra/(ra+rb) (xb - xa)
+        r1 = fadd(d, r0);                // p - xb
+        vrel = fsub(fsub(fadd(va, fscl(wa, F2{-r0.y, r0.x})), vb), fscl(wb, F2{-r1.y, r1.x}));
+      } else { // KinematicObjectCircleConstraint.cpp
+        weight = C.weighted ? (float)C.w[a] : 1.0f;
+        r0 = fscl(-ra, n);
+        const F2 arm = fadd(d, r0); // p - xb
+        const F2 vk = fadd(vb, fscl(wb, F2{-arm.y, arm.x}));
+        vrel = fsub(fadd(va, fscl(wa, F2{-r0.y, r0.x})), vk);
+      }
+      cpx = qax + (double)r0.x;
+      cpy = qay + (double)r0.y;
+    }
+    // tangential spring carry
+    F2 ds;
+    const int o = find_old(C, key);
+    if (o >= 0) {
+      ds = F2{(float)C.old_rec[(int64_t)o * RW + 6], (float)C.old_rec[(int64_t)o * RW + 7]};
+      ds = fadd(ds, fscl(dt, vrel));
+    } else {
+      ds = fscl(dt, vrel);
+    }
+    ds = fsub(ds, fscl(fdot(n, ds), n));
+    // penalty force (PenaltyImpactFrictionMap.cpp:616-1081)
+    const float w = weight;
+    const F2 vt = fsub(vrel, fscl(fdot(n, vrel), n));
+    const F2 vn = fsub(vrel, vt);
+    const F2 fn = fsub(fscl(-kn * w * depth, n), fscl(0.5f * gn * w, vn));
+    F2 ft = fsub(fscl(-kt * w, ds), fscl(0.5f * gt * w, vt));
+    const float mu_fn = mu * fnrm(fn);
+    if (0.5f * gt * w * fnrm(vt) > mu_fn) {
+      ds = F2{0.0f, 0.0f};
+      ft = fscl(mu_fn, fnormalized(fscl(-0.5f * gt * w, vt)));
+    } else if (fnrm(ft) > mu_fn) {
+      // secondRootOfQuadratic (PenaltyImpactFrictionMap.cpp:601-614)
+      const float qa_ = kt * w * kt * w * fdot(ds, ds);
+      const float qb_ = kt * w * gt * w * fdot(ds, vt);
+      const float qc_ = 0.25f * gt * w * gt * w * fdot(vt, vt) - mu * mu * fdot(fn, fn);
+      const float sq = sqrtf(fmaxf(qb_ * qb_ - 4.0f * qa_ * qc_, 0.0f));
+      const float root1 = qb_ > 0.0f ? (2.0f * qc_) / (-qb_ - sq) : (-qb_ + sq) / (2.0f * qa_);
+      ds = fscl(root1, ds);
+      ft = fsub(fscl(-kt * w, ds), fscl(0.5f * gt * w, vt));
+    }
+    double *o_ = C.rec + k * RW;
+    o_[0] = kind;
+    o_[1] = a;
+    o_[2] = b;
+    o_[3] = depth;
+    o_[4] = n.x;
+    o_[5] = n.y;
+    o_[6] = ds.x;
+    o_[7] = ds.y;
+    o_[8] = vrel.x;
+    o_[9] = vrel.y;
+    o_[10] = r0.x;
+    o_[11] = r0.y;
+    o_[12] = r1.x;
+    o_[13] = r1.y;
+    o_[14] = weight;
+    o_[15] = cpx;
+    o_[16] = cpy;
+    o_[17] = fn.x;
+    o_[18] = fn.y;
+    o_[19] = ft.x;
+    o_[20] = ft.y;
+    o_[21] = 0.0;
+  }
+}
+
+// Force gather (the FP64 kernel's summation order) and symplectic Euler in
+// FP32; q += dt v in FP64.
+__global__ void kdx_integrate(int64_t n, double dt, double *q, double *v,
+                              const double4 *__restrict__ terms,
+                              const uint8_t *__restrict__ fixed,
+                              const int32_t *__restrict__ cnt, const int32_t *__restrict__ off,
+                              const double *__restrict__ rec,
+                              const int32_t *__restrict__ in_count,
+                              const int32_t *__restrict__ in_off, int32_t *in_list,
+                              uint32_t *status) {
+  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const double4 bt = terms[j];
+  float Fx = (float)bt.x, Fy = (float)bt.y, T = 0.0f;
+  auto add = [&](int64_t k, int which, float sign) {
+    const double *r = rec + k * RW;
+    const F2 f = fadd(F2{(float)r[17], (float)r[18]}, F2{(float)r[19], (float)r[20]});
+    Fx += sign * f.x;
+    Fy += sign * f.y;
+    T += sign * fcross(F2{(float)r[10 + 2 * which], (float)r[11 + 2 * which]}, f);
+  };
+  for (int64_t k = off[j], e = off[j] + cnt[j]; k < e; ++k) add(k, 0, 1.0f);
+  {
+    int *lst = in_list + in_off[j];
+    const int c = in_count[j];
+    for (int i = 1; i < c; ++i) { // contact indices sorted = first indices sorted
+      const int key = lst[i];
+      int t = i - 1;
+      while (t >= 0 && lst[t] > key) {
+        lst[t + 1] = lst[t];
+        --t;
+      }
+      lst[t + 1] = key;
+    }
+    for (int i = 0; i < c; ++i) add(lst[i], 1, -1.0f);
+  }
+  for (int64_t k = off[n + j], e = off[n + j] + cnt[n + j]; k < e; ++k) add(k, 0, 1.0f);
+  for (int64_t k = off[2 * n + j], e = off[2 * n + j] + cnt[2 * n + j]; k < e; ++k)
+    add(k, 0, 1.0f);
+  if (fixed[j]) Fx = Fy = T = 0.0f;
+  const float v0 = (float)v[3 * j] + (float)bt.z * Fx;
+  const float v1 = (float)v[3 * j + 1] + (float)bt.z * Fy;
+  const float v2 = (float)v[3 * j + 2] + (float)bt.w * T;
+  v[3 * j] = v0;
+  v[3 * j + 1] = v1;
+  v[3 * j + 2] = v2;
+  const double q0 = q[3 * j] + dt * (double)v0, q1 = q[3 * j + 1] + dt * (double)v1,
+               q2 = q[3 * j + 2] + dt * (double)v2;
+  q[3 * j] = q0;
+  q[3 * j + 1] = q1;
+  q[3 * j + 2] = q2;
+  if (!finite_bits(q0) || !finite_bits(q1) || !isfinite(v0) || !isfinite(v1))
+    atomicOr(status, (uint32_t)HG_STATUS_NONFINITE);
+}
+
+
 // Candidate pairs of explicit boxes (SpatialGrid::getPotentialOverlaps).
 template <bool EMIT>
 __global__ void kd_box_pairs(BroadArgs B, const int2 *__restrict__ home,
@@ -873,7 +1065,10 @@ hg_status dem_step(hg_dem *d, double dt, int weighted) {
   Cg.old_rec = d->crec[d->cc].p;
   Cg.old_count = d->c_count.p + d->cc;
   Cg.ccap = d->ccap;
-  HG_LAUNCH(kd_contacts, d->ctx->num_sms * 4, 256, 0, s, Cg);
+  if (d->p.precision == HG_PRECISION_MIXED)
+    HG_LAUNCH(kdx_contacts, d->ctx->num_sms * 4, 256, 0, s, Cg);
+  else
+    HG_LAUNCH(kd_contacts, d->ctx->num_sms * 4, 256, 0, s, Cg);
   HG_CHECK_LAUNCH();
   HG_CUDA_TRY(cudaMemsetAsync(d->in_count.p, 0, sizeof(int32_t) * (n + 1), s));
   HG_CUDA_TRY(cudaMemsetAsync(d->in_cursor.p, 0, sizeof(int32_t) * n, s));
@@ -884,7 +1079,8 @@ hg_status dem_step(hg_dem *d, double dt, int weighted) {
   HG_LAUNCH(kd_in_fill, d->ctx->num_sms * 2, 256, 0, s, n, d->per_body_off.p, d->ckey[nb].p,
             d->in_off.p, d->in_cursor.p, d->in_list.p);
   HG_CHECK_LAUNCH();
-  HG_LAUNCH(kd_integrate, blocks_for(n, 128), 128, 0, s, n, dt, d->q.p, d->v.p,
+  auto integrate = d->p.precision == HG_PRECISION_MIXED ? kdx_integrate : kd_integrate;
+  HG_LAUNCH(integrate, blocks_for(n, 128), 128, 0, s, n, dt, d->q.p, d->v.p,
             reinterpret_cast<const double4 *>(d->minv.p), d->fixed.p, d->per_body.p,
             d->per_body_off.p,
             d->crec[nb].p, d->in_count.p, d->in_off.p, d->in_list.p, d->status.p);

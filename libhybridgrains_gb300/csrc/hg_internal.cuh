@@ -334,6 +334,7 @@ struct DemParams {
   double g[2];
   double kn, kt, gn, gt, mu;
   double cell_scale;
+  int precision; // HG_PRECISION_FP64 (bit-exact) or HG_PRECISION_MIXED
   int nplanes;
   double px[HG_MAX_PLANES][2], pn[HG_MAX_PLANES][2];
 };

@@ -181,3 +181,51 @@ def test_edit_async_matches_the_scene_without_the_removed_pile(ctx):
         x.edit_async(bad)
     x.close()
     y.close()
+
+
+def test_mixed_precision_against_fp64(ctx):
+    """HG_PRECISION_MIXED (FP32 contact law and integration; FP64 positions,
+    pairwise differences, contact points and position update) against the
+    bit-exact FP64 step from the same settled state with its contact
+    history. The contact set is identical (the broadphase and the contact
+    tests are shared and exact); after one step every output field is within
+    FP32 rounding of the FP64 values (measured: 4e-8 relative for velocities,
+    6e-8 for depths and spring lengths, 1e-7 for forces, 7e-11 m for
+    positions); positions stay within 1e-7 m after 10 more steps (measured
+    1.2e-9 m; contacts amplify the difference over longer runs)."""
+    sc = scenes.dem_column(n=4000, per_row=40)
+    dp = scenes.dem_params()
+    planes = [((0.0, 0.0), (0.0, 1.0))]
+
+    def make(precision):
+        return hg.DEM(ctx, scenes.GRAVITY, dp["kn"], dp["kt"], dp["gamman"], dp["gammat"],
+                      dp["mu"], planes, capacity=4000, precision=precision)
+
+    base = make(hg.FP64)
+    base.upload(sc["q"], sc["v"], sc["r"], sc["m"], sc["I"], sc["fixed"])
+    base.flow(1e-5, 2000)  # settle into contact, with friction history
+    blob = base.state()
+    f64, mix = make(hg.FP64), make(hg.MIXED)
+    f64.load_state(blob)
+    mix.load_state(blob)
+    f64.flow(1e-5, 1)
+    mix.flow(1e-5, 1)
+    ca, cb = f64.contacts(), mix.contacts()
+    assert len(ca) > 300 and np.array_equal(ca[:, :3], cb[:, :3])  # same contact set
+
+    def rel(a, b):
+        return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+    (qa, va), (qb, vb) = f64.download(), mix.download()
+    assert rel(vb[:, :2], va[:, :2]) <= 2e-6
+    assert rel(vb[:, 2], va[:, 2]) <= 2e-6
+    assert np.abs(qb - qa).max() <= 1e-9
+    # depth, spring, relative velocity, lever arms, normal and friction force
+    for cols in ((3,), (6, 7), (8, 9), (10, 11), (17, 18), (19, 20)):
+        assert rel(cb[:, cols], ca[:, cols]) <= 5e-6, cols
+    f64.flow(1e-5, 10)
+    mix.flow(1e-5, 10)
+    assert np.abs(mix.download()[0] - f64.download()[0]).max() <= 1e-7
+    assert mix.status() == 0
+    for d in (base, f64, mix):
+        d.close()
