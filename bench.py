@@ -392,25 +392,38 @@ def run_dem(args, ctx):
     gpu_rate = n * args.dem_steps / (ms * 1e-3)
     # per disk-step 128 B, per contact 40 B (FP64 figures of the scope table)
     alg = n * 128 + contacts * 40
+    # the HG_PRECISION_MIXED step on the same column (FP32 contact law)
+    dm = hg.DEM(ctx, scenes.GRAVITY, dp["kn"], dp["kt"], dp["gamman"], dp["gammat"], dp["mu"],
+                planes, capacity=n, precision=hg.MIXED)
+    dm.upload(sc["q"], sc["v"], sc["r"], sc["m"], sc["I"], sc["fixed"])
+    dm.flow(dt, 20)
+    ctx.synchronize()
+    ctx.timer_begin()
+    dm.flow(dt, args.dem_steps)
+    msm = ctx.timer_end()
+    mixed = {"disk_steps_per_s": n * args.dem_steps / (msm * 1e-3),
+             "us_per_step": 1e3 * msm / args.dem_steps}
+    dm.close()
     large = None
     if args.dem_large_disks > 0:
         # the same lattice at a size where the step is no longer launch-bound
         nl = args.dem_large_disks
         sl = scenes.dem_column(n=nl, per_row=1000)
-        dl = hg.DEM(ctx, scenes.GRAVITY, dp["kn"], dp["kt"], dp["gamman"], dp["gammat"],
-                    dp["mu"], planes, capacity=nl, contact_capacity=4 * nl)
-        dl.upload(sl["q"], sl["v"], sl["r"], sl["m"], sl["I"], sl["fixed"])
-        dl.flow(1.0e-5, 200)
-        ctx.synchronize()
-        ctx.timer_begin()
-        dl.flow(1.0e-5, args.dem_large_steps)
-        msl = ctx.timer_end()
         large = {"workload": "%d disks, the same lattice 1000 per row, dt 1e-5 s" % nl,
-                 "disk_steps_per_s": nl * args.dem_large_steps / (msl * 1e-3),
-                 "us_per_step": 1e3 * msl / args.dem_large_steps,
-                 "steps": args.dem_large_steps, "contacts": dl.num_contacts(),
-                 "status": dl.status()}
-        dl.close()
+                 "steps": args.dem_large_steps}
+        for name, prec in (("fp64", hg.FP64), ("mixed", hg.MIXED)):
+            dl = hg.DEM(ctx, scenes.GRAVITY, dp["kn"], dp["kt"], dp["gamman"], dp["gammat"],
+                        dp["mu"], planes, capacity=nl, contact_capacity=4 * nl, precision=prec)
+            dl.upload(sl["q"], sl["v"], sl["r"], sl["m"], sl["I"], sl["fixed"])
+            dl.flow(1.0e-5, 200)
+            ctx.synchronize()
+            ctx.timer_begin()
+            dl.flow(1.0e-5, args.dem_large_steps)
+            msl = ctx.timer_end()
+            large[name] = {"disk_steps_per_s": nl * args.dem_large_steps / (msl * 1e-3),
+                           "us_per_step": 1e3 * msl / args.dem_large_steps,
+                           "contacts": dl.num_contacts(), "status": dl.status()}
+            dl.close()
     return {"workload": "DEM column: 10,000 disks, hex pitch 2.2 mm, r U[0.9,1.1] mm, dt 1e-6 s, "
                         "FP64 penalty contacts with friction history",
             "disk_steps_per_s": gpu_rate, "us_per_step": 1e3 * ms / args.dem_steps,
@@ -421,7 +434,7 @@ def run_dem(args, ctx):
             "cpu_baseline": {"value": n * csteps / cs, "unit": "disk-steps/s", "cores": 1,
                              "kind": "port", "sample": "%d steps of the same column (%.1f s)" %
                              (csteps, cs)},
-            "large": large}
+            "mixed": mixed, "large": large}
 
 
 def run_hybrid(args, ctx):
