@@ -51,7 +51,9 @@ enum {
   HG_STATUS_OUT_OF_GRID = 1u << 1,      /* a particle left the MPM grid */
   HG_STATUS_CONTACT_OVERFLOW = 1u << 2, /* DEM contact capacity exceeded */
   HG_STATUS_CELL_OVERFLOW = 1u << 3,    /* DEM broadphase bucket overflow */
-  HG_STATUS_NEGATIVE_MASS = 1u << 4     /* a grain coupled to an empty node */
+  HG_STATUS_NEGATIVE_MASS = 1u << 4,    /* a grain coupled to an empty node */
+  HG_STATUS_INDEX = 1u << 5             /* bounds-checking build: an index out of
+                                           its array (the access was skipped) */
 };
 
 typedef struct hg_context hg_context;

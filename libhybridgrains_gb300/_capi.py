@@ -7,7 +7,10 @@ import ctypes
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "libhg_gpu.so")
+# HG_GPU_VARIANT=bounds selects the bounds-checking build
+LIB_PATH = (os.path.join(HERE, "_build_bounds", "libhg_gpu_bounds.so")
+            if os.environ.get("HG_GPU_VARIANT") == "bounds"
+            else os.path.join(HERE, "_build", "libhg_gpu.so"))
 
 HG_MAX_PLANES = 8
 HG_DEM_RECORD_WIDTH = 22

@@ -167,12 +167,13 @@ __global__ void kd_bodies_home(HomeArgs A) {
 // Places each body in its bucket. bucket_pos holds the bucket starts and
 // ends up holding the bucket ends (start + count).
 __global__ void kd_fill_ends(int64_t n, uint32_t mask, const float4 *__restrict__ rec,
-                             int32_t *bucket_pos, int32_t *items) {
+                             int32_t *bucket_pos, int32_t *items, uint32_t *status) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float4 h = rec[2 * i + 1];
-  items[atomicAdd(&bucket_pos[cell_hash(__float_as_int(h.x), __float_as_int(h.y), mask)], 1)] =
-      (int32_t)i;
+  const int p = atomicAdd(&bucket_pos[cell_hash(__float_as_int(h.x), __float_as_int(h.y), mask)], 1);
+  if (!HG_INDEX_OK(p, n, status)) return;
+  items[p] = (int32_t)i;
 }
 
 // The per-body terms of kd_integrate that change only with the masses, the
@@ -244,7 +245,9 @@ __device__ __forceinline__ void for_each_partner(const PairArgs &A, int a, F &&f
     const int dx = c % 3 - 1, dy = c / 3 - 1;
     const int cx = ha.x + dx, cy = ha.y + dy;
     for (int k = bs[c]; k < be[c]; ++k) {
+      if (!HG_INDEX_OK(k, A.n, A.status)) break;
       const int b = A.items[k];
+      if (!HG_INDEX_OK(b, A.n, A.status)) continue;
       if (b == a) continue;
       const float4 pb = A.rec[2 * b], cb = A.rec[2 * b + 1];
       if (__float_as_int(cb.x) != cx || __float_as_int(cb.y) != cy)
@@ -281,6 +284,7 @@ __constant__ int HALF_CELLS[5][2] = {{0, 0}, {1, 0}, {-1, 1}, {0, 1}, {1, 1}};
 
 __device__ __forceinline__ void credit(const PairArgs &A, int first, int second, bool kin,
                                        bool &overflow) {
+  if (!HG_INDEX_OK(first, A.n, A.status)) return;
   int32_t *c = A.cnt + (kin ? 2 : 1) * A.n + first;
   if (atomicAdd(c, 1) >= MAXP) {
     atomicSub(c, 1);
@@ -314,7 +318,9 @@ __global__ void kd_pairs_count(PairArgs A) {
     const int dx = HALF_CELLS[c][0], dy = HALF_CELLS[c][1];
     const int cx = ha.x + dx, cy = ha.y + dy;
     for (int k = bs[c]; k < be[c]; ++k) {
+      if (!HG_INDEX_OK(k, n, A.status)) break;
       const int b = A.items[k];
+      if (!HG_INDEX_OK(b, n, A.status)) continue;
       if (b == a || (c == 0 && b < a)) continue;
       const float4 pb = A.rec[2 * b], cb = A.rec[2 * b + 1];
       if (__float_as_int(cb.x) != cx || __float_as_int(cb.y) != cy)
@@ -432,6 +438,7 @@ struct ContactArgs {
   const double *old_rec;
   const int32_t *old_count; // device count of the previous step's contacts
   int64_t ccap;
+  uint32_t *status;
 };
 
 __device__ __forceinline__ int find_old(const ContactArgs &C, int64_t key) {
@@ -460,6 +467,9 @@ __global__ void kd_contacts(ContactArgs C) {
     const int kind = (int)(key >> 60);
     const int a = (int)((key >> 30) & 0x3FFFFFFF);
     const int b = (int)(key & 0x3FFFFFFF);
+    if (!HG_INDEX_OK(a, C.n, C.status) ||
+        !HG_INDEX_OK(b, kind == K_PLANE ? (int64_t)C.nplanes : C.n, C.status))
+      continue;
     const D2 qa{C.q[3 * a], C.q[3 * a + 1]};
     const D2 va{C.v[3 * a], C.v[3 * a + 1]};
     const double wa = C.v[3 * a + 2];
@@ -623,6 +633,7 @@ __global__ void kd_integrate(int64_t n, double dt, double *q, double *v,
     }
     for (int i = 0; i < c; ++i) {
       const int64_t k = lst[i];
+      if (!HG_INDEX_OK(k, off[3 * n], status)) continue;
       D2 f;
       total(k, f);
       Fx -= f.x;
@@ -696,6 +707,9 @@ __global__ void kdx_contacts(ContactArgs C) {
     const int kind = (int)(key >> 60);
     const int a = (int)((key >> 30) & 0x3FFFFFFF);
     const int b = (int)(key & 0x3FFFFFFF);
+    if (!HG_INDEX_OK(a, C.n, C.status) ||
+        !HG_INDEX_OK(b, kind == K_PLANE ? (int64_t)C.nplanes : C.n, C.status))
+      continue;
     const double qax = C.q[3 * a], qay = C.q[3 * a + 1];
     const F2 va{(float)C.v[3 * a], (float)C.v[3 * a + 1]};
     const float wa = (float)C.v[3 * a + 2];
@@ -831,7 +845,8 @@ __global__ void kdx_integrate(int64_t n, double dt, double *q, double *v,
       }
       lst[t + 1] = key;
     }
-    for (int i = 0; i < c; ++i) add(lst[i], 1, -1.0f);
+    for (int i = 0; i < c; ++i)
+      if (HG_INDEX_OK(lst[i], off[3 * n], status)) add(lst[i], 1, -1.0f);
   }
   for (int64_t k = off[n + j], e = off[n + j] + cnt[n + j]; k < e; ++k) add(k, 0, 1.0f);
   for (int64_t k = off[2 * n + j], e = off[2 * n + j] + cnt[2 * n + j]; k < e; ++k)
@@ -999,7 +1014,7 @@ hg_status dem_step(hg_dem *d, double dt, int weighted) {
     HG_CHECK_LAUNCH();
     if ((st = exclusive_scan_i32(d->bcount.p, d->bstart.p, T, d->scan_tmp.p, s))) return st;
     HG_LAUNCH(kd_fill_ends, blocks_for(n, 256), 256, 0, s, n, mask, d->brec.p, d->bstart.p,
-              d->items.p);
+              d->items.p, d->status.p);
     HG_CHECK_LAUNCH();
   }
   PairArgs A;
@@ -1065,6 +1080,7 @@ hg_status dem_step(hg_dem *d, double dt, int weighted) {
   Cg.old_rec = d->crec[d->cc].p;
   Cg.old_count = d->c_count.p + d->cc;
   Cg.ccap = d->ccap;
+  Cg.status = d->status.p;
   if (d->p.precision == HG_PRECISION_MIXED)
     HG_LAUNCH(kdx_contacts, d->ctx->num_sms * 4, 256, 0, s, Cg);
   else

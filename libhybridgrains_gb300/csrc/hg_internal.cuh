@@ -31,6 +31,14 @@ hg_status cuda_fail(cudaError_t e, const char *what);
 extern std::atomic<int64_t> g_launches;
 // An NVTX range over a C-ABI call, for timelines of profiling tools (a no-op
 // when no tool is attached).
+#ifdef HG_BOUNDS_CHECK
+__device__ __forceinline__ bool index_ok(int64_t i, int64_t n, uint32_t *status) {
+  if (i >= 0 && i < n) return true;
+  atomicOr(status, (uint32_t)HG_STATUS_INDEX);
+  return false;
+}
+#endif
+
 struct TraceRange {
   explicit TraceRange(const char *name) { nvtxRangePushA(name); }
   ~TraceRange() { nvtxRangePop(); }
@@ -39,6 +47,16 @@ struct TraceRange {
 };
 
 #define HG_TRACE(name) ::hg::TraceRange hg_trace_range_(name)
+
+// Index checks of the bounds-checking build (compiled with HG_BOUNDS_CHECK,
+// libhg_gpu_bounds.so): a computed index outside [0, n) sets HG_STATUS_INDEX
+// in the object's status word and the caller skips the access. In the
+// regular build the check is the constant true and compiles away.
+#ifdef HG_BOUNDS_CHECK
+#define HG_INDEX_OK(i, n, status) ::hg::index_ok((int64_t)(i), (int64_t)(n), (status))
+#else
+#define HG_INDEX_OK(i, n, status) true
+#endif
 
 #define HG_LAUNCH(kernel, grid, block, smem, stream, ...)                     \
   do {                                                                        \

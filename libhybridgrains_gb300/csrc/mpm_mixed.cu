@@ -214,6 +214,7 @@ __device__ __forceinline__ void scatter_global(const MixedArgs &A, int cx, int c
       add.w = r.b.z * gx + r.b.w * gy;
     }
     const int64_t node = (int64_t)iy * row + ix;
+    if (!HG_INDEX_OK(node, (int64_t)row * (A.ny + 1), A.status)) continue;
     atomicAdd(&A.accm[node], w * r.a.z);
     atomicAdd(&A.acc4[node], add);
   }
@@ -301,8 +302,10 @@ __device__ __forceinline__ void fused_tile(const MixedArgs &A, const int bin, Fu
     // s_slow is zero here: zeroed at kernel start and by the previous
     // tile's flush
     if (tid < 2) s_out[tid] = 0;
-    const int ps = A.offsets[bin * BIN_CELLS + tid];
-    const int pe = A.offsets[bin * BIN_CELLS + tid + 1];
+    int ps = A.offsets[bin * BIN_CELLS + tid];
+    int pe = A.offsets[bin * BIN_CELLS + tid + 1];
+    if (!HG_INDEX_OK(ps, (int64_t)A.n + 1, A.status) || !HG_INDEX_OK(pe, (int64_t)A.n + 1, A.status))
+      ps = pe = 0;
     const int gcx = X0 + lcx, gcy = Y0 + lcy;
     // Planes that can touch a point of this tile's window: the window corners
     // bound every position a point of the tile can take this step.
@@ -375,10 +378,14 @@ __device__ __forceinline__ void fused_tile(const MixedArgs &A, const int bin, Fu
           n11 = s_va[k0 + VA_W + 1];
         } else {
           const int k0 = cy * row + cx;
-          n00 = A.va[k0];
-          n10 = A.va[k0 + 1];
-          n01 = A.va[k0 + row];
-          n11 = A.va[k0 + row + 1];
+          if (HG_INDEX_OK(k0 + row + 1, (int64_t)row * (A.ny + 1), A.status)) {
+            n00 = A.va[k0];
+            n10 = A.va[k0 + 1];
+            n01 = A.va[k0 + row];
+            n11 = A.va[k0 + row + 1];
+          } else {
+            n00 = n10 = n01 = n11 = make_float4(0.f, 0.f, 0.f, 0.f);
+          }
         }
         const float wx0 = 1.0f - fx, wx1 = fx, wy0 = 1.0f - fy, wy1 = fy;
         const float w00 = wx0 * wy0, w10 = wx1 * wy0, w01 = wx0 * wy1, w11 = wx1 * wy1;
@@ -524,6 +531,7 @@ __device__ __forceinline__ void fused_tile(const MixedArgs &A, const int bin, Fu
       const int ix = WX + i, iy = WY + j;
       if (ix < 0 || iy < 0 || ix > A.nx || iy > A.ny) continue;
       const int node = iy * row + ix;
+      if (!HG_INDEX_OK(node, (int64_t)row * (A.ny + 1), A.status)) continue;
       atomicAdd(&A.accm[node], sum[0]);
       atomicAdd(&A.acc4[node], make_float4(sum[1], sum[2], sum[3], sum[4]));
     }
@@ -545,7 +553,11 @@ __global__ void __launch_bounds__(THREADS, 3) kx_g2p2g(const __grid_constant__ M
   __shared__ FusedSmem S;
   zero_slow(S);
   const int nact = *A.nactive;
-  for (int t = blockIdx.x; t < nact; t += gridDim.x) fused_tile<PRIME>(A, A.active[t], S);
+  for (int t = blockIdx.x; t < nact; t += gridDim.x) {
+    const int tile = A.active[t];
+    if (!HG_INDEX_OK(tile, (int64_t)A.ntx * A.nty, A.status)) continue;
+    fused_tile<PRIME>(A, tile, S);
+  }
 }
 
 // Exclusive prefix of the scenes' work-item counts, in shared memory
@@ -687,7 +699,11 @@ __device__ __forceinline__ void update_tile(const MixedArgs &A, const int tile) 
 
 __global__ void __launch_bounds__(THREADS) kx_grid_update(const __grid_constant__ MixedArgs A) {
   const int nact = *A.nactive;
-  for (int t = blockIdx.x; t < nact; t += gridDim.x) update_tile(A, A.active[t]);
+  for (int t = blockIdx.x; t < nact; t += gridDim.x) {
+    const int tile = A.active[t];
+    if (!HG_INDEX_OK(tile, (int64_t)A.ntx * A.nty, A.status)) continue;
+    update_tile(A, tile);
+  }
 }
 
 __global__ void __launch_bounds__(THREADS) kb_grid_update(const MixedArgs *__restrict__ slots,

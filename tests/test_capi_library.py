@@ -95,3 +95,12 @@ def test_tuning_table_round_trip(lib, tmp_path):
     hg.tune_clear()
     hg.tune_save(str(q))
     assert q.read_text() == ""
+
+
+def test_bounds_variant_builds_and_exports(lib):
+    """The bounds-checking variant compiles for sm_103a and exports the same
+    entry points (loaded here without a GPU only to list its symbols)."""
+    path = build.build(bounds_check=True)
+    assert path.endswith("libhg_gpu_bounds.so") and os.path.exists(path)
+    other = ctypes.CDLL(path)
+    assert all(hasattr(other, s) for s in _capi.declared_symbols())
