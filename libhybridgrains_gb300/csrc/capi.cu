@@ -375,8 +375,6 @@ static hg_status validate_desc(const hg_mpm_desc *d) {
     return fail(HG_ERR_INVALID_ARGUMENT, "unknown basis");
   if (d->precision != HG_PRECISION_FP64 && d->precision != HG_PRECISION_MIXED)
     return fail(HG_ERR_INVALID_ARGUMENT, "unknown precision");
-  if (d->precision == HG_PRECISION_MIXED && d->basis != HG_BASIS_LINEAR)
-    return fail(HG_ERR_UNSUPPORTED, "MIXED precision supports the linear basis only");
   if (d->num_planes < 0 || d->num_planes > HG_MAX_PLANES)
     return fail(HG_ERR_INVALID_ARGUMENT, "num_planes out of range");
   if (d->capacity < 0 || d->capacity > (int64_t)INT32_MAX)
@@ -708,6 +706,20 @@ static hg_status upload_impl(hg_mpm *m, int64_t n, const double *q, const double
       if ((st = h2d(s, m->stage_u8.p, kin, n))) return st;
     } else {
       HG_CUDA_TRY(cudaMemsetAsync(m->stage_u8.p, 0, n, s));
+    }
+    if (m->p.basis == HG_BASIS_UGIMP && n > 0) {
+      // the uGIMP kernel takes one half-width for all points (the reference's
+      // scenes seed every point with h / (2 samples per dimension))
+      if (!hl) return fail(HG_ERR_INVALID_ARGUMENT, "the uGIMP basis needs the half-widths hl");
+      std::vector<double> h(n);
+      HG_CUDA_TRY(cudaMemcpy(h.data(), hl, sizeof(double) * n, cudaMemcpyDefault));
+      for (int64_t i = 0; i < n; ++i)
+        if (!(std::fabs(h[i] - h[0]) <= 1e-12 * std::fabs(h[0])))
+          return fail(HG_ERR_UNSUPPORTED, "MIXED uGIMP needs one half-width for all points");
+      const double cells = h[0] / m->p.h;
+      if (!(cells > 0.0 && cells <= 0.5))
+        return fail(HG_ERR_UNSUPPORTED, "MIXED uGIMP needs 0 < hl <= h / 2");
+      m->hl_cells = (float)cells;
     }
     m->primed = false;
     if ((st = mixed_upload(m, sq, sv, sm, svol, sbe, sJ, m->stage_i.p, m->stage_u8.p)))
@@ -1045,6 +1057,8 @@ hg_status hg_batch_add(hg_batch *b, hg_mpm *m, double dt) {
   if (m->ctx != b->ctx) return fail(HG_ERR_INVALID_ARGUMENT, "member of another context");
   if (m->p.precision != HG_PRECISION_MIXED)
     return fail(HG_ERR_UNSUPPORTED, "batches hold MIXED precision MPM objects");
+  if (m->p.basis != HG_BASIS_LINEAR)
+    return fail(HG_ERR_UNSUPPORTED, "batches hold MPM objects with the linear basis");
   if (!(dt > 0.0) || !std::isfinite(dt)) return fail(HG_ERR_INVALID_ARGUMENT, "dt must be positive");
   for (hg_mpm *x : b->members)
     if (x == m) return fail(HG_ERR_INVALID_ARGUMENT, "already a member");

@@ -213,6 +213,7 @@ struct hg_mpm {
   hg::DevBuf<uint8_t> mflags_[2];
   hg::DevBuf<int32_t> mid_[2];
   int cur = 0; // which buffer of the pairs above is live
+  float hl_cells = 0.f; // uGIMP: the points' common half-width in cells
   hg::DevBuf<float4> acc4; // (px, py, fx, fy) accumulated for the next update
   hg::DevBuf<float> accm;  // mass accumulated for the next update
   hg::DevBuf<float4> va;   // (vx, vy, ax, ay) of the last update

@@ -65,6 +65,7 @@ struct alignas(16) MixedArgs {
   // Half-width (in cells) of the band around a plane in which the FP32
   // plane test is redone exactly in FP64.
   float pmargin;
+  float hl; // uGIMP half-width of every point in cells (0: linear basis)
   int nplanes;
   const int32_t *offsets;
   const int32_t *active;  // active bins or tiles
@@ -648,6 +649,183 @@ __global__ void __launch_bounds__(THREADS, 3) kb_g2p2g(const MixedArgs *__restri
   }
 }
 
+// ---- MIXED step with the uGIMP basis --------------------------------------
+//
+// uGIMPLinearBasisFunctions (uGIMPLinearBasisFunctions.cpp:6-156) in FP32
+// grid units: the weight of node i along one axis is the hat function
+// integrated over the point's extent [u - hl, u + hl], divided by 2 hl, with
+// derivative d/du; for hl <= 1/2 a point of fraction f in cell c touches the
+// nodes c-1 (f < hl), c, c+1 and c+2 (f > 1 - hl). One thread per material
+// point: G2P from the global grid, the same constitutive and position update
+// as the linear kernel, and P2G with global FP32 atomics (the points are
+// sorted by cell, so the atomics of a warp stay in a few cache lines).
+__device__ __forceinline__ void ugimp_1d(float d, float hl, float &w, float &g) {
+  // d = u - x_i; lin_integral / lin_integral_grad with w = 1, over 2 hl
+  const float a = fabsf(d), s = d >= 0.0f ? 1.0f : -1.0f, i2 = 0.5f / hl;
+  if (a >= 1.0f + hl) {
+    w = 0.0f;
+    g = 0.0f;
+  } else if (a >= 1.0f - hl) {
+    const float t = 1.0f + hl - a;
+    w = 0.5f * t * t * i2;
+    g = -s * t * i2;
+  } else if (a >= hl) {
+    w = 2.0f * hl * (1.0f - a) * i2;
+    g = -s * 2.0f * hl * i2;
+  } else {
+    w = (2.0f * hl - (hl * hl + a * a)) * i2;
+    g = -2.0f * d * i2;
+  }
+}
+
+// Weights and derivatives of the nodes c-1 .. c+2 along one axis; false if a
+// node of non-zero weight lies outside 0 .. n (the reference's stencil would
+// leave its grid).
+__device__ __forceinline__ bool ugimp_axis(int c, float f, float hl, int n, float w[4],
+                                           float g[4]) {
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    ugimp_1d(f - (float)(k - 1), hl, w[k], g[k]);
+    const int i = c + k - 1;
+    if ((w[k] != 0.0f || g[k] != 0.0f) && (i < 0 || i > n)) ok = false;
+  }
+  return ok;
+}
+
+template <bool PRIME>
+__global__ void __launch_bounds__(THREADS) kxu_step(const __grid_constant__ MixedArgs A) {
+  const float hl = A.hl;
+  const int row = A.nx + 1;
+  const int64_t nn = (int64_t)row * (A.ny + 1);
+  unsigned moved = 0;
+  bool nonfinite = false;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < A.n;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    double2 un = A.u[p];
+    const float2 mv = A.mv[p];
+    float2 vel = A.v[p];
+    float4 st = A.strain[p];
+    const int fl = A.flags[p];
+    int jh = fl & 1;
+    int cx, cy;
+    float fx, fy;
+    split_u(un.x, cx, fx);
+    split_u(un.y, cy, fy);
+    far_edge(A.nx, cx, fx);
+    far_edge(A.ny, cy, fy);
+    float wx[4], gx[4], wy[4], gy[4];
+    if (!in_grid_cell(A, cx, cy) || !ugimp_axis(cx, fx, hl, A.nx, wx, gx) ||
+        !ugimp_axis(cy, fy, hl, A.ny, wy, gy)) {
+      atomicOr(A.status, (uint32_t)HG_STATUS_OUT_OF_GRID);
+      continue;
+    }
+    int ncx = cx, ncy = cy;
+    float nfx = fx, nfy = fy;
+    if (!PRIME) {
+      // ---- G2P of this step at the start-of-step position ----
+      float Lxx = 0.f, Lxy = 0.f, Lyx = 0.f, Lyy = 0.f, vpx = 0.f, vpy = 0.f, apx = 0.f,
+            apy = 0.f;
+#pragma unroll
+      for (int ky = 0; ky < 4; ++ky) {
+        if (wy[ky] == 0.0f && gy[ky] == 0.0f) continue;
+#pragma unroll
+        for (int kx = 0; kx < 4; ++kx) {
+          if (wx[kx] == 0.0f && gx[kx] == 0.0f) continue;
+          const int64_t node = (int64_t)(cy + ky - 1) * row + (cx + kx - 1);
+          if (!HG_INDEX_OK(node, nn, A.status)) continue;
+          const float4 nv = A.va[node];
+          const float w = wx[kx] * wy[ky], dX = gx[kx] * wy[ky], dY = wx[kx] * gy[ky];
+          Lxx += nv.x * dX;
+          Lxy += nv.x * dY;
+          Lyx += nv.y * dX;
+          Lyy += nv.y * dY;
+          vpx += w * nv.x;
+          vpy += w * nv.y;
+          apx += w * nv.z;
+          apy += w * nv.w;
+        }
+      }
+      const float ih = A.inv_h;
+      constitutive_update(st, jh, Lxx * ih, Lxy * ih, Lyx * ih, Lyy * ih, A.dt, A.kappa, A.mu,
+                          A.dp_alpha);
+      const bool kin = (fl & 2) != 0;
+      const float dtih = A.dt * A.inv_h;
+      const float dux = dtih * (kin ? vel.x : vpx);
+      const float duy = dtih * (kin ? vel.y : vpy);
+      {
+        const float a = A.flip_alpha;
+        const float fvx = (1.0f - a) * vpx + a * (vel.x + A.dt * apx);
+        const float fvy = (1.0f - a) * vpy + a * (vel.y + A.dt * apy);
+        vel.x = kin ? vel.x : fvx;
+        vel.y = kin ? vel.y : fvy;
+      }
+      un = make_double2(un.x + widen(dux), un.y + widen(duy));
+      // MaterialPoints::resolvePlaneCollisions (MaterialPoints.cpp:371-423) in
+      // grid units, FP64 on the positions
+      for (int k = 0; k < A.nplanes; ++k) {
+        const MpmPlaneDev &pl = A.planes[k];
+        if (un.y < pl.ulb) continue;
+        const double d = pl.n[0] * (un.x - pl.ux[0]) + pl.n[1] * (un.y - pl.ux[1]);
+        if (d > 0.0) continue;
+        un.x += -d * pl.n[0];
+        un.y += -d * pl.n[1];
+        if (!pl.sticking) {
+          const float vn = pl.fn[0] * vel.x + pl.fn[1] * vel.y;
+          if (vn > 0.0f) continue;
+          vel.x -= vn * pl.fn[0];
+          vel.y -= vn * pl.fn[1];
+        } else {
+          vel = make_float2(0.0f, 0.0f);
+        }
+      }
+      split_u(un.x, ncx, nfx);
+      split_u(un.y, ncy, nfy);
+      far_edge(A.nx, ncx, nfx);
+      far_edge(A.ny, ncy, nfy);
+      nonfinite |= !finite_d(un.x) | !finite_d(un.y) | !isfinite(vel.x + vel.y) |
+                   !isfinite(st.x);
+      A.u[p] = un;
+      A.v[p] = vel;
+      A.strain[p] = st;
+      A.flags[p] = (uint8_t)((fl & ~1) | jh);
+      moved += (ncx != cx) | (ncy != cy);
+      if (!in_grid_cell(A, ncx, ncy) || !ugimp_axis(ncx, nfx, hl, A.nx, wx, gx) ||
+          !ugimp_axis(ncy, nfy, hl, A.ny, wy, gy)) {
+        atomicOr(A.status, (uint32_t)HG_STATUS_OUT_OF_GRID);
+        continue;
+      }
+    }
+    // ---- P2G contribution for the next step ----
+    float s00, s01, s11;
+    stress_factor(st, jh, mv.y, A.inv_h, A.kappa, A.mu, s00, s01, s11);
+    const float mvx = mv.x * vel.x, mvy = mv.x * vel.y;
+#pragma unroll
+    for (int ky = 0; ky < 4; ++ky) {
+      if (wy[ky] == 0.0f && gy[ky] == 0.0f) continue;
+#pragma unroll
+      for (int kx = 0; kx < 4; ++kx) {
+        if (wx[kx] == 0.0f && gx[kx] == 0.0f) continue;
+        const int64_t node = (int64_t)(ncy + ky - 1) * row + (ncx + kx - 1);
+        if (!HG_INDEX_OK(node, nn, A.status)) continue;
+        const float w = wx[kx] * wy[ky];
+        float4 add = make_float4(w * mvx, w * mvy, 0.0f, 0.0f);
+        if (w != 0.0f) { // nodes of zero weight get no force (PhysicsGrid.cpp:439-441)
+          const float dX = gx[kx] * wy[ky], dY = wx[kx] * gy[ky];
+          add.z = s00 * dX + s01 * dY;
+          add.w = s01 * dX + s11 * dY;
+        }
+        atomicAdd(&A.accm[node], w * mv.x);
+        atomicAdd(&A.acc4[node], add);
+      }
+    }
+  }
+  if (nonfinite) atomicOr(A.status, (uint32_t)HG_STATUS_NONFINITE);
+  // points that changed cell: the re-sort trigger of the linear kernel
+  for (int o = 16; o > 0; o >>= 1) moved += __shfl_down_sync(0xffffffffu, moved, o);
+  if ((threadIdx.x & 31) == 0 && moved) atomicAdd(&A.outside[1], moved);
+}
+
 // Node update of one tile; one thread per node of the 16x16 tile.
 __device__ __forceinline__ void update_tile(const MixedArgs &A, const int tile) {
   float4 *va = A.va_out;
@@ -1062,6 +1240,7 @@ MixedArgs make_args(hg_mpm *m, double dt, bool tiles) {
   A.gx = (float)P.g[0];
   A.gy = (float)P.g[1];
   A.pmargin = 0.01f + 4.0e-7f * (float)(P.nx + P.ny);
+  A.hl = P.basis == HG_BASIS_UGIMP ? m->hl_cells : 0.0f;
   A.nplanes = P.nplanes;
   for (int k = 0; k < HG_MAX_PLANES; ++k) A.planes[k] = P.planes[k];
   A.offsets = m->offsets.p;
@@ -1198,6 +1377,20 @@ int update_per_sm(const hg_launch_shape &s) {
   return s.update_ctas_per_sm > 0 ? s.update_ctas_per_sm : DEFAULT_UPDATE_CTAS;
 }
 int fused_blocks(hg_mpm *m) { return m->ctx->num_sms * fused_per_sm(m->shape); }
+// the uGIMP kernel walks the points: up to 8 CTAs per SM
+int ugimp_blocks(hg_mpm *m) {
+  const int64_t b = (m->n + THREADS - 1) / THREADS;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)m->ctx->num_sms * 8));
+}
+// G2P of this step fused with P2G of the next (or the first P2G, PRIME)
+template <bool PRIME>
+void launch_particle_kernel(hg_mpm *m, const MixedArgs &A, cudaStream_t s) {
+  if (m->p.basis == HG_BASIS_UGIMP) {
+    HG_LAUNCH(kxu_step<PRIME>, ugimp_blocks(m), THREADS, 0, s, A);
+  } else {
+    HG_LAUNCH(kx_g2p2g<PRIME>, fused_blocks(m), THREADS, fused_smem_bytes(), s, A);
+  }
+}
 int update_blocks(hg_mpm *m) { return m->ctx->num_sms * update_per_sm(m->shape); }
 bool same_shape(const hg_launch_shape &a, const hg_launch_shape &b) {
   return a.fused_ctas_per_sm == b.fused_ctas_per_sm &&
@@ -1250,7 +1443,7 @@ hg_status prime(hg_mpm *m) {
   hg_status st = rebin(m);
   if (st != HG_OK) return st;
   MixedArgs A = make_args(m, 0.0, false);
-  HG_LAUNCH(kx_g2p2g<true>, fused_blocks(m), THREADS, fused_smem_bytes(), s, A);
+  launch_particle_kernel<true>(m, A, s);
   HG_CHECK_LAUNCH();
   m->primed = true;
   return HG_OK;
@@ -1403,7 +1596,7 @@ hg_status mixed_chunk_graph(hg_mpm *m, double dt) {
   hg_status st = HG_OK;
   for (int k = 0; k < CHUNK_STEPS && st == HG_OK; ++k) {
     HG_LAUNCH(kx_grid_update, update_blocks(m), THREADS, 0, s, At);
-    HG_LAUNCH(kx_g2p2g<false>, fused_blocks(m), THREADS, smem, s, Ab);
+    launch_particle_kernel<false>(m, Ab, s);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) st = cuda_fail(e, "kernel launch");
   }
@@ -1477,7 +1670,7 @@ hg_status mixed_step(hg_mpm *m, double dt, int nsteps) {
     HG_CHECK_LAUNCH();
     if (m->profile) HG_CUDA_TRY(cudaEventRecord(ev[1], s));
     MixedArgs Ab = make_args(m, dt, false);
-    HG_LAUNCH(kx_g2p2g<false>, fused_blocks(m), THREADS, smem, s, Ab);
+    launch_particle_kernel<false>(m, Ab, s);
     HG_CHECK_LAUNCH();
     if (m->profile) HG_CUDA_TRY(cudaEventRecord(ev[2], s));
     m->steps_since_rebin++;

@@ -136,6 +136,9 @@ void mpm_meta(const hg_mpm *m, int64_t meta[16]) {
   meta[5] = m->primed ? 1 : 0;
   meta[6] = m->steps_since_rebin;
   meta[7] = m->rebins;
+  int32_t hb;
+  std::memcpy(&hb, &m->hl_cells, sizeof hb);
+  meta[8] = hb; // uGIMP half-width in cells (MIXED)
 }
 
 // Segments of the live state; buf selects the particle buffer of the pair.
@@ -237,6 +240,8 @@ hg_status mpm_state_load(hg_mpm *m, const void *src, int64_t bytes) {
   m->primed = h.meta[5] != 0;
   m->steps_since_rebin = h.meta[6];
   m->rebins = h.meta[7];
+  const int32_t hb = (int32_t)h.meta[8];
+  std::memcpy(&m->hl_cells, &hb, sizeof hb);
   m->outside_pending = false;
   return HG_OK;
 }

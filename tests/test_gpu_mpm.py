@@ -189,6 +189,52 @@ def test_mixed_fast_particles_resort(ctx):
     assert g.rebin_count() >= 2
 
 
+def test_mixed_ugimp_against_the_oracle(ctx, cfg0):
+    """MIXED with the uGIMP basis (FP32 weights of the particle-size
+    integrated hat functions, 3 x 3 stencils near cell edges) against the
+    FP64 oracle with uGIMP: one-step grid-velocity error from a stressed FP64
+    state within the MIXED bound, and positions / J after 20 steps within the
+    linear path's tolerances."""
+    cfg = dict(cfg0, grid_min=(-0.01, -0.01))
+    c = cpu_mpm(cfg, basis=1)
+    p = scenes.seed_column_points(cfg)
+    c.set_particles(p["q"], p["v"], p["m"], p["vol"], p["hl"])
+    c.step(cfg["dt"], 200)
+    s = c.particles()
+    g = gpu_mpm(ctx, cfg, hg.MIXED, basis=hg.UGIMP)
+    g.upload(s["q"], s["v"], p["m"], p["vol"], p["hl"], s["be"], s["J"], s["jh"])
+    dt = cfg["dt"]
+    g.flow(dt)
+    c.step(dt)
+    G, C = g.grid(), c.grid()
+    # the edges of uGIMP supports carry weights down to FP32's underflow:
+    # compare on the nodes that hold a non-negligible mass
+    act = C["mass"] > 1e-6 * C["mass"].max()
+    assert (G["mass"][act] > 0).all()
+    assert (C["mass"][G["mass"] > 1e-6 * C["mass"].max()] > 0).all()
+    err = np.linalg.norm(G["vel"][act] - C["vel"][act]) / np.linalg.norm(C["vel"][act])
+    assert err <= 1e-5, err
+    assert rel(G["mass"], C["mass"]) <= 1e-6
+    P, Q = g.download(), c.particles()
+    assert np.abs(P["q"] - Q["q"]).max() <= 1e-12
+    g.flow(dt, 20)
+    c.step(dt, 20)
+    P, Q = g.download(), c.particles()
+    assert np.abs(P["q"] - Q["q"]).max() <= 1e-9
+    assert np.abs(P["J"] - Q["J"]).max() <= 1e-6
+    assert np.abs(P["be"] - Q["be"]).max() <= 1e-6
+    assert g.status() == 0
+    # one half-width for all points; batches take the linear basis
+    hl = p["hl"].copy()
+    hl[3] *= 1.5
+    with pytest.raises(hg.HGError):
+        g.upload(p["q"], p["v"], p["m"], p["vol"], hl)
+    b = hg.Batch(ctx, 2)
+    with pytest.raises(hg.HGError):
+        b.add(g, dt)
+    b.close()
+
+
 @pytest.mark.parametrize("precision", [0, 1])
 def test_cell_index_bit_exact(ctx, cfg0, precision):
     rng = np.random.default_rng(9)
@@ -231,5 +277,3 @@ def test_invalid_arguments_are_rejected(ctx, cfg0):
         g.upload(p["q"], p["v"], p["m"], p["vol"], p["hl"])  # over capacity
     with pytest.raises(hg.HGError):
         g.flow_zero_phase()  # phase calls need FP64
-    with pytest.raises(hg.HGError):
-        hg.MPM(ctx, (0, 0), (1, 1), 0.01, 1, 1, 0.3, 0.99, basis=hg.UGIMP, precision=hg.MIXED)
