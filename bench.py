@@ -197,6 +197,7 @@ def run_reference(args, rank, world):
 def run_ours(args, rank, world, local):
     import libhybridgrains_gb300 as hg
     from libhybridgrains_gb300 import build as gbuild
+    from libhybridgrains_gb300 import scenes as hg_scenes
     gbuild.build()
     ctx = hg.Context(local)
     cfg, pts = scene()
@@ -255,6 +256,30 @@ def run_ours(args, rank, world, local):
                 "grid_velocity_rel_error": vel_err,
                 "error_state": "after %d FP64 steps from rest" % (fsteps + 3)}
         del chk, f64
+
+    # ---- the uGIMP basis (the reference's shipped scenes use it) --------------------
+    ugimp = None
+    if args.ugimp_steps > 0:
+        cu = dict(cfg, grid_min=(cfg["grid_min"][0] - 4 * cfg["h"],
+                                 cfg["grid_min"][1] - 4 * cfg["h"]))
+        rates = {}
+        for name, prec, k in (("mixed", hg.MIXED, args.ugimp_steps), ("fp64", hg.FP64, 5)):
+            mu_ = hg.MPM(ctx, cu["grid_min"], cu["grid_max"], cu["h"], cu["shear_modulus"],
+                         cu["bulk_modulus"], cu["dp_alpha"], cu["flip_alpha"],
+                         hg_scenes.GRAVITY,
+                         cu["planes"], basis=hg.UGIMP, precision=prec, capacity=n)
+            mu_.upload(pts["q"], pts["v"], pts["m"], pts["vol"], pts["hl"])
+            mu_.flow(dt, 3)
+            ctx.synchronize()
+            ctx.timer_begin()
+            mu_.flow(dt, k)
+            ums = ctx.timer_end()
+            rates[name] = {"value": n * k / (ums * 1e-3), "ms_per_step": ums / k, "steps": k,
+                           "status": mu_.status()}
+            mu_.close()
+        ugimp = {"workload": "column_2M with the uGIMP basis (half-width h/4), grid extended by "
+                             "4 cells below and left", **rates,
+                 "speedup_mixed_over_fp64": rates["mixed"]["value"] / rates["fp64"]["value"]}
 
     # ---- end to end through the C ABI with host buffers --------------------------
     e2e = None
@@ -337,6 +362,7 @@ def run_ours(args, rank, world, local):
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "launch_shape": tune},
         "fp64": fp64,
+        "ugimp": ugimp,
         "roofline": {"bound": "hbm", "kernel": "kx_g2p2g", "achieved": achieved, "peak": peak,
                      "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "algorithmic_bytes": alg_bytes,
@@ -544,6 +570,7 @@ def main():
     ap.add_argument("--hybrid-steps", type=int, default=1000)
     ap.add_argument("--dem-cpu-steps", type=int, default=200)
     ap.add_argument("--tune-steps", type=int, default=20)
+    ap.add_argument("--ugimp-steps", type=int, default=200)
     ap.add_argument("--dem-large-disks", type=int, default=1000000)
     ap.add_argument("--dem-large-steps", type=int, default=200)
     ap.add_argument("--serve-requests", type=int, default=256)
