@@ -516,6 +516,16 @@ hg_status hg_dem_edit_async(hg_dem *d, int64_t n_old, const int32_t *old_to_new,
  * queued steps, without waiting (valid once a later fence is done). */
 hg_status hg_dem_frame_async(hg_dem *d, double *q, double *v);
 hg_status hg_dem_num_bodies(hg_dem *d, int64_t *n);
+/* Concurrent mode (no reference counterpart): on != 0 gives the DEM object a
+ * stream of its own, so its steps overlap the work queued on the context's
+ * stream; hg_dem_wait_context orders the DEM's later work after everything
+ * the context's stream has queued, hg_dem_join orders the context's later
+ * work (frames, fences) after everything the DEM has queued. Synchronous DEM
+ * calls synchronise the DEM's stream. A DEM in a hybrid step stays on the
+ * context's stream. */
+hg_status hg_dem_set_concurrent(hg_dem *d, int32_t on);
+hg_status hg_dem_wait_context(hg_dem *d);
+hg_status hg_dem_join(hg_dem *d);
 /* RigidBody2DState::updateCurrentMassUsingMassWeights
  * (RigidBody2DState.cpp:1182-1200). */
 hg_status hg_dem_set_weights(hg_dem *d, const double *w);

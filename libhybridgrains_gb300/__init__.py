@@ -450,6 +450,16 @@ class DEM:
     def frame_async(self, q=None, v=None):
         check("hg_dem_frame_async", self._h, _d(q), _d(v))
 
+    def set_concurrent(self, on=True):
+        """hg_dem_set_concurrent: run on a stream of its own."""
+        check("hg_dem_set_concurrent", self._h, 1 if on else 0)
+
+    def wait_context(self):
+        check("hg_dem_wait_context", self._h)
+
+    def join(self):
+        check("hg_dem_join", self._h)
+
     def state(self):
         """Bodies and contact history as a blob (hg_dem_state_save)."""
         return _save_blob("hg_dem_state", self._h)

@@ -159,6 +159,9 @@ SIGNATURES = {
     "hg_tune_save": [ctypes.c_char_p],
     "hg_tune_load": [ctypes.c_char_p],
     "hg_tune_clear": [],
+    "hg_dem_set_concurrent": [_P, _i32],
+    "hg_dem_wait_context": [_P],
+    "hg_dem_join": [_P],
     "hg_mpm_state_bytes": [_P, _I64],
     "hg_mpm_state_save": [_P, _P, _i64],
     "hg_mpm_state_load": [_P, _P, _i64],

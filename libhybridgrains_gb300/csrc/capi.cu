@@ -1214,11 +1214,63 @@ hg_status hg_dem_destroy(hg_dem *d) {
   hg_context *ctx = d->ctx;
   {
     DeviceGuard g(ctx);
+    if (d->own) cudaStreamSynchronize(d->own);
     cudaStreamSynchronize(ctx->stream);
     if (d->pair_exec) cudaGraphExecDestroy(d->pair_exec);
+    if (d->own) cudaStreamDestroy(d->own);
+    if (d->own_ev) cudaEventDestroy(d->own_ev);
+    if (d->ctx_ev) cudaEventDestroy(d->ctx_ev);
     delete d;
   }
   context_release(ctx);
+  return HG_OK;
+}
+
+// Concurrent mode: the DEM's work runs on a stream of its own, so that its
+// steps overlap work queued on the context's stream (the MPM steps of a
+// serving batch). The two streams meet only at hg_dem_wait_context (the DEM
+// waits for what the context's stream has queued) and hg_dem_join (the
+// context's stream waits for what the DEM has queued).
+hg_status hg_dem_set_concurrent(hg_dem *d, int32_t on) {
+  if (!d) return fail(HG_ERR_INVALID_ARGUMENT, "d is NULL");
+  DeviceGuard g(d->ctx);
+  if (on && !d->own) {
+    HG_CUDA_TRY(cudaStreamCreateWithFlags(&d->own, cudaStreamNonBlocking));
+    HG_CUDA_TRY(cudaEventCreateWithFlags(&d->own_ev, cudaEventDisableTiming));
+    HG_CUDA_TRY(cudaEventCreateWithFlags(&d->ctx_ev, cudaEventDisableTiming));
+    // everything queued so far (allocation, uploads) comes first
+    HG_CUDA_TRY(cudaEventRecord(d->ctx_ev, d->ctx->stream));
+    HG_CUDA_TRY(cudaStreamWaitEvent(d->own, d->ctx_ev, 0));
+  } else if (!on && d->own) {
+    HG_CUDA_TRY(cudaStreamSynchronize(d->own));
+    if (d->pair_exec) { // captured on the own stream; rebuilt on the next step
+      cudaGraphExecDestroy(d->pair_exec);
+      d->pair_exec = nullptr;
+    }
+    cudaStreamDestroy(d->own);
+    cudaEventDestroy(d->own_ev);
+    cudaEventDestroy(d->ctx_ev);
+    d->own = nullptr;
+    d->own_ev = d->ctx_ev = nullptr;
+  }
+  return HG_OK;
+}
+
+hg_status hg_dem_wait_context(hg_dem *d) {
+  if (!d) return fail(HG_ERR_INVALID_ARGUMENT, "d is NULL");
+  if (!d->own) return HG_OK;
+  DeviceGuard g(d->ctx);
+  HG_CUDA_TRY(cudaEventRecord(d->ctx_ev, d->ctx->stream));
+  HG_CUDA_TRY(cudaStreamWaitEvent(d->own, d->ctx_ev, 0));
+  return HG_OK;
+}
+
+hg_status hg_dem_join(hg_dem *d) {
+  if (!d) return fail(HG_ERR_INVALID_ARGUMENT, "d is NULL");
+  if (!d->own) return HG_OK;
+  DeviceGuard g(d->ctx);
+  HG_CUDA_TRY(cudaEventRecord(d->own_ev, d->own));
+  HG_CUDA_TRY(cudaStreamWaitEvent(d->ctx->stream, d->own_ev, 0));
   return HG_OK;
 }
 
@@ -1257,10 +1309,11 @@ static hg_status dem_upload_impl(hg_dem *d, int64_t n, const double *q, const do
     rmax = std::max(rmax, r[i]);
   }
   DeviceGuard g(d->ctx);
+  AllocScope dem_scope(dem_stream(d)); // temporaries on the DEM's stream
   // Broadphase cell width: the widest disk AABB plus a relative margin, so a
   // disk's partners lie in the 3x3 cells around the cell of its AABB minimum.
   d->cell_h = 2.0 * rmax * (1.0 + 1.0e-6);
-  cudaStream_t s = d->ctx->stream;
+  cudaStream_t s = dem_stream(d);
   d->n = n;
   d->inv_valid = false;
   hg_status st;
@@ -1307,6 +1360,7 @@ hg_status hg_dem_edit_async(hg_dem *d, int64_t n_old, const int32_t *old_to_new,
     rmax = std::max(rmax, r[i]);
   }
   DeviceGuard g(d->ctx);
+  AllocScope dem_scope(dem_stream(d)); // temporaries on the DEM's stream
   // the broadphase cell only grows: the candidate set does not depend on it
   d->cell_h = std::max(d->cell_h, 2.0 * rmax * (1.0 + 1.0e-6));
   return dem_edit(d, n_old, old_to_new, keep, n_add, q, v, r, mass, inertia, fixed);
@@ -1315,8 +1369,9 @@ hg_status hg_dem_edit_async(hg_dem *d, int64_t n_old, const int32_t *old_to_new,
 hg_status hg_dem_frame_async(hg_dem *d, double *q, double *v) {
   if (!d) return fail(HG_ERR_INVALID_ARGUMENT, "d is NULL");
   DeviceGuard g(d->ctx);
+  AllocScope dem_scope(dem_stream(d)); // temporaries on the DEM's stream
   hg_status st;
-  if ((st = d2h(d->ctx->stream, q, d->q.p, 3 * d->n)) || (st = d2h(d->ctx->stream, v, d->v.p, 3 * d->n)))
+  if ((st = d2h(dem_stream(d), q, d->q.p, 3 * d->n)) || (st = d2h(dem_stream(d), v, d->v.p, 3 * d->n)))
     return st;
   return HG_OK;
 }
@@ -1332,31 +1387,34 @@ hg_status hg_dem_set_weights(hg_dem *d, const double *w) {
   for (int64_t i = 0; i < d->n; ++i)
     if (!(w[i] >= 0.0 && w[i] <= 1.0)) return fail(HG_ERR_INVALID_ARGUMENT, "weights must lie in [0, 1]");
   DeviceGuard g(d->ctx);
-  hg_status st = h2d(d->ctx->stream, d->w.p, w, d->n);
+  AllocScope dem_scope(dem_stream(d)); // temporaries on the DEM's stream
+  hg_status st = h2d(dem_stream(d), d->w.p, w, d->n);
   if (st) return st;
   d->inv_valid = false;
-  HG_CUDA_TRY(cudaStreamSynchronize(d->ctx->stream));
+  HG_CUDA_TRY(cudaStreamSynchronize(dem_stream(d)));
   return HG_OK;
 }
 
 hg_status hg_dem_set_state(hg_dem *d, const double *q, const double *v) {
   if (!d) return fail(HG_ERR_INVALID_ARGUMENT, "d is NULL");
   DeviceGuard g(d->ctx);
+  AllocScope dem_scope(dem_stream(d)); // temporaries on the DEM's stream
   hg_status st;
-  if (q && (st = h2d(d->ctx->stream, d->q.p, q, 3 * d->n))) return st;
-  if (v && (st = h2d(d->ctx->stream, d->v.p, v, 3 * d->n))) return st;
-  HG_CUDA_TRY(cudaStreamSynchronize(d->ctx->stream));
+  if (q && (st = h2d(dem_stream(d), d->q.p, q, 3 * d->n))) return st;
+  if (v && (st = h2d(dem_stream(d), d->v.p, v, 3 * d->n))) return st;
+  HG_CUDA_TRY(cudaStreamSynchronize(dem_stream(d)));
   return HG_OK;
 }
 
 hg_status hg_dem_download(hg_dem *d, double *q, double *v) {
   if (!d) return fail(HG_ERR_INVALID_ARGUMENT, "d is NULL");
   DeviceGuard g(d->ctx);
+  AllocScope dem_scope(dem_stream(d)); // temporaries on the DEM's stream
   hg_status st;
-  if ((st = d2h(d->ctx->stream, q, d->q.p, 3 * d->n)) ||
-      (st = d2h(d->ctx->stream, v, d->v.p, 3 * d->n)))
+  if ((st = d2h(dem_stream(d), q, d->q.p, 3 * d->n)) ||
+      (st = d2h(dem_stream(d), v, d->v.p, 3 * d->n)))
     return st;
-  HG_CUDA_TRY(cudaStreamSynchronize(d->ctx->stream));
+  HG_CUDA_TRY(cudaStreamSynchronize(dem_stream(d)));
   return HG_OK;
 }
 
@@ -1370,7 +1428,7 @@ static hg_status dem_pair_graph(hg_dem *d, double dt, int weighted) {
     cudaGraphExecDestroy(d->pair_exec);
     d->pair_exec = nullptr;
   }
-  cudaStream_t s = d->ctx->stream;
+  cudaStream_t s = dem_stream(d);
   const int cc0 = d->cc;
   const bool hv0 = d->history_valid;
   const int64_t l0 = g_launches.load();
@@ -1412,6 +1470,7 @@ hg_status hg_dem_step(hg_dem *d, double dt, int32_t nsteps, int32_t weighted) {
   if (!(dt > 0.0) || !std::isfinite(dt)) return fail(HG_ERR_INVALID_ARGUMENT, "dt must be positive");
   if (nsteps < 0) return fail(HG_ERR_INVALID_ARGUMENT, "negative step count");
   DeviceGuard g(d->ctx);
+  AllocScope dem_scope(dem_stream(d)); // temporaries on the DEM's stream
   int k = 0;
   if (nsteps >= 4 && d->n > 0) {
     // Repeated steps replay a captured pair of steps: one graph launch in
@@ -1420,7 +1479,7 @@ hg_status hg_dem_step(hg_dem *d, double dt, int32_t nsteps, int32_t weighted) {
     if (st == HG_OK) st = dem_pair_graph(d, dt, weighted);
     if (st != HG_OK) return st;
     for (; k + 2 <= nsteps; k += 2) {
-      HG_CUDA_TRY(cudaGraphLaunch(d->pair_exec, d->ctx->stream));
+      HG_CUDA_TRY(cudaGraphLaunch(d->pair_exec, dem_stream(d)));
       g_launches.fetch_add(d->pair_launches, std::memory_order_relaxed);
     }
   }
@@ -1434,11 +1493,12 @@ hg_status hg_dem_step(hg_dem *d, double dt, int32_t nsteps, int32_t weighted) {
 hg_status hg_dem_num_contacts(hg_dem *d, int64_t *n) {
   if (!d || !n) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
   DeviceGuard g(d->ctx);
+  AllocScope dem_scope(dem_stream(d)); // temporaries on the DEM's stream
   int32_t c = 0;
   if (d->history_valid) {
     HG_CUDA_TRY(cudaMemcpyAsync(&c, d->c_count.p + d->cc, sizeof(int32_t),
-                                cudaMemcpyDeviceToHost, d->ctx->stream));
-    HG_CUDA_TRY(cudaStreamSynchronize(d->ctx->stream));
+                                cudaMemcpyDeviceToHost, dem_stream(d)));
+    HG_CUDA_TRY(cudaStreamSynchronize(dem_stream(d)));
   }
   *n = c;
   return HG_OK;
@@ -1447,15 +1507,17 @@ hg_status hg_dem_num_contacts(hg_dem *d, int64_t *n) {
 hg_status hg_dem_download_contacts(hg_dem *d, int64_t cap, double *rec, int64_t *count) {
   if (!d || !count || (cap > 0 && !rec)) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
   DeviceGuard g(d->ctx);
+  AllocScope dem_scope(dem_stream(d)); // temporaries on the DEM's stream
   return dem_download_contacts(d, cap, rec, count);
 }
 
 hg_status hg_dem_status(hg_dem *d, uint32_t *word) {
   if (!d || !word) return fail(HG_ERR_INVALID_ARGUMENT, "NULL argument");
   DeviceGuard g(d->ctx);
+  AllocScope dem_scope(dem_stream(d)); // temporaries on the DEM's stream
   HG_CUDA_TRY(cudaMemcpyAsync(word, d->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost,
-                              d->ctx->stream));
-  HG_CUDA_TRY(cudaStreamSynchronize(d->ctx->stream));
+                              dem_stream(d)));
+  HG_CUDA_TRY(cudaStreamSynchronize(dem_stream(d)));
   return HG_OK;
 }
 
@@ -1481,6 +1543,8 @@ hg_status hg_hybrid_create(hg_context *ctx, hg_mpm *m, hg_dem *d, hg_hybrid **ou
     return fail(HG_ERR_INVALID_ARGUMENT, "objects belong to another context");
   if (m->p.precision != HG_PRECISION_FP64)
     return fail(HG_ERR_UNSUPPORTED, "the hybrid step needs an FP64 MPM object");
+  if (d->own)
+    return fail(HG_ERR_UNSUPPORTED, "the hybrid step runs the DEM on the context's stream");
   DeviceGuard g(ctx);
   hg_hybrid *h = new (std::nothrow) hg_hybrid();
   if (!h) return fail(HG_ERR_OUT_OF_MEMORY, "host allocation failed");
@@ -1510,6 +1574,8 @@ hg_status hg_hybrid_destroy(hg_hybrid *h) {
 }
 
 hg_status hg_hybrid_step(hg_hybrid *h, double dt, int32_t nsteps, int32_t flags) {
+  if (h && h->d && h->d->own)
+    return fail(HG_ERR_UNSUPPORTED, "the hybrid step runs the DEM on the context's stream");
   HG_TRACE("hg_hybrid_step");
   if (!h) return fail(HG_ERR_INVALID_ARGUMENT, "h is NULL");
   if (!(dt > 0.0) || !std::isfinite(dt)) return fail(HG_ERR_INVALID_ARGUMENT, "dt must be positive");

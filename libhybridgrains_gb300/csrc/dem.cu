@@ -959,7 +959,7 @@ hg_status dem_alloc(hg_dem *d) {
       (st = d->in_off.alloc(N + 1)) || (st = d->in_list.alloc(C)) ||
       (st = d->in_cursor.alloc(N)) || (st = d->overflow.alloc(1)))
     return st;
-  cudaStream_t s = d->ctx->stream;
+  cudaStream_t s = dem_stream(d);
   HG_CUDA_TRY(cudaMemsetAsync(d->status.p, 0, sizeof(uint32_t), s));
   HG_CUDA_TRY(cudaMemsetAsync(d->c_count.p, 0, 2 * sizeof(int32_t), s));
   HG_CUDA_TRY(cudaStreamSynchronize(s));
@@ -967,14 +967,14 @@ hg_status dem_alloc(hg_dem *d) {
 }
 
 hg_status dem_reset_history(hg_dem *d) {
-  HG_CUDA_TRY(cudaMemsetAsync(d->c_count.p, 0, 2 * sizeof(int32_t), d->ctx->stream));
+  HG_CUDA_TRY(cudaMemsetAsync(d->c_count.p, 0, 2 * sizeof(int32_t), dem_stream(d)));
   d->history_valid = false;
   return HG_OK;
 }
 
 hg_status dem_prepare(hg_dem *d, double dt) {
   if ((d->inv_valid && d->terms_dt == dt) || d->n == 0) return HG_OK;
-  HG_LAUNCH(kd_body_terms, blocks_for(d->n, 256), 256, 0, d->ctx->stream, d->n, dt, d->p.g[0],
+  HG_LAUNCH(kd_body_terms, blocks_for(d->n, 256), 256, 0, dem_stream(d), d->n, dt, d->p.g[0],
             d->p.g[1], d->m0.p, d->I0.p, d->w.p, reinterpret_cast<double4 *>(d->minv.p));
   HG_CHECK_LAUNCH();
   d->inv_valid = true;
@@ -983,7 +983,7 @@ hg_status dem_prepare(hg_dem *d, double dt) {
 }
 
 hg_status dem_step(hg_dem *d, double dt, int weighted) {
-  cudaStream_t s = d->ctx->stream;
+  cudaStream_t s = dem_stream(d);
   const int64_t n = d->n;
   if (n == 0) return HG_OK;
   hg_status st;
@@ -1159,7 +1159,7 @@ __global__ void kd_relabel_move(int64_t ccap, const int32_t *__restrict__ count,
 
 hg_status dem_relabel_device(hg_dem *d, const int32_t *map, int64_t nmap) {
   if (!d->history_valid) return HG_OK;
-  cudaStream_t s = d->ctx->stream;
+  cudaStream_t s = dem_stream(d);
   const int64_t C = d->ccap;
   DevBuf<int32_t> keep, off, tmp;
   hg_status st;
@@ -1180,7 +1180,7 @@ hg_status dem_relabel_device(hg_dem *d, const int32_t *map, int64_t nmap) {
 
 hg_status dem_relabel(hg_dem *d, const int32_t *map_host, int64_t nmap) {
   if (!d->history_valid) return HG_OK;
-  cudaStream_t s = d->ctx->stream;
+  cudaStream_t s = dem_stream(d);
   DevBuf<int32_t> map;
   hg_status st;
   if ((st = map.alloc(std::max<int64_t>(nmap, 1)))) return st;
@@ -1227,7 +1227,7 @@ __global__ void kd_ones(double *a, int64_t n) {
 hg_status dem_edit(hg_dem *d, int64_t n_old, const int32_t *map_host, int64_t n_keep,
                    int64_t n_add, const double *q, const double *v, const double *r,
                    const double *m, const double *I, const uint8_t *fixed) {
-  cudaStream_t s = d->ctx->stream;
+  cudaStream_t s = dem_stream(d);
   hg_status st;
   DevBuf<int32_t> map;
   if (n_old > 0) {
@@ -1276,7 +1276,7 @@ hg_status dem_edit(hg_dem *d, int64_t n_old, const int32_t *map_host, int64_t n_
 
 
 hg_status dem_download_contacts(hg_dem *d, int64_t cap, double *rec, int64_t *count) {
-  cudaStream_t s = d->ctx->stream;
+  cudaStream_t s = dem_stream(d);
   int32_t c = 0;
   if (d->history_valid) {
     HG_CUDA_TRY(cudaMemcpyAsync(&c, d->c_count.p + d->cc, sizeof(int32_t),

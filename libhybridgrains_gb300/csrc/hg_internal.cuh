@@ -362,6 +362,10 @@ struct DemParams {
 
 struct hg_dem {
   hg_context *ctx = nullptr;
+  // concurrent mode (hg_dem_set_concurrent): the DEM runs on a stream of its
+  // own, ordered against the context's stream only at explicit joins
+  cudaStream_t own = nullptr;
+  cudaEvent_t own_ev = nullptr, ctx_ev = nullptr;
   hg::DemParams p{};
   int64_t cap = 0, ccap = 0, n = 0;
   hg::DevBuf<uint32_t> status;
@@ -403,6 +407,8 @@ struct hg_dem {
 };
 
 namespace hg {
+// the stream a DEM object's work runs on
+inline cudaStream_t dem_stream(const hg_dem *d) { return d->own ? d->own : d->ctx->stream; }
 hg_status dem_alloc(hg_dem *d);
 hg_status dem_reset_history(hg_dem *d);
 // renumber the contact history by old_to_new (-1: removed) of nmap bodies

@@ -190,8 +190,8 @@ hg_status dem_live_count(hg_dem *d, int32_t *count) {
   *count = 0;
   if (!d->history_valid) return HG_OK;
   HG_CUDA_TRY(cudaMemcpyAsync(count, d->c_count.p + d->cc, sizeof(int32_t), cudaMemcpyDeviceToHost,
-                              d->ctx->stream));
-  HG_CUDA_TRY(cudaStreamSynchronize(d->ctx->stream));
+                              dem_stream(d)));
+  HG_CUDA_TRY(cudaStreamSynchronize(dem_stream(d)));
   *count = (int32_t)std::min<int64_t>(*count, d->ccap);
   return HG_OK;
 }
@@ -264,7 +264,7 @@ hg_status dem_state_save(hg_dem *d, void *dst, int64_t bytes) {
   meta[2] = d->history_valid ? 1 : 0;
   std::memcpy(&meta[3], &d->cell_h, sizeof(double));
   meta[4] = d->ncontacts_host;
-  return write_blob(d->ctx->stream, KIND_DEM, meta, dem_segments(d, d->n, c, d->cc), dst, bytes);
+  return write_blob(dem_stream(d), KIND_DEM, meta, dem_segments(d, d->n, c, d->cc), dst, bytes);
 }
 
 hg_status dem_state_load(hg_dem *d, const void *src, int64_t bytes) {
@@ -275,11 +275,11 @@ hg_status dem_state_load(hg_dem *d, const void *src, int64_t bytes) {
   if (n < 0 || n > d->cap) return fail(HG_ERR_CAPACITY, "state blob holds more bodies than the capacity");
   if (c < 0 || c > d->ccap) return fail(HG_ERR_CAPACITY, "state blob holds more contacts than the capacity");
   // the live contact history becomes buffer 0
-  if ((st = read_segments(d->ctx->stream, src, bytes, h, dem_segments(d, n, c, 0)))) return st;
+  if ((st = read_segments(dem_stream(d), src, bytes, h, dem_segments(d, n, c, 0)))) return st;
   const int32_t c32 = (int32_t)c;
   HG_CUDA_TRY(cudaMemcpyAsync(d->c_count.p, &c32, sizeof(int32_t), cudaMemcpyHostToDevice,
-                              d->ctx->stream));
-  HG_CUDA_TRY(cudaStreamSynchronize(d->ctx->stream));
+                              dem_stream(d)));
+  HG_CUDA_TRY(cudaStreamSynchronize(dem_stream(d)));
   d->n = n;
   d->cc = 0;
   d->history_valid = h.meta[2] != 0;

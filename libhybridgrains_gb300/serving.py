@@ -368,6 +368,8 @@ class DeviceBackend(Backend):
         """One DEM edit: drop the piles that left, append the opened ones."""
         if self.dem is None:
             self.dem = dem_for_piles(self.ctx, self.dem_capacity)
+            # the piles step on a stream of their own, beside the MPM batch
+            self.dem.set_concurrent(True)
         n_old = sum(r.ndisks for r in self.order)
         old_to_new = np.full(n_old, -1, dtype=np.int32)
         keep, o, k = [], 0, 0
@@ -395,7 +397,7 @@ class DeviceBackend(Backend):
                 o += r.ndisks
         self.dem.edit_async(old_to_new, **arrays)
         if n_add:
-            self.staging.append((self.ctx.fence(), buf))
+            self.staging.append((self.fence(), buf))
         self.order = keep + [r for r, _ in self.adds]
         self.adds, self.drops = [], set()
 
@@ -404,9 +406,9 @@ class DeviceBackend(Backend):
             self._give(self.staging.pop(0)[1])
         if self.adds or self.drops:
             self._edit_piles()
-        self.batch.step(nsteps)
+        self.batch.step(nsteps)  # on the context's stream
         if self.dem is not None and self.dem.n > 0:
-            self.dem.flow(self.dem_dt, nsteps)
+            self.dem.flow(self.dem_dt, nsteps)  # on the DEM's stream, concurrently
         self.chunk += 1
 
     def frame(self, req, slot):
@@ -431,6 +433,8 @@ class DeviceBackend(Backend):
             self.drops.add(req.rid)
 
     def fence(self):
+        if self.dem is not None:
+            self.dem.join()  # the fence covers the DEM's steps, edits and frames
         return self.ctx.fence()
 
     def fence_done(self, f):

@@ -229,3 +229,44 @@ def test_mixed_precision_against_fp64(ctx):
     assert mix.status() == 0
     for d in (base, f64, mix):
         d.close()
+
+
+def test_concurrent_stream_gives_the_same_steps(ctx):
+    """A DEM object in concurrent mode (its own stream) steps, edits and
+    copies frames exactly as on the context's stream, the MPM work queued in
+    between notwithstanding; join orders the context's later work after it."""
+    from libhybridgrains_gb300 import serving
+
+    def pile(rid, n, lane):
+        return serving.dem_pile(serving.Request(rid, 0.0, None, 0, ndisks=n, aspect=1.5), lane)
+
+    A, B = pile(1, 800, 0), pile(2, 500, 1)
+    cfg = scenes.serving_column(20000, 1.5, 30.0)
+    p = scenes.seed_column_points(cfg)
+    out = []
+    for concurrent in (False, True):
+        d = serving.dem_for_piles(ctx, 2000)
+        d.set_concurrent(concurrent)
+        d.edit_async(np.zeros(0, dtype=np.int32), **{f: A[f] for f in ("q", "v", "r", "m", "I")})
+        m = hg.MPM(ctx, cfg["grid_min"], cfg["grid_max"], cfg["h"], cfg["shear_modulus"],
+                   cfg["bulk_modulus"], cfg["dp_alpha"], cfg["flip_alpha"], scenes.GRAVITY,
+                   cfg["planes"], capacity=len(p["m"]))
+        m.upload(p["q"], p["v"], p["m"], p["vol"], p["hl"])
+        frame = hg.pinned((2000, 3))
+        for k in range(3):
+            m.flow(cfg["dt"], 100)       # context stream
+            d.flow(1e-5, 100)            # DEM stream in concurrent mode
+            if k == 1:
+                d.edit_async(np.arange(800, dtype=np.int32),
+                             **{f: B[f] for f in ("q", "v", "r", "m", "I")})
+        d.frame_async(frame[:d.n])
+        d.join()
+        f = ctx.fence()
+        ctx.fence_wait(f)
+        out.append((frame[:d.n].copy(), d.download()[0], d.contacts(), d.status()))
+        m.close()
+        d.close()
+    (fa, qa, ca, sa), (fb, qb, cb, sb) = out
+    assert sa == 0 and sb == 0
+    assert np.array_equal(fa, qa) and np.array_equal(fb, qb)  # frames landed by the fence
+    assert np.array_equal(qa, qb) and np.array_equal(ca, cb)
