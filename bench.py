@@ -17,7 +17,12 @@ the large mixed-precision configuration. Prints one JSON line:
              over the host cores) on a bounded sample of the same workload.
 
 ``--impl reference`` times the CPU oracle alone on the same workload (the
-reference itself cannot be built here).
+reference itself needs Eigen and RapidXML, which are not available, so its
+own build cannot run).
+
+The line also carries the batched serving loop (``serving``), the DEM column
+and a 1,000,000-disk pile (``dem``), the hybrid column (``hybrid``) and the
+column with the uGIMP basis (``ugimp``).
 Multi-GPU runs are replicas: every rank steps its own copy of the scene.
 """
 import argparse
