@@ -3,7 +3,8 @@
 An FP64 C++ restatement of the reference's per-step MPM, penalty-DEM and
 node-node coupling code, loaded through ctypes. Only ``tests/``,
 ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` use it,
-always as the checker or the timed CPU baseline, never as the product path.
+always as the reference the GPU results are compared with or as the timed CPU
+baseline, never as the product path.
 
 Parity with the reference binary is unpinned: the reference needs Eigen 3.3.3
 and RapidXML 1.13, which are absent, and its own tests hold no golden vectors

@@ -2,7 +2,7 @@
 // helpers.
 //
 // TEST INFRASTRUCTURE ONLY. Nothing in the product library links, loads or
-// calls this code; it is the checker that the CUDA path is compared against,
+// calls this code; the tests compare the CUDA path against it,
 // and the CPU baseline that bench.py times beside the GPU numbers.
 //
 // The reference evaluates these operations through Eigen 3.3 fixed-size
