@@ -322,7 +322,7 @@ def run_ours(args, rank, world, local):
 
     serve = None
     if args.serve_requests > 0:
-        serve = run_serving(args, ctx)
+        serve = run_serving(args, ctx, rank, world)
     dem = None
     if args.dem_steps > 0:
         dem = run_dem(args, ctx)
@@ -503,43 +503,63 @@ def run_hybrid(args, ctx):
             "status": [sim.mpm.status(), sim.dem.status()]}
 
 
-def run_serving(args, ctx):
+def gather_parts(part, world):
+    """Every rank's summary_parts (one object per rank)."""
+    if world <= 1:
+        return [part]
+    import torch.distributed as dist
+    out = [None] * world
+    dist.all_gather_object(out, part)
+    return out
+
+
+def run_serving(args, ctx, rank=0, world=1):
     """Batched serving of column-collapse requests: Poisson arrivals with
     continuous batching (latency), the same requests all queued at once
-    (saturated throughput) and served one scene at a time (baseline)."""
+    (saturated throughput) and served one scene at a time (baseline). With
+    several ranks each serves its share of the requests on its own GPU
+    (serving.shard_requests) and the figures cover all of them."""
     from libhybridgrains_gb300 import serving
 
     def copies(reqs, at_once=False):
         return [r.copy(0.0 if at_once else None) for r in reqs]
 
     budget = int(args.serve_budget_gb * 2**30)
-    reqs = serving.column_requests(n=args.serve_requests, rate=args.serve_rate,
-                                   steps=args.serve_steps, seed=2024)
+    all_reqs = serving.column_requests(n=args.serve_requests, rate=args.serve_rate,
+                                       steps=args.serve_steps, seed=2024)
+    reqs = serving.shard_requests(all_reqs, rank, world)
     be = serving.DeviceBackend(ctx, max_members=min(256, args.serve_requests))
     # warm-up: a few short requests (library load, pools)
     serving.Server(be, budget).run(copies(serving.column_requests(n=8, rate=1e3, steps=200,
                                                                    seed=7)))
     launches0 = __import__("libhybridgrains_gb300").kernel_launch_count()
+    barrier(world)
     srv = serving.Server(be, budget, max_members=min(256, args.serve_requests))
     live = srv.run(copies(reqs))
-    poisson = serving.summary(live, srv.makespan)
+    poisson = serving.summary_of_parts(gather_parts(serving.summary_parts(live, srv.makespan),
+                                                    world))
     launches = __import__("libhybridgrains_gb300").kernel_launch_count() - launches0
+    barrier(world)
     srv2 = serving.Server(be, budget, max_members=min(256, args.serve_requests))
     sat_reqs = srv2.run(copies(reqs, at_once=True))
-    saturated = serving.summary(sat_reqs, srv2.makespan)
+    saturated = serving.summary_of_parts(
+        gather_parts(serving.summary_parts(sat_reqs, srv2.makespan), world))
     be.shutdown()
     alone = copies(reqs)
-    alone_s = serving.run_one_at_a_time(ctx, alone)
-    psteps = float(sum(r.npoints * r.steps for r in reqs))
-    dsteps = float(sum(r.ndisks * r.steps for r in reqs))
-    diff = max(serving.frame_diff(a[1], b[1])
-               for r1, r2 in zip(live, alone) for a, b in zip(r1.frames, r2.frames))
+    barrier(world)
+    alone_s = barrier_max(serving.run_one_at_a_time(ctx, alone), world)
+    psteps = float(sum(r.npoints * r.steps for r in all_reqs))
+    dsteps = float(sum(r.ndisks * r.steps for r in all_reqs))
+    diff = barrier_max(max((serving.frame_diff(a[1], b[1])
+                            for r1, r2 in zip(live, alone) for a, b in zip(r1.frames, r2.frames)),
+                           default=0.0), world)
     return {
         "workload": "%d column-collapse requests, Poisson arrivals %.0f/s (seed 2024), points "
                     "log-U[2e3,2e5], aspect U[0.5,4], friction angle U[20,40] deg, a DEM pile "
                     "of U[0,0.2] x the point count in disks, %d steps, a frame (positions) "
-                    "every 100 steps" % (len(reqs), args.serve_rate, args.serve_steps),
-        "disks": int(sum(r.ndisks for r in reqs)),
+                    "every 100 steps" % (len(all_reqs), args.serve_rate, args.serve_steps),
+        "ranks": world,
+        "disks": int(sum(r.ndisks for r in all_reqs)),
         "p50_latency_s": poisson["p50_latency_s"], "p99_latency_s": poisson["p99_latency_s"],
         "max_latency_s": poisson["max_latency_s"],
         "p99_admission_wait_s": poisson["p99_admission_wait_s"],
@@ -556,7 +576,7 @@ def run_serving(args, ctx):
                       "makespan_s": saturated["makespan_s"]},
         "one_at_a_time": {"particle_steps_per_s": psteps / alone_s,
                           "disk_steps_per_s": dsteps / alone_s,
-                          "requests_per_s": len(reqs) / alone_s, "seconds": alone_s},
+                          "requests_per_s": len(all_reqs) / alone_s, "seconds": alone_s},
         "batched_over_one_at_a_time": saturated["particle_steps_per_s"] * alone_s / psteps,
         "max_frame_front_diff_m": diff,
     }

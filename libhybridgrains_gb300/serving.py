@@ -273,12 +273,32 @@ class Server:
         closing[:] = keep
 
 
-def summary(requests, makespan):
-    lat = np.array([r.latency for r in requests])
-    wait = np.array([r.admitted - r.arrival for r in requests])
-    psteps = float(sum(r.npoints * r.steps for r in requests))
-    dsteps = float(sum(r.ndisks * r.steps for r in requests))
-    return dict(requests=len(requests), p50_latency_s=float(np.percentile(lat, 50)),
+def shard_requests(requests, rank, world):
+    """The requests rank serves out of world ranks, one GPU each: every
+    world-th request in arrival order (scenes are independent, so the ranks
+    exchange nothing while they serve)."""
+    ordered = sorted(requests, key=lambda r: (r.arrival, r.rid))
+    return ordered[rank::world]
+
+
+def summary_parts(requests, makespan):
+    """The raw figures of one rank's run, for summary_of_parts."""
+    return dict(latencies=[float(r.latency) for r in requests],
+                waits=[float(r.admitted - r.arrival) for r in requests],
+                particle_steps=float(sum(r.npoints * r.steps for r in requests)),
+                disk_steps=float(sum(r.ndisks * r.steps for r in requests)),
+                makespan_s=float(makespan))
+
+
+def summary_of_parts(parts):
+    """Latency percentiles over all ranks' requests; throughput over the
+    slowest rank's makespan."""
+    lat = np.array([x for p in parts for x in p["latencies"]])
+    wait = np.array([x for p in parts for x in p["waits"]])
+    psteps = sum(p["particle_steps"] for p in parts)
+    dsteps = sum(p["disk_steps"] for p in parts)
+    makespan = max(p["makespan_s"] for p in parts)
+    return dict(requests=len(lat), p50_latency_s=float(np.percentile(lat, 50)),
                 p99_latency_s=float(np.percentile(lat, 99)),
                 max_latency_s=float(lat.max()),
                 p50_admission_wait_s=float(np.percentile(wait, 50)),
@@ -286,7 +306,11 @@ def summary(requests, makespan):
                 makespan_s=makespan, particle_steps=psteps,
                 particle_steps_per_s=psteps / makespan,
                 disk_steps=dsteps, disk_steps_per_s=dsteps / makespan,
-                requests_per_s=len(requests) / makespan)
+                requests_per_s=len(lat) / makespan)
+
+
+def summary(requests, makespan):
+    return summary_of_parts([summary_parts(requests, makespan)])
 
 
 class DeviceBackend(Backend):
