@@ -23,24 +23,32 @@ which accumulates the current step a second time inside the branch.
 """
 import numpy as np
 
-from . import DEM, FP64, MPM, Hybrid, Resampler, Zones, scenes
+from . import DEM, FP64, MPM, Hybrid, Resampler, Zones, scene_xml, scenes
 
 
 class HybridSim:
-    def __init__(self, ctx, scene, basis=1, point_headroom=2.0, grain_headroom=3.0):
+    def __init__(self, ctx, scene, basis=None, point_headroom=2.0, grain_headroom=3.0):
         cfg, sc, dp = scene["mpm"], scene["dem"], scene["dem_params"]
         zs, rs = scene["zones"], scene["resampling"]
         self.ctx, self.cfg, self.dt = ctx, cfg, cfg["dt"]
-        p = scenes.seed_column_points(cfg)
+        if basis is None:  # the continuum scene's basis, uGIMP where it names none
+            basis = 0 if cfg.get("basis") == "linear" else 1
+        # scenes read from the reference's files seed every rectangle with its
+        # velocity; the library's column scenes seed one at rest
+        p = scene_xml.seed_points(cfg) if "rectangles" in cfg else scenes.seed_column_points(cfg)
         n, nd = len(p["m"]), len(sc["r"])
+        gravity = cfg.get("gravity", scenes.GRAVITY)
         self.mpm = MPM(ctx, cfg["grid_min"], cfg["grid_max"], cfg["h"], cfg["shear_modulus"],
-                       cfg["bulk_modulus"], cfg["dp_alpha"], cfg["flip_alpha"], scenes.GRAVITY,
+                       cfg["bulk_modulus"], cfg["dp_alpha"], cfg["flip_alpha"], gravity,
                        cfg["planes"], basis=basis, precision=FP64,
                        capacity=int(point_headroom * n) + 1024)
         self.mpm.upload(p["q"], p["v"], p["m"], p["vol"], p["hl"])
-        planes = [(pl[0], pl[1]) for pl in cfg["planes"]]  # the same walls for the grains
-        self.dem = DEM(ctx, scenes.GRAVITY, dp["kn"], dp["kt"], dp["gamman"], dp["gammat"],
-                       dp["mu"], planes, capacity=int(grain_headroom * nd) + 1024)
+        # the discrete scene's planes, else the continuum's walls for the grains too
+        planes = dp.get("planes") or [(pl[0], pl[1]) for pl in cfg["planes"]]
+        # (the spatial grid's cell is one mean diameter in hybrid runs, whatever
+        # the discrete scene's cell_scale)
+        self.dem = DEM(ctx, dp.get("gravity", gravity), dp["kn"], dp["kt"], dp["gamman"],
+                       dp["gammat"], dp["mu"], planes, capacity=int(grain_headroom * nd) + 1024)
         self.dem.upload(sc["q"], sc["v"], sc["r"], sc["m"], sc["I"], sc["fixed"])
         self.hyb = Hybrid(ctx, self.mpm, self.dem)
         g = self.mpm

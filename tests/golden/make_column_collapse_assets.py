@@ -2,7 +2,7 @@
 (assets/hybridgrains2dnew/column-collapse/{hybrid,mpm,dem}.xml) as test
 inputs:
 
-* column_collapse_dem.npz: the 6,695 disks (x, y, theta, r, fixed), in file
+* column_collapse_dem.npz: the 6,694 disks (x, y, theta, r, fixed), in file
   order;
 * column_collapse_scene.json: the MPM grid, material, rectangle and planes,
   the DEM penalty parameters and the hybrid (zone / resampling) settings.

@@ -7,7 +7,7 @@ Everything here is bit-exact: packing fractions, signed distances, level-set
 and MPM cell labels, zone lists, deletion lists and weights are FP64 results
 that feed threshold tests, so they must agree to the last bit. Inputs are the
 reference's column-collapse hybrid scene (tests/golden/column_collapse_*,
-made by tests/golden/make_column_collapse_assets.py): 6,695 disks of the
+made by tests/golden/make_column_collapse_assets.py): 6,694 disks of the
 settled column, with and without a block of MPM points, over successive
 updates so that the hysteresis on the previous labels is exercised.
 """
