@@ -20,11 +20,12 @@ def frame_path(directory, frame, width=5, stem="config"):
     return os.path.join(directory, "%s_%0*d.npz" % (stem, width, frame))
 
 
-def mpm_frame(mpm, cfg, m, volume, hl=None, prefix="mpm"):
+def mpm_frame(mpm, cfg, m, volume, hl=None, prefix="mpm", hybrid_factors=None):
     """Datasets of one MPM frame from a device object and the host-held
     masses and volumes: npoints, q, v, m, r (the half widths), J, jhf, the
-    grid node positions, masses and hybrid factors, and the pressure
-    -tr(sigma) / 2 per point."""
+    grid node positions, masses and hybrid factors (zero unless given), and
+    the pressure -tr(sigma) / 2 per point. An empty prefix puts them at the
+    file's root, as mpmgrains2d_cli does (writeBinaryState with group "")."""
     st = mpm.download()
     G = mpm.grid()
     n = len(st["q"])
@@ -41,8 +42,10 @@ def mpm_frame(mpm, cfg, m, volume, hl=None, prefix="mpm"):
     out = {"npoints": np.array(n, dtype=np.uint32), "q": st["q"].T.copy(), "v": st["v"].T.copy(),
            "m": np.asarray(m, dtype=np.float64), "r": hl, "J": st["J"], "jhf": st["jh"],
            "grid_node_positions": nodes, "grid_node_masses": G["mass"],
-           "grid_node_hybrid_factors": np.zeros(len(G["mass"])), "p": p}
-    return {prefix + "/" + k: v for k, v in out.items()}
+           "grid_node_hybrid_factors": (np.zeros(len(G["mass"])) if hybrid_factors is None
+                                        else np.asarray(hybrid_factors, dtype=np.float64)),
+           "p": p}
+    return {(prefix + "/" if prefix else "") + k: v for k, v in out.items()}
 
 
 def dem_frame(dem, radius, mass, fixed=None):
