@@ -83,7 +83,10 @@ def main():
                    "phi_window_size": float(cf.get("phi_window_size")),
                    "phi_samples_per_cell_side": int(cf.get("phi_samples_per_cell_side")),
                    "level_set_cell_width": float(cf.get("level_set_cell_width")),
-                   "rho_dem": float(cf.get("rho_dem"))},
+                   "rho_dem": float(cf.get("rho_dem")),
+                   "homogenize_stress": int(cf.get("homogenize_stress", "0")) != 0,
+                   "homogenize_velocity": int(cf.get("homogenize_velocity", "0")) != 0,
+                   "end_time": float(hyb.find("end_time").get("t"))},
     }
     with open(os.path.join(HERE, "column_collapse_scene.json"), "w") as f:
         json.dump(scene, f, indent=1)
