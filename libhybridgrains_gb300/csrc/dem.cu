@@ -142,6 +142,9 @@ struct HomeArgs {
   const uint8_t *fixed;
   float4 *rec; // 2 per body: (offset x, offset y, radius, flags), (home cell x, y)
   int32_t *bucket_count;
+  // this step's per-body counters, zeroed here in place of memsets: contact
+  // counts (3n + 1), pair fill (n), incoming counts (n + 1) and cursors (n)
+  int32_t *per_body, *pfill, *in_count, *in_cursor;
 };
 
 enum : uint32_t { REL_FIXED = 1u, REL_PLANE0 = 2u };
@@ -149,6 +152,14 @@ enum : uint32_t { REL_FIXED = 1u, REL_PLANE0 = 2u };
 __global__ void kd_bodies_home(HomeArgs A) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= A.n) return;
+  A.per_body[3 * i] = A.per_body[3 * i + 1] = A.per_body[3 * i + 2] = 0;
+  A.pfill[i] = 0;
+  A.in_count[i] = 0;
+  A.in_cursor[i] = 0;
+  if (i == 0) {
+    A.per_body[3 * A.n] = 0;
+    A.in_count[A.n] = 0;
+  }
   // CircleGeometry::computeCollisionAABB (CircleGeometry.cpp:22-30), q0 == q1
   const double x = A.q[3 * i], y = A.q[3 * i + 1], ri = A.r[i];
   const int cx = (int)floor((x - ri) * A.invH), cy = (int)floor((y - ri) * A.invH);
@@ -1010,6 +1021,10 @@ hg_status dem_step(hg_dem *d, double dt, int weighted) {
     H.fixed = d->fixed.p;
     H.rec = d->brec.p;
     H.bucket_count = d->bcount.p;
+    H.per_body = d->per_body.p;
+    H.pfill = d->pfill.p;
+    H.in_count = d->in_count.p;
+    H.in_cursor = d->in_cursor.p;
     HG_LAUNCH(kd_bodies_home, blocks_for(n, 256), 256, 0, s, H);
     HG_CHECK_LAUNCH();
     if ((st = exclusive_scan_i32(d->bcount.p, d->bstart.p, T, d->scan_tmp.p, s))) return st;
@@ -1038,22 +1053,37 @@ hg_status dem_step(hg_dem *d, double dt, int weighted) {
   A.overflow = d->overflow.p;
   A.status = d->status.p;
   A.pfill = d->pfill.p;
-  HG_CUDA_TRY(cudaMemsetAsync(d->per_body.p, 0, sizeof(int32_t) * (3 * n + 1), s));
-  HG_CUDA_TRY(cudaMemsetAsync(d->pfill.p, 0, sizeof(int32_t) * n, s));
+  // (per_body and pfill were zeroed by kd_bodies_home)
   HG_LAUNCH(kd_pairs_count, blocks_for(n, 128), 128, 0, s, A);
   HG_CHECK_LAUNCH();
-  if ((st = exclusive_scan_i32(d->per_body.p, d->per_body_off.p, 3 * n + 1, d->scan_tmp.p, s)))
-    return st;
-  HG_LAUNCH(kd_check_capacity, 1, 32, 0, s, n, d->per_body_off.p, d->ccap, d->overflow.p,
-            d->status.p);
-  HG_CHECK_LAUNCH();
-  HG_LAUNCH(kd_drop_if_overflow, blocks_for(3 * n + 1, 256), 256, 0, s, n, d->overflow.p,
-            d->per_body.p, d->per_body_off.p);
-  HG_CHECK_LAUNCH();
+  // offsets, the contact-capacity check (all contacts dropped when the list
+  // would overflow) and the contact count
+  const bool small = 3 * n + 1 <= small_scan_max();
+  if (small) {
+    ScanLimit lim;
+    lim.limit = d->ccap;
+    lim.overflow = d->overflow.p;
+    lim.status = d->status.p;
+    lim.status_bit = HG_STATUS_CONTACT_OVERFLOW;
+    lim.total = d->c_count.p + nb;
+    if ((st = exclusive_scan_i32_limited(d->per_body.p, d->per_body_off.p, 3 * n + 1, lim, s)))
+      return st;
+  } else {
+    if ((st = exclusive_scan_i32(d->per_body.p, d->per_body_off.p, 3 * n + 1, d->scan_tmp.p,
+                                 s)))
+      return st;
+    HG_LAUNCH(kd_check_capacity, 1, 32, 0, s, n, d->per_body_off.p, d->ccap, d->overflow.p,
+              d->status.p);
+    HG_CHECK_LAUNCH();
+    HG_LAUNCH(kd_drop_if_overflow, blocks_for(3 * n + 1, 256), 256, 0, s, n, d->overflow.p,
+              d->per_body.p, d->per_body_off.p);
+    HG_CHECK_LAUNCH();
+  }
   HG_LAUNCH(kd_pairs_emit, blocks_for(n, 128), 128, 0, s, A);
   HG_CHECK_LAUNCH();
-  HG_CUDA_TRY(cudaMemcpyAsync(d->c_count.p + nb, d->per_body_off.p + 3 * n, sizeof(int32_t),
-                              cudaMemcpyDeviceToDevice, s));
+  if (!small)
+    HG_CUDA_TRY(cudaMemcpyAsync(d->c_count.p + nb, d->per_body_off.p + 3 * n, sizeof(int32_t),
+                                cudaMemcpyDeviceToDevice, s));
   ContactArgs Cg;
   Cg.n = n;
   Cg.dt = dt;
@@ -1086,8 +1116,7 @@ hg_status dem_step(hg_dem *d, double dt, int weighted) {
   else
     HG_LAUNCH(kd_contacts, d->ctx->num_sms * 4, 256, 0, s, Cg);
   HG_CHECK_LAUNCH();
-  HG_CUDA_TRY(cudaMemsetAsync(d->in_count.p, 0, sizeof(int32_t) * (n + 1), s));
-  HG_CUDA_TRY(cudaMemsetAsync(d->in_cursor.p, 0, sizeof(int32_t) * n, s));
+  // (in_count and in_cursor were zeroed by kd_bodies_home)
   HG_LAUNCH(kd_in_count, d->ctx->num_sms * 2, 256, 0, s, n, d->per_body_off.p, d->ckey[nb].p,
             d->in_count.p);
   HG_CHECK_LAUNCH();

@@ -430,6 +430,21 @@ hg_status dem_candidate_pairs(hg_context *ctx, int64_t n, const double *mn,
 hg_status exclusive_scan_i32(const int32_t *in, int32_t *out, int64_t n,
                              int32_t *tmp, cudaStream_t s);
 int64_t scan_tmp_size(int64_t n);
+// A capacity limit checked by the scan that produces the offsets: when the
+// total exceeds limit (>= 0), *overflow is set, status_bit raised in
+// *status and every count and offset written as zero; *total (when given)
+// receives the total, or 0 when the limit is exceeded.
+struct ScanLimit {
+  int64_t limit = -1;
+  int32_t *overflow = nullptr;
+  uint32_t *status = nullptr;
+  uint32_t status_bit = 0;
+  int32_t *total = nullptr;
+};
+// The largest n exclusive_scan_i32_limited takes (one CTA, one launch).
+int64_t small_scan_max();
+hg_status exclusive_scan_i32_limited(int32_t *in, int32_t *out, int64_t n, const ScanLimit &lim,
+                                     cudaStream_t s);
 } // namespace hg
 
 struct hg_hybrid {

@@ -53,7 +53,82 @@ __global__ void k_tile_scan(const int32_t *__restrict__ in, int64_t n,
   }
 }
 
+// Up to small_scan_max() elements: one CTA and one launch in place of three
+// (in a captured step the launches, not the bytes, are the cost at these
+// sizes). Warp w owns the 1024 consecutive elements from w * 1024 and reads
+// them 32 at a time with coalesced loads; 32 warp scans with a running
+// carry give each element its prefix within the warp's segment, one scan of
+// the 32 warp totals the segment offsets. No large shared-memory staging, so
+// the launch needs no change of the shared-memory carve-out.
+constexpr int SMALL_THREADS = 1024;
+constexpr int SMALL_ITEMS = 32;
+constexpr int SMALL_N = SMALL_THREADS * SMALL_ITEMS;
+
+__global__ void __launch_bounds__(SMALL_THREADS)
+    k_small_scan(int32_t *__restrict__ in, int64_t n64, int32_t *__restrict__ out, ScanLimit lim) {
+  __shared__ int s_warp[SMALL_THREADS / 32];
+  __shared__ int s_total;
+  const int n = (int)n64; // <= SMALL_N
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int seg = wid * (SMALL_ITEMS * 32);
+  int v[SMALL_ITEMS];
+#pragma unroll
+  for (int k = 0; k < SMALL_ITEMS; ++k) {
+    const int i = seg + k * 32 + lane;
+    v[k] = i < n ? in[i] : 0;
+  }
+  int carry = 0;
+#pragma unroll
+  for (int k = 0; k < SMALL_ITEMS; ++k) {
+    const int inc = warp_incl_scan(v[k]);
+    const int tot = __shfl_sync(0xffffffffu, inc, 31);
+    v[k] = carry + inc - v[k]; // exclusive prefix within the segment
+    carry += tot;
+  }
+  if (lane == 0) s_warp[wid] = carry;
+  __syncthreads();
+  if (wid == 0) {
+    const int w = s_warp[lane];
+    const int inc = warp_incl_scan(w);
+    s_warp[lane] = inc - w;
+    if (lane == 31) s_total = inc;
+  }
+  __syncthreads();
+  const int off = s_warp[wid], total = s_total;
+  // the same decision in every thread: the total is block-wide
+  const bool over = lim.limit >= 0 && (int64_t)total > lim.limit;
+  if (threadIdx.x == 0) {
+    if (lim.overflow) *lim.overflow = over ? 1 : 0;
+    if (over && lim.status) atomicOr(lim.status, lim.status_bit);
+    if (lim.total) *lim.total = over ? 0 : total;
+  }
+#pragma unroll
+  for (int k = 0; k < SMALL_ITEMS; ++k) {
+    const int i = seg + k * 32 + lane;
+    if (i < n) {
+      out[i] = over ? 0 : off + v[k];
+      if (over) in[i] = 0; // every count and offset dropped
+    }
+  }
+}
+
+hg_status launch_small_scan(int32_t *in, int64_t n, int32_t *out, const ScanLimit &lim,
+                            cudaStream_t s) {
+  HG_LAUNCH(k_small_scan, 1, SMALL_THREADS, 0, s, in, n, out, lim);
+  HG_CHECK_LAUNCH();
+  return HG_OK;
+}
+
 } // namespace
+
+int64_t small_scan_max() { return SMALL_N; }
+
+hg_status exclusive_scan_i32_limited(int32_t *in, int32_t *out, int64_t n, const ScanLimit &lim,
+                                     cudaStream_t s) {
+  if (n <= 0 || n > small_scan_max())
+    return fail(HG_ERR_INVALID_ARGUMENT, "limited scan: size out of range");
+  return launch_small_scan(in, n, out, lim, s);
+}
 
 int64_t scan_tmp_size(int64_t n) {
   int64_t total = 0;
@@ -75,6 +150,8 @@ hg_status exclusive_scan_i32(const int32_t *in, int32_t *out, int64_t n,
     HG_CHECK_LAUNCH();
     return HG_OK;
   }
+  if (n <= small_scan_max()) // (writes to its input only when a limit is exceeded)
+    return launch_small_scan(const_cast<int32_t *>(in), n, out, ScanLimit{}, s);
   const int64_t tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
   int32_t *sums = tmp;
   int32_t *sums_scanned = tmp + tiles;

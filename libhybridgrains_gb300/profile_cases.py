@@ -1,13 +1,15 @@
 """Small fixed workloads for kernel profilers (ncu launch lists and captures).
 
     python -m libhybridgrains_gb300.profile_cases dem --disks 1000000 --steps 12
+    python -m libhybridgrains_gb300.profile_cases dem --disks 10000 --per-row 100 --steps 12
     python -m libhybridgrains_gb300.profile_cases hybrid --steps 6
     python -m libhybridgrains_gb300.profile_cases column --steps 8
 
 Each case builds its scene, runs one warm-up step, then ``--steps`` steps one
 call per step (so that every kernel is a separate launch a profiler can
 select), synchronises and prints the wall time per step and the status words.
-The DEM case is the DEM column's lattice at 1000 disks per row (dt 1e-5 s);
+The DEM case is the DEM column's lattice (1000 disks per row unless
+--per-row says otherwise; dt 1e-5 s);
 the hybrid case is the hybrid column (100,000 points under 20,000 disks)
 after its initial resampling; the column case is the 2,000,000-point MIXED
 column.
@@ -24,10 +26,11 @@ def main(argv=None):
     ap.add_argument("case", choices=["dem", "hybrid", "column"])
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--disks", type=int, default=1000000)
+    ap.add_argument("--per-row", type=int, default=1000, help="DEM lattice disks per row")
     args = ap.parse_args(argv)
     ctx = hg.Context(0)
     if args.case == "dem":
-        sc = scenes.dem_column(n=args.disks, per_row=1000)
+        sc = scenes.dem_column(n=args.disks, per_row=args.per_row)
         obj = serving.dem_for_piles(ctx, args.disks)
         obj.upload(sc["q"], sc["v"], sc["r"], sc["m"], sc["I"], sc["fixed"])
 
