@@ -480,38 +480,46 @@ def run_dem(args, ctx):
 
 
 def run_hybrid(args, ctx):
-    """Hybrid column (100,000 material points under 20,000 disks, FP64,
-    uGIMP, node-node coupling, resampling every 200 steps on the host):
-    steps/s of the whole loop, with the share of the host resampling."""
-    from libhybridgrains_gb300 import hybrid, scenes
-    scene = scenes.hybrid_column()
-    sim = hybrid.HybridSim(ctx, scene)
-    sim.step(1)  # initial resampling and one step
-    ctx.synchronize()
-    t0 = time.perf_counter()
+    """Hybrid column (100,000 material points under 20,000 disks, uGIMP,
+    node-node coupling, resampling every 200 steps on the host): steps/s of
+    the whole loop, with the share of the host resampling, with the MPM bulk
+    in FP64 (the reference's arithmetic) and in mixed precision (FP32 bulk,
+    FP64 positions)."""
     import libhybridgrains_gb300 as hg
-    rs0 = sim.resamplings
-    host = [0.0]
-    orig = sim._resample
+    from libhybridgrains_gb300 import hybrid, scenes
 
-    def timed():
+    def run(precision):
+        sim = hybrid.HybridSim(ctx, scenes.hybrid_column(), precision=precision)
+        sim.step(1)  # initial resampling and one step
         ctx.synchronize()
-        t = time.perf_counter()
-        orig()
-        host[0] += time.perf_counter() - t
-    sim._resample = timed
-    sim.step(args.hybrid_steps)
-    ctx.synchronize()
-    wall = time.perf_counter() - t0
-    n, nd = sim.counts()
-    return {"workload": "hybrid column: 100,000 MPM points (h 2.5 mm, uGIMP, FP64) under 20,000 "
-                        "disks, node-node coupling, homogenised stress and velocity, resampling "
-                        "every 200 steps, dt 1e-6 s",
-            "steps": args.hybrid_steps, "steps_per_s": args.hybrid_steps / wall,
-            "ms_per_step": 1e3 * wall / args.hybrid_steps,
-            "resamplings": sim.resamplings - rs0, "resampling_host_s": host[0],
-            "points": n, "disks": nd,
-            "status": [sim.mpm.status(), sim.dem.status()]}
+        t0 = time.perf_counter()
+        rs0 = sim.resamplings
+        host = [0.0]
+        orig = sim._resample
+
+        def timed():
+            ctx.synchronize()
+            t = time.perf_counter()
+            orig()
+            host[0] += time.perf_counter() - t
+        sim._resample = timed
+        sim.step(args.hybrid_steps)
+        ctx.synchronize()
+        wall = time.perf_counter() - t0
+        n, nd = sim.counts()
+        out = {"steps": args.hybrid_steps, "steps_per_s": args.hybrid_steps / wall,
+               "ms_per_step": 1e3 * wall / args.hybrid_steps,
+               "resamplings": sim.resamplings - rs0, "resampling_host_s": host[0],
+               "device_ms_per_step": 1e3 * (wall - host[0]) / args.hybrid_steps,
+               "points": n, "disks": nd, "status": [sim.mpm.status(), sim.dem.status()]}
+        return out
+
+    fp64 = run(hg.FP64)
+    mixed = run(hg.MIXED)
+    return dict(fp64, workload="hybrid column: 100,000 MPM points (h 2.5 mm, uGIMP) under "
+                               "20,000 disks, node-node coupling, homogenised stress and "
+                               "velocity, resampling every 200 steps, dt 1e-6 s; top level: "
+                               "FP64 MPM bulk", mixed=mixed)
 
 
 def gather_parts(part, world):

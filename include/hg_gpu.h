@@ -581,8 +581,11 @@ enum {
   HG_HYBRID_HOMOGENIZE_VELOCITY = 2
 };
 
-/* HybridGrains2DSim over an FP64 MPM object and a DEM object on the same
- * context (hybridgrains2dnew/HybridGrains2DSim.cpp:21-73). */
+/* HybridGrains2DSim over an MPM object and a DEM object on the same context
+ * (hybridgrains2dnew/HybridGrains2DSim.cpp:21-73). With an FP64 MPM object
+ * the step follows the reference's arithmetic; with a MIXED one the MPM bulk
+ * runs in FP32 (positions FP64) and the coupling exchange is formed in FP64
+ * from the FP32 grid. */
 hg_status hg_hybrid_create(hg_context *ctx, hg_mpm *m, hg_dem *d,
                            hg_hybrid **out);
 hg_status hg_hybrid_destroy(hg_hybrid *h);

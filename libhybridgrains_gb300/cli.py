@@ -125,7 +125,8 @@ def _common(p, resume=True, snapshots=True, impulses=False):
         p.add_argument("-s", "--serialize_snapshots", type=int, choices=(0, 1), metavar="bool",
                        help="0: overwrite serial.bin at every output; 1: a new snapshot each")
     p.add_argument("--precision", choices=("fp64", "mixed"), default=None,
-                   help="arithmetic of the MPM / DEM step (default: mixed MPM, fp64 DEM)")
+                   help="arithmetic of the MPM / DEM step (default: mixed MPM, fp64 DEM "
+                        "and fp64 hybrid bulk)")
     p.add_argument("--device", type=int, default=0)
     p.add_argument("-q", "--quiet", action="store_true")
 
@@ -289,7 +290,7 @@ def run_hybrid(args):
     prec = display_precision(dt_r, None)
     stop = final_iteration(0, end, dt)
     ctx = hg.Context(args.device)
-    sim = hybrid.HybridSim(ctx, scene)
+    sim = hybrid.HybridSim(ctx, scene, precision=_precision(args, hg.FP64))
     out = args.output_dir
     if out:
         os.makedirs(out, exist_ok=True)

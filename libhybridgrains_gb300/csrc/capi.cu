@@ -1541,8 +1541,6 @@ hg_status hg_hybrid_create(hg_context *ctx, hg_mpm *m, hg_dem *d, hg_hybrid **ou
   *out = nullptr;
   if (m->ctx != ctx || d->ctx != ctx)
     return fail(HG_ERR_INVALID_ARGUMENT, "objects belong to another context");
-  if (m->p.precision != HG_PRECISION_FP64)
-    return fail(HG_ERR_UNSUPPORTED, "the hybrid step needs an FP64 MPM object");
   if (d->own)
     return fail(HG_ERR_UNSUPPORTED, "the hybrid step runs the DEM on the context's stream");
   DeviceGuard g(ctx);
@@ -1621,7 +1619,9 @@ hg_status hg_hybrid_download(hg_hybrid *h, int32_t *pg, int32_t *pn, double *dm,
   if ((st = d2h(s, pg, h->packed_dem.p, c[0])) || (st = d2h(s, pn, h->packed_mpm.p, c[1])) ||
       (st = d2h(s, dm, h->dem_mass.p, nn)) || (st = d2h(s, dp, h->dem_mom.p, 2 * nn)) ||
       (st = d2h(s, va, h->v_after.p, 2 * nn)) || (st = d2h(s, aa, h->a_after.p, 2 * nn)) ||
-      (st = d2h(s, hf, h->m->g_homog.p, nn)) || (st = d2h(s, hs, h->hstress.p, 4 * nn)) ||
+      (st = d2h(s, hf, h->m->p.precision == HG_PRECISION_MIXED ? h->homog.p : h->m->g_homog.p,
+                nn)) ||
+      (st = d2h(s, hs, h->hstress.p, 4 * nn)) ||
       (st = d2h(s, hv, h->hvel.p, 2 * nn)))
     return st;
   HG_CUDA_TRY(cudaStreamSynchronize(s));

@@ -40,10 +40,13 @@ __device__ __forceinline__ bool node_ok(const GridGeom &G, int ix, int iy) {
   return ix >= 0 && iy >= 0 && ix <= G.nx && iy <= G.ny;
 }
 
+// M: the MPM node mass type (double for an FP64 object, float for MIXED,
+// where it is the P2G sum of this step before the grid update).
+template <typename M>
 __global__ void kc_grain_mass(GridGeom G, int64_t nb, const double *__restrict__ pos,
                               const double *__restrict__ hl0, const uint8_t *__restrict__ fixed,
                               const double *__restrict__ m0, const double *__restrict__ w,
-                              const double *__restrict__ g_mass, double *dem_mass,
+                              const M *__restrict__ g_mass, double *dem_mass,
                               int32_t *coupled) {
   const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (b >= nb) return;
@@ -57,7 +60,7 @@ __global__ void kc_grain_mass(GridGeom G, int64_t nb, const double *__restrict__
   for (int iy = y0; iy <= y1; ++iy)
     for (int ix = x0; ix <= x1; ++ix) {
       if (!node_ok(G, ix, iy)) continue;
-      if (g_mass[(int64_t)iy * (G.nx + 1) + ix] <= 1.0e-6) all_pos = false;
+      if ((double)g_mass[(int64_t)iy * (G.nx + 1) + ix] <= 1.0e-6) all_pos = false;
     }
   if (!all_pos) return;
   coupled[b] = 1;
@@ -137,11 +140,56 @@ __global__ void kc_update_nodes(const int32_t *__restrict__ count,
   }
 }
 
-__global__ void kc_homog(int64_t nn, const double *__restrict__ g_mass,
+template <typename M>
+__global__ void kc_homog(int64_t nn, const M *__restrict__ g_mass,
                          const double *__restrict__ dem_mass, double *homog) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= nn) return;
-  homog[i] = dem_mass[i] > 0.0 ? 0.5 : (g_mass[i] > 0.0 ? 1.0 : 0.0);
+  homog[i] = dem_mass[i] > 0.0 ? 0.5 : ((double)g_mass[i] > 0.0 ? 1.0 : 0.0);
+}
+
+// updateVelocitiesOnGrid (Coupling.cpp:533-579) on a MIXED grid: the MPM
+// node momentum after the grid update is gm v (FP32 velocity and mass), the
+// exchange lambda is formed in FP64 as in kc_update_nodes, and the node's
+// velocity and acceleration (va: v, a) take p_new - lambda; the acceleration
+// (p_new - p) / (m dt) loses lambda / (m dt). Nodes without MPM mass keep
+// their zero velocity, as (p_new = 0) / m is never formed for them.
+__global__ void kc_update_nodes_x(const int32_t *__restrict__ count,
+                                  const int32_t *__restrict__ packed,
+                                  const float *__restrict__ gm,
+                                  const double *__restrict__ dem_mass,
+                                  const double *__restrict__ dem_mom, double dt, float4 *va,
+                                  double *v_after, double *a_after) {
+  const int c = *count;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < c;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = packed[k];
+    const double m_mpm = (double)gm[i], m_dem = dem_mass[i];
+    float4 g = va[i];
+    const double px = m_mpm * (double)g.x, py = m_mpm * (double)g.y;
+    const double msum = m_mpm + m_dem;
+    const double lx = (m_dem * px - m_mpm * dem_mom[2 * i]) / msum;
+    const double ly = (m_dem * py - m_mpm * dem_mom[2 * i + 1]) / msum;
+    if (m_mpm > 0.0) {
+      g.x = (float)((px - lx) / m_mpm);
+      g.y = (float)((py - ly) / m_mpm);
+      g.z = (float)((double)g.z - lx / (m_mpm * dt));
+      g.w = (float)((double)g.w - ly / (m_mpm * dt));
+      va[i] = g;
+    }
+    const double ax = dem_mom[2 * i] + lx, ay = dem_mom[2 * i + 1] + ly;
+    v_after[2 * i] = ax / m_dem;
+    v_after[2 * i + 1] = ay / m_dem;
+    a_after[2 * i] = lx / m_dem;
+    a_after[2 * i + 1] = ly / m_dem;
+  }
+}
+
+__global__ void kc_set_scalar(double *dst, double v) { *dst = v; }
+
+__global__ void kc_fill(double *dst, int64_t n, double v) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = v;
 }
 
 __global__ void kc_transfer(GridGeom G, const int32_t *__restrict__ count,
@@ -273,6 +321,14 @@ hg_status hybrid_alloc(hg_hybrid *h) {
       (st = h->counts.alloc(2)))
     return st;
   cudaStream_t s = h->ctx->stream;
+  if (h->m->p.precision == HG_PRECISION_MIXED) {
+    if ((st = h->homog.alloc(nn)) || (st = h->hl0.alloc(1))) return st;
+    HG_LAUNCH(kc_set_scalar, 1, 1, 0, s, h->hl0.p, 0.0);
+    HG_CHECK_LAUNCH();
+    h->hl0_value = 0.0;
+    HG_LAUNCH(kc_fill, blocks_for(nn, 256), 256, 0, s, h->homog.p, nn, 1.0);
+    HG_CHECK_LAUNCH();
+  }
   HG_CUDA_TRY(cudaMemsetAsync(h->counts.p, 0, 2 * sizeof(int32_t), s));
   HG_CUDA_TRY(cudaMemsetAsync(h->dem_mass.p, 0, sizeof(double) * nn, s));
   HG_CUDA_TRY(cudaMemsetAsync(h->dem_mom.p, 0, sizeof(double) * 2 * nn, s));
@@ -305,13 +361,36 @@ hg_status hybrid_step(hg_hybrid *h, double dt, int flags) {
   if (nb > 0)
     HG_CUDA_TRY(cudaMemcpyAsync(h->pos_before.p, d->q.p, sizeof(double) * 3 * nb,
                                 cudaMemcpyDeviceToDevice, s));
-  if ((st = mpm64_phase0(m))) return st;
+  // A MIXED MPM object (FP32 bulk, FP64 positions) runs the same sequence on
+  // its FP32 grid: its P2G for this step was done by the previous particle
+  // launch (or the upload), its grid update and G2P are separate launches.
+  const bool mixed = m->p.precision == HG_PRECISION_MIXED;
+  const double *hl0 = m->hl.p;
+  if (mixed) {
+    if ((st = mixed_step_begin(m))) return st;
+    // points.hl(0) in world units (one half-width for all MIXED points)
+    const double v = m->p.basis == HG_BASIS_UGIMP ? (double)m->hl_cells * m->p.h : 0.0;
+    if (v != h->hl0_value) {
+      HG_LAUNCH(kc_set_scalar, 1, 1, 0, s, h->hl0.p, v);
+      HG_CHECK_LAUNCH();
+      h->hl0_value = v;
+    }
+    hl0 = h->hl0.p;
+  } else if ((st = mpm64_phase0(m))) {
+    return st;
+  }
   // rasterizeGrainMass (pre-step positions, no partially filled cells)
   HG_CUDA_TRY(cudaMemsetAsync(h->dem_mass.p, 0, sizeof(double) * nn, s));
-  HG_CUDA_TRY(cudaMemsetAsync(m->g_hyb.p, 0, sizeof(int32_t) * nn, s));
+  if (!mixed) HG_CUDA_TRY(cudaMemsetAsync(m->g_hyb.p, 0, sizeof(int32_t) * nn, s));
   if (nb > 0) {
-    HG_LAUNCH(kc_grain_mass, blocks_for(nb, 128), 128, 0, s, G, nb, h->pos_before.p, m->hl.p,
-              d->fixed.p, d->m0.p, d->w.p, m->g_mass.p, h->dem_mass.p, h->coupled.p);
+    if (mixed)
+      HG_LAUNCH(kc_grain_mass<float>, blocks_for(nb, 128), 128, 0, s, G, nb, h->pos_before.p,
+                hl0, d->fixed.p, d->m0.p, d->w.p, (const float *)m->accm.p, h->dem_mass.p,
+                h->coupled.p);
+    else
+      HG_LAUNCH(kc_grain_mass<double>, blocks_for(nb, 128), 128, 0, s, G, nb, h->pos_before.p,
+                hl0, d->fixed.p, d->m0.p, d->w.p, (const double *)m->g_mass.p, h->dem_mass.p,
+                h->coupled.p);
     HG_CHECK_LAUNCH();
   }
   HG_CUDA_TRY(cudaMemsetAsync(h->coupled.p + nb, 0, sizeof(int32_t), s));
@@ -329,25 +408,34 @@ hg_status hybrid_step(hg_hybrid *h, double dt, int flags) {
   HG_CHECK_LAUNCH();
   // DiscreteIntegrator::step -> flowWithWeight (DiscreteIntegrator.cpp:99-116)
   if ((st = dem_step(d, dt, 1))) return st;
-  if ((st = mpm64_phase1(m, dt))) return st;
+  if ((st = mixed ? mixed_grid_update(m, dt) : mpm64_phase1(m, dt))) return st;
   // rasterizeGrainMom
   HG_CUDA_TRY(cudaMemsetAsync(h->dem_mom.p, 0, sizeof(double) * 2 * nn, s));
   HG_LAUNCH(kc_grain_mom, gs, 128, 0, s, G, h->counts.p, h->packed_dem.p, h->pos_before.p,
-            m->hl.p, d->fixed.p, d->m0.p, d->w.p, d->v.p, h->dem_mom.p);
+            hl0, d->fixed.p, d->m0.p, d->w.p, d->v.p, h->dem_mom.p);
   HG_CHECK_LAUNCH();
   // updateVelocitiesOnGrid
   HG_CUDA_TRY(cudaMemsetAsync(h->v_after.p, 0, sizeof(double) * 2 * nn, s));
   HG_CUDA_TRY(cudaMemsetAsync(h->a_after.p, 0, sizeof(double) * 2 * nn, s));
-  HG_LAUNCH(kc_update_nodes, gs, 256, 0, s, h->counts.p + 1, h->packed_mpm.p, m->g_mass.p,
-            h->dem_mass.p, h->dem_mom.p, m->g_mom_new.p, h->v_after.p, h->a_after.p);
-  HG_CHECK_LAUNCH();
-  HG_LAUNCH(kc_homog, blocks_for(nn, 256), 256, 0, s, nn, m->g_mass.p, h->dem_mass.p,
-            m->g_homog.p);
+  if (mixed) {
+    HG_LAUNCH(kc_update_nodes_x, gs, 256, 0, s, h->counts.p + 1, h->packed_mpm.p,
+              (const float *)m->gm.p, h->dem_mass.p, h->dem_mom.p, dt, m->va.p, h->v_after.p,
+              h->a_after.p);
+    HG_CHECK_LAUNCH();
+    HG_LAUNCH(kc_homog<float>, blocks_for(nn, 256), 256, 0, s, nn, (const float *)m->gm.p,
+              h->dem_mass.p, h->homog.p);
+  } else {
+    HG_LAUNCH(kc_update_nodes, gs, 256, 0, s, h->counts.p + 1, h->packed_mpm.p, m->g_mass.p,
+              h->dem_mass.p, h->dem_mom.p, m->g_mom_new.p, h->v_after.p, h->a_after.p);
+    HG_CHECK_LAUNCH();
+    HG_LAUNCH(kc_homog<double>, blocks_for(nn, 256), 256, 0, s, nn, (const double *)m->g_mass.p,
+              h->dem_mass.p, m->g_homog.p);
+  }
   HG_CHECK_LAUNCH();
   HG_LAUNCH(kc_transfer, gs, 128, 0, s, G, h->counts.p, h->packed_dem.p, h->pos_before.p,
-            m->hl.p, d->fixed.p, h->v_after.p, h->a_after.p, d->v.p);
+            hl0, d->fixed.p, h->v_after.p, h->a_after.p, d->v.p);
   HG_CHECK_LAUNCH();
-  if ((st = mpm64_phase2(m, dt))) return st;
+  if ((st = mixed ? mixed_particles(m, dt) : mpm64_phase2(m, dt))) return st;
   HG_LAUNCH(kc_advect, gs, 128, 0, s, dt, h->counts.p, h->packed_dem.p, h->pos_before.p, d->v.p,
             d->q.p);
   HG_CHECK_LAUNCH();

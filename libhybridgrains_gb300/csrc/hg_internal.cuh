@@ -456,9 +456,19 @@ struct hg_hybrid {
   hg::DevBuf<int32_t> coupled, packed_dem, packed_mpm, flag_tmp, scan_tmp,
       node_flag, node_pos, counts; // counts[2]: packed sizes
   int64_t n_packed_dem = 0, n_packed_mpm = 0;
+  // with a MIXED MPM object: the node homogenisation factors (an FP64 object
+  // keeps them in its grid) and the points' half-width hl(0) in world units
+  hg::DevBuf<double> homog, hl0;
+  double hl0_value = -1.0;
 };
 
 namespace hg {
+// The MIXED step in the three parts the hybrid step interleaves with the
+// coupling: re-sort if due (this step's P2G sums are then in accm/acc4), the
+// grid update (gm, va), and G2P of this step fused with P2G of the next.
+hg_status mixed_step_begin(hg_mpm *m);
+hg_status mixed_grid_update(hg_mpm *m, double dt);
+hg_status mixed_particles(hg_mpm *m, double dt);
 hg_status hybrid_alloc(hg_hybrid *h);
 hg_status hybrid_step(hg_hybrid *h, double dt, int flags);
 hg_status hybrid_clear_homogenized(hg_hybrid *h);

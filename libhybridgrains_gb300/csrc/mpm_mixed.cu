@@ -1684,6 +1684,42 @@ hg_status mixed_step(hg_mpm *m, double dt, int nsteps) {
   return HG_OK;
 }
 
+// The per-step body of mixed_step in three parts, for the hybrid step.
+hg_status mixed_step_begin(hg_mpm *m) {
+  if (!m->primed) {
+    hg_status st = prime(m);
+    if (st != HG_OK) return st;
+  }
+  bool need = m->steps_since_rebin >= MAX_STEPS_BETWEEN_REBINS;
+  if (!need && m->outside_pending && cudaEventQuery(m->outside_ev) == cudaSuccess) {
+    m->outside_pending = false;
+    need = m->h_outside[0] > 0 || (int64_t)m->h_outside[1] * 32 > m->n;
+  }
+  return need ? rebin(m) : HG_OK;
+}
+
+hg_status mixed_grid_update(hg_mpm *m, double dt) {
+  MixedArgs A = make_args(m, dt, true);
+  HG_LAUNCH(kx_grid_update, update_blocks(m), THREADS, 0, m->ctx->stream, A);
+  HG_CHECK_LAUNCH();
+  return HG_OK;
+}
+
+hg_status mixed_particles(hg_mpm *m, double dt) {
+  cudaStream_t s = m->ctx->stream;
+  MixedArgs A = make_args(m, dt, false);
+  launch_particle_kernel<false>(m, A, s);
+  HG_CHECK_LAUNCH();
+  m->steps_since_rebin++;
+  if (!m->outside_pending) {
+    HG_CUDA_TRY(cudaMemcpyAsync(m->h_outside, m->outside.p, 2 * sizeof(uint32_t),
+                                cudaMemcpyDeviceToHost, s));
+    HG_CUDA_TRY(cudaEventRecord(m->outside_ev, s));
+    m->outside_pending = true;
+  }
+  return HG_OK;
+}
+
 } // namespace hg
 
 // ---- batches ---------------------------------------------------------------------

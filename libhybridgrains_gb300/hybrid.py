@@ -13,6 +13,9 @@ state copied from the device, and the result is copied back
   the zones and the resampling step run, points and grains are uploaded (the
   DEM contact history renumbered), and the accumulators are cleared.
 
+``precision=MIXED`` runs the MPM bulk in FP32 with FP64 positions (the
+coupling exchange is still formed in FP64); the default is the FP64 step.
+
 Host copies kept between intervals: reference positions q0, initial masses
 and volumes (m0, volume0) and half widths of the points; reference
 positions, radii and initial masses of the grains.
@@ -27,7 +30,8 @@ from . import DEM, FP64, MPM, Hybrid, Resampler, Zones, scene_xml, scenes
 
 
 class HybridSim:
-    def __init__(self, ctx, scene, basis=None, point_headroom=2.0, grain_headroom=3.0):
+    def __init__(self, ctx, scene, basis=None, point_headroom=2.0, grain_headroom=3.0,
+                 precision=FP64):
         cfg, sc, dp = scene["mpm"], scene["dem"], scene["dem_params"]
         zs, rs = scene["zones"], scene["resampling"]
         self.ctx, self.cfg, self.dt = ctx, cfg, cfg["dt"]
@@ -40,7 +44,7 @@ class HybridSim:
         gravity = cfg.get("gravity", scenes.GRAVITY)
         self.mpm = MPM(ctx, cfg["grid_min"], cfg["grid_max"], cfg["h"], cfg["shear_modulus"],
                        cfg["bulk_modulus"], cfg["dp_alpha"], cfg["flip_alpha"], gravity,
-                       cfg["planes"], basis=basis, precision=FP64,
+                       cfg["planes"], basis=basis, precision=precision,
                        capacity=int(point_headroom * n) + 1024)
         self.mpm.upload(p["q"], p["v"], p["m"], p["vol"], p["hl"])
         # the discrete scene's planes, else the continuum's walls for the grains too
