@@ -2,7 +2,7 @@
 
     python -m libhybridgrains_gb300.profile_cases dem --disks 1000000 --steps 12
     python -m libhybridgrains_gb300.profile_cases dem --disks 10000 --per-row 100 --steps 12
-    python -m libhybridgrains_gb300.profile_cases hybrid --steps 6
+    python -m libhybridgrains_gb300.profile_cases hybrid --steps 6 [--precision mixed]
     python -m libhybridgrains_gb300.profile_cases column --steps 8
 
 Each case builds its scene, runs one warm-up step, then ``--steps`` steps one
@@ -27,6 +27,8 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--disks", type=int, default=1000000)
     ap.add_argument("--per-row", type=int, default=1000, help="DEM lattice disks per row")
+    ap.add_argument("--precision", choices=("fp64", "mixed"), default="fp64",
+                    help="the hybrid case's MPM bulk")
     args = ap.parse_args(argv)
     ctx = hg.Context(0)
     if args.case == "dem":
@@ -39,7 +41,8 @@ def main(argv=None):
         status = obj.status
     elif args.case == "hybrid":
         from libhybridgrains_gb300.hybrid import HybridSim
-        sim = HybridSim(ctx, scenes.hybrid_column())
+        sim = HybridSim(ctx, scenes.hybrid_column(),
+                        precision=hg.MIXED if args.precision == "mixed" else hg.FP64)
         sim.step(1)
 
         def step():
