@@ -159,8 +159,16 @@ hg_status fill_regions(hg_resampler &R, const std::vector<Box> &regions, double 
   grid.reset(g0x, g0y, (unsigned)std::ceil((g1x - g0x) / cw), (unsigned)std::ceil((g1y - g0y) / cw),
              cw);
   std::vector<int> mail(px.size(), 0);
-  for (size_t b = 0; b < px.size(); ++b)
+  for (size_t b = 0; b < px.size(); ++b) {
+    // A body wholly outside the grid's extent cannot conflict with a sample
+    // (samples lie in the regions, six mean radii inside that extent, and
+    // conflicts need centres closer than the two radii); left in, it would
+    // pile up in the clamped edge cells that every nearby test scans.
+    if (px[b] + rad[b] < g0x || px[b] - rad[b] > g1x || py[b] + rad[b] < g0y ||
+        py[b] - rad[b] > g1y)
+      continue;
     grid.add_box(px[b] - rad[b], py[b] - rad[b], px[b] + rad[b], py[b] + rad[b], (int)b);
+  }
   auto next_test = [&]() {
     if (++R.test_id == 0) R.test_id = 1;
   };
