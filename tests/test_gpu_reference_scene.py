@@ -3,7 +3,8 @@ column-collapse: 6,694 disks, 615 of them fixed, over a uGIMP MPM column in
 CGS units) run by the library from scene files. The files are written here
 from the fixtures tests/golden/make_column_collapse_assets.py made from the
 reference's XML, read back by scene_xml and stepped by hybrid.HybridSim
-through three resampling intervals."""
+through three resampling intervals, with the MPM bulk in FP64 and in mixed
+precision."""
 import json
 import os
 
@@ -81,12 +82,14 @@ def write_scene(d):
     return sc, z
 
 
-def test_reference_column_collapse_runs(ctx, tmp_path):
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_reference_column_collapse_runs(ctx, tmp_path, precision):
+    import libhybridgrains_gb300 as hg
     sc, z = write_scene(str(tmp_path))
     scene = scene_xml.read_hybrid(str(tmp_path / "hybrid.xml"))
     assert scene["dt"] == sc["hybrid"]["dt"] and len(scene["dem"]["r"]) == len(z["r"]) == 6694
     assert int(scene["dem"]["fixed"].sum()) == 615 and scene["mpm"]["basis"] == "ugimp"
-    sim = hybrid.HybridSim(ctx, scene)
+    sim = hybrid.HybridSim(ctx, scene, precision=hg.MIXED if precision == "mixed" else hg.FP64)
     sim.step(250)  # resamplings at iterations 0, 100 and 200
     assert sim.resamplings >= 3
     assert sim.mpm.status() == 0 and sim.dem.status() == 0
@@ -107,7 +110,7 @@ def test_reference_column_collapse_cli(tmp_path):
     out = tmp_path / "out"
     # 1000080 / 2160 = 463 steps per output; 0.0005 s is 501 steps
     assert cli.main(["hybridgrains2d", str(tmp_path / "hybrid.xml"), "-e", "0.0005",
-                     "-o", str(out), "-f", "2160", "-q"]) == 0
+                     "-o", str(out), "-f", "2160", "--precision", "mixed", "-q"]) == 0
     names = sorted(os.listdir(str(out)))
     assert names == ["config_0.npz", "config_1.npz"]
     f = frames.read(str(out / "config_1.npz"))
