@@ -462,9 +462,18 @@ def run_dem(args, ctx):
             ctx.timer_begin()
             dl.flow(1.0e-5, args.dem_large_steps)
             msl = ctx.timer_end()
+            ncl = dl.num_contacts()
+            # algorithmic bytes per step: FP64 128 B per disk + 40 per contact,
+            # mixed 88 + 24 (the scope table's per-unit figures)
+            per_disk, per_contact = (128, 40) if prec == hg.FP64 else (88, 24)
+            algl = nl * per_disk + ncl * per_contact
+            achl = algl / (msl * 1e-3 / args.dem_large_steps) / 1e9
+            peak = measured_peaks().get("hbm_gbs") or 6800.0
             large[name] = {"disk_steps_per_s": nl * args.dem_large_steps / (msl * 1e-3),
                            "us_per_step": 1e3 * msl / args.dem_large_steps,
-                           "contacts": dl.num_contacts(), "status": dl.status()}
+                           "contacts": ncl, "status": dl.status(),
+                           "algorithmic_bytes_per_step": algl, "achieved_gbs": achl,
+                           "hbm_frac": achl / peak}
             dl.close()
     return {"workload": "DEM column: 10,000 disks, hex pitch 2.2 mm, r U[0.9,1.1] mm, dt 1e-6 s, "
                         "FP64 penalty contacts with friction history",
