@@ -98,7 +98,8 @@ def _zones_sig(f):
 def lib():
     global _lib
     if _lib is None:
-        path = _build.build()
+        # HG_ORACLE_LIB: a separately built copy (the sanitizer test's build)
+        path = os.environ.get("HG_ORACLE_LIB") or _build.build()
         _lib = ctypes.CDLL(path)
         _sig(_lib)
         _zones_sig(_lib)
