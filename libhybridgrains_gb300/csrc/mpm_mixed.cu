@@ -61,6 +61,7 @@ constexpr int MAX_BATCH = HG_MAX_BATCH; // scenes per batched launch
 struct alignas(16) MixedArgs {
   int nx, ny, ntx, nty;
   int64_t n;
+  double gmin[2], h; // grid origin and cell width (the node plane test)
   float dt, inv_h, kappa, mu, dp_alpha, flip_alpha, gx, gy;
   // Half-width (in cells) of the band around a plane in which the FP32
   // plane test is redone exactly in FP64.
@@ -258,6 +259,30 @@ __device__ __forceinline__ double widen(float f) {
   return __hiloint2double((int)hi, (int)(m << 29));
 }
 
+// Signed distance n . (u - x) of a position in grid units from a plane, each
+// product and sum rounded on its own (no contraction into FMA), so that a
+// point lying on a plane gives 0 as in the reference's expression
+// (MaterialPoints.cpp:381).
+__device__ __forceinline__ double plane_distance_u(const MpmPlaneDev &pl, double ux, double uy) {
+  return __dadd_rn(__dmul_rn(pl.n[0], __dsub_rn(ux, pl.ux[0])),
+                   __dmul_rn(pl.n[1], __dsub_rn(uy, pl.ux[1])));
+}
+
+// PhysicsGrid::resolvePlaneCollisions' test of node (ix, iy)
+// (PhysicsGrid.cpp:614-629) on the node's world position
+// computeGridPointLocation = min + h (i, j) (PhysicsGrid.cpp:71-74), with the
+// reference's operations rounded one by one: true when the plane acts on the
+// node. Nodes on a plane or on its lower bound decide as in the reference.
+__device__ __forceinline__ bool node_behind_plane(const MixedArgs &A, const MpmPlaneDev &pl,
+                                                  int ix, int iy) {
+  const double px = __dadd_rn(A.gmin[0], __dmul_rn(A.h, (double)ix));
+  const double py = __dadd_rn(A.gmin[1], __dmul_rn(A.h, (double)iy));
+  if (py < pl.lower_bound) return false;
+  const double d = __dadd_rn(__dmul_rn(pl.n[0], __dsub_rn(px, pl.x[0])),
+                             __dmul_rn(pl.n[1], __dsub_rn(py, pl.x[1])));
+  return !(d > 0.0);
+}
+
 __device__ __forceinline__ bool finite_d(double x) {
   return ((unsigned)__double2hiint(x) & 0x7FF00000u) != 0x7FF00000u;
 }
@@ -437,7 +462,7 @@ __device__ __forceinline__ void fused_tile(const MixedArgs &A, const int bin, Fu
           const float dapprox = pl.fn[0] * (ufx - pl.fux[0]) + pl.fn[1] * (ufy - pl.fux[1]);
           if (dapprox > A.pmargin) continue;
           if (un.y < pl.ulb) continue;
-          const double d = pl.n[0] * (un.x - pl.ux[0]) + pl.n[1] * (un.y - pl.ux[1]);
+          const double d = plane_distance_u(pl, un.x, un.y);
           if (d > 0.0) continue;
           un.x += -d * pl.n[0];
           un.y += -d * pl.n[1];
@@ -766,7 +791,7 @@ __global__ void __launch_bounds__(THREADS) kxu_step(const __grid_constant__ Mixe
       for (int k = 0; k < A.nplanes; ++k) {
         const MpmPlaneDev &pl = A.planes[k];
         if (un.y < pl.ulb) continue;
-        const double d = pl.n[0] * (un.x - pl.ux[0]) + pl.n[1] * (un.y - pl.ux[1]);
+        const double d = plane_distance_u(pl, un.x, un.y);
         if (d > 0.0) continue;
         un.x += -d * pl.n[0];
         un.y += -d * pl.n[1];
@@ -848,9 +873,9 @@ __device__ __forceinline__ void update_tile(const MixedArgs &A, const int tile) 
         if (fy_node < pl.fulb - A.pmargin) continue;
         float d = pl.fn[0] * ((float)ix - pl.fux[0]) + pl.fn[1] * (fy_node - pl.fux[1]);
         if (fabsf(d) < A.pmargin || fabsf(fy_node - pl.fulb) < A.pmargin) {
-          if ((double)iy < pl.ulb) continue;
-          const double dd = pl.n[0] * ((double)ix - pl.ux[0]) + pl.n[1] * ((double)iy - pl.ux[1]);
-          d = dd > 0.0 ? 1.0f : -1.0f;
+          // near the plane or its lower bound the reference's own test decides
+          if (!node_behind_plane(A, pl, ix, iy)) continue;
+          d = -1.0f;
         }
         if (d > 0.0f) continue;
         if (!pl.sticking) {
@@ -1231,6 +1256,9 @@ MixedArgs make_args(hg_mpm *m, double dt, bool tiles) {
   A.ntx = m->ntx;
   A.nty = m->nty;
   A.n = m->n;
+  A.gmin[0] = P.gmin[0];
+  A.gmin[1] = P.gmin[1];
+  A.h = P.h;
   A.dt = (float)dt;
   A.inv_h = (float)P.inv_h;
   A.kappa = (float)P.kappa;

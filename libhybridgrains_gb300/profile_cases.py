@@ -2,6 +2,7 @@
 
     python -m libhybridgrains_gb300.profile_cases dem --disks 1000000 --steps 12
     python -m libhybridgrains_gb300.profile_cases dem --disks 10000 --per-row 100 --steps 12
+    python -m libhybridgrains_gb300.profile_cases dem --disks 1000000 --packed --steps 12
     python -m libhybridgrains_gb300.profile_cases hybrid --steps 6 [--precision mixed]
     python -m libhybridgrains_gb300.profile_cases column --steps 8
 
@@ -9,7 +10,9 @@ Each case builds its scene, runs one warm-up step, then ``--steps`` steps one
 call per step (so that every kernel is a separate launch a profiler can
 select), synchronises and prints the wall time per step and the status words.
 The DEM case is the DEM column's lattice (1000 disks per row unless
---per-row says otherwise; dt 1e-5 s);
+--per-row says otherwise; dt 1e-5 s), or with --packed the same disks
+compacted to a 1.9 mm pitch between a floor and two walls (about 2.5
+contacts per disk; dt 1e-6 s);
 the hybrid case is the hybrid column (100,000 points under 20,000 disks)
 after its initial resampling; the column case is the 2,000,000-point MIXED
 column.
@@ -27,17 +30,28 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--disks", type=int, default=1000000)
     ap.add_argument("--per-row", type=int, default=1000, help="DEM lattice disks per row")
+    ap.add_argument("--packed", action="store_true",
+                    help="DEM: the compacted lattice (scenes.dem_packed)")
     ap.add_argument("--precision", choices=("fp64", "mixed"), default="fp64",
                     help="the hybrid case's MPM bulk")
     args = ap.parse_args(argv)
     ctx = hg.Context(0)
     if args.case == "dem":
-        sc = scenes.dem_column(n=args.disks, per_row=args.per_row)
-        obj = serving.dem_for_piles(ctx, args.disks)
+        if args.packed:
+            sc = scenes.dem_packed(n=args.disks, per_row=args.per_row)
+            dp = scenes.dem_params()
+            obj = hg.DEM(ctx, scenes.GRAVITY, dp["kn"], dp["kt"], dp["gamman"], dp["gammat"],
+                         dp["mu"], sc["planes"], capacity=args.disks,
+                         contact_capacity=4 * args.disks)
+            ddt = 1.0e-6
+        else:
+            sc = scenes.dem_column(n=args.disks, per_row=args.per_row)
+            obj = serving.dem_for_piles(ctx, args.disks)
+            ddt = 1.0e-5
         obj.upload(sc["q"], sc["v"], sc["r"], sc["m"], sc["I"], sc["fixed"])
 
         def step():
-            obj.flow(1.0e-5, 1)
+            obj.flow(ddt, 1)
         status = obj.status
     elif args.case == "hybrid":
         from libhybridgrains_gb300.hybrid import HybridSim

@@ -138,6 +138,19 @@ def dem_column(n=10000, per_row=100, pitch=2.2e-3, rmin=0.9e-3, rmax=1.1e-3, jit
     return dict(q=q, v=v, r=r, m=m, I=I, fixed=np.zeros(n, dtype=np.uint8))
 
 
+def dem_packed(n=10000, per_row=100, pitch=1.9e-3, seed=12345):
+    """The DEM column's disks (radii U[0.9, 1.1] mm, jitter 0.05 mm, rho 2600)
+    on a hex lattice compacted to a pitch below the mean diameter, between a
+    floor and two walls: about 2.5 contacts per disk from the first step (the
+    loose 2.2 mm lattice has about 0.03). The planes (floor at y = 0, walls
+    at x = 0 and x = (per_row + 1/2) pitch) are returned with the bodies; the
+    walls keep the lattice compacted across its width while the top relaxes."""
+    sc = dem_column(n=n, per_row=per_row, pitch=pitch, seed=seed)
+    sc["planes"] = [((0.0, 0.0), (0.0, 1.0)), ((0.0, 0.0), (1.0, 0.0)),
+                    (((per_row + 0.5) * pitch, 0.0), (-1.0, 0.0))]
+    return sc
+
+
 def dem_params(kn=1.0e5, mu=0.5, restitution=0.5, r_mean=1.0e-3, rho=2600.0):
     """Penalty parameters: restitution-matched normal damping for the mean disk.
 

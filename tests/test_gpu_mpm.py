@@ -277,3 +277,88 @@ def test_invalid_arguments_are_rejected(ctx, cfg0):
         g.upload(p["q"], p["v"], p["m"], p["vol"], p["hl"])  # over capacity
     with pytest.raises(hg.HGError):
         g.flow_zero_phase()  # phase calls need FP64
+
+
+def sliding_scene(cfg0, seed=3):
+    """The 12,800-point column with every plane behaviour of MPMStaticPlane
+    (mpmgrains2d/StaticPlane.h:6-22): a sticking floor; a SLIDING left wall 2
+    mm inside the column, so that points start behind it; a SLIDING right wall
+    2 mm inside the column that acts only from y = 0.2 m up (finite
+    lower_bound); a tilted SLIDING plane across the column's upper left corner
+    from y = 0.3 m up; and the sticking far wall. Random velocities of 0.5 m/s
+    give both signs of the normal velocity at every plane, so the separating
+    (v_n > 0) and the projecting branches of PhysicsGrid.cpp:611-673 and
+    MaterialPoints.cpp:371-423 both run."""
+    cfg = dict(cfg0)
+    p = column(cfg, seed=seed, vscale=0.5)
+    s = 1.0 / np.sqrt(2.0)
+    cfg["planes"] = [((0.0, 0.0), (0.0, 1.0), True, -np.inf),
+                     ((0.102, 0.0), (1.0, 0.0), False, -np.inf),
+                     ((0.298, 0.0), (-1.0, 0.0), False, 0.2),
+                     ((0.1, 0.37), (s, -s), False, 0.3),
+                     ((1.0, 0.0), (-1.0, 0.0), True, -np.inf)]
+    return cfg, p
+
+
+@pytest.mark.parametrize("basis", [0, 1])
+def test_fp64_sliding_planes_and_lower_bound_match_oracle(ctx, cfg0, basis):
+    cfg, p = sliding_scene(cfg0)
+    if basis == 1:
+        cfg["grid_min"] = (-0.01, -0.01)
+    g = gpu_mpm(ctx, cfg, hg.FP64, basis=basis)
+    c = cpu_mpm(cfg, basis=basis)
+    g.upload(p["q"], p["v"], p["m"], p["vol"], p["hl"])
+    c.set_particles(p["q"], p["v"], p["m"], p["vol"], p["hl"])
+    q0 = p["q"]
+    behind_left = q0[:, 0] < 0.102
+    behind_right_high = (q0[:, 0] > 0.298) & (q0[:, 1] >= 0.2)
+    behind_right_low = (q0[:, 0] > 0.298) & (q0[:, 1] < 0.2)
+    assert behind_left.sum() > 100 and behind_right_high.sum() > 50 and behind_right_low.sum() > 50
+    dt = cfg["dt"]
+    for nsteps in (1, 9):
+        g.flow(dt, nsteps)
+        c.step(dt, nsteps)
+        G, C = g.grid(), c.grid()
+        for k in ("mass", "mom", "mom_new", "force", "vel", "acc"):
+            assert rel(G[k], C[k]) <= 1e-12, k
+        P, Q = g.download(), c.particles()
+        assert np.abs(P["q"] - Q["q"]).max() <= 1e-15
+        assert rel(P["v"], Q["v"]) <= 1e-12
+        assert np.abs(P["J"] - Q["J"]).max() <= 1e-13
+        assert np.abs(P["be"] - Q["be"]).max() <= 1e-13
+    # the planes acted: points behind the left wall and behind the bounded
+    # right wall above its lower bound were projected onto them, points
+    # below that bound were not
+    Q = c.particles()
+    assert (Q["q"][behind_left, 0] >= 0.102 - 1e-12).all()
+    assert (Q["q"][behind_right_high, 0] <= 0.298 + 1e-12).all()
+    assert (Q["q"][behind_right_low, 0] > 0.298).any()
+    assert g.status() == 0
+
+
+def test_mixed_sliding_planes_and_lower_bound_track_oracle(ctx, cfg0):
+    cfg, p = sliding_scene(cfg0)
+    g = gpu_mpm(ctx, cfg, hg.MIXED)
+    c = cpu_mpm(cfg)
+    g.upload(p["q"], p["v"], p["m"], p["vol"], p["hl"])
+    c.set_particles(p["q"], p["v"], p["m"], p["vol"], p["hl"])
+    dt = cfg["dt"]
+    g.flow(dt)
+    c.step(dt)
+    G, C = g.grid(), c.grid()
+    act = C["mass"] > 0
+    assert np.array_equal(G["mass"] > 0, act)
+    err = np.linalg.norm(G["vel"][act] - C["vel"][act]) / np.linalg.norm(C["vel"][act])
+    assert err <= 1e-5, err
+    P, Q = g.download(), c.particles()
+    # the projection onto a plane is formed in FP64 on both sides
+    assert np.abs(P["q"] - Q["q"]).max() <= 1e-12
+    assert np.linalg.norm(P["v"] - Q["v"]) / np.linalg.norm(Q["v"]) <= 1e-5
+    g.flow(dt, 19)
+    c.step(dt, 19)
+    P, Q = g.download(), c.particles()
+    assert np.abs(P["q"] - Q["q"]).max() <= 1e-9
+    assert np.abs(P["J"] - Q["J"]).max() <= 1e-6
+    assert np.abs(P["be"] - Q["be"]).max() <= 1e-6
+    assert np.linalg.norm(P["v"] - Q["v"]) / np.linalg.norm(Q["v"]) <= 1e-4
+    assert g.status() == 0
