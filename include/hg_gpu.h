@@ -564,10 +564,12 @@ hg_status hg_dem_candidate_pairs(hg_context *ctx, int64_t n,
  * and returns at most HG_STATIC_PAIRS_MAX_PAIRS pairs; larger inputs are
  * rejected with HG_ERR_CAPACITY. It allocates nothing: no cudaMalloc, no
  * cudaFree. The first call on each device looks up the array's device
- * address; make that first call before any stream capture. Calls share the
- * array: calls that overlap on the GPU (from several threads or contexts on
- * one device) race, so serialise them. Same inputs, outputs and results as
- * hg_dem_candidate_pairs. */
+ * address; make that first call before any stream capture. The address is
+ * kept until the process exits: a cudaDeviceReset ends every context of this
+ * library on that device, and this entry point may not be called after one.
+ * Calls share the array: calls that overlap on the GPU (from several threads
+ * or contexts on one device) race, so serialise them. Same inputs, outputs
+ * and results as hg_dem_candidate_pairs. */
 enum { HG_STATIC_PAIRS_MAX_BOXES = 16384, HG_STATIC_PAIRS_MAX_PAIRS = 262144 };
 hg_status hg_dem_candidate_pairs_static(hg_context *ctx, int64_t n,
                                         const double *aabb_min,

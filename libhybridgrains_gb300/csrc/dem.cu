@@ -1410,7 +1410,11 @@ constexpr size_t SP_ITEMS = SP_BCURSOR + sp_align(sizeof(int32_t) * SP_TABLE);
 constexpr size_t SP_CNT = SP_ITEMS + sp_align(sizeof(int32_t) * SP_MAX_BOXES);
 constexpr size_t SP_OFF = SP_CNT + sp_align(sizeof(int32_t) * (SP_MAX_BOXES + 1));
 constexpr size_t SP_TMP = SP_OFF + sp_align(sizeof(int32_t) * (SP_MAX_BOXES + 1));
-constexpr size_t SP_TMP_INTS = 256; // >= scan_tmp_size(max(SP_TABLE, SP_MAX_BOXES + 1))
+// the scans run over the bucket table and over the per-box counts
+constexpr size_t SP_TMP_INTS = 256;
+static_assert(SP_TMP_INTS >= (size_t)scan_tmp_size(SP_TABLE > SP_MAX_BOXES + 1 ? SP_TABLE
+                                                                             : SP_MAX_BOXES + 1),
+              "scan scratch region too small for the largest scan");
 constexpr size_t SP_PAIRS = SP_TMP + sp_align(sizeof(int32_t) * SP_TMP_INTS);
 constexpr size_t SP_STATUS = SP_PAIRS + sp_align(sizeof(int32_t) * 2 * SP_MAX_PAIRS);
 constexpr size_t SP_BYTES = SP_STATUS + 256;
@@ -1431,7 +1435,10 @@ std::mutex g_sp_mutex;
 unsigned char *g_sp_ptr[256] = {};
 
 // Device address of g_pairs_scratch on the current device, looked up once per
-// device (the lookup initialises the module on that device).
+// device (the lookup initialises the module on that device). The address is
+// kept for the life of the process: a cudaDeviceReset of the device unloads
+// the module and ends every context of this library on it, this address
+// included, so no call may follow a reset.
 hg_status static_scratch(int device, unsigned char **out) {
   if (device < 0 || device >= 256) return fail(HG_ERR_INVALID_ARGUMENT, "device index out of range");
   std::lock_guard<std::mutex> lock(g_sp_mutex);

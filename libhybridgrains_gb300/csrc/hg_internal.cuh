@@ -429,7 +429,19 @@ hg_status dem_candidate_pairs(hg_context *ctx, int64_t n, const double *mn,
                               int64_t *count);
 hg_status exclusive_scan_i32(const int32_t *in, int32_t *out, int64_t n,
                              int32_t *tmp, cudaStream_t s);
-int64_t scan_tmp_size(int64_t n);
+// Elements per tile of exclusive_scan_i32 (256 threads x 8 elements).
+constexpr int SCAN_TILE_ELEMS = 2048;
+// Ints of temporary storage exclusive_scan_i32 needs for n elements: two per
+// tile at every level of the recursive scan of tile sums, plus two.
+constexpr int64_t scan_tmp_size(int64_t n) {
+  int64_t total = 0;
+  while (n > SCAN_TILE_ELEMS) {
+    const int64_t tiles = (n + SCAN_TILE_ELEMS - 1) / SCAN_TILE_ELEMS;
+    total += 2 * tiles;
+    n = tiles;
+  }
+  return total + 2;
+}
 // A capacity limit checked by the scan that produces the offsets: when the
 // total exceeds limit (>= 0), *overflow is set, status_bit raised in
 // *status and every count and offset written as zero; *total (when given)

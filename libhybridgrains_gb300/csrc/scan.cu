@@ -15,6 +15,7 @@ namespace {
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 8;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+static_assert(SCAN_TILE == SCAN_TILE_ELEMS, "scan_tmp_size assumes this tile size");
 
 __global__ void k_tile_sums(const int32_t *__restrict__ in, int64_t n,
                             int32_t *__restrict__ sums) {
@@ -128,16 +129,6 @@ hg_status exclusive_scan_i32_limited(int32_t *in, int32_t *out, int64_t n, const
   if (n <= 0 || n > small_scan_max())
     return fail(HG_ERR_INVALID_ARGUMENT, "limited scan: size out of range");
   return launch_small_scan(in, n, out, lim, s);
-}
-
-int64_t scan_tmp_size(int64_t n) {
-  int64_t total = 0;
-  while (n > SCAN_TILE) {
-    const int64_t tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
-    total += 2 * tiles;
-    n = tiles;
-  }
-  return total + 2;
 }
 
 // out[i] = sum(in[0..i)); in and out may not alias. tmp must hold

@@ -7,9 +7,10 @@ inputs:
 * column_collapse_scene.json: the MPM grid, material, rectangle and planes,
   the DEM penalty parameters and the hybrid (zone / resampling) settings.
 
-Run from the repository root where the reference checkout is available:
+Run from the repository root where the reference checkout is available,
+naming it as the argument or in $HG_REFERENCE_ROOT:
 
-    python tests/golden/make_column_collapse_assets.py [reference_root]
+    python tests/golden/make_column_collapse_assets.py <reference_root>
 """
 import json
 import os
@@ -34,7 +35,10 @@ def frac(s):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("HG_REFERENCE_ROOT", "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("HG_REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: make_column_collapse_assets.py <reference_root> "
+                 "(or set HG_REFERENCE_ROOT)")
     d = os.path.join(root, "assets", "hybridgrains2dnew", "column-collapse")
     dem = ET.parse(os.path.join(d, "dem.xml")).getroot()
     geo = [float(g.get("r")) for g in dem.findall("geometry")]

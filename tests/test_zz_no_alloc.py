@@ -62,3 +62,42 @@ def test_static_pairs_rejects_too_many_boxes(ctx):
                                            ctypes.byref(cnt))
     assert st == 4  # HG_ERR_CAPACITY
     assert b"at most" in lib.hg_last_error()
+
+
+def call_static(ctx, mn, mx, cap):
+    lib = _capi.load()
+    n = mn.shape[0]
+    cnt = ctypes.c_int64()
+    out = np.zeros((max(cap, 1), 2), dtype=np.int32)
+    st = lib.hg_dem_candidate_pairs_static(ctx._h, n, mn.ctypes.data_as(_capi._D),
+                                           mx.ctypes.data_as(_capi._D), cap,
+                                           out.ctypes.data_as(_capi._I32), ctypes.byref(cnt))
+    return st, cnt.value, out[:cap]
+
+
+def test_static_pairs_rejects_too_many_pairs(ctx):
+    # 128 x 128 boxes of width 3.2 on a unit lattice: each overlaps its 48
+    # neighbours within three cells, 24 of them later in index order (within
+    # the per-box limit of 32), about 376,000 pairs in all
+    k = np.arange(128, dtype=np.float64)
+    c = np.stack(np.meshgrid(k, k), axis=-1).reshape(-1, 2)
+    mn, mx = np.ascontiguousarray(c - 1.6), np.ascontiguousarray(c + 1.6)
+    assert len(mn) <= _capi.HG_STATIC_PAIRS_MAX_BOXES
+    ref = hg.candidate_pairs(ctx, mn, mx)
+    assert len(ref) > _capi.HG_STATIC_PAIRS_MAX_PAIRS
+    st, _, _ = call_static(ctx, mn, mx, 0)
+    assert st == 4  # HG_ERR_CAPACITY
+    assert b"holds at most" in _capi.load().hg_last_error()
+
+
+def test_static_pairs_truncates_to_cap(ctx):
+    # a cap below the count: the full count comes back, and the first cap
+    # pairs of the sorted set
+    mn, mx = boxes(1, 12000, 0.12)
+    ref = hg.candidate_pairs(ctx, mn, mx)
+    cap = 100
+    assert len(ref) > cap
+    st, count, got = call_static(ctx, mn, mx, cap)
+    assert st == 0
+    assert count == len(ref)
+    assert np.array_equal(got, ref[:cap])
