@@ -217,7 +217,6 @@ def run_ours(args, rank, world, local):
     tune = mix.autotune(dt, args.tune_steps) if args.tune_steps > 0 else None
     mix.flow(dt, args.warmup)
     ctx.synchronize()
-    pre_steps = (len(tune["tried"]) * (args.tune_steps + 1) if tune else 0) + args.warmup
     barrier(world)
     launches0 = hg.kernel_launch_count()
     with ClockSampler(local) as clk:
@@ -232,15 +231,27 @@ def run_ours(args, rank, world, local):
     G = mix.grid()
     n_active = int((G["mass"] > 0).sum())
     # Per-kernel durations for the roofline: the timed steps replay 16-step
-    # CUDA graphs, which carry no events, so the same steps run again from the
-    # same start, one call per step with CUDA events around each launch (each
-    # interval also holds the gap to the neighbouring launch).
+    # CUDA graphs, which carry no events, so the column runs again from the
+    # same start with CUDA events around each launch (each interval also holds
+    # the gap to the neighbouring launch) over two fixed windows of a
+    # 10,000-step run, whatever --steps is: steps 0-2,000 (the column at
+    # rest) and 8,000-10,000 (flowing, more points on the plastic branch).
     mix.upload(pts["q"], pts["v"], pts["m"], pts["vol"], pts["hl"])
-    mix.flow(dt, pre_steps)
-    mix.profile(True)
-    mix.flow(dt, args.steps)
-    g2p2g_ms, update_ms, prof_steps = mix.profile_read()
-    mix.profile(False)
+    windows = []
+    for start, length in ((0, args.roofline_window), (args.roofline_span - args.roofline_window,
+                                                      args.roofline_window)):
+        done = sum(w["start"] + w["steps"] for w in windows[-1:])
+        if start > done:
+            mix.flow(dt, start - done)
+        mix.profile(True)
+        mix.flow(dt, length)
+        f_ms, u_ms, k = mix.profile_read()
+        mix.profile(False)
+        windows.append({"start": start, "steps": k, "g2p2g_us": 1e3 * f_ms / max(k, 1),
+                        "grid_update_us": 1e3 * u_ms / max(k, 1)})
+    g2p2g_ms = sum(w["g2p2g_us"] * w["steps"] for w in windows) * 1e-3
+    update_ms = sum(w["grid_update_us"] * w["steps"] for w in windows) * 1e-3
+    prof_steps = sum(w["steps"] for w in windows)
     status |= mix.status()
 
     # ---- plain FP64 GPU step on the same workload ------------------------------
@@ -348,14 +359,19 @@ def run_ours(args, rank, world, local):
     alg_bytes = n * BYTES_PER_PARTICLE + n_active * BYTES_PER_ACTIVE_NODE
     per_launch_s = (g2p2g_ms * 1e-3) / max(prof_steps, 1)
     achieved = alg_bytes / per_launch_s / 1e9
-    traffic = None  # DRAM bytes per launch from the committed ncu summary
+    traffic = ncu_dram_pct = None  # from the committed ncu summary of this kernel
     tpath = os.path.join(ROOT, "profiles", "kx_g2p2g_column_2M.md")
     if os.path.exists(tpath):
         import re
         with open(tpath) as f:
-            mt = re.search(r"traffic_bytes_per_launch = (\d+)", f.read())
+            text = f.read()
+        mt = re.search(r"traffic_bytes_per_launch = (\d+)", text)
         if mt:
             traffic = int(mt.group(1))
+        mt = re.search(r"dram_throughput_pct = ([0-9.]+)", text)
+        if mt:
+            ncu_dram_pct = float(mt.group(1))
+    fused_min = n * FUSED_MIN_BYTES_PER_PARTICLE + n_active * FUSED_MIN_BYTES_PER_ACTIVE_NODE
 
     cpu = None
     if world == 1 and args.cpu_steps > 0:
@@ -380,12 +396,17 @@ def run_ours(args, rank, world, local):
         "roofline": {"bound": "hbm", "kernel": "kx_g2p2g", "achieved": achieved, "peak": peak,
                      "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "algorithmic_bytes": alg_bytes,
-                     "fused_min_bytes": n * FUSED_MIN_BYTES_PER_PARTICLE
-                                        + n_active * FUSED_MIN_BYTES_PER_ACTIVE_NODE,
+                     "fused_min_bytes": fused_min,
+                     "frac_fused_min": fused_min / per_launch_s / 1e9 / peak,
+                     "ncu_dram_throughput_pct": ncu_dram_pct,
                      "kernel_ms": per_launch_s * 1e3,
                      "grid_update_ms": update_ms / max(prof_steps, 1),
-                     "timing": "CUDA events around each launch over a replay of the timed "
-                               "steps from the same start"},
+                     "windows": windows,
+                     "timing": "CUDA events around each launch, steps 0-%d and %d-%d of a "
+                               "%d-step run from rest (the mean of both windows)"
+                               % (args.roofline_window,
+                                  args.roofline_span - args.roofline_window,
+                                  args.roofline_span, args.roofline_span)},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "serving": serve,
@@ -475,8 +496,10 @@ def run_dem(args, ctx):
                            "algorithmic_bytes_per_step": algl, "achieved_gbs": achl,
                            "hbm_frac": achl / peak}
             dl.close()
+    dense = run_dem_dense(args, ctx) if args.dem_dense_steps > 0 else None
     return {"workload": "DEM column: 10,000 disks, hex pitch 2.2 mm, r U[0.9,1.1] mm, dt 1e-6 s, "
                         "FP64 penalty contacts with friction history",
+            "dense": dense,
             "disk_steps_per_s": gpu_rate, "us_per_step": 1e3 * ms / args.dem_steps,
             "steps": args.dem_steps, "contacts": contacts,
             "launches_per_step": launches / args.dem_steps,
@@ -486,6 +509,70 @@ def run_dem(args, ctx):
                              "kind": "port", "sample": "%d steps of the same column (%.1f s)" %
                              (csteps, cs)},
             "mixed": mixed, "large": large}
+
+
+def run_dem_dense(args, ctx):
+    """The DEM column's disks compacted to a 1.9 mm hex pitch between a floor
+    and two walls (scenes.dem_packed: about 2.8 contacts per disk, so the
+    contact law carries the load), at 10,000 and 1,000,000 disks, FP64
+    (bit-exact with the oracle) and mixed precision; disk-steps/s, contacts
+    per disk and algorithmic bandwidth against the measured HBM copy rate.
+    The oracle times the 10,000-disk case on one host core (the reference's
+    penalty map is serial)."""
+    import libhybridgrains_gb300 as hg
+    import oracle
+    from libhybridgrains_gb300 import scenes
+    dp = scenes.dem_params()
+    peak = measured_peaks().get("hbm_gbs") or 6800.0
+    dt = 1.0e-6
+    out = {"workload": "disks of the DEM column on a 1.9 mm hex pitch (r U[0.9,1.1] mm, seed "
+                       "12345) between a floor and two walls, dt 1e-6 s, 200 settling steps "
+                       "before timing"}
+    for label, n, per_row, steps in (("10k", 10000, 100, args.dem_dense_steps),
+                                     ("1M", 1000000, 1000, args.dem_dense_large_steps)):
+        if steps <= 0:
+            continue
+        sc = scenes.dem_packed(n=n, per_row=per_row)
+        case = {"disks": n, "steps": steps}
+        for name, prec in (("fp64", hg.FP64), ("mixed", hg.MIXED)):
+            d = hg.DEM(ctx, scenes.GRAVITY, dp["kn"], dp["kt"], dp["gamman"], dp["gammat"],
+                       dp["mu"], sc["planes"], capacity=n, contact_capacity=4 * n,
+                       precision=prec)
+            d.upload(sc["q"], sc["v"], sc["r"], sc["m"], sc["I"], sc["fixed"])
+            d.flow(dt, 200)
+            ctx.synchronize()
+            l0 = hg.kernel_launch_count()
+            ctx.timer_begin()
+            d.flow(dt, steps)
+            ms = ctx.timer_end()
+            launches = hg.kernel_launch_count() - l0
+            nc = d.num_contacts()
+            per_disk, per_contact = (128, 40) if prec == hg.FP64 else (88, 24)
+            alg = n * per_disk + nc * per_contact
+            ach = alg / (ms * 1e-3 / steps) / 1e9
+            case[name] = {"disk_steps_per_s": n * steps / (ms * 1e-3),
+                          "us_per_step": 1e3 * ms / steps, "contacts": nc,
+                          "contacts_per_disk": nc / n, "launches_per_step": launches / steps,
+                          "algorithmic_bytes_per_step": alg, "achieved_gbs": ach,
+                          "hbm_frac": ach / peak, "status": d.status()}
+            d.close()
+        if label == "10k" and args.dem_cpu_steps > 0:
+            o = oracle.DEM(sc["q"], sc["v"], sc["r"], sc["m"], sc["I"], sc["fixed"],
+                           scenes.GRAVITY, dp["kn"], dp["kt"], dp["gamman"], dp["gammat"],
+                           dp["mu"], 1.0)
+            for (x, nn) in sc["planes"]:
+                o.add_plane(x, nn)
+            o.step(dt, 1)
+            csteps = max(1, args.dem_cpu_steps)
+            t0 = time.perf_counter()
+            o.step(dt, csteps)
+            cs = time.perf_counter() - t0
+            case["cpu_baseline"] = {"value": n * csteps / cs, "unit": "disk-steps/s",
+                                    "cores": 1, "kind": "port",
+                                    "sample": "%d steps of the same packing (%.1f s)"
+                                              % (csteps, cs)}
+        out[label] = case
+    return out
 
 
 def run_hybrid(args, ctx):
@@ -623,9 +710,13 @@ def main():
     ap.add_argument("--hybrid-steps", type=int, default=1000)
     ap.add_argument("--dem-cpu-steps", type=int, default=200)
     ap.add_argument("--tune-steps", type=int, default=20)
+    ap.add_argument("--roofline-span", type=int, default=10000)
+    ap.add_argument("--roofline-window", type=int, default=2000)
     ap.add_argument("--ugimp-steps", type=int, default=200)
     ap.add_argument("--dem-large-disks", type=int, default=1000000)
     ap.add_argument("--dem-large-steps", type=int, default=200)
+    ap.add_argument("--dem-dense-steps", type=int, default=2000)
+    ap.add_argument("--dem-dense-large-steps", type=int, default=200)
     ap.add_argument("--serve-requests", type=int, default=256)
     ap.add_argument("--serve-rate", type=float, default=50.0)
     ap.add_argument("--serve-steps", type=int, default=2000)

@@ -2,7 +2,8 @@
 
     python -m libhybridgrains_gb300.profile_cases dem --disks 1000000 --steps 12
     python -m libhybridgrains_gb300.profile_cases dem --disks 10000 --per-row 100 --steps 12
-    python -m libhybridgrains_gb300.profile_cases dem --disks 1000000 --packed --steps 12
+    python -m libhybridgrains_gb300.profile_cases dem --disks 1000000 --packed --steps 12 \
+        [--precision mixed]
     python -m libhybridgrains_gb300.profile_cases hybrid --steps 6 [--precision mixed]
     python -m libhybridgrains_gb300.profile_cases column --steps 8
 
@@ -33,7 +34,7 @@ def main(argv=None):
     ap.add_argument("--packed", action="store_true",
                     help="DEM: the compacted lattice (scenes.dem_packed)")
     ap.add_argument("--precision", choices=("fp64", "mixed"), default="fp64",
-                    help="the hybrid case's MPM bulk")
+                    help="the hybrid case's MPM bulk; the packed DEM case's contact law")
     args = ap.parse_args(argv)
     ctx = hg.Context(0)
     if args.case == "dem":
@@ -42,7 +43,8 @@ def main(argv=None):
             dp = scenes.dem_params()
             obj = hg.DEM(ctx, scenes.GRAVITY, dp["kn"], dp["kt"], dp["gamman"], dp["gammat"],
                          dp["mu"], sc["planes"], capacity=args.disks,
-                         contact_capacity=4 * args.disks)
+                         contact_capacity=4 * args.disks,
+                         precision=hg.MIXED if args.precision == "mixed" else hg.FP64)
             ddt = 1.0e-6
         else:
             sc = scenes.dem_column(n=args.disks, per_row=args.per_row)
