@@ -464,8 +464,20 @@ typedef struct {
   double n[2];
 } hg_dem_plane;
 
+/* RigidBody2DStaticDrum (rigidbody2d/RigidBody2DStaticDrum.h:6-33): a fixed
+ * circular wall of radius r centred at x that holds the disks inside it
+ * (StaticDrumCircleConstraint.cpp:7-13: a disk touches it once its centre is
+ * r - r_disk or more from x). Scene files give only x and r; the drum does
+ * not move. */
+typedef struct {
+  double x[2];
+  double r;
+} hg_dem_drum;
+enum { HG_MAX_DRUMS = 8 };
+
 /* PenaltyImpactFrictionMap parameters (rigidbody2d/PenaltyImpactFrictionMap.
- * cpp:15-26) plus NearEarthGravityForce and the body/contact capacities. */
+ * cpp:15-26) plus NearEarthGravityForce, the static planes and drums and the
+ * body/contact capacities. */
 typedef struct {
   double gravity[2];
   double kn, kt, gamman, gammat, mu;
@@ -480,7 +492,8 @@ typedef struct {
    * pairwise position difference, contact points and the position update in
    * FP64 (velocities and records keep FP64 storage holding FP32 values). */
   int32_t precision;
-  int32_t pad2_;
+  int32_t num_drums;
+  hg_dem_drum drums[HG_MAX_DRUMS];
 } hg_dem_desc;
 
 hg_status hg_dem_create(hg_context *ctx, const hg_dem_desc *desc, hg_dem **out);
@@ -537,11 +550,18 @@ hg_status hg_dem_download(hg_dem *d, double *q, double *v);
 hg_status hg_dem_step(hg_dem *d, double dt, int32_t nsteps, int32_t weighted);
 hg_status hg_dem_num_contacts(hg_dem *d, int64_t *n);
 /* The collision cache (PenaltyImpactFrictionMap::getCollisionCache), one
- * record of HG_DEM_RECORD_WIDTH doubles per contact, ordered plane contacts
- * (body-major), circle-circle (body-major), kinematic circle-circle
- * (body-major): kind, first, second, depth, n[2], delta_s[2], vrel[2],
- * r0[2], r1[2], weight, contact_point[2], normal_force[2],
- * friction_force[2], 0. */
+ * record of HG_DEM_RECORD_WIDTH doubles per contact, ordered: contacts with
+ * static objects (body-major; each body's plane contacts, then its drum
+ * contacts), circle-circle (body-major), kinematic circle-circle
+ * (body-major). Fields: kind (HG_DEM_KIND_*), first, second (the plane or
+ * drum index for static objects), depth, n[2], delta_s[2], vrel[2], r0[2],
+ * r1[2], weight, contact_point[2], normal_force[2], friction_force[2], 0. */
+enum {
+  HG_DEM_KIND_PLANE = 0,
+  HG_DEM_KIND_CIRCLE = 1,
+  HG_DEM_KIND_KINEMATIC = 2,
+  HG_DEM_KIND_DRUM = 3
+};
 enum { HG_DEM_RECORD_WIDTH = 22 };
 hg_status hg_dem_download_contacts(hg_dem *d, int64_t cap, double *records,
                                    int64_t *count);

@@ -383,7 +383,9 @@ class DEM:
     """Circle bodies with the penalty impact-friction map (rigidbody2d)."""
 
     def __init__(self, ctx, gravity, kn, kt, gamman, gammat, mu, planes=(), cell_scale=1.0,
-                 capacity=0, contact_capacity=0, precision=0):
+                 capacity=0, contact_capacity=0, precision=0, drums=()):
+        """planes: ((x, y), (nx, ny)) static half-planes; drums: ((x, y), r)
+        static drums (RigidBody2DStaticDrum) holding the disks inside."""
         self.ctx = ctx
         d = _capi.DemDesc()
         d.gravity[:] = list(map(float, gravity))
@@ -394,6 +396,13 @@ class DEM:
         for k, (x, n) in enumerate(planes):
             d.planes[k].x[:] = list(map(float, x))
             d.planes[k].n[:] = list(map(float, n))
+        drums = list(drums)
+        if len(drums) > _capi.HG_MAX_DRUMS:
+            raise HGError("at most %d drums" % _capi.HG_MAX_DRUMS)
+        d.num_drums = len(drums)
+        for k, (x, r) in enumerate(drums):
+            d.drums[k].x[:] = list(map(float, x))
+            d.drums[k].r = float(r)
         d.capacity = int(capacity)
         d.contact_capacity = int(contact_capacity or 8 * max(capacity, 1))
         d.precision = int(precision)

@@ -13,6 +13,8 @@ LIB_PATH = (os.path.join(HERE, "_build_bounds", "libhg_gpu_bounds.so")
             else os.path.join(HERE, "_build", "libhg_gpu.so"))
 
 HG_MAX_PLANES = 8
+HG_MAX_DRUMS = 8
+HG_DEM_KIND_PLANE, HG_DEM_KIND_CIRCLE, HG_DEM_KIND_KINEMATIC, HG_DEM_KIND_DRUM = 0, 1, 2, 3
 HG_DEM_RECORD_WIDTH = 22
 HG_STATIC_PAIRS_MAX_BOXES = 16384
 HG_STATIC_PAIRS_MAX_PAIRS = 262144
@@ -45,6 +47,10 @@ class MpmDesc(ctypes.Structure):
 
 class DemPlane(ctypes.Structure):
     _fields_ = [("x", ctypes.c_double * 2), ("n", ctypes.c_double * 2)]
+
+
+class DemDrum(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_double * 2), ("r", ctypes.c_double)]
 
 
 class ZonesDesc(ctypes.Structure):
@@ -90,7 +96,8 @@ class DemDesc(ctypes.Structure):
                 ("cell_scale", ctypes.c_double), ("num_planes", ctypes.c_int32),
                 ("pad_", ctypes.c_int32), ("planes", DemPlane * HG_MAX_PLANES),
                 ("capacity", ctypes.c_int64), ("contact_capacity", ctypes.c_int64),
-                ("precision", ctypes.c_int32), ("pad2_", ctypes.c_int32)]
+                ("precision", ctypes.c_int32), ("num_drums", ctypes.c_int32),
+                ("drums", DemDrum * HG_MAX_DRUMS)]
 
 
 _P = ctypes.c_void_p

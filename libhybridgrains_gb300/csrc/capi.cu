@@ -1156,6 +1156,11 @@ hg_status hg_dem_create(hg_context *ctx, const hg_dem_desc *d, hg_dem **out) {
   *out = nullptr;
   if (d->num_planes < 0 || d->num_planes > HG_MAX_PLANES)
     return fail(HG_ERR_INVALID_ARGUMENT, "num_planes out of range");
+  if (d->num_drums < 0 || d->num_drums > HG_MAX_DRUMS)
+    return fail(HG_ERR_INVALID_ARGUMENT, "num_drums out of range");
+  for (int k = 0; k < d->num_drums; ++k)
+    if (!finite_all(d->drums[k].x, 2) || !(d->drums[k].r > 0.0) || !std::isfinite(d->drums[k].r))
+      return fail(HG_ERR_INVALID_ARGUMENT, "invalid drum");
   if (d->capacity < 0 || d->capacity > (int64_t)(1 << 30) || d->contact_capacity < 0 ||
       d->contact_capacity > (int64_t)INT32_MAX)
     return fail(HG_ERR_INVALID_ARGUMENT, "capacity out of range");
@@ -1197,6 +1202,12 @@ hg_status hg_dem_create(hg_context *ctx, const hg_dem_desc *d, hg_dem **out) {
     P.px[k][1] = pl.x[1];
     P.pn[k][0] = pl.n[0] / nn;
     P.pn[k][1] = pl.n[1] / nn;
+  }
+  P.ndrums = d->num_drums;
+  for (int k = 0; k < d->num_drums; ++k) {
+    P.dx[k][0] = d->drums[k].x[0];
+    P.dx[k][1] = d->drums[k].x[1];
+    P.dr[k] = d->drums[k].r;
   }
   dm->cap = d->capacity;
   dm->ccap = d->contact_capacity;

@@ -129,7 +129,8 @@ __device__ __forceinline__ void sort_small(int *keys, int n) {
 // (StaticPlaneCircleConstraint::isActive, StaticPlaneCircleConstraint.cpp:
 // 12-17, in FP64) as bits. The FP64 arithmetic per body is a few operations;
 // per candidate pair the search needs FP32 only, except for the exact tests
-// of the pairs that survive the FP32 filter. The home cell only has to be a
+// of the pairs that survive the FP32 filter. Active static drums take the
+// bits after the planes'. The home cell only has to be a
 // consistent binning (the search covers the neighbouring cells), so it is
 // floor(x_min / H) computed as x_min * (1 / H).
 struct HomeArgs {
@@ -138,6 +139,8 @@ struct HomeArgs {
   uint32_t mask;
   int nplanes;
   double px[HG_MAX_PLANES][2], pn[HG_MAX_PLANES][2];
+  int ndrums;
+  double dx[HG_MAX_DRUMS][2], dr[HG_MAX_DRUMS];
   const double *q, *r;
   const uint8_t *fixed;
   float4 *rec; // 2 per body: (offset x, offset y, radius, flags), (home cell x, y)
@@ -148,6 +151,7 @@ struct HomeArgs {
 };
 
 enum : uint32_t { REL_FIXED = 1u, REL_PLANE0 = 2u };
+static_assert(1 + HG_MAX_PLANES + HG_MAX_DRUMS <= 32, "static-object bits of the body record");
 
 __global__ void kd_bodies_home(HomeArgs A) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -167,6 +171,12 @@ __global__ void kd_bodies_home(HomeArgs A) {
   for (int k = 0; k < A.nplanes; ++k) {
     const double d = A.pn[k][0] * (x - A.px[k][0]) + A.pn[k][1] * (y - A.px[k][1]);
     if (d <= ri) flags |= REL_PLANE0 << k;
+  }
+  // StaticDrumCircleConstraint::isActive (StaticDrumCircleConstraint.cpp:7-13):
+  // |x_drum - x|^2 >= (r_drum - r)^2; drum k is static object nplanes + k
+  for (int k = 0; k < A.ndrums; ++k) {
+    const double ex = A.dx[k][0] - x, ey = A.dx[k][1] - y, g = A.dr[k] - ri;
+    if (ex * ex + ey * ey >= g * g) flags |= REL_PLANE0 << (A.nplanes + k);
   }
   // one 32-byte record: the FP32 part, then the home cell
   A.rec[2 * i] = make_float4((float)(x - (double)cx * A.H), (float)(y - (double)cy * A.H),
@@ -214,7 +224,7 @@ struct PairArgs {
   const int32_t *items;
   const double *q;
   const double *r;
-  int nplanes;
+  int nstatic;        // static objects: the planes, then the drums
   int32_t *cnt;       // 3N counts [kind][body]
   uint32_t *plist;    // PW partners per body (fixed partners flagged by bit 31)
   int32_t *pfill;     // partners credited to each body (counting pass)
@@ -291,7 +301,6 @@ __device__ __forceinline__ void for_each_partner(const PairArgs &A, int a, F &&f
 // and the first PW partners in plist (in no particular order; the emission
 // pass sorts them). The survivors of the FP32 filter take the same FP64 tests
 // as the full search, which are symmetric in the two bodies.
-__constant__ int HALF_CELLS[5][2] = {{0, 0}, {1, 0}, {-1, 1}, {0, 1}, {1, 1}};
 
 __device__ __forceinline__ void credit(const PairArgs &A, int first, int second, bool kin,
                                        bool &overflow) {
@@ -306,53 +315,52 @@ __device__ __forceinline__ void credit(const PairArgs &A, int first, int second,
   if (slot < PW) A.plist[(int64_t)first * PW + slot] = (uint32_t)second | (kin ? 0x80000000u : 0u);
 }
 
+// One thread per (body, cell of the half neighbourhood): thread t takes cell
+// t / n of body t % n, so a warp's lanes read consecutive bodies' records and
+// each thread follows one bucket instead of five.
 __global__ void kd_pairs_count(PairArgs A) {
   const int64_t n = A.n;
-  const int a = (int)(blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
-  if (a >= n) return;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= 5 * n) return;
+  const int c = (int)(t / n);
+  const int a = (int)(t - (int64_t)c * n);
   const float4 pa = A.rec[2 * a], ca = A.rec[2 * a + 1];
   const uint32_t flags = __float_as_uint(pa.w);
   const bool af = (flags & REL_FIXED) != 0u;
-  if (!af) A.cnt[a] = __popc(flags >> 1); // static planes
-  const int2 ha = make_int2(__float_as_int(ca.x), __float_as_int(ca.y));
+  if (c == 0 && !af) A.cnt[a] = __popc(flags >> 1); // static planes
+  // cell c of the half neighbourhood: (0, 0), (1, 0), (-1, 1), (0, 1), (1, 1)
+  const int dy = c >= 2 ? 1 : 0;
+  const int dx = c == 0 ? 0 : (c == 1 ? 1 : c - 3);
+  const int cx = __float_as_int(ca.x) + dx, cy = __float_as_int(ca.y) + dy;
+  const uint32_t bk = cell_hash(cx, cy, A.mask);
+  const int be = A.bucket_end[bk], bs = be - A.bucket_count[bk];
+  if (bs >= be) return;
   const double xa = A.q[3 * a], ya = A.q[3 * a + 1], ra = A.r[a];
-  int bs[5], be[5];
-#pragma unroll
-  for (int c = 0; c < 5; ++c) {
-    const uint32_t bk = cell_hash(ha.x + HALF_CELLS[c][0], ha.y + HALF_CELLS[c][1], A.mask);
-    be[c] = A.bucket_end[bk];
-    bs[c] = be[c] - A.bucket_count[bk];
-  }
   bool overflow = false;
-#pragma unroll
-  for (int c = 0; c < 5; ++c) {
-    const int dx = HALF_CELLS[c][0], dy = HALF_CELLS[c][1];
-    const int cx = ha.x + dx, cy = ha.y + dy;
-    for (int k = bs[c]; k < be[c]; ++k) {
-      if (!HG_INDEX_OK(k, n, A.status)) break;
-      const int b = A.items[k];
-      if (!HG_INDEX_OK(b, n, A.status)) continue;
-      if (b == a || (c == 0 && b < a)) continue;
-      const float4 pb = A.rec[2 * b], cb = A.rec[2 * b + 1];
-      if (__float_as_int(cb.x) != cx || __float_as_int(cb.y) != cy)
-        continue; // bucket shared by another cell
-      const bool bf = (__float_as_uint(pb.w) & REL_FIXED) != 0u;
-      if (af && bf) continue;
-      const float reach = pa.z + pb.z + A.tol;
-      const float ex = (float)dx * A.Hf + (pb.x - pa.x);
-      const float ey = (float)dy * A.Hf + (pb.y - pa.y);
-      if (ex * ex + ey * ey > reach * reach) continue;
-      const double xb = A.q[3 * b], yb = A.q[3 * b + 1], rb = A.r[b];
-      if (!((xa + ra >= xb - rb && ya + ra >= yb - rb) &&
-            (xb + rb >= xa - ra && yb + rb >= ya - ra)))
-        continue;
-      const double ddx = xa - xb, ddy = ya - yb;
-      const double c0 = (ddx * ddx + ddy * ddy) - (ra + rb) * (ra + rb);
-      if (!(c0 <= 0.0)) continue;
-      if (af) credit(A, b, a, true, overflow);
-      else if (bf) credit(A, a, b, true, overflow);
-      else credit(A, min(a, b), max(a, b), false, overflow);
-    }
+  for (int k = bs; k < be; ++k) {
+    if (!HG_INDEX_OK(k, n, A.status)) break;
+    const int b = A.items[k];
+    if (!HG_INDEX_OK(b, n, A.status)) continue;
+    if (b == a || (c == 0 && b < a)) continue;
+    const float4 pb = A.rec[2 * b], cb = A.rec[2 * b + 1];
+    if (__float_as_int(cb.x) != cx || __float_as_int(cb.y) != cy)
+      continue; // bucket shared by another cell
+    const bool bf = (__float_as_uint(pb.w) & REL_FIXED) != 0u;
+    if (af && bf) continue;
+    const float reach = pa.z + pb.z + A.tol;
+    const float ex = (float)dx * A.Hf + (pb.x - pa.x);
+    const float ey = (float)dy * A.Hf + (pb.y - pa.y);
+    if (ex * ex + ey * ey > reach * reach) continue;
+    const double xb = A.q[3 * b], yb = A.q[3 * b + 1], rb = A.r[b];
+    if (!((xa + ra >= xb - rb && ya + ra >= yb - rb) &&
+          (xb + rb >= xa - ra && yb + rb >= ya - ra)))
+      continue;
+    const double ddx = xa - xb, ddy = ya - yb;
+    const double c0 = (ddx * ddx + ddy * ddy) - (ra + rb) * (ra + rb);
+    if (!(c0 <= 0.0)) continue;
+    if (af) credit(A, b, a, true, overflow);
+    else if (bf) credit(A, a, b, true, overflow);
+    else credit(A, min(a, b), max(a, b), false, overflow);
   }
   if (overflow) atomicOr(A.status, (uint32_t)HG_STATUS_CELL_OVERFLOW);
 }
@@ -373,7 +381,7 @@ __global__ void kd_pairs_emit(PairArgs A) {
   }
   const uint32_t flags = __float_as_uint(A.rec[2 * a].w);
   int j = 0;
-  for (int k = 0; k < A.nplanes; ++k)
+  for (int k = 0; k < A.nstatic; ++k)
     if (flags & (REL_PLANE0 << k)) A.keys[o0 + j++] = ckey(K_PLANE, a, k);
   if (ncc + nkin <= PW) {
     // odd-even transposition sort of the flagged indices: circle-circle
@@ -441,6 +449,8 @@ struct ContactArgs {
   double kn, kt, gn, gt, mu;
   int nplanes;
   double px[HG_MAX_PLANES][2], pn[HG_MAX_PLANES][2];
+  int ndrums; // static objects nplanes .. nplanes + ndrums - 1
+  double dx[HG_MAX_DRUMS][2], dr[HG_MAX_DRUMS];
   const double *q, *v, *r, *w;
   const int32_t *count; // device count (total contacts)
   const int64_t *keys;
@@ -479,7 +489,7 @@ __global__ void kd_contacts(ContactArgs C) {
     const int a = (int)((key >> 30) & 0x3FFFFFFF);
     const int b = (int)(key & 0x3FFFFFFF);
     if (!HG_INDEX_OK(a, C.n, C.status) ||
-        !HG_INDEX_OK(b, kind == K_PLANE ? (int64_t)C.nplanes : C.n, C.status))
+        !HG_INDEX_OK(b, kind == K_PLANE ? (int64_t)(C.nplanes + C.ndrums) : C.n, C.status))
       continue;
     const D2 qa{C.q[3 * a], C.q[3 * a + 1]};
     const D2 va{C.v[3 * a], C.v[3 * a + 1]};
@@ -487,7 +497,24 @@ __global__ void kd_contacts(ContactArgs C) {
     double depth, weight;
     D2 n, cp{0.0, 0.0}, r0, r1{0.0, 0.0}, vrel;
     const double ra = C.r[a];
-    if (kind == K_PLANE) { // PenaltyImpactFrictionMap.cpp:316-359
+    if (kind == K_PLANE && b >= C.nplanes) { // PenaltyImpactFrictionMap.cpp:361-401
+      // StaticDrumCircleConstraint.cpp:100-159: the normal points from the
+      // disk's centre to the drum's; the contact point is the disk's point
+      // farthest from the drum's centre
+      const int dk = b - C.nplanes;
+      const D2 xd{C.dx[dk][0], C.dx[dk][1]};
+      n = dnormalized(dsub(xd, qa));
+      cp = dsub(qa, dscl(ra, n));
+      weight = C.weighted ? C.w[a] : 1.0;
+      const double gap = -(dnorm(dsub(xd, qa)) - (C.dr[dk] - ra));
+      depth = gap < 0.0 ? gap : 0.0; // std::min(0.0, gap)
+      r0 = dscl(-ra, n);
+      const D2 t0{-r0.y, r0.x};
+      const D2 arm = dsub(cp, xd);
+      const D2 tp{-arm.y, arm.x};
+      const D2 vp{0.0 + 0.0 * tp.x, 0.0 + 0.0 * tp.y}; // the drum is static
+      vrel = dsub(dadd(va, dscl(wa, t0)), vp);
+    } else if (kind == K_PLANE) { // PenaltyImpactFrictionMap.cpp:316-359
       const D2 xp{C.px[b][0], C.px[b][1]};
       n = D2{C.pn[b][0], C.pn[b][1]};
       cp = dsub(qa, dscl(ra, n));
@@ -719,7 +746,7 @@ __global__ void kdx_contacts(ContactArgs C) {
     const int a = (int)((key >> 30) & 0x3FFFFFFF);
     const int b = (int)(key & 0x3FFFFFFF);
     if (!HG_INDEX_OK(a, C.n, C.status) ||
-        !HG_INDEX_OK(b, kind == K_PLANE ? (int64_t)C.nplanes : C.n, C.status))
+        !HG_INDEX_OK(b, kind == K_PLANE ? (int64_t)(C.nplanes + C.ndrums) : C.n, C.status))
       continue;
     const double qax = C.q[3 * a], qay = C.q[3 * a + 1];
     const F2 va{(float)C.v[3 * a], (float)C.v[3 * a + 1]};
@@ -728,7 +755,22 @@ __global__ void kdx_contacts(ContactArgs C) {
     float depth, weight;
     F2 n, r0, r1{0.0f, 0.0f}, vrel;
     double cpx, cpy;
-    if (kind == K_PLANE) { // PenaltyImpactFrictionMap.cpp:316-359
+    if (kind == K_PLANE && b >= C.nplanes) { // PenaltyImpactFrictionMap.cpp:361-401
+      const int dk = b - C.nplanes;
+      const double ex = C.dx[dk][0] - qax, ey = C.dx[dk][1] - qay; // FP64 difference
+      const F2 e{(float)ex, (float)ey};
+      n = fnormalized(e); // towards the drum's centre
+      // -(|e| - (R - r)) as ((R - r)^2 - |e|^2) / (|e| + R - r): the
+      // cancelling difference in FP64, the rest in FP32
+      const double g = C.dr[dk] - C.r[a];
+      const double g2 = g * g - (ex * ex + ey * ey);
+      depth = g2 < 0.0 ? (float)g2 / (fnrm(e) + (float)g) : 0.0f;
+      weight = C.weighted ? (float)C.w[a] : 1.0f;
+      r0 = fscl(-ra, n);
+      cpx = qax + (double)r0.x;
+      cpy = qay + (double)r0.y;
+      vrel = fadd(va, fscl(wa, F2{-r0.y, r0.x})); // the drum is static
+    } else if (kind == K_PLANE) { // PenaltyImpactFrictionMap.cpp:316-359
       n = F2{(float)C.pn[b][0], (float)C.pn[b][1]};
       // penetration from FP64 positions (a difference of nearly equal terms)
       const double dist = C.pn[b][0] * (qax - C.px[b][0]) + C.pn[b][1] * (qay - C.px[b][1]);
@@ -1011,6 +1053,12 @@ hg_status dem_step(hg_dem *d, double dt, int weighted) {
     H.invH = 1.0 / d->cell_h;
     H.mask = mask;
     H.nplanes = d->p.nplanes;
+    H.ndrums = d->p.ndrums;
+    for (int k = 0; k < HG_MAX_DRUMS; ++k) {
+      H.dx[k][0] = d->p.dx[k][0];
+      H.dx[k][1] = d->p.dx[k][1];
+      H.dr[k] = d->p.dr[k];
+    }
     for (int k = 0; k < HG_MAX_PLANES; ++k)
       for (int c = 0; c < 2; ++c) {
         H.px[k][c] = d->p.px[k][c];
@@ -1044,7 +1092,7 @@ hg_status dem_step(hg_dem *d, double dt, int weighted) {
   A.items = d->items.p;
   A.q = d->q.p;
   A.r = d->r.p;
-  A.nplanes = d->p.nplanes;
+  A.nstatic = d->p.nplanes + d->p.ndrums;
   A.cnt = d->per_body.p;
   A.off = d->per_body_off.p;
   const int nb = 1 - d->cc; // buffer receiving this step's contacts
@@ -1054,7 +1102,7 @@ hg_status dem_step(hg_dem *d, double dt, int weighted) {
   A.status = d->status.p;
   A.pfill = d->pfill.p;
   // (per_body and pfill were zeroed by kd_bodies_home)
-  HG_LAUNCH(kd_pairs_count, blocks_for(n, 128), 128, 0, s, A);
+  HG_LAUNCH(kd_pairs_count, blocks_for(5 * n, 128), 128, 0, s, A);
   HG_CHECK_LAUNCH();
   // offsets, the contact-capacity check (all contacts dropped when the list
   // would overflow) and the contact count
@@ -1094,6 +1142,12 @@ hg_status dem_step(hg_dem *d, double dt, int weighted) {
   Cg.gt = d->p.gt;
   Cg.mu = d->p.mu;
   Cg.nplanes = d->p.nplanes;
+  Cg.ndrums = d->p.ndrums;
+  for (int k = 0; k < HG_MAX_DRUMS; ++k) {
+    Cg.dx[k][0] = d->p.dx[k][0];
+    Cg.dx[k][1] = d->p.dx[k][1];
+    Cg.dr[k] = d->p.dr[k];
+  }
   for (int k = 0; k < HG_MAX_PLANES; ++k)
     for (int c = 0; c < 2; ++c) {
       Cg.px[k][c] = d->p.px[k][c];
@@ -1319,6 +1373,16 @@ hg_status dem_download_contacts(hg_dem *d, int64_t cap, double *rec, int64_t *co
     HG_CUDA_TRY(cudaMemcpyAsync(rec, d->crec[d->cc].p, sizeof(double) * RW * k,
                                 cudaMemcpyDeviceToHost, s));
     HG_CUDA_TRY(cudaStreamSynchronize(s));
+    // drum contacts are static objects after the planes on the device; the
+    // export names them by kind and drum index
+    if (d->p.ndrums > 0)
+      for (int64_t i = 0; i < k; ++i) {
+        double *o = rec + i * RW;
+        if (o[0] == (double)K_PLANE && o[2] >= (double)d->p.nplanes) {
+          o[0] = (double)HG_DEM_KIND_DRUM;
+          o[2] -= (double)d->p.nplanes;
+        }
+      }
   }
   return HG_OK;
 }

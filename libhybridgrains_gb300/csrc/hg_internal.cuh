@@ -356,6 +356,10 @@ struct DemParams {
   int precision; // HG_PRECISION_FP64 (bit-exact) or HG_PRECISION_MIXED
   int nplanes;
   double px[HG_MAX_PLANES][2], pn[HG_MAX_PLANES][2];
+  // static drums; their contacts share the plane contacts' list as static
+  // objects nplanes .. nplanes + ndrums - 1
+  int ndrums;
+  double dx[HG_MAX_DRUMS][2], dr[HG_MAX_DRUMS];
 };
 
 } // namespace hg

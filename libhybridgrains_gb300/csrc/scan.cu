@@ -56,46 +56,50 @@ __global__ void k_tile_scan(const int32_t *__restrict__ in, int64_t n,
 
 // Up to small_scan_max() elements: one CTA and one launch in place of three
 // (in a captured step the launches, not the bytes, are the cost at these
-// sizes). Warp w owns the 1024 consecutive elements from w * 1024 and reads
-// them 32 at a time with coalesced loads; 32 warp scans with a running
-// carry give each element its prefix within the warp's segment, one scan of
-// the 32 warp totals the segment offsets. No large shared-memory staging, so
-// the launch needs no change of the shared-memory carve-out.
+// sizes). Thread t owns the SMALL_ITEMS consecutive elements from
+// t * SMALL_ITEMS: it reads them as 16-byte vectors (all loads in flight at
+// once), scans them sequentially in registers, and one block scan of the
+// 1,024 thread totals gives each run its offset. The chain of dependent steps
+// is one pass over 32 registers and one block scan, instead of 32 warp scans.
+// No large shared-memory staging, so the launch needs no change of the
+// shared-memory carve-out.
 constexpr int SMALL_THREADS = 1024;
 constexpr int SMALL_ITEMS = 32;
 constexpr int SMALL_N = SMALL_THREADS * SMALL_ITEMS;
+static_assert(SMALL_ITEMS % 4 == 0, "runs are read as int4");
 
 __global__ void __launch_bounds__(SMALL_THREADS)
     k_small_scan(int32_t *__restrict__ in, int64_t n64, int32_t *__restrict__ out, ScanLimit lim) {
-  __shared__ int s_warp[SMALL_THREADS / 32];
-  __shared__ int s_total;
   const int n = (int)n64; // <= SMALL_N
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int seg = wid * (SMALL_ITEMS * 32);
+  const int base = threadIdx.x * SMALL_ITEMS;
+  // whole runs of 16-byte aligned arrays move as int4
+  const bool vec =
+      ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15u) == 0 &&
+      base + SMALL_ITEMS <= n;
   int v[SMALL_ITEMS];
+  if (vec) {
+    const int4 *p = reinterpret_cast<const int4 *>(in + base);
 #pragma unroll
-  for (int k = 0; k < SMALL_ITEMS; ++k) {
-    const int i = seg + k * 32 + lane;
-    v[k] = i < n ? in[i] : 0;
-  }
-  int carry = 0;
+    for (int k = 0; k < SMALL_ITEMS / 4; ++k) {
+      const int4 q = p[k];
+      v[4 * k] = q.x;
+      v[4 * k + 1] = q.y;
+      v[4 * k + 2] = q.z;
+      v[4 * k + 3] = q.w;
+    }
+  } else {
 #pragma unroll
-  for (int k = 0; k < SMALL_ITEMS; ++k) {
-    const int inc = warp_incl_scan(v[k]);
-    const int tot = __shfl_sync(0xffffffffu, inc, 31);
-    v[k] = carry + inc - v[k]; // exclusive prefix within the segment
-    carry += tot;
+    for (int k = 0; k < SMALL_ITEMS; ++k) v[k] = base + k < n ? in[base + k] : 0;
   }
-  if (lane == 0) s_warp[wid] = carry;
-  __syncthreads();
-  if (wid == 0) {
-    const int w = s_warp[lane];
-    const int inc = warp_incl_scan(w);
-    s_warp[lane] = inc - w;
-    if (lane == 31) s_total = inc;
+  int sum = 0;
+#pragma unroll
+  for (int k = 0; k < SMALL_ITEMS; ++k) { // exclusive prefix within the run
+    const int x = v[k];
+    v[k] = sum;
+    sum += x;
   }
-  __syncthreads();
-  const int off = s_warp[wid], total = s_total;
+  int total;
+  const int off = block_excl_scan<SMALL_THREADS>(sum, &total);
   // the same decision in every thread: the total is block-wide
   const bool over = lim.limit >= 0 && (int64_t)total > lim.limit;
   if (threadIdx.x == 0) {
@@ -103,12 +107,26 @@ __global__ void __launch_bounds__(SMALL_THREADS)
     if (over && lim.status) atomicOr(lim.status, lim.status_bit);
     if (lim.total) *lim.total = over ? 0 : total;
   }
+  if (vec) {
+    int4 *q = reinterpret_cast<int4 *>(out + base);
 #pragma unroll
-  for (int k = 0; k < SMALL_ITEMS; ++k) {
-    const int i = seg + k * 32 + lane;
-    if (i < n) {
-      out[i] = over ? 0 : off + v[k];
-      if (over) in[i] = 0; // every count and offset dropped
+    for (int k = 0; k < SMALL_ITEMS / 4; ++k)
+      q[k] = over ? make_int4(0, 0, 0, 0)
+                  : make_int4(off + v[4 * k], off + v[4 * k + 1], off + v[4 * k + 2],
+                              off + v[4 * k + 3]);
+    if (over) { // every count and offset dropped
+      int4 *c = reinterpret_cast<int4 *>(in + base);
+#pragma unroll
+      for (int k = 0; k < SMALL_ITEMS / 4; ++k) c[k] = make_int4(0, 0, 0, 0);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < SMALL_ITEMS; ++k) {
+      const int i = base + k;
+      if (i < n) {
+        out[i] = over ? 0 : off + v[k];
+        if (over) in[i] = 0;
+      }
     }
   }
 }

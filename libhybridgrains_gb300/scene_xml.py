@@ -22,7 +22,7 @@ list, ``inf``/``-inf`` accepted in lists, and time steps as exact rationals
 ("1 / 1000080", "0.000001") converted by one division. Elements that only
 drive the reference's viewers (camera, cairo_settings) or its Python hooks
 (scripting) are ignored. Features outside this library's path (box and
-annulus bodies, static drums, portals, cubic basis functions, other hybrid
+annulus bodies, portals, cubic basis functions, other hybrid
 integrator styles) raise ``SceneError`` naming the element, where the
 reference's parser would accept them.
 
@@ -328,7 +328,7 @@ def make_mpm(ctx, cfg, precision=None, capacity=0, points=None):
 
 # ---- rigidbody2d ------------------------------------------------------------------
 
-_DEM_UNSUPPORTED = ("planar_portal", "lees_edwards_portal", "static_drum")
+_DEM_UNSUPPORTED = ("planar_portal", "lees_edwards_portal")
 
 
 def read_dem(source):
@@ -378,6 +378,14 @@ def read_dem(source):
     d["gravity"] = tuple(g)
     # loadStaticPlanes (:219-270)
     d["planes"] = [(_list(nd, "x", 2), _list(nd, "n", 2)) for nd in root.findall("static_plane")]
+    # loadStaticDrums (:541-585): centre x and a positive radius r
+    d["drums"] = []
+    for nd in root.findall("static_drum"):
+        x = _list(nd, "x", 2)
+        r = _scalar(nd, "r")
+        if not r > 0.0:
+            raise SceneError("static_drum: r must be a positive scalar")
+        d["drums"].append((x, r))
     # loadGeometry (:610-725)
     geo = []
     for nd in root.findall("geometry"):
@@ -428,7 +436,8 @@ def make_dem(ctx, d, precision=None, capacity=0, contact_capacity=0):
     n = len(d["r"])
     obj = DEM(ctx, d["gravity"], d["kn"], d["kt"], d["gamman"], d["gammat"], d["mu"],
               d["planes"], cell_scale=d["cell_scale"], capacity=max(int(capacity), n),
-              contact_capacity=contact_capacity, precision=FP64 if precision is None else precision)
+              contact_capacity=contact_capacity, precision=FP64 if precision is None else precision,
+              drums=d.get("drums", ()))
     obj.upload(d["q"], d["v"], d["r"], d["m"], d["I"], d["fixed"])
     return obj
 

@@ -54,6 +54,7 @@ def _sig(lib):
                                  ctypes.c_double, ctypes.c_double]
     f.hgo_dem_destroy.argtypes = [_P]
     f.hgo_dem_add_plane.argtypes = [_P, _D, _D]
+    f.hgo_dem_add_drum.argtypes = [_P, _D, ctypes.c_double]
     f.hgo_dem_set_weights.argtypes = [_P, _D]
     f.hgo_dem_set_state.argtypes = [_P, _D, _D]
     f.hgo_dem_step.argtypes = [_P, ctypes.c_double, ctypes.c_int, ctypes.c_int]
@@ -261,6 +262,9 @@ class DEM:
 
     def add_plane(self, x, n):
         lib().hgo_dem_add_plane(self._h, _d(_f64(x)), _d(_f64(n)))
+
+    def add_drum(self, x, r):
+        lib().hgo_dem_add_drum(self._h, _d(_f64(x)), float(r))
 
     def set_weights(self, w):
         lib().hgo_dem_set_weights(self._h, _d(_f64(w)))

@@ -81,7 +81,7 @@ void getPotentialOverlaps(const std::vector<AABB> &aabbs, double h_scale,
   }
 }
 
-enum Kind { K_PLANE = 0, K_CC = 1, K_KIN = 2 };
+enum Kind { K_PLANE = 0, K_CC = 1, K_KIN = 2, K_DRUM = 3 };
 
 struct Constraint {
   int kind;
@@ -152,6 +152,27 @@ void computeActiveSet(const DemState &s, std::vector<Constraint> &out) {
       }
     }
   }
+  // computeBodyDrumActiveSetAllPairs (RigidBody2DSim.cpp:844-884)
+  for (int di = 0; di < (int)s.drums.size(); ++di) {
+    const DemDrum &dr = s.drums[di];
+    for (int b = 0; b < s.n; ++b) {
+      if (s.fixed[b]) continue;
+      // StaticDrumCircleConstraint::isActive (StaticDrumCircleConstraint.cpp:7-13)
+      const V2 d = sub(dr.x, qpos(s, b));
+      const double gap = dr.r - s.r[b];
+      if (sqnorm(d) >= gap * gap) {
+        Constraint c;
+        c.kind = K_DRUM;
+        c.i0 = b;
+        c.i1 = di;
+        c.n = {0, 0};
+        c.p = {0, 0};
+        c.ra = s.r[b];
+        c.rb = 0;
+        out.push_back(c);
+      }
+    }
+  }
 }
 
 inline V2 carryDeltaS(const Record *old, V2 vrel, V2 n, double dt) {
@@ -187,6 +208,27 @@ void updateCollisionCache(DemState &s, double dt, bool weighted) {
       const Record *old = s.cache.plane.find(c.i0, c.i1);
       rec.delta_s = carryDeltaS(old, rec.vrel, rec.n, dt);
       s.old_cache.plane.insert(c.i0, c.i1, rec);
+    } else if (c.kind == K_DRUM) {
+      const DemDrum &dr = s.drums[c.i1];
+      const V2 x = qpos(s, c.i0);
+      // StaticDrumCircleConstraint.cpp:100-159: the normal points from the
+      // disk's centre to the drum's, the contact point is the disk's point
+      // farthest from the drum's centre
+      const V2 n = normalized(sub(dr.x, x));
+      rec.contact_point = sub(x, scl(c.ra, n));
+      rec.weight = weighted ? s.w[c.i0] : 1.0;
+      rec.depth = std::min(0.0, -(norm(sub(dr.x, x)) - (dr.r - c.ra)));
+      rec.n = n;
+      rec.r0 = scl(-c.ra, n);
+      const V2 t0{-rec.r0.y, rec.r0.x};
+      // the static drum's collision point velocity is v + omega*t = 0
+      const V2 arm = sub(rec.contact_point, dr.x);
+      const V2 tp{-arm.y, arm.x};
+      const V2 vdrum{0.0 + 0.0 * tp.x, 0.0 + 0.0 * tp.y};
+      rec.vrel = sub(add(vlin(s, c.i0), scl(s.v[3 * c.i0 + 2], t0)), vdrum);
+      const Record *old = s.cache.drum.find(c.i0, c.i1);
+      rec.delta_s = carryDeltaS(old, rec.vrel, rec.n, dt);
+      s.old_cache.drum.insert(c.i0, c.i1, rec);
     } else if (c.kind == K_CC) {
       const V2 qa = qpos(s, c.i0), qb = qpos(s, c.i1);
       rec.contact_point = c.p;
@@ -269,6 +311,13 @@ V2 contactForce(const DemState &s, Record &rec) {
 void accumulateForces(DemState &s, std::vector<double> &F) {
   for (int b = 0; b < s.n; ++b) // circle vs plane
     for (auto &e : s.cache.plane.entries[b]) {
+      const V2 f = contactForce(s, e.second);
+      F[3 * b] += f.x;
+      F[3 * b + 1] += f.y;
+      F[3 * b + 2] += cross(e.second.r0, f);
+    }
+  for (int b = 0; b < s.n; ++b) // circle vs drum
+    for (auto &e : s.cache.drum.entries[b]) {
       const V2 f = contactForce(s, e.second);
       F[3 * b] += f.x;
       F[3 * b + 1] += f.y;
@@ -394,6 +443,10 @@ void hgo_dem_add_plane(void *h, const double *x, const double *n) {
       DemPlane{V2{x[0], x[1]}, normalized(V2{n[0], n[1]})});
 }
 
+void hgo_dem_add_drum(void *h, const double *x, double r) {
+  static_cast<DemState *>(h)->drums.push_back(DemDrum{V2{x[0], x[1]}, r});
+}
+
 void hgo_dem_set_weights(void *h, const double *w) {
   DemState &s = *static_cast<DemState *>(h);
   s.w.assign(w, w + s.n);
@@ -419,19 +472,26 @@ void hgo_dem_get_state(void *h, double *q, double *v) {
 
 int hgo_dem_record_width() { return REC_WIDTH; }
 
-// All cached contacts, ordered plane (body-major), circle-circle
-// (body-major), kinematic (body-major). Returns the count; writes at most cap.
+// All cached contacts: contacts with static objects (body-major; each
+// body's plane contacts, then its drum contacts), circle-circle
+// (body-major), kinematic (body-major), the order of the library's
+// export. Returns the count; writes at most cap.
 int hgo_dem_get_contacts(void *h, int cap, double *out) {
   DemState &s = *static_cast<DemState *>(h);
   int k = 0;
-  auto emit = [&](TypeCache &tc, int kind) {
-    for (int b = 0; b < s.n; ++b)
-      for (auto &e : tc.entries[b]) {
-        if (k < cap) packRecord(e.second, kind, b, e.first, out + REC_WIDTH * k);
-        ++k;
-      }
+  auto emit_body = [&](TypeCache &tc, int kind, int b) {
+    for (auto &e : tc.entries[b]) {
+      if (k < cap) packRecord(e.second, kind, b, e.first, out + REC_WIDTH * k);
+      ++k;
+    }
   };
-  emit(s.cache.plane, K_PLANE);
+  auto emit = [&](TypeCache &tc, int kind) {
+    for (int b = 0; b < s.n; ++b) emit_body(tc, kind, b);
+  };
+  for (int b = 0; b < s.n; ++b) {
+    emit_body(s.cache.plane, K_PLANE, b);
+    emit_body(s.cache.drum, K_DRUM, b);
+  }
   emit(s.cache.cc, K_CC);
   emit(s.cache.kin, K_KIN);
   return k;

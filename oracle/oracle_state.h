@@ -81,6 +81,11 @@ struct DemPlane { // rigidbody2d/RigidBody2DStaticPlane.h (static: v = 0, omega 
   V2 x, n;
 };
 
+struct DemDrum { // rigidbody2d/RigidBody2DStaticDrum.h:6-33 (static: v = 0, omega = 0)
+  V2 x;
+  double r;
+};
+
 // CollisionTypeCache (PenaltyImpactFrictionMap.h:167-273): one list per body.
 struct TypeCache {
   std::vector<std::vector<std::pair<int, Record>>> entries;
@@ -101,10 +106,11 @@ struct TypeCache {
   }
 };
 
-struct Cache {
-  TypeCache plane, cc, kin;
+struct Cache { // CollisionCache (PenaltyImpactFrictionMap.h): the circle kinds
+  TypeCache plane, drum, cc, kin;
   void reset(int n) {
     plane.reset(n);
+    drum.reset(n);
     cc.reset(n);
     kin.reset(n);
   }
@@ -115,6 +121,7 @@ struct DemState {
   std::vector<double> q, v, r, m0, I0, w, M, Minv; // M, Minv: 3 per body
   std::vector<unsigned char> fixed;
   std::vector<DemPlane> planes;
+  std::vector<DemDrum> drums;
   V2 g{0, 0};
   double kn = 0, kt = 0, gn = 0, gt = 0, mu = 0, cell_scale = 1.0;
   Cache cache, old_cache;

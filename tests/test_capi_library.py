@@ -44,15 +44,16 @@ def test_struct_layouts_match_header(lib):
     with tempfile.TemporaryDirectory() as d:
         src = os.path.join(d, "s.c")
         with open(src, "w") as f:
-            f.write('#include <stdio.h>\n#include "hg_gpu.h"\nint main(void){printf("%zu %zu %zu %zu",'
+            f.write('#include <stdio.h>\n#include "hg_gpu.h"\nint main(void){printf("%zu %zu %zu %zu %zu",'
                     ' sizeof(hg_mpm_desc), sizeof(hg_mpm_plane), sizeof(hg_dem_desc),'
-                    ' sizeof(hg_dem_plane)); return 0;}\n')
+                    ' sizeof(hg_dem_plane), sizeof(hg_dem_drum)); return 0;}\n')
         exe = os.path.join(d, "s")
         subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), src, "-o", exe], check=True)
         out = subprocess.run([exe], capture_output=True, text=True).stdout.split()
     sizes = list(map(int, out))
     assert sizes == [ctypes.sizeof(_capi.MpmDesc), ctypes.sizeof(_capi.MpmPlane),
-                     ctypes.sizeof(_capi.DemDesc), ctypes.sizeof(_capi.DemPlane)]
+                     ctypes.sizeof(_capi.DemDesc), ctypes.sizeof(_capi.DemPlane),
+                     ctypes.sizeof(_capi.DemDrum)]
 
 
 def test_status_strings(lib):

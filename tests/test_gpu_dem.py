@@ -270,3 +270,93 @@ def test_concurrent_stream_gives_the_same_steps(ctx):
     assert sa == 0 and sb == 0
     assert np.array_equal(fa, qa) and np.array_equal(fb, qb)  # frames landed by the fence
     assert np.array_equal(qa, qb) and np.array_equal(ca, cb)
+
+
+def drum_scene():
+    """Disks of the DEM column's lattice inside two static drums of radius
+    50 mm whose centres lie 2 mm apart (each drum is the nearer wall on one
+    side), above a floor plane that cuts the drums' bottom, moving outwards
+    at 2 m/s: contacts with both drums, with the floor and with each other,
+    several static objects per body near the bottom."""
+    c = np.array([0.05, 0.05])
+    c2 = c + np.array([0.002, 0.0])
+    sc = scenes.dem_column(n=2400, per_row=48, x0=0.0, y0=0.0)
+    xy = sc["q"][:, :2]
+    d1 = np.linalg.norm(xy - c, axis=1)
+    d2 = np.linalg.norm(xy - c2, axis=1)
+    # 1.05 mm below the lattice's seventh row (rows at 2.2 mm (1/2 + k sqrt(3)/2))
+    floor_y = 2.2e-3 * (0.5 + 6.0 * np.sqrt(3.0) / 2.0) - 1.05e-3
+    keep = (d1 <= 0.0495) & (d2 <= 0.0495) & (xy[:, 1] >= floor_y + 0.95e-3)
+    for k in ("q", "v", "r", "m", "I", "fixed"):
+        sc[k] = np.ascontiguousarray(sc[k][keep])
+    rel = sc["q"][:, :2] - c
+    sc["v"][:, :2] = 2.0 * rel / np.maximum(np.linalg.norm(rel, axis=1), 1e-12)[:, None]
+    drums = [(tuple(c), 0.05), (tuple(c2), 0.05)]
+    planes = [((0.0, floor_y), (0.0, 1.0))]
+    return sc, drums, planes
+
+
+@pytest.mark.parametrize("weighted", [False, True])
+def test_static_drums_bit_exact(ctx, weighted):
+    """StaticDrumCircleConstraint (StaticDrumCircleConstraint.cpp:7-159),
+    the drum branch of the collision cache and force loop
+    (PenaltyImpactFrictionMap.cpp:84-111, 361-401, 696-767) and the drum
+    active set (RigidBody2DSim.cpp:844-884), FP64 against the oracle."""
+    sc, drums, planes = drum_scene()
+    n = len(sc["r"])
+    assert n > 1000
+    p = scenes.dem_params()
+    g = hg.DEM(ctx, scenes.GRAVITY, p["kn"], p["kt"], p["gamman"], p["gammat"], p["mu"], planes,
+               capacity=n, contact_capacity=8 * n, drums=drums)
+    g.upload(sc["q"], sc["v"], sc["r"], sc["m"], sc["I"], sc["fixed"])
+    c = oracle.DEM(sc["q"], sc["v"], sc["r"], sc["m"], sc["I"], sc["fixed"], scenes.GRAVITY,
+                   p["kn"], p["kt"], p["gamman"], p["gammat"], p["mu"], 1.0)
+    for (x, nn) in planes:
+        c.add_plane(x, nn)
+    for (x, r) in drums:
+        c.add_drum(x, r)
+    if weighted:
+        w = np.where(np.arange(n) % 3 == 0, 0.5, 1.0)
+        g.set_weights(w)
+        c.set_weights(w)
+    for _ in range(3):
+        if weighted:
+            g.flow_with_weights(1e-6, 100)
+        else:
+            g.flow(1e-6, 100)
+        c.step(1e-6, 100, weighted=weighted)
+        Qg, Vg = g.download()
+        Qc, Vc = c.state()
+        assert np.array_equal(Qg, Qc)
+        assert np.array_equal(Vg, Vc)
+        Rg, Rc = g.contacts(), c.contacts()
+        assert Rg.shape == Rc.shape
+        assert np.array_equal(Rg, Rc)
+    kinds = Rc[:, 0]
+    assert (kinds == 0).any() and (kinds == 1).any()
+    drum_rows = Rc[kinds == 3]
+    assert set(drum_rows[:, 2].astype(int)) == {0, 1}
+    assert g.status() == 0
+
+
+def test_static_drums_mixed_precision_tracks_fp64(ctx):
+    sc, drums, planes = drum_scene()
+    n = len(sc["r"])
+    p = scenes.dem_params()
+    objs = []
+    for prec in (hg.FP64, hg.MIXED):
+        d = hg.DEM(ctx, scenes.GRAVITY, p["kn"], p["kt"], p["gamman"], p["gammat"], p["mu"],
+                   planes, capacity=n, contact_capacity=8 * n, drums=drums, precision=prec)
+        d.upload(sc["q"], sc["v"], sc["r"], sc["m"], sc["I"], sc["fixed"])
+        d.flow(1e-6, 10)
+        objs.append(d)
+    (qf, vf), (qm, vm) = objs[0].download(), objs[1].download()
+    Rf, Rm = objs[0].contacts(), objs[1].contacts()
+    assert np.array_equal(Rf[:, :3], Rm[:, :3])  # the same contacts
+    assert (Rf[:, 0] == 3).sum() > 10
+    assert np.abs(qf[:, :2] - qm[:, :2]).max() <= 1e-9
+    assert np.linalg.norm(vf - vm) / np.linalg.norm(vf) <= 1e-5
+    # the drum contacts' normal forces, FP32 against FP64
+    dr = Rf[:, 0] == 3
+    assert np.abs(Rm[dr, 17:19] - Rf[dr, 17:19]).max() <= 1e-5 * np.abs(Rf[dr, 17:19]).max()
+    assert objs[1].status() == 0

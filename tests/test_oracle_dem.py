@@ -104,3 +104,32 @@ def test_fixed_bodies_and_planes():
     assert np.array_equal(Q[:20], q0[:20])  # fixed bodies do not move
     kinds = d.contacts()[:, 0]
     assert (kinds == 2).any()  # kinematic circle-circle contacts exist
+
+
+def test_static_drum_contact_known_answer():
+    """StaticDrumCircleConstraint (StaticDrumCircleConstraint.cpp:7-159): a
+    disk at rest pressed 0.5 mm into the wall of a drum of radius 0.1 m is
+    pushed back towards the drum's centre by kn * 0.5 mm; a disk well inside
+    the drum and a fixed disk against the wall have no drum contact."""
+    kn = 1.0e5
+    r = np.array([0.01, 0.01, 0.01])
+    q = np.array([[0.0905, 0.0, 0.0], [0.0, 0.02, 0.0], [-0.0905, 0.0, 0.0]])
+    v = np.zeros((3, 3))
+    m = 2600.0 * math.pi * r * r
+    fixed = np.array([0, 0, 1], dtype=np.uint8)
+    d = oracle.DEM(q, v, r, m, 0.5 * m * r * r, fixed, (0.0, 0.0), kn, 0.0, 0.0, 0.0, 0.5, 1.0)
+    d.add_drum((0.0, 0.0), 0.1)
+    dt = 1e-6
+    d.step(dt, 1)
+    R = d.contacts()
+    assert len(R) == 1
+    kind, a, b, depth = R[0, :4]
+    assert (kind, a, b) == (3, 0, 0)
+    assert depth == pytest.approx(-5e-4, rel=1e-9)
+    assert R[0, 4:6].tolist() == [-1.0, 0.0]           # towards the drum's centre
+    assert R[0, 15:17] == pytest.approx([0.1005, 0.0])  # the disk's far point
+    assert R[0, 10:12] == pytest.approx([0.01, 0.0])    # lever arm -r n
+    assert R[0, 17:19] == pytest.approx([-kn * 5e-4, 0.0], rel=1e-9)
+    q1, v1 = d.state()
+    assert v1[0, 0] == pytest.approx(-dt * kn * 5e-4 / m[0], rel=1e-9)
+    assert np.array_equal(v1[1:], np.zeros((2, 3)))

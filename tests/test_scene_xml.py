@@ -96,6 +96,16 @@ def test_mpm_multiple_rectangles_in_file_order():
     assert p["hl"][-1] == 0.0025 and p["m"][-1] == 1000.0 * 0.005 * 0.005
 
 
+def test_dem_scene_static_drums():
+    # loadStaticDrums (RigidBody2DSceneParser.cpp:541-585)
+    d = sx.read_dem(DEM_XML.replace('<near_earth_gravity f="0.0 -9.0"/>',
+                                    '<near_earth_gravity f="0.0 -9.0"/>'
+                                    '<static_drum x="0.5 0.25" r="0.2"/>'
+                                    '<static_drum x="1 2" r="3 4"/>'))
+    assert d["drums"] == [((0.5, 0.25), 0.2), ((1.0, 2.0), 3.0)]
+    assert sx.read_dem(DEM_XML)["drums"] == []
+
+
 @pytest.mark.parametrize("old,new,msg", [
     ('<material shear_modulus="384615.4" bulk_modulus="833333.3" alpha="0.3266"/>', "",
      "material"),
@@ -162,7 +172,8 @@ def test_dem_scene_fields():
     ('geo_idx="2"', 'geo_idx="1"', "box bodies"),
     ('geo_idx="2"', 'geo_idx="5"', "out of range"),
     ('fixed="1"', 'fixed="2"', "boolean"),
-    ('<near_earth_gravity f="0.0 -9.0"/>', '<static_drum x="0 0" r="1"/>', "static_drum"),
+    ('<near_earth_gravity f="0.0 -9.0"/>', '<static_drum x="0 0" r="0"/>', "static_drum"),
+    ('<near_earth_gravity f="0.0 -9.0"/>', '<planar_portal/>', "planar_portal"),
     ('<penalty_impact_map dt="0.000001" kn="100000" gamman="0.5" kt="28571.4" gammat="0.5" '
      'mu="0.5"/>', "", "penalty_impact_map"),
     ('broadphase="spatial_grid"', 'broadphase="all_pairs"', "spatial_grid"),
