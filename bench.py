@@ -349,6 +349,9 @@ def run_ours(args, rank, world, local):
     hyb = None
     if args.hybrid_steps > 0:
         hyb = run_hybrid(args, ctx)
+    c0 = None
+    if args.c0_steps > 0 and world == 1:
+        c0 = run_column_12800(args, ctx)
 
     if rank != 0:
         return
@@ -412,6 +415,7 @@ def run_ours(args, rank, world, local):
         "serving": serve,
         "dem": dem,
         "hybrid": hyb,
+        "column_12800": c0,
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "status_word": status,
@@ -612,10 +616,80 @@ def run_hybrid(args, ctx):
 
     fp64 = run(hg.FP64)
     mixed = run(hg.MIXED)
+    cpu = None
+    if args.hybrid_cpu_steps > 0:
+        cpu = hybrid_cpu_baseline(args.hybrid_cpu_steps)
     return dict(fp64, workload="hybrid column: 100,000 MPM points (h 2.5 mm, uGIMP) under "
                                "20,000 disks, node-node coupling, homogenised stress and "
                                "velocity, resampling every 200 steps, dt 1e-6 s; top level: "
-                               "FP64 MPM bulk", mixed=mixed)
+                               "FP64 MPM bulk", mixed=mixed, cpu_baseline=cpu)
+
+
+def hybrid_cpu_baseline(steps):
+    """The oracle's node-node step (HybridGrains2DSim.cpp:116-220 restated in
+    FP64: MPM with OpenMP over the host cores, the penalty map serial as in
+    the reference) on the hybrid column's scene before its first resampling,
+    with the coupling band's grains weighted 1/2. The resampling interval is
+    host code on both sides (this library's is a restatement of the
+    reference's), so the baseline times the device-side step only."""
+    import oracle
+    from libhybridgrains_gb300 import scenes
+    scene = scenes.hybrid_column()
+    cfg, sc, dp = scene["mpm"], scene["dem"], scene["dem_params"]
+    p = scenes.seed_column_points(cfg)
+    threads = os.cpu_count() or 1
+    cm = oracle.MPM(cfg["grid_min"], cfg["grid_max"], cfg["h"], basis=1,
+                    shear_modulus=cfg["shear_modulus"], bulk_modulus=cfg["bulk_modulus"],
+                    dp_alpha=cfg["dp_alpha"], flip_alpha=cfg["flip_alpha"],
+                    gravity=scenes.GRAVITY, threads=threads)
+    for (x, n, st, lb) in cfg["planes"]:
+        cm.add_plane(x, n, st, lb)
+    cm.set_particles(p["q"], p["v"], p["m"], p["vol"], p["hl"])
+    cd = oracle.DEM(sc["q"], sc["v"], sc["r"], sc["m"], sc["I"], sc["fixed"], scenes.GRAVITY,
+                    dp["kn"], dp["kt"], dp["gamman"], dp["gammat"], dp["mu"], 1.0)
+    for (x, n, _st, _lb) in cfg["planes"]:
+        cd.add_plane(x, n)
+    cd.set_weights(np.where(sc["q"][:, 1] < cfg["rect_max"][1], 0.5, 1.0))
+    ch = oracle.Hybrid(cm, cd)
+    ch.step(cfg["dt"], 1, homogenize_stress=True, homogenize_velocity=True)
+    t0 = time.perf_counter()
+    ch.step(cfg["dt"], steps, homogenize_stress=True, homogenize_velocity=True)
+    secs = time.perf_counter() - t0
+    return {"value": steps / secs, "unit": "hybrid steps/s", "cores": threads, "kind": "port",
+            "sample": "%d node-node steps of the hybrid column, 100,000 points and 20,000 "
+                      "disks, before resampling (%.1f s)" % (steps, secs)}
+
+
+def run_column_12800(args, ctx):
+    """The 12,800-point MPM column (1.0 x 0.5 m domain, h = 5 mm, dt 1e-5 s)
+    on the GPU in mixed precision and FP64, and the oracle (FP64, OpenMP over
+    the host cores) on a sample of the same steps: particle-steps/s each."""
+    import libhybridgrains_gb300 as hg
+    import oracle
+    from libhybridgrains_gb300 import scenes
+    cfg = scenes.mpm_column("column_12800")
+    pts = scenes.seed_column_points(cfg)
+    n = len(pts["m"])
+    out = {"workload": "column_12800: 12,800-point MPM granular column, 200x100 grid, h=5 mm, "
+                       "dt=1e-5 s, sticking floor and walls", "particles": n,
+           "steps": args.c0_steps}
+    for name, prec in (("mixed", hg.MIXED), ("fp64", hg.FP64)):
+        m = make_mpm(ctx, cfg, prec, n)
+        m.upload(pts["q"], pts["v"], pts["m"], pts["vol"], pts["hl"])
+        m.flow(cfg["dt"], 20)
+        ctx.synchronize()
+        ctx.timer_begin()
+        m.flow(cfg["dt"], args.c0_steps)
+        ms = ctx.timer_end()
+        out[name] = {"value": n * args.c0_steps / (ms * 1e-3), "unit": UNIT,
+                     "ms_per_step": ms / args.c0_steps, "status": m.status()}
+        m.close()
+    threads = os.cpu_count() or 1
+    rate, secs = cpu_oracle_rate(cfg, pts, args.c0_cpu_steps, threads)
+    out["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                           "sample": "%d steps of the same column (%.1f s)"
+                                     % (args.c0_cpu_steps, secs)}
+    return out
 
 
 def gather_parts(part, world):
@@ -663,6 +737,8 @@ def run_serving(args, ctx, rank=0, world=1):
     alone = copies(reqs)
     barrier(world)
     alone_s = barrier_max(serving.run_one_at_a_time(ctx, alone), world)
+    cpu = serving_cpu_baseline(all_reqs, args) if (args.serve_cpu_requests > 0 and rank == 0) \
+        else None
     psteps = float(sum(r.npoints * r.steps for r in all_reqs))
     dsteps = float(sum(r.ndisks * r.steps for r in all_reqs))
     diff = barrier_max(max((serving.frame_diff(a[1], b[1])
@@ -693,8 +769,54 @@ def run_serving(args, ctx, rank=0, world=1):
                           "disk_steps_per_s": dsteps / alone_s,
                           "requests_per_s": len(all_reqs) / alone_s, "seconds": alone_s},
         "batched_over_one_at_a_time": saturated["particle_steps_per_s"] * alone_s / psteps,
+        "dem_precision": "mixed (FP32 contact law, FP64 positions and pair differences)",
+        "cpu_baseline": cpu,
         "max_frame_front_diff_m": diff,
     }
+
+
+def serving_cpu_baseline(reqs, args):
+    """The serving mix run one scene at a time on the CPU: the oracle (FP64;
+    the column with OpenMP over the host cores, its DEM pile serially, as the
+    reference runs them) steps each of the first few requests in arrival order
+    for a sample of its steps; a request's time is scaled to its full step
+    count. Reports requests/s and particle-steps/s of that sequential serving."""
+    import oracle
+    from libhybridgrains_gb300 import scenes, serving
+    threads = os.cpu_count() or 1
+    sample = sorted(reqs, key=lambda r: r.arrival)[:args.serve_cpu_requests]
+    total_s = 0.0
+    psteps = 0.0
+    for r in sample:
+        c = r.cfg
+        pts = scenes.seed_column_points(c)
+        o = oracle.MPM(c["grid_min"], c["grid_max"], c["h"], shear_modulus=c["shear_modulus"],
+                       bulk_modulus=c["bulk_modulus"], dp_alpha=c["dp_alpha"],
+                       flip_alpha=c["flip_alpha"], gravity=scenes.GRAVITY, threads=threads)
+        for (x, n, st, lb) in c["planes"]:
+            o.add_plane(x, n, st, lb)
+        o.set_particles(pts["q"], pts["v"], pts["m"], pts["vol"], pts["hl"])
+        od = None
+        if r.ndisks > 0:
+            pl = serving.dem_pile(r, 0)
+            dp = scenes.dem_params()
+            od = oracle.DEM(pl["q"], pl["v"], pl["r"], pl["m"], pl["I"], pl["fixed"],
+                            scenes.GRAVITY, dp["kn"], dp["kt"], dp["gamman"], dp["gammat"],
+                            dp["mu"], 1.0)
+            od.add_plane((0.0, 0.0), (0.0, 1.0))
+        k = min(args.serve_cpu_steps, r.steps)
+        t0 = time.perf_counter()
+        o.step(r.dt, k)
+        if od is not None:
+            od.step(r.dt, k)
+        total_s += (time.perf_counter() - t0) * r.steps / k
+        psteps += float(r.npoints) * r.steps
+    return {"value": len(sample) / total_s, "unit": "requests/s", "cores": threads,
+            "kind": "port", "particle_steps_per_s": psteps / total_s,
+            "sample": "the first %d requests in arrival order, %d of their steps each, scaled "
+                      "to their 2,000 steps (%.1f s of CPU work)"
+                      % (len(sample), args.serve_cpu_steps,
+                         total_s * args.serve_cpu_steps / 2000.0)}
 
 
 def main():
@@ -708,6 +830,11 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=10)
     ap.add_argument("--dem-steps", type=int, default=2000)
     ap.add_argument("--hybrid-steps", type=int, default=1000)
+    ap.add_argument("--hybrid-cpu-steps", type=int, default=20)
+    ap.add_argument("--c0-steps", type=int, default=1000)
+    ap.add_argument("--c0-cpu-steps", type=int, default=200)
+    ap.add_argument("--serve-cpu-requests", type=int, default=4)
+    ap.add_argument("--serve-cpu-steps", type=int, default=100)
     ap.add_argument("--dem-cpu-steps", type=int, default=200)
     ap.add_argument("--tune-steps", type=int, default=20)
     ap.add_argument("--roofline-span", type=int, default=10000)

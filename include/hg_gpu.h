@@ -263,12 +263,17 @@ hg_status hg_batch_profile_read(hg_batch *b, double *resort_ms, double *table_ms
  * update; 0 keeps the built-in choice (3 and 8). The autotuner times
  * HG_TUNE_CANDIDATES shapes on the live object with CUDA events, each for
  * steps_per_candidate steps (the scene advances by all of them: a shape only
- * changes the order of FP32 atomic sums), keeps the fastest for each kernel,
- * and records the result in a process-wide table under the object's size
+ * changes the order of FP32 atomic sums). A batch keeps the fastest shape for
+ * each kernel. A single scene then times the whole step, replayed as graphs
+ * in which the two kernels overlap, for every pair of a fused and an update
+ * shape (48 more steps each) and keeps the fastest pair. The result is
+ * recorded in a process-wide table under the object's size
  * class: the device's SM count, the tile count (single scenes) and the point
  * count, both rounded up to powers of two. MIXED objects and batches look up
  * their class before their first step. The table can be saved to and merged
- * from a text file. */
+ * from a text file. hg_mpm_autotune also records the object's step graphs
+ * for dt with the chosen shape (for both particle buffers), so that the
+ * steps after it replay them without capturing one on first use. */
 enum { HG_TUNE_CANDIDATES = 4 };
 typedef struct hg_launch_shape {
   int32_t fused_ctas_per_sm;
@@ -277,9 +282,14 @@ typedef struct hg_launch_shape {
 typedef struct hg_tune_report {
   int32_t candidates;
   hg_launch_shape tried[HG_TUNE_CANDIDATES];
-  double fused_ms[HG_TUNE_CANDIDATES];  /* mean per step */
-  double update_ms[HG_TUNE_CANDIDATES]; /* mean per step */
+  double fused_ms[HG_TUNE_CANDIDATES];  /* mean per step, per kernel */
+  double update_ms[HG_TUNE_CANDIDATES]; /* mean per step, per kernel */
   hg_launch_shape chosen;
+  /* single scenes: the whole step (graph replays, kernels overlapping as in
+   * production) with fused shape i and update shape j, mean per step; the
+   * chosen shape is the fastest pair. Batches: 0 (chosen per kernel). */
+  double step_ms[HG_TUNE_CANDIDATES][HG_TUNE_CANDIDATES];
+  int64_t steps; /* steps the object or every member advanced while tuning */
 } hg_tune_report;
 hg_status hg_mpm_autotune(hg_mpm *m, double dt, int32_t steps_per_candidate,
                           hg_tune_report *report);

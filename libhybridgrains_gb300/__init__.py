@@ -81,6 +81,8 @@ def _report(r):
                        for i in range(k)],
                 fused_ms=[r.fused_ms[i] for i in range(k)],
                 update_ms=[r.update_ms[i] for i in range(k)],
+                step_ms=[[r.step_ms[i][j] for j in range(k)] for i in range(k)],
+                steps=r.steps,
                 chosen=(r.chosen.fused_ctas_per_sm, r.chosen.update_ctas_per_sm))
 
 

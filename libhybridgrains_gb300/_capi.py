@@ -86,7 +86,9 @@ class LaunchShape(ctypes.Structure):
 class TuneReport(ctypes.Structure):
     _fields_ = [("candidates", ctypes.c_int32), ("tried", LaunchShape * HG_TUNE_CANDIDATES),
                 ("fused_ms", ctypes.c_double * HG_TUNE_CANDIDATES),
-                ("update_ms", ctypes.c_double * HG_TUNE_CANDIDATES), ("chosen", LaunchShape)]
+                ("update_ms", ctypes.c_double * HG_TUNE_CANDIDATES), ("chosen", LaunchShape),
+                ("step_ms", (ctypes.c_double * HG_TUNE_CANDIDATES) * HG_TUNE_CANDIDATES),
+                ("steps", ctypes.c_int64)]
 
 
 class DemDesc(ctypes.Structure):

@@ -315,6 +315,63 @@ __device__ __forceinline__ void credit(const PairArgs &A, int first, int second,
   if (slot < PW) A.plist[(int64_t)first * PW + slot] = (uint32_t)second | (kin ? 0x80000000u : 0u);
 }
 
+// cell c of the half neighbourhood: (0, 0), (1, 0), (-1, 1), (0, 1), (1, 1)
+__device__ __forceinline__ int half_dx(int c) { return c == 0 ? 0 : (c == 1 ? 1 : c - 3); }
+__device__ __forceinline__ int half_dy(int c) { return c >= 2 ? 1 : 0; }
+
+// One thread per body over its five cells: fewer loads of the body's own
+// record than kd_pairs_count when the bodies alone fill the GPU.
+__global__ void kd_pairs_count_body(PairArgs A) {
+  const int64_t n = A.n;
+  const int a = (int)(blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+  if (a >= n) return;
+  const float4 pa = A.rec[2 * a], ca = A.rec[2 * a + 1];
+  const uint32_t flags = __float_as_uint(pa.w);
+  const bool af = (flags & REL_FIXED) != 0u;
+  if (!af) A.cnt[a] = __popc(flags >> 1); // static planes
+  const int2 ha = make_int2(__float_as_int(ca.x), __float_as_int(ca.y));
+  const double xa = A.q[3 * a], ya = A.q[3 * a + 1], ra = A.r[a];
+  int bs[5], be[5];
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    const uint32_t bk = cell_hash(ha.x + half_dx(c), ha.y + half_dy(c), A.mask);
+    be[c] = A.bucket_end[bk];
+    bs[c] = be[c] - A.bucket_count[bk];
+  }
+  bool overflow = false;
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    const int dx = half_dx(c), dy = half_dy(c);
+    const int cx = ha.x + dx, cy = ha.y + dy;
+    for (int k = bs[c]; k < be[c]; ++k) {
+      if (!HG_INDEX_OK(k, n, A.status)) break;
+      const int b = A.items[k];
+      if (!HG_INDEX_OK(b, n, A.status)) continue;
+      if (b == a || (c == 0 && b < a)) continue;
+      const float4 pb = A.rec[2 * b], cb = A.rec[2 * b + 1];
+      if (__float_as_int(cb.x) != cx || __float_as_int(cb.y) != cy)
+        continue; // bucket shared by another cell
+      const bool bf = (__float_as_uint(pb.w) & REL_FIXED) != 0u;
+      if (af && bf) continue;
+      const float reach = pa.z + pb.z + A.tol;
+      const float ex = (float)dx * A.Hf + (pb.x - pa.x);
+      const float ey = (float)dy * A.Hf + (pb.y - pa.y);
+      if (ex * ex + ey * ey > reach * reach) continue;
+      const double xb = A.q[3 * b], yb = A.q[3 * b + 1], rb = A.r[b];
+      if (!((xa + ra >= xb - rb && ya + ra >= yb - rb) &&
+            (xb + rb >= xa - ra && yb + rb >= ya - ra)))
+        continue;
+      const double ddx = xa - xb, ddy = ya - yb;
+      const double c0 = (ddx * ddx + ddy * ddy) - (ra + rb) * (ra + rb);
+      if (!(c0 <= 0.0)) continue;
+      if (af) credit(A, b, a, true, overflow);
+      else if (bf) credit(A, a, b, true, overflow);
+      else credit(A, min(a, b), max(a, b), false, overflow);
+    }
+  }
+  if (overflow) atomicOr(A.status, (uint32_t)HG_STATUS_CELL_OVERFLOW);
+}
+
 // One thread per (body, cell of the half neighbourhood): thread t takes cell
 // t / n of body t % n, so a warp's lanes read consecutive bodies' records and
 // each thread follows one bucket instead of five.
@@ -328,9 +385,7 @@ __global__ void kd_pairs_count(PairArgs A) {
   const uint32_t flags = __float_as_uint(pa.w);
   const bool af = (flags & REL_FIXED) != 0u;
   if (c == 0 && !af) A.cnt[a] = __popc(flags >> 1); // static planes
-  // cell c of the half neighbourhood: (0, 0), (1, 0), (-1, 1), (0, 1), (1, 1)
-  const int dy = c >= 2 ? 1 : 0;
-  const int dx = c == 0 ? 0 : (c == 1 ? 1 : c - 3);
+  const int dx = half_dx(c), dy = half_dy(c);
   const int cx = __float_as_int(ca.x) + dx, cy = __float_as_int(ca.y) + dy;
   const uint32_t bk = cell_hash(cx, cy, A.mask);
   const int be = A.bucket_end[bk], bs = be - A.bucket_count[bk];
@@ -1102,7 +1157,13 @@ hg_status dem_step(hg_dem *d, double dt, int weighted) {
   A.status = d->status.p;
   A.pfill = d->pfill.p;
   // (per_body and pfill were zeroed by kd_bodies_home)
-  HG_LAUNCH(kd_pairs_count, blocks_for(5 * n, 128), 128, 0, s, A);
+  // Below about one body per thread slot of the GPU, five threads per body
+  // hide the bucket walks' latency; above it, one thread per body reads each
+  // body's record once.
+  if (n < (int64_t)d->ctx->num_sms * 1024)
+    HG_LAUNCH(kd_pairs_count, blocks_for(5 * n, 128), 128, 0, s, A);
+  else
+    HG_LAUNCH(kd_pairs_count_body, blocks_for(n, 128), 128, 0, s, A);
   HG_CHECK_LAUNCH();
   // offsets, the contact-capacity check (all contacts dropped when the list
   // would overflow) and the contact count

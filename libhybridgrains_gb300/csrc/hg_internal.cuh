@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <atomic>
+#include <utility>
 #include <string>
 #include <vector>
 
@@ -63,6 +64,40 @@ struct TraceRange {
     kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);               \
     ::hg::g_launches.fetch_add(1, std::memory_order_relaxed);                 \
   } while (0)
+
+// Programmatic dependent launch: the kernel's CTAs may be scheduled while the
+// previous kernel on the stream is finishing (in a captured graph the edge
+// becomes programmatic). Such a kernel calls pdl_wait() before its first
+// access to global memory, which returns once the previous kernel has
+// completed and its writes are visible, and pdl_trigger() to let the next
+// kernel be scheduled in turn. After a copy, a memset or an ordinary launch
+// the wait returns at once and the ordering is the stream's.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                              cudaStream_t stream, Args &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
+#define HG_LAUNCH_PDL(kernel, grid, block, smem, stream, ...)                 \
+  do {                                                                        \
+    ::hg::launch_pdl(kernel, (grid), (block), (smem), (stream), __VA_ARGS__); \
+    ::hg::g_launches.fetch_add(1, std::memory_order_relaxed);                 \
+  } while (0)
+
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
 
 #define HG_CHECK_LAUNCH()                                                     \
   do {                                                                        \

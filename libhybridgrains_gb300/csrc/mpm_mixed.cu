@@ -383,11 +383,13 @@ __device__ __forceinline__ void fused_tile(const MixedArgs &A, const int bin, Fu
       float fx, fy;
       split_u(u.x, cx, fx);
       split_u(u.y, cy, fy);
-      far_edge(A.nx, cx, fx);
-      far_edge(A.ny, cy, fy);
-      if (!in_grid_cell(A, cx, cy)) {
-        atomicOr(A.status, (uint32_t)HG_STATUS_OUT_OF_GRID);
-        continue;
+      if (!in_grid_cell(A, cx, cy)) { // the grid's far edge, or outside it
+        far_edge(A.nx, cx, fx);
+        far_edge(A.ny, cy, fy);
+        if (!in_grid_cell(A, cx, cy)) {
+          atomicOr(A.status, (uint32_t)HG_STATUS_OUT_OF_GRID);
+          continue;
+        }
       }
       int jh = fl & 1;
       int ncx = cx, ncy = cy;
@@ -482,18 +484,21 @@ __device__ __forceinline__ void fused_tile(const MixedArgs &A, const int bin, Fu
           // FP64 position decides)
           split_u(un.x, ncx, nfx);
           split_u(un.y, ncy, nfy);
+          far_edge(A.nx, ncx, nfx);
+          far_edge(A.ny, ncy, nfy);
         }
-        far_edge(A.nx, ncx, nfx);
-        far_edge(A.ny, ncy, nfy);
-        nonfinite |= !finite_d(un.x) | !finite_d(un.y) | !isfinite(vel.x + vel.y) |
-                     !isfinite(st.x);
+        // the position stays finite while its increments do (it was finite
+        // and inside the grid): one test covers position, velocity and J
+        nonfinite |= !isfinite((dux + duy) + (vel.x + vel.y) + st.x);
         A.u[p] = un;
         A.v[p] = vel;
         A.strain[p] = st;
         A.flags[p] = (uint8_t)((fl & ~1) | jh);
-        const int ngx = ncx - (X0 - DRIFT), ngy = ncy - (Y0 - DRIFT);
-        left_window += (ngx < 0) | (ngy < 0) | (ngx > VA_W - 2) | (ngy > VA_W - 2);
-        left_cell += (ncx != gcx) | (ncy != gcy);
+        if ((ncx != gcx) | (ncy != gcy)) { // a point in its sorted cell is in the window
+          const int ngx = ncx - (X0 - DRIFT), ngy = ncy - (Y0 - DRIFT);
+          left_window += (ngx < 0) | (ngy < 0) | (ngx > VA_W - 2) | (ngy > VA_W - 2);
+          ++left_cell;
+        }
       }
       if (!in_grid_cell(A, ncx, ncy)) {
         atomicOr(A.status, (uint32_t)HG_STATUS_OUT_OF_GRID);
@@ -578,6 +583,10 @@ __global__ void __launch_bounds__(THREADS, 3) kx_g2p2g(const __grid_constant__ M
   // the arguments stay in the constant bank: operands need no registers
   __shared__ FusedSmem S;
   zero_slow(S);
+  // launched with programmatic dependence on the grid update before it: only
+  // shared memory is touched before the wait
+  pdl_wait();
+  pdl_trigger();
   const int nact = *A.nactive;
   for (int t = blockIdx.x; t < nact; t += gridDim.x) {
     const int tile = A.active[t];
@@ -901,6 +910,9 @@ __device__ __forceinline__ void update_tile(const MixedArgs &A, const int tile) 
 }
 
 __global__ void __launch_bounds__(THREADS) kx_grid_update(const __grid_constant__ MixedArgs A) {
+  // launched with programmatic dependence on the fused kernel before it
+  pdl_wait();
+  pdl_trigger();
   const int nact = *A.nactive;
   for (int t = blockIdx.x; t < nact; t += gridDim.x) {
     const int tile = A.active[t];
@@ -1416,7 +1428,7 @@ void launch_particle_kernel(hg_mpm *m, const MixedArgs &A, cudaStream_t s) {
   if (m->p.basis == HG_BASIS_UGIMP) {
     HG_LAUNCH(kxu_step<PRIME>, ugimp_blocks(m), THREADS, 0, s, A);
   } else {
-    HG_LAUNCH(kx_g2p2g<PRIME>, fused_blocks(m), THREADS, fused_smem_bytes(), s, A);
+    HG_LAUNCH_PDL(kx_g2p2g<PRIME>, fused_blocks(m), THREADS, fused_smem_bytes(), s, A);
   }
 }
 int update_blocks(hg_mpm *m) { return m->ctx->num_sms * update_per_sm(m->shape); }
@@ -1623,7 +1635,7 @@ hg_status mixed_chunk_graph(hg_mpm *m, double dt) {
   HG_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   hg_status st = HG_OK;
   for (int k = 0; k < CHUNK_STEPS && st == HG_OK; ++k) {
-    HG_LAUNCH(kx_grid_update, update_blocks(m), THREADS, 0, s, At);
+    HG_LAUNCH_PDL(kx_grid_update, update_blocks(m), THREADS, 0, s, At);
     launch_particle_kernel<false>(m, Ab, s);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) st = cuda_fail(e, "kernel launch");
@@ -1694,7 +1706,7 @@ hg_status mixed_step(hg_mpm *m, double dt, int nsteps) {
       HG_CUDA_TRY(cudaEventRecord(ev[0], s));
     }
     MixedArgs At = make_args(m, dt, true);
-    HG_LAUNCH(kx_grid_update, update_blocks(m), THREADS, 0, s, At);
+    HG_LAUNCH_PDL(kx_grid_update, update_blocks(m), THREADS, 0, s, At);
     HG_CHECK_LAUNCH();
     if (m->profile) HG_CUDA_TRY(cudaEventRecord(ev[1], s));
     MixedArgs Ab = make_args(m, dt, false);
@@ -1728,7 +1740,7 @@ hg_status mixed_step_begin(hg_mpm *m) {
 
 hg_status mixed_grid_update(hg_mpm *m, double dt) {
   MixedArgs A = make_args(m, dt, true);
-  HG_LAUNCH(kx_grid_update, update_blocks(m), THREADS, 0, m->ctx->stream, A);
+  HG_LAUNCH_PDL(kx_grid_update, update_blocks(m), THREADS, 0, m->ctx->stream, A);
   HG_CHECK_LAUNCH();
   return HG_OK;
 }
@@ -2023,17 +2035,62 @@ hg_status mixed_autotune(hg_mpm *m, double dt, int steps, hg_tune_report *report
     r.fused_ms[i] = n > 0 ? g2p2g / n : std::numeric_limits<double>::infinity();
     r.update_ms[i] = n > 0 ? update / n : std::numeric_limits<double>::infinity();
   }
-  m->profile = prof0;
+  m->profile = false;
   m->prof_used = 0;
+  r.steps = (int64_t)HG_TUNE_CANDIDATES * (1 + steps);
+  // The whole step for every pair of a fused and an update shape, replayed
+  // as graphs like the production steps (where the two kernels overlap under
+  // programmatic dependent launch, which per-kernel events do not see): one
+  // chunk captures and warms the pair's graph, two chunks are timed.
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (st == HG_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
+    st = fail(HG_ERR_CUDA, "cudaEventCreate");
+  int bi = 0, bj = 0;
+  cudaStream_t s = m->ctx->stream;
+  for (int i = 0; i < HG_TUNE_CANDIDATES && st == HG_OK; ++i)
+    for (int j = 0; j < HG_TUNE_CANDIDATES && st == HG_OK; ++j) {
+      m->shape = hg_launch_shape{TUNE_CANDIDATES[i].fused_ctas_per_sm,
+                                 TUNE_CANDIDATES[j].update_ctas_per_sm};
+      st = mixed_step(m, dt, CHUNK_STEPS);
+      if (st != HG_OK) break;
+      float ms = 0.0f;
+      cudaError_t e = cudaEventRecord(e0, s);
+      if (e == cudaSuccess) st = mixed_step(m, dt, 2 * CHUNK_STEPS);
+      if (e == cudaSuccess && st == HG_OK) e = cudaEventRecord(e1, s);
+      if (e == cudaSuccess && st == HG_OK) e = cudaEventSynchronize(e1);
+      if (e == cudaSuccess && st == HG_OK) e = cudaEventElapsedTime(&ms, e0, e1);
+      if (e != cudaSuccess && st == HG_OK) st = cuda_fail(e, "autotune timing");
+      r.step_ms[i][j] = (double)ms / (2 * CHUNK_STEPS);
+      r.steps += 3 * CHUNK_STEPS;
+      if (r.step_ms[i][j] < r.step_ms[bi][bj]) {
+        bi = i;
+        bj = j;
+      }
+    }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  m->profile = prof0;
   if (st != HG_OK) {
     m->shape = hg_launch_shape{0, 0};
     return st;
   }
-  pick(r);
+  r.chosen = hg_launch_shape{TUNE_CANDIDATES[bi].fused_ctas_per_sm,
+                             TUNE_CANDIDATES[bj].update_ctas_per_sm};
   m->shape = r.chosen;
   m->shape_set = true;
   tune_store(mixed_key(m), r.chosen);
   if (report) *report = r;
+  // the step graphs of both particle buffers for the chosen shape and this
+  // dt, so that later steps replay them instead of capturing one on first
+  // use (capture only records the launches: the buffer swap is undone)
+  for (int k = 0; k < 2; ++k) {
+    st = mixed_chunk_graph(m, dt);
+    m->cur ^= 1;
+    if (st != HG_OK) {
+      if (k == 0) m->cur ^= 1;
+      return st;
+    }
+  }
   return HG_OK;
 }
 
@@ -2068,6 +2125,7 @@ hg_status batch_autotune(hg_batch *b, int steps, hg_tune_report *report) {
     b->shape_class = -1;
     return st;
   }
+  r.steps = (int64_t)HG_TUNE_CANDIDATES * (1 + steps);
   pick(r);
   b->shape = r.chosen;
   b->shape_class = batch_key(b, points)[3];

@@ -510,15 +510,25 @@ void grain_quantities(hg_resampler &R, int64_t before, int64_t after, int64_t po
   }
 }
 
-// Mass-weighted node field of the first n points (Grid::rasterizeMass +
-// rasterizeMassWeightedValues* + normalizationByMass, Grid.cpp:148-348).
-void mass_weighted_field(const hg_resampler &R, int64_t n, int len, const std::vector<double> &vals,
-                         const double *dflt, std::vector<double> &out) {
+// Mass-weighted node fields of the first n points (Grid::rasterizeMass +
+// rasterizeMassWeightedValues* + normalizationByMass, Grid.cpp:148-348) for
+// J, velocity and be_bar together: the reference builds each field in a pass
+// of its own with the same stencils, weights and node mass; one pass over
+// the points accumulates every field in the same per-node order, so each
+// sum is bit for bit the separate pass's.
+struct NodeField {
+  int len;
+  const std::vector<double> *vals;
+  const double *dflt;
+  std::vector<double> *out;
+};
+
+void mass_weighted_fields(const hg_resampler &R, int64_t n, NodeField *f, int nf) {
   const hg_zones_desc &zd = R.d.zones;
   const int nx = zd.mpm_cells[0], ny = zd.mpm_cells[1];
   const size_t nn = (size_t)(nx + 1) * (ny + 1);
   std::vector<double> mass(nn, 0.0);
-  out.assign(nn * len, 0.0);
+  for (int k = 0; k < nf; ++k) f[k].out->assign(nn * f[k].len, 0.0);
   const double h1 = R.hl.empty() ? 0.0 : R.hl[0];
   for (int64_t p = 0; p < n; ++p) {
     const double x = R.q[2 * p], y = R.q[2 * p + 1];
@@ -532,14 +542,23 @@ void mass_weighted_field(const hg_resampler &R, int64_t n, int len, const std::v
                                         zd.mpm_grid_min[1], R.grid_h);
         const size_t node = (size_t)iy * (nx + 1) + ix;
         mass[node] += wgt * R.m[p];
-        for (int c = 0; c < len; ++c) out[node * len + c] += wgt * R.m[p] * vals[(size_t)p * len + c];
+        for (int k = 0; k < nf; ++k) {
+          const int len = f[k].len;
+          const double *v = f[k].vals->data() + (size_t)p * len;
+          double *o = f[k].out->data() + node * len;
+          for (int c = 0; c < len; ++c) o[c] += wgt * R.m[p] * v[c];
+        }
       }
   }
-  for (size_t node = 0; node < nn; ++node) {
-    if (mass[node] > 0.0) {
-      for (int c = 0; c < len; ++c) out[node * len + c] /= mass[node];
-    } else {
-      for (int c = 0; c < len; ++c) out[node * len + c] = dflt[c];
+  for (int k = 0; k < nf; ++k) {
+    const int len = f[k].len;
+    double *o = f[k].out->data();
+    for (size_t node = 0; node < nn; ++node) {
+      if (mass[node] > 0.0) {
+        for (int c = 0; c < len; ++c) o[node * len + c] /= mass[node];
+      } else {
+        for (int c = 0; c < len; ++c) o[node * len + c] = f[k].dflt[c];
+      }
     }
   }
 }
@@ -551,9 +570,8 @@ void inner_point_quantities(hg_resampler &R, int64_t before, int64_t after, cons
   const hg_zones_desc &zd = R.d.zones;
   std::vector<double> fJ, fv, fb;
   const double dJ[1] = {1.0}, dv[2] = {0.0, 0.0}, db[4] = {1.0, 0.0, 0.0, 1.0};
-  mass_weighted_field(R, before, 1, R.J, dJ, fJ);
-  mass_weighted_field(R, before, 2, R.v, dv, fv);
-  mass_weighted_field(R, before, 4, R.be, db, fb);
+  NodeField fields[3] = {{1, &R.J, dJ, &fJ}, {2, &R.v, dv, &fv}, {4, &R.be, db, &fb}};
+  mass_weighted_fields(R, before, fields, 3);
   const double size = R.d.initial_particle_size;
   const double sigma = 0.5 * size, rr = 2.0 * size;
   for (int64_t i = before; i < after; ++i) { // gatherMassAndVolume

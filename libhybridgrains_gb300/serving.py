@@ -108,14 +108,17 @@ def dem_pile(req, lane):
                              x0=lane * LANE)
 
 
-def dem_for_piles(ctx, capacity):
+def dem_for_piles(ctx, capacity, precision=None):
     """A DEM object for piles: the penalty parameters of the DEM column and
-    the floor (y = 0) as the only plane."""
-    from . import DEM
+    the floor (y = 0) as the only plane; the contact law in mixed precision
+    (FP32 with FP64 positions and pair differences) unless precision says
+    otherwise."""
+    from . import DEM, MIXED
     p = scenes.dem_params()
     return DEM(ctx, scenes.GRAVITY, p["kn"], p["kt"], p["gamman"], p["gammat"], p["mu"],
                [((0.0, 0.0), (0.0, 1.0))], capacity=capacity,
-               contact_capacity=4 * max(capacity, 1))
+               contact_capacity=4 * max(capacity, 1),
+               precision=MIXED if precision is None else precision)
 
 
 def frame_diff(a, b):
@@ -318,7 +321,7 @@ class DeviceBackend(Backend):
     piles in one DEM object of ``dem_capacity`` bodies (a fixed pool outside
     the HBM budget; a request waits while its pile does not fit)."""
 
-    def __init__(self, ctx, max_members=256, depth=3, dem_capacity=1 << 21):
+    def __init__(self, ctx, max_members=256, depth=3, dem_capacity=1 << 21, dem_precision=None):
         from . import Batch  # noqa: WPS433 (package import cycle)
         self.ctx = ctx
         self.batch = Batch(ctx, max_members)
@@ -329,6 +332,7 @@ class DeviceBackend(Backend):
         # DEM piles
         self.dem = None
         self.dem_capacity = int(dem_capacity)
+        self.dem_precision = dem_precision
         self.dem_dt = None
         self.free_lanes = list(range(max_members - 1, -1, -1))  # pop() gives the lowest
         self.order = []        # requests with disks in the DEM object, in body order
@@ -391,7 +395,7 @@ class DeviceBackend(Backend):
     def _edit_piles(self):
         """One DEM edit: drop the piles that left, append the opened ones."""
         if self.dem is None:
-            self.dem = dem_for_piles(self.ctx, self.dem_capacity)
+            self.dem = dem_for_piles(self.ctx, self.dem_capacity, self.dem_precision)
             # the piles step on a stream of their own, beside the MPM batch
             self.dem.set_concurrent(True)
         n_old = sum(r.ndisks for r in self.order)
@@ -498,7 +502,7 @@ class DeviceBackend(Backend):
             self.dem.close()
 
 
-def run_one_at_a_time(ctx, requests):
+def run_one_at_a_time(ctx, requests, dem_precision=None):
     """The same requests served one after another, each scene alone
     (hg_mpm_step and, with disks, hg_dem_step of its own DEM object per frame
     interval, frames read synchronously); returns wall seconds."""
@@ -513,7 +517,7 @@ def run_one_at_a_time(ctx, requests):
         d = None
         if r.ndisks > 0:
             p = dem_pile(r, 0)
-            d = dem_for_piles(ctx, r.ndisks)
+            d = dem_for_piles(ctx, r.ndisks, dem_precision)
             d.upload(p["q"], p["v"], p["r"], p["m"], p["I"], p["fixed"])
         q = np.zeros((r.npoints, 2))
         for k in range(r.steps // r.frame_every):

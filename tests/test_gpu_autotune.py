@@ -1,8 +1,9 @@
 """Launch-shape autotuning of the MIXED kernels on the GPU.
 
-* the tuner times every candidate shape with CUDA events and keeps, per
-  kernel, the fastest; the choice is recorded under the scene's size class
-  and a later scene of the same class starts with it;
+* the tuner times every candidate shape per kernel with CUDA events, then
+  every pair of a fused and an update shape on whole graph-replayed steps,
+  and keeps the fastest pair; the choice is recorded under the scene's size
+  class and a later scene of the same class starts with it;
 * a shape changes only the order of FP32 atomic sums: a tuned scene follows
   an untuned twin stepped the same number of steps within 1e-9 m;
 * the batched kernels are tuned the same way.
@@ -35,12 +36,16 @@ def test_autotune_picks_the_fastest_and_records_it(ctx):
     assert len(r["tried"]) == 4
     for k in ("fused_ms", "update_ms"):
         assert all(np.isfinite(t) and t > 0 for t in r[k])
-    fi = int(np.argmin(r["fused_ms"]))
-    ui = int(np.argmin(r["update_ms"]))
-    assert r["chosen"] == (r["tried"][fi][0], r["tried"][ui][1])
+    # the fastest pair of shapes on whole graph-replayed steps
+    sm = np.array(r["step_ms"])
+    assert sm.shape == (4, 4) and np.isfinite(sm).all() and (sm > 0).all()
+    i, j = np.unravel_index(int(np.argmin(sm)), sm.shape)
+    assert r["chosen"] == (r["tried"][i][0], r["tried"][j][1])
     assert a.launch_shape() == r["chosen"]
-    # 4 candidates x (1 untimed + 10 timed) steps; the twin keeps the default
-    b.flow(cfg["dt"], 44)
+    # 4 candidates x (1 untimed + 10 timed) steps per kernel, then 16 pairs x
+    # 3 graph chunks of 16 steps; the twin keeps the default
+    assert r["steps"] == 4 * 11 + 16 * 48
+    b.flow(cfg["dt"], r["steps"])
     assert np.abs(a.download()["q"] - b.download()["q"]).max() <= 1e-9
     assert a.status() == 0 and b.status() == 0
     # a new scene of the same size class starts with the recorded shape
@@ -67,6 +72,7 @@ def test_batch_autotune(ctx):
         ms.append(m)
     r = batch.autotune(5)
     assert len(r["tried"]) == 4 and all(t > 0 for t in r["fused_ms"])
+    assert r["steps"] == 4 * 6
     assert batch.launch_shape() == r["chosen"]
     batch.step(40)
     assert all(m.status() == 0 for m in ms)

@@ -6,7 +6,8 @@
   object really holds after upload and downloads, within 10% + 1 MiB;
 * continuous batching: every request's frames (the column's front and its
   DEM pile's front per 100 steps) equal those of the same scene served alone
-  within 1e-9 m. For the columns FP32 atomic summation order is the only
+  within 1e-9 m, with the piles' contact law in mixed precision (the
+  serving default) and in FP64. For the columns FP32 atomic summation order is the only
   difference; the piles share one DEM object in the mix, shifted by their
   lane, where alone each sits at x = 0, so their FP64 positions round
   differently.
@@ -98,17 +99,18 @@ def test_estimate_bounds_device_bytes(ctx):
     m.close()
 
 
-def test_serving_results_match_scenes_served_alone(ctx):
+@pytest.mark.parametrize("dem_precision", [hg.MIXED, hg.FP64])
+def test_serving_results_match_scenes_served_alone(ctx, dem_precision):
     reqs = serving.column_requests(n=6, rate=400.0, seed=11, steps=300, nmax=3.0e4)
     for r, t in zip(reqs, (0.0, 0.0, 0.0, 0.002, 0.004, 0.006)):
         r.arrival = t  # three at once, three while those run
     assert sum(r.ndisks > 0 for r in reqs) >= 4
     alone = [r.copy() for r in reqs]
-    be = serving.DeviceBackend(ctx, max_members=8)
+    be = serving.DeviceBackend(ctx, max_members=8, dem_precision=dem_precision)
     srv = serving.Server(be, 2**33, max_members=8)
     srv.run(reqs)
     be.shutdown()
-    serving.run_one_at_a_time(ctx, alone)
+    serving.run_one_at_a_time(ctx, alone, dem_precision=dem_precision)
     assert srv.peak_members >= 2  # they overlapped on the device
     for a, b in zip(reqs, alone):
         assert [s for s, _ in a.frames] == [100, 200, 300]
