@@ -4,7 +4,9 @@
 // Compiled with --fmad=false. Grain-to-grid scatters use FP64 atomics (sums
 // differ from the serial reference in order only); the packed grain and node
 // lists are built with a scan, so they keep the reference's stable-partition
-// order (Coupling.cpp:113-127).
+// order (Coupling.cpp:113-127). With a MIXED (FP32) MPM bulk the grains' and
+// contacts' stencil weights are FP32 (for_stencil_weights32) over the same
+// FP64 stencils; the grids and the exchange stay FP64.
 //
 // Kernels:
 //   kc_grain_mass     rasterizeGrainMass (Coupling.cpp:22-140)
@@ -30,10 +32,22 @@ namespace {
 struct GridGeom {
   int basis, nx, ny;
   double gx, gy, h;
+  double inv_h;
 };
 
 GridGeom geom(const hg_mpm *m) {
-  return GridGeom{m->p.basis, m->p.nx, m->p.ny, m->p.gmin[0], m->p.gmin[1], m->p.h};
+  return GridGeom{m->p.basis, m->p.nx, m->p.ny, m->p.gmin[0], m->p.gmin[1], m->p.h, m->p.inv_h};
+}
+
+// The grid weights of a grain's or contact's stencil: FP32 (W32, for a MIXED
+// bulk) or FP64 in the reference's operation order (an FP64 bulk).
+template <bool W32, class F>
+__device__ __forceinline__ void stencil_weights(const GridGeom &G, double x, double y, double hl,
+                                                int x0, int y0, int x1, int y1, F &&f) {
+  if (W32)
+    for_stencil_weights32(G.basis, x, y, hl, x0, y0, x1, y1, G.gx, G.gy, G.h, G.inv_h, f);
+  else
+    for_stencil_weights(G.basis, x, y, hl, x0, y0, x1, y1, G.gx, G.gy, G.h, f);
 }
 
 __device__ __forceinline__ bool node_ok(const GridGeom &G, int ix, int iy) {
@@ -65,7 +79,7 @@ __global__ void kc_grain_mass(GridGeom G, int64_t nb, const double *__restrict__
   if (!all_pos) return;
   coupled[b] = 1;
   const double pm = m0[b] * w[b]; // RigidBody2DState::getTotalMass
-  for_stencil_weights(G.basis, x, y, hl, x0, y0, x1, y1, G.gx, G.gy, G.h,
+  stencil_weights<sizeof(M) == sizeof(float)>(G, x, y, hl, x0, y0, x1, y1,
                       [&](int ix, int iy, double wt) {
                         if (!node_ok(G, ix, iy)) return;
                         atomicAdd(&dem_mass[(int64_t)iy * (G.nx + 1) + ix], wt * pm);
@@ -90,6 +104,7 @@ __global__ void kc_pack(int64_t n, const int32_t *__restrict__ flag,
   if (flag[i]) out[pos[i]] = (int32_t)i;
 }
 
+template <bool W32>
 __global__ void kc_grain_mom(GridGeom G, const int32_t *__restrict__ count,
                              const int32_t *__restrict__ packed, const double *__restrict__ pos,
                              const double *__restrict__ hl0, const uint8_t *__restrict__ fixed,
@@ -106,7 +121,7 @@ __global__ void kc_grain_mom(GridGeom G, const int32_t *__restrict__ count,
     stencil64(G.basis, x, y, hl, G.gx, G.gy, G.h, x0, y0, x1, y1);
     const double pm = m0[b] * w[b];
     const double px = pm * v[3 * b], py = pm * v[3 * b + 1];
-    for_stencil_weights(G.basis, x, y, hl, x0, y0, x1, y1, G.gx, G.gy, G.h,
+    stencil_weights<W32>(G, x, y, hl, x0, y0, x1, y1,
                         [&](int ix, int iy, double wt) {
                           if (!node_ok(G, ix, iy)) return;
                           const int64_t i = (int64_t)iy * (G.nx + 1) + ix;
@@ -192,6 +207,7 @@ __global__ void kc_fill(double *dst, int64_t n, double v) {
   if (i < n) dst[i] = v;
 }
 
+template <bool W32>
 __global__ void kc_transfer(GridGeom G, const int32_t *__restrict__ count,
                             const int32_t *__restrict__ packed, const double *__restrict__ pos,
                             const double *__restrict__ hl0, const uint8_t *__restrict__ fixed,
@@ -208,7 +224,7 @@ __global__ void kc_transfer(GridGeom G, const int32_t *__restrict__ count,
     int x0, y0, x1, y1;
     stencil64(G.basis, x, y, hl, G.gx, G.gy, G.h, x0, y0, x1, y1);
     double vpx = 0.0, vpy = 0.0, atx = 0.0, aty = 0.0;
-    for_stencil_weights(G.basis, x, y, hl, x0, y0, x1, y1, G.gx, G.gy, G.h,
+    stencil_weights<W32>(G, x, y, hl, x0, y0, x1, y1,
                         [&](int ix, int iy, double wt) {
                           if (!node_ok(G, ix, iy)) return;
                           const int64_t i = (int64_t)iy * (G.nx + 1) + ix;
@@ -235,6 +251,7 @@ __global__ void kc_advect(double dt, const int32_t *__restrict__ count,
   }
 }
 
+template <bool W32>
 __global__ void kc_hstress(GridGeom G, int64_t nb, const int32_t *__restrict__ off,
                            const double *__restrict__ rec, const double *__restrict__ q,
                            double *hs) {
@@ -257,7 +274,7 @@ __global__ void kc_hstress(GridGeom G, int64_t nb, const int32_t *__restrict__ o
     const double s11 = -0.5 * (fy * ry + ry * fy);
     int x0, y0, x1, y1;
     stencil64(G.basis, px, py, hl, G.gx, G.gy, G.h, x0, y0, x1, y1);
-    for_stencil_weights(G.basis, px, py, hl, x0, y0, x1, y1, G.gx, G.gy, G.h,
+    stencil_weights<W32>(G, px, py, hl, x0, y0, x1, y1,
                         [&](int ix, int iy, double wt) {
                           if (!node_ok(G, ix, iy)) return;
                           const int64_t i = (int64_t)iy * (G.nx + 1) + ix;
@@ -269,6 +286,7 @@ __global__ void kc_hstress(GridGeom G, int64_t nb, const int32_t *__restrict__ o
   }
 }
 
+template <bool W32>
 __global__ void kc_hvel_scatter(GridGeom G, int64_t nb, const double *__restrict__ q,
                                 const double *__restrict__ v, const uint8_t *__restrict__ fixed,
                                 const double *__restrict__ m0, const double *__restrict__ w,
@@ -281,7 +299,7 @@ __global__ void kc_hvel_scatter(GridGeom G, int64_t nb, const double *__restrict
   const double x = q[3 * b], y = q[3 * b + 1];
   int x0, y0, x1, y1;
   stencil64(G.basis, x, y, hl, G.gx, G.gy, G.h, x0, y0, x1, y1);
-  for_stencil_weights(G.basis, x, y, hl, x0, y0, x1, y1, G.gx, G.gy, G.h,
+  stencil_weights<W32>(G, x, y, hl, x0, y0, x1, y1,
                       [&](int ix, int iy, double wt) {
                         if (!node_ok(G, ix, iy)) return;
                         const int64_t i = (int64_t)iy * (G.nx + 1) + ix;
@@ -348,7 +366,11 @@ hg_status hybrid_clear_homogenized(hg_hybrid *h) {
   return HG_OK;
 }
 
-hg_status hybrid_step(hg_hybrid *h, double dt, int flags) {
+namespace {
+
+// W32: the stencil weights of the coupling kernels in FP32 (a MIXED bulk)
+template <bool W32>
+hg_status hybrid_step_impl(hg_hybrid *h, double dt, int flags) {
   hg_mpm *m = h->m;
   hg_dem *d = h->d;
   cudaStream_t s = h->ctx->stream;
@@ -411,7 +433,7 @@ hg_status hybrid_step(hg_hybrid *h, double dt, int flags) {
   if ((st = mixed ? mixed_grid_update(m, dt) : mpm64_phase1(m, dt))) return st;
   // rasterizeGrainMom
   HG_CUDA_TRY(cudaMemsetAsync(h->dem_mom.p, 0, sizeof(double) * 2 * nn, s));
-  HG_LAUNCH(kc_grain_mom, gs, 128, 0, s, G, h->counts.p, h->packed_dem.p, h->pos_before.p,
+  HG_LAUNCH(kc_grain_mom<W32>, gs, 128, 0, s, G, h->counts.p, h->packed_dem.p, h->pos_before.p,
             hl0, d->fixed.p, d->m0.p, d->w.p, d->v.p, h->dem_mom.p);
   HG_CHECK_LAUNCH();
   // updateVelocitiesOnGrid
@@ -432,7 +454,7 @@ hg_status hybrid_step(hg_hybrid *h, double dt, int flags) {
               h->dem_mass.p, m->g_homog.p);
   }
   HG_CHECK_LAUNCH();
-  HG_LAUNCH(kc_transfer, gs, 128, 0, s, G, h->counts.p, h->packed_dem.p, h->pos_before.p,
+  HG_LAUNCH(kc_transfer<W32>, gs, 128, 0, s, G, h->counts.p, h->packed_dem.p, h->pos_before.p,
             hl0, d->fixed.p, h->v_after.p, h->a_after.p, d->v.p);
   HG_CHECK_LAUNCH();
   if ((st = mixed ? mixed_particles(m, dt) : mpm64_phase2(m, dt))) return st;
@@ -440,14 +462,14 @@ hg_status hybrid_step(hg_hybrid *h, double dt, int flags) {
             d->q.p);
   HG_CHECK_LAUNCH();
   if ((flags & HG_HYBRID_HOMOGENIZE_STRESS) && nb > 0) {
-    HG_LAUNCH(kc_hstress, gs, 128, 0, s, G, nb, d->per_body_off.p, d->crec[d->cc].p, d->q.p,
+    HG_LAUNCH(kc_hstress<W32>, gs, 128, 0, s, G, nb, d->per_body_off.p, d->crec[d->cc].p, d->q.p,
               h->hstress.p);
     HG_CHECK_LAUNCH();
   }
   if ((flags & HG_HYBRID_HOMOGENIZE_VELOCITY) && nb > 0) {
     HG_CUDA_TRY(cudaMemsetAsync(h->hmom.p, 0, sizeof(double) * 2 * nn, s));
     HG_CUDA_TRY(cudaMemsetAsync(h->hmass.p, 0, sizeof(double) * nn, s));
-    HG_LAUNCH(kc_hvel_scatter, blocks_for(nb, 128), 128, 0, s, G, nb, d->q.p, d->v.p,
+    HG_LAUNCH(kc_hvel_scatter<W32>, blocks_for(nb, 128), 128, 0, s, G, nb, d->q.p, d->v.p,
               d->fixed.p, d->m0.p, d->w.p, h->hmom.p, h->hmass.p);
     HG_CHECK_LAUNCH();
     HG_LAUNCH(kc_hvel_finish, blocks_for(nn, 256), 256, 0, s, nn, h->hmom.p, h->hmass.p,
@@ -455,6 +477,13 @@ hg_status hybrid_step(hg_hybrid *h, double dt, int flags) {
     HG_CHECK_LAUNCH();
   }
   return HG_OK;
+}
+
+} // namespace
+
+hg_status hybrid_step(hg_hybrid *h, double dt, int flags) {
+  return h->m->p.precision == HG_PRECISION_MIXED ? hybrid_step_impl<true>(h, dt, flags)
+                                                 : hybrid_step_impl<false>(h, dt, flags);
 }
 
 } // namespace hg

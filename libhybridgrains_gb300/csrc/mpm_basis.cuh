@@ -186,4 +186,51 @@ __device__ __forceinline__ void for_stencil_weights(int basis, double x, double 
     for (int ix = x0; ix <= x1; ++ix) f(ix, iy, weight64(basis, x, y, hl, ix, iy, gx, gy, h));
 }
 
+// The same stencil's weights in FP32, for the mixed-precision hybrid step
+// (its MPM bulk is FP32). The offset of the position from the stencil's
+// first node, in cell widths, is formed in FP64 and rounded to FP32 once; the
+// 1-D weights are those of LinearBasisFunctions.cpp:6-13 and
+// uGIMPLinearBasisFunctions.cpp:6-22 in units of the cell width (for uGIMP,
+// L(d) with a = hl / h: (1 + a - d)^2 / 2, 2a (1 - d) or 2a - (a^2 + d^2)
+// by band, and the 2-D weight Lx Ly / (4 a^2)). The node range is the FP64
+// stencil's, so the coupled nodes are the FP64 path's. Stencils wider than
+// STENCIL_AXIS take the FP64 weights.
+__device__ __forceinline__ float weight1d32(int basis, float d, float a) {
+  const float dd = fabsf(d);
+  if (basis == HG_BASIS_LINEAR) return dd < 1.0f ? 1.0f - dd : 0.0f;
+  if (dd >= 1.0f + a) return 0.0f;
+  if (dd >= 1.0f - a) return 0.5f * (1.0f + a - dd) * (1.0f + a - dd);
+  if (dd >= a) return 2.0f * a * (1.0f - dd);
+  return 2.0f * a - (a * a + dd * dd);
+}
+template <class F>
+__device__ __forceinline__ void for_stencil_weights32(int basis, double x, double y, double hl,
+                                                      int x0, int y0, int x1, int y1, double gx,
+                                                      double gy, double h, double inv_h, F &&f) {
+  const int nxs = x1 - x0 + 1, nys = y1 - y0 + 1;
+  if (nxs > STENCIL_AXIS || nys > STENCIL_AXIS) {
+    for_stencil_weights(basis, x, y, hl, x0, y0, x1, y1, gx, gy, h, f);
+    return;
+  }
+  const float ox = (float)((x - gx) * inv_h - (double)x0);
+  const float oy = (float)((y - gy) * inv_h - (double)y0);
+  const float a = (float)(hl * inv_h);
+  const float norm = basis == HG_BASIS_LINEAR ? 1.0f : 1.0f / (4.0f * a * a);
+  float ax[STENCIL_AXIS], ay[STENCIL_AXIS];
+#pragma unroll
+  for (int k = 0; k < STENCIL_AXIS; ++k) {
+    ax[k] = k < nxs ? weight1d32(basis, ox - (float)k, a) : 0.0f;
+    ay[k] = k < nys ? weight1d32(basis, oy - (float)k, a) * norm : 0.0f;
+  }
+#pragma unroll
+  for (int ky = 0; ky < STENCIL_AXIS; ++ky) {
+    if (ky >= nys) break;
+#pragma unroll
+    for (int kx = 0; kx < STENCIL_AXIS; ++kx) {
+      if (kx >= nxs) break;
+      f(x0 + kx, y0 + ky, (double)(ax[kx] * ay[ky]));
+    }
+  }
+}
+
 } // namespace hg

@@ -1,5 +1,6 @@
 """The hybrid column with the MPM bulk in mixed precision (FP32 bulk, FP64
-positions) against the same scene with the FP64 MPM step: one step from the
+positions; the coupling kernels' stencil weights FP32 over the same FP64
+stencils) against the same scene with the FP64 MPM step: one step from the
 same state agrees to FP32 rounding on the grid and on the grains, and a run
 through two resampling intervals stays close."""
 import numpy as np
@@ -35,7 +36,8 @@ def test_mixed_hybrid_one_step(ctx):
     print(errs)
     assert len(ca["packed_dem"]) == len(cb["packed_dem"]) > 0
     assert errs["grid_velocity"] < 1e-5 and errs["grid_mass"] < 1e-6
-    assert errs["dem_mass"] < 1e-12 and errs["v_after"] < 1e-5
+    # the grains' stencil weights are FP32 with the MIXED bulk
+    assert errs["dem_mass"] < 1e-6 and errs["v_after"] < 1e-5
     assert errs["grain_velocity"] < 1e-5 and errs["grain_position"] < 1e-12
 
 
