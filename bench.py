@@ -340,6 +340,9 @@ def run_ours(args, rank, world, local):
                "steps": args.e2e_steps, "ms_per_step": 1e3 * e2e_s / args.e2e_steps}
         del e2
 
+    batch = None
+    if args.batch_steps > 0 and args.batch_scenes > 0:
+        batch = run_batch(args, ctx, value / world, world)
     serve = None
     if args.serve_requests > 0:
         serve = run_serving(args, ctx, rank, world)
@@ -412,6 +415,7 @@ def run_ours(args, rank, world, local):
                                   args.roofline_span, args.roofline_span)},
         "cpu_baseline": cpu,
         "e2e": e2e,
+        "batch": batch,
         "serving": serve,
         "dem": dem,
         "hybrid": hyb,
@@ -603,13 +607,17 @@ def run_hybrid(args, ctx):
             orig()
             host[0] += time.perf_counter() - t
         sim._resample = timed
+        phases0 = dict(sim.host_s)
         sim.step(args.hybrid_steps)
         ctx.synchronize()
         wall = time.perf_counter() - t0
         n, nd = sim.counts()
+        phases = {k: sim.host_s[k] - phases0[k] for k in phases0}
         out = {"steps": args.hybrid_steps, "steps_per_s": args.hybrid_steps / wall,
                "ms_per_step": 1e3 * wall / args.hybrid_steps,
                "resamplings": sim.resamplings - rs0, "resampling_host_s": host[0],
+               "resampling_host_s_by_phase": phases,
+               "resampling_share": host[0] / wall,
                "device_ms_per_step": 1e3 * (wall - host[0]) / args.hybrid_steps,
                "points": n, "disks": nd, "status": [sim.mpm.status(), sim.dem.status()]}
         return out
@@ -700,6 +708,75 @@ def gather_parts(part, world):
     out = [None] * world
     dist.all_gather_object(out, part)
     return out
+
+
+def run_batch(args, ctx, single_rate, world=1):
+    """The requests of the serving section (seed 2024) as MIXED scenes all
+    resident in one batch: whole steps timed with CUDA events over
+    --batch-steps steps (16-step graph chunks), the per-phase split from the
+    profiled per-step path, and the same scenes stepped one at a time through
+    their own graphs. The point-step rate is compared with the 2M column's
+    (single_rate, this run's headline value per GPU)."""
+    import libhybridgrains_gb300 as hg
+    from libhybridgrains_gb300 import scenes as hg_scenes
+    from libhybridgrains_gb300 import serving
+    reqs = serving.column_requests(n=args.batch_scenes, rate=args.serve_rate,
+                                   steps=args.serve_steps, seed=2024)
+    b = hg.Batch(ctx, max_members=len(reqs))
+    members = []
+    for r in reqs:
+        c = r.cfg
+        m = hg.MPM(ctx, c["grid_min"], c["grid_max"], c["h"], c["shear_modulus"],
+                   c["bulk_modulus"], c["dp_alpha"], c["flip_alpha"], hg_scenes.GRAVITY,
+                   c["planes"], capacity=r.npoints)
+        m.seed_rectangle_device(c["rect_min"], c["rect_max"], c["rho"], c["samples_per_dim"])
+        b.add(m, r.dt)
+        members.append((m, r.dt))
+    npts = sum(r.npoints for r in reqs)
+    tune = b.autotune(args.tune_steps) if args.tune_steps > 0 else None
+    b.step(max(args.warmup, 16))
+    ctx.synchronize()
+    barrier(world)
+    ctx.timer_begin()
+    b.step(args.batch_steps)
+    ms = barrier_max(ctx.timer_end(), world)
+    b.profile(True)
+    b.step(32)
+    prof = b.profile_read()
+    b.profile(False)
+    status = max(m.status() for m, _ in members)
+    b.close()
+    # the same scenes one at a time, each through its own step graphs
+    for m, dt in members:
+        m.flow(dt, 16)
+    ctx.synchronize()
+    alone_ms = 0.0
+    for m, dt in members:
+        ctx.timer_begin()
+        m.flow(dt, args.batch_alone_steps)
+        alone_ms += ctx.timer_end()
+    for m, _ in members:
+        m.close()
+    rate = npts * args.batch_steps / (ms * 1e-3)
+    steps = max(prof["steps"], 1)
+    return {
+        "workload": "the %d serving requests (seed 2024; points log-U[2e3,2e5], aspect "
+                    "U[0.5,4]) as MIXED scenes, all resident in one batch" % len(reqs),
+        "scenes": len(reqs), "points": npts, "steps": args.batch_steps,
+        "ms_per_step": ms / args.batch_steps,
+        "particle_steps_per_s": rate,
+        "of_single_scene_rate": rate / single_rate,
+        "single_scene_rate": single_rate,
+        "per_step_profile_ms": {"fused": prof["fused_ms"] / steps,
+                                "update": prof["update_ms"] / steps,
+                                "resort": prof["resort_ms"] / steps,
+                                "table": prof["table_ms"] / steps},
+        "one_at_a_time": {"steps": args.batch_alone_steps,
+                          "particle_steps_per_s": npts * args.batch_alone_steps
+                          / (alone_ms * 1e-3)},
+        "launch_shape": tune,
+        "status": int(status),
+    }
 
 
 def run_serving(args, ctx, rank=0, world=1):
@@ -844,6 +921,9 @@ def main():
     ap.add_argument("--dem-large-steps", type=int, default=200)
     ap.add_argument("--dem-dense-steps", type=int, default=2000)
     ap.add_argument("--dem-dense-large-steps", type=int, default=200)
+    ap.add_argument("--batch-scenes", type=int, default=256)
+    ap.add_argument("--batch-steps", type=int, default=400)
+    ap.add_argument("--batch-alone-steps", type=int, default=64)
     ap.add_argument("--serve-requests", type=int, default=256)
     ap.add_argument("--serve-rate", type=float, default=50.0)
     ap.add_argument("--serve-steps", type=int, default=2000)

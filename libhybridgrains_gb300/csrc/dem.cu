@@ -235,24 +235,44 @@ struct PairArgs {
   uint32_t *status;
 };
 
+// The contact test of a candidate pair (a, b), b's home cell offset by
+// (dx, dy) from a's. The FP32 offsets from the home cells' corners give the
+// centre distance to within about 1e-6 of a cell; the slack tol is 1e-4 of
+// a cell. So a pair whose FP32 distance exceeds ra + rb + tol is no contact,
+// and one whose FP32 distance is below ra + rb - tol is a contact under the
+// reference's FP64 tests as well (its AABBs overlap and c0 < 0 by about
+// 2 tol (ra + rb), far beyond FP64 rounding). Only the pairs in between take
+// those tests: AABB overlap (SpatialGrid.cpp:14-19, with the AABB corners
+// x -+ r evaluated as CircleGeometry.cpp:22-30 does) and
+// ballBallCCDCollisionHappens with q0 == q1 (active iff c0 <= 0).
+__device__ __forceinline__ bool is_contact(const PairArgs &A, float4 pa, float4 pb, int dx,
+                                           int dy, int a, int b) {
+  const float ex = (float)dx * A.Hf + (pb.x - pa.x);
+  const float ey = (float)dy * A.Hf + (pb.y - pa.y);
+  const float d2 = ex * ex + ey * ey;
+  const float outer = pa.z + pb.z + A.tol, inner = pa.z + pb.z - A.tol;
+  if (d2 > outer * outer) return false;
+  if (inner > 0.0f && d2 < inner * inner) return true;
+  const double xa = A.q[3 * a], ya = A.q[3 * a + 1], ra = A.r[a];
+  const double xb = A.q[3 * b], yb = A.q[3 * b + 1], rb = A.r[b];
+  if (!((xa + ra >= xb - rb && ya + ra >= yb - rb) && (xb + rb >= xa - ra && yb + rb >= ya - ra)))
+    return false;
+  const double ddx = xa - xb, ddy = ya - yb;
+  const double c0 = (ddx * ddx + ddy * ddy) - (ra + rb) * (ra + rb);
+  return c0 <= 0.0;
+}
+
 // Contact enumeration for body a as the first index: circle-circle with
 // b > a non-fixed, kinematic with b fixed (any index; the reference swaps the
 // fixed body into the second slot). Fixed bodies emit none.
 //
 // A partner b overlapping a's AABB has its home cell within one cell of a's
 // (the cell width is at least every AABB's width), so the 3x3 cells around
-// a's home cell hold every candidate. The FP32 filter passes b when the
-// centres lie within ra + rb (plus slack) of each other; the offsets are
-// exact to about 1e-7 of a cell and the slack is 1e-4 of a cell, so every
-// pair that is a contact in FP64 passes. The survivors take the reference's
-// FP64 tests: AABB overlap (SpatialGrid.cpp:14-19, with the AABB corners
-// x -+ r evaluated as CircleGeometry.cpp:22-30 does) and
-// ballBallCCDCollisionHappens with q0 == q1 (active iff c0 <= 0).
+// a's home cell hold every candidate.
 template <class F>
 __device__ __forceinline__ void for_each_partner(const PairArgs &A, int a, F &&found) {
   const float4 pa = A.rec[2 * a], ca = A.rec[2 * a + 1];
   const int2 ha = make_int2(__float_as_int(ca.x), __float_as_int(ca.y));
-  const double xa = A.q[3 * a], ya = A.q[3 * a + 1], ra = A.r[a];
   // the nine bucket ranges first: independent loads instead of a chain
   int bs[9], be[9];
 #pragma unroll
@@ -275,17 +295,7 @@ __device__ __forceinline__ void for_each_partner(const PairArgs &A, int a, F &&f
         continue; // bucket shared by another cell
       const bool bf = (__float_as_uint(pb.w) & REL_FIXED) != 0u;
       if (!(b > a || bf)) continue;
-      const float reach = pa.z + pb.z + A.tol;
-      const float ex = (float)dx * A.Hf + (pb.x - pa.x);
-      const float ey = (float)dy * A.Hf + (pb.y - pa.y);
-      if (ex * ex + ey * ey > reach * reach) continue;
-      const double xb = A.q[3 * b], yb = A.q[3 * b + 1], rb = A.r[b];
-      if (!((xa + ra >= xb - rb && ya + ra >= yb - rb) &&
-            (xb + rb >= xa - ra && yb + rb >= ya - ra)))
-        continue;
-      const double ddx = xa - xb, ddy = ya - yb;
-      const double c0 = (ddx * ddx + ddy * ddy) - (ra + rb) * (ra + rb);
-      if (!(c0 <= 0.0)) continue;
+      if (!is_contact(A, pa, pb, dx, dy, a, b)) continue;
       found(b, bf);
     }
   }
@@ -330,7 +340,6 @@ __global__ void kd_pairs_count_body(PairArgs A) {
   const bool af = (flags & REL_FIXED) != 0u;
   if (!af) A.cnt[a] = __popc(flags >> 1); // static planes
   const int2 ha = make_int2(__float_as_int(ca.x), __float_as_int(ca.y));
-  const double xa = A.q[3 * a], ya = A.q[3 * a + 1], ra = A.r[a];
   int bs[5], be[5];
 #pragma unroll
   for (int c = 0; c < 5; ++c) {
@@ -353,17 +362,7 @@ __global__ void kd_pairs_count_body(PairArgs A) {
         continue; // bucket shared by another cell
       const bool bf = (__float_as_uint(pb.w) & REL_FIXED) != 0u;
       if (af && bf) continue;
-      const float reach = pa.z + pb.z + A.tol;
-      const float ex = (float)dx * A.Hf + (pb.x - pa.x);
-      const float ey = (float)dy * A.Hf + (pb.y - pa.y);
-      if (ex * ex + ey * ey > reach * reach) continue;
-      const double xb = A.q[3 * b], yb = A.q[3 * b + 1], rb = A.r[b];
-      if (!((xa + ra >= xb - rb && ya + ra >= yb - rb) &&
-            (xb + rb >= xa - ra && yb + rb >= ya - ra)))
-        continue;
-      const double ddx = xa - xb, ddy = ya - yb;
-      const double c0 = (ddx * ddx + ddy * ddy) - (ra + rb) * (ra + rb);
-      if (!(c0 <= 0.0)) continue;
+      if (!is_contact(A, pa, pb, dx, dy, a, b)) continue;
       if (af) credit(A, b, a, true, overflow);
       else if (bf) credit(A, a, b, true, overflow);
       else credit(A, min(a, b), max(a, b), false, overflow);
@@ -390,7 +389,6 @@ __global__ void kd_pairs_count(PairArgs A) {
   const uint32_t bk = cell_hash(cx, cy, A.mask);
   const int be = A.bucket_end[bk], bs = be - A.bucket_count[bk];
   if (bs >= be) return;
-  const double xa = A.q[3 * a], ya = A.q[3 * a + 1], ra = A.r[a];
   bool overflow = false;
   for (int k = bs; k < be; ++k) {
     if (!HG_INDEX_OK(k, n, A.status)) break;
@@ -402,17 +400,7 @@ __global__ void kd_pairs_count(PairArgs A) {
       continue; // bucket shared by another cell
     const bool bf = (__float_as_uint(pb.w) & REL_FIXED) != 0u;
     if (af && bf) continue;
-    const float reach = pa.z + pb.z + A.tol;
-    const float ex = (float)dx * A.Hf + (pb.x - pa.x);
-    const float ey = (float)dy * A.Hf + (pb.y - pa.y);
-    if (ex * ex + ey * ey > reach * reach) continue;
-    const double xb = A.q[3 * b], yb = A.q[3 * b + 1], rb = A.r[b];
-    if (!((xa + ra >= xb - rb && ya + ra >= yb - rb) &&
-          (xb + rb >= xa - ra && yb + rb >= ya - ra)))
-      continue;
-    const double ddx = xa - xb, ddy = ya - yb;
-    const double c0 = (ddx * ddx + ddy * ddy) - (ra + rb) * (ra + rb);
-    if (!(c0 <= 0.0)) continue;
+    if (!is_contact(A, pa, pb, dx, dy, a, b)) continue;
     if (af) credit(A, b, a, true, overflow);
     else if (bf) credit(A, a, b, true, overflow);
     else credit(A, min(a, b), max(a, b), false, overflow);

@@ -351,6 +351,9 @@ struct hg_batch {
   cudaEvent_t rtable_ev[NBUF] = {};
   int rb = 0;
   hg::DevBuf<uint32_t> outside; // 2 counters per member
+  // work queues of the batched kernels: [fused cursor, fused done, update
+  // cursor, update done], zero between launches
+  hg::DevBuf<int32_t> queue;
   uint32_t *h_outside = nullptr;
   cudaEvent_t out_ev = nullptr;
   bool out_pending = false;

@@ -644,13 +644,6 @@ __device__ __forceinline__ void load_slot(const MixedArgs *slots, int s, MixedAr
   __syncthreads();
 }
 
-// This CTA's contiguous share [begin, end) of the batch's work items, so
-// that a CTA crosses few scene boundaries.
-__device__ __forceinline__ void cta_range(int total, int &begin, int &end) {
-  begin = (int)((int64_t)total * blockIdx.x / gridDim.x);
-  end = (int)((int64_t)total * (blockIdx.x + 1) / gridDim.x);
-}
-
 __device__ __forceinline__ int batch_slot(const int *prefix, int nslots, int item) {
   int lo = 0, hi = nslots - 1;
   while (lo < hi) { // largest s with prefix[s] <= item
@@ -661,26 +654,71 @@ __device__ __forceinline__ int batch_slot(const int *prefix, int nslots, int ite
   return lo;
 }
 
+// Work queue of a batched launch over its (scene, tile) items. q[0] is the
+// next unclaimed item and q[1] counts the CTAs that found the queue empty;
+// the last of those resets both, so every launch (ordered after the previous
+// one on the stream) starts from zero. Thread 0 claims guided chunks: about
+// a 1/(2 x CTAs) share of what it last saw remaining, 1 to QUEUE_MAX_CHUNK
+// items, so that early claims keep consecutive items (one scene's tiles)
+// together and the last ones balance the tail one tile at a time. Tiles
+// differ widely in point count across scenes of 2e3 to 2e5 points, which a
+// static split by item count cannot balance.
+constexpr int QUEUE_MAX_CHUNK = 8;
+
+__device__ __forceinline__ int2 queue_claim(int32_t *q, int total, int seen) {
+  const int g = max(1, min(QUEUE_MAX_CHUNK, (total - seen) / (2 * (int)gridDim.x)));
+  return make_int2(atomicAdd(q, g), g);
+}
+
+__device__ __forceinline__ void queue_done(int32_t *q) {
+  if (threadIdx.x != 0) return;
+  __threadfence();
+  if (atomicAdd(q + 1, 1) == (int)gridDim.x - 1) {
+    q[0] = 0;
+    q[1] = 0;
+  }
+}
+
+// Drains the queue: tile(A, tile index) for every claimed item, the scene's
+// arguments copied into A whenever the item's scene changes. The next chunk
+// is claimed while this one runs.
+template <class F>
+__device__ __forceinline__ void drain_queue(const MixedArgs *slots, int nslots, const int *prefix,
+                                            int32_t *q, MixedArgs &A, F &&tile) {
+  __shared__ int2 s_claim;
+  const int total = prefix[nslots];
+  int2 claim = threadIdx.x == 0 ? queue_claim(q, total, 0) : make_int2(0, 0);
+  int s = -1;
+  for (;;) {
+    if (threadIdx.x == 0) s_claim = claim;
+    __syncthreads();
+    const int2 c = s_claim;
+    __syncthreads();
+    if (c.x >= total) break;
+    if (threadIdx.x == 0) claim = queue_claim(q, total, c.x + c.y);
+    const int end = min(c.x + c.y, total);
+    for (int item = c.x; item < end; ++item) {
+      if (s < 0 || item >= prefix[s + 1] || item < prefix[s]) {
+        s = batch_slot(prefix, nslots, item);
+        load_slot(slots, s, A);
+      }
+      tile(A, A.active[item - prefix[s]]);
+    }
+  }
+  queue_done(q);
+}
+
+
 // All scenes of a batch in one launch: the CTAs drain (scene, tile) items.
 __global__ void __launch_bounds__(THREADS, 3) kb_g2p2g(const MixedArgs *__restrict__ slots,
-                                                     int nslots) {
+                                                     int nslots, int32_t *queue) {
   __shared__ FusedSmem S;
   __shared__ MixedArgs A;
   __shared__ int prefix[PREFIX_LEN];
   zero_slow(S);
   batch_prefix(slots, nslots, prefix);
-  int begin, end;
-  cta_range(prefix[nslots], begin, end);
-  if (begin >= end) return;
-  int s = batch_slot(prefix, nslots, begin);
-  load_slot(slots, s, A);
-  for (int item = begin; item < end; ++item) {
-    if (item >= prefix[s + 1]) {
-      do ++s; while (item >= prefix[s + 1]);
-      load_slot(slots, s, A);
-    }
-    fused_tile<false>(A, A.active[item - prefix[s]], S);
-  }
+  drain_queue(slots, nslots, prefix, queue, A,
+              [&](const MixedArgs &a, int tile) { fused_tile<false>(a, tile, S); });
 }
 
 // ---- MIXED step with the uGIMP basis --------------------------------------
@@ -922,22 +960,12 @@ __global__ void __launch_bounds__(THREADS) kx_grid_update(const __grid_constant_
 }
 
 __global__ void __launch_bounds__(THREADS) kb_grid_update(const MixedArgs *__restrict__ slots,
-                                                          int nslots) {
+                                                          int nslots, int32_t *queue) {
   __shared__ MixedArgs A;
   __shared__ int prefix[PREFIX_LEN];
   batch_prefix(slots, nslots, prefix);
-  int begin, end;
-  cta_range(prefix[nslots], begin, end);
-  if (begin >= end) return;
-  int s = batch_slot(prefix, nslots, begin);
-  load_slot(slots, s, A);
-  for (int item = begin; item < end; ++item) {
-    if (item >= prefix[s + 1]) {
-      do ++s; while (item >= prefix[s + 1]);
-      load_slot(slots, s, A);
-    }
-    update_tile(A, A.active[item - prefix[s]]);
-  }
+  drain_queue(slots, nslots, prefix, queue, A,
+              [&](const MixedArgs &a, int tile) { update_tile(a, tile); });
 }
 
 // Copies every member's out-of-window counters into one array, for a single
@@ -1769,8 +1797,10 @@ namespace hg {
 hg_status batch_alloc(hg_batch *b) {
   const size_t tsz = 2 * (size_t)b->max_members * sizeof(MixedArgs);
   hg_status st;
-  if ((st = b->table.alloc(tsz)) || (st = b->outside.alloc(2 * (size_t)b->max_members)))
+  if ((st = b->table.alloc(tsz)) || (st = b->outside.alloc(2 * (size_t)b->max_members)) ||
+      (st = b->queue.alloc(4)))
     return st;
+  HG_CUDA_TRY(cudaMemsetAsync(b->queue.p, 0, 4 * sizeof(int32_t), b->ctx->stream));
   for (int k = 0; k < hg_batch::NBUF; ++k) {
     HG_CUDA_TRY(cudaMallocHost(&b->h_table[k], tsz));
     HG_CUDA_TRY(cudaEventCreateWithFlags(&b->table_ev[k], cudaEventDisableTiming));
@@ -1833,8 +1863,8 @@ hg_status batch_chunk_graph(hg_batch *b, int S) {
   HG_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   hg_status st = HG_OK;
   for (int k = 0; k < CHUNK_STEPS && st == HG_OK; ++k) {
-    HG_LAUNCH(kb_grid_update, gu, THREADS, 0, s, dt, S);
-    HG_LAUNCH(kb_g2p2g, gf, THREADS, 0, s, db, S);
+    HG_LAUNCH(kb_grid_update, gu, THREADS, 0, s, dt, S, b->queue.p + 2);
+    HG_LAUNCH(kb_g2p2g, gf, THREADS, 0, s, db, S, b->queue.p);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) st = cuda_fail(e, "kernel launch");
   }
@@ -1975,10 +2005,11 @@ hg_status batch_step(hg_batch *b, int nsteps) {
     const MixedArgs *dt = reinterpret_cast<const MixedArgs *>(b->table.p);
     const MixedArgs *db = dt + S;
     const int nsm = b->ctx->num_sms;
-    HG_LAUNCH(kb_grid_update, nsm * update_per_sm(b->shape), THREADS, 0, s, dt, S);
+    HG_LAUNCH(kb_grid_update, nsm * update_per_sm(b->shape), THREADS, 0, s, dt, S,
+              b->queue.p + 2);
     HG_CHECK_LAUNCH();
     if (b->profile) HG_CUDA_TRY(cudaEventRecord(ev[3], s));
-    HG_LAUNCH(kb_g2p2g, nsm * fused_per_sm(b->shape), THREADS, 0, s, db, S);
+    HG_LAUNCH(kb_g2p2g, nsm * fused_per_sm(b->shape), THREADS, 0, s, db, S, b->queue.p);
     HG_CHECK_LAUNCH();
     if (b->profile) HG_CUDA_TRY(cudaEventRecord(ev[4], s));
     for (hg_mpm *m : b->members) m->steps_since_rebin++;

@@ -24,6 +24,8 @@ The homogenised fields are accumulated once per device step, so at a
 resampling step the finalised field has one term less than the reference's,
 which accumulates the current step a second time inside the branch.
 """
+import time
+
 import numpy as np
 
 from . import DEM, FP64, MPM, Hybrid, Resampler, Zones, scene_xml, scenes
@@ -79,8 +81,13 @@ class HybridSim:
         self.resamplings = 0
         self.steps = 0
         self.stats = []
+        # host seconds of the resampling intervals by phase: device->host
+        # copies, zone update, resampling proper, host->device uploads
+        self.host_s = dict(download=0.0, zones=0.0, resampling=0.0, upload=0.0)
 
     def _resample(self):
+        clock = time.perf_counter
+        t0 = clock()
         st = self.mpm.download()
         q3, v3 = self.dem.download()
         P, G = self.P, self.G
@@ -89,17 +96,24 @@ class HybridSim:
         if self.hom[0] or self.hom[1]:
             c = self.hyb.coupling()
             hs, hv = c["homog_stress"] / self.freq, c["homog_velocity"] / self.freq
+        t1 = clock()
         self.zones.update(q3, G["r"], G["fixed"], st["q"])
+        t2 = clock()
         self.res.set_points(P["q0"], st["q"], st["v"], P["m0"] * P["w"], P["vol0"] * P["w"],
                             P["m0"], P["vol0"], P["hl"], st["be"], st["J"], st["jh"])
         self.res.set_grains(G["q0"], q3, v3, G["r"], G["M0"], G["fixed"])
         self.res.set_homogenized(hs, hv)
         self.res.run(self.zones)
         a, b = self.res.points(), self.res.grains()
+        t3 = clock()
         self.mpm.upload(a["q"], a["v"], a["m"], a["vol"], a["hl"], a["be"], a["J"], a["jh"])
         self.dem.upload_relabel(b["q"], b["v"], b["r"], b["M0"][:, 0], b["M0"][:, 2], b["fixed"],
                                 b["old_to_new"])
         self.dem.set_weights(b["w"])
+        t4 = clock()
+        for k, dt_ in (("download", t1 - t0), ("zones", t2 - t1), ("resampling", t3 - t2),
+                       ("upload", t4 - t3)):
+            self.host_s[k] += dt_
         self.P = dict(q0=a["q0"], m0=a["m0"], vol0=a["vol0"], hl=a["hl"], w=a["w"])
         self.G = dict(q0=b["q0"], r=b["r"], M0=b["M0"], fixed=b["fixed"], w=b["w"])
         self.hyb.clear_homogenized()

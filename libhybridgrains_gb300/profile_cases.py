@@ -6,6 +6,7 @@
         [--precision mixed]
     python -m libhybridgrains_gb300.profile_cases hybrid --steps 6 [--precision mixed]
     python -m libhybridgrains_gb300.profile_cases column --steps 8
+    python -m libhybridgrains_gb300.profile_cases batch --scenes 256 --steps 8
 
 Each case builds its scene, runs one warm-up step, then ``--steps`` steps one
 call per step (so that every kernel is a separate launch a profiler can
@@ -16,7 +17,8 @@ compacted to a 1.9 mm pitch between a floor and two walls (about 2.5
 contacts per disk; dt 1e-6 s);
 the hybrid case is the hybrid column (100,000 points under 20,000 disks)
 after its initial resampling; the column case is the 2,000,000-point MIXED
-column.
+column; the batch case is the serving mix (the first --scenes requests of
+seed 2024) as MIXED scenes in one batch.
 """
 import argparse
 import time
@@ -27,7 +29,8 @@ def main(argv=None):
     from libhybridgrains_gb300 import scenes, serving
 
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["dem", "hybrid", "column"])
+    ap.add_argument("case", choices=["dem", "hybrid", "column", "batch"])
+    ap.add_argument("--scenes", type=int, default=256, help="batch: serving requests")
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--disks", type=int, default=1000000)
     ap.add_argument("--per-row", type=int, default=1000, help="DEM lattice disks per row")
@@ -66,6 +69,24 @@ def main(argv=None):
 
         def status():
             return sim.mpm.status(), sim.dem.status()
+    elif args.case == "batch":
+        reqs = serving.column_requests(n=args.scenes, seed=2024)
+        obj = hg.Batch(ctx, max_members=len(reqs))
+        members = []
+        for r in reqs:
+            c = r.cfg
+            m = hg.MPM(ctx, c["grid_min"], c["grid_max"], c["h"], c["shear_modulus"],
+                       c["bulk_modulus"], c["dp_alpha"], c["flip_alpha"], scenes.GRAVITY,
+                       c["planes"], capacity=r.npoints)
+            m.seed_rectangle_device(c["rect_min"], c["rect_max"], c["rho"], c["samples_per_dim"])
+            obj.add(m, r.dt)
+            members.append(m)
+
+        def step():
+            obj.step(1)
+
+        def status():
+            return max(m.status() for m in members)
     else:
         cfg = scenes.mpm_column("column_2M")
         p = scenes.seed_column_points(cfg)
