@@ -284,16 +284,20 @@ def run_ours(args, rank, world, local):
 
     # ---- the uGIMP basis (the reference's shipped scenes use it) --------------------
     ugimp = None
-    if args.ugimp_steps > 0:
+    if args.ugimp_steps >= 0:
         cu = dict(cfg, grid_min=(cfg["grid_min"][0] - 4 * cfg["h"],
                                  cfg["grid_min"][1] - 4 * cfg["h"]))
         rates = {}
-        for name, prec, k in (("mixed", hg.MIXED, args.ugimp_steps), ("fp64", hg.FP64, 5)):
+        usteps = args.ugimp_steps if args.ugimp_steps > 0 else args.steps
+        for name, prec, k in (("mixed", hg.MIXED, usteps), ("fp64", hg.FP64, 5)):
             mu_ = hg.MPM(ctx, cu["grid_min"], cu["grid_max"], cu["h"], cu["shear_modulus"],
                          cu["bulk_modulus"], cu["dp_alpha"], cu["flip_alpha"],
                          hg_scenes.GRAVITY,
                          cu["planes"], basis=hg.UGIMP, precision=prec, capacity=n)
             mu_.upload(pts["q"], pts["v"], pts["m"], pts["vol"], pts["hl"])
+            utune = None
+            if prec == hg.MIXED and args.tune_steps > 0:
+                utune = mu_.autotune(dt, args.tune_steps)
             mu_.flow(dt, 3)
             ctx.synchronize()
             ctx.timer_begin()
@@ -301,6 +305,24 @@ def run_ours(args, rank, world, local):
             ums = ctx.timer_end()
             rates[name] = {"value": n * k / (ums * 1e-3), "ms_per_step": ums / k, "steps": k,
                            "status": mu_.status()}
+            if prec == hg.MIXED:
+                # the fused uGIMP kernel against the same per-unit bytes as
+                # the linear one, event-timed over the next window of steps
+                ua = int((mu_.grid()["mass"] > 0).sum())
+                mu_.profile(True)
+                mu_.flow(dt, args.roofline_window)
+                f_ms, u_ms, kk = mu_.profile_read()
+                mu_.profile(False)
+                per = f_ms * 1e-3 / max(kk, 1)
+                ub = n * BYTES_PER_PARTICLE + ua * BYTES_PER_ACTIVE_NODE
+                rates[name].update(
+                    launch_shape=utune, active_nodes=ua, status=mu_.status(),
+                    of_linear_step_time=(ums / k) / (ms / args.steps),
+                    roofline={"kernel": "kxu_g2p2g", "algorithmic_bytes": ub,
+                              "kernel_ms": per * 1e3, "grid_update_ms": u_ms / max(kk, 1),
+                              "achieved_gbs": ub / per / 1e9,
+                              "timing": "CUDA events around each launch, %d steps after the "
+                                        "timed ones" % kk})
             mu_.close()
         ugimp = {"workload": "column_2M with the uGIMP basis (half-width h/4), grid extended by "
                              "4 cells below and left", **rates,
@@ -608,15 +630,22 @@ def run_hybrid(args, ctx):
             host[0] += time.perf_counter() - t
         sim._resample = timed
         phases0 = dict(sim.host_s)
+        st0 = len(sim.stats)
         sim.step(args.hybrid_steps)
         ctx.synchronize()
         wall = time.perf_counter() - t0
         n, nd = sim.counts()
         phases = {k: sim.host_s[k] - phases0[k] for k in phases0}
+        # inside the resampling proper, summed over the timed intervals
+        inner = {k: sum(x[k] for x in sim.stats[st0:]) for k in
+                 ("ms_insert_grains", "ms_insert_points", "ms_point_grids", "ms_quantities",
+                  "ms_delete", "points_inserted", "grains_inserted", "points_deleted",
+                  "grains_deleted")}
         out = {"steps": args.hybrid_steps, "steps_per_s": args.hybrid_steps / wall,
                "ms_per_step": 1e3 * wall / args.hybrid_steps,
                "resamplings": sim.resamplings - rs0, "resampling_host_s": host[0],
                "resampling_host_s_by_phase": phases,
+               "resampler_by_phase": inner,
                "resampling_share": host[0] / wall,
                "device_ms_per_step": 1e3 * (wall - host[0]) / args.hybrid_steps,
                "points": n, "disks": nd, "status": [sim.mpm.status(), sim.dem.status()]}
@@ -916,7 +945,8 @@ def main():
     ap.add_argument("--tune-steps", type=int, default=20)
     ap.add_argument("--roofline-span", type=int, default=10000)
     ap.add_argument("--roofline-window", type=int, default=2000)
-    ap.add_argument("--ugimp-steps", type=int, default=200)
+    ap.add_argument("--ugimp-steps", type=int, default=0,
+                    help="steps of the uGIMP column (0: as many as --steps, <0: skip)")
     ap.add_argument("--dem-large-disks", type=int, default=1000000)
     ap.add_argument("--dem-large-steps", type=int, default=200)
     ap.add_argument("--dem-dense-steps", type=int, default=2000)

@@ -70,6 +70,10 @@ const char *hg_status_string(hg_status s);
 const char *hg_last_error(void);
 /* Number of kernels this library has launched in the process so far. */
 int64_t hg_kernel_launch_count(void);
+/* Host threads the library's host-side loops (zone update, resampling) may
+ * use, process-wide: n >= 1, or 0 for the default (the hardware concurrency,
+ * at most 16). Results do not depend on it. */
+hg_status hg_set_host_threads(int32_t n);
 /* Measurement hooks (no counterpart in the reference): CUDA events recorded
  * on the context's stream; _end synchronises and returns the elapsed time. */
 hg_status hg_context_timer_begin(hg_context *ctx);
@@ -415,8 +419,13 @@ typedef struct {
   double kappa, mu;                 /* bulk and shear modulus */
   int32_t homogenize_stress, homogenize_velocity;
 } hg_resampler_desc;
+/* Counts of the last hg_resampler_run and its host time by phase (ms):
+ * grain insertion, point insertion (transition, direct and inner regions),
+ * the point search grids, the quantities of the inserted points and grains,
+ * and deletion with the weight update. */
 typedef struct {
   int64_t points_inserted, grains_inserted, points_deleted, grains_deleted;
+  double ms_insert_grains, ms_insert_points, ms_point_grids, ms_quantities, ms_delete;
 } hg_resampler_stats;
 hg_status hg_resampler_create(const hg_resampler_desc *desc, hg_resampler **out);
 hg_status hg_resampler_destroy(hg_resampler *r);

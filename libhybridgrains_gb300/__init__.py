@@ -105,6 +105,12 @@ def kernel_launch_count():
     return int(load().hg_kernel_launch_count())
 
 
+def set_host_threads(n):
+    """Host threads of the library's host loops (zone update, resampling),
+    process-wide; 0 restores the default. Results do not depend on it."""
+    check("hg_set_host_threads", int(n))
+
+
 class Context:
     """A device and the CUDA stream all objects of the context run on."""
 
@@ -824,7 +830,12 @@ class Resampler:
         return n.value, g.value, dict(points_inserted=s.points_inserted,
                                       grains_inserted=s.grains_inserted,
                                       points_deleted=s.points_deleted,
-                                      grains_deleted=s.grains_deleted)
+                                      grains_deleted=s.grains_deleted,
+                                      ms_insert_grains=s.ms_insert_grains,
+                                      ms_insert_points=s.ms_insert_points,
+                                      ms_point_grids=s.ms_point_grids,
+                                      ms_quantities=s.ms_quantities,
+                                      ms_delete=s.ms_delete)
 
     def points(self):
         n, _, _ = self.stats()

@@ -73,7 +73,10 @@ class ResamplerDesc(ctypes.Structure):
 
 class ResamplerStats(ctypes.Structure):
     _fields_ = [("points_inserted", ctypes.c_int64), ("grains_inserted", ctypes.c_int64),
-                ("points_deleted", ctypes.c_int64), ("grains_deleted", ctypes.c_int64)]
+                ("points_deleted", ctypes.c_int64), ("grains_deleted", ctypes.c_int64),
+                ("ms_insert_grains", ctypes.c_double), ("ms_insert_points", ctypes.c_double),
+                ("ms_point_grids", ctypes.c_double), ("ms_quantities", ctypes.c_double),
+                ("ms_delete", ctypes.c_double)]
 
 
 HG_TUNE_CANDIDATES = 4
@@ -121,6 +124,7 @@ SIGNATURES = {
     "hg_status_string": [_i32],
     "hg_last_error": [],
     "hg_kernel_launch_count": [],
+    "hg_set_host_threads": [_i32],
     "hg_context_timer_begin": [_P],
     "hg_context_timer_end": [_P, _D],
     "hg_mpm_create": [_P, ctypes.POINTER(MpmDesc), _PP],

@@ -14,6 +14,7 @@
 namespace hg {
 
 std::atomic<int64_t> g_launches{0};
+std::atomic<int> g_host_threads{0};
 thread_local cudaStream_t t_alloc_stream = nullptr;
 
 namespace {
@@ -237,6 +238,12 @@ const char *hg_status_string(hg_status s) {
 const char *hg_last_error(void) { return hg::last_error_cstr(); }
 
 int64_t hg_kernel_launch_count(void) { return g_launches.load(); }
+
+hg_status hg_set_host_threads(int32_t n) {
+  if (n < 0 || n > 1024) return fail(HG_ERR_INVALID_ARGUMENT, "host threads must be 0 .. 1024");
+  g_host_threads.store(n);
+  return HG_OK;
+}
 
 // ---- context --------------------------------------------------------------
 
@@ -676,13 +683,14 @@ static hg_status upload_impl(hg_mpm *m, int64_t n, const double *q, const double
     }
     HG_CUDA_TRY(cudaMemsetAsync(m->sigma.p, 0, sizeof(double) * 4 * n, s));
   } else {
-    // stage in upload order, then convert and sort on the device
-    const int64_t nd = 11 * n;
+    // stage in upload order, then convert and sort on the device (the
+    // half-widths only with the uGIMP basis)
+    const int64_t nd = (m->p.basis == HG_BASIS_UGIMP ? 12 : 11) * n;
     if (m->stage_d.n < (size_t)nd && (st = m->stage_d.alloc(nd))) return st;
     if (m->stage_i.n < (size_t)n && (st = m->stage_i.alloc(n))) return st;
     if (m->stage_u8.n < (size_t)n && (st = m->stage_u8.alloc(n))) return st;
     double *sq = m->stage_d.p, *sv = sq + 2 * n, *sm = sv + 2 * n, *svol = sm + n,
-           *sbe = svol + n, *sJ = sbe + 4 * n;
+           *sbe = svol + n, *sJ = sbe + 4 * n, *shl = sJ + n;
     if ((st = h2d(s, sq, q, 2 * n)) || (st = h2d(s, sv, v, 2 * n)) ||
         (st = h2d(s, sm, mass, n)) || (st = h2d(s, svol, volume, n)))
       return st;
@@ -707,22 +715,23 @@ static hg_status upload_impl(hg_mpm *m, int64_t n, const double *q, const double
     } else {
       HG_CUDA_TRY(cudaMemsetAsync(m->stage_u8.p, 0, n, s));
     }
-    if (m->p.basis == HG_BASIS_UGIMP && n > 0) {
-      // the uGIMP kernel takes one half-width for all points (the reference's
-      // scenes seed every point with h / (2 samples per dimension))
-      if (!hl) return fail(HG_ERR_INVALID_ARGUMENT, "the uGIMP basis needs the half-widths hl");
+    const bool ugimp = m->p.basis == HG_BASIS_UGIMP;
+    if (ugimp && n > 0) {
+      // per-point half-widths; the FP32 weights of the MIXED kernel take
+      // 0 < hl <= h / 2 (the stencil of nodes c-1 .. c+2)
       std::vector<double> h(n);
       HG_CUDA_TRY(cudaMemcpy(h.data(), hl, sizeof(double) * n, cudaMemcpyDefault));
-      for (int64_t i = 0; i < n; ++i)
-        if (!(std::fabs(h[i] - h[0]) <= 1e-12 * std::fabs(h[0])))
-          return fail(HG_ERR_UNSUPPORTED, "MIXED uGIMP needs one half-width for all points");
-      const double cells = h[0] / m->p.h;
-      if (!(cells > 0.0 && cells <= 0.5))
-        return fail(HG_ERR_UNSUPPORTED, "MIXED uGIMP needs 0 < hl <= h / 2");
-      m->hl_cells = (float)cells;
+      for (int64_t i = 0; i < n; ++i) {
+        const double cells = h[i] / m->p.h;
+        if (!(cells > 0.0 && cells <= 0.5))
+          return fail(HG_ERR_UNSUPPORTED, "MIXED uGIMP needs 0 < hl <= h / 2");
+      }
+      m->hl_cells = (float)(h[0] / m->p.h);
+      if ((st = h2d(s, shl, hl, n))) return st;
     }
     m->primed = false;
-    if ((st = mixed_upload(m, sq, sv, sm, svol, sbe, sJ, m->stage_i.p, m->stage_u8.p)))
+    if ((st = mixed_upload(m, sq, sv, sm, svol, ugimp ? shl : nullptr, sbe, sJ, m->stage_i.p,
+                           m->stage_u8.p)))
       return st;
   }
   // the caller may reuse its buffers as soon as this returns
@@ -775,8 +784,10 @@ hg_status hg_mpm_estimate_bytes(const hg_mpm_desc *d, int64_t *bytes) {
     b += cap * (2 * 16 + 3 * 8 + 32 + 8 + 32 + 4 + 1); // q v | m vol hl | be | J | sigma | jh | kin
     b += nn * (8 + 6 * 16 + 8 + 4);                    // grid fields
   } else {
+    const bool ugimp = d->basis == HG_BASIS_UGIMP;
     b += mixed_device_bytes(P.nx, P.ny, cap);
-    b += 8 * std::max<int64_t>(11 * cap, 5 * nn) + cap; // upload / download staging
+    if (ugimp) b += 2 * 4 * cap; // per-point half-widths, both buffers
+    b += 8 * std::max<int64_t>((ugimp ? 12 : 11) * cap, 5 * nn) + cap; // upload / download staging
   }
   b += 4 * 2 * cap; // int staging (upload, cell index)
   *bytes = b;

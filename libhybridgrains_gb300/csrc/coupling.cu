@@ -272,16 +272,21 @@ __global__ void kc_hstress(GridGeom G, int64_t nb, const int32_t *__restrict__ o
     const double s10 = -0.5 * (fy * rx + ry * fx);
     const double s01 = -0.5 * (fx * ry + rx * fy);
     const double s11 = -0.5 * (fy * ry + ry * fy);
+    // FP64 bulk: the reference's (w s) / area per node. Mixed bulk: w (s /
+    // area), one division per component and contact instead of one per node
+    // (FP64 division is a long sequence on the FP64 pipe).
+    const double d00 = W32 ? s00 / area : s00, d10 = W32 ? s10 / area : s10;
+    const double d01 = W32 ? s01 / area : s01, d11 = W32 ? s11 / area : s11;
     int x0, y0, x1, y1;
     stencil64(G.basis, px, py, hl, G.gx, G.gy, G.h, x0, y0, x1, y1);
     stencil_weights<W32>(G, px, py, hl, x0, y0, x1, y1,
                         [&](int ix, int iy, double wt) {
                           if (!node_ok(G, ix, iy)) return;
                           const int64_t i = (int64_t)iy * (G.nx + 1) + ix;
-                          atomicAdd(&hs[4 * i], wt * s00 / area);
-                          atomicAdd(&hs[4 * i + 1], wt * s10 / area);
-                          atomicAdd(&hs[4 * i + 2], wt * s01 / area);
-                          atomicAdd(&hs[4 * i + 3], wt * s11 / area);
+                          atomicAdd(&hs[4 * i], W32 ? wt * d00 : wt * d00 / area);
+                          atomicAdd(&hs[4 * i + 1], W32 ? wt * d10 : wt * d10 / area);
+                          atomicAdd(&hs[4 * i + 2], W32 ? wt * d01 : wt * d01 / area);
+                          atomicAdd(&hs[4 * i + 3], W32 ? wt * d11 : wt * d11 / area);
                         });
   }
 }
@@ -390,7 +395,7 @@ hg_status hybrid_step_impl(hg_hybrid *h, double dt, int flags) {
   const double *hl0 = m->hl.p;
   if (mixed) {
     if ((st = mixed_step_begin(m))) return st;
-    // points.hl(0) in world units (one half-width for all MIXED points)
+    // points.hl(0) in world units: the half-width of the first uploaded point
     const double v = m->p.basis == HG_BASIS_UGIMP ? (double)m->hl_cells * m->p.h : 0.0;
     if (v != h->hl0_value) {
       HG_LAUNCH(kc_set_scalar, 1, 1, 0, s, h->hl0.p, v);

@@ -4,7 +4,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <atomic>
+#include <thread>
 #include <utility>
 #include <string>
 #include <vector>
@@ -30,6 +32,7 @@ hg_status cuda_fail(cudaError_t e, const char *what);
 // Launch bookkeeping: every kernel launch goes through HG_LAUNCH so that the
 // number of library kernels launched is observable (hg_kernel_launch_count).
 extern std::atomic<int64_t> g_launches;
+extern std::atomic<int> g_host_threads; // hg_set_host_threads; 0: default
 // An NVTX range over a C-ABI call, for timelines of profiling tools (a no-op
 // when no tool is attached).
 #ifdef HG_BOUNDS_CHECK
@@ -174,6 +177,26 @@ struct hg_context {
 };
 
 namespace hg {
+// Host loop over [0, n) split into contiguous ranges over the host threads
+// (hg_set_host_threads, by default the hardware concurrency up to 16), at
+// least min_per_worker items each; f(begin, end) must only write what its
+// range owns.
+template <typename F>
+void host_parallel(size_t n, size_t min_per_worker, F f) {
+  const int set = g_host_threads.load();
+  const size_t hw = set > 0 ? (size_t)set
+                            : std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  const size_t workers = std::min(hw, std::max<size_t>(1, n / std::max<size_t>(min_per_worker, 1)));
+  if (workers <= 1) {
+    f((size_t)0, n);
+    return;
+  }
+  std::vector<std::thread> pool;
+  for (size_t t = 1; t < workers; ++t) pool.emplace_back(f, n * t / workers, n * (t + 1) / workers);
+  f((size_t)0, n / workers);
+  for (auto &th : pool) th.join();
+}
+
 void context_retain(hg_context *c);
 void context_release(hg_context *c);
 // two page-locked uint32 words; NULL when page-locked memory is exhausted
@@ -225,6 +248,7 @@ struct MixedParticles {
   float4 *strain; // (J - 1, be_bar - I: xx, xy, yy)
   uint8_t *flags; // bit0 just_homogenized, bit1 kinematically scripted
   int32_t *id;    // upload index
+  float *hl;      // uGIMP half-width in cells (nullptr for the linear basis)
 };
 
 } // namespace hg
@@ -247,8 +271,11 @@ struct hg_mpm {
   hg::DevBuf<float4> mstrain_[2];
   hg::DevBuf<uint8_t> mflags_[2];
   hg::DevBuf<int32_t> mid_[2];
+  hg::DevBuf<float> mhl_[2]; // uGIMP only
   int cur = 0; // which buffer of the pairs above is live
-  float hl_cells = 0.f; // uGIMP: the points' common half-width in cells
+  // uGIMP: the half-width of the first uploaded point in cells (the grains'
+  // stencil half-width of the hybrid coupling, points.hl(0))
+  float hl_cells = 0.f;
   hg::DevBuf<float4> acc4; // (px, py, fx, fy) accumulated for the next update
   hg::DevBuf<float> accm;  // mass accumulated for the next update
   hg::DevBuf<float4> va;   // (vx, vy, ax, ay) of the last update
@@ -291,8 +318,10 @@ hg_status mpm64_phase1(hg_mpm *m, double dt);
 hg_status mpm64_phase2(hg_mpm *m, double dt);
 
 hg_status mixed_alloc(hg_mpm *m);
+// hl: device array of half-widths (world units) for the uGIMP basis, else
+// nullptr
 hg_status mixed_upload(hg_mpm *m, const double *q, const double *v,
-                       const double *mass, const double *vol,
+                       const double *mass, const double *vol, const double *hl,
                        const double *be, const double *J, const int32_t *jh,
                        const uint8_t *kin);
 hg_status mixed_download(hg_mpm *m, double *q, double *v, double *be,

@@ -20,7 +20,8 @@
 //
 // Layout in HBM. Particles are SoA, sorted by (tile, cell within tile) with
 // 16x16-cell tiles: u = (x - grid_min)/h as double2, v float2, (m, V) float2,
-// strain float4 = (J - 1, be_bar - I [xx, xy, yy]) and a flag byte. Storing
+// strain float4 = (J - 1, be_bar - I [xx, xy, yy]), a flag byte and, with the
+// uGIMP basis, the half-width in cells as a float. Storing
 // J and be_bar as offsets from 1 and I keeps FP32's 24 bits on the strain
 // itself rather than on the leading 1. Grid fields are dense node-major
 // float4/float arrays; only tiles near particles are touched.
@@ -29,7 +30,8 @@
 // points sorted into its cell in registers (no atomics); points that left
 // their cell since the last re-sort use shared-memory atomics on the tile's
 // node window. Window sums go to global memory with one float4 + one float
-// atomic per touched node.
+// atomic per touched node. With the uGIMP basis (up to 4 x 4 nodes per point)
+// every contribution goes through shared-memory atomics on the window.
 //
 // Re-sorting (counting sort by cell key) runs when a point has drifted out of
 // its tile's window, when more than 1/32 of the points have left their sorted
@@ -66,7 +68,6 @@ struct alignas(16) MixedArgs {
   // Half-width (in cells) of the band around a plane in which the FP32
   // plane test is redone exactly in FP64.
   float pmargin;
-  float hl; // uGIMP half-width of every point in cells (0: linear basis)
   int nplanes;
   const int32_t *offsets;
   const int32_t *active;  // active bins or tiles
@@ -76,6 +77,7 @@ struct alignas(16) MixedArgs {
   const float2 *mv;
   float4 *strain;
   uint8_t *flags;
+  const float *hl; // uGIMP half-widths in cells (nullptr for the linear basis)
   const float4 *va;
   float4 *va_out; // the same array, written by the grid update
   float4 *acc4;
@@ -727,58 +729,138 @@ __global__ void __launch_bounds__(THREADS, 3) kb_g2p2g(const MixedArgs *__restri
 // grid units: the weight of node i along one axis is the hat function
 // integrated over the point's extent [u - hl, u + hl], divided by 2 hl, with
 // derivative d/du; for hl <= 1/2 a point of fraction f in cell c touches the
-// nodes c-1 (f < hl), c, c+1 and c+2 (f > 1 - hl). One thread per material
-// point: G2P from the global grid, the same constitutive and position update
-// as the linear kernel, and P2G with global FP32 atomics (the points are
-// sorted by cell, so the atomics of a warp stay in a few cache lines).
-__device__ __forceinline__ void ugimp_1d(float d, float hl, float &w, float &g) {
-  // d = u - x_i; lin_integral / lin_integral_grad with w = 1, over 2 hl
-  const float a = fabsf(d), s = d >= 0.0f ? 1.0f : -1.0f, i2 = 0.5f / hl;
-  if (a >= 1.0f + hl) {
-    w = 0.0f;
-    g = 0.0f;
-  } else if (a >= 1.0f - hl) {
-    const float t = 1.0f + hl - a;
-    w = 0.5f * t * t * i2;
-    g = -s * t * i2;
-  } else if (a >= hl) {
-    w = 2.0f * hl * (1.0f - a) * i2;
-    g = -s * 2.0f * hl * i2;
-  } else {
-    w = (2.0f * hl - (hl * hl + a * a)) * i2;
-    g = -2.0f * d * i2;
-  }
-}
+// nodes c-1 (f < hl), c, c+1 and c+2 (f > 1 - hl). The kernel below walks
+// the same tiles and sorted cells as the linear one, with node windows one
+// node wider on each side.
 
-// Weights and derivatives of the nodes c-1 .. c+2 along one axis; false if a
-// node of non-zero weight lies outside 0 .. n (the reference's stencil would
-// leave its grid).
-__device__ __forceinline__ bool ugimp_axis(int c, float f, float hl, int n, float w[4],
-                                           float g[4]) {
+// Weights and derivatives along one axis of the three nodes b .. b+2 that
+// can carry weight when hl <= 1/2: b = c - 1 for f < 1/2 (node c+2 then has
+// none, |f - 2| >= 1 + hl) and b = c otherwise (node c-1 has none). Each
+// node's offset is f - k as in the reference's stencil over c-1 .. c+2.
+// False if a node of non-zero weight lies outside 0 .. n (the reference's
+// stencil would leave its grid).
+__device__ __forceinline__ bool ugimp_axis(int c, float f, float hl, int n, int &b, float w[3],
+                                           float g[3]) {
+  const int up = f >= 0.5f ? 1 : 0;
+  b = c - 1 + up;
+  // With a = |d|, d = u - x_i, and i2 = 1 / (2 hl) (lin_integral and
+  // lin_integral_grad with unit weight): w = 0 for a >= 1 + hl;
+  // w = (1 + hl - a)^2 i2 / 2, dw/du = -sign(d) (1 + hl - a) i2 for
+  // a >= 1 - hl; w = 2 hl (1 - a) i2, dw/du = -sign(d) 2 hl i2 for a >= hl;
+  // else w = (2 hl - (hl^2 + a^2)) i2, dw/du = -2 d i2. The middle node lies
+  // within 1/2 of the point and the outer two at least 1/2 away (>= hl), so
+  // each takes only the cases it can reach.
+  const float i2 = 0.5f / hl, h2 = 2.0f * hl;
+#pragma unroll
+  for (int m = 0; m < 3; m += 2) {
+    const float d = f - (float)(m - 1 + up);
+    const float a = fabsf(d), sg = d >= 0.0f ? 1.0f : -1.0f;
+    if (a >= 1.0f + hl) {
+      w[m] = 0.0f;
+      g[m] = 0.0f;
+    } else if (a >= 1.0f - hl) {
+      const float t = 1.0f + hl - a;
+      w[m] = 0.5f * t * t * i2;
+      g[m] = -sg * t * i2;
+    } else {
+      w[m] = h2 * (1.0f - a) * i2;
+      g[m] = -sg * h2 * i2;
+    }
+  }
+  {
+    const float d = f - (float)up;
+    const float a = fabsf(d), sg = d >= 0.0f ? 1.0f : -1.0f;
+    if (a >= hl) { // (at a = 1 - hl = hl = 1/2 the second case gives the same)
+      w[1] = h2 * (1.0f - a) * i2;
+      g[1] = -sg * h2 * i2;
+    } else {
+      w[1] = (h2 - (hl * hl + a * a)) * i2;
+      g[1] = -2.0f * d * i2;
+    }
+  }
   bool ok = true;
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    ugimp_1d(f - (float)(k - 1), hl, w[k], g[k]);
-    const int i = c + k - 1;
-    if ((w[k] != 0.0f || g[k] != 0.0f) && (i < 0 || i > n)) ok = false;
+  for (int m = 0; m < 3; ++m) {
+    const int i = b + m;
+    if ((w[m] != 0.0f || g[m] != 0.0f) && (i < 0 || i > n)) ok = false;
   }
   return ok;
 }
 
+// Node windows of the uGIMP kernel: a point of cell c reads and writes the
+// nodes c-1 .. c+2. G2P covers the cells [X0 - DRIFT, X0 + BIN + DRIFT) of a
+// tile with origin X0 (where its points are while they stay within DRIFT
+// cells of the cell they were sorted into), P2G one cell further (where those
+// points land after a step of less than a cell).
+constexpr int UVA_W = BIN + 2 * DRIFT + 3;
+constexpr int UACC_W = BIN + 2 * DRIFT + 5;
+
+struct UgimpSmem {
+  float4 va[UVA_W * UVA_W];
+  float acc[5][UACC_W * UACC_W];
+  unsigned out[2]; // left the tile window / left the sorted cell
+};
+
+// ugimp_tile expects the P2G window to be zero on entry (it leaves it zero).
+__device__ __forceinline__ void zero_uacc(UgimpSmem &S) {
+  float *a = &S.acc[0][0];
+  for (int k = threadIdx.x; k < 5 * UACC_W * UACC_W; k += THREADS) a[k] = 0.f;
+}
+
+// One tile with the uGIMP basis. One thread per cell of the tile walks the
+// points sorted into its cell, so at each stencil position the lanes of a
+// warp add to different nodes. G2P reads the shared copy of the grid window;
+// the point update is the linear kernel's; P2G adds to a shared node window
+// with shared-memory atomics, flushed to the global accumulators with one
+// atomic per touched node and field. Points outside the windows read and add
+// to the global grid (and count towards the next re-sort). Each point has its
+// own half-width (ResamplingTools.cpp:58-104 assigns them to inserted points).
 template <bool PRIME>
-__global__ void __launch_bounds__(THREADS) kxu_step(const __grid_constant__ MixedArgs A) {
-  const float hl = A.hl;
+__device__ __forceinline__ void ugimp_tile(const MixedArgs &A, const int bin, UgimpSmem &S) {
+  const int tid = threadIdx.x;
   const int row = A.nx + 1;
-  const int64_t nn = (int64_t)row * (A.ny + 1);
-  unsigned moved = 0;
+  [[maybe_unused]] const int64_t nn = (int64_t)row * (A.ny + 1); // bounds-checked builds
+  const int X0 = (bin % A.ntx) * BIN, Y0 = (bin / A.ntx) * BIN;
+  const int VX = X0 - DRIFT - 1, VY = Y0 - DRIFT - 1; // G2P window origin (node)
+  const int WX = X0 - DRIFT - 2, WY = Y0 - DRIFT - 2; // P2G window origin (node)
+  if (!PRIME) {
+    for (int k = tid; k < UVA_W * UVA_W; k += THREADS) {
+      const int ix = VX + k % UVA_W, iy = VY + k / UVA_W;
+      float4 val = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (ix >= 0 && iy >= 0 && ix <= A.nx && iy <= A.ny)
+        val = A.va[iy * row + ix]; // MIXED grids have < 2^30 nodes
+      S.va[k] = val;
+    }
+  }
+  if (tid < 2) S.out[tid] = 0;
+  int ps = A.offsets[bin * BIN_CELLS + tid];
+  int pe = A.offsets[bin * BIN_CELLS + tid + 1];
+  if (!HG_INDEX_OK(ps, (int64_t)A.n + 1, A.status) || !HG_INDEX_OK(pe, (int64_t)A.n + 1, A.status))
+    ps = pe = 0;
+  const int gcx = X0 + tid % BIN, gcy = Y0 + tid / BIN;
+  // Planes that can touch a point that starts in the G2P window and moves
+  // less than a cell, as in the linear kernel
+  unsigned plane_mask = 0;
+  for (int k = 0; k < A.nplanes; ++k) {
+    const MpmPlaneDev &pl = A.planes[k];
+    const float x0 = (float)(X0 - DRIFT - 1), y0 = (float)(Y0 - DRIFT - 1);
+    const float x1 = (float)(X0 + BIN + DRIFT + 2), y1 = (float)(Y0 + BIN + DRIFT + 2);
+    float dmin = fminf(fminf(pl.fn[0] * (x0 - pl.fux[0]) + pl.fn[1] * (y0 - pl.fux[1]),
+                             pl.fn[0] * (x1 - pl.fux[0]) + pl.fn[1] * (y0 - pl.fux[1])),
+                       fminf(pl.fn[0] * (x0 - pl.fux[0]) + pl.fn[1] * (y1 - pl.fux[1]),
+                             pl.fn[0] * (x1 - pl.fux[0]) + pl.fn[1] * (y1 - pl.fux[1])));
+    if (dmin <= 2.0f * A.pmargin && y1 >= pl.fulb - A.pmargin) plane_mask |= 1u << k;
+  }
+  __syncthreads();
+  unsigned left_window = 0, left_cell = 0;
   bool nonfinite = false;
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < A.n;
-       p += (int64_t)gridDim.x * blockDim.x) {
+  for (int p = ps; p < pe; ++p) {
     double2 un = A.u[p];
     const float2 mv = A.mv[p];
     float2 vel = A.v[p];
     float4 st = A.strain[p];
     const int fl = A.flags[p];
+    const float hl = A.hl[p];
     int jh = fl & 1;
     int cx, cy;
     float fx, fy;
@@ -786,27 +868,35 @@ __global__ void __launch_bounds__(THREADS) kxu_step(const __grid_constant__ Mixe
     split_u(un.y, cy, fy);
     far_edge(A.nx, cx, fx);
     far_edge(A.ny, cy, fy);
-    float wx[4], gx[4], wy[4], gy[4];
-    if (!in_grid_cell(A, cx, cy) || !ugimp_axis(cx, fx, hl, A.nx, wx, gx) ||
-        !ugimp_axis(cy, fy, hl, A.ny, wy, gy)) {
+    int bx, by;
+    float wx[3], gx[3], wy[3], gy[3];
+    if (!in_grid_cell(A, cx, cy) || !ugimp_axis(cx, fx, hl, A.nx, bx, wx, gx) ||
+        !ugimp_axis(cy, fy, hl, A.ny, by, wy, gy)) {
       atomicOr(A.status, (uint32_t)HG_STATUS_OUT_OF_GRID);
       continue;
     }
     int ncx = cx, ncy = cy;
-    float nfx = fx, nfy = fy;
     if (!PRIME) {
       // ---- G2P of this step at the start-of-step position ----
+      const bool in_window = cx - 1 - VX >= 0 && cy - 1 - VY >= 0 && cx + 2 - VX < UVA_W &&
+                             cy + 2 - VY < UVA_W;
       float Lxx = 0.f, Lxy = 0.f, Lyx = 0.f, Lyy = 0.f, vpx = 0.f, vpy = 0.f, apx = 0.f,
             apy = 0.f;
 #pragma unroll
-      for (int ky = 0; ky < 4; ++ky) {
-        if (wy[ky] == 0.0f && gy[ky] == 0.0f) continue;
+      for (int ky = 0; ky < 3; ++ky) {
 #pragma unroll
-        for (int kx = 0; kx < 4; ++kx) {
-          if (wx[kx] == 0.0f && gx[kx] == 0.0f) continue;
-          const int64_t node = (int64_t)(cy + ky - 1) * row + (cx + kx - 1);
-          if (!HG_INDEX_OK(node, nn, A.status)) continue;
-          const float4 nv = A.va[node];
+        for (int kx = 0; kx < 3; ++kx) {
+          float4 nv;
+          if (in_window) {
+            nv = S.va[(by - VY + ky) * UVA_W + bx - VX + kx];
+          } else {
+            // nodes of zero weight may lie outside the grid
+            if (wx[kx] == 0.0f && gx[kx] == 0.0f) continue;
+            if (wy[ky] == 0.0f && gy[ky] == 0.0f) continue;
+            const int64_t node = (int64_t)(by + ky) * row + (bx + kx);
+            if (!HG_INDEX_OK(node, nn, A.status)) continue;
+            nv = A.va[node];
+          }
           const float w = wx[kx] * wy[ky], dX = gx[kx] * wy[ky], dY = wx[kx] * gy[ky];
           Lxx += nv.x * dX;
           Lxy += nv.x * dY;
@@ -834,9 +924,18 @@ __global__ void __launch_bounds__(THREADS) kxu_step(const __grid_constant__ Mixe
       }
       un = make_double2(un.x + widen(dux), un.y + widen(duy));
       // MaterialPoints::resolvePlaneCollisions (MaterialPoints.cpp:371-423) in
-      // grid units, FP64 on the positions
-      for (int k = 0; k < A.nplanes; ++k) {
-        const MpmPlaneDev &pl = A.planes[k];
+      // grid units: FP32 test first, FP64 on the positions where the point is
+      // within pmargin cells of a plane. The tile's plane mask bounds points
+      // that start in the window and move less than a cell; any other point
+      // tests every plane.
+      const bool exact = !(fabsf(dux) < 1.0f && fabsf(duy) < 1.0f);
+      const unsigned pmask = (in_window && !exact) ? plane_mask : (1u << A.nplanes) - 1u;
+      const float ufx = ((float)cx + fx) + dux, ufy = ((float)cy + fy) + duy;
+      for (unsigned mk = pmask; mk; mk &= mk - 1) {
+        const MpmPlaneDev &pl = A.planes[__ffs(mk) - 1];
+        if (ufy < pl.fulb - A.pmargin) continue;
+        const float dapprox = pl.fn[0] * (ufx - pl.fux[0]) + pl.fn[1] * (ufy - pl.fux[1]);
+        if (dapprox > A.pmargin) continue;
         if (un.y < pl.ulb) continue;
         const double d = plane_distance_u(pl, un.x, un.y);
         if (d > 0.0) continue;
@@ -851,6 +950,7 @@ __global__ void __launch_bounds__(THREADS) kxu_step(const __grid_constant__ Mixe
           vel = make_float2(0.0f, 0.0f);
         }
       }
+      float nfx, nfy;
       split_u(un.x, ncx, nfx);
       split_u(un.y, ncy, nfy);
       far_edge(A.nx, ncx, nfx);
@@ -861,9 +961,14 @@ __global__ void __launch_bounds__(THREADS) kxu_step(const __grid_constant__ Mixe
       A.v[p] = vel;
       A.strain[p] = st;
       A.flags[p] = (uint8_t)((fl & ~1) | jh);
-      moved += (ncx != cx) | (ncy != cy);
-      if (!in_grid_cell(A, ncx, ncy) || !ugimp_axis(ncx, nfx, hl, A.nx, wx, gx) ||
-          !ugimp_axis(ncy, nfy, hl, A.ny, wy, gy)) {
+      if ((ncx != gcx) | (ncy != gcy)) {
+        ++left_cell;
+        // the next step's G2P window
+        left_window += (ncx - 1 - VX < 0) | (ncy - 1 - VY < 0) | (ncx + 2 - VX >= UVA_W) |
+                       (ncy + 2 - VY >= UVA_W);
+      }
+      if (!in_grid_cell(A, ncx, ncy) || !ugimp_axis(ncx, nfx, hl, A.nx, bx, wx, gx) ||
+          !ugimp_axis(ncy, nfy, hl, A.ny, by, wy, gy)) {
         atomicOr(A.status, (uint32_t)HG_STATUS_OUT_OF_GRID);
         continue;
       }
@@ -872,30 +977,74 @@ __global__ void __launch_bounds__(THREADS) kxu_step(const __grid_constant__ Mixe
     float s00, s01, s11;
     stress_factor(st, jh, mv.y, A.inv_h, A.kappa, A.mu, s00, s01, s11);
     const float mvx = mv.x * vel.x, mvy = mv.x * vel.y;
+    const bool in_acc = ncx - 1 - WX >= 0 && ncy - 1 - WY >= 0 && ncx + 2 - WX < UACC_W &&
+                        ncy + 2 - WY < UACC_W;
 #pragma unroll
-    for (int ky = 0; ky < 4; ++ky) {
-      if (wy[ky] == 0.0f && gy[ky] == 0.0f) continue;
+    for (int ky = 0; ky < 3; ++ky) {
 #pragma unroll
-      for (int kx = 0; kx < 4; ++kx) {
-        if (wx[kx] == 0.0f && gx[kx] == 0.0f) continue;
-        const int64_t node = (int64_t)(ncy + ky - 1) * row + (ncx + kx - 1);
-        if (!HG_INDEX_OK(node, nn, A.status)) continue;
+      for (int kx = 0; kx < 3; ++kx) {
         const float w = wx[kx] * wy[ky];
+        const float dX = gx[kx] * wy[ky], dY = wx[kx] * gy[ky];
+        if (w == 0.0f && dX == 0.0f && dY == 0.0f) continue; // outside the support
         float4 add = make_float4(w * mvx, w * mvy, 0.0f, 0.0f);
         if (w != 0.0f) { // nodes of zero weight get no force (PhysicsGrid.cpp:439-441)
-          const float dX = gx[kx] * wy[ky], dY = wx[kx] * gy[ky];
           add.z = s00 * dX + s01 * dY;
           add.w = s01 * dX + s11 * dY;
         }
-        atomicAdd(&A.accm[node], w * mv.x);
-        atomicAdd(&A.acc4[node], add);
+        if (in_acc) {
+          const int k = (by - WY + ky) * UACC_W + bx - WX + kx;
+          atomicAdd(&S.acc[0][k], w * mv.x);
+          atomicAdd(&S.acc[1][k], add.x);
+          atomicAdd(&S.acc[2][k], add.y);
+          atomicAdd(&S.acc[3][k], add.z);
+          atomicAdd(&S.acc[4][k], add.w);
+        } else {
+          const int64_t node = (int64_t)(by + ky) * row + (bx + kx);
+          if (!HG_INDEX_OK(node, nn, A.status)) continue;
+          atomicAdd(&A.accm[node], w * mv.x);
+          atomicAdd(&A.acc4[node], add);
+        }
       }
     }
   }
   if (nonfinite) atomicOr(A.status, (uint32_t)HG_STATUS_NONFINITE);
-  // points that changed cell: the re-sort trigger of the linear kernel
-  for (int o = 16; o > 0; o >>= 1) moved += __shfl_down_sync(0xffffffffu, moved, o);
-  if ((threadIdx.x & 31) == 0 && moved) atomicAdd(&A.outside[1], moved);
+  if (left_window) atomicAdd(&S.out[0], left_window);
+  if (left_cell) atomicAdd(&S.out[1], left_cell);
+  __syncthreads();
+  // ---- the node window, flushed to the global accumulators ----
+  for (int k = tid; k < UACC_W * UACC_W; k += THREADS) {
+    float sum[5];
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      sum[c] = S.acc[c][k];
+      S.acc[c][k] = 0.f; // ready for the next tile
+    }
+    if (sum[0] == 0.f && sum[1] == 0.f && sum[2] == 0.f && sum[3] == 0.f && sum[4] == 0.f)
+      continue;
+    const int ix = WX + k % UACC_W, iy = WY + k / UACC_W;
+    if (ix < 0 || iy < 0 || ix > A.nx || iy > A.ny) continue;
+    const int node = iy * row + ix;
+    atomicAdd(&A.accm[node], sum[0]);
+    atomicAdd(&A.acc4[node], make_float4(sum[1], sum[2], sum[3], sum[4]));
+  }
+  __syncthreads();
+  if (tid < 2 && S.out[tid]) atomicAdd(&A.outside[tid], S.out[tid]);
+}
+
+template <bool PRIME>
+__global__ void __launch_bounds__(THREADS, 3) kxu_g2p2g(const __grid_constant__ MixedArgs A) {
+  __shared__ UgimpSmem S;
+  zero_uacc(S);
+  // launched with programmatic dependence on the grid update before it: only
+  // shared memory is touched before the wait
+  pdl_wait();
+  pdl_trigger();
+  const int nact = *A.nactive;
+  for (int t = blockIdx.x; t < nact; t += gridDim.x) {
+    const int tile = A.active[t];
+    if (!HG_INDEX_OK(tile, (int64_t)A.ntx * A.nty, A.status)) continue;
+    ugimp_tile<PRIME>(A, tile, S);
+  }
 }
 
 // Node update of one tile; one thread per node of the 16x16 tile.
@@ -1014,6 +1163,7 @@ __global__ void kx_scatter(int64_t n, const int32_t *__restrict__ keys,
   dst.strain[d] = src.strain[p];
   dst.flags[d] = src.flags[p];
   dst.id[d] = src.id[p];
+  if (src.hl) dst.hl[d] = src.hl[p];
 }
 
 __global__ void kx_active(int ntx, int nty, const int32_t *__restrict__ offsets,
@@ -1191,6 +1341,7 @@ __global__ void kr_scatter(const RebinArgs *__restrict__ R, RebinPrefix P) {
     a.dst.strain[d] = a.src.strain[p];
     a.dst.flags[d] = a.src.flags[p];
     a.dst.id[d] = a.src.id[p];
+    if (a.src.hl) a.dst.hl[d] = a.src.hl[p];
   }
 }
 
@@ -1224,11 +1375,12 @@ __global__ void kr_active(const RebinArgs *__restrict__ R, RebinPrefix P) {
 __global__ void kx_upload(int64_t n, double gx, double gy, double h,
                           const double *__restrict__ q, const double *__restrict__ v,
                           const double *__restrict__ m, const double *__restrict__ vol,
-                          const double *__restrict__ be, const double *__restrict__ J,
-                          const int32_t *__restrict__ jh, const uint8_t *__restrict__ kin,
-                          MixedParticles dst) {
+                          const double *__restrict__ hl, const double *__restrict__ be,
+                          const double *__restrict__ J, const int32_t *__restrict__ jh,
+                          const uint8_t *__restrict__ kin, MixedParticles dst) {
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (p >= n) return;
+  if (dst.hl) dst.hl[p] = (float)(hl[p] / h);
   dst.u[p] = make_double2((q[2 * p] - gx) / h, (q[2 * p + 1] - gy) / h);
   dst.v[p] = make_float2((float)v[2 * p], (float)v[2 * p + 1]);
   dst.mv[p] = make_float2((float)m[p], (float)vol[p]);
@@ -1283,6 +1435,7 @@ MixedParticles parts(hg_mpm *m, int which) {
   P.strain = m->mstrain_[which].p;
   P.flags = m->mflags_[which].p;
   P.id = m->mid_[which].p;
+  P.hl = m->mhl_[which].p; // nullptr for the linear basis
   return P;
 }
 
@@ -1308,7 +1461,6 @@ MixedArgs make_args(hg_mpm *m, double dt, bool tiles) {
   A.gx = (float)P.g[0];
   A.gy = (float)P.g[1];
   A.pmargin = 0.01f + 4.0e-7f * (float)(P.nx + P.ny);
-  A.hl = P.basis == HG_BASIS_UGIMP ? m->hl_cells : 0.0f;
   A.nplanes = P.nplanes;
   for (int k = 0; k < HG_MAX_PLANES; ++k) A.planes[k] = P.planes[k];
   A.offsets = m->offsets.p;
@@ -1320,6 +1472,7 @@ MixedArgs make_args(hg_mpm *m, double dt, bool tiles) {
   A.mv = cur.mv;
   A.strain = cur.strain;
   A.flags = cur.flags;
+  A.hl = cur.hl;
   A.va = m->va.p;
   A.va_out = m->va.p;
   A.acc4 = m->acc4.p;
@@ -1445,16 +1598,11 @@ int update_per_sm(const hg_launch_shape &s) {
   return s.update_ctas_per_sm > 0 ? s.update_ctas_per_sm : DEFAULT_UPDATE_CTAS;
 }
 int fused_blocks(hg_mpm *m) { return m->ctx->num_sms * fused_per_sm(m->shape); }
-// the uGIMP kernel walks the points: up to 8 CTAs per SM
-int ugimp_blocks(hg_mpm *m) {
-  const int64_t b = (m->n + THREADS - 1) / THREADS;
-  return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)m->ctx->num_sms * 8));
-}
 // G2P of this step fused with P2G of the next (or the first P2G, PRIME)
 template <bool PRIME>
 void launch_particle_kernel(hg_mpm *m, const MixedArgs &A, cudaStream_t s) {
   if (m->p.basis == HG_BASIS_UGIMP) {
-    HG_LAUNCH(kxu_step<PRIME>, ugimp_blocks(m), THREADS, 0, s, A);
+    HG_LAUNCH_PDL(kxu_g2p2g<PRIME>, fused_blocks(m), THREADS, 0, s, A);
   } else {
     HG_LAUNCH_PDL(kx_g2p2g<PRIME>, fused_blocks(m), THREADS, fused_smem_bytes(), s, A);
   }
@@ -1532,6 +1680,7 @@ hg_status mixed_alloc(hg_mpm *m) {
         (st = m->mmv_[b].alloc(m->cap)) || (st = m->mstrain_[b].alloc(m->cap)) ||
         (st = m->mflags_[b].alloc(m->cap)) || (st = m->mid_[b].alloc(m->cap)))
       return st;
+    if (m->p.basis == HG_BASIS_UGIMP && (st = m->mhl_[b].alloc(m->cap))) return st;
   }
   hg_status st;
   if ((st = m->acc4.alloc(nn)) || (st = m->accm.alloc(nn)) || (st = m->va.alloc(nn)) ||
@@ -1568,13 +1717,15 @@ int64_t mixed_device_bytes(int nx, int ny, int64_t cap) {
 }
 
 hg_status mixed_upload(hg_mpm *m, const double *q, const double *v, const double *mass,
-                       const double *vol, const double *be, const double *J,
+                       const double *vol, const double *hl, const double *be, const double *J,
                        const int32_t *jh, const uint8_t *kin) {
   cudaStream_t s = m->ctx->stream;
   const int64_t n = m->n;
+  if (m->p.basis == HG_BASIS_UGIMP && n > 0 && !hl)
+    return fail(HG_ERR_INVALID_ARGUMENT, "the uGIMP basis needs the half-widths hl");
   if (n > 0) {
     HG_LAUNCH(kx_upload, blocks_for(n, 256), 256, 0, s, n, m->p.gmin[0], m->p.gmin[1], m->p.h,
-              q, v, mass, vol, be, J, jh, kin, parts(m, m->cur));
+              q, v, mass, vol, hl, be, J, jh, kin, parts(m, m->cur));
     HG_CHECK_LAUNCH();
   }
   return prime(m);

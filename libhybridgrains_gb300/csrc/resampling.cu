@@ -28,6 +28,8 @@
 #include "zones_internal.cuh"
 
 #include <algorithm>
+#include <array>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -72,40 +74,52 @@ inline double dist2d(double ax, double ay, double bx, double by) {
   return std::sqrt(dx * dx + dy * dy);
 }
 
-// CUniformGridH2D (uniformgrid.cpp) with growable per-cell id lists.
+// CUniformGridH2D (uniformgrid.cpp) with points registered by the cell that
+// holds them: per-cell id lists in CSR form, each in increasing id order (the
+// order in which the reference appends them).
 struct CellLists {
   double mn[2] = {0, 0}, cw = 1.0;
   unsigned res[2] = {1, 1};
-  std::vector<std::vector<int>> ids;
+  std::vector<int> start, ids;
+  struct Span {
+    const int *b, *e;
+    const int *begin() const { return b; }
+    const int *end() const { return e; }
+    size_t size() const { return (size_t)(e - b); }
+  };
   void reset(double x0, double y0, unsigned rx, unsigned ry, double w) {
     mn[0] = x0;
     mn[1] = y0;
     res[0] = std::max(rx, 1u);
     res[1] = std::max(ry, 1u);
     cw = w;
-    ids.assign((size_t)res[0] * res[1], {});
+    start.assign((size_t)res[0] * res[1] + 1, 0);
+    ids.clear();
   }
   void cell(double x, double y, unsigned &i, unsigned &j) const {
     const double u = (x - mn[0]) / cw, v = (y - mn[1]) / cw;
     i = (unsigned)std::max<int>(0, std::min<int>((int)res[0] - 1, (int)std::floor(u)));
     j = (unsigned)std::max<int>(0, std::min<int>((int)res[1] - 1, (int)std::floor(v)));
   }
-  void add_box(double x0, double y0, double x1, double y1, int id) {
-    unsigned i0, j0, i1, j1;
-    cell(x0, y0, i0, j0);
-    cell(x1, y1, i1, j1);
-    for (unsigned j = j0; j <= j1; ++j)
-      for (unsigned i = i0; i <= i1; ++i) ids[(size_t)j * res[0] + i].push_back(id);
+  // n points at xy[stride k], xy[stride k + 1] with ids 0 .. n-1 (a counting
+  // sort by cell, stable in id order)
+  void add_points(const double *xy, int stride, size_t n) {
+    std::vector<int> c(n);
+    for (size_t k = 0; k < n; ++k) {
+      unsigned i, j;
+      cell(xy[stride * k], xy[stride * k + 1], i, j);
+      c[k] = (int)((size_t)j * res[0] + i);
+      start[c[k] + 1]++;
+    }
+    for (size_t q = 0; q + 1 < start.size(); ++q) start[q + 1] += start[q];
+    ids.assign(n, 0);
+    std::vector<int> fill(start.begin(), start.end() - 1);
+    for (size_t k = 0; k < n; ++k) ids[fill[c[k]]++] = (int)k;
   }
-  void add_point(double x, double y, int id) {
-    unsigned i, j;
-    cell(x, y, i, j);
-    ids[(size_t)j * res[0] + i].push_back(id);
-  }
-  const std::vector<int> &at(unsigned i, unsigned j) const {
-    static const std::vector<int> none;
-    if (i >= res[0] || j >= res[1]) return none;
-    return ids[(size_t)j * res[0] + i];
+  Span at(unsigned i, unsigned j) const {
+    if (i >= res[0] || j >= res[1]) return Span{nullptr, nullptr};
+    const size_t c = (size_t)j * res[0] + i;
+    return Span{ids.data() + start[c], ids.data() + start[c + 1]};
   }
 };
 
@@ -138,11 +152,91 @@ using Box = hg_zones::Box;
 size_t npoints(const hg_resampler &r) { return r.m.size(); }
 size_t nbodies(const hg_resampler &r) { return r.dr.size(); }
 
+// Candidate search of fill_regions. A sample conflicts with a body when
+// their centres are closer than 0.97 (r_body + r_sample); whether one does
+// is all the reference's search (AvoidAvoid.cpp:133-165, bodies registered in
+// every cell their boxes cover, each tested once per sample) decides, so any
+// search that reaches every body within that distance decides the same.
+// Bodies of radius at most cw / 2 are kept by the cell of their centre: the
+// ones present at the start contiguously per cell (centre and radius
+// inline), the samples accepted since in per-cell lists. A body within
+// conflict distance of a sample of radius r lies within 0.97 (cw / 2 + r) of
+// it, so the cells within ceil((cw / 2 + r) / cw) of the sample's hold it
+// (the 3 x 3 around it when r <= cw / 2). Wider bodies are tested by every
+// sample. Squared distances decide outside a 1e-12 relative band around the
+// limit; inside it the reference's expression sqrt(dx^2 + dy^2) < 0.97
+// (r_body + r) does, on the same dx and dy.
+inline bool conflicts(double bx, double by, double br, double x, double y, double r) {
+  const double dx = bx - x, dy = by - y;
+  const double d2 = dx * dx + dy * dy, lim = (br + r) * 0.97, l2 = lim * lim;
+  if (d2 > l2 * (1.0 + 1.0e-12)) return false;
+  if (d2 < l2 * (1.0 - 1.0e-12)) return true;
+  return dist2d(bx, by, x, y) < lim;
+}
+
+struct FillGrid {
+  double x0 = 0, y0 = 0, cw = 1;
+  int nx = 1, ny = 1;
+  std::vector<int> start;              // per cell, into the initial bodies
+  std::vector<double> bx, by, br;      // initial bodies in cell order
+  std::vector<double> ix, iy, ir;      // initial bodies wider than cw / 2
+  std::vector<int> head, next;         // samples accepted since: per-cell lists
+  std::vector<double> sx, sy, sr;
+  std::vector<double> wx, wy, wr;      // accepted samples wider than cw / 2
+  int cx(double x) const { return std::max(0, std::min(nx - 1, (int)std::floor((x - x0) / cw))); }
+  int cy(double y) const { return std::max(0, std::min(ny - 1, (int)std::floor((y - y0) / cw))); }
+  void add_sample(double x, double y, double r) {
+    if (r > 0.5 * cw) {
+      wx.push_back(x);
+      wy.push_back(y);
+      wr.push_back(r);
+      return;
+    }
+    const int c = cy(y) * nx + cx(x);
+    next.push_back(head[c]);
+    head[c] = (int)sx.size();
+    sx.push_back(x);
+    sy.push_back(y);
+    sr.push_back(r);
+  }
+  // the cells a body within conflict distance of (x, y, r) can be in
+  template <typename F>
+  bool any_cell(double x, double y, double r, F f) const {
+    const int reach = (int)std::ceil((0.5 * cw + r) / cw);
+    const int i = cx(x), j = cy(y);
+    const int i0 = std::max(0, i - reach), i1 = std::min(nx - 1, i + reach);
+    const int j0 = std::max(0, j - reach), j1 = std::min(ny - 1, j + reach);
+    for (int jj = j0; jj <= j1; ++jj)
+      for (int ii = i0; ii <= i1; ++ii)
+        if (f(jj * nx + ii)) return true;
+    return false;
+  }
+  bool conflict_initial(double x, double y, double r) const {
+    for (size_t k = 0; k < ix.size(); ++k)
+      if (conflicts(ix[k], iy[k], ir[k], x, y, r)) return true;
+    return any_cell(x, y, r, [&](int c) {
+      for (int k = start[c]; k < start[c + 1]; ++k)
+        if (conflicts(bx[k], by[k], br[k], x, y, r)) return true;
+      return false;
+    });
+  }
+  bool conflict_accepted(double x, double y, double r) const {
+    for (size_t k = 0; k < wx.size(); ++k)
+      if (conflicts(wx[k], wy[k], wr[k], x, y, r)) return true;
+    return any_cell(x, y, r, [&](int c) {
+      for (int k = head[c]; k >= 0; k = next[k])
+        if (conflicts(sx[k], sy[k], sr[k], x, y, r)) return true;
+      return false;
+    });
+  }
+};
+
 // CAvoidAVoid::avoidAVoid with randomFillRegion (AvoidAvoid.cpp:103-183):
-// bodies (px, py, rad) grow by the accepted samples.
+// bodies (px, py, rad) grow by the accepted samples, whose radii are at most
+// r_max.
 template <typename Sampler>
 hg_status fill_regions(hg_resampler &R, const std::vector<Box> &regions, double mean_r,
-                       std::vector<double> &px, std::vector<double> &py,
+                       double r_max, std::vector<double> &px, std::vector<double> &py,
                        std::vector<double> &rad, Sampler sampler) {
   if (regions.empty()) return HG_OK;
   double lo[2] = {regions[0].b[0], regions[0].b[1]}, up[2] = {regions[0].b[2], regions[0].b[3]};
@@ -154,58 +248,83 @@ hg_status fill_regions(hg_resampler &R, const std::vector<Box> &regions, double 
   }
   const double g0x = lo[0] - 6.0 * mean_r, g0y = lo[1] - 6.0 * mean_r;
   const double g1x = up[0] + 6.0 * mean_r, g1y = up[1] + 6.0 * mean_r;
-  const double cw = 4.0 * mean_r;
-  CellLists grid;
-  grid.reset(g0x, g0y, (unsigned)std::ceil((g1x - g0x) / cw), (unsigned)std::ceil((g1y - g0y) / cw),
-             cw);
-  std::vector<int> mail(px.size(), 0);
+  // cells twice the largest radius of the samples and of the bodies up to
+  // four mean radii (wider ones go to the list every sample scans)
+  double rc = r_max;
+  for (size_t b = 0; b < px.size(); ++b)
+    if (rad[b] > rc && rad[b] <= 4.0 * mean_r) rc = rad[b];
+  FillGrid grid;
+  grid.x0 = g0x;
+  grid.y0 = g0y;
+  grid.cw = 2.0 * rc;
+  grid.nx = std::max(1, (int)std::ceil((g1x - g0x) / grid.cw));
+  grid.ny = std::max(1, (int)std::ceil((g1y - g0y) / grid.cw));
+  const size_t ncell = (size_t)grid.nx * grid.ny;
+  // counting sort of the initial bodies by the cell of their centre. A body
+  // wholly outside the grid's extent cannot conflict with a sample (samples
+  // lie in the regions, six mean radii inside that extent); the reference's
+  // grid leaves it out too.
+  std::vector<int> cell_of(px.size(), -1);
+  grid.start.assign(ncell + 1, 0);
   for (size_t b = 0; b < px.size(); ++b) {
-    // A body wholly outside the grid's extent cannot conflict with a sample
-    // (samples lie in the regions, six mean radii inside that extent, and
-    // conflicts need centres closer than the two radii); left in, it would
-    // pile up in the clamped edge cells that every nearby test scans.
     if (px[b] + rad[b] < g0x || px[b] - rad[b] > g1x || py[b] + rad[b] < g0y ||
         py[b] - rad[b] > g1y)
       continue;
-    grid.add_box(px[b] - rad[b], py[b] - rad[b], px[b] + rad[b], py[b] + rad[b], (int)b);
+    if (rad[b] > 0.5 * grid.cw) {
+      grid.ix.push_back(px[b]);
+      grid.iy.push_back(py[b]);
+      grid.ir.push_back(rad[b]);
+      continue;
+    }
+    cell_of[b] = grid.cy(py[b]) * grid.nx + grid.cx(px[b]);
+    grid.start[cell_of[b] + 1]++;
   }
-  auto next_test = [&]() {
-    if (++R.test_id == 0) R.test_id = 1;
-  };
-  auto conflict = [&](double x, double y, double r) {
-    const int t = R.test_id;
-    unsigned i0, j0, i1, j1;
-    grid.cell(x - r, y - r, i0, j0);
-    grid.cell(x + r, y + r, i1, j1);
-    for (unsigned j = j0; j <= j1; ++j)
-      for (unsigned i = i0; i <= i1; ++i)
-        for (int id : grid.at(i, j)) {
-          if (mail[id] == t) continue;
-          mail[id] = t;
-          if (dist2d(px[id], py[id], x, y) < (rad[id] + r) * 0.97) {
-            next_test();
-            return true;
-          }
-        }
-    next_test();
-    return false;
-  };
+  for (size_t c = 0; c < ncell; ++c) grid.start[c + 1] += grid.start[c];
+  const int nb = grid.start[ncell];
+  grid.bx.resize(nb);
+  grid.by.resize(nb);
+  grid.br.resize(nb);
+  {
+    std::vector<int> fill(grid.start.begin(), grid.start.end() - 1);
+    for (size_t b = 0; b < px.size(); ++b) {
+      if (cell_of[b] < 0) continue;
+      const int k = fill[cell_of[b]]++;
+      grid.bx[k] = px[b];
+      grid.by[k] = py[b];
+      grid.br[k] = rad[b];
+    }
+  }
+  grid.head.assign(ncell, -1);
+  // 16 trials per region in the reference's order. Neither the positions
+  // (R.mt) nor the radii (the sampler's own engine) depend on which trials
+  // are accepted, so all are drawn first. A trial is accepted when it
+  // conflicts neither with the bodies present at the start (tested for all
+  // trials at once, over host threads) nor with the trials accepted before
+  // it (tested in trial order).
+  const size_t T = 16 * regions.size();
+  std::vector<double> tx(T), ty(T), tr(T);
+  size_t t = 0;
   for (const Box &reg : regions) {
     const double dx = reg.b[2] - reg.b[0], dy = reg.b[3] - reg.b[1];
-    for (int trial = 0; trial < 16; ++trial) {
-      const double x = (double)R.mt.uniform() * dx + reg.b[0];
-      const double y = (double)R.mt.uniform() * dy + reg.b[1];
-      double r;
-      const hg_status st = sampler(r);
+    for (int trial = 0; trial < 16; ++trial, ++t) {
+      tx[t] = (double)R.mt.uniform() * dx + reg.b[0];
+      ty[t] = (double)R.mt.uniform() * dy + reg.b[1];
+      const hg_status st = sampler(tr[t]);
       if (st != HG_OK) return st;
-      if (conflict(x, y, r)) continue;
-      const int id = (int)px.size();
-      px.push_back(x);
-      py.push_back(y);
-      rad.push_back(r);
-      mail.push_back(0);
-      grid.add_box(x - r, y - r, x + r, y + r, id);
     }
+  }
+  std::vector<uint8_t> hit(T);
+  hg::host_parallel(T, 4096, [&](size_t b, size_t e) {
+    for (size_t k = b; k < e; ++k) hit[k] = grid.conflict_initial(tx[k], ty[k], tr[k]) ? 1 : 0;
+  });
+  for (size_t k = 0; k < T; ++k) {
+    // the reference's mailbox stamp advances once per test
+    if (++R.test_id == 0) R.test_id = 1;
+    if (hit[k] || grid.conflict_accepted(tx[k], ty[k], tr[k])) continue;
+    px.push_back(tx[k]);
+    py.push_back(ty[k]);
+    rad.push_back(tr[k]);
+    grid.add_sample(tx[k], ty[k], tr[k]);
   }
   return HG_OK;
 }
@@ -221,7 +340,7 @@ hg_status insert_points(hg_resampler &R, const std::vector<Box> &zones, int64_t 
     px[p] = R.q[2 * p];
     py[p] = R.q[2 * p + 1];
   }
-  const hg_status st = fill_regions(R, zones, rp, px, py, rad, [&](double &r) -> hg_status {
+  const hg_status st = fill_regions(R, zones, rp, rp, px, py, rad, [&](double &r) -> hg_status {
     r = rp;
     return HG_OK;
   });
@@ -269,7 +388,9 @@ hg_status insert_grains(hg_resampler &R, const std::vector<Box> &zones, int64_t 
     R.radius_dist = std::normal_distribution<double>(rad[0], 0.0);
     unset = true;
   }
-  const hg_status st = fill_regions(R, zones, r_mean, px, py, rad, [&](double &r) -> hg_status {
+  const double r_max = unset ? rad[0] : hi;
+  const hg_status st = fill_regions(R, zones, r_mean, r_max, px, py, rad,
+                                   [&](double &r) -> hg_status {
     if (unset) {
       // the reference's rejection bounds stay at the unset mean and would
       // never accept: take the sampled radius as is
@@ -310,8 +431,8 @@ void point_grids(const hg_resampler &R, CellLists &cont, CellLists &disc) {
              zd.mpm_cell_width);
   disc.reset(zd.mpm_grid_min[0], zd.mpm_grid_min[1], zd.mpm_cells[0], zd.mpm_cells[1],
              zd.mpm_cell_width);
-  for (size_t p = 0; p < npoints(R); ++p) cont.add_point(R.q[2 * p], R.q[2 * p + 1], (int)p);
-  for (size_t b = 0; b < nbodies(R); ++b) disc.add_point(R.dq[3 * b], R.dq[3 * b + 1], (int)b);
+  cont.add_points(R.q.data(), 2, npoints(R));
+  disc.add_points(R.dq.data(), 3, nbodies(R));
 }
 
 template <typename F>
@@ -380,7 +501,7 @@ void hybrid_point_quantities(hg_resampler &R, const std::vector<Box> &zones, int
   const double cell_volume = zd.mpm_cell_width * zd.mpm_cell_width;
   const double mass_per_cell = R.d.material_density * cell_volume;
   for (const Box &z : zones) {
-    const std::vector<int> &ids = cont.at((unsigned)z.c[0], (unsigned)z.c[1]);
+    const CellLists::Span ids = cont.at((unsigned)z.c[0], (unsigned)z.c[1]);
     const int n = (int)ids.size();
     for (int id : ids) {
       R.m0[id] = mass_per_cell / n;
@@ -390,7 +511,10 @@ void hybrid_point_quantities(hg_resampler &R, const std::vector<Box> &zones, int
   const double size = R.d.initial_particle_size;
   const double sigma = 0.5 * size, max_dist = 3.0 * size;
   const double hh = zd.mpm_cell_width * 0.25;
-  for (int64_t p = before; p < after; ++p) {
+  // each inserted point reads only the points and grains that were there
+  // before the insertion and writes only its own entries: over host threads
+  hg::host_parallel((size_t)(after - before), 256, [&](size_t pb, size_t pe) {
+  for (int64_t p = before + (int64_t)pb; p < before + (int64_t)pe; ++p) {
     const double x = R.q[2 * p], y = R.q[2 * p + 1];
     double vs[2] = {0, 0}, q0s[2] = {0, 0}, Js = 0.0, bes[4] = {0, 0, 0, 0}, ws = 0.0;
     int nn = 0;
@@ -461,13 +585,17 @@ void hybrid_point_quantities(hg_resampler &R, const std::vector<Box> &zones, int
     }
     for (int c = 0; c < 4; ++c) R.be[4 * p + c] = ben[c];
   }
+  });
 }
 
 // determineDEMQuantitiesForHybridZones (ResamplingTools.cpp:646-725)
 void grain_quantities(hg_resampler &R, int64_t before, int64_t after, int64_t points_before,
                       const CellLists &cont, const CellLists &disc) {
   const double sigma = R.d.dem_r_mean, max_dist = 6.0 * R.d.dem_r_mean;
-  for (int64_t b = before; b < after; ++b) {
+  // each inserted grain reads only the bodies and points there before the
+  // insertion: over host threads
+  hg::host_parallel((size_t)(after - before), 256, [&](size_t gb, size_t ge) {
+  for (int64_t b = before + (int64_t)gb; b < before + (int64_t)ge; ++b) {
     const double x = R.dq[3 * b], y = R.dq[3 * b + 1];
     double vs[3] = {0, 0, 0}, q0s[3] = {0, 0, 0}, ws = 0.0;
     for_range(disc, x - max_dist, y - max_dist, x + max_dist, y + max_dist, [&](int id) {
@@ -508,6 +636,7 @@ void grain_quantities(hg_resampler &R, int64_t before, int64_t after, int64_t po
       }
     }
   }
+  });
 }
 
 // Mass-weighted node fields of the first n points (Grid::rasterizeMass +
@@ -530,37 +659,55 @@ void mass_weighted_fields(const hg_resampler &R, int64_t n, NodeField *f, int nf
   std::vector<double> mass(nn, 0.0);
   for (int k = 0; k < nf; ++k) f[k].out->assign(nn * f[k].len, 0.0);
   const double h1 = R.hl.empty() ? 0.0 : R.hl[0];
-  for (int64_t p = 0; p < n; ++p) {
-    const double x = R.q[2 * p], y = R.q[2 * p + 1];
-    int x0, y0, x1, y1, i0, i1, j0, j1;
-    hg::stencil64(R.d.basis, x, y, h1, zd.mpm_grid_min[0], zd.mpm_grid_min[1], R.grid_h, x0, y0,
-                  x1, y1);
-    if (!stencil_range(y0, y1, ny, j0, j1) || !stencil_range(x0, x1, nx, i0, i1)) continue;
-    for (int iy = j0; iy <= j1; ++iy)
-      for (int ix = i0; ix <= i1; ++ix) {
-        const double wgt = hg::weight64(R.d.basis, x, y, h1, ix, iy, zd.mpm_grid_min[0],
-                                        zd.mpm_grid_min[1], R.grid_h);
-        const size_t node = (size_t)iy * (nx + 1) + ix;
-        mass[node] += wgt * R.m[p];
-        for (int k = 0; k < nf; ++k) {
-          const int len = f[k].len;
-          const double *v = f[k].vals->data() + (size_t)p * len;
-          double *o = f[k].out->data() + node * len;
-          for (int c = 0; c < len; ++c) o[c] += wgt * R.m[p] * v[c];
+  // the node range of every point's stencil (empty: j0 > j1)
+  std::vector<std::array<int, 4>> range((size_t)n);
+  hg::host_parallel((size_t)n, 4096, [&](size_t b, size_t e) {
+    for (size_t p = b; p < e; ++p) {
+      int x0, y0, x1, y1, i0, i1, j0, j1;
+      hg::stencil64(R.d.basis, R.q[2 * p], R.q[2 * p + 1], h1, zd.mpm_grid_min[0],
+                    zd.mpm_grid_min[1], R.grid_h, x0, y0, x1, y1);
+      if (!stencil_range(y0, y1, ny, j0, j1) || !stencil_range(x0, x1, nx, i0, i1))
+        range[p] = {0, -1, 0, -1};
+      else
+        range[p] = {i0, i1, j0, j1};
+    }
+  });
+  // node rows split over host threads; each thread walks the points in
+  // order, so every node sums its points in the reference's order
+  hg::host_parallel((size_t)ny + 1, 4, [&](size_t rb, size_t re) {
+    for (int64_t p = 0; p < n; ++p) {
+      const std::array<int, 4> &r = range[p];
+      const int j0 = std::max(r[2], (int)rb), j1 = std::min(r[3], (int)re - 1);
+      if (j0 > j1) continue;
+      const double x = R.q[2 * p], y = R.q[2 * p + 1];
+      for (int iy = j0; iy <= j1; ++iy)
+        for (int ix = r[0]; ix <= r[1]; ++ix) {
+          const double wgt = hg::weight64(R.d.basis, x, y, h1, ix, iy, zd.mpm_grid_min[0],
+                                          zd.mpm_grid_min[1], R.grid_h);
+          const size_t node = (size_t)iy * (nx + 1) + ix;
+          mass[node] += wgt * R.m[p];
+          for (int k = 0; k < nf; ++k) {
+            const int len = f[k].len;
+            const double *v = f[k].vals->data() + (size_t)p * len;
+            double *o = f[k].out->data() + node * len;
+            for (int c = 0; c < len; ++c) o[c] += wgt * R.m[p] * v[c];
+          }
+        }
+    }
+  });
+  hg::host_parallel(nn, 4096, [&](size_t b, size_t e) {
+    for (int k = 0; k < nf; ++k) {
+      const int len = f[k].len;
+      double *o = f[k].out->data();
+      for (size_t node = b; node < e; ++node) {
+        if (mass[node] > 0.0) {
+          for (int c = 0; c < len; ++c) o[node * len + c] /= mass[node];
+        } else {
+          for (int c = 0; c < len; ++c) o[node * len + c] = f[k].dflt[c];
         }
       }
-  }
-  for (int k = 0; k < nf; ++k) {
-    const int len = f[k].len;
-    double *o = f[k].out->data();
-    for (size_t node = 0; node < nn; ++node) {
-      if (mass[node] > 0.0) {
-        for (int c = 0; c < len; ++c) o[node * len + c] /= mass[node];
-      } else {
-        for (int c = 0; c < len; ++c) o[node * len + c] = f[k].dflt[c];
-      }
     }
-  }
+  });
 }
 
 // determineMPMQuantitiesForInnerContinuumZones (ResamplingTools.cpp:353-377)
@@ -605,7 +752,9 @@ void inner_point_quantities(hg_resampler &R, int64_t before, int64_t after, cons
     }
   }
   const double h1 = R.hl.empty() ? 0.0 : R.hl[0];
-  for (int64_t p = before; p < after; ++p) {
+  // node fields to each inserted point, independently: over host threads
+  hg::host_parallel((size_t)(after - before), 256, [&](size_t pb, size_t pe) {
+  for (int64_t p = before + (int64_t)pb; p < before + (int64_t)pe; ++p) {
     const double x = R.q[2 * p], y = R.q[2 * p + 1];
     double Jv[1], be[4], vel[2];
     interp_nodes(R, x, y, h1, zd.mpm_grid_min[0], zd.mpm_grid_min[1], R.grid_h, zd.mpm_cells[0],
@@ -626,6 +775,7 @@ void inner_point_quantities(hg_resampler &R, int64_t before, int64_t after, cons
     }
     for (int c = 0; c < 4; ++c) R.be[4 * p + c] = be[c];
   }
+  });
 }
 
 template <typename T> void compact(std::vector<T> &a, const std::vector<uint8_t> &keep, int width) {
@@ -698,13 +848,22 @@ void update_weights(hg_resampler &R, const hg_zones &z) {
   }
 }
 
+double ms_since(std::chrono::steady_clock::time_point &t) {
+  const auto now = std::chrono::steady_clock::now();
+  const double ms = std::chrono::duration<double, std::milli>(now - t).count();
+  t = now;
+  return ms;
+}
+
 hg_status run(hg_resampler &R, const hg_zones &z) {
   R.stats = hg_resampler_stats{};
+  auto t = std::chrono::steady_clock::now();
   const bool direct = z.d.allow_direct_transitions != 0;
   hg_status st;
   int64_t g_before = 0, p_before = 0, p_after = 0, p_mid = 0, dummy = 0;
   if ((st = insert_grains(R, z.rzones, g_before))) return st;
   const int64_t g_after = (int64_t)nbodies(R);
+  R.stats.ms_insert_grains = ms_since(t);
   if ((st = insert_points(R, z.rzones, p_before))) return st;
   p_mid = (int64_t)npoints(R);
   if (direct && (st = insert_points(R, z.direct, dummy))) return st;
@@ -716,8 +875,10 @@ hg_status run(hg_resampler &R, const hg_zones &z) {
     if ((st = insert_points(R, inner, i_before))) return st;
     i_after = (int64_t)npoints(R);
   }
+  R.stats.ms_insert_points = ms_since(t);
   CellLists cont, disc;
   point_grids(R, cont, disc);
+  R.stats.ms_point_grids = ms_since(t);
   if (direct) {
     hybrid_point_quantities(R, z.rzones, p_before, p_mid, g_before, cont, disc);
     hybrid_point_quantities(R, z.direct, p_mid, p_after, g_before, cont, disc);
@@ -726,8 +887,10 @@ hg_status run(hg_resampler &R, const hg_zones &z) {
   }
   grain_quantities(R, g_before, g_after, p_before, cont, disc);
   inner_point_quantities(R, i_before, i_after, cont);
+  R.stats.ms_quantities = ms_since(t);
   delete_by_zone(R, z);
   update_weights(R, z);
+  R.stats.ms_delete = ms_since(t);
   return HG_OK;
 }
 

@@ -138,7 +138,7 @@ void mpm_meta(const hg_mpm *m, int64_t meta[16]) {
   meta[7] = m->rebins;
   int32_t hb;
   std::memcpy(&hb, &m->hl_cells, sizeof hb);
-  meta[8] = hb; // uGIMP half-width in cells (MIXED)
+  meta[8] = hb; // uGIMP half-width of the first uploaded point in cells (MIXED)
 }
 
 // Segments of the live state; buf selects the particle buffer of the pair.
@@ -160,6 +160,7 @@ std::vector<Seg> mpm_segments(hg_mpm *m, int64_t n, int buf) {
     v.push_back(whole(13, m->active_tiles));
     v.push_back(whole(14, m->nactive));
     v.push_back(whole(15, m->outside));
+    if (m->p.basis == HG_BASIS_UGIMP) v.push_back(seg(16, m->mhl_[buf], n));
   } else {
     v.push_back(seg(1, m->q, 2 * n));
     v.push_back(seg(2, m->v, 2 * n));

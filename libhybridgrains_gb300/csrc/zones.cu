@@ -145,16 +145,7 @@ void packing_fraction(hg_zones &z, int64_t nd, const double *q3, const double *r
         z.phi[(size_t)j * nx + i] = pf / (double)(S * S);
       }
   };
-  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-  const unsigned workers = std::min<unsigned>(hw, std::max(1u, ny / 8));
-  if (workers <= 1) {
-    rows(0, ny);
-  } else {
-    std::vector<std::thread> pool;
-    for (unsigned t = 0; t < workers; ++t)
-      pool.emplace_back(rows, ny * t / workers, ny * (t + 1) / workers);
-    for (auto &th : pool) th.join();
-  }
+  hg::host_parallel(ny, 8, [&](size_t jb, size_t je) { rows((unsigned)jb, (unsigned)je); });
   // cells within half a window of a material point count as dense; the
   // reference's test excludes the first row and column (gid > 0)
   for (int64_t p = 0; p < np; ++p) {

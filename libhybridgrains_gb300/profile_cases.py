@@ -5,7 +5,7 @@
     python -m libhybridgrains_gb300.profile_cases dem --disks 1000000 --packed --steps 12 \
         [--precision mixed]
     python -m libhybridgrains_gb300.profile_cases hybrid --steps 6 [--precision mixed]
-    python -m libhybridgrains_gb300.profile_cases column --steps 8
+    python -m libhybridgrains_gb300.profile_cases column --steps 8 [--basis ugimp]
     python -m libhybridgrains_gb300.profile_cases batch --scenes 256 --steps 8
 
 Each case builds its scene, runs one warm-up step, then ``--steps`` steps one
@@ -17,7 +17,8 @@ compacted to a 1.9 mm pitch between a floor and two walls (about 2.5
 contacts per disk; dt 1e-6 s);
 the hybrid case is the hybrid column (100,000 points under 20,000 disks)
 after its initial resampling; the column case is the 2,000,000-point MIXED
-column; the batch case is the serving mix (the first --scenes requests of
+column (with --basis ugimp on a grid 4 cells wider below and left, as the
+bench runs it); the batch case is the serving mix (the first --scenes requests of
 seed 2024) as MIXED scenes in one batch.
 """
 import argparse
@@ -31,6 +32,8 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("case", choices=["dem", "hybrid", "column", "batch"])
     ap.add_argument("--scenes", type=int, default=256, help="batch: serving requests")
+    ap.add_argument("--basis", choices=("linear", "ugimp"), default="linear",
+                    help="column: the MPM basis")
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--disks", type=int, default=1000000)
     ap.add_argument("--per-row", type=int, default=1000, help="DEM lattice disks per row")
@@ -90,9 +93,14 @@ def main(argv=None):
     else:
         cfg = scenes.mpm_column("column_2M")
         p = scenes.seed_column_points(cfg)
+        basis = hg.LINEAR
+        if args.basis == "ugimp":
+            basis = hg.UGIMP
+            cfg = dict(cfg, grid_min=(cfg["grid_min"][0] - 4 * cfg["h"],
+                                      cfg["grid_min"][1] - 4 * cfg["h"]))
         obj = hg.MPM(ctx, cfg["grid_min"], cfg["grid_max"], cfg["h"], cfg["shear_modulus"],
                      cfg["bulk_modulus"], cfg["dp_alpha"], cfg["flip_alpha"], scenes.GRAVITY,
-                     cfg["planes"], capacity=len(p["m"]))
+                     cfg["planes"], basis=basis, capacity=len(p["m"]))
         obj.upload(p["q"], p["v"], p["m"], p["vol"], p["hl"])
 
         def step():

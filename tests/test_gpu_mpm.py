@@ -153,12 +153,14 @@ def test_mixed_multi_step_tracks_oracle(ctx, cfg0):
     assert g.status() == 0
 
 
-def test_mixed_fast_particles_resort(ctx):
+@pytest.mark.parametrize("basis", [0, 1])
+def test_mixed_fast_particles_resort(ctx, basis):
     """Isolated points crossing several tiles: exercises the out-of-window
     path and the re-sort, stepping both per step (calls of fewer steps than a
     captured chunk, re-sort decisions every step) and through the graph of
     captured chunks (decisions between chunks); results follow the FP64
-    oracle either way."""
+    oracle either way. With the uGIMP basis every point has its own
+    half-width, which the re-sorts carry along."""
     # no elastic stiffness: at 0.2 cells per step the elastic CFL limit of the
     # column material would be exceeded, so these points carry no stress
     cfg = scenes.mpm_column("column_12800", shear_modulus=0.0, bulk_modulus=0.0)
@@ -169,10 +171,10 @@ def test_mixed_fast_particles_resort(ctx):
     v = np.tile([[2.0, 1.0]], (n, 1))
     m = np.full(n, 1e-3)
     vol = np.full(n, 1e-6)
-    hl = np.full(n, 1.25e-3)
-    g = gpu_mpm(ctx, cfg, hg.MIXED)
-    gc = gpu_mpm(ctx, cfg, hg.MIXED)
-    c = cpu_mpm(cfg)
+    hl = np.full(n, 1.25e-3) if basis == 0 else rng.uniform(0.15, 0.5, n) * cfg["h"]
+    g = gpu_mpm(ctx, cfg, hg.MIXED, basis=basis)
+    gc = gpu_mpm(ctx, cfg, hg.MIXED, basis=basis)
+    c = cpu_mpm(cfg, basis=basis)
     g.upload(q, v, m, vol, hl)
     gc.upload(q, v, m, vol, hl)
     c.set_particles(q, v, m, vol, hl)
@@ -189,20 +191,26 @@ def test_mixed_fast_particles_resort(ctx):
     assert g.rebin_count() >= 2
 
 
-def test_mixed_ugimp_against_the_oracle(ctx, cfg0):
+@pytest.mark.parametrize("varying", [False, True])
+def test_mixed_ugimp_against_the_oracle(ctx, cfg0, varying):
     """MIXED with the uGIMP basis (FP32 weights of the particle-size
     integrated hat functions, 3 x 3 stencils near cell edges) against the
     FP64 oracle with uGIMP: one-step grid-velocity error from a stressed FP64
     state within the MIXED bound, and positions / J after 20 steps within the
-    linear path's tolerances."""
+    linear path's tolerances; with the seeded half-width h / 4 for every
+    point, and with per-point half-widths from 0.15 h to h / 2 (the resampling
+    gives inserted points their own)."""
     cfg = dict(cfg0, grid_min=(-0.01, -0.01))
     c = cpu_mpm(cfg, basis=1)
     p = scenes.seed_column_points(cfg)
-    c.set_particles(p["q"], p["v"], p["m"], p["vol"], p["hl"])
+    hl = p["hl"].copy()
+    if varying:
+        hl *= np.random.default_rng(5).uniform(0.6, 2.0, len(hl))
+    c.set_particles(p["q"], p["v"], p["m"], p["vol"], hl)
     c.step(cfg["dt"], 200)
     s = c.particles()
     g = gpu_mpm(ctx, cfg, hg.MIXED, basis=hg.UGIMP)
-    g.upload(s["q"], s["v"], p["m"], p["vol"], p["hl"], s["be"], s["J"], s["jh"])
+    g.upload(s["q"], s["v"], p["m"], p["vol"], hl, s["be"], s["J"], s["jh"])
     dt = cfg["dt"]
     g.flow(dt)
     c.step(dt)
@@ -224,11 +232,11 @@ def test_mixed_ugimp_against_the_oracle(ctx, cfg0):
     assert np.abs(P["J"] - Q["J"]).max() <= 1e-6
     assert np.abs(P["be"] - Q["be"]).max() <= 1e-6
     assert g.status() == 0
-    # one half-width for all points; batches take the linear basis
-    hl = p["hl"].copy()
-    hl[3] *= 1.5
+    # half-widths above h / 2 are refused; batches take the linear basis
+    wide = hl.copy()
+    wide[3] = 0.6 * cfg["h"]
     with pytest.raises(hg.HGError):
-        g.upload(p["q"], p["v"], p["m"], p["vol"], hl)
+        g.upload(p["q"], p["v"], p["m"], p["vol"], wide)
     b = hg.Batch(ctx, 2)
     with pytest.raises(hg.HGError):
         b.add(g, dt)

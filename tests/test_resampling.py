@@ -112,7 +112,7 @@ def compare(ours, ref):
     assert np.array_equal(G["fixed"], np.array(RG["fixed"], dtype=np.uint8))
     assert np.array_equal(G["old_to_new"], np.array(ref.dem_map, dtype=np.int32))
     _, _, st = ours.stats()
-    assert st == ref.stats
+    assert {k: st[k] for k in ref.stats} == ref.stats  # the counts; st also has timings
     return st
 
 
