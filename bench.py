@@ -318,7 +318,7 @@ def run_ours(args, rank, world, local):
                 rates[name].update(
                     launch_shape=utune, active_nodes=ua, status=mu_.status(),
                     of_linear_step_time=(ums / k) / (ms / args.steps),
-                    roofline={"kernel": "kxu_g2p2g", "algorithmic_bytes": ub,
+                    roofline={"kernel": "kxu_step", "algorithmic_bytes": ub,
                               "kernel_ms": per * 1e3, "grid_update_ms": u_ms / max(kk, 1),
                               "achieved_gbs": ub / per / 1e9,
                               "timing": "CUDA events around each launch, %d steps after the "

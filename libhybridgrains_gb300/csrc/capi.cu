@@ -1620,6 +1620,8 @@ hg_status hg_hybrid_clear_homogenized(hg_hybrid *h) {
 hg_status hg_hybrid_num_packed(hg_hybrid *h, int64_t *ng, int64_t *nn) {
   if (!h) return fail(HG_ERR_INVALID_ARGUMENT, "h is NULL");
   DeviceGuard g(h->ctx);
+  hg_status st = hybrid_pack_lists(h);
+  if (st != HG_OK) return st;
   int32_t c[2] = {0, 0};
   HG_CUDA_TRY(cudaMemcpyAsync(c, h->counts.p, sizeof(c), cudaMemcpyDeviceToHost, h->ctx->stream));
   HG_CUDA_TRY(cudaStreamSynchronize(h->ctx->stream));
@@ -1633,11 +1635,12 @@ hg_status hg_hybrid_download(hg_hybrid *h, int32_t *pg, int32_t *pn, double *dm,
   if (!h) return fail(HG_ERR_INVALID_ARGUMENT, "h is NULL");
   DeviceGuard g(h->ctx);
   cudaStream_t s = h->ctx->stream;
+  hg_status st = hybrid_pack_lists(h);
+  if (st != HG_OK) return st;
   int32_t c[2] = {0, 0};
   HG_CUDA_TRY(cudaMemcpyAsync(c, h->counts.p, sizeof(c), cudaMemcpyDeviceToHost, s));
   HG_CUDA_TRY(cudaStreamSynchronize(s));
   const int64_t nn = (int64_t)(h->m->p.nx + 1) * (h->m->p.ny + 1);
-  hg_status st;
   if ((st = d2h(s, pg, h->packed_dem.p, c[0])) || (st = d2h(s, pn, h->packed_mpm.p, c[1])) ||
       (st = d2h(s, dm, h->dem_mass.p, nn)) || (st = d2h(s, dp, h->dem_mom.p, 2 * nn)) ||
       (st = d2h(s, va, h->v_after.p, 2 * nn)) || (st = d2h(s, aa, h->a_after.p, 2 * nn)) ||

@@ -14,9 +14,10 @@
 //   kc_pack             (Coupling.cpp:113-127)
 //   kc_grain_mom      rasterizeGrainMom (Coupling.cpp:287-363)
 //   kc_update_nodes   updateVelocitiesOnGrid (Coupling.cpp:533-579) and the
-//                     homog_factor loop (HybridGrains2DSim.cpp:183-197)
-//   kc_transfer       transferToGrain, FLIP with alpha = 1 (Coupling.cpp:468-527)
-//   kc_advect         updatePositions_node_node (Coupling.cpp:581-591)
+//                     homog_factor loop (HybridGrains2DSim.cpp:183-197), over
+//                     every node
+//   kc_transfer       transferToGrain, FLIP with alpha = 1 (Coupling.cpp:468-527),
+//                     then updatePositions_node_node (Coupling.cpp:581-591)
 //   kc_hstress        ResamplingTools::homogenizeStress (ResamplingTools.cpp:744-813)
 //   kc_hvel_scatter / ResamplingTools::homogenizeVelocity
 //   kc_hvel_finish      (ResamplingTools.cpp:830-884)
@@ -105,16 +106,14 @@ __global__ void kc_pack(int64_t n, const int32_t *__restrict__ flag,
 }
 
 template <bool W32>
-__global__ void kc_grain_mom(GridGeom G, const int32_t *__restrict__ count,
-                             const int32_t *__restrict__ packed, const double *__restrict__ pos,
+__global__ void kc_grain_mom(GridGeom G, int64_t nb, const int32_t *__restrict__ coupled,
+                             const double *__restrict__ pos,
                              const double *__restrict__ hl0, const uint8_t *__restrict__ fixed,
                              const double *__restrict__ m0, const double *__restrict__ w,
                              const double *__restrict__ v, double *dem_mom) {
-  const int c = *count;
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < c;
-       k += (int64_t)gridDim.x * blockDim.x) {
-    const int b = packed[k];
-    if (fixed[b]) continue;
+  for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nb;
+       b += (int64_t)gridDim.x * blockDim.x) {
+    if (!coupled[b] || fixed[b]) continue;
     const double hl = hl0[0];
     const double x = pos[3 * b], y = pos[3 * b + 1];
     int x0, y0, x1, y1;
@@ -131,17 +130,23 @@ __global__ void kc_grain_mom(GridGeom G, const int32_t *__restrict__ count,
   }
 }
 
-__global__ void kc_update_nodes(const int32_t *__restrict__ count,
-                                const int32_t *__restrict__ packed,
-                                const double *__restrict__ g_mass,
+// Every node: its homogenisation factor (HybridGrains2DSim.cpp:183-197: 1/2
+// where the DEM has mass, else 1 where the MPM has), and on the coupled nodes
+// (DEM mass > 0) updateVelocitiesOnGrid; v_after and a_after are zero
+// elsewhere.
+__global__ void kc_update_nodes(int64_t nn, const double *__restrict__ g_mass,
                                 const double *__restrict__ dem_mass,
                                 const double *__restrict__ dem_mom, double *g_mom_new,
-                                double *v_after, double *a_after) {
-  const int c = *count;
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < c;
-       k += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = packed[k];
+                                double *v_after, double *a_after, double *homog) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nn;
+       i += (int64_t)gridDim.x * blockDim.x) {
     const double m_mpm = g_mass[i], m_dem = dem_mass[i];
+    homog[i] = m_dem > 0.0 ? 0.5 : (m_mpm > 0.0 ? 1.0 : 0.0);
+    if (!(m_dem > 0.0)) {
+      v_after[2 * i] = v_after[2 * i + 1] = 0.0;
+      a_after[2 * i] = a_after[2 * i + 1] = 0.0;
+      continue;
+    }
     const double msum = m_mpm + m_dem;
     const double lx = (m_dem * g_mom_new[2 * i] - m_mpm * dem_mom[2 * i]) / msum;
     const double ly = (m_dem * g_mom_new[2 * i + 1] - m_mpm * dem_mom[2 * i + 1]) / msum;
@@ -155,31 +160,25 @@ __global__ void kc_update_nodes(const int32_t *__restrict__ count,
   }
 }
 
-template <typename M>
-__global__ void kc_homog(int64_t nn, const M *__restrict__ g_mass,
-                         const double *__restrict__ dem_mass, double *homog) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= nn) return;
-  homog[i] = dem_mass[i] > 0.0 ? 0.5 : ((double)g_mass[i] > 0.0 ? 1.0 : 0.0);
-}
-
 // updateVelocitiesOnGrid (Coupling.cpp:533-579) on a MIXED grid: the MPM
 // node momentum after the grid update is gm v (FP32 velocity and mass), the
 // exchange lambda is formed in FP64 as in kc_update_nodes, and the node's
 // velocity and acceleration (va: v, a) take p_new - lambda; the acceleration
 // (p_new - p) / (m dt) loses lambda / (m dt). Nodes without MPM mass keep
 // their zero velocity, as (p_new = 0) / m is never formed for them.
-__global__ void kc_update_nodes_x(const int32_t *__restrict__ count,
-                                  const int32_t *__restrict__ packed,
-                                  const float *__restrict__ gm,
+__global__ void kc_update_nodes_x(int64_t nn, const float *__restrict__ gm,
                                   const double *__restrict__ dem_mass,
                                   const double *__restrict__ dem_mom, double dt, float4 *va,
-                                  double *v_after, double *a_after) {
-  const int c = *count;
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < c;
-       k += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = packed[k];
+                                  double *v_after, double *a_after, double *homog) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nn;
+       i += (int64_t)gridDim.x * blockDim.x) {
     const double m_mpm = (double)gm[i], m_dem = dem_mass[i];
+    homog[i] = m_dem > 0.0 ? 0.5 : (m_mpm > 0.0 ? 1.0 : 0.0); // as kc_update_nodes
+    if (!(m_dem > 0.0)) {
+      v_after[2 * i] = v_after[2 * i + 1] = 0.0;
+      a_after[2 * i] = a_after[2 * i + 1] = 0.0;
+      continue;
+    }
     float4 g = va[i];
     const double px = m_mpm * (double)g.x, py = m_mpm * (double)g.y;
     const double msum = m_mpm + m_dem;
@@ -208,17 +207,23 @@ __global__ void kc_fill(double *dst, int64_t n, double v) {
 }
 
 template <bool W32>
-__global__ void kc_transfer(GridGeom G, const int32_t *__restrict__ count,
-                            const int32_t *__restrict__ packed, const double *__restrict__ pos,
+// transferToGrain (Coupling.cpp:468-527) and then, as nothing between them
+// touches the grains, updatePositions_node_node (Coupling.cpp:581-591):
+// q = q_before + dt v for every coupled grain (fixed ones keep their v)
+__global__ void kc_transfer(GridGeom G, int64_t nb, const int32_t *__restrict__ coupled,
+                            const double *__restrict__ pos,
                             const double *__restrict__ hl0, const uint8_t *__restrict__ fixed,
                             const double *__restrict__ v_after,
-                            const double *__restrict__ a_after, double *v) {
-  const int c = *count;
+                            const double *__restrict__ a_after, double dt, double *v, double *q) {
   const double alpha = 1.0;
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < c;
-       k += (int64_t)gridDim.x * blockDim.x) {
-    const int b = packed[k];
-    if (fixed[b]) continue;
+  for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nb;
+       b += (int64_t)gridDim.x * blockDim.x) {
+    if (!coupled[b]) continue;
+    if (fixed[b]) {
+      q[3 * b] = pos[3 * b] + dt * v[3 * b];
+      q[3 * b + 1] = pos[3 * b + 1] + dt * v[3 * b + 1];
+      continue;
+    }
     const double hl = hl0[0];
     const double x = pos[3 * b], y = pos[3 * b + 1];
     int x0, y0, x1, y1;
@@ -234,20 +239,11 @@ __global__ void kc_transfer(GridGeom G, const int32_t *__restrict__ count,
                           aty = aty + wt * a_after[2 * i + 1];
                         });
     const double fx = v[3 * b] + atx, fy = v[3 * b + 1] + aty;
-    v[3 * b] = vpx * (1.0 - alpha) + fx * alpha;
-    v[3 * b + 1] = vpy * (1.0 - alpha) + fy * alpha;
-  }
-}
-
-__global__ void kc_advect(double dt, const int32_t *__restrict__ count,
-                          const int32_t *__restrict__ packed, const double *__restrict__ pos,
-                          const double *__restrict__ v, double *q) {
-  const int c = *count;
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < c;
-       k += (int64_t)gridDim.x * blockDim.x) {
-    const int b = packed[k];
-    q[3 * b] = pos[3 * b] + dt * v[3 * b];
-    q[3 * b + 1] = pos[3 * b + 1] + dt * v[3 * b + 1];
+    const double vx = vpx * (1.0 - alpha) + fx * alpha, vy = vpy * (1.0 - alpha) + fy * alpha;
+    v[3 * b] = vx;
+    v[3 * b + 1] = vy;
+    q[3 * b] = pos[3 * b] + dt * vx;
+    q[3 * b + 1] = pos[3 * b + 1] + dt * vy;
   }
 }
 
@@ -363,6 +359,31 @@ hg_status hybrid_alloc(hg_hybrid *h) {
   return HG_OK;
 }
 
+hg_status hybrid_pack_lists(hg_hybrid *h) {
+  if (h->packed_valid) return HG_OK;
+  cudaStream_t s = h->ctx->stream;
+  const int64_t nn = (int64_t)(h->m->p.nx + 1) * (h->m->p.ny + 1), nb = h->step_bodies;
+  hg_status st;
+  // std::stable_partition of the grains (Coupling.cpp:113-127): kc_grain_mass
+  // flagged them
+  HG_CUDA_TRY(cudaMemsetAsync(h->coupled.p + nb, 0, sizeof(int32_t), s));
+  if ((st = exclusive_scan_i32(h->coupled.p, h->flag_tmp.p, nb + 1, h->scan_tmp.p, s))) return st;
+  HG_LAUNCH(kc_pack, blocks_for(nb + 1, 256), 256, 0, s, nb, h->coupled.p, h->flag_tmp.p,
+            h->packed_dem.p, h->counts.p);
+  HG_CHECK_LAUNCH();
+  // and of the nodes with DEM mass
+  HG_LAUNCH(kc_flag_nodes, blocks_for(nn, 256), 256, 0, s, nn, h->dem_mass.p, h->node_flag.p);
+  HG_CHECK_LAUNCH();
+  HG_CUDA_TRY(cudaMemsetAsync(h->node_flag.p + nn, 0, sizeof(int32_t), s));
+  if ((st = exclusive_scan_i32(h->node_flag.p, h->node_pos.p, nn + 1, h->scan_tmp.p, s)))
+    return st;
+  HG_LAUNCH(kc_pack, blocks_for(nn + 1, 256), 256, 0, s, nn, h->node_flag.p, h->node_pos.p,
+            h->packed_mpm.p, h->counts.p + 1);
+  HG_CHECK_LAUNCH();
+  h->packed_valid = true;
+  return HG_OK;
+}
+
 hg_status hybrid_clear_homogenized(hg_hybrid *h) {
   const int64_t nn = (int64_t)(h->m->p.nx + 1) * (h->m->p.ny + 1);
   cudaStream_t s = h->ctx->stream;
@@ -420,52 +441,34 @@ hg_status hybrid_step_impl(hg_hybrid *h, double dt, int flags) {
                 h->coupled.p);
     HG_CHECK_LAUNCH();
   }
-  HG_CUDA_TRY(cudaMemsetAsync(h->coupled.p + nb, 0, sizeof(int32_t), s));
-  if ((st = exclusive_scan_i32(h->coupled.p, h->flag_tmp.p, nb + 1, h->scan_tmp.p, s))) return st;
-  HG_LAUNCH(kc_pack, blocks_for(nb + 1, 256), 256, 0, s, nb, h->coupled.p, h->flag_tmp.p,
-            h->packed_dem.p, h->counts.p);
-  HG_CHECK_LAUNCH();
-  HG_LAUNCH(kc_flag_nodes, blocks_for(nn, 256), 256, 0, s, nn, h->dem_mass.p, h->node_flag.p);
-  HG_CHECK_LAUNCH();
-  HG_CUDA_TRY(cudaMemsetAsync(h->node_flag.p + nn, 0, sizeof(int32_t), s));
-  if ((st = exclusive_scan_i32(h->node_flag.p, h->node_pos.p, nn + 1, h->scan_tmp.p, s)))
-    return st;
-  HG_LAUNCH(kc_pack, blocks_for(nn + 1, 256), 256, 0, s, nn, h->node_flag.p, h->node_pos.p,
-            h->packed_mpm.p, h->counts.p + 1);
-  HG_CHECK_LAUNCH();
+  // The coupled grains (flagged by kc_grain_mass) and nodes (DEM mass > 0)
+  // are walked in place: each is handled on its own and the scatters use
+  // atomics, so the reference's packed order (Coupling.cpp:113-127) matters
+  // only to callers of the lists, which hybrid_pack_lists builds on demand.
+  h->packed_valid = false;
+  h->step_bodies = nb;
   // DiscreteIntegrator::step -> flowWithWeight (DiscreteIntegrator.cpp:99-116)
   if ((st = dem_step(d, dt, 1))) return st;
   if ((st = mixed ? mixed_grid_update(m, dt) : mpm64_phase1(m, dt))) return st;
   // rasterizeGrainMom
   HG_CUDA_TRY(cudaMemsetAsync(h->dem_mom.p, 0, sizeof(double) * 2 * nn, s));
-  HG_LAUNCH(kc_grain_mom<W32>, gs, 128, 0, s, G, h->counts.p, h->packed_dem.p, h->pos_before.p,
-            hl0, d->fixed.p, d->m0.p, d->w.p, d->v.p, h->dem_mom.p);
+  HG_LAUNCH(kc_grain_mom<W32>, blocks_for(nb, 128), 128, 0, s, G, nb, h->coupled.p,
+            h->pos_before.p, hl0, d->fixed.p, d->m0.p, d->w.p, d->v.p, h->dem_mom.p);
   HG_CHECK_LAUNCH();
-  // updateVelocitiesOnGrid
-  HG_CUDA_TRY(cudaMemsetAsync(h->v_after.p, 0, sizeof(double) * 2 * nn, s));
-  HG_CUDA_TRY(cudaMemsetAsync(h->a_after.p, 0, sizeof(double) * 2 * nn, s));
+  // updateVelocitiesOnGrid and the homogenisation factors
   if (mixed) {
-    HG_LAUNCH(kc_update_nodes_x, gs, 256, 0, s, h->counts.p + 1, h->packed_mpm.p,
-              (const float *)m->gm.p, h->dem_mass.p, h->dem_mom.p, dt, m->va.p, h->v_after.p,
-              h->a_after.p);
-    HG_CHECK_LAUNCH();
-    HG_LAUNCH(kc_homog<float>, blocks_for(nn, 256), 256, 0, s, nn, (const float *)m->gm.p,
-              h->dem_mass.p, h->homog.p);
+    HG_LAUNCH(kc_update_nodes_x, blocks_for(nn, 256), 256, 0, s, nn, (const float *)m->gm.p,
+              h->dem_mass.p, h->dem_mom.p, dt, m->va.p, h->v_after.p, h->a_after.p,
+              h->homog.p);
   } else {
-    HG_LAUNCH(kc_update_nodes, gs, 256, 0, s, h->counts.p + 1, h->packed_mpm.p, m->g_mass.p,
-              h->dem_mass.p, h->dem_mom.p, m->g_mom_new.p, h->v_after.p, h->a_after.p);
-    HG_CHECK_LAUNCH();
-    HG_LAUNCH(kc_homog<double>, blocks_for(nn, 256), 256, 0, s, nn, (const double *)m->g_mass.p,
-              h->dem_mass.p, m->g_homog.p);
+    HG_LAUNCH(kc_update_nodes, blocks_for(nn, 256), 256, 0, s, nn, m->g_mass.p, h->dem_mass.p,
+              h->dem_mom.p, m->g_mom_new.p, h->v_after.p, h->a_after.p, m->g_homog.p);
   }
   HG_CHECK_LAUNCH();
-  HG_LAUNCH(kc_transfer<W32>, gs, 128, 0, s, G, h->counts.p, h->packed_dem.p, h->pos_before.p,
-            hl0, d->fixed.p, h->v_after.p, h->a_after.p, d->v.p);
+  HG_LAUNCH(kc_transfer<W32>, blocks_for(nb, 128), 128, 0, s, G, nb, h->coupled.p,
+            h->pos_before.p, hl0, d->fixed.p, h->v_after.p, h->a_after.p, dt, d->v.p, d->q.p);
   HG_CHECK_LAUNCH();
   if ((st = mixed ? mixed_particles(m, dt) : mpm64_phase2(m, dt))) return st;
-  HG_LAUNCH(kc_advect, gs, 128, 0, s, dt, h->counts.p, h->packed_dem.p, h->pos_before.p, d->v.p,
-            d->q.p);
-  HG_CHECK_LAUNCH();
   if ((flags & HG_HYBRID_HOMOGENIZE_STRESS) && nb > 0) {
     HG_LAUNCH(kc_hstress<W32>, gs, 128, 0, s, G, nb, d->per_body_off.p, d->crec[d->cc].p, d->q.p,
               h->hstress.p);

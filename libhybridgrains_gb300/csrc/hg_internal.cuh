@@ -539,6 +539,9 @@ struct hg_hybrid {
   hg::DevBuf<int32_t> coupled, packed_dem, packed_mpm, flag_tmp, scan_tmp,
       node_flag, node_pos, counts; // counts[2]: packed sizes
   int64_t n_packed_dem = 0, n_packed_mpm = 0;
+  // the packed lists (and counts) describe the last step; built on demand
+  bool packed_valid = false;
+  int64_t step_bodies = 0; // DEM bodies at the last step
   // with a MIXED MPM object: the node homogenisation factors (an FP64 object
   // keeps them in its grid) and the points' half-width hl(0) in world units
   hg::DevBuf<double> homog, hl0;
@@ -555,4 +558,7 @@ hg_status mixed_particles(hg_mpm *m, double dt);
 hg_status hybrid_alloc(hg_hybrid *h);
 hg_status hybrid_step(hg_hybrid *h, double dt, int flags);
 hg_status hybrid_clear_homogenized(hg_hybrid *h);
+// The last step's coupled grains and nodes as packed index lists in the
+// reference's stable-partition order, for callers that read them.
+hg_status hybrid_pack_lists(hg_hybrid *h);
 } // namespace hg

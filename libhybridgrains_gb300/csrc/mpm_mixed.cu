@@ -30,8 +30,8 @@
 // points sorted into its cell in registers (no atomics); points that left
 // their cell since the last re-sort use shared-memory atomics on the tile's
 // node window. Window sums go to global memory with one float4 + one float
-// atomic per touched node. With the uGIMP basis (up to 4 x 4 nodes per point)
-// every contribution goes through shared-memory atomics on the window.
+// atomic per touched node. With the uGIMP basis (up to 3 x 3 nodes per point)
+// one thread per point adds to the grid with global reductions.
 //
 // Re-sorting (counting sort by cell key) runs when a point has drifted out of
 // its tile's window, when more than 1/32 of the points have left their sorted
@@ -729,9 +729,8 @@ __global__ void __launch_bounds__(THREADS, 3) kb_g2p2g(const MixedArgs *__restri
 // grid units: the weight of node i along one axis is the hat function
 // integrated over the point's extent [u - hl, u + hl], divided by 2 hl, with
 // derivative d/du; for hl <= 1/2 a point of fraction f in cell c touches the
-// nodes c-1 (f < hl), c, c+1 and c+2 (f > 1 - hl). The kernel below walks
-// the same tiles and sorted cells as the linear one, with node windows one
-// node wider on each side.
+// nodes c-1 (f < hl), c, c+1 and c+2 (f > 1 - hl). The kernel below shares
+// the linear path's sorting, active tiles, grid update and chunk graphs.
 
 // Weights and derivatives along one axis of the three nodes b .. b+2 that
 // can carry weight when hl <= 1/2: b = c - 1 for f < 1/2 (node c+2 then has
@@ -778,6 +777,7 @@ __device__ __forceinline__ bool ugimp_axis(int c, float f, float hl, int n, int 
       g[1] = -2.0f * d * i2;
     }
   }
+  if (c >= 1 && c + 2 <= n) return true; // nodes c-1 .. c+2 all on the grid
   bool ok = true;
 #pragma unroll
   for (int m = 0; m < 3; ++m) {
@@ -787,74 +787,34 @@ __device__ __forceinline__ bool ugimp_axis(int c, float f, float hl, int n, int 
   return ok;
 }
 
-// Node windows of the uGIMP kernel: a point of cell c reads and writes the
-// nodes c-1 .. c+2. G2P covers the cells [X0 - DRIFT, X0 + BIN + DRIFT) of a
-// tile with origin X0 (where its points are while they stay within DRIFT
-// cells of the cell they were sorted into), P2G one cell further (where those
-// points land after a step of less than a cell).
-constexpr int UVA_W = BIN + 2 * DRIFT + 3;
-constexpr int UACC_W = BIN + 2 * DRIFT + 5;
-
-struct UgimpSmem {
-  float4 va[UVA_W * UVA_W];
-  float acc[5][UACC_W * UACC_W];
-  unsigned out[2]; // left the tile window / left the sorted cell
-};
-
-// ugimp_tile expects the P2G window to be zero on entry (it leaves it zero).
-__device__ __forceinline__ void zero_uacc(UgimpSmem &S) {
-  float *a = &S.acc[0][0];
-  for (int k = threadIdx.x; k < 5 * UACC_W * UACC_W; k += THREADS) a[k] = 0.f;
+// Nodes of a 3-node axis that carry weight or derivative (a node is in the
+// point's support when it does along both axes; outside it, it may lie off
+// the grid)
+__device__ __forceinline__ unsigned ugimp_support(const float w[3], const float g[3]) {
+  return (w[0] != 0.0f || g[0] != 0.0f ? 1u : 0u) | (w[1] != 0.0f || g[1] != 0.0f ? 2u : 0u) |
+         (w[2] != 0.0f || g[2] != 0.0f ? 4u : 0u);
 }
 
-// One tile with the uGIMP basis. One thread per cell of the tile walks the
-// points sorted into its cell, so at each stencil position the lanes of a
-// warp add to different nodes. G2P reads the shared copy of the grid window;
-// the point update is the linear kernel's; P2G adds to a shared node window
-// with shared-memory atomics, flushed to the global accumulators with one
-// atomic per touched node and field. Points outside the windows read and add
-// to the global grid (and count towards the next re-sort). Each point has its
-// own half-width (ResamplingTools.cpp:58-104 assigns them to inserted points).
+// One thread per point, in the sorted order: a warp's points lie in a few
+// neighbouring cells, so its gathers from the grid and its P2G atomics (one
+// float4 and one float reduction per node) stay within a few cache lines.
+// Each point has its own half-width (ResamplingTools.cpp:58-104 assigns them
+// to inserted points). Planes take the linear kernel's FP32 test first and
+// the FP64 test only within pmargin cells of a plane. (A tile-window form of
+// this kernel, with shared-memory G2P and P2G, was slower: five shared
+// atomics per node against two global reductions, at a third of the
+// occupancy.)
 template <bool PRIME>
-__device__ __forceinline__ void ugimp_tile(const MixedArgs &A, const int bin, UgimpSmem &S) {
-  const int tid = threadIdx.x;
+__global__ void __launch_bounds__(THREADS) kxu_step(const __grid_constant__ MixedArgs A) {
+  // launched with programmatic dependence on the grid update before it
+  pdl_wait();
+  pdl_trigger();
   const int row = A.nx + 1;
   [[maybe_unused]] const int64_t nn = (int64_t)row * (A.ny + 1); // bounds-checked builds
-  const int X0 = (bin % A.ntx) * BIN, Y0 = (bin / A.ntx) * BIN;
-  const int VX = X0 - DRIFT - 1, VY = Y0 - DRIFT - 1; // G2P window origin (node)
-  const int WX = X0 - DRIFT - 2, WY = Y0 - DRIFT - 2; // P2G window origin (node)
-  if (!PRIME) {
-    for (int k = tid; k < UVA_W * UVA_W; k += THREADS) {
-      const int ix = VX + k % UVA_W, iy = VY + k / UVA_W;
-      float4 val = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (ix >= 0 && iy >= 0 && ix <= A.nx && iy <= A.ny)
-        val = A.va[iy * row + ix]; // MIXED grids have < 2^30 nodes
-      S.va[k] = val;
-    }
-  }
-  if (tid < 2) S.out[tid] = 0;
-  int ps = A.offsets[bin * BIN_CELLS + tid];
-  int pe = A.offsets[bin * BIN_CELLS + tid + 1];
-  if (!HG_INDEX_OK(ps, (int64_t)A.n + 1, A.status) || !HG_INDEX_OK(pe, (int64_t)A.n + 1, A.status))
-    ps = pe = 0;
-  const int gcx = X0 + tid % BIN, gcy = Y0 + tid / BIN;
-  // Planes that can touch a point that starts in the G2P window and moves
-  // less than a cell, as in the linear kernel
-  unsigned plane_mask = 0;
-  for (int k = 0; k < A.nplanes; ++k) {
-    const MpmPlaneDev &pl = A.planes[k];
-    const float x0 = (float)(X0 - DRIFT - 1), y0 = (float)(Y0 - DRIFT - 1);
-    const float x1 = (float)(X0 + BIN + DRIFT + 2), y1 = (float)(Y0 + BIN + DRIFT + 2);
-    float dmin = fminf(fminf(pl.fn[0] * (x0 - pl.fux[0]) + pl.fn[1] * (y0 - pl.fux[1]),
-                             pl.fn[0] * (x1 - pl.fux[0]) + pl.fn[1] * (y0 - pl.fux[1])),
-                       fminf(pl.fn[0] * (x0 - pl.fux[0]) + pl.fn[1] * (y1 - pl.fux[1]),
-                             pl.fn[0] * (x1 - pl.fux[0]) + pl.fn[1] * (y1 - pl.fux[1])));
-    if (dmin <= 2.0f * A.pmargin && y1 >= pl.fulb - A.pmargin) plane_mask |= 1u << k;
-  }
-  __syncthreads();
-  unsigned left_window = 0, left_cell = 0;
+  unsigned moved = 0;
   bool nonfinite = false;
-  for (int p = ps; p < pe; ++p) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < A.n;
+       p += (int64_t)gridDim.x * blockDim.x) {
     double2 un = A.u[p];
     const float2 mv = A.mv[p];
     float2 vel = A.v[p];
@@ -875,29 +835,20 @@ __device__ __forceinline__ void ugimp_tile(const MixedArgs &A, const int bin, Ug
       atomicOr(A.status, (uint32_t)HG_STATUS_OUT_OF_GRID);
       continue;
     }
-    int ncx = cx, ncy = cy;
     if (!PRIME) {
       // ---- G2P of this step at the start-of-step position ----
-      const bool in_window = cx - 1 - VX >= 0 && cy - 1 - VY >= 0 && cx + 2 - VX < UVA_W &&
-                             cy + 2 - VY < UVA_W;
       float Lxx = 0.f, Lxy = 0.f, Lyx = 0.f, Lyy = 0.f, vpx = 0.f, vpy = 0.f, apx = 0.f,
             apy = 0.f;
+      const unsigned sx = ugimp_support(wx, gx), sy = ugimp_support(wy, gy);
 #pragma unroll
       for (int ky = 0; ky < 3; ++ky) {
 #pragma unroll
         for (int kx = 0; kx < 3; ++kx) {
-          float4 nv;
-          if (in_window) {
-            nv = S.va[(by - VY + ky) * UVA_W + bx - VX + kx];
-          } else {
-            // nodes of zero weight may lie outside the grid
-            if (wx[kx] == 0.0f && gx[kx] == 0.0f) continue;
-            if (wy[ky] == 0.0f && gy[ky] == 0.0f) continue;
-            const int64_t node = (int64_t)(by + ky) * row + (bx + kx);
-            if (!HG_INDEX_OK(node, nn, A.status)) continue;
-            nv = A.va[node];
-          }
+          if (!((sx >> kx) & (sy >> ky) & 1u)) continue; // outside the support
           const float w = wx[kx] * wy[ky], dX = gx[kx] * wy[ky], dY = wx[kx] * gy[ky];
+          const int64_t node = (int64_t)(by + ky) * row + (bx + kx);
+          if (!HG_INDEX_OK(node, nn, A.status)) continue;
+          const float4 nv = A.va[node];
           Lxx += nv.x * dX;
           Lxy += nv.x * dY;
           Lyx += nv.y * dX;
@@ -924,15 +875,11 @@ __device__ __forceinline__ void ugimp_tile(const MixedArgs &A, const int bin, Ug
       }
       un = make_double2(un.x + widen(dux), un.y + widen(duy));
       // MaterialPoints::resolvePlaneCollisions (MaterialPoints.cpp:371-423) in
-      // grid units: FP32 test first, FP64 on the positions where the point is
-      // within pmargin cells of a plane. The tile's plane mask bounds points
-      // that start in the window and move less than a cell; any other point
-      // tests every plane.
-      const bool exact = !(fabsf(dux) < 1.0f && fabsf(duy) < 1.0f);
-      const unsigned pmask = (in_window && !exact) ? plane_mask : (1u << A.nplanes) - 1u;
+      // grid units: FP32 test first, FP64 on the positions within pmargin
+      // cells of a plane
       const float ufx = ((float)cx + fx) + dux, ufy = ((float)cy + fy) + duy;
-      for (unsigned mk = pmask; mk; mk &= mk - 1) {
-        const MpmPlaneDev &pl = A.planes[__ffs(mk) - 1];
+      for (int k = 0; k < A.nplanes; ++k) {
+        const MpmPlaneDev &pl = A.planes[k];
         if (ufy < pl.fulb - A.pmargin) continue;
         const float dapprox = pl.fn[0] * (ufx - pl.fux[0]) + pl.fn[1] * (ufy - pl.fux[1]);
         if (dapprox > A.pmargin) continue;
@@ -950,6 +897,7 @@ __device__ __forceinline__ void ugimp_tile(const MixedArgs &A, const int bin, Ug
           vel = make_float2(0.0f, 0.0f);
         }
       }
+      int ncx, ncy;
       float nfx, nfy;
       split_u(un.x, ncx, nfx);
       split_u(un.y, ncy, nfy);
@@ -961,12 +909,7 @@ __device__ __forceinline__ void ugimp_tile(const MixedArgs &A, const int bin, Ug
       A.v[p] = vel;
       A.strain[p] = st;
       A.flags[p] = (uint8_t)((fl & ~1) | jh);
-      if ((ncx != gcx) | (ncy != gcy)) {
-        ++left_cell;
-        // the next step's G2P window
-        left_window += (ncx - 1 - VX < 0) | (ncy - 1 - VY < 0) | (ncx + 2 - VX >= UVA_W) |
-                       (ncy + 2 - VY >= UVA_W);
-      }
+      moved += (ncx != cx) | (ncy != cy);
       if (!in_grid_cell(A, ncx, ncy) || !ugimp_axis(ncx, nfx, hl, A.nx, bx, wx, gx) ||
           !ugimp_axis(ncy, nfy, hl, A.ny, by, wy, gy)) {
         atomicOr(A.status, (uint32_t)HG_STATUS_OUT_OF_GRID);
@@ -977,74 +920,30 @@ __device__ __forceinline__ void ugimp_tile(const MixedArgs &A, const int bin, Ug
     float s00, s01, s11;
     stress_factor(st, jh, mv.y, A.inv_h, A.kappa, A.mu, s00, s01, s11);
     const float mvx = mv.x * vel.x, mvy = mv.x * vel.y;
-    const bool in_acc = ncx - 1 - WX >= 0 && ncy - 1 - WY >= 0 && ncx + 2 - WX < UACC_W &&
-                        ncy + 2 - WY < UACC_W;
+    const unsigned sx = ugimp_support(wx, gx), sy = ugimp_support(wy, gy);
 #pragma unroll
     for (int ky = 0; ky < 3; ++ky) {
 #pragma unroll
       for (int kx = 0; kx < 3; ++kx) {
+        if (!((sx >> kx) & (sy >> ky) & 1u)) continue; // outside the support
         const float w = wx[kx] * wy[ky];
         const float dX = gx[kx] * wy[ky], dY = wx[kx] * gy[ky];
-        if (w == 0.0f && dX == 0.0f && dY == 0.0f) continue; // outside the support
+        const int64_t node = (int64_t)(by + ky) * row + (bx + kx);
+        if (!HG_INDEX_OK(node, nn, A.status)) continue;
         float4 add = make_float4(w * mvx, w * mvy, 0.0f, 0.0f);
         if (w != 0.0f) { // nodes of zero weight get no force (PhysicsGrid.cpp:439-441)
           add.z = s00 * dX + s01 * dY;
           add.w = s01 * dX + s11 * dY;
         }
-        if (in_acc) {
-          const int k = (by - WY + ky) * UACC_W + bx - WX + kx;
-          atomicAdd(&S.acc[0][k], w * mv.x);
-          atomicAdd(&S.acc[1][k], add.x);
-          atomicAdd(&S.acc[2][k], add.y);
-          atomicAdd(&S.acc[3][k], add.z);
-          atomicAdd(&S.acc[4][k], add.w);
-        } else {
-          const int64_t node = (int64_t)(by + ky) * row + (bx + kx);
-          if (!HG_INDEX_OK(node, nn, A.status)) continue;
-          atomicAdd(&A.accm[node], w * mv.x);
-          atomicAdd(&A.acc4[node], add);
-        }
+        atomicAdd(&A.accm[node], w * mv.x);
+        atomicAdd(&A.acc4[node], add);
       }
     }
   }
   if (nonfinite) atomicOr(A.status, (uint32_t)HG_STATUS_NONFINITE);
-  if (left_window) atomicAdd(&S.out[0], left_window);
-  if (left_cell) atomicAdd(&S.out[1], left_cell);
-  __syncthreads();
-  // ---- the node window, flushed to the global accumulators ----
-  for (int k = tid; k < UACC_W * UACC_W; k += THREADS) {
-    float sum[5];
-#pragma unroll
-    for (int c = 0; c < 5; ++c) {
-      sum[c] = S.acc[c][k];
-      S.acc[c][k] = 0.f; // ready for the next tile
-    }
-    if (sum[0] == 0.f && sum[1] == 0.f && sum[2] == 0.f && sum[3] == 0.f && sum[4] == 0.f)
-      continue;
-    const int ix = WX + k % UACC_W, iy = WY + k / UACC_W;
-    if (ix < 0 || iy < 0 || ix > A.nx || iy > A.ny) continue;
-    const int node = iy * row + ix;
-    atomicAdd(&A.accm[node], sum[0]);
-    atomicAdd(&A.acc4[node], make_float4(sum[1], sum[2], sum[3], sum[4]));
-  }
-  __syncthreads();
-  if (tid < 2 && S.out[tid]) atomicAdd(&A.outside[tid], S.out[tid]);
-}
-
-template <bool PRIME>
-__global__ void __launch_bounds__(THREADS, 3) kxu_g2p2g(const __grid_constant__ MixedArgs A) {
-  __shared__ UgimpSmem S;
-  zero_uacc(S);
-  // launched with programmatic dependence on the grid update before it: only
-  // shared memory is touched before the wait
-  pdl_wait();
-  pdl_trigger();
-  const int nact = *A.nactive;
-  for (int t = blockIdx.x; t < nact; t += gridDim.x) {
-    const int tile = A.active[t];
-    if (!HG_INDEX_OK(tile, (int64_t)A.ntx * A.nty, A.status)) continue;
-    ugimp_tile<PRIME>(A, tile, S);
-  }
+  // points that changed cell: the re-sort trigger of the linear kernel
+  for (int o = 16; o > 0; o >>= 1) moved += __shfl_down_sync(0xffffffffu, moved, o);
+  if ((threadIdx.x & 31) == 0 && moved) atomicAdd(&A.outside[1], moved);
 }
 
 // Node update of one tile; one thread per node of the 16x16 tile.
@@ -1598,11 +1497,16 @@ int update_per_sm(const hg_launch_shape &s) {
   return s.update_ctas_per_sm > 0 ? s.update_ctas_per_sm : DEFAULT_UPDATE_CTAS;
 }
 int fused_blocks(hg_mpm *m) { return m->ctx->num_sms * fused_per_sm(m->shape); }
+// the uGIMP kernel walks the points: up to 8 CTAs per SM
+int ugimp_blocks(hg_mpm *m) {
+  const int64_t b = (m->n + THREADS - 1) / THREADS;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)m->ctx->num_sms * 8));
+}
 // G2P of this step fused with P2G of the next (or the first P2G, PRIME)
 template <bool PRIME>
 void launch_particle_kernel(hg_mpm *m, const MixedArgs &A, cudaStream_t s) {
   if (m->p.basis == HG_BASIS_UGIMP) {
-    HG_LAUNCH_PDL(kxu_g2p2g<PRIME>, fused_blocks(m), THREADS, 0, s, A);
+    HG_LAUNCH_PDL(kxu_step<PRIME>, ugimp_blocks(m), THREADS, 0, s, A);
   } else {
     HG_LAUNCH_PDL(kx_g2p2g<PRIME>, fused_blocks(m), THREADS, fused_smem_bytes(), s, A);
   }

@@ -53,10 +53,16 @@ struct Mt19937 {
   uint32_t next() {
     if (i >= N) {
       if (i == N + 1) seed(4357u);
-      for (int k = 0; k < N; ++k) {
-        const uint32_t y = (s[k] & 0x80000000u) | (s[(k + 1) % N] & 0x7fffffffu);
-        s[k] = s[(k + M) % N] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
-      }
+      // the twist of every word in place, in order; the index arithmetic
+      // mod N split into its three ranges
+      auto twist = [&](int k, int k1, int km) {
+        const uint32_t y = (s[k] & 0x80000000u) | (s[k1] & 0x7fffffffu);
+        s[k] = s[km] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+      };
+      int k = 0;
+      for (; k < N - M; ++k) twist(k, k + 1, k + M);
+      for (; k < N - 1; ++k) twist(k, k + 1, k + M - N);
+      twist(N - 1, 0, M - 1);
       i = 0;
     }
     uint32_t y = s[i++];
@@ -231,6 +237,17 @@ struct FillGrid {
   }
 };
 
+// t advanced k times by "if (++t == 0) t = 1": the stamps run through
+// 1 .. 2^32 - 1 in a cycle, and 0 (not yet stamped) comes before 1.
+inline void advance_test_id(int &t, uint64_t k) {
+  if (k == 0) return;
+  const uint64_t cycle = 0xFFFFFFFFull; // stamps 1 .. 2^32 - 1
+  const uint64_t u = (uint32_t)t;
+  // index in the cycle: stamp 1 is 0, stamp 0 (the start) is -1
+  const uint64_t idx = u == 0 ? (k - 1) % cycle : (u - 1 + k % cycle) % cycle;
+  t = (int)(uint32_t)(idx + 1);
+}
+
 // CAvoidAVoid::avoidAVoid with randomFillRegion (AvoidAvoid.cpp:103-183):
 // bodies (px, py, rad) grow by the accepted samples, whose radii are at most
 // r_max.
@@ -253,7 +270,31 @@ hg_status fill_regions(hg_resampler &R, const std::vector<Box> &regions, double 
   double rc = r_max;
   for (size_t b = 0; b < px.size(); ++b)
     if (rad[b] > rc && rad[b] <= 4.0 * mean_r) rc = rad[b];
-  FillGrid grid;
+  // scratch kept between calls (the interval repeats with similar sizes, and
+  // fresh pages would be faulted in on every call)
+  // (per calling thread; the worker threads below reach the caller's through
+  // these references)
+  static thread_local FillGrid tl_grid;
+  static thread_local std::vector<int> tl_cell_of;
+  static thread_local std::vector<double> tl_tx, tl_ty, tl_tr;
+  static thread_local std::vector<uint8_t> tl_hit;
+  FillGrid &grid = tl_grid;
+  std::vector<int> &cell_of = tl_cell_of;
+  std::vector<double> &tx = tl_tx, &ty = tl_ty, &tr = tl_tr;
+  std::vector<uint8_t> &hit = tl_hit;
+  grid.bx.clear();
+  grid.by.clear();
+  grid.br.clear();
+  grid.ix.clear();
+  grid.iy.clear();
+  grid.ir.clear();
+  grid.next.clear();
+  grid.sx.clear();
+  grid.sy.clear();
+  grid.sr.clear();
+  grid.wx.clear();
+  grid.wy.clear();
+  grid.wr.clear();
   grid.x0 = g0x;
   grid.y0 = g0y;
   grid.cw = 2.0 * rc;
@@ -264,20 +305,26 @@ hg_status fill_regions(hg_resampler &R, const std::vector<Box> &regions, double 
   // wholly outside the grid's extent cannot conflict with a sample (samples
   // lie in the regions, six mean radii inside that extent); the reference's
   // grid leaves it out too.
-  std::vector<int> cell_of(px.size(), -1);
+  // cell of each body's centre (-1: outside the extent, -2: wider than
+  // cw / 2), over host threads; then a counting sort
+  cell_of.assign(px.size(), -1);
+  hg::host_parallel(px.size(), 16384, [&](size_t b0, size_t b1) {
+    for (size_t b = b0; b < b1; ++b) {
+      if (px[b] + rad[b] < g0x || px[b] - rad[b] > g1x || py[b] + rad[b] < g0y ||
+          py[b] - rad[b] > g1y)
+        continue;
+      cell_of[b] = rad[b] > 0.5 * grid.cw ? -2 : grid.cy(py[b]) * grid.nx + grid.cx(px[b]);
+    }
+  });
   grid.start.assign(ncell + 1, 0);
   for (size_t b = 0; b < px.size(); ++b) {
-    if (px[b] + rad[b] < g0x || px[b] - rad[b] > g1x || py[b] + rad[b] < g0y ||
-        py[b] - rad[b] > g1y)
-      continue;
-    if (rad[b] > 0.5 * grid.cw) {
+    if (cell_of[b] == -2) {
       grid.ix.push_back(px[b]);
       grid.iy.push_back(py[b]);
       grid.ir.push_back(rad[b]);
-      continue;
+    } else if (cell_of[b] >= 0) {
+      grid.start[cell_of[b] + 1]++;
     }
-    cell_of[b] = grid.cy(py[b]) * grid.nx + grid.cx(px[b]);
-    grid.start[cell_of[b] + 1]++;
   }
   for (size_t c = 0; c < ncell; ++c) grid.start[c + 1] += grid.start[c];
   const int nb = grid.start[ncell];
@@ -302,7 +349,9 @@ hg_status fill_regions(hg_resampler &R, const std::vector<Box> &regions, double 
   // trials at once, over host threads) nor with the trials accepted before
   // it (tested in trial order).
   const size_t T = 16 * regions.size();
-  std::vector<double> tx(T), ty(T), tr(T);
+  tx.resize(T);
+  ty.resize(T);
+  tr.resize(T);
   size_t t = 0;
   for (const Box &reg : regions) {
     const double dx = reg.b[2] - reg.b[0], dy = reg.b[3] - reg.b[1];
@@ -313,19 +362,20 @@ hg_status fill_regions(hg_resampler &R, const std::vector<Box> &regions, double 
       if (st != HG_OK) return st;
     }
   }
-  std::vector<uint8_t> hit(T);
+  hit.resize(T);
   hg::host_parallel(T, 4096, [&](size_t b, size_t e) {
     for (size_t k = b; k < e; ++k) hit[k] = grid.conflict_initial(tx[k], ty[k], tr[k]) ? 1 : 0;
   });
   for (size_t k = 0; k < T; ++k) {
-    // the reference's mailbox stamp advances once per test
-    if (++R.test_id == 0) R.test_id = 1;
     if (hit[k] || grid.conflict_accepted(tx[k], ty[k], tr[k])) continue;
     px.push_back(tx[k]);
     py.push_back(ty[k]);
     rad.push_back(tr[k]);
     grid.add_sample(tx[k], ty[k], tr[k]);
   }
+  // the reference's mailbox stamp advances once per test, through 1 .. 2^32 - 1
+  // (0 is skipped on the wrap)
+  advance_test_id(R.test_id, T);
   return HG_OK;
 }
 

@@ -148,16 +148,21 @@ void packing_fraction(hg_zones &z, int64_t nd, const double *q3, const double *r
   hg::host_parallel(ny, 8, [&](size_t jb, size_t je) { rows((unsigned)jb, (unsigned)je); });
   // cells within half a window of a material point count as dense; the
   // reference's test excludes the first row and column (gid > 0)
-  for (int64_t p = 0; p < np; ++p) {
-    const double x = pq[2 * p] - z.ls_min[0], y = pq[2 * p + 1] - z.ls_min[1];
-    const int gi0 = (int)std::floor((x - w * 0.5) / z.ls_h);
-    const int gj0 = (int)std::floor((y - w * 0.5) / z.ls_h);
-    const int gi1 = (int)std::floor((x + w * 0.5) / z.ls_h);
-    const int gj1 = (int)std::floor((y + w * 0.5) / z.ls_h);
-    for (int j = std::max(gj0, 1); j <= std::min(gj1, (int)ny - 1); ++j)
-      for (int i = std::max(gi0, 1); i <= std::min(gi1, (int)nx - 1); ++i)
-        z.phi[(size_t)j * nx + i] = 1.0;
-  }
+  // (over host threads by bands of rows: each band sets only its own cells)
+  hg::host_parallel(ny, 16, [&](size_t rb, size_t re) {
+    for (int64_t p = 0; p < np; ++p) {
+      const double x = pq[2 * p] - z.ls_min[0], y = pq[2 * p + 1] - z.ls_min[1];
+      const int gj0 = (int)std::floor((y - w * 0.5) / z.ls_h);
+      const int gj1 = (int)std::floor((y + w * 0.5) / z.ls_h);
+      const int j0 = std::max({gj0, 1, (int)rb}), j1 = std::min({gj1, (int)ny - 1, (int)re - 1});
+      if (j0 > j1) continue;
+      const int gi0 = (int)std::floor((x - w * 0.5) / z.ls_h);
+      const int gi1 = (int)std::floor((x + w * 0.5) / z.ls_h);
+      for (int j = j0; j <= j1; ++j)
+        for (int i = std::max(gi0, 1); i <= std::min(gi1, (int)nx - 1); ++i)
+          z.phi[(size_t)j * nx + i] = 1.0;
+    }
+  });
 }
 
 void distance_field(hg_zones &z) {
@@ -203,27 +208,33 @@ void distance_field(hg_zones &z) {
   auto gpx = [&](int i) { return W * (double)i / (double)nx + z.ls_min[0]; };
   auto gpy = [&](int j) { return H * (double)j / (double)ny + z.ls_min[1]; };
   auto norm = [](double a, double b) { return std::sqrt(a * a + b * b); };
-  for (size_t p = 0; p < sx.size(); ++p) {
-    const double r = 3.0 * h;
-    const double x0 = sx[p] - r, y0 = sy[p] - r, x1 = sx[p] + r, y1 = sy[p] + r;
-    auto lo = [&](double v, double m, double ext, unsigned n) {
-      return std::max<int>(0, std::min<int>((int)n, (int)std::floor((double)n * (v - m) / ext)));
-    };
-    auto up = [&](double v, double m, double ext, unsigned n) {
-      return std::max<int>(0, std::min<int>((int)n, (int)std::ceil((double)n * (v - m) / ext)));
-    };
-    const int i0 = lo(x0, z.ls_min[0], W, nx), j0 = lo(y0, z.ls_min[1], H, ny);
-    const int i1 = up(x1, z.ls_min[0], W, nx), j1 = up(y1, z.ls_min[1], H, ny);
-    for (int j = j0; j <= j1; ++j)
-      for (int i = i0; i <= i1; ++i) {
-        const size_t f = (size_t)j * (nx + 1) + i;
-        const double dd = norm(gpx(i) - sx[p], gpy(j) - sy[p]);
-        if (dd < d[f]) {
-          d[f] = dd;
-          closest[f] = (int64_t)p;
+  // (over host threads by bands of grid rows: every grid point still sees
+  // the samples in order, so ties go to the same sample)
+  hg::host_parallel((size_t)ny + 1, 16, [&](size_t rb, size_t re) {
+    for (size_t p = 0; p < sx.size(); ++p) {
+      const double r = 3.0 * h;
+      const double x0 = sx[p] - r, y0 = sy[p] - r, x1 = sx[p] + r, y1 = sy[p] + r;
+      auto lo = [&](double v, double m, double ext, unsigned n) {
+        return std::max<int>(0, std::min<int>((int)n, (int)std::floor((double)n * (v - m) / ext)));
+      };
+      auto up = [&](double v, double m, double ext, unsigned n) {
+        return std::max<int>(0, std::min<int>((int)n, (int)std::ceil((double)n * (v - m) / ext)));
+      };
+      const int j0 = std::max(lo(y0, z.ls_min[1], H, ny), (int)rb);
+      const int j1 = std::min(up(y1, z.ls_min[1], H, ny), (int)re - 1);
+      if (j0 > j1) continue;
+      const int i0 = lo(x0, z.ls_min[0], W, nx), i1 = up(x1, z.ls_min[0], W, nx);
+      for (int j = j0; j <= j1; ++j)
+        for (int i = i0; i <= i1; ++i) {
+          const size_t f = (size_t)j * (nx + 1) + i;
+          const double dd = norm(gpx(i) - sx[p], gpy(j) - sy[p]);
+          if (dd < d[f]) {
+            d[f] = dd;
+            closest[f] = (int64_t)p;
+          }
         }
-      }
-  }
+    }
+  });
   std::vector<size_t> ring;
   ring.reserve(npts);
   for (size_t f = 0; f < npts; ++f)
@@ -262,8 +273,22 @@ void distance_field(hg_zones &z) {
 void labels(hg_zones &z) {
   const unsigned nx = z.N[0], ny = z.N[1];
   const double lvl = z.d.rzone_level_set, half = z.d.rzone_half_thickness;
+  // Both passes over host threads in chunks of rows, each chunk listing its
+  // boxes in (row, column) order; the lists join in chunk order, the order of
+  // the sequential pass.
+  constexpr unsigned ROWS = 8;
+  auto chunked = [](unsigned rows, std::vector<hg_zones::Box> &out, auto body) {
+    const size_t nc = (rows + ROWS - 1) / ROWS;
+    std::vector<std::vector<hg_zones::Box>> part(nc);
+    hg::host_parallel(nc, 2, [&](size_t cb, size_t ce) {
+      for (size_t c = cb; c < ce; ++c)
+        body((unsigned)(c * ROWS), std::min<unsigned>(rows, (unsigned)((c + 1) * ROWS)), part[c]);
+    });
+    for (auto &v : part) out.insert(out.end(), v.begin(), v.end());
+  };
   z.ls_rzones.clear();
-  for (unsigned j = 0; j < ny; ++j)
+  chunked(ny, z.ls_rzones, [&](unsigned jb, unsigned je, std::vector<hg_zones::Box> &ls_rzones) {
+  for (unsigned j = jb; j < je; ++j)
     for (unsigned i = 0; i < nx; ++i) {
       const size_t a = (size_t)j * (nx + 1) + i, b = a + (nx + 1);
       const double dmin = std::min(std::min(z.dist[a], z.dist[a + 1]), std::min(z.dist[b], z.dist[b + 1]));
@@ -280,9 +305,10 @@ void labels(hg_zones &z) {
         hg_zones::Box bx{{z.ls_min[0] + ddx * (double)i, z.ls_min[1] + ddy * (double)j,
                           z.ls_min[0] + ddx * (i + 1.0), z.ls_min[1] + ddy * (j + 1.0)},
                          {(int32_t)i, (int32_t)j}};
-        z.ls_rzones.push_back(bx);
+        ls_rzones.push_back(bx);
       }
     }
+  });
   // MPM cells from the level-set cells they overlap, with hysteresis
   z.prev = z.label;
   z.rzones.clear();
@@ -290,7 +316,12 @@ void labels(hg_zones &z) {
   const int mx = z.d.mpm_cells[0], my = z.d.mpm_cells[1];
   const double cw = z.d.mpm_cell_width;
   const bool direct_ok = z.d.allow_direct_transitions != 0;
-  for (int j = 0; j < my; ++j)
+  // the direct transitions of each chunk, joined after the pass
+  const size_t nchunk = ((unsigned)my + ROWS - 1) / ROWS;
+  std::vector<std::vector<hg_zones::Box>> direct_part(nchunk);
+  chunked((unsigned)my, z.rzones, [&](unsigned jb, unsigned je, std::vector<hg_zones::Box> &rzones) {
+  std::vector<hg_zones::Box> &direct = direct_part[jb / ROWS];
+  for (int j = (int)jb; j < (int)je; ++j)
     for (int i = 0; i < mx; ++i) {
       const double x0 = z.d.mpm_grid_min[0] + (double)i * cw;
       const double y0 = z.d.mpm_grid_min[1] + (double)j * cw;
@@ -320,14 +351,16 @@ void labels(hg_zones &z) {
       } else if (nc > 0) {
         if (direct_ok) {
           lab = ZC;
-          if (was == ZD) z.direct.push_back(bx);
+          if (was == ZD) direct.push_back(bx);
         } else {
           lab = (was == ZC || was == ZH) ? ZC : ZH;
         }
       }
       z.label[f] = lab;
-      if (lab == ZH && nh + nc + nd > 0) z.rzones.push_back(bx);
+      if (lab == ZH && nh + nc + nd > 0) rzones.push_back(bx);
     }
+  });
+  for (auto &v : direct_part) z.direct.insert(z.direct.end(), v.begin(), v.end());
 }
 
 

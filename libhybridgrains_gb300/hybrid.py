@@ -14,7 +14,10 @@ state copied from the device, and the result is copied back
   DEM contact history renumbered), and the accumulators are cleared.
 
 ``precision=MIXED`` runs the MPM bulk in FP32 with FP64 positions (the
-coupling exchange is still formed in FP64); the default is the FP64 step.
+coupling exchange is still formed in FP64) and, unless ``dem_precision`` says
+otherwise, the DEM contact law in FP32 with FP64 positions and pairwise
+differences; the default is the FP64 step of both, the reference's
+arithmetic.
 
 Host copies kept between intervals: reference positions q0, initial masses
 and volumes (m0, volume0) and half widths of the points; reference
@@ -33,7 +36,7 @@ from . import DEM, FP64, MPM, Hybrid, Resampler, Zones, scene_xml, scenes
 
 class HybridSim:
     def __init__(self, ctx, scene, basis=None, point_headroom=2.0, grain_headroom=3.0,
-                 precision=FP64):
+                 precision=FP64, dem_precision=None):
         cfg, sc, dp = scene["mpm"], scene["dem"], scene["dem_params"]
         zs, rs = scene["zones"], scene["resampling"]
         self.ctx, self.cfg, self.dt = ctx, cfg, cfg["dt"]
@@ -54,7 +57,8 @@ class HybridSim:
         # (the spatial grid's cell is one mean diameter in hybrid runs, whatever
         # the discrete scene's cell_scale)
         self.dem = DEM(ctx, dp.get("gravity", gravity), dp["kn"], dp["kt"], dp["gamman"],
-                       dp["gammat"], dp["mu"], planes, capacity=int(grain_headroom * nd) + 1024)
+                       dp["gammat"], dp["mu"], planes, capacity=int(grain_headroom * nd) + 1024,
+                       precision=precision if dem_precision is None else dem_precision)
         self.dem.upload(sc["q"], sc["v"], sc["r"], sc["m"], sc["I"], sc["fixed"])
         self.hyb = Hybrid(ctx, self.mpm, self.dem)
         g = self.mpm

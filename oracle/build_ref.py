@@ -10,9 +10,10 @@ lie in the reference checkout:
   ``seedMT``, ``randomMT``, ``randomMT_i``).
 
 The rest of the reference needs Eigen, RapidXML and HDF5, which are absent.
-The checkout is looked up in $HG_REFERENCE_ROOT, else /root/reference; when it
-is absent (as on machines that only run the GPU tests), nothing is built and
-the tests that need the library are skipped.
+The checkout is the argument (``python oracle/build_ref.py <reference_root>``,
+or ``build(root)``), else $HG_REFERENCE_ROOT. Without one, an earlier build
+is reused; where none exists (as on machines that only run the GPU tests)
+nothing is built and the tests that need the library are skipped.
 """
 import os
 import subprocess
@@ -23,16 +24,15 @@ OUT_DIR = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT_DIR, "libhg_ref.so")
 
 
-def reference_root():
-    return os.environ.get("HG_REFERENCE_ROOT", "/root/reference")
-
-
-def build(force=False):
-    src_dir = os.path.join(reference_root(), "hybridgrains2dnew")
+def build(root=None, force=False):
+    root = root or os.environ.get("HG_REFERENCE_ROOT")
+    if not root:
+        return LIB if os.path.exists(LIB) else None
+    src_dir = os.path.join(root, "hybridgrains2dnew")
     sources = [os.path.join(src_dir, "CircleRectangleIntersection.cpp"),
                os.path.join(src_dir, "random.c"), os.path.join(HERE, "ref_shim.cpp")]
     if not all(os.path.exists(s) for s in sources[:2]):
-        return None
+        return LIB if os.path.exists(LIB) else None
     if not force and os.path.exists(LIB) and \
             all(os.path.getmtime(s) <= os.path.getmtime(LIB) for s in sources):
         return LIB
@@ -50,4 +50,5 @@ def build(force=False):
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv))
+    args = [a for a in sys.argv[1:] if a != "--force"]
+    print(build(args[0] if args else None, force="--force" in sys.argv))

@@ -78,7 +78,15 @@ def run(ctx, precision):
         while done < steps:
             m.flow(cfg["dt"], 1000)
             done += 1000
-        assert m.status() == 0
+            st = m.status()
+            if st != 0:  # say which points left the grid, and where
+                d = m.download()
+                q, v = d["q"], d["v"]
+                off = (q[:, 0] < cfg["grid_min"][0]) | (q[:, 0] > cfg["grid_max"][0]) | \
+                      (q[:, 1] < cfg["grid_min"][1]) | (q[:, 1] > cfg["grid_max"][1]) | \
+                      ~np.isfinite(q).all(1)
+                raise AssertionError("status %d after %d steps; off the grid: %s at %s, v %s"
+                                     % (st, done, np.where(off)[0][:5], q[off][:5], v[off][:5]))
         out[steps] = m.download()["q"]
     return out
 

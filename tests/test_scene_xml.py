@@ -222,8 +222,9 @@ def test_hybrid_scene(tmp_path):
 
 
 def _reference_column_collapse():
-    from oracle.build_ref import reference_root
-    d = os.path.join(reference_root(), "assets", "hybridgrains2dnew", "column-collapse")
+    import __graft_entry__
+    root = os.environ.get("HG_REFERENCE_ROOT") or __graft_entry__.REFERENCE_CHECKOUT
+    d = os.path.join(root, "assets", "hybridgrains2dnew", "column-collapse")
     if not os.path.exists(os.path.join(d, "hybrid.xml")):
         pytest.skip("reference checkout absent")
     return d
