@@ -9,6 +9,8 @@
 #include <limits>
 #include <new>
 #include <string>
+#include <condition_variable>
+#include <mutex>
 #include <vector>
 
 namespace hg {
@@ -219,6 +221,78 @@ void set_dimensions(MpmParams &P, const double gmin[2], const double gmax[2], do
 } // namespace capi_impl
 
 using namespace capi_impl;
+
+namespace hg {
+namespace {
+
+// Worker threads of host_pool_run. A dispatch publishes the task and its
+// count under the lock and bumps the generation; workers and the caller
+// claim task indices from an atomic counter; the caller waits until every
+// claimed task has finished.
+struct HostPool {
+  std::mutex dispatch;                // one dispatch at a time
+  std::mutex m;
+  std::condition_variable wake, idle;
+  // written under m before next is reset (sequentially consistent), so a
+  // worker that claims an index below ntasks sees that dispatch's task
+  std::atomic<const std::function<void(size_t)> *> task{nullptr};
+  std::atomic<size_t> ntasks{0};
+  std::atomic<size_t> next{0};
+  size_t running = 0;                 // workers inside the current dispatch
+  uint64_t gen = 0;
+  size_t nthreads = 0;
+
+  void claim_all() {
+    for (size_t i; (i = next.fetch_add(1)) < ntasks.load();) (*task.load())(i);
+  }
+  void worker() {
+    uint64_t seen = 0;
+    std::unique_lock<std::mutex> lk(m);
+    for (;;) {
+      wake.wait(lk, [&] { return gen != seen; });
+      seen = gen;
+      ++running;
+      lk.unlock();
+      claim_all();
+      lk.lock();
+      if (--running == 0) idle.notify_all();
+    }
+  }
+  void run(size_t n, const std::function<void(size_t)> &f) {
+    std::lock_guard<std::mutex> d(dispatch);
+    {
+      std::lock_guard<std::mutex> lk(m);
+      const size_t want = std::min<size_t>(n - 1, 15);
+      while (nthreads < want) { // the pool lives as long as the process
+        std::thread(&HostPool::worker, this).detach();
+        ++nthreads;
+      }
+      task.store(&f);
+      ntasks.store(n);
+      next.store(0);
+      ++gen;
+    }
+    wake.notify_all();
+    claim_all();
+    std::unique_lock<std::mutex> lk(m);
+    idle.wait(lk, [&] { return running == 0 && next.load() >= ntasks.load(); });
+    task.store(nullptr);
+  }
+};
+
+} // namespace
+
+void host_pool_run(size_t ntasks, const std::function<void(size_t)> &task) {
+  static HostPool *pool = new HostPool(); // never destroyed: its threads outlive exit
+  if (ntasks == 0) return;
+  if (ntasks == 1) {
+    task(0);
+    return;
+  }
+  pool->run(ntasks, task);
+}
+
+} // namespace hg
 
 extern "C" {
 

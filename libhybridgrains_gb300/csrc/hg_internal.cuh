@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <functional>
 #include <thread>
 #include <utility>
 #include <string>
@@ -177,6 +178,12 @@ struct hg_context {
 };
 
 namespace hg {
+// Runs task(0) .. task(ntasks - 1) on the calling thread and the process's
+// pool of host worker threads (created on first use, kept for the life of
+// the process); returns when all are done. Calls from several host threads
+// take turns.
+void host_pool_run(size_t ntasks, const std::function<void(size_t)> &task);
+
 // Host loop over [0, n) split into contiguous ranges over the host threads
 // (hg_set_host_threads, by default the hardware concurrency up to 16), at
 // least min_per_worker items each; f(begin, end) must only write what its
@@ -191,10 +198,7 @@ void host_parallel(size_t n, size_t min_per_worker, F f) {
     f((size_t)0, n);
     return;
   }
-  std::vector<std::thread> pool;
-  for (size_t t = 1; t < workers; ++t) pool.emplace_back(f, n * t / workers, n * (t + 1) / workers);
-  f((size_t)0, n / workers);
-  for (auto &th : pool) th.join();
+  host_pool_run(workers, [&](size_t t) { f(n * t / workers, n * (t + 1) / workers); });
 }
 
 void context_retain(hg_context *c);
