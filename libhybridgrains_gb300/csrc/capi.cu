@@ -111,6 +111,23 @@ hg_status h2d(cudaStream_t s, T *dst, const T *src, size_t n) {
   return HG_OK;
 }
 
+// The address at which kernels reach p: p itself for device (or managed)
+// memory, the mapped address for page-locked host memory; nullptr for
+// pageable host memory (and for nullptr), which is copied instead.
+template <typename T> T *device_view(T *p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError(); // (clears the error of an unknown pointer)
+    return nullptr;
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return p;
+  if (a.type == cudaMemoryTypeHost && a.devicePointer) return static_cast<T *>(a.devicePointer);
+  return nullptr;
+}
+
+inline bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
 template <typename T>
 hg_status d2h(cudaStream_t s, T *dst, const T *src, size_t n) {
   if (n == 0 || dst == nullptr) return HG_OK;
@@ -566,6 +583,7 @@ hg_status hg_mpm_destroy(hg_mpm *m) {
     // buffers are released stream-ordered behind the queued work; the
     // read-back slot goes back to the context's pool for later work
     context_return_pair(ctx, m->h_outside);
+    context_return_pair(ctx, m->h_flag);
     if (m->outside_ev) cudaEventDestroy(m->outside_ev);
     for (cudaGraphExec_t &e : m->chunk_exec)
       if (e) cudaGraphExecDestroy(e);
@@ -765,30 +783,6 @@ static hg_status upload_impl(hg_mpm *m, int64_t n, const double *q, const double
     if (m->stage_u8.n < (size_t)n && (st = m->stage_u8.alloc(n))) return st;
     double *sq = m->stage_d.p, *sv = sq + 2 * n, *sm = sv + 2 * n, *svol = sm + n,
            *sbe = svol + n, *sJ = sbe + 4 * n, *shl = sJ + n;
-    if ((st = h2d(s, sq, q, 2 * n)) || (st = h2d(s, sv, v, 2 * n)) ||
-        (st = h2d(s, sm, mass, n)) || (st = h2d(s, svol, volume, n)))
-      return st;
-    if (be) {
-      if ((st = h2d(s, sbe, be, 4 * n))) return st;
-    } else {
-      HG_CUDA_TRY(cudaMemsetAsync(sbe, 0, sizeof(double) * 4 * n, s));
-      if ((st = fill(s, sbe, n, 1.0, 4, 0)) || (st = fill(s, sbe, n, 1.0, 4, 3))) return st;
-    }
-    if (J) {
-      if ((st = h2d(s, sJ, J, n))) return st;
-    } else if ((st = fill(s, sJ, n, 1.0))) {
-      return st;
-    }
-    if (jh) {
-      if ((st = h2d(s, m->stage_i.p, jh, n))) return st;
-    } else {
-      HG_CUDA_TRY(cudaMemsetAsync(m->stage_i.p, 0, sizeof(int32_t) * n, s));
-    }
-    if (kin) {
-      if ((st = h2d(s, m->stage_u8.p, kin, n))) return st;
-    } else {
-      HG_CUDA_TRY(cudaMemsetAsync(m->stage_u8.p, 0, n, s));
-    }
     const bool ugimp = m->p.basis == HG_BASIS_UGIMP;
     if (ugimp && n > 0) {
       // per-point half-widths; the FP32 weights of the MIXED kernel take
@@ -801,9 +795,48 @@ static hg_status upload_impl(hg_mpm *m, int64_t n, const double *q, const double
           return fail(HG_ERR_UNSUPPORTED, "MIXED uGIMP needs 0 < hl <= h / 2");
       }
       m->hl_cells = (float)(h[0] / m->p.h);
-      if ((st = h2d(s, shl, hl, n))) return st;
     }
+    // defaults of the arrays the caller leaves out, ahead of every chunk
+    if (!be) {
+      HG_CUDA_TRY(cudaMemsetAsync(sbe, 0, sizeof(double) * 4 * n, s));
+      if ((st = fill(s, sbe, n, 1.0, 4, 0)) || (st = fill(s, sbe, n, 1.0, 4, 3))) return st;
+    }
+    if (!J && (st = fill(s, sJ, n, 1.0))) return st;
+    if (!jh) HG_CUDA_TRY(cudaMemsetAsync(m->stage_i.p, 0, sizeof(int32_t) * n, s));
+    if (!kin) HG_CUDA_TRY(cudaMemsetAsync(m->stage_u8.p, 0, n, s));
+    // the copies of upload indices [i0, i1) into the staging arrays
+    auto copy = [&](int64_t i0, int64_t i1) -> hg_status {
+      const int64_t k = i1 - i0;
+      hg_status r;
+      if ((r = h2d(s, sq + 2 * i0, q + 2 * i0, 2 * k)) ||
+          (r = h2d(s, sv + 2 * i0, v + 2 * i0, 2 * k)) ||
+          (r = h2d(s, sm + i0, mass + i0, k)) || (r = h2d(s, svol + i0, volume + i0, k)))
+        return r;
+      if (be && (r = h2d(s, sbe + 4 * i0, be + 4 * i0, 4 * k))) return r;
+      if (J && (r = h2d(s, sJ + i0, J + i0, k))) return r;
+      if (jh && (r = h2d(s, m->stage_i.p + i0, jh + i0, k))) return r;
+      if (kin && (r = h2d(s, m->stage_u8.p + i0, kin + i0, k))) return r;
+      if (ugimp && (r = h2d(s, shl + i0, hl + i0, k))) return r;
+      return HG_OK;
+    };
     m->primed = false;
+    if (wait && n > 0) {
+      // arrays the GPU can reach (page-locked host or device memory) are
+      // read in place by the conversion kernel, without staging copies
+      const double *dq = device_view(q), *dv = device_view(v), *dm = device_view(mass),
+                   *dvol = device_view(volume), *dhl = device_view(hl),
+                   *dbe = device_view(be), *dJ = device_view(J);
+      const int32_t *djh = device_view(jh);
+      const uint8_t *dkin = device_view(kin);
+      if (dq && dv && dm && dvol && (!ugimp || dhl) && (!be || dbe) && (!J || dJ) &&
+          (!jh || djh) && (!kin || dkin))
+        return mixed_upload_direct(m, dq, dv, dm, dvol, ugimp ? dhl : nullptr, dbe, dJ, djh,
+                                   dkin);
+    }
+    if ((st = copy(0, n))) return st;
+    if (wait) // (synchronises)
+      return mixed_upload_direct(m, sq, sv, sm, svol, ugimp ? shl : nullptr, sbe, sJ,
+                                 m->stage_i.p, m->stage_u8.p);
     if ((st = mixed_upload(m, sq, sv, sm, svol, ugimp ? shl : nullptr, sbe, sJ, m->stage_i.p,
                            m->stage_u8.p)))
       return st;
@@ -886,11 +919,30 @@ hg_status hg_mpm_download(hg_mpm *m, double *q, double *v, double *be, double *J
     if (m->stage_d.n < (size_t)nd && (st = m->stage_d.alloc(nd))) return st;
     if (m->stage_i.n < (size_t)n && (st = m->stage_i.alloc(n))) return st;
     double *sq = m->stage_d.p, *sv = sq + 2 * n, *sbe = sv + 2 * n, *sJ = sbe + 4 * n;
-    if ((st = mixed_download(m, sq, sv, sbe, sJ, m->stage_i.p))) return st;
-    if ((st = d2h(s, q, sq, 2 * n)) || (st = d2h(s, v, sv, 2 * n)) ||
-        (st = d2h(s, be, sbe, 4 * n)) || (st = d2h(s, J, sJ, n)) ||
-        (st = d2h(s, jh, m->stage_i.p, n)))
+    int32_t *sjh = m->stage_i.p;
+    // the copies of output indices [i0, i1) out of the staging arrays
+    auto copy = [&](int64_t i0, int64_t i1) -> hg_status {
+      const int64_t k = i1 - i0;
+      hg_status r;
+      if ((q && (r = d2h(s, q + 2 * i0, sq + 2 * i0, 2 * k))) ||
+          (v && (r = d2h(s, v + 2 * i0, sv + 2 * i0, 2 * k))) ||
+          (be && (r = d2h(s, be + 4 * i0, sbe + 4 * i0, 4 * k))) ||
+          (J && (r = d2h(s, J + i0, sJ + i0, k))) || (jh && (r = d2h(s, jh + i0, sjh + i0, k))))
+        return r;
+      return HG_OK;
+    };
+    // outputs the GPU can reach are written in place by the conversion kernel
+    double *dq = device_view(q), *dv = device_view(v), *dbe = device_view(be),
+           *dJ = device_view(J);
+    int32_t *djh = device_view(jh);
+    bool done = false;
+    if ((!q || dq) && (!v || dv) && (!be || dbe) && (!J || dJ) && (!jh || djh) &&
+        aligned16(dq) && aligned16(dv) && aligned16(dbe) && aligned16(dJ) && aligned16(djh) &&
+        (st = mixed_download_direct(m, dq, dv, dbe, dJ, djh, &done)))
       return st;
+    if (!done) {
+      if ((st = mixed_download(m, sq, sv, sbe, sJ, sjh)) || (st = copy(0, n))) return st;
+    }
   }
   HG_CUDA_TRY(cudaStreamSynchronize(s));
   return HG_OK;

@@ -313,6 +313,14 @@ struct hg_mpm {
   hg::DevBuf<double> stage_d;
   hg::DevBuf<int32_t> stage_i;
   hg::DevBuf<uint8_t> stage_u8;
+  // MIXED: the live buffer's order as the last single-object re-sort left
+  // it: inv[i] is the slot of upload index i, skey[slot] the cell key the
+  // slot was sorted under; order_valid while they describe the live buffer
+  hg::DevBuf<int32_t> inv, skey;
+  bool order_valid = false;
+  int64_t order_n = 0; // the point count they were written for
+  hg::DevBuf<uint32_t> d_flag; // points outside their slot's window at upload
+  uint32_t *h_flag = nullptr;  // pinned mirror (a pair slot of the context)
 };
 
 namespace hg {
@@ -330,6 +338,21 @@ hg_status mixed_upload(hg_mpm *m, const double *q, const double *v,
                        const uint8_t *kin);
 hg_status mixed_download(hg_mpm *m, double *q, double *v, double *be,
                          double *J, int32_t *jh);
+// Transfers of the MIXED state straight between the caller's arrays (in the
+// reference's layouts, page-locked host or device memory) and the particle
+// buffers, by kernels that read or write them over the host link.
+// mixed_upload_direct: when the live buffer's order is still known (same
+// point count, nothing re-sorted it since) the points go to their slots and
+// the re-sort is skipped unless a point left its slot's tile window.
+// Absent be, J, jh, kin take the identity, 1, 0, 0. Synchronises.
+hg_status mixed_upload_direct(hg_mpm *m, const double *q, const double *v, const double *mass,
+                              const double *vol, const double *hl, const double *be,
+                              const double *J, const int32_t *jh, const uint8_t *kin);
+// mixed_download_direct: every output index from its slot; false in *done
+// when the order is unknown (the caller then takes mixed_download). Absent
+// outputs are skipped. Queued on the context's stream.
+hg_status mixed_download_direct(hg_mpm *m, double *q, double *v, double *be, double *J,
+                                int32_t *jh, bool *done);
 hg_status mixed_step(hg_mpm *m, double dt, int nsteps);
 hg_status mixed_download_grid(hg_mpm *m, double *mass, double *vel,
                               double *acc);

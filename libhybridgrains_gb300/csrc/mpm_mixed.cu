@@ -1051,18 +1051,22 @@ __global__ void kx_keys(int64_t n, int nx, int ny, int ntx, const double2 *__res
 
 __global__ void kx_scatter(int64_t n, const int32_t *__restrict__ keys,
                            const int32_t *__restrict__ offsets, int32_t *cursor,
-                           MixedParticles src, MixedParticles dst) {
+                           MixedParticles src, MixedParticles dst, int32_t *inv, int32_t *skey) {
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (p >= n) return;
   const int key = keys[p];
   const int64_t d = offsets[key] + atomicAdd(&cursor[key], 1);
+  const int32_t id = src.id[p];
   dst.u[d] = src.u[p];
   dst.v[d] = src.v[p];
   dst.mv[d] = src.mv[p];
   dst.strain[d] = src.strain[p];
   dst.flags[d] = src.flags[p];
-  dst.id[d] = src.id[p];
+  dst.id[d] = id;
   if (src.hl) dst.hl[d] = src.hl[p];
+  // the order tables: ids are upload indices 0 .. n-1
+  skey[d] = key;
+  if (id >= 0 && id < n) inv[id] = (int32_t)d;
 }
 
 __global__ void kx_active(int ntx, int nty, const int32_t *__restrict__ offsets,
@@ -1087,9 +1091,49 @@ __global__ void kx_active(int ntx, int nty, const int32_t *__restrict__ offsets,
   if (any) tiles[atomicAdd(&nactive[1], 1)] = b;
 }
 
+// True when tile b is in the active tile set: within one tile of a tile that
+// holds points (the tiles the grid update covers).
+__device__ __forceinline__ bool tile_active(const int32_t *__restrict__ off, int ntx, int nty,
+                                            int b) {
+  const int tx = b % ntx, ty = b / ntx;
+  for (int dy = -1; dy <= 1; ++dy)
+    for (int dx = -1; dx <= 1; ++dx) {
+      const int x = tx + dx, y = ty + dy;
+      if (x < 0 || y < 0 || x >= ntx || y >= nty) continue;
+      const int t = y * ntx + x;
+      if (off[(t + 1) * BIN_CELLS] > off[t * BIN_CELLS]) return true;
+    }
+  return false;
+}
+
+// The grid update writes (va, gm) only on active tiles. After a re-sort,
+// nodes of tiles outside the new set are cleared (those still holding a
+// mass), so that a tile that dropped out does not keep its last update.
+// One block of 256 threads per tile, one thread per node.
+__device__ __forceinline__ void clear_inactive_tile(int nx, int ny, int ntx, int nty,
+                                                    const int32_t *__restrict__ off, int b,
+                                                    float4 *va, float *gm) {
+  if (tile_active(off, ntx, nty, b)) return;
+  const int ix = (b % ntx) * BIN + (int)threadIdx.x % BIN;
+  const int iy = (b / ntx) * BIN + (int)threadIdx.x / BIN;
+  if (ix > nx || iy > ny) return;
+  const int64_t i = (int64_t)iy * (nx + 1) + ix;
+  if (gm[i] != 0.f) {
+    gm[i] = 0.f;
+    va[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+}
+
+__global__ void __launch_bounds__(BIN_CELLS) kx_clear_inactive(int nx, int ny, int ntx, int nty,
+                                                               const int32_t *__restrict__ off,
+                                                               float4 *va, float *gm) {
+  for (int b = blockIdx.x; b < ntx * nty; b += gridDim.x)
+    clear_inactive_tile(nx, ny, ntx, nty, off, b, va, gm);
+}
+
 // ---- batched re-sort -------------------------------------------------------------
 //
-// The re-sort of every batch member that needs one in a step, in six launches
+// The re-sort of every batch member that needs one in a step, in eight launches
 // whatever their number: the same counting sort as above, over (member, item)
 // work items. The host lays out, per member, the item counts of each pass as
 // prefix sums (points, keys, scan chunks, bins); a thread finds its member by
@@ -1101,6 +1145,8 @@ struct RebinArgs {
   MixedParticles src, dst;
   int32_t *keys, *counts, *offsets, *cursor, *bins, *tiles, *nactive, *chunk_sums;
   uint32_t *status, *outside;
+  float4 *va; // the grid update's outputs (cleared on tiles that leave the set)
+  float *gm;
 };
 
 struct RebinPrefix {
@@ -1269,47 +1315,200 @@ __global__ void kr_active(const RebinArgs *__restrict__ R, RebinPrefix P) {
   }
 }
 
+// kx_clear_inactive over (member, tile) items, one block per item
+__global__ void __launch_bounds__(BIN_CELLS) kr_clear_inactive(const RebinArgs *__restrict__ R,
+                                                               RebinPrefix P) {
+  const int64_t total = P.bins[P.nmem];
+  for (int64_t i = blockIdx.x; i < total; i += gridDim.x) {
+    const int m = member_of(P.bins, P.nmem, i);
+    const RebinArgs &a = R[m];
+    clear_inactive_tile(a.nx, a.ny, a.ntx, a.nty, a.offsets, (int)(i - P.bins[m]), a.va, a.gm);
+  }
+}
+
 // ---- upload / download conversion -------------------------------------------
 
-__global__ void kx_upload(int64_t n, double gx, double gy, double h,
+// Elements 2k and 2k + 1 of a: one 16-byte load when a is 16-byte aligned.
+__device__ __forceinline__ double2 pair_at(const double *__restrict__ a, int64_t k) {
+  if (((uintptr_t)a & 15u) == 0) return reinterpret_cast<const double2 *>(a)[k];
+  return make_double2(a[2 * k], a[2 * k + 1]);
+}
+
+// Upload index i of the staging arrays (reference layouts) converted into
+// slot d of dst; returns the point's position in grid units.
+__device__ __forceinline__ double2 upload_point(int64_t i, int64_t d, double gx, double gy,
+                                                double h, const double *__restrict__ q,
+                                                const double *__restrict__ v,
+                                                const double *__restrict__ m,
+                                                const double *__restrict__ vol,
+                                                const double *__restrict__ hl,
+                                                const double *__restrict__ be,
+                                                const double *__restrict__ J,
+                                                const int32_t *__restrict__ jh,
+                                                const uint8_t *__restrict__ kin,
+                                                MixedParticles dst) {
+  if (dst.hl) dst.hl[d] = (float)(hl[i] / h);
+  // pairs read as one 16-byte load where the array allows it (arrays read
+  // over the host link arrive in fewer, fuller requests)
+  const double2 qq = pair_at(q, i), vv = pair_at(v, i);
+  const double2 u = make_double2((qq.x - gx) / h, (qq.y - gy) / h);
+  dst.u[d] = u;
+  dst.v[d] = make_float2((float)vv.x, (float)vv.y);
+  dst.mv[d] = make_float2((float)m[i], (float)vol[i]);
+  // absent be, J, jh, kin: the identity, 1, 0 and 0 (a first upload)
+  float4 strain = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (be) {
+    const double2 c0 = pair_at(be, 2 * i), c1 = pair_at(be, 2 * i + 1);
+    const double b00 = c0.x, b10 = c0.y, b01 = c1.x, b11 = c1.y;
+    strain.y = (float)(b00 - 1.0);
+    strain.z = (float)(0.5 * (b10 + b01));
+    strain.w = (float)(b11 - 1.0);
+  }
+  if (J) strain.x = (float)(J[i] - 1.0);
+  dst.strain[d] = strain;
+  dst.flags[d] = (uint8_t)((jh && jh[i] != 0 ? 1 : 0) | (kin && kin[i] != 0 ? 2 : 0));
+  dst.id[d] = (int32_t)i;
+  return u;
+}
+
+// Upload indices [i0, i1) into the same slots (the re-sort follows).
+__global__ void kx_upload(int64_t i0, int64_t i1, double gx, double gy, double h,
                           const double *__restrict__ q, const double *__restrict__ v,
                           const double *__restrict__ m, const double *__restrict__ vol,
                           const double *__restrict__ hl, const double *__restrict__ be,
                           const double *__restrict__ J, const int32_t *__restrict__ jh,
                           const uint8_t *__restrict__ kin, MixedParticles dst) {
-  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  if (dst.hl) dst.hl[p] = (float)(hl[p] / h);
-  dst.u[p] = make_double2((q[2 * p] - gx) / h, (q[2 * p + 1] - gy) / h);
-  dst.v[p] = make_float2((float)v[2 * p], (float)v[2 * p + 1]);
-  dst.mv[p] = make_float2((float)m[p], (float)vol[p]);
-  const double b00 = be[4 * p], b10 = be[4 * p + 1], b01 = be[4 * p + 2], b11 = be[4 * p + 3];
-  dst.strain[p] = make_float4((float)(J[p] - 1.0), (float)(b00 - 1.0),
-                              (float)(0.5 * (b10 + b01)), (float)(b11 - 1.0));
-  dst.flags[p] = (uint8_t)((jh[p] != 0 ? 1 : 0) | (kin[p] != 0 ? 2 : 0));
-  dst.id[p] = (int32_t)p;
+  const int64_t i = i0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= i1) return;
+  upload_point(i, i, gx, gy, h, q, v, m, vol, hl, be, J, jh, kin, dst);
+}
+
+// Upload indices [i0, i1) into the slots the last re-sort gave them
+// (inv); *flag is set when a point is not in the G2P window of its slot's
+// tile (skey), or not in the grid: the kernels' tile lists then do not cover
+// it and the points must be re-sorted before they are used.
+__global__ void kx_upload_slots(int64_t i0, int64_t i1, int64_t n, int nx, int ny, int ntx,
+                                double gx, double gy, double h, const double *__restrict__ q,
+                                const double *__restrict__ v, const double *__restrict__ m,
+                                const double *__restrict__ vol, const double *__restrict__ hl,
+                                const double *__restrict__ be, const double *__restrict__ J,
+                                const int32_t *__restrict__ jh, const uint8_t *__restrict__ kin,
+                                const int32_t *__restrict__ inv,
+                                const int32_t *__restrict__ skey, MixedParticles dst,
+                                uint32_t *flag) {
+  const int64_t i = i0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= i1) return;
+  const int32_t d = inv[i];
+  if (d < 0 || d >= n) {
+    atomicOr(flag, 1u);
+    return;
+  }
+  const double2 u = upload_point(i, d, gx, gy, h, q, v, m, vol, hl, be, J, jh, kin, dst);
+  int cx, cy;
+  float fx, fy;
+  split_u(u.x, cx, fx);
+  split_u(u.y, cy, fy);
+  far_edge(nx, cx, fx);
+  far_edge(ny, cy, fy);
+  const int tile = skey[d] / BIN_CELLS;
+  const int wx = cx - ((tile % ntx) * BIN - DRIFT), wy = cy - ((tile / ntx) * BIN - DRIFT);
+  const bool in_grid = cx >= 0 && cy >= 0 && cx < nx && cy < ny;
+  if (!in_grid || (unsigned)wx > (unsigned)(VA_W - 2) || (unsigned)wy > (unsigned)(VA_W - 2))
+    atomicOr(flag, 1u);
+}
+
+// Slot k of src into output index o (reference layouts).
+__device__ __forceinline__ void download_point(int64_t k, int64_t o, double gx, double gy,
+                                               double h, MixedParticles src, double *q,
+                                               double *v, double *be, double *J, int32_t *jh) {
+  if (q) {
+    const double2 u = src.u[k];
+    q[2 * o] = gx + u.x * h;
+    q[2 * o + 1] = gy + u.y * h;
+  }
+  if (v) {
+    const float2 vv = src.v[k];
+    v[2 * o] = vv.x;
+    v[2 * o + 1] = vv.y;
+  }
+  if (be || J) {
+    const float4 s = src.strain[k];
+    if (be) {
+      be[4 * o] = 1.0 + (double)s.y;
+      be[4 * o + 1] = (double)s.z;
+      be[4 * o + 2] = (double)s.z;
+      be[4 * o + 3] = 1.0 + (double)s.w;
+    }
+    if (J) J[o] = 1.0 + (double)s.x;
+  }
+  if (jh) jh[o] = src.flags[k] & 1;
 }
 
 __global__ void kx_download(int64_t n, double gx, double gy, double h, MixedParticles src,
                             double *q, double *v, double *be, double *J, int32_t *jh) {
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k >= n) return;
-  const int64_t o = src.id[k];
-  const double2 u = src.u[k];
-  q[2 * o] = gx + u.x * h;
-  q[2 * o + 1] = gy + u.y * h;
-  const float2 vv = src.v[k];
-  v[2 * o] = vv.x;
-  v[2 * o + 1] = vv.y;
-  if (!be) return; // frames: positions and velocities only
-  const float4 s = src.strain[k];
-  be[4 * o] = 1.0 + (double)s.y;
-  be[4 * o + 1] = (double)s.z;
-  be[4 * o + 2] = (double)s.z;
-  be[4 * o + 3] = 1.0 + (double)s.w;
-  J[o] = 1.0 + (double)s.x;
-  jh[o] = src.flags[k] & 1;
+  download_point(k, src.id[k], gx, gy, h, src, q, v, be, J, jh);
 }
+
+// Output indices from the slots inv gives them, 256 per block, written to the
+// caller's arrays through shared memory: each warp store then covers whole
+// 16-byte pieces of consecutive outputs (over the host link, stores that
+// leave parts of a line for a later instruction cost a read-modify-write at
+// the host). The arrays must be 16-byte aligned; absent ones are skipped.
+__global__ void __launch_bounds__(256) kx_download_lines(int64_t n, double gx, double gy,
+                                                         double h, MixedParticles src,
+                                                         const int32_t *__restrict__ inv,
+                                                         double *q, double *v, double *be,
+                                                         double *J, int32_t *jh) {
+  __shared__ __align__(16) double s_q[512], s_v[512], s_be[1024], s_J[256];
+  __shared__ __align__(16) int32_t s_jh[256];
+  const int t = threadIdx.x;
+  const int64_t o0 = (int64_t)blockIdx.x * 256;
+  const int cnt = (int)(n - o0 < 256 ? n - o0 : 256);
+  if (t < cnt) {
+    int32_t k = inv[o0 + t];
+    if (k < 0 || k >= n) k = 0; // (the order tables cover every upload index)
+    const double2 u = src.u[k];
+    s_q[2 * t] = gx + u.x * h;
+    s_q[2 * t + 1] = gy + u.y * h;
+    const float2 vv = src.v[k];
+    s_v[2 * t] = vv.x;
+    s_v[2 * t + 1] = vv.y;
+    const float4 st = src.strain[k];
+    s_be[4 * t] = 1.0 + (double)st.y;
+    s_be[4 * t + 1] = (double)st.z;
+    s_be[4 * t + 2] = (double)st.z;
+    s_be[4 * t + 3] = 1.0 + (double)st.w;
+    s_J[t] = 1.0 + (double)st.x;
+    s_jh[t] = src.flags[k] & 1;
+  }
+  __syncthreads();
+  const double2 *q2 = reinterpret_cast<const double2 *>(s_q);
+  const double2 *v2 = reinterpret_cast<const double2 *>(s_v);
+  const double2 *b2 = reinterpret_cast<const double2 *>(s_be);
+  if (q && t < cnt) reinterpret_cast<double2 *>(q + 2 * o0)[t] = q2[t];
+  if (v && t < cnt) reinterpret_cast<double2 *>(v + 2 * o0)[t] = v2[t];
+  if (be) {
+    double2 *d = reinterpret_cast<double2 *>(be + 4 * o0);
+    for (int c = t; c < 2 * cnt; c += 256) d[c] = b2[c];
+  }
+  if (J) {
+    if (2 * t + 1 < cnt) {
+      reinterpret_cast<double2 *>(J + o0)[t] = reinterpret_cast<const double2 *>(s_J)[t];
+    } else if (2 * t + 1 == cnt) {
+      J[o0 + 2 * t] = s_J[2 * t];
+    }
+  }
+  if (jh) {
+    if (4 * t + 3 < cnt) {
+      reinterpret_cast<int4 *>(jh + o0)[t] = reinterpret_cast<const int4 *>(s_jh)[t];
+    } else {
+      for (int c = 4 * t; c < cnt && c < 4 * t + 4; ++c) jh[o0 + c] = s_jh[c];
+    }
+  }
+}
+
 
 __global__ void kx_grid_download(int64_t nn, const float *__restrict__ gm,
                                  const float4 *__restrict__ va, double *mass, double *vel,
@@ -1398,12 +1597,17 @@ hg_status rebin(hg_mpm *m) {
   if (st != HG_OK) return st;
   if (m->n > 0) {
     HG_LAUNCH(kx_scatter, blocks_for(m->n, 256), 256, 0, s, m->n, m->keys.p, m->offsets.p,
-              m->cursor.p, parts(m, m->cur), parts(m, 1 - m->cur));
+              m->cursor.p, parts(m, m->cur), parts(m, 1 - m->cur), m->inv.p, m->skey.p);
     HG_CHECK_LAUNCH();
   }
   m->cur = 1 - m->cur;
+  m->order_valid = true;
+  m->order_n = m->n;
   HG_LAUNCH(kx_active, blocks_for((int64_t)m->ntx * m->nty, 256), 256, 0, s, m->ntx, m->nty,
             m->offsets.p, m->active_bins.p, m->active_tiles.p, m->nactive.p);
+  HG_CHECK_LAUNCH();
+  HG_LAUNCH(kx_clear_inactive, std::min(m->ntx * m->nty, m->ctx->num_sms * 8), BIN_CELLS, 0, s,
+            m->p.nx, m->p.ny, m->ntx, m->nty, m->offsets.p, m->va.p, m->gm.p);
   HG_CHECK_LAUNCH();
   m->steps_since_rebin = 0;
   m->outside_pending = false;
@@ -1416,7 +1620,7 @@ size_t rebin_table_bytes(int nmax) {
   return (size_t)nmax * sizeof(RebinArgs) + 4 * (size_t)(nmax + 1) * sizeof(int64_t);
 }
 
-// Re-sorts the given members in six launches. table: page-locked host staging
+// Re-sorts the given members in eight launches. table: page-locked host staging
 // (rebin_table_bytes), dtable: its device copy; both free to overwrite.
 hg_status rebin_batch(hg_context *ctx, const std::vector<hg_mpm *> &R, unsigned char *table,
                       unsigned char *dtable) {
@@ -1448,6 +1652,8 @@ hg_status rebin_batch(hg_context *ctx, const std::vector<hg_mpm *> &R, unsigned 
     a.chunk_sums = m->scan_tmp.p;
     a.status = m->status.p;
     a.outside = m->outside.p;
+    a.va = m->va.p;
+    a.gm = m->gm.p;
     pp[i + 1] = pp[i] + m->n;
     pk[i + 1] = pk[i] + nkeys + 1;
     pc[i + 1] = pc[i] + (nkeys + 1 + RB_CHUNK - 1) / RB_CHUNK;
@@ -1478,8 +1684,12 @@ hg_status rebin_batch(hg_context *ctx, const std::vector<hg_mpm *> &R, unsigned 
   HG_CHECK_LAUNCH();
   HG_LAUNCH(kr_active, grid(pb[nm]), 256, 0, s, dR, P);
   HG_CHECK_LAUNCH();
+  HG_LAUNCH(kr_clear_inactive, (int)std::max<int64_t>(1, std::min<int64_t>(pb[nm], cap)),
+            BIN_CELLS, 0, s, dR, P);
+  HG_CHECK_LAUNCH();
   for (hg_mpm *m : R) {
     m->cur = 1 - m->cur;
+    m->order_valid = false; // the batched re-sort keeps no order tables
     m->steps_since_rebin = 0;
     m->outside_pending = false;
     m->rebins++;
@@ -1601,8 +1811,11 @@ hg_status mixed_alloc(hg_mpm *m) {
   HG_CUDA_TRY(cudaMemsetAsync(m->va.p, 0, sizeof(float4) * nn, s));
   HG_CUDA_TRY(cudaMemsetAsync(m->gm.p, 0, sizeof(float) * nn, s));
   HG_CUDA_TRY(cudaMemsetAsync(m->nactive.p, 0, sizeof(int32_t) * 2, s));
+  if ((st = m->inv.alloc(m->cap)) || (st = m->skey.alloc(m->cap)) || (st = m->d_flag.alloc(1)))
+    return st;
   m->h_outside = context_pinned_pair(m->ctx);
-  if (!m->h_outside) return fail(HG_ERR_OUT_OF_MEMORY, "page-locked host memory");
+  m->h_flag = context_pinned_pair(m->ctx);
+  if (!m->h_outside || !m->h_flag) return fail(HG_ERR_OUT_OF_MEMORY, "page-locked host memory");
   m->h_outside[0] = m->h_outside[1] = 0;
   HG_CUDA_TRY(cudaEventCreateWithFlags(&m->outside_ev, cudaEventDisableTiming));
   return HG_OK;
@@ -1613,7 +1826,7 @@ int64_t mixed_device_bytes(int nx, int ny, int64_t cap) {
   const int64_t ntx = (nx + 1 + BIN - 1) / BIN, nty = (ny + 1 + BIN - 1) / BIN;
   const int64_t nkeys = ntx * nty * BIN_CELLS;
   const int64_t per_point = sizeof(double2) + 2 * sizeof(float2) + sizeof(float4) + 1 + 4;
-  int64_t b = 2 * cap * per_point + cap * 4;                 // particle pairs, keys
+  int64_t b = 2 * cap * per_point + cap * 4 * 3;             // particle pairs, keys, order tables
   b += nn * (2 * sizeof(float4) + 2 * sizeof(float));       // acc4, va, accm, gm
   b += 4 * (3 * nkeys + 2 + scan_tmp_size(nkeys + 1));      // counts, offsets, cursor
   b += 4 * (2 * ntx * nty + 4);                             // active lists, counters
@@ -1628,8 +1841,8 @@ hg_status mixed_upload(hg_mpm *m, const double *q, const double *v, const double
   if (m->p.basis == HG_BASIS_UGIMP && n > 0 && !hl)
     return fail(HG_ERR_INVALID_ARGUMENT, "the uGIMP basis needs the half-widths hl");
   if (n > 0) {
-    HG_LAUNCH(kx_upload, blocks_for(n, 256), 256, 0, s, n, m->p.gmin[0], m->p.gmin[1], m->p.h,
-              q, v, mass, vol, hl, be, J, jh, kin, parts(m, m->cur));
+    HG_LAUNCH(kx_upload, blocks_for(n, 256), 256, 0, s, (int64_t)0, n, m->p.gmin[0],
+              m->p.gmin[1], m->p.h, q, v, mass, vol, hl, be, J, jh, kin, parts(m, m->cur));
     HG_CHECK_LAUNCH();
   }
   return prime(m);
@@ -1640,6 +1853,68 @@ hg_status mixed_download(hg_mpm *m, double *q, double *v, double *be, double *J,
   HG_LAUNCH(kx_download, blocks_for(m->n, 256), 256, 0, m->ctx->stream, m->n, m->p.gmin[0],
             m->p.gmin[1], m->p.h, parts(m, m->cur), q, v, be, J, jh);
   HG_CHECK_LAUNCH();
+  return HG_OK;
+}
+
+namespace {
+// The first P2G of points already in the live buffer's sorted order.
+hg_status prime_in_order(hg_mpm *m) {
+  cudaStream_t s = m->ctx->stream;
+  if (!m->shape_set && !tune_lookup(mixed_key(m), &m->shape)) m->shape = hg_launch_shape{0, 0};
+  const int64_t nn = (int64_t)(m->p.nx + 1) * (m->p.ny + 1);
+  HG_CUDA_TRY(cudaMemsetAsync(m->accm.p, 0, sizeof(float) * nn, s));
+  HG_CUDA_TRY(cudaMemsetAsync(m->acc4.p, 0, sizeof(float4) * nn, s));
+  MixedArgs A = make_args(m, 0.0, false);
+  launch_particle_kernel<true>(m, A, s);
+  HG_CHECK_LAUNCH();
+  m->primed = true;
+  return HG_OK;
+}
+} // namespace
+
+hg_status mixed_upload_direct(hg_mpm *m, const double *q, const double *v, const double *mass,
+                              const double *vol, const double *hl, const double *be,
+                              const double *J, const int32_t *jh, const uint8_t *kin) {
+  cudaStream_t s = m->ctx->stream;
+  const int64_t n = m->n;
+  if (m->p.basis == HG_BASIS_UGIMP && n > 0 && !hl)
+    return fail(HG_ERR_INVALID_ARGUMENT, "the uGIMP basis needs the half-widths hl");
+  const MixedParticles dst = parts(m, m->cur);
+  const double gx = m->p.gmin[0], gy = m->p.gmin[1], h = m->p.h;
+  hg_status st;
+  // the points keep the slots of the last re-sort when it sorted this many
+  if (n > 0 && m->order_valid && m->order_n == n) {
+    HG_CUDA_TRY(cudaMemsetAsync(m->d_flag.p, 0, sizeof(uint32_t), s));
+    HG_LAUNCH(kx_upload_slots, blocks_for(n, 256), 256, 0, s, (int64_t)0, n, n, m->p.nx,
+              m->p.ny, m->ntx, gx, gy, h, q, v, mass, vol, hl, be, J, jh, kin, m->inv.p,
+              m->skey.p, dst, m->d_flag.p);
+    HG_CHECK_LAUNCH();
+    HG_CUDA_TRY(cudaMemcpyAsync(m->h_flag, m->d_flag.p, sizeof(uint32_t),
+                                cudaMemcpyDeviceToHost, s));
+    if ((st = prime_in_order(m))) return st;
+    HG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (m->h_flag[0] == 0) return HG_OK;
+    m->primed = false; // a point left its slot's window: a first upload follows
+  }
+  if (n > 0) {
+    HG_LAUNCH(kx_upload, blocks_for(n, 256), 256, 0, s, (int64_t)0, n, gx, gy, h, q, v, mass,
+              vol, hl, be, J, jh, kin, dst);
+    HG_CHECK_LAUNCH();
+  }
+  if ((st = prime(m))) return st;
+  HG_CUDA_TRY(cudaStreamSynchronize(s));
+  return HG_OK;
+}
+
+hg_status mixed_download_direct(hg_mpm *m, double *q, double *v, double *be, double *J,
+                                int32_t *jh, bool *done) {
+  *done = false;
+  const int64_t n = m->n;
+  if (n <= 0 || !m->order_valid || m->order_n != n) return HG_OK;
+  HG_LAUNCH(kx_download_lines, blocks_for(n, 256), 256, 0, m->ctx->stream, n, m->p.gmin[0],
+            m->p.gmin[1], m->p.h, parts(m, m->cur), m->inv.p, q, v, be, J, jh);
+  HG_CHECK_LAUNCH();
+  *done = true;
   return HG_OK;
 }
 

@@ -238,6 +238,7 @@ hg_status mpm_state_load(hg_mpm *m, const void *src, int64_t bytes) {
   if ((st = read_segments(m->ctx->stream, src, bytes, h, mpm_segments(m, n, 0)))) return st;
   m->n = n;
   m->cur = 0;
+  m->order_valid = false; // the blob keeps no order tables
   m->primed = h.meta[5] != 0;
   m->steps_since_rebin = h.meta[6];
   m->rebins = h.meta[7];
