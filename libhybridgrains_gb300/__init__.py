@@ -839,10 +839,11 @@ class Resampler:
 
     def points(self):
         n, _, _ = self.stats()
-        out = dict(q0=np.zeros((n, 2)), q=np.zeros((n, 2)), v=np.zeros((n, 2)), m=np.zeros(n),
-                   vol=np.zeros(n), m0=np.zeros(n), vol0=np.zeros(n), w=np.zeros(n),
-                   hl=np.zeros(n), be=np.zeros((n, 4)), J=np.zeros(n),
-                   jh=np.zeros(n, dtype=np.int32), kin=np.zeros(n, dtype=np.uint8))
+        # (every element is written by the call)
+        out = dict(q0=np.empty((n, 2)), q=np.empty((n, 2)), v=np.empty((n, 2)), m=np.empty(n),
+                   vol=np.empty(n), m0=np.empty(n), vol0=np.empty(n), w=np.empty(n),
+                   hl=np.empty(n), be=np.empty((n, 4)), J=np.empty(n),
+                   jh=np.empty(n, dtype=np.int32), kin=np.empty(n, dtype=np.uint8))
         check("hg_resampler_get_points", self._h, *[_d(out[k]) for k in
               ("q0", "q", "v", "m", "vol", "m0", "vol0", "w", "hl", "be", "J")],
               _i32(out["jh"]), _u8(out["kin"]))

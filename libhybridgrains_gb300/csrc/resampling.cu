@@ -73,7 +73,32 @@ struct Mt19937 {
     return y;
   }
   float uniform() { return (float)next() * 2.3283064365386963e-10f; }
+  // the next n outputs, as n calls of next() would give them (tempered a
+  // block of the state at a time)
+  void fill(uint32_t *out, size_t n) {
+    size_t k = 0;
+    while (k < n) {
+      if (i >= N) { // the twist of next()
+        out[k++] = next();
+        continue;
+      }
+      const size_t take = std::min(n - k, (size_t)(N - i));
+      for (size_t j = 0; j < take; ++j) {
+        uint32_t y = s[i + j];
+        y ^= y >> 11;
+        y ^= (y << 7) & 0x9d2c5680u;
+        y ^= (y << 15) & 0xefc60000u;
+        y ^= y >> 18;
+        out[k + j] = y;
+      }
+      i += (int)take;
+      k += take;
+    }
+  }
 };
+
+// uniform() of a raw output
+inline float mt_uniform(uint32_t w) { return (float)w * 2.3283064365386963e-10f; }
 
 inline double dist2d(double ax, double ay, double bx, double by) {
   const double dx = ax - bx, dy = ay - by;
@@ -210,11 +235,13 @@ struct FillGrid {
   bool any_cell(double x, double y, double r, F f) const {
     const int reach = (int)std::ceil((0.5 * cw + r) / cw);
     const int i = cx(x), j = cy(y);
+    // the sample's own cell first: most conflicts are found there
+    if (f(j * nx + i)) return true;
     const int i0 = std::max(0, i - reach), i1 = std::min(nx - 1, i + reach);
     const int j0 = std::max(0, j - reach), j1 = std::min(ny - 1, j + reach);
     for (int jj = j0; jj <= j1; ++jj)
       for (int ii = i0; ii <= i1; ++ii)
-        if (f(jj * nx + ii)) return true;
+        if ((ii != i || jj != j) && f(jj * nx + ii)) return true;
     return false;
   }
   bool conflict_initial(double x, double y, double r) const {
@@ -248,40 +275,15 @@ inline void advance_test_id(int &t, uint64_t k) {
   t = (int)(uint32_t)(idx + 1);
 }
 
-// CAvoidAVoid::avoidAVoid with randomFillRegion (AvoidAvoid.cpp:103-183):
-// bodies (px, py, rad) grow by the accepted samples, whose radii are at most
-// r_max.
-template <typename Sampler>
-hg_status fill_regions(hg_resampler &R, const std::vector<Box> &regions, double mean_r,
-                       double r_max, std::vector<double> &px, std::vector<double> &py,
-                       std::vector<double> &rad, Sampler sampler) {
-  if (regions.empty()) return HG_OK;
-  double lo[2] = {regions[0].b[0], regions[0].b[1]}, up[2] = {regions[0].b[2], regions[0].b[3]};
-  for (size_t k = 1; k < regions.size(); ++k) {
-    lo[0] = std::min(lo[0], regions[k].b[0]);
-    lo[1] = std::min(lo[1], regions[k].b[1]);
-    up[0] = std::max(up[0], regions[k].b[2]);
-    up[1] = std::max(up[1], regions[k].b[3]);
-  }
-  const double g0x = lo[0] - 6.0 * mean_r, g0y = lo[1] - 6.0 * mean_r;
-  const double g1x = up[0] + 6.0 * mean_r, g1y = up[1] + 6.0 * mean_r;
-  // cells twice the largest radius of the samples and of the bodies up to
-  // four mean radii (wider ones go to the list every sample scans)
-  double rc = r_max;
-  for (size_t b = 0; b < px.size(); ++b)
-    if (rad[b] > rc && rad[b] <= 4.0 * mean_r) rc = rad[b];
+// The search grid of fill_trials over the bodies (px, py, rad), for samples
+// in [g0x, g1x] x [g0y, g1y], with cells 2 rc wide.
+void build_fill_grid(FillGrid &grid, double g0x, double g0y, double g1x, double g1y, double rc,
+                     const std::vector<double> &px, const std::vector<double> &py,
+                     const std::vector<double> &rad) {
   // scratch kept between calls (the interval repeats with similar sizes, and
   // fresh pages would be faulted in on every call)
-  // (per calling thread; the worker threads below reach the caller's through
-  // these references)
-  static thread_local FillGrid tl_grid;
   static thread_local std::vector<int> tl_cell_of;
-  static thread_local std::vector<double> tl_tx, tl_ty, tl_tr;
-  static thread_local std::vector<uint8_t> tl_hit;
-  FillGrid &grid = tl_grid;
   std::vector<int> &cell_of = tl_cell_of;
-  std::vector<double> &tx = tl_tx, &ty = tl_ty, &tr = tl_tr;
-  std::vector<uint8_t> &hit = tl_hit;
   grid.bx.clear();
   grid.by.clear();
   grid.br.clear();
@@ -342,29 +344,49 @@ hg_status fill_regions(hg_resampler &R, const std::vector<Box> &regions, double 
     }
   }
   grid.head.assign(ncell, -1);
+}
+
+// The trials of CAvoidAVoid::avoidAVoid with randomFillRegion
+// (AvoidAvoid.cpp:103-183) over the regions, against the bodies of the grid
+// (built over the bodies present, plus the samples accepted since): accepted
+// samples are appended to (px, py, rad) and added to the grid.
+template <typename Sampler>
+hg_status fill_trials(hg_resampler &R, FillGrid &grid, const std::vector<Box> &regions,
+                      std::vector<double> &px, std::vector<double> &py,
+                      std::vector<double> &rad, Sampler sampler) {
+  if (regions.empty()) return HG_OK;
+  static thread_local std::vector<double> tl_tx, tl_ty, tl_tr;
+  static thread_local std::vector<uint8_t> tl_hit;
+  static thread_local std::vector<uint32_t> tl_raw;
+  std::vector<double> &tx = tl_tx, &ty = tl_ty, &tr = tl_tr;
+  std::vector<uint8_t> &hit = tl_hit;
+  std::vector<uint32_t> &raw = tl_raw;
   // 16 trials per region in the reference's order. Neither the positions
   // (R.mt) nor the radii (the sampler's own engine) depend on which trials
-  // are accepted, so all are drawn first. A trial is accepted when it
-  // conflicts neither with the bodies present at the start (tested for all
-  // trials at once, over host threads) nor with the trials accepted before
-  // it (tested in trial order).
+  // are accepted, so all are drawn first: the position words in one run of
+  // the generator, converted over host threads, the radii in trial order. A
+  // trial is accepted when it conflicts neither with the bodies present at
+  // the start (tested for all trials at once, over host threads) nor with
+  // the trials accepted before it (tested in trial order).
   const size_t T = 16 * regions.size();
   tx.resize(T);
   ty.resize(T);
   tr.resize(T);
-  size_t t = 0;
-  for (const Box &reg : regions) {
-    const double dx = reg.b[2] - reg.b[0], dy = reg.b[3] - reg.b[1];
-    for (int trial = 0; trial < 16; ++trial, ++t) {
-      tx[t] = (double)R.mt.uniform() * dx + reg.b[0];
-      ty[t] = (double)R.mt.uniform() * dy + reg.b[1];
-      const hg_status st = sampler(tr[t]);
-      if (st != HG_OK) return st;
-    }
+  raw.resize(2 * T);
+  R.mt.fill(raw.data(), 2 * T);
+  for (size_t t = 0; t < T; ++t) {
+    const hg_status st = sampler(tr[t]);
+    if (st != HG_OK) return st;
   }
   hit.resize(T);
   hg::host_parallel(T, 4096, [&](size_t b, size_t e) {
-    for (size_t k = b; k < e; ++k) hit[k] = grid.conflict_initial(tx[k], ty[k], tr[k]) ? 1 : 0;
+    for (size_t k = b; k < e; ++k) {
+      const Box &reg = regions[k / 16];
+      const double dx = reg.b[2] - reg.b[0], dy = reg.b[3] - reg.b[1];
+      tx[k] = (double)mt_uniform(raw[2 * k]) * dx + reg.b[0];
+      ty[k] = (double)mt_uniform(raw[2 * k + 1]) * dy + reg.b[1];
+      hit[k] = grid.conflict_initial(tx[k], ty[k], tr[k]) ? 1 : 0;
+    }
   });
   for (size_t k = 0; k < T; ++k) {
     if (hit[k] || grid.conflict_accepted(tx[k], ty[k], tr[k])) continue;
@@ -379,24 +401,59 @@ hg_status fill_regions(hg_resampler &R, const std::vector<Box> &regions, double 
   return HG_OK;
 }
 
+// The bounding box of the regions, widened by six mean radii.
+void regions_extent(const std::vector<Box> &regions, double mean_r, double e[4]) {
+  double lo[2] = {regions[0].b[0], regions[0].b[1]}, up[2] = {regions[0].b[2], regions[0].b[3]};
+  for (size_t k = 1; k < regions.size(); ++k) {
+    lo[0] = std::min(lo[0], regions[k].b[0]);
+    lo[1] = std::min(lo[1], regions[k].b[1]);
+    up[0] = std::max(up[0], regions[k].b[2]);
+    up[1] = std::max(up[1], regions[k].b[3]);
+  }
+  e[0] = lo[0] - 6.0 * mean_r;
+  e[1] = lo[1] - 6.0 * mean_r;
+  e[2] = up[0] + 6.0 * mean_r;
+  e[3] = up[1] + 6.0 * mean_r;
+}
+
+// CAvoidAVoid::avoidAVoid with randomFillRegion (AvoidAvoid.cpp:103-183):
+// bodies (px, py, rad) grow by the accepted samples, whose radii are at most
+// r_max.
+template <typename Sampler>
+hg_status fill_regions(hg_resampler &R, const std::vector<Box> &regions, double mean_r,
+                       double r_max, std::vector<double> &px, std::vector<double> &py,
+                       std::vector<double> &rad, Sampler sampler) {
+  if (regions.empty()) return HG_OK;
+  double e[4];
+  regions_extent(regions, mean_r, e);
+  // cells twice the largest radius of the samples and of the bodies up to
+  // four mean radii (wider ones go to the list every sample scans)
+  double rc = r_max;
+  for (size_t b = 0; b < px.size(); ++b)
+    if (rad[b] > rc && rad[b] <= 4.0 * mean_r) rc = rad[b];
+  static thread_local FillGrid tl_grid;
+  build_fill_grid(tl_grid, e[0], e[1], e[2], e[3], rc, px, py, rad);
+  return fill_trials(R, tl_grid, regions, px, py, rad, sampler);
+}
+
 // avoidAVoidMPMparticlesInsideZonesWithTentativeQuantities
-// (ResamplingTools.cpp:58-104): returns the count before insertion.
-hg_status insert_points(hg_resampler &R, const std::vector<Box> &zones, int64_t &before) {
+// (ResamplingTools.cpp:58-104): returns the count before insertion. grid:
+// the search grid over the points, shared by the interval's point
+// insertions (a sample of one insertion is a body of the next: it is one of
+// the grid's accepted samples, which every later trial tests).
+hg_status insert_points(hg_resampler &R, const std::vector<Box> &zones, int64_t &before,
+                        FillGrid &grid) {
   const double rp = 0.5 * R.d.initial_particle_size;
   const size_t n = npoints(R);
   before = (int64_t)n;
-  std::vector<double> px(n), py(n), rad(n, rp);
-  for (size_t p = 0; p < n; ++p) {
-    px[p] = R.q[2 * p];
-    py[p] = R.q[2 * p + 1];
-  }
-  const hg_status st = fill_regions(R, zones, rp, rp, px, py, rad, [&](double &r) -> hg_status {
+  std::vector<double> px, py, rad;
+  const hg_status st = fill_trials(R, grid, zones, px, py, rad, [&](double &r) -> hg_status {
     r = rp;
     return HG_OK;
   });
   if (st != HG_OK) return st;
   const double hl0 = R.d.initial_particle_size * 0.5;
-  for (size_t p = n; p < px.size(); ++p) { // addMaterialPoint, MaterialPoints.cpp:439-467
+  for (size_t p = 0; p < px.size(); ++p) { // addMaterialPoint, MaterialPoints.cpp:439-467
     R.q0.push_back(px[p]);
     R.q0.push_back(py[p]);
     R.q.push_back(px[p]);
@@ -415,7 +472,7 @@ hg_status insert_points(hg_resampler &R, const std::vector<Box> &zones, int64_t 
     R.jh.push_back(0);
     R.kin.push_back(0);
   }
-  R.stats.points_inserted += (int64_t)(px.size() - n);
+  R.stats.points_inserted += (int64_t)px.size();
   return HG_OK;
 }
 
@@ -842,60 +899,62 @@ template <typename T> void compact(std::vector<T> &a, const std::vector<uint8_t>
 // deleteParticlesUsingZoneIndicators (ResamplingTools.cpp:28-56) with
 // MaterialPoints::deleteMaterialPoint and RigidBody2DState::removeBodies.
 void delete_by_zone(hg_resampler &R, const hg_zones &z) {
+  // labels over host threads; each array compacted as one task of the pool
+  // (every array keeps the same elements in the same order)
   const size_t n = npoints(R);
   std::vector<uint8_t> keep(n, 1);
-  for (size_t p = 0; p < n; ++p) {
-    const int32_t l = hg::zone_label_at(z, R.q[2 * p], R.q[2 * p + 1]);
-    if (l < 0 || l == HG_ZONE_DISCRETE) keep[p] = 0;
-  }
+  hg::host_parallel(n, 8192, [&](size_t b, size_t e) {
+    for (size_t p = b; p < e; ++p) {
+      const int32_t l = hg::zone_label_at(z, R.q[2 * p], R.q[2 * p + 1]);
+      if (l < 0 || l == HG_ZONE_DISCRETE) keep[p] = 0;
+    }
+  });
   R.stats.points_deleted += (int64_t)std::count(keep.begin(), keep.end(), 0);
-  compact(R.q0, keep, 2);
-  compact(R.q, keep, 2);
-  compact(R.v, keep, 2);
-  compact(R.m, keep, 1);
-  compact(R.vol, keep, 1);
-  compact(R.m0, keep, 1);
-  compact(R.vol0, keep, 1);
-  compact(R.w, keep, 1);
-  compact(R.hl, keep, 1);
-  compact(R.be, keep, 4);
-  compact(R.J, keep, 1);
-  compact(R.jh, keep, 1);
-  compact(R.kin, keep, 1);
   const size_t nb = nbodies(R);
   std::vector<uint8_t> keepb(nb, 1);
-  for (size_t b = 0; b < nb; ++b) {
-    if (R.fixed[b]) continue;
-    const int32_t l = hg::zone_label_at(z, R.dq[3 * b], R.dq[3 * b + 1]);
-    if (l < 0 || l == HG_ZONE_CONTINUUM) keepb[b] = 0;
-  }
+  hg::host_parallel(nb, 8192, [&](size_t b0, size_t b1) {
+    for (size_t b = b0; b < b1; ++b) {
+      if (R.fixed[b]) continue;
+      const int32_t l = hg::zone_label_at(z, R.dq[3 * b], R.dq[3 * b + 1]);
+      if (l < 0 || l == HG_ZONE_CONTINUUM) keepb[b] = 0;
+    }
+  });
   R.dem_map.assign(nb, -1);
   int32_t next = 0;
   for (size_t b = 0; b < nb; ++b)
     if (keepb[b]) R.dem_map[b] = next++;
   R.stats.grains_deleted += (int64_t)(nb - (size_t)next);
-  compact(R.dq0, keepb, 3);
-  compact(R.dq, keepb, 3);
-  compact(R.dv, keepb, 3);
-  compact(R.dr, keepb, 1);
-  compact(R.M0, keepb, 3);
-  compact(R.dw, keepb, 1);
-  compact(R.fixed, keepb, 1);
+  const std::function<void()> tasks[] = {
+      [&] { compact(R.q0, keep, 2); },    [&] { compact(R.q, keep, 2); },
+      [&] { compact(R.v, keep, 2); },     [&] { compact(R.m, keep, 1); },
+      [&] { compact(R.vol, keep, 1); },   [&] { compact(R.m0, keep, 1); },
+      [&] { compact(R.vol0, keep, 1); },  [&] { compact(R.w, keep, 1); },
+      [&] { compact(R.hl, keep, 1); },    [&] { compact(R.be, keep, 4); },
+      [&] { compact(R.J, keep, 1); },     [&] { compact(R.jh, keep, 1); },
+      [&] { compact(R.kin, keep, 1); },   [&] { compact(R.dq0, keepb, 3); },
+      [&] { compact(R.dq, keepb, 3); },   [&] { compact(R.dv, keepb, 3); },
+      [&] { compact(R.dr, keepb, 1); },   [&] { compact(R.M0, keepb, 3); },
+      [&] { compact(R.dw, keepb, 1); },   [&] { compact(R.fixed, keepb, 1); }};
+  hg::host_pool_run(sizeof(tasks) / sizeof(tasks[0]), [&](size_t k) { tasks[k](); });
 }
 
 // demWeight / mpmWeight with updateMassWeights / updateWeights
-// (HybridGrains2DSim.cpp:512-528)
+// (HybridGrains2DSim.cpp:512-528), over host threads
 void update_weights(hg_resampler &R, const hg_zones &z) {
-  for (size_t b = 0; b < nbodies(R); ++b) {
-    const int32_t l = hg::zone_label_at(z, R.dq[3 * b], R.dq[3 * b + 1]);
-    R.dw[b] = l == HG_ZONE_HYBRID ? 0.5 : (l == HG_ZONE_DISCRETE ? 1.0 : 0.0);
-  }
-  for (size_t p = 0; p < npoints(R); ++p) {
-    const int32_t l = hg::zone_label_at(z, R.q[2 * p], R.q[2 * p + 1]);
-    R.w[p] = l == HG_ZONE_HYBRID ? 0.5 : (l == HG_ZONE_CONTINUUM ? 1.0 : 0.0);
-    R.m[p] = R.m0[p] * R.w[p];
-    R.vol[p] = R.vol0[p] * R.w[p];
-  }
+  hg::host_parallel(nbodies(R), 8192, [&](size_t b0, size_t b1) {
+    for (size_t b = b0; b < b1; ++b) {
+      const int32_t l = hg::zone_label_at(z, R.dq[3 * b], R.dq[3 * b + 1]);
+      R.dw[b] = l == HG_ZONE_HYBRID ? 0.5 : (l == HG_ZONE_DISCRETE ? 1.0 : 0.0);
+    }
+  });
+  hg::host_parallel(npoints(R), 8192, [&](size_t b, size_t e) {
+    for (size_t p = b; p < e; ++p) {
+      const int32_t l = hg::zone_label_at(z, R.q[2 * p], R.q[2 * p + 1]);
+      R.w[p] = l == HG_ZONE_HYBRID ? 0.5 : (l == HG_ZONE_CONTINUUM ? 1.0 : 0.0);
+      R.m[p] = R.m0[p] * R.w[p];
+      R.vol[p] = R.vol0[p] * R.w[p];
+    }
+  });
 }
 
 double ms_since(std::chrono::steady_clock::time_point &t) {
@@ -914,15 +973,44 @@ hg_status run(hg_resampler &R, const hg_zones &z) {
   if ((st = insert_grains(R, z.rzones, g_before))) return st;
   const int64_t g_after = (int64_t)nbodies(R);
   R.stats.ms_insert_grains = ms_since(t);
-  if ((st = insert_points(R, z.rzones, p_before))) return st;
-  p_mid = (int64_t)npoints(R);
-  if (direct && (st = insert_points(R, z.direct, dummy))) return st;
-  p_after = (int64_t)npoints(R);
   std::vector<Box> inner;
   hg::zone_inner_continuum(z, direct, inner);
+  // one search grid over the points for the three insertions, over the
+  // extent of all their regions
+  static thread_local FillGrid tl_pgrid;
+  {
+    const double rp = 0.5 * R.d.initial_particle_size;
+    double e[4] = {0.0, 0.0, 0.0, 0.0};
+    bool any = false;
+    const std::vector<Box> *all[3] = {&z.rzones, &z.direct, &inner};
+    for (const std::vector<Box> *regs : all) {
+      if (regs->empty() || (regs == &z.direct && !direct)) continue;
+      double f[4];
+      regions_extent(*regs, rp, f);
+      if (!any) std::copy(f, f + 4, e);
+      e[0] = std::min(e[0], f[0]);
+      e[1] = std::min(e[1], f[1]);
+      e[2] = std::max(e[2], f[2]);
+      e[3] = std::max(e[3], f[3]);
+      any = true;
+    }
+    if (any) {
+      const size_t n = npoints(R);
+      std::vector<double> px(n), py(n), rad(n, rp);
+      for (size_t p = 0; p < n; ++p) {
+        px[p] = R.q[2 * p];
+        py[p] = R.q[2 * p + 1];
+      }
+      build_fill_grid(tl_pgrid, e[0], e[1], e[2], e[3], rp, px, py, rad);
+    }
+  }
+  if ((st = insert_points(R, z.rzones, p_before, tl_pgrid))) return st;
+  p_mid = (int64_t)npoints(R);
+  if (direct && (st = insert_points(R, z.direct, dummy, tl_pgrid))) return st;
+  p_after = (int64_t)npoints(R);
   int64_t i_before = p_after, i_after = p_after;
   if (!inner.empty()) {
-    if ((st = insert_points(R, inner, i_before))) return st;
+    if ((st = insert_points(R, inner, i_before, tl_pgrid))) return st;
     i_after = (int64_t)npoints(R);
   }
   R.stats.ms_insert_points = ms_since(t);
@@ -1068,21 +1156,23 @@ hg_status hg_resampler_set_points(hg_resampler *r, int64_t n, const double *q0, 
   if (n > 0 && (!q0 || !q || !v || !m || !vol || !m0 || !vol0 || !hl || !be || !J))
     return fail(HG_ERR_INVALID_ARGUMENT, "NULL array");
   const size_t k = (size_t)n;
-  r->q0.assign(q0, q0 + 2 * k);
-  r->q.assign(q, q + 2 * k);
-  r->v.assign(v, v + 2 * k);
-  r->m.assign(m, m + k);
-  r->vol.assign(vol, vol + k);
-  r->m0.assign(m0, m0 + k);
-  r->vol0.assign(vol0, vol0 + k);
-  r->w.assign(k, 1.0);
-  r->hl.assign(hl, hl + k);
-  r->be.assign(be, be + 4 * k);
-  r->J.assign(J, J + k);
-  if (jh) r->jh.assign(jh, jh + k);
-  else r->jh.assign(k, 0);
-  if (kin) r->kin.assign(kin, kin + k);
-  else r->kin.assign(k, 0);
+  // one array per task of the host pool
+  const std::function<void()> tasks[] = {
+      [&] { r->q0.assign(q0, q0 + 2 * k); },   [&] { r->q.assign(q, q + 2 * k); },
+      [&] { r->v.assign(v, v + 2 * k); },      [&] { r->m.assign(m, m + k); },
+      [&] { r->vol.assign(vol, vol + k); },    [&] { r->m0.assign(m0, m0 + k); },
+      [&] { r->vol0.assign(vol0, vol0 + k); }, [&] { r->w.assign(k, 1.0); },
+      [&] { r->hl.assign(hl, hl + k); },       [&] { r->be.assign(be, be + 4 * k); },
+      [&] { r->J.assign(J, J + k); },
+      [&] {
+        if (jh) r->jh.assign(jh, jh + k);
+        else r->jh.assign(k, 0);
+      },
+      [&] {
+        if (kin) r->kin.assign(kin, kin + k);
+        else r->kin.assign(k, 0);
+      }};
+  hg::host_pool_run(sizeof(tasks) / sizeof(tasks[0]), [&](size_t t) { tasks[t](); });
   return HG_OK;
 }
 
@@ -1143,19 +1233,14 @@ hg_status hg_resampler_get_points(hg_resampler *r, double *q0, double *q, double
   auto put = [](const auto &src, auto *dst) {
     if (dst) std::copy(src.begin(), src.end(), dst);
   };
-  put(r->q0, q0);
-  put(r->q, q);
-  put(r->v, v);
-  put(r->m, m);
-  put(r->vol, vol);
-  put(r->m0, m0);
-  put(r->vol0, vol0);
-  put(r->w, w);
-  put(r->hl, hl);
-  put(r->be, be);
-  put(r->J, J);
-  put(r->jh, jh);
-  put(r->kin, kin);
+  // one array per task of the host pool
+  const std::function<void()> tasks[] = {
+      [&] { put(r->q0, q0); },     [&] { put(r->q, q); },   [&] { put(r->v, v); },
+      [&] { put(r->m, m); },       [&] { put(r->vol, vol); }, [&] { put(r->m0, m0); },
+      [&] { put(r->vol0, vol0); }, [&] { put(r->w, w); },   [&] { put(r->hl, hl); },
+      [&] { put(r->be, be); },     [&] { put(r->J, J); },   [&] { put(r->jh, jh); },
+      [&] { put(r->kin, kin); }};
+  hg::host_pool_run(sizeof(tasks) / sizeof(tasks[0]), [&](size_t t) { tasks[t](); });
   return HG_OK;
 }
 

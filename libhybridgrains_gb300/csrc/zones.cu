@@ -235,27 +235,34 @@ void distance_field(hg_zones &z) {
         }
     }
   });
-  std::vector<size_t> ring;
-  ring.reserve(npts);
+  // (grid point coordinates tabulated with the same expressions; queue
+  // entries carry their column and row)
+  std::vector<double> tgx(nx + 1), tgy(ny + 1);
+  for (unsigned i = 0; i <= nx; ++i) tgx[i] = gpx((int)i);
+  for (unsigned j = 0; j <= ny; ++j) tgy[j] = gpy((int)j);
+  std::vector<uint32_t> ring; // (column, row) pairs
+  ring.reserve(2 * npts);
   for (size_t f = 0; f < npts; ++f)
-    if (closest[f] >= 0) ring.push_back(f);
-  for (size_t head = 0; head < ring.size(); ++head) {
-    const size_t f = ring[head];
+    if (closest[f] >= 0) {
+      ring.push_back((uint32_t)(f % (nx + 1)));
+      ring.push_back((uint32_t)(f / (nx + 1)));
+    }
+  for (size_t head = 0; head < ring.size(); head += 2) {
+    const unsigned gi = ring[head], gj = ring[head + 1];
+    const size_t f = (size_t)gj * (nx + 1) + gi;
     const int64_t cp = closest[f];
-    const unsigned gi = (unsigned)(f % (nx + 1)), gj = (unsigned)(f / (nx + 1));
-    long nb[4] = {gi > 0 ? (long)(gj * (nx + 1) + gi - 1) : -1,
-                  gj > 0 ? (long)((gj - 1) * (nx + 1) + gi) : -1,
-                  gi < nx ? (long)(gj * (nx + 1) + gi + 1) : -1,
-                  gj < ny ? (long)((gj + 1) * (nx + 1) + gi) : -1};
+    const double spx = sx[cp], spy = sy[cp];
+    const bool ok[4] = {gi > 0, gj > 0, gi < nx, gj < ny};
+    const unsigned ni[4] = {gi - 1, gi, gi + 1, gi}, nj[4] = {gj, gj - 1, gj, gj + 1};
     for (int l = 0; l < 4; ++l) {
-      if (nb[l] < 0) continue;
-      const size_t g = (size_t)nb[l];
-      const int ii = (int)(g % (nx + 1)), jj = (int)(g / (nx + 1));
-      const double dd = norm(gpx(ii) - sx[cp], gpy(jj) - sy[cp]);
+      if (!ok[l]) continue;
+      const size_t g = (size_t)nj[l] * (nx + 1) + ni[l];
+      const double dd = norm(tgx[ni[l]] - spx, tgy[nj[l]] - spy);
       if (dd < d[g] || closest[g] < 0) {
         d[g] = dd;
         closest[g] = cp;
-        ring.push_back(g);
+        ring.push_back(ni[l]);
+        ring.push_back(nj[l]);
       }
     }
   }
