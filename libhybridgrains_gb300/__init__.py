@@ -498,6 +498,10 @@ class DEM:
         check("hg_dem_download", self._h, _d(q), _d(v))
         return q, v
 
+    def download_into(self, q=None, v=None):
+        """Download into caller-provided (N, 3) float64 arrays (e.g. pinned)."""
+        check("hg_dem_download", self._h, _d(q), _d(v))
+
     def flow(self, dt, nsteps=1):
         check("hg_dem_step", self._h, float(dt), int(nsteps), 0)
 
@@ -570,6 +574,12 @@ class Hybrid:
 
     def clear_homogenized(self):
         check("hg_hybrid_clear_homogenized", self._h)
+
+    def homogenized_into(self, stress, velocity):
+        """The interval's homogenised stress (nn, 4) and velocity (nn, 2)
+        sums into caller-provided float64 arrays (e.g. pinned)."""
+        check("hg_hybrid_download", self._h, None, None, None, None, None, None, None,
+              _d(stress), _d(velocity))
 
     def coupling(self):
         ng, nn_ = ctypes.c_int64(), ctypes.c_int64()
@@ -837,13 +847,14 @@ class Resampler:
                                       ms_quantities=s.ms_quantities,
                                       ms_delete=s.ms_delete)
 
-    def points(self):
+    def points(self, alloc=np.empty):
+        """The points after the step; alloc(shape, dtype) makes the arrays
+        (e.g. ``pinned``); every element is written by the call."""
         n, _, _ = self.stats()
-        # (every element is written by the call)
-        out = dict(q0=np.empty((n, 2)), q=np.empty((n, 2)), v=np.empty((n, 2)), m=np.empty(n),
-                   vol=np.empty(n), m0=np.empty(n), vol0=np.empty(n), w=np.empty(n),
-                   hl=np.empty(n), be=np.empty((n, 4)), J=np.empty(n),
-                   jh=np.empty(n, dtype=np.int32), kin=np.empty(n, dtype=np.uint8))
+        f = lambda shape, dtype=np.float64: alloc(shape, dtype=dtype)  # noqa: E731
+        out = dict(q0=f((n, 2)), q=f((n, 2)), v=f((n, 2)), m=f(n), vol=f(n), m0=f(n),
+                   vol0=f(n), w=f(n), hl=f(n), be=f((n, 4)), J=f(n),
+                   jh=f(n, dtype=np.int32), kin=f(n, dtype=np.uint8))
         check("hg_resampler_get_points", self._h, *[_d(out[k]) for k in
               ("q0", "q", "v", "m", "vol", "m0", "vol0", "w", "hl", "be", "J")],
               _i32(out["jh"]), _u8(out["kin"]))

@@ -31,7 +31,7 @@ import time
 
 import numpy as np
 
-from . import DEM, FP64, MPM, Hybrid, Resampler, Zones, scene_xml, scenes
+from . import DEM, FP64, MPM, Hybrid, Resampler, Zones, pinned, scene_xml, scenes
 
 
 class HybridSim:
@@ -47,17 +47,19 @@ class HybridSim:
         p = scene_xml.seed_points(cfg) if "rectangles" in cfg else scenes.seed_column_points(cfg)
         n, nd = len(p["m"]), len(sc["r"])
         gravity = cfg.get("gravity", scenes.GRAVITY)
+        self._cap = dict(points=int(point_headroom * n) + 1024,
+                         grains=int(grain_headroom * nd) + 1024)
         self.mpm = MPM(ctx, cfg["grid_min"], cfg["grid_max"], cfg["h"], cfg["shear_modulus"],
                        cfg["bulk_modulus"], cfg["dp_alpha"], cfg["flip_alpha"], gravity,
                        cfg["planes"], basis=basis, precision=precision,
-                       capacity=int(point_headroom * n) + 1024)
+                       capacity=self._cap["points"])
         self.mpm.upload(p["q"], p["v"], p["m"], p["vol"], p["hl"])
         # the discrete scene's planes, else the continuum's walls for the grains too
         planes = dp.get("planes") or [(pl[0], pl[1]) for pl in cfg["planes"]]
         # (the spatial grid's cell is one mean diameter in hybrid runs, whatever
         # the discrete scene's cell_scale)
         self.dem = DEM(ctx, dp.get("gravity", gravity), dp["kn"], dp["kt"], dp["gamman"],
-                       dp["gammat"], dp["mu"], planes, capacity=int(grain_headroom * nd) + 1024,
+                       dp["gammat"], dp["mu"], planes, capacity=self._cap["grains"],
                        precision=precision if dem_precision is None else dem_precision)
         self.dem.upload(sc["q"], sc["v"], sc["r"], sc["m"], sc["I"], sc["fixed"])
         self.hyb = Hybrid(ctx, self.mpm, self.dem)
@@ -88,27 +90,77 @@ class HybridSim:
         # host seconds of the resampling intervals by phase: device->host
         # copies, zone update, resampling proper, host->device uploads
         self.host_s = dict(download=0.0, zones=0.0, resampling=0.0, upload=0.0)
+        # page-locked host arrays of the interval's transfers, sized for the
+        # objects' capacities and kept for the simulation's life (the
+        # library's kernels read and write them in place)
+        self._cap["nodes"] = self.mpm.nnodes
+        self._pin = {}
+        # (all allocated here: page-locking is slow and would land in an
+        # interval otherwise)
+        for key, w, dt_ in (("pq", 2, np.float64), ("pv", 2, np.float64),
+                            ("pbe", 4, np.float64), ("pJ", 1, np.float64),
+                            ("pjh", 1, np.int32), ("gq", 3, np.float64), ("gv", 3, np.float64),
+                            ("nhs", 4, np.float64), ("nhv", 2, np.float64), ("pmw", 1, np.float64),
+                            ("pvw", 1, np.float64)):
+            self._pinned(key, (1, w), dt_)
+        for parity in (0, 1):
+            for k, (w, dt_) in enumerate(((2, np.float64),) * 3 + ((1, np.float64),) * 6 +
+                                         ((4, np.float64), (1, np.float64), (1, np.int32),
+                                          (1, np.uint8))):
+                self._pinned("p%d_%d" % (parity, k), (1, w), dt_)
+
+    def _pinned(self, key, shape, dtype=np.float64):
+        """A page-locked host array of this shape, a view of the key's buffer
+        (allocated once, for the capacity of the rows' kind: key's first
+        letter p, g or n for points, grains or nodes)."""
+        shape = (shape,) if np.isscalar(shape) else tuple(shape)
+        n = int(np.prod(shape))
+        b = self._pin.get(key)
+        if b is None or b.size < n or b.dtype != np.dtype(dtype):
+            per_row = n // shape[0] if shape[0] else 1
+            kind = {"p": "points", "g": "grains", "n": "nodes"}[key[0]]
+            b = pinned(max(n, per_row * self._cap[kind], 1), dtype)
+            self._pin[key] = b
+        return b[:n].reshape(shape)
 
     def _resample(self):
         clock = time.perf_counter
         t0 = clock()
-        st = self.mpm.download()
-        q3, v3 = self.dem.download()
+        n, nd = self.mpm.n, self.dem.n
+        st = dict(q=self._pinned("pq", (n, 2)), v=self._pinned("pv", (n, 2)),
+                  be=self._pinned("pbe", (n, 4)), J=self._pinned("pJ", n),
+                  jh=self._pinned("pjh", n, np.int32))
+        self.mpm.download_into(st["q"], st["v"], st["be"], st["J"], st["jh"])
+        q3, v3 = self._pinned("gq", (nd, 3)), self._pinned("gv", (nd, 3))
+        self.dem.download_into(q3, v3)
         P, G = self.P, self.G
         nn = self.mpm.nnodes
         hs, hv = np.zeros((nn, 4)), np.zeros((nn, 2))
         if self.hom[0] or self.hom[1]:
-            c = self.hyb.coupling()
-            hs, hv = c["homog_stress"] / self.freq, c["homog_velocity"] / self.freq
+            hs, hv = self._pinned("nhs", (nn, 4)), self._pinned("nhv", (nn, 2))
+            self.hyb.homogenized_into(hs, hv)
+            np.divide(hs, self.freq, out=hs)
+            np.divide(hv, self.freq, out=hv)
         t1 = clock()
         self.zones.update(q3, G["r"], G["fixed"], st["q"])
         t2 = clock()
-        self.res.set_points(P["q0"], st["q"], st["v"], P["m0"] * P["w"], P["vol0"] * P["w"],
+        mw, vw = self._pinned("pmw", n), self._pinned("pvw", n)
+        np.multiply(P["m0"], P["w"], out=mw)
+        np.multiply(P["vol0"], P["w"], out=vw)
+        self.res.set_points(P["q0"], st["q"], st["v"], mw, vw,
                             P["m0"], P["vol0"], P["hl"], st["be"], st["J"], st["jh"])
         self.res.set_grains(G["q0"], q3, v3, G["r"], G["M0"], G["fixed"])
         self.res.set_homogenized(hs, hv)
         self.res.run(self.zones)
-        a, b = self.res.points(), self.res.grains()
+        # the new points in page-locked arrays, two sets used in turn (the
+        # previous interval's stay valid until this one has read them)
+        order = iter(range(64))
+        parity = self.resamplings % 2
+        a = self.res.points(lambda shape, dtype=np.float64: self._pinned(
+            "p%d_%d" % (parity, next(order)), shape, dtype))
+        # (points beyond the MPM capacity fail at the upload below; their
+        # arrays are then sized as requested)
+        b = self.res.grains()
         t3 = clock()
         self.mpm.upload(a["q"], a["v"], a["m"], a["vol"], a["hl"], a["be"], a["J"], a["jh"])
         self.dem.upload_relabel(b["q"], b["v"], b["r"], b["M0"][:, 0], b["M0"][:, 2], b["fixed"],
