@@ -748,34 +748,25 @@ __device__ __forceinline__ bool ugimp_axis(int c, float f, float hl, int n, int 
   // a >= 1 - hl; w = 2 hl (1 - a) i2, dw/du = -sign(d) 2 hl i2 for a >= hl;
   // else w = (2 hl - (hl^2 + a^2)) i2, dw/du = -2 d i2. The middle node lies
   // within 1/2 of the point and the outer two at least 1/2 away (>= hl), so
-  // each takes only the cases it can reach.
-  const float i2 = 0.5f / hl, h2 = 2.0f * hl;
+  // each takes only the cases it can reach. The cases are selected, not
+  // branched on (the lanes of a warp take different ones).
+  const float i2 = 0.5f / hl, h2 = 2.0f * hl, h2i2 = h2 * i2;
 #pragma unroll
   for (int m = 0; m < 3; m += 2) {
     const float d = f - (float)(m - 1 + up);
     const float a = fabsf(d), sg = d >= 0.0f ? 1.0f : -1.0f;
-    if (a >= 1.0f + hl) {
-      w[m] = 0.0f;
-      g[m] = 0.0f;
-    } else if (a >= 1.0f - hl) {
-      const float t = 1.0f + hl - a;
-      w[m] = 0.5f * t * t * i2;
-      g[m] = -sg * t * i2;
-    } else {
-      w[m] = h2 * (1.0f - a) * i2;
-      g[m] = -sg * h2 * i2;
-    }
+    const float t = 1.0f + hl - a;
+    const bool out = a >= 1.0f + hl, edge = a >= 1.0f - hl;
+    w[m] = out ? 0.0f : (edge ? 0.5f * t * t * i2 : (1.0f - a) * h2i2);
+    g[m] = out ? 0.0f : (edge ? -sg * t * i2 : -sg * h2i2);
   }
   {
     const float d = f - (float)up;
     const float a = fabsf(d), sg = d >= 0.0f ? 1.0f : -1.0f;
-    if (a >= hl) { // (at a = 1 - hl = hl = 1/2 the second case gives the same)
-      w[1] = h2 * (1.0f - a) * i2;
-      g[1] = -sg * h2 * i2;
-    } else {
-      w[1] = (h2 - (hl * hl + a * a)) * i2;
-      g[1] = -2.0f * d * i2;
-    }
+    // (at a = 1 - hl = hl = 1/2 the two cases agree)
+    const bool far = a >= hl;
+    w[1] = far ? (1.0f - a) * h2i2 : (h2 - (hl * hl + a * a)) * i2;
+    g[1] = far ? -sg * h2i2 : -2.0f * d * i2;
   }
   if (c >= 1 && c + 2 <= n) return true; // nodes c-1 .. c+2 all on the grid
   bool ok = true;
@@ -846,7 +837,7 @@ __global__ void __launch_bounds__(THREADS) kxu_step(const __grid_constant__ Mixe
         for (int kx = 0; kx < 3; ++kx) {
           if (!((sx >> kx) & (sy >> ky) & 1u)) continue; // outside the support
           const float w = wx[kx] * wy[ky], dX = gx[kx] * wy[ky], dY = wx[kx] * gy[ky];
-          const int64_t node = (int64_t)(by + ky) * row + (bx + kx);
+          const int node = (by + ky) * row + (bx + kx); // MIXED grids have < 2^30 nodes
           if (!HG_INDEX_OK(node, nn, A.status)) continue;
           const float4 nv = A.va[node];
           Lxx += nv.x * dX;
@@ -928,7 +919,7 @@ __global__ void __launch_bounds__(THREADS) kxu_step(const __grid_constant__ Mixe
         if (!((sx >> kx) & (sy >> ky) & 1u)) continue; // outside the support
         const float w = wx[kx] * wy[ky];
         const float dX = gx[kx] * wy[ky], dY = wx[kx] * gy[ky];
-        const int64_t node = (int64_t)(by + ky) * row + (bx + kx);
+        const int node = (by + ky) * row + (bx + kx); // MIXED grids have < 2^30 nodes
         if (!HG_INDEX_OK(node, nn, A.status)) continue;
         float4 add = make_float4(w * mvx, w * mvy, 0.0f, 0.0f);
         if (w != 0.0f) { // nodes of zero weight get no force (PhysicsGrid.cpp:439-441)
