@@ -7,6 +7,7 @@
     python -m libhybridgrains_gb300.profile_cases hybrid --steps 6 [--precision mixed]
     python -m libhybridgrains_gb300.profile_cases column --steps 8 [--basis ugimp]
     python -m libhybridgrains_gb300.profile_cases batch --scenes 256 --steps 8
+    python -m libhybridgrains_gb300.profile_cases e2e --steps 8
 
 Each case builds its scene, runs one warm-up step, then ``--steps`` steps one
 call per step (so that every kernel is a separate launch a profiler can
@@ -19,7 +20,10 @@ the hybrid case is the hybrid column (100,000 points under 20,000 disks)
 after its initial resampling; the column case is the 2,000,000-point MIXED
 column (with --basis ugimp on a grid 4 cells wider below and left, as the
 bench runs it); the batch case is the serving mix (the first --scenes requests of
-seed 2024) as MIXED scenes in one batch.
+seed 2024) as MIXED scenes in one batch; the e2e case is the bench's end-to-end
+step on the 2,000,000-point column: the state in the reference's layouts in
+page-locked host memory, uploaded, stepped once and downloaded again each
+step.
 """
 import argparse
 import time
@@ -30,7 +34,7 @@ def main(argv=None):
     from libhybridgrains_gb300 import scenes, serving
 
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["dem", "hybrid", "column", "batch"])
+    ap.add_argument("case", choices=["dem", "hybrid", "column", "batch", "e2e"])
     ap.add_argument("--scenes", type=int, default=256, help="batch: serving requests")
     ap.add_argument("--basis", choices=("linear", "ugimp"), default="linear",
                     help="column: the MPM basis")
@@ -90,6 +94,30 @@ def main(argv=None):
 
         def status():
             return max(m.status() for m in members)
+    elif args.case == "e2e":
+        import numpy as np
+        cfg = scenes.mpm_column("column_2M")
+        p = scenes.seed_column_points(cfg)
+        n = len(p["m"])
+        host = {k: hg.pinned(p[k].shape) for k in ("q", "v", "m", "vol")}
+        for k in host:
+            host[k][...] = p[k]
+        host["be"] = hg.pinned((n, 4))
+        host["be"][...] = [1.0, 0.0, 0.0, 1.0]
+        host["J"] = hg.pinned(n)
+        host["J"][...] = 1.0
+        host["jh"] = hg.pinned(n, np.int32)
+        host["jh"][...] = 0
+        obj = hg.MPM(ctx, cfg["grid_min"], cfg["grid_max"], cfg["h"], cfg["shear_modulus"],
+                     cfg["bulk_modulus"], cfg["dp_alpha"], cfg["flip_alpha"], scenes.GRAVITY,
+                     cfg["planes"], precision=hg.MIXED, capacity=n)
+
+        def step():
+            obj.upload(host["q"], host["v"], host["m"], host["vol"], None, host["be"],
+                       host["J"], host["jh"])
+            obj.flow(cfg["dt"], 1)
+            obj.download_into(host["q"], host["v"], host["be"], host["J"], host["jh"])
+        status = obj.status
     else:
         cfg = scenes.mpm_column("column_2M")
         p = scenes.seed_column_points(cfg)
