@@ -1197,10 +1197,15 @@ hg_status hg_resampler_set_grains(hg_resampler *r, int64_t n, const double *q0, 
 hg_status hg_resampler_set_homogenized(hg_resampler *r, const double *stress, const double *velocity) {
   if (!r) return fail(HG_ERR_INVALID_ARGUMENT, "r is NULL");
   const size_t nn = (size_t)(r->d.zones.mpm_cells[0] + 1) * (r->d.zones.mpm_cells[1] + 1);
-  if (stress) r->hs.assign(stress, stress + 4 * nn);
-  else r->hs.assign(4 * nn, 0.0);
-  if (velocity) r->hv.assign(velocity, velocity + 2 * nn);
-  else r->hv.assign(2 * nn, 0.0);
+  hg::host_pool_run(2, [&](size_t t) {
+    if (t == 0) {
+      if (stress) r->hs.assign(stress, stress + 4 * nn);
+      else r->hs.assign(4 * nn, 0.0);
+    } else {
+      if (velocity) r->hv.assign(velocity, velocity + 2 * nn);
+      else r->hv.assign(2 * nn, 0.0);
+    }
+  });
   return HG_OK;
 }
 

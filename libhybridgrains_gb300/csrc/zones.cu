@@ -148,20 +148,28 @@ void packing_fraction(hg_zones &z, int64_t nd, const double *q3, const double *r
   hg::host_parallel(ny, 8, [&](size_t jb, size_t je) { rows((unsigned)jb, (unsigned)je); });
   // cells within half a window of a material point count as dense; the
   // reference's test excludes the first row and column (gid > 0)
-  // (over host threads by bands of rows: each band sets only its own cells)
-  hg::host_parallel(ny, 16, [&](size_t rb, size_t re) {
-    for (int64_t p = 0; p < np; ++p) {
+  // (marks over host threads by points, each a relaxed atomic store of the
+  // same value; then the marked cells' fractions set to 1)
+  static thread_local std::vector<uint8_t> tl_mark;
+  std::vector<uint8_t> &mark = tl_mark;
+  mark.assign((size_t)nx * ny, 0);
+  hg::host_parallel((size_t)np, 8192, [&](size_t pb, size_t pe) {
+    for (size_t p = pb; p < pe; ++p) {
       const double x = pq[2 * p] - z.ls_min[0], y = pq[2 * p + 1] - z.ls_min[1];
       const int gj0 = (int)std::floor((y - w * 0.5) / z.ls_h);
       const int gj1 = (int)std::floor((y + w * 0.5) / z.ls_h);
-      const int j0 = std::max({gj0, 1, (int)rb}), j1 = std::min({gj1, (int)ny - 1, (int)re - 1});
+      const int j0 = std::max(gj0, 1), j1 = std::min(gj1, (int)ny - 1);
       if (j0 > j1) continue;
       const int gi0 = (int)std::floor((x - w * 0.5) / z.ls_h);
       const int gi1 = (int)std::floor((x + w * 0.5) / z.ls_h);
       for (int j = j0; j <= j1; ++j)
         for (int i = std::max(gi0, 1); i <= std::min(gi1, (int)nx - 1); ++i)
-          z.phi[(size_t)j * nx + i] = 1.0;
+          __atomic_store_n(&mark[(size_t)j * nx + i], (uint8_t)1, __ATOMIC_RELAXED);
     }
+  });
+  hg::host_parallel((size_t)nx * ny, 16384, [&](size_t cb, size_t ce) {
+    for (size_t c = cb; c < ce; ++c)
+      if (mark[c]) z.phi[c] = 1.0;
   });
 }
 
@@ -257,7 +265,11 @@ void distance_field(hg_zones &z) {
     for (int l = 0; l < 4; ++l) {
       if (!ok[l]) continue;
       const size_t g = (size_t)nj[l] * (nx + 1) + ni[l];
-      const double dd = norm(tgx[ni[l]] - spx, tgy[nj[l]] - spy);
+      const double ex = tgx[ni[l]] - spx, ey = tgy[nj[l]] - spy, e2 = ex * ex + ey * ey;
+      // a squared distance clearly above the stored one cannot win: the
+      // square root (rounded to half an ulp) stays above it too
+      if (closest[g] >= 0 && e2 > d[g] * d[g] * (1.0 + 1.0e-12)) continue;
+      const double dd = norm(ex, ey);
       if (dd < d[g] || closest[g] < 0) {
         d[g] = dd;
         closest[g] = cp;
