@@ -73,32 +73,33 @@ struct Mt19937 {
     return y;
   }
   float uniform() { return (float)next() * 2.3283064365386963e-10f; }
-  // the next n outputs, as n calls of next() would give them (tempered a
-  // block of the state at a time)
-  void fill(uint32_t *out, size_t n) {
+  static uint32_t temper(uint32_t y) {
+    y ^= y >> 11;
+    y ^= (y << 7) & 0x9d2c5680u;
+    y ^= (y << 15) & 0xefc60000u;
+    y ^= y >> 18;
+    return y;
+  }
+  // the state words behind the next n outputs, untempered (temper(w) of
+  // each is what n calls of next() would give), a block of the state at a
+  // time: the caller tempers them where it uses them
+  void fill_raw(uint32_t *out, size_t n) {
     size_t k = 0;
     while (k < n) {
-      if (i >= N) { // the twist of next()
-        out[k++] = next();
-        continue;
+      if (i >= N) { // the twist of next(), undone to its raw word
+        next();
+        --i;
       }
       const size_t take = std::min(n - k, (size_t)(N - i));
-      for (size_t j = 0; j < take; ++j) {
-        uint32_t y = s[i + j];
-        y ^= y >> 11;
-        y ^= (y << 7) & 0x9d2c5680u;
-        y ^= (y << 15) & 0xefc60000u;
-        y ^= y >> 18;
-        out[k + j] = y;
-      }
+      std::memcpy(out + k, s + i, take * sizeof(uint32_t));
       i += (int)take;
       k += take;
     }
   }
 };
 
-// uniform() of a raw output
-inline float mt_uniform(uint32_t w) { return (float)w * 2.3283064365386963e-10f; }
+// uniform() of an untempered state word
+inline float mt_uniform(uint32_t raw) { return (float)Mt19937::temper(raw) * 2.3283064365386963e-10f; }
 
 inline double dist2d(double ax, double ay, double bx, double by) {
   const double dx = ax - bx, dy = ay - by;
@@ -350,10 +351,11 @@ void build_fill_grid(FillGrid &grid, double g0x, double g0y, double g1x, double 
 // (AvoidAvoid.cpp:103-183) over the regions, against the bodies of the grid
 // (built over the bodies present, plus the samples accepted since): accepted
 // samples are appended to (px, py, rad) and added to the grid.
+// (fixed_r > 0: every sample has that radius and the sampler is not called)
 template <typename Sampler>
 hg_status fill_trials(hg_resampler &R, FillGrid &grid, const std::vector<Box> &regions,
                       std::vector<double> &px, std::vector<double> &py,
-                      std::vector<double> &rad, Sampler sampler) {
+                      std::vector<double> &rad, Sampler sampler, double fixed_r = -1.0) {
   if (regions.empty()) return HG_OK;
   static thread_local std::vector<double> tl_tx, tl_ty, tl_tr;
   static thread_local std::vector<uint8_t> tl_hit;
@@ -373,10 +375,14 @@ hg_status fill_trials(hg_resampler &R, FillGrid &grid, const std::vector<Box> &r
   ty.resize(T);
   tr.resize(T);
   raw.resize(2 * T);
-  R.mt.fill(raw.data(), 2 * T);
-  for (size_t t = 0; t < T; ++t) {
-    const hg_status st = sampler(tr[t]);
-    if (st != HG_OK) return st;
+  R.mt.fill_raw(raw.data(), 2 * T);
+  if (fixed_r > 0.0) {
+    std::fill(tr.begin(), tr.begin() + T, fixed_r);
+  } else {
+    for (size_t t = 0; t < T; ++t) {
+      const hg_status st = sampler(tr[t]);
+      if (st != HG_OK) return st;
+    }
   }
   hit.resize(T);
   hg::host_parallel(T, 4096, [&](size_t b, size_t e) {
@@ -450,7 +456,7 @@ hg_status insert_points(hg_resampler &R, const std::vector<Box> &zones, int64_t 
   const hg_status st = fill_trials(R, grid, zones, px, py, rad, [&](double &r) -> hg_status {
     r = rp;
     return HG_OK;
-  });
+  }, rp);
   if (st != HG_OK) return st;
   const double hl0 = R.d.initial_particle_size * 0.5;
   for (size_t p = 0; p < px.size(); ++p) { // addMaterialPoint, MaterialPoints.cpp:439-467
