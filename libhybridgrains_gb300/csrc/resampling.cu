@@ -351,11 +351,14 @@ void build_fill_grid(FillGrid &grid, double g0x, double g0y, double g1x, double 
 // (AvoidAvoid.cpp:103-183) over the regions, against the bodies of the grid
 // (built over the bodies present, plus the samples accepted since): accepted
 // samples are appended to (px, py, rad) and added to the grid.
-// (fixed_r > 0: every sample has that radius and the sampler is not called)
+// (fixed_r > 0: every sample has that radius and the sampler is not called;
+// words: the trials' 2 x 16 x regions position words drawn already, in
+// their order in R.mt's stream, the test id then advanced by the caller)
 template <typename Sampler>
 hg_status fill_trials(hg_resampler &R, FillGrid &grid, const std::vector<Box> &regions,
                       std::vector<double> &px, std::vector<double> &py,
-                      std::vector<double> &rad, Sampler sampler, double fixed_r = -1.0) {
+                      std::vector<double> &rad, Sampler sampler, double fixed_r = -1.0,
+                      const uint32_t *words = nullptr) {
   if (regions.empty()) return HG_OK;
   static thread_local std::vector<double> tl_tx, tl_ty, tl_tr;
   static thread_local std::vector<uint8_t> tl_hit;
@@ -374,8 +377,12 @@ hg_status fill_trials(hg_resampler &R, FillGrid &grid, const std::vector<Box> &r
   tx.resize(T);
   ty.resize(T);
   tr.resize(T);
-  raw.resize(2 * T);
-  R.mt.fill_raw(raw.data(), 2 * T);
+  const uint32_t *rw = words;
+  if (!rw) {
+    raw.resize(2 * T);
+    R.mt.fill_raw(raw.data(), 2 * T);
+    rw = raw.data();
+  }
   if (fixed_r > 0.0) {
     std::fill(tr.begin(), tr.begin() + T, fixed_r);
   } else {
@@ -389,8 +396,8 @@ hg_status fill_trials(hg_resampler &R, FillGrid &grid, const std::vector<Box> &r
     for (size_t k = b; k < e; ++k) {
       const Box &reg = regions[k / 16];
       const double dx = reg.b[2] - reg.b[0], dy = reg.b[3] - reg.b[1];
-      tx[k] = (double)mt_uniform(raw[2 * k]) * dx + reg.b[0];
-      ty[k] = (double)mt_uniform(raw[2 * k + 1]) * dy + reg.b[1];
+      tx[k] = (double)mt_uniform(rw[2 * k]) * dx + reg.b[0];
+      ty[k] = (double)mt_uniform(rw[2 * k + 1]) * dy + reg.b[1];
       hit[k] = grid.conflict_initial(tx[k], ty[k], tr[k]) ? 1 : 0;
     }
   });
@@ -403,7 +410,7 @@ hg_status fill_trials(hg_resampler &R, FillGrid &grid, const std::vector<Box> &r
   }
   // the reference's mailbox stamp advances once per test, through 1 .. 2^32 - 1
   // (0 is skipped on the wrap)
-  advance_test_id(R.test_id, T);
+  if (!words) advance_test_id(R.test_id, T);
   return HG_OK;
 }
 
@@ -428,7 +435,8 @@ void regions_extent(const std::vector<Box> &regions, double mean_r, double e[4])
 template <typename Sampler>
 hg_status fill_regions(hg_resampler &R, const std::vector<Box> &regions, double mean_r,
                        double r_max, std::vector<double> &px, std::vector<double> &py,
-                       std::vector<double> &rad, Sampler sampler) {
+                       std::vector<double> &rad, Sampler sampler,
+                       const uint32_t *words = nullptr) {
   if (regions.empty()) return HG_OK;
   double e[4];
   regions_extent(regions, mean_r, e);
@@ -439,7 +447,7 @@ hg_status fill_regions(hg_resampler &R, const std::vector<Box> &regions, double 
     if (rad[b] > rc && rad[b] <= 4.0 * mean_r) rc = rad[b];
   static thread_local FillGrid tl_grid;
   build_fill_grid(tl_grid, e[0], e[1], e[2], e[3], rc, px, py, rad);
-  return fill_trials(R, tl_grid, regions, px, py, rad, sampler);
+  return fill_trials(R, tl_grid, regions, px, py, rad, sampler, -1.0, words);
 }
 
 // avoidAVoidMPMparticlesInsideZonesWithTentativeQuantities
@@ -448,7 +456,7 @@ hg_status fill_regions(hg_resampler &R, const std::vector<Box> &regions, double 
 // insertions (a sample of one insertion is a body of the next: it is one of
 // the grid's accepted samples, which every later trial tests).
 hg_status insert_points(hg_resampler &R, const std::vector<Box> &zones, int64_t &before,
-                        FillGrid &grid) {
+                        FillGrid &grid, const uint32_t *words) {
   const double rp = 0.5 * R.d.initial_particle_size;
   const size_t n = npoints(R);
   before = (int64_t)n;
@@ -456,7 +464,7 @@ hg_status insert_points(hg_resampler &R, const std::vector<Box> &zones, int64_t 
   const hg_status st = fill_trials(R, grid, zones, px, py, rad, [&](double &r) -> hg_status {
     r = rp;
     return HG_OK;
-  }, rp);
+  }, rp, words);
   if (st != HG_OK) return st;
   const double hl0 = R.d.initial_particle_size * 0.5;
   for (size_t p = 0; p < px.size(); ++p) { // addMaterialPoint, MaterialPoints.cpp:439-467
@@ -484,7 +492,8 @@ hg_status insert_points(hg_resampler &R, const std::vector<Box> &zones, int64_t 
 
 // avoidAVoidDEMparticlesInsideZonesWithTentativeQuantities
 // (ResamplingTools.cpp:106-196) with randomRadiusSampler (:19-26).
-hg_status insert_grains(hg_resampler &R, const std::vector<Box> &zones, int64_t &before) {
+hg_status insert_grains(hg_resampler &R, const std::vector<Box> &zones, int64_t &before,
+                        const uint32_t *words) {
   const size_t n = nbodies(R);
   before = (int64_t)n;
   std::vector<double> px(n), py(n), rad(R.dr);
@@ -516,7 +525,7 @@ hg_status insert_grains(hg_resampler &R, const std::vector<Box> &zones, int64_t 
       r = R.radius_dist(R.gen);
     }
     return HG_OK;
-  });
+  }, words);
   if (st != HG_OK) return st;
   const double pi = 3.14159265358979323846;
   for (size_t b = n; b < px.size(); ++b) { // RigidBody2DState::addBodies
@@ -974,13 +983,32 @@ hg_status run(hg_resampler &R, const hg_zones &z) {
   R.stats = hg_resampler_stats{};
   auto t = std::chrono::steady_clock::now();
   const bool direct = z.d.allow_direct_transitions != 0;
-  hg_status st;
   int64_t g_before = 0, p_before = 0, p_after = 0, p_mid = 0, dummy = 0;
-  if ((st = insert_grains(R, z.rzones, g_before))) return st;
-  const int64_t g_after = (int64_t)nbodies(R);
-  R.stats.ms_insert_grains = ms_since(t);
   std::vector<Box> inner;
   hg::zone_inner_continuum(z, direct, inner);
+  // The insertions draw their trial positions from R.mt in this order: the
+  // grains over the hybrid zone, then the points over the hybrid zone, the
+  // direct transitions and the inner continuum (two words per trial, 16
+  // trials per region). The words are drawn here in that order; the grain
+  // insertion (grains only, radii from its own engine) then runs on a
+  // second host thread beside the point insertions (points only). The
+  // mailbox stamp advances by all their tests at the end.
+  const size_t Tg = 16 * z.rzones.size(), Tp1 = 16 * z.rzones.size();
+  const size_t Tp2 = direct ? 16 * z.direct.size() : 0, Tp3 = 16 * inner.size();
+  static thread_local std::vector<uint32_t> tl_words;
+  std::vector<uint32_t> &words = tl_words;
+  words.resize(2 * (Tg + Tp1 + Tp2 + Tp3));
+  R.mt.fill_raw(words.data(), words.size());
+  const uint32_t *wg = words.data(), *wp1 = wg + 2 * Tg, *wp2 = wp1 + 2 * Tp1,
+                 *wp3 = wp2 + 2 * Tp2;
+  hg_status gst = HG_OK;
+  double g_ms = 0.0;
+  std::thread grains([&] {
+    auto tg = std::chrono::steady_clock::now();
+    gst = insert_grains(R, z.rzones, g_before, wg);
+    g_ms = ms_since(tg);
+  });
+  hg_status st = HG_OK;
   // one search grid over the points for the three insertions, over the
   // extent of all their regions
   static thread_local FillGrid tl_pgrid;
@@ -1010,15 +1038,24 @@ hg_status run(hg_resampler &R, const hg_zones &z) {
       build_fill_grid(tl_pgrid, e[0], e[1], e[2], e[3], rp, px, py, rad);
     }
   }
-  if ((st = insert_points(R, z.rzones, p_before, tl_pgrid))) return st;
+  int64_t i_before = 0, i_after = 0;
+  st = insert_points(R, z.rzones, p_before, tl_pgrid, wp1);
   p_mid = (int64_t)npoints(R);
-  if (direct && (st = insert_points(R, z.direct, dummy, tl_pgrid))) return st;
+  if (st == HG_OK && direct) st = insert_points(R, z.direct, dummy, tl_pgrid, wp2);
   p_after = (int64_t)npoints(R);
-  int64_t i_before = p_after, i_after = p_after;
-  if (!inner.empty()) {
-    if ((st = insert_points(R, inner, i_before, tl_pgrid))) return st;
+  i_before = i_after = p_after;
+  if (st == HG_OK && !inner.empty()) {
+    st = insert_points(R, inner, i_before, tl_pgrid, wp3);
     i_after = (int64_t)npoints(R);
   }
+  grains.join();
+  if (gst != HG_OK) return gst;
+  if (st != HG_OK) return st;
+  advance_test_id(R.test_id, Tg + Tp1 + Tp2 + Tp3);
+  const int64_t g_after = (int64_t)nbodies(R);
+  // (the grain insertion's own time; the point insertions' wall time, with
+  // the grain insertion beside them)
+  R.stats.ms_insert_grains = g_ms;
   R.stats.ms_insert_points = ms_since(t);
   CellLists cont, disc;
   point_grids(R, cont, disc);

@@ -27,6 +27,7 @@ The homogenised fields are accumulated once per device step, so at a
 resampling step the finalised field has one term less than the reference's,
 which accumulates the current step a second time inside the branch.
 """
+import threading
 import time
 
 import numpy as np
@@ -88,7 +89,8 @@ class HybridSim:
         self.steps = 0
         self.stats = []
         # host seconds of the resampling intervals by phase: device->host
-        # copies, zone update, resampling proper, host->device uploads
+        # copies, zone update (with the resampler's inputs set alongside),
+        # resampling proper, host->device uploads
         self.host_s = dict(download=0.0, zones=0.0, resampling=0.0, upload=0.0)
         # page-locked host arrays of the interval's transfers, sized for the
         # objects' capacities and kept for the simulation's life (the
@@ -142,15 +144,30 @@ class HybridSim:
             np.divide(hs, self.freq, out=hs)
             np.divide(hv, self.freq, out=hv)
         t1 = clock()
-        self.zones.update(q3, G["r"], G["fixed"], st["q"])
+        # the zone update runs on a second host thread while this one hands
+        # the interval's arrays to the resampler (the two meet at run)
+        failed = []
+
+        def zone_update():
+            try:
+                self.zones.update(q3, G["r"], G["fixed"], st["q"])
+            except Exception as e:  # re-raised on this thread below
+                failed.append(e)
+        zt = threading.Thread(target=zone_update)
+        zt.start()
+        try:
+            mw, vw = self._pinned("pmw", n), self._pinned("pvw", n)
+            np.multiply(P["m0"], P["w"], out=mw)
+            np.multiply(P["vol0"], P["w"], out=vw)
+            self.res.set_points(P["q0"], st["q"], st["v"], mw, vw,
+                                P["m0"], P["vol0"], P["hl"], st["be"], st["J"], st["jh"])
+            self.res.set_grains(G["q0"], q3, v3, G["r"], G["M0"], G["fixed"])
+            self.res.set_homogenized(hs, hv)
+        finally:
+            zt.join()
+        if failed:
+            raise failed[0]
         t2 = clock()
-        mw, vw = self._pinned("pmw", n), self._pinned("pvw", n)
-        np.multiply(P["m0"], P["w"], out=mw)
-        np.multiply(P["vol0"], P["w"], out=vw)
-        self.res.set_points(P["q0"], st["q"], st["v"], mw, vw,
-                            P["m0"], P["vol0"], P["hl"], st["be"], st["J"], st["jh"])
-        self.res.set_grains(G["q0"], q3, v3, G["r"], G["M0"], G["fixed"])
-        self.res.set_homogenized(hs, hv)
         self.res.run(self.zones)
         # the new points in page-locked arrays, two sets used in turn (the
         # previous interval's stay valid until this one has read them)
