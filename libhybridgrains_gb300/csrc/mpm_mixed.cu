@@ -865,6 +865,19 @@ __global__ void __launch_bounds__(THREADS) kxu_step(const __grid_constant__ Mixe
         vel.y = kin ? vel.y : fvy;
       }
       un = make_double2(un.x + widen(dux), un.y + widen(duy));
+      // new cell and fraction by FP32 carry of the old fraction, as in the
+      // linear kernel; the FP64 position decides after a plane projection,
+      // a move of a cell or more, or a carry that leaves the grid
+      bool exact = !(fabsf(dux) < 1.0f && fabsf(duy) < 1.0f);
+      int ncx = cx, ncy = cy;
+      float nfx = fx + dux, nfy = fy + duy;
+      {
+        const float cx1 = floorf(nfx), cy1 = floorf(nfy); // -1, 0 or 1
+        ncx += (int)cx1;
+        ncy += (int)cy1;
+        nfx -= cx1;
+        nfy -= cy1;
+      }
       // MaterialPoints::resolvePlaneCollisions (MaterialPoints.cpp:371-423) in
       // grid units: FP32 test first, FP64 on the positions within pmargin
       // cells of a plane
@@ -879,6 +892,7 @@ __global__ void __launch_bounds__(THREADS) kxu_step(const __grid_constant__ Mixe
         if (d > 0.0) continue;
         un.x += -d * pl.n[0];
         un.y += -d * pl.n[1];
+        exact = true;
         if (!pl.sticking) {
           const float vn = pl.fn[0] * vel.x + pl.fn[1] * vel.y;
           if (vn > 0.0f) continue;
@@ -888,14 +902,15 @@ __global__ void __launch_bounds__(THREADS) kxu_step(const __grid_constant__ Mixe
           vel = make_float2(0.0f, 0.0f);
         }
       }
-      int ncx, ncy;
-      float nfx, nfy;
-      split_u(un.x, ncx, nfx);
-      split_u(un.y, ncy, nfy);
-      far_edge(A.nx, ncx, nfx);
-      far_edge(A.ny, ncy, nfy);
-      nonfinite |= !finite_d(un.x) | !finite_d(un.y) | !isfinite(vel.x + vel.y) |
-                   !isfinite(st.x);
+      if (exact || !in_grid_cell(A, ncx, ncy)) {
+        split_u(un.x, ncx, nfx);
+        split_u(un.y, ncy, nfy);
+        far_edge(A.nx, ncx, nfx);
+        far_edge(A.ny, ncy, nfy);
+      }
+      // the position stays finite while its increments do (it was finite
+      // and inside the grid)
+      nonfinite |= !isfinite((dux + duy) + (vel.x + vel.y) + st.x);
       A.u[p] = un;
       A.v[p] = vel;
       A.strain[p] = st;
