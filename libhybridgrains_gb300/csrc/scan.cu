@@ -54,6 +54,38 @@ __global__ void k_tile_scan(const int32_t *__restrict__ in, int64_t n,
   }
 }
 
+// The per-tile scan of a device-wide scan with few tiles: each CTA forms its
+// tile's offset itself, summing the sums of the tiles before it (at most
+// FUSED_TILES of them, a few loads per thread), so that the scan of the tile
+// sums needs no launch of its own.
+constexpr int64_t FUSED_TILES = 2048;
+
+__global__ void k_tile_scan_summed(const int32_t *__restrict__ in, int64_t n,
+                                   const int32_t *__restrict__ sums,
+                                   int32_t *__restrict__ out) {
+  int before = 0;
+  for (int k = threadIdx.x; k < (int)blockIdx.x; k += SCAN_THREADS) before += sums[k];
+  int tile_off;
+  block_excl_scan<SCAN_THREADS>(before, &tile_off);
+  const int64_t base = (int64_t)blockIdx.x * SCAN_TILE;
+  int v[SCAN_ITEMS];
+  int s = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS; ++k) {
+    const int64_t i = base + (int64_t)threadIdx.x * SCAN_ITEMS + k;
+    v[k] = i < n ? in[i] : 0;
+    s += v[k];
+  }
+  int total;
+  int run = block_excl_scan<SCAN_THREADS>(s, &total) + tile_off;
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS; ++k) {
+    const int64_t i = base + (int64_t)threadIdx.x * SCAN_ITEMS + k;
+    if (i < n) out[i] = run;
+    run += v[k];
+  }
+}
+
 // Up to small_scan_max() elements: one CTA and one launch in place of three
 // (in a captured step the launches, not the bytes, are the cost at these
 // sizes). Thread t owns the SMALL_ITEMS consecutive elements from
@@ -166,6 +198,11 @@ hg_status exclusive_scan_i32(const int32_t *in, int32_t *out, int64_t n,
   int32_t *sums_scanned = tmp + tiles;
   HG_LAUNCH(k_tile_sums, (int)tiles, SCAN_THREADS, 0, s, in, n, sums);
   HG_CHECK_LAUNCH();
+  if (tiles <= FUSED_TILES) { // two launches in place of three
+    HG_LAUNCH(k_tile_scan_summed, (int)tiles, SCAN_THREADS, 0, s, in, n, sums, out);
+    HG_CHECK_LAUNCH();
+    return HG_OK;
+  }
   hg_status st = exclusive_scan_i32(sums, sums_scanned, tiles, tmp + 2 * tiles, s);
   if (st != HG_OK) return st;
   HG_LAUNCH(k_tile_scan, (int)tiles, SCAN_THREADS, 0, s, in, n, sums_scanned, out);
