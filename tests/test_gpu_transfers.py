@@ -118,3 +118,70 @@ def test_chunked_download_equals_the_frame_path(ctx):
     ctx.synchronize()
     assert np.array_equal(D["q"], fq)
     assert np.array_equal(D["v"], fv)
+
+
+def test_unaligned_and_tiny_host_arrays(ctx):
+    """Page-locked arrays that start 8 bytes past a 16-byte boundary (the
+    upload reads them element by element, the download takes the staging
+    copies), and uploads of 1 and 0 points, give what aligned arrays give."""
+    torch = pytest.importorskip("torch")
+    cfg, p = column(h=2.5e-3)
+    n = len(p["m"])
+    dt = cfg["dt"]
+
+    def shifted(a):
+        # a page-locked copy of a whose data starts 8 bytes past the buffer
+        raw = torch.empty(a.size + 2, dtype=torch.float64, pin_memory=True).numpy()
+        flat = raw[1:1 + a.size]
+        assert flat.ctypes.data % 16 == 8
+        flat[...] = a.ravel()
+        return flat.reshape(a.shape)
+
+    ref = make(ctx, cfg, n)
+    ref.upload(p["q"], p["v"], p["m"], p["vol"], p["hl"])
+    ref.flow(dt, 3)
+    R = ref.download()
+    b = make(ctx, cfg, n)
+    q, v, m, vol = (shifted(p[k]) for k in ("q", "v", "m", "vol"))
+    b.upload(q, v, m, vol, None)
+    b.flow(dt, 3)
+    out = {"q": shifted(np.zeros((n, 2))), "v": shifted(np.zeros((n, 2))),
+           "be": shifted(np.zeros((n, 4))), "J": shifted(np.zeros(n))}
+    jh = np.zeros(n, dtype=np.int32)
+    b.download_into(out["q"], out["v"], out["be"], out["J"], jh)
+    assert np.abs(out["q"] - R["q"]).max() <= 1e-12
+    assert np.abs(out["J"] - R["J"]).max() <= 1e-9
+    assert np.linalg.norm(out["v"] - R["v"]) / np.linalg.norm(R["v"]) <= 1e-6
+    for k in (1, 0):
+        t = make(ctx, cfg, max(k, 1))
+        t.upload(p["q"][:k].copy(), p["v"][:k].copy(), p["m"][:k].copy(), p["vol"][:k].copy(),
+                 None)
+        t.flow(dt, 2)
+        t.upload(p["q"][:k].copy(), p["v"][:k].copy(), p["m"][:k].copy(), p["vol"][:k].copy(),
+                 None)
+        t.flow(dt, 1)
+        D = t.download()
+        assert D["q"].shape == (k, 2) and t.status() == 0
+        if k:
+            assert np.abs(D["q"] - p["q"][:k]).max() < cfg["h"]
+
+
+def test_upload_of_a_different_point_count_resorts(ctx):
+    cfg, p = column(h=2.5e-3)
+    n = len(p["m"])
+    dt = cfg["dt"]
+    b = make(ctx, cfg, n)
+    b.upload(p["q"], p["v"], p["m"], p["vol"], p["hl"])
+    b.flow(dt, 2)
+    k = n // 2  # the first half of the points: a new point count
+    sub = {x: p[x][:k].copy() for x in ("q", "v", "m", "vol")}
+    b.upload(sub["q"], sub["v"], sub["m"], sub["vol"], None)
+    b.flow(dt, 2)
+    f = make(ctx, cfg, n)
+    f.upload(sub["q"], sub["v"], sub["m"], sub["vol"], None)
+    f.flow(dt, 2)
+    G, F = b.grid(), f.grid()
+    assert np.array_equal(G["mass"] > 0, F["mass"] > 0)
+    act = F["mass"] > 0
+    assert np.linalg.norm(G["vel"][act] - F["vel"][act]) / np.linalg.norm(F["vel"][act]) <= 1e-6
+    assert np.abs(b.download()["q"] - f.download()["q"]).max() <= 1e-12
