@@ -1325,6 +1325,7 @@ hg_status hg_dem_create(hg_context *ctx, const hg_dem_desc *d, hg_dem **out) {
     return fail(HG_ERR_INVALID_ARGUMENT, "precision must be HG_PRECISION_FP64 or HG_PRECISION_MIXED");
   }
   P.precision = d->precision;
+  dem_set_launch_shapes(dm);
   P.nplanes = d->num_planes;
   for (int k = 0; k < d->num_planes; ++k) {
     const hg_dem_plane &pl = d->planes[k];

@@ -188,17 +188,43 @@ void host_pool_run(size_t ntasks, const std::function<void(size_t)> &task);
 // (hg_set_host_threads, by default the hardware concurrency up to 16), at
 // least min_per_worker items each; f(begin, end) must only write what its
 // range owns.
+// The host threads the loops below use: hg_set_host_threads, by default the
+// hardware concurrency up to 16.
+inline size_t host_workers() {
+  const int set = g_host_threads.load();
+  return set > 0 ? (size_t)set : std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+}
+
 template <typename F>
 void host_parallel(size_t n, size_t min_per_worker, F f) {
-  const int set = g_host_threads.load();
-  const size_t hw = set > 0 ? (size_t)set
-                            : std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  const size_t hw = host_workers();
   const size_t workers = std::min(hw, std::max<size_t>(1, n / std::max<size_t>(min_per_worker, 1)));
   if (workers <= 1) {
     f((size_t)0, n);
     return;
   }
   host_pool_run(workers, [&](size_t t) { f(n * t / workers, n * (t + 1) / workers); });
+}
+
+// Host loop over [0, n) in ranges of `chunk` items that the host threads
+// take in turn as they finish (for loops whose cost per item varies, such as
+// rows of a grid with material in a band of it); f(begin, end) must only
+// write what its range owns.
+template <typename F>
+void host_parallel_dynamic(size_t n, size_t chunk, F f) {
+  chunk = std::max<size_t>(chunk, 1);
+  const size_t hw = host_workers();
+  const size_t chunks = (n + chunk - 1) / chunk;
+  const size_t workers = std::min(hw, chunks);
+  if (workers <= 1) {
+    if (n) f((size_t)0, n);
+    return;
+  }
+  std::atomic<size_t> next{0};
+  host_pool_run(workers, [&](size_t) {
+    for (size_t c = next.fetch_add(1); c < chunks; c = next.fetch_add(1))
+      f(c * chunk, std::min(n, (c + 1) * chunk));
+  });
 }
 
 void context_retain(hg_context *c);
@@ -492,6 +518,7 @@ struct hg_dem {
   int cc = 0;                                  // live contact buffer
   int64_t ncontacts_host = 0;                  // count after the last step
   bool history_valid = false;
+  int contact_grid = 0; // blocks of the contact law's grid-stride launch
   // body gather lists for deterministic force accumulation
   hg::DevBuf<int32_t> in_count, in_off, in_list, in_cursor;
   hg::DevBuf<int32_t> out_off; // first contact index of each body
@@ -517,6 +544,7 @@ hg_status dem_edit(hg_dem *d, int64_t n_old, const int32_t *old_to_new, int64_t 
                    int64_t n_add, const double *q, const double *v, const double *r,
                    const double *m, const double *I, const uint8_t *fixed);
 hg_status dem_step(hg_dem *d, double dt, int weighted);
+void dem_set_launch_shapes(hg_dem *d);
 // per-body terms that dem_step needs and that only change with the bodies
 // or the time step; called before a step is captured into a graph
 hg_status dem_prepare(hg_dem *d, double dt);

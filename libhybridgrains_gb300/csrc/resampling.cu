@@ -778,11 +778,16 @@ void mass_weighted_fields(const hg_resampler &R, int64_t n, NodeField *f, int nf
   const hg_zones_desc &zd = R.d.zones;
   const int nx = zd.mpm_cells[0], ny = zd.mpm_cells[1];
   const size_t nn = (size_t)(nx + 1) * (ny + 1);
-  std::vector<double> mass(nn, 0.0);
+  // (scratch kept between calls)
+  static thread_local std::vector<double> tl_mass;
+  std::vector<double> &mass = tl_mass;
+  mass.assign(nn, 0.0);
   for (int k = 0; k < nf; ++k) f[k].out->assign(nn * f[k].len, 0.0);
   const double h1 = R.hl.empty() ? 0.0 : R.hl[0];
   // the node range of every point's stencil (empty: j0 > j1)
-  std::vector<std::array<int, 4>> range((size_t)n);
+  static thread_local std::vector<std::array<int, 4>> tl_range;
+  std::vector<std::array<int, 4>> &range = tl_range;
+  range.resize((size_t)n);
   hg::host_parallel((size_t)n, 4096, [&](size_t b, size_t e) {
     for (size_t p = b; p < e; ++p) {
       int x0, y0, x1, y1, i0, i1, j0, j1;
@@ -794,9 +799,32 @@ void mass_weighted_fields(const hg_resampler &R, int64_t n, NodeField *f, int nf
         range[p] = {i0, i1, j0, j1};
     }
   });
-  // node rows split over host threads; each thread walks the points in
-  // order, so every node sums its points in the reference's order
-  hg::host_parallel((size_t)ny + 1, 4, [&](size_t rb, size_t re) {
+  // node rows split over host threads in bands of about equal work (the
+  // stencil rows the points put on them: the points fill part of the grid);
+  // each thread walks the points in order, so every node sums its points in
+  // the reference's order
+  const size_t workers = std::max<size_t>(1, std::min(hg::host_workers(), (size_t)ny + 1));
+  // (rows j0 .. j1 <= ny: +w at j0 + 1, -w at j1 + 2 <= ny + 2)
+  std::vector<int64_t> work((size_t)ny + 3, 0);
+  for (int64_t p = 0; p < n; ++p)
+    if (range[p][2] <= range[p][3]) {
+      const int64_t w = range[p][1] - range[p][0] + 1;
+      work[range[p][2] + 1] += w;
+      work[range[p][3] + 2] -= w;
+    }
+  // work per row, then its running sum
+  for (size_t j = 1; j < work.size(); ++j) work[j] += work[j - 1];
+  for (size_t j = 1; j < work.size(); ++j) work[j] += work[j - 1];
+  std::vector<size_t> band(workers + 1, (size_t)ny + 1);
+  band[0] = 0;
+  for (size_t t = 1, j = 0; t < workers; ++t) {
+    const int64_t goal = (int64_t)((double)work[ny + 1] * (double)t / (double)workers);
+    while (j < (size_t)ny + 1 && work[j] < goal) ++j;
+    band[t] = std::max(j, band[t - 1]);
+  }
+  hg::host_pool_run(workers, [&](size_t t) {
+    const size_t rb = band[t], re = band[t + 1];
+    if (rb >= re) return;
     for (int64_t p = 0; p < n; ++p) {
       const std::array<int, 4> &r = range[p];
       const int j0 = std::max(r[2], (int)rb), j1 = std::min(r[3], (int)re - 1);
@@ -837,7 +865,11 @@ void mass_weighted_fields(const hg_resampler &R, int64_t n, NodeField *f, int nf
 // (:198-274) and reassignJVelAndBebarForInternalMaterialPoint (:335-366).
 void inner_point_quantities(hg_resampler &R, int64_t before, int64_t after, const CellLists &cont) {
   const hg_zones_desc &zd = R.d.zones;
-  std::vector<double> fJ, fv, fb;
+  if (after <= before) return; // no inner point inserted: nothing to assign
+  // node fields kept between calls (fresh pages would be faulted in on
+  // every call)
+  static thread_local std::vector<double> tl_fJ, tl_fv, tl_fb;
+  std::vector<double> &fJ = tl_fJ, &fv = tl_fv, &fb = tl_fb;
   const double dJ[1] = {1.0}, dv[2] = {0.0, 0.0}, db[4] = {1.0, 0.0, 0.0, 1.0};
   NodeField fields[3] = {{1, &R.J, dJ, &fJ}, {2, &R.v, dv, &fv}, {4, &R.be, db, &fb}};
   mass_weighted_fields(R, before, fields, 3);
@@ -995,10 +1027,13 @@ hg_status run(hg_resampler &R, const hg_zones &z) {
   // mailbox stamp advances by all their tests at the end.
   const size_t Tg = 16 * z.rzones.size(), Tp1 = 16 * z.rzones.size();
   const size_t Tp2 = direct ? 16 * z.direct.size() : 0, Tp3 = 16 * inner.size();
+  // (the grains' words first, so that their insertion can start; the
+  // points' words on a third thread while this one builds the points'
+  // search grid)
   static thread_local std::vector<uint32_t> tl_words;
   std::vector<uint32_t> &words = tl_words;
   words.resize(2 * (Tg + Tp1 + Tp2 + Tp3));
-  R.mt.fill_raw(words.data(), words.size());
+  R.mt.fill_raw(words.data(), 2 * Tg);
   const uint32_t *wg = words.data(), *wp1 = wg + 2 * Tg, *wp2 = wp1 + 2 * Tp1,
                  *wp3 = wp2 + 2 * Tp2;
   hg_status gst = HG_OK;
@@ -1008,6 +1043,8 @@ hg_status run(hg_resampler &R, const hg_zones &z) {
     gst = insert_grains(R, z.rzones, g_before, wg);
     g_ms = ms_since(tg);
   });
+  std::thread point_words(
+      [&] { R.mt.fill_raw(words.data() + 2 * Tg, words.size() - 2 * Tg); });
   hg_status st = HG_OK;
   // one search grid over the points for the three insertions, over the
   // extent of all their regions
@@ -1038,6 +1075,7 @@ hg_status run(hg_resampler &R, const hg_zones &z) {
       build_fill_grid(tl_pgrid, e[0], e[1], e[2], e[3], rp, px, py, rad);
     }
   }
+  point_words.join();
   int64_t i_before = 0, i_after = 0;
   st = insert_points(R, z.rzones, p_before, tl_pgrid, wp1);
   p_mid = (int64_t)npoints(R);

@@ -19,6 +19,9 @@ static_assert(SCAN_TILE == SCAN_TILE_ELEMS, "scan_tmp_size assumes this tile siz
 
 __global__ void k_tile_sums(const int32_t *__restrict__ in, int64_t n,
                             int32_t *__restrict__ sums) {
+  // (launched with programmatic dependence on the kernel before it)
+  pdl_wait();
+  pdl_trigger();
   const int64_t base = (int64_t)blockIdx.x * SCAN_TILE;
   int s = 0;
 #pragma unroll
@@ -34,6 +37,9 @@ __global__ void k_tile_sums(const int32_t *__restrict__ in, int64_t n,
 __global__ void k_tile_scan(const int32_t *__restrict__ in, int64_t n,
                             const int32_t *__restrict__ tile_off,
                             int32_t *__restrict__ out) {
+  // (launched with programmatic dependence on the kernel before it)
+  pdl_wait();
+  pdl_trigger();
   const int64_t base = (int64_t)blockIdx.x * SCAN_TILE;
   // Each thread owns SCAN_ITEMS consecutive elements.
   int v[SCAN_ITEMS];
@@ -63,6 +69,9 @@ constexpr int64_t FUSED_TILES = 2048;
 __global__ void k_tile_scan_summed(const int32_t *__restrict__ in, int64_t n,
                                    const int32_t *__restrict__ sums,
                                    int32_t *__restrict__ out) {
+  // (launched with programmatic dependence on the kernel before it)
+  pdl_wait();
+  pdl_trigger();
   int before = 0;
   for (int k = threadIdx.x; k < (int)blockIdx.x; k += SCAN_THREADS) before += sums[k];
   int tile_off;
@@ -102,6 +111,9 @@ static_assert(SMALL_ITEMS % 4 == 0, "runs are read as int4");
 
 __global__ void __launch_bounds__(SMALL_THREADS)
     k_small_scan(int32_t *__restrict__ in, int64_t n64, int32_t *__restrict__ out, ScanLimit lim) {
+  // (launched with programmatic dependence on the kernel before it)
+  pdl_wait();
+  pdl_trigger();
   const int n = (int)n64; // <= SMALL_N
   const int base = threadIdx.x * SMALL_ITEMS;
   // whole runs of 16-byte aligned arrays move as int4
@@ -165,7 +177,7 @@ __global__ void __launch_bounds__(SMALL_THREADS)
 
 hg_status launch_small_scan(int32_t *in, int64_t n, int32_t *out, const ScanLimit &lim,
                             cudaStream_t s) {
-  HG_LAUNCH(k_small_scan, 1, SMALL_THREADS, 0, s, in, n, out, lim);
+  HG_LAUNCH_PDL(k_small_scan, 1, SMALL_THREADS, 0, s, in, n, out, lim);
   HG_CHECK_LAUNCH();
   return HG_OK;
 }
@@ -187,7 +199,7 @@ hg_status exclusive_scan_i32(const int32_t *in, int32_t *out, int64_t n,
                              int32_t *tmp, cudaStream_t s) {
   if (n <= 0) return HG_OK;
   if (n <= SCAN_TILE) {
-    HG_LAUNCH(k_tile_scan, 1, SCAN_THREADS, 0, s, in, n, nullptr, out);
+    HG_LAUNCH_PDL(k_tile_scan, 1, SCAN_THREADS, 0, s, in, n, nullptr, out);
     HG_CHECK_LAUNCH();
     return HG_OK;
   }
@@ -196,16 +208,16 @@ hg_status exclusive_scan_i32(const int32_t *in, int32_t *out, int64_t n,
   const int64_t tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
   int32_t *sums = tmp;
   int32_t *sums_scanned = tmp + tiles;
-  HG_LAUNCH(k_tile_sums, (int)tiles, SCAN_THREADS, 0, s, in, n, sums);
+  HG_LAUNCH_PDL(k_tile_sums, (int)tiles, SCAN_THREADS, 0, s, in, n, sums);
   HG_CHECK_LAUNCH();
   if (tiles <= FUSED_TILES) { // two launches in place of three
-    HG_LAUNCH(k_tile_scan_summed, (int)tiles, SCAN_THREADS, 0, s, in, n, sums, out);
+    HG_LAUNCH_PDL(k_tile_scan_summed, (int)tiles, SCAN_THREADS, 0, s, in, n, sums, out);
     HG_CHECK_LAUNCH();
     return HG_OK;
   }
   hg_status st = exclusive_scan_i32(sums, sums_scanned, tiles, tmp + 2 * tiles, s);
   if (st != HG_OK) return st;
-  HG_LAUNCH(k_tile_scan, (int)tiles, SCAN_THREADS, 0, s, in, n, sums_scanned, out);
+  HG_LAUNCH_PDL(k_tile_scan, (int)tiles, SCAN_THREADS, 0, s, in, n, sums_scanned, out);
   HG_CHECK_LAUNCH();
   return HG_OK;
 }

@@ -145,7 +145,8 @@ void packing_fraction(hg_zones &z, int64_t nd, const double *q3, const double *r
         z.phi[(size_t)j * nx + i] = pf / (double)(S * S);
       }
   };
-  hg::host_parallel(ny, 8, [&](size_t jb, size_t je) { rows((unsigned)jb, (unsigned)je); });
+  // (rows taken in turn by the host threads: the disks fill a band of them)
+  hg::host_parallel_dynamic(ny, 2, [&](size_t jb, size_t je) { rows((unsigned)jb, (unsigned)je); });
   // cells within half a window of a material point count as dense; the
   // reference's test excludes the first row and column (gid > 0)
   // (marks over host threads by points, each a relaxed atomic store of the
@@ -210,8 +211,12 @@ void distance_field(hg_zones &z) {
   // nearest sample per grid point: seed within 3h of every sample, then
   // propagate to the four neighbours breadth first
   const size_t npts = (size_t)(nx + 1) * (ny + 1);
-  std::vector<double> d(npts, 1.0e10);
-  std::vector<int64_t> closest(npts, -1);
+  // distance and sample per grid point side by side (one line per visit)
+  struct Nearest {
+    double d;
+    int64_t sample; // -1: none yet
+  };
+  std::vector<Nearest> near(npts, Nearest{1.0e10, -1});
   const double W = z.ls_max[0] - z.ls_min[0], H = z.ls_max[1] - z.ls_min[1];
   auto gpx = [&](int i) { return W * (double)i / (double)nx + z.ls_min[0]; };
   auto gpy = [&](int j) { return H * (double)j / (double)ny + z.ls_min[1]; };
@@ -236,9 +241,9 @@ void distance_field(hg_zones &z) {
         for (int i = i0; i <= i1; ++i) {
           const size_t f = (size_t)j * (nx + 1) + i;
           const double dd = norm(gpx(i) - sx[p], gpy(j) - sy[p]);
-          if (dd < d[f]) {
-            d[f] = dd;
-            closest[f] = (int64_t)p;
+          if (dd < near[f].d) {
+            near[f].d = dd;
+            near[f].sample = (int64_t)p;
           }
         }
     }
@@ -251,32 +256,34 @@ void distance_field(hg_zones &z) {
   std::vector<uint32_t> ring; // (column, row) pairs
   ring.reserve(2 * npts);
   for (size_t f = 0; f < npts; ++f)
-    if (closest[f] >= 0) {
+    if (near[f].sample >= 0) {
       ring.push_back((uint32_t)(f % (nx + 1)));
       ring.push_back((uint32_t)(f / (nx + 1)));
     }
   for (size_t head = 0; head < ring.size(); head += 2) {
     const unsigned gi = ring[head], gj = ring[head + 1];
     const size_t f = (size_t)gj * (nx + 1) + gi;
-    const int64_t cp = closest[f];
+    const int64_t cp = near[f].sample;
     const double spx = sx[cp], spy = sy[cp];
-    const bool ok[4] = {gi > 0, gj > 0, gi < nx, gj < ny};
-    const unsigned ni[4] = {gi - 1, gi, gi + 1, gi}, nj[4] = {gj, gj - 1, gj, gj + 1};
-    for (int l = 0; l < 4; ++l) {
-      if (!ok[l]) continue;
-      const size_t g = (size_t)nj[l] * (nx + 1) + ni[l];
-      const double ex = tgx[ni[l]] - spx, ey = tgy[nj[l]] - spy, e2 = ex * ex + ey * ey;
+    auto visit = [&](unsigned ni, unsigned nj) {
+      Nearest &g = near[(size_t)nj * (nx + 1) + ni];
+      const double ex = tgx[ni] - spx, ey = tgy[nj] - spy, e2 = ex * ex + ey * ey;
       // a squared distance clearly above the stored one cannot win: the
       // square root (rounded to half an ulp) stays above it too
-      if (closest[g] >= 0 && e2 > d[g] * d[g] * (1.0 + 1.0e-12)) continue;
+      if (g.sample >= 0 && e2 > g.d * g.d * (1.0 + 1.0e-12)) return;
       const double dd = norm(ex, ey);
-      if (dd < d[g] || closest[g] < 0) {
-        d[g] = dd;
-        closest[g] = cp;
-        ring.push_back(ni[l]);
-        ring.push_back(nj[l]);
+      if (dd < g.d || g.sample < 0) {
+        g.d = dd;
+        g.sample = cp;
+        ring.push_back(ni);
+        ring.push_back(nj);
       }
-    }
+    };
+    // left, below, right, above
+    if (gi > 0) visit(gi - 1, gj);
+    if (gj > 0) visit(gi, gj - 1);
+    if (gi < nx) visit(gi + 1, gj);
+    if (gj < ny) visit(gi, gj + 1);
   }
   // sign: positive at the corners of dense cells
   std::vector<uint8_t> pos(npts, 0);
@@ -286,7 +293,7 @@ void distance_field(hg_zones &z) {
         const size_t bl = (size_t)j * (nx + 1) + i, tl = bl + (nx + 1);
         pos[bl] = pos[bl + 1] = pos[tl] = pos[tl + 1] = 1;
       }
-  for (size_t f = 0; f < npts; ++f) z.dist[f] = pos[f] ? std::fabs(d[f]) : -std::fabs(d[f]);
+  for (size_t f = 0; f < npts; ++f) z.dist[f] = pos[f] ? std::fabs(near[f].d) : -std::fabs(near[f].d);
 }
 
 void labels(hg_zones &z) {
