@@ -137,15 +137,10 @@ class HybridSim:
         self.dem.download_into(q3, v3)
         P, G = self.P, self.G
         nn = self.mpm.nnodes
-        hs, hv = np.zeros((nn, 4)), np.zeros((nn, 2))
-        if self.hom[0] or self.hom[1]:
-            hs, hv = self._pinned("nhs", (nn, 4)), self._pinned("nhv", (nn, 2))
-            self.hyb.homogenized_into(hs, hv)
-            np.divide(hs, self.freq, out=hs)
-            np.divide(hv, self.freq, out=hv)
         t1 = clock()
-        # the zone update runs on a second host thread while this one hands
-        # the interval's arrays to the resampler (the two meet at run)
+        # the zone update (positions only) runs on a second host thread
+        # while this one reads the homogenised fields and hands the
+        # interval's arrays to the resampler (the two meet at run)
         failed = []
 
         def zone_update():
@@ -156,6 +151,12 @@ class HybridSim:
         zt = threading.Thread(target=zone_update)
         zt.start()
         try:
+            hs, hv = np.zeros((nn, 4)), np.zeros((nn, 2))
+            if self.hom[0] or self.hom[1]:
+                hs, hv = self._pinned("nhs", (nn, 4)), self._pinned("nhv", (nn, 2))
+                self.hyb.homogenized_into(hs, hv)
+                np.divide(hs, self.freq, out=hs)
+                np.divide(hv, self.freq, out=hv)
             mw, vw = self._pinned("pmw", n), self._pinned("pvw", n)
             np.multiply(P["m0"], P["w"], out=mw)
             np.multiply(P["vol0"], P["w"], out=vw)
