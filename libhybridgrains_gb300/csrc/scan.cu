@@ -115,35 +115,44 @@ __global__ void __launch_bounds__(SMALL_THREADS)
   pdl_wait();
   pdl_trigger();
   const int n = (int)n64; // <= SMALL_N
-  const int base = threadIdx.x * SMALL_ITEMS;
-  // whole runs of 16-byte aligned arrays move as int4
+  // Each warp owns 32 x SMALL_ITEMS consecutive counts, read and written in
+  // rows of 128 (4 per lane: one coalesced 512-byte access per row); each
+  // row is scanned across the warp, the rows one after another.
+  constexpr int ROWS = SMALL_ITEMS / 4;
+  const int lane = threadIdx.x & 31;
+  const int wbase = (threadIdx.x >> 5) * (32 * SMALL_ITEMS);
   const bool vec =
       ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15u) == 0 &&
-      base + SMALL_ITEMS <= n;
-  int v[SMALL_ITEMS];
-  if (vec) {
-    const int4 *p = reinterpret_cast<const int4 *>(in + base);
+      wbase + 32 * SMALL_ITEMS <= n;
+  int v[ROWS][4];
 #pragma unroll
-    for (int k = 0; k < SMALL_ITEMS / 4; ++k) {
-      const int4 q = p[k];
-      v[4 * k] = q.x;
-      v[4 * k + 1] = q.y;
-      v[4 * k + 2] = q.z;
-      v[4 * k + 3] = q.w;
+  for (int r = 0; r < ROWS; ++r) {
+    const int i = wbase + 128 * r + 4 * lane;
+    if (vec) {
+      const int4 q = *reinterpret_cast<const int4 *>(in + i);
+      v[r][0] = q.x;
+      v[r][1] = q.y;
+      v[r][2] = q.z;
+      v[r][3] = q.w;
+    } else {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) v[r][j] = i + j < n ? in[i + j] : 0;
     }
-  } else {
-#pragma unroll
-    for (int k = 0; k < SMALL_ITEMS; ++k) v[k] = base + k < n ? in[base + k] : 0;
   }
-  int sum = 0;
+  // pre[r]: the offset of the lane's first count of row r in the warp's run
+  int pre[ROWS];
+  int carry = 0;
 #pragma unroll
-  for (int k = 0; k < SMALL_ITEMS; ++k) { // exclusive prefix within the run
-    const int x = v[k];
-    v[k] = sum;
-    sum += x;
+  for (int r = 0; r < ROWS; ++r) {
+    const int x = v[r][0] + v[r][1] + v[r][2] + v[r][3];
+    const int inc = warp_incl_scan(x);
+    pre[r] = carry + inc - x;
+    carry += __shfl_sync(0xffffffffu, inc, 31);
   }
+  // the warps' runs: lane 31 carries its warp's total, so every lane's
+  // exclusive prefix is the sum of the warps before its own
   int total;
-  const int off = block_excl_scan<SMALL_THREADS>(sum, &total);
+  const int off = block_excl_scan<SMALL_THREADS>(lane == 31 ? carry : 0, &total);
   // the same decision in every thread: the total is block-wide
   const bool over = lim.limit >= 0 && (int64_t)total > lim.limit;
   if (threadIdx.x == 0) {
@@ -151,26 +160,26 @@ __global__ void __launch_bounds__(SMALL_THREADS)
     if (over && lim.status) atomicOr(lim.status, lim.status_bit);
     if (lim.total) *lim.total = over ? 0 : total;
   }
-  if (vec) {
-    int4 *q = reinterpret_cast<int4 *>(out + base);
 #pragma unroll
-    for (int k = 0; k < SMALL_ITEMS / 4; ++k)
-      q[k] = over ? make_int4(0, 0, 0, 0)
-                  : make_int4(off + v[4 * k], off + v[4 * k + 1], off + v[4 * k + 2],
-                              off + v[4 * k + 3]);
-    if (over) { // every count and offset dropped
-      int4 *c = reinterpret_cast<int4 *>(in + base);
+  for (int r = 0; r < ROWS; ++r) {
+    const int i = wbase + 128 * r + 4 * lane;
+    int o[4];
+    o[0] = off + pre[r];
+    o[1] = o[0] + v[r][0];
+    o[2] = o[1] + v[r][1];
+    o[3] = o[2] + v[r][2];
+    if (vec) {
+      *reinterpret_cast<int4 *>(out + i) =
+          over ? make_int4(0, 0, 0, 0) : make_int4(o[0], o[1], o[2], o[3]);
+      if (over) // every count and offset dropped
+        *reinterpret_cast<int4 *>(in + i) = make_int4(0, 0, 0, 0);
+    } else {
 #pragma unroll
-      for (int k = 0; k < SMALL_ITEMS / 4; ++k) c[k] = make_int4(0, 0, 0, 0);
-    }
-  } else {
-#pragma unroll
-    for (int k = 0; k < SMALL_ITEMS; ++k) {
-      const int i = base + k;
-      if (i < n) {
-        out[i] = over ? 0 : off + v[k];
-        if (over) in[i] = 0;
-      }
+      for (int j = 0; j < 4; ++j)
+        if (i + j < n) {
+          out[i + j] = over ? 0 : o[j];
+          if (over) in[i + j] = 0;
+        }
     }
   }
 }
